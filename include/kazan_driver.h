@@ -1,0 +1,77 @@
+/*
+ * kazan_driver.h - C ABI of libkazan_driver.so, the GB300 drop-in for the kazan Vulkan driver's draw path.
+ *
+ * Loader-facing exports (same names, signatures and semantics as the reference):
+ *   vk_icdGetInstanceProcAddr                 replaces vulkan-driver/src/lib.rs:38-43
+ *   vk_icdNegotiateLoaderICDInterfaceVersion  replaces vulkan-driver/src/lib.rs:51-63 (clamps to 5)
+ *   vk_icdGetPhysicalDeviceProcAddr           replaces vulkan-driver/src/lib.rs:68-130
+ * Every vk* entry point is reached through vk_icdGetInstanceProcAddr, as in the reference's
+ * get_proc_address (vulkan-driver/src/api_impl.rs:432-860).  The draw path's entry points replace:
+ *   vkCmdDraw api_impl.rs:4632, vkCmdDrawIndexed :4643, vkCmdClearColorImage :4780,
+ *   vkCmdClearDepthStencilImage :4792, vkCmdBindVertexBuffers :4621, vkCmdBindIndexBuffer :4611,
+ *   vkCmdPushConstants :4932, vkCmdBindPipeline :4506, vkCmdSetViewport :4515, vkCmdSetScissor :4525,
+ *   vkCmdBeginRenderPass :4944, vkCmdEndRenderPass :4961, vkCreateFramebuffer :4383,
+ *   vkCreateRenderPass :4402, vkCreateCommandPool :4436, vkAllocateCommandBuffers :4464,
+ *   vkBeginCommandBuffer :4483, vkEndCommandBuffer :4491, vkQueueSubmit :3414, vkQueueWaitIdle :3424,
+ *   vkCreateFence :3653, vkWaitForFences :3689, vkCreateGraphicsPipelines :4018,
+ *   vkCreatePipelineLayout :4061, vkCreateShaderModule :3946, vkAllocateMemory :3434, vkMapMemory :3488,
+ *   vkCreateBuffer :3795, vkCreateImage :3851, vkBindBufferMemory2 :4975, vkBindImageMemory2 :5013.
+ *
+ * The kz* functions below have no counterpart in the reference: they expose the driver's execution
+ * options and statistics to the benchmark and tests without a Vulkan extension.
+ */
+#ifndef KAZAN_DRIVER_H
+#define KAZAN_DRIVER_H
+
+#include <stdint.h>
+
+#include "kz_vk_abi.h"
+
+#define KZ_API __attribute__((visibility("default")))
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+KZ_API PFN_vkVoidFunction vk_icdGetInstanceProcAddr(VkInstance instance, const char* pName);
+KZ_API VkResult vk_icdNegotiateLoaderICDInterfaceVersion(uint32_t* pSupportedVersion);
+KZ_API PFN_vkVoidFunction vk_icdGetPhysicalDeviceProcAddr(VkInstance instance, const char* pName);
+
+/* Execution options, read at vkEndCommandBuffer.  Keys and values:
+ *   "mode"  "persistent" (default: one cooperative kernel per run of render passes, captured in a CUDA
+ *           graph), "batched" (one launch per pipeline phase per render pass, captured in a CUDA graph),
+ *           "perdraw" (one launch per phase per draw, launched at submit: the plain baseline)
+ *   "tile"  screen-tile side in pixels: "8", "16", "32" or "64"
+ *   "trace" "0" / "1": log lowering and linking decisions to stderr
+ *   "fault_alloc" "N": the Nth device allocation from now fails with VK_ERROR_OUT_OF_DEVICE_MEMORY
+ * Returns 0, or -1 for an unknown key or value.  The KZ_MODE, KZ_TILE, KZ_TRACE and KZ_FAULT=alloc:N
+ * environment variables set the initial values. */
+KZ_API int kzDriverSetOption(const char* key, const char* value);
+
+/* The CUDA stream (cudaStream_t) a queue executes on, for callers that time submissions with CUDA
+ * events on that stream. */
+KZ_API void* kzGetQueueStream(VkQueue queue);
+
+typedef struct KzCommandBufferStats {
+  uint64_t triangles;     /* triangles submitted (all draws, all instances) */
+  uint32_t draws;
+  uint32_t segments;      /* raster segments after lowering */
+  uint32_t mode;          /* 0 persistent, 1 batched, 2 per-draw */
+  uint32_t tile;          /* tile side in pixels */
+  uint32_t status;        /* KzStatusBits of the last completed execution */
+  uint32_t records;       /* largest number of triangle records any segment produced */
+  uint32_t pairs;         /* largest number of (tile, record) pairs any segment produced */
+  uint32_t fragments;     /* covered fragments of the last execution (low 32 bits) */
+  uint32_t rec_cap, pair_cap;
+  float gpu_ms;           /* device time of the last execution (CUDA events around the kernels) */
+  uint32_t launches;      /* kernel launches per execution */
+} KzCommandBufferStats;
+
+/* Statistics of a command buffer's lowering and last completed execution (0 = success). */
+KZ_API int kzGetCommandBufferStats(VkCommandBuffer commandBuffer, KzCommandBufferStats* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KAZAN_DRIVER_H */

@@ -1,0 +1,1059 @@
+/*
+ * kz_vk_abi.h - the subset of the Vulkan 1.1 C ABI that the kazan draw path uses.
+ *
+ * Written from the Vulkan specification (types, enumerant values and struct member order are the
+ * ones the specification fixes, so any Vulkan application or loader can talk to this driver).  The
+ * reference driver obtains the same declarations through bindgen over Vulkan-Headers
+ * (vulkan-driver/build.rs:44-176, vulkan-driver/vulkan-wrapper.h:1-20); those headers are not
+ * vendored with it, so this project declares what it needs itself.
+ *
+ * Only 64-bit targets are supported: every non-dispatchable handle is a pointer-sized opaque
+ * handle, as the specification defines for 64-bit platforms.
+ */
+#ifndef KZ_VK_ABI_H
+#define KZ_VK_ABI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VKAPI_ATTR
+#define VKAPI_CALL
+#define VKAPI_PTR
+
+#define VK_MAKE_VERSION(major, minor, patch) \
+  ((((uint32_t)(major)) << 22) | (((uint32_t)(minor)) << 12) | ((uint32_t)(patch)))
+#define VK_API_VERSION_1_0 VK_MAKE_VERSION(1, 0, 0)
+#define VK_API_VERSION_1_1 VK_MAKE_VERSION(1, 1, 0)
+
+#define VK_TRUE 1u
+#define VK_FALSE 0u
+#define VK_WHOLE_SIZE (~0ULL)
+#define VK_ATTACHMENT_UNUSED (~0U)
+#define VK_QUEUE_FAMILY_IGNORED (~0U)
+#define VK_SUBPASS_EXTERNAL (~0U)
+#define VK_REMAINING_MIP_LEVELS (~0U)
+#define VK_REMAINING_ARRAY_LAYERS (~0U)
+#define VK_MAX_PHYSICAL_DEVICE_NAME_SIZE 256
+#define VK_UUID_SIZE 16
+#define VK_MAX_EXTENSION_NAME_SIZE 256
+#define VK_MAX_DESCRIPTION_SIZE 256
+#define VK_MAX_MEMORY_TYPES 32
+#define VK_MAX_MEMORY_HEAPS 16
+
+/* loader <-> ICD contract: first word of every dispatchable object */
+#define ICD_LOADER_MAGIC 0x01CDC0DEu
+
+typedef uint32_t VkFlags;
+typedef uint32_t VkBool32;
+typedef uint64_t VkDeviceSize;
+typedef uint32_t VkSampleMask;
+
+#define KZ_DEFINE_HANDLE(object) typedef struct object##_T* object;
+KZ_DEFINE_HANDLE(VkInstance)
+KZ_DEFINE_HANDLE(VkPhysicalDevice)
+KZ_DEFINE_HANDLE(VkDevice)
+KZ_DEFINE_HANDLE(VkQueue)
+KZ_DEFINE_HANDLE(VkCommandBuffer)
+KZ_DEFINE_HANDLE(VkSemaphore)
+KZ_DEFINE_HANDLE(VkFence)
+KZ_DEFINE_HANDLE(VkDeviceMemory)
+KZ_DEFINE_HANDLE(VkBuffer)
+KZ_DEFINE_HANDLE(VkImage)
+KZ_DEFINE_HANDLE(VkEvent)
+KZ_DEFINE_HANDLE(VkQueryPool)
+KZ_DEFINE_HANDLE(VkBufferView)
+KZ_DEFINE_HANDLE(VkImageView)
+KZ_DEFINE_HANDLE(VkShaderModule)
+KZ_DEFINE_HANDLE(VkPipelineCache)
+KZ_DEFINE_HANDLE(VkPipelineLayout)
+KZ_DEFINE_HANDLE(VkRenderPass)
+KZ_DEFINE_HANDLE(VkPipeline)
+KZ_DEFINE_HANDLE(VkDescriptorSetLayout)
+KZ_DEFINE_HANDLE(VkSampler)
+KZ_DEFINE_HANDLE(VkDescriptorPool)
+KZ_DEFINE_HANDLE(VkDescriptorSet)
+KZ_DEFINE_HANDLE(VkFramebuffer)
+KZ_DEFINE_HANDLE(VkCommandPool)
+#undef KZ_DEFINE_HANDLE
+
+typedef enum VkResult {
+  VK_SUCCESS = 0,
+  VK_NOT_READY = 1,
+  VK_TIMEOUT = 2,
+  VK_EVENT_SET = 3,
+  VK_EVENT_RESET = 4,
+  VK_INCOMPLETE = 5,
+  VK_ERROR_OUT_OF_HOST_MEMORY = -1,
+  VK_ERROR_OUT_OF_DEVICE_MEMORY = -2,
+  VK_ERROR_INITIALIZATION_FAILED = -3,
+  VK_ERROR_DEVICE_LOST = -4,
+  VK_ERROR_MEMORY_MAP_FAILED = -5,
+  VK_ERROR_LAYER_NOT_PRESENT = -6,
+  VK_ERROR_EXTENSION_NOT_PRESENT = -7,
+  VK_ERROR_FEATURE_NOT_PRESENT = -8,
+  VK_ERROR_INCOMPATIBLE_DRIVER = -9,
+  VK_ERROR_TOO_MANY_OBJECTS = -10,
+  VK_ERROR_FORMAT_NOT_SUPPORTED = -11,
+  VK_ERROR_FRAGMENTED_POOL = -12,
+  VK_ERROR_UNKNOWN = -13,
+  VK_ERROR_INVALID_SHADER_NV = -1000012000,
+  VK_RESULT_MAX_ENUM = 0x7FFFFFFF
+} VkResult;
+
+typedef enum VkStructureType {
+  VK_STRUCTURE_TYPE_APPLICATION_INFO = 0,
+  VK_STRUCTURE_TYPE_INSTANCE_CREATE_INFO = 1,
+  VK_STRUCTURE_TYPE_DEVICE_QUEUE_CREATE_INFO = 2,
+  VK_STRUCTURE_TYPE_DEVICE_CREATE_INFO = 3,
+  VK_STRUCTURE_TYPE_SUBMIT_INFO = 4,
+  VK_STRUCTURE_TYPE_MEMORY_ALLOCATE_INFO = 5,
+  VK_STRUCTURE_TYPE_MAPPED_MEMORY_RANGE = 6,
+  VK_STRUCTURE_TYPE_BIND_SPARSE_INFO = 7,
+  VK_STRUCTURE_TYPE_FENCE_CREATE_INFO = 8,
+  VK_STRUCTURE_TYPE_SEMAPHORE_CREATE_INFO = 9,
+  VK_STRUCTURE_TYPE_EVENT_CREATE_INFO = 10,
+  VK_STRUCTURE_TYPE_QUERY_POOL_CREATE_INFO = 11,
+  VK_STRUCTURE_TYPE_BUFFER_CREATE_INFO = 12,
+  VK_STRUCTURE_TYPE_BUFFER_VIEW_CREATE_INFO = 13,
+  VK_STRUCTURE_TYPE_IMAGE_CREATE_INFO = 14,
+  VK_STRUCTURE_TYPE_IMAGE_VIEW_CREATE_INFO = 15,
+  VK_STRUCTURE_TYPE_SHADER_MODULE_CREATE_INFO = 16,
+  VK_STRUCTURE_TYPE_PIPELINE_CACHE_CREATE_INFO = 17,
+  VK_STRUCTURE_TYPE_PIPELINE_SHADER_STAGE_CREATE_INFO = 18,
+  VK_STRUCTURE_TYPE_PIPELINE_VERTEX_INPUT_STATE_CREATE_INFO = 19,
+  VK_STRUCTURE_TYPE_PIPELINE_INPUT_ASSEMBLY_STATE_CREATE_INFO = 20,
+  VK_STRUCTURE_TYPE_PIPELINE_TESSELLATION_STATE_CREATE_INFO = 21,
+  VK_STRUCTURE_TYPE_PIPELINE_VIEWPORT_STATE_CREATE_INFO = 22,
+  VK_STRUCTURE_TYPE_PIPELINE_RASTERIZATION_STATE_CREATE_INFO = 23,
+  VK_STRUCTURE_TYPE_PIPELINE_MULTISAMPLE_STATE_CREATE_INFO = 24,
+  VK_STRUCTURE_TYPE_PIPELINE_DEPTH_STENCIL_STATE_CREATE_INFO = 25,
+  VK_STRUCTURE_TYPE_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO = 26,
+  VK_STRUCTURE_TYPE_PIPELINE_DYNAMIC_STATE_CREATE_INFO = 27,
+  VK_STRUCTURE_TYPE_GRAPHICS_PIPELINE_CREATE_INFO = 28,
+  VK_STRUCTURE_TYPE_COMPUTE_PIPELINE_CREATE_INFO = 29,
+  VK_STRUCTURE_TYPE_PIPELINE_LAYOUT_CREATE_INFO = 30,
+  VK_STRUCTURE_TYPE_SAMPLER_CREATE_INFO = 31,
+  VK_STRUCTURE_TYPE_DESCRIPTOR_SET_LAYOUT_CREATE_INFO = 32,
+  VK_STRUCTURE_TYPE_DESCRIPTOR_POOL_CREATE_INFO = 33,
+  VK_STRUCTURE_TYPE_DESCRIPTOR_SET_ALLOCATE_INFO = 34,
+  VK_STRUCTURE_TYPE_WRITE_DESCRIPTOR_SET = 35,
+  VK_STRUCTURE_TYPE_COPY_DESCRIPTOR_SET = 36,
+  VK_STRUCTURE_TYPE_FRAMEBUFFER_CREATE_INFO = 37,
+  VK_STRUCTURE_TYPE_RENDER_PASS_CREATE_INFO = 38,
+  VK_STRUCTURE_TYPE_COMMAND_POOL_CREATE_INFO = 39,
+  VK_STRUCTURE_TYPE_COMMAND_BUFFER_ALLOCATE_INFO = 40,
+  VK_STRUCTURE_TYPE_COMMAND_BUFFER_INHERITANCE_INFO = 41,
+  VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO = 42,
+  VK_STRUCTURE_TYPE_RENDER_PASS_BEGIN_INFO = 43,
+  VK_STRUCTURE_TYPE_BUFFER_MEMORY_BARRIER = 44,
+  VK_STRUCTURE_TYPE_IMAGE_MEMORY_BARRIER = 45,
+  VK_STRUCTURE_TYPE_MEMORY_BARRIER = 46,
+  VK_STRUCTURE_TYPE_LOADER_INSTANCE_CREATE_INFO = 47,
+  VK_STRUCTURE_TYPE_LOADER_DEVICE_CREATE_INFO = 48,
+  VK_STRUCTURE_TYPE_BIND_BUFFER_MEMORY_INFO = 1000157000,
+  VK_STRUCTURE_TYPE_BIND_IMAGE_MEMORY_INFO = 1000157001,
+  VK_STRUCTURE_TYPE_MAX_ENUM = 0x7FFFFFFF
+} VkStructureType;
+
+typedef enum VkFormat {
+  VK_FORMAT_UNDEFINED = 0,
+  VK_FORMAT_R8G8B8A8_UNORM = 37,
+  VK_FORMAT_R8G8B8A8_SRGB = 43,
+  VK_FORMAT_B8G8R8A8_UNORM = 44,
+  VK_FORMAT_R32_UINT = 98,
+  VK_FORMAT_R32_SINT = 99,
+  VK_FORMAT_R32_SFLOAT = 100,
+  VK_FORMAT_R32G32_UINT = 101,
+  VK_FORMAT_R32G32_SINT = 102,
+  VK_FORMAT_R32G32_SFLOAT = 103,
+  VK_FORMAT_R32G32B32_UINT = 104,
+  VK_FORMAT_R32G32B32_SINT = 105,
+  VK_FORMAT_R32G32B32_SFLOAT = 106,
+  VK_FORMAT_R32G32B32A32_UINT = 107,
+  VK_FORMAT_R32G32B32A32_SINT = 108,
+  VK_FORMAT_R32G32B32A32_SFLOAT = 109,
+  VK_FORMAT_D16_UNORM = 124,
+  VK_FORMAT_D32_SFLOAT = 126,
+  VK_FORMAT_D24_UNORM_S8_UINT = 129,
+  VK_FORMAT_MAX_ENUM = 0x7FFFFFFF
+} VkFormat;
+
+typedef enum VkImageType { VK_IMAGE_TYPE_1D = 0, VK_IMAGE_TYPE_2D = 1, VK_IMAGE_TYPE_3D = 2, VK_IMAGE_TYPE_MAX_ENUM = 0x7FFFFFFF } VkImageType;
+typedef enum VkImageTiling { VK_IMAGE_TILING_OPTIMAL = 0, VK_IMAGE_TILING_LINEAR = 1, VK_IMAGE_TILING_MAX_ENUM = 0x7FFFFFFF } VkImageTiling;
+typedef enum VkImageViewType {
+  VK_IMAGE_VIEW_TYPE_1D = 0, VK_IMAGE_VIEW_TYPE_2D = 1, VK_IMAGE_VIEW_TYPE_3D = 2, VK_IMAGE_VIEW_TYPE_CUBE = 3,
+  VK_IMAGE_VIEW_TYPE_1D_ARRAY = 4, VK_IMAGE_VIEW_TYPE_2D_ARRAY = 5, VK_IMAGE_VIEW_TYPE_CUBE_ARRAY = 6,
+  VK_IMAGE_VIEW_TYPE_MAX_ENUM = 0x7FFFFFFF
+} VkImageViewType;
+typedef enum VkImageLayout {
+  VK_IMAGE_LAYOUT_UNDEFINED = 0,
+  VK_IMAGE_LAYOUT_GENERAL = 1,
+  VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL = 2,
+  VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL = 3,
+  VK_IMAGE_LAYOUT_DEPTH_STENCIL_READ_ONLY_OPTIMAL = 4,
+  VK_IMAGE_LAYOUT_SHADER_READ_ONLY_OPTIMAL = 5,
+  VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL = 6,
+  VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL = 7,
+  VK_IMAGE_LAYOUT_PREINITIALIZED = 8,
+  VK_IMAGE_LAYOUT_PRESENT_SRC_KHR = 1000001002,
+  VK_IMAGE_LAYOUT_MAX_ENUM = 0x7FFFFFFF
+} VkImageLayout;
+typedef enum VkSharingMode { VK_SHARING_MODE_EXCLUSIVE = 0, VK_SHARING_MODE_CONCURRENT = 1, VK_SHARING_MODE_MAX_ENUM = 0x7FFFFFFF } VkSharingMode;
+typedef enum VkComponentSwizzle {
+  VK_COMPONENT_SWIZZLE_IDENTITY = 0, VK_COMPONENT_SWIZZLE_ZERO = 1, VK_COMPONENT_SWIZZLE_ONE = 2,
+  VK_COMPONENT_SWIZZLE_R = 3, VK_COMPONENT_SWIZZLE_G = 4, VK_COMPONENT_SWIZZLE_B = 5, VK_COMPONENT_SWIZZLE_A = 6,
+  VK_COMPONENT_SWIZZLE_MAX_ENUM = 0x7FFFFFFF
+} VkComponentSwizzle;
+typedef enum VkPhysicalDeviceType {
+  VK_PHYSICAL_DEVICE_TYPE_OTHER = 0, VK_PHYSICAL_DEVICE_TYPE_INTEGRATED_GPU = 1, VK_PHYSICAL_DEVICE_TYPE_DISCRETE_GPU = 2,
+  VK_PHYSICAL_DEVICE_TYPE_VIRTUAL_GPU = 3, VK_PHYSICAL_DEVICE_TYPE_CPU = 4, VK_PHYSICAL_DEVICE_TYPE_MAX_ENUM = 0x7FFFFFFF
+} VkPhysicalDeviceType;
+typedef enum VkVertexInputRate { VK_VERTEX_INPUT_RATE_VERTEX = 0, VK_VERTEX_INPUT_RATE_INSTANCE = 1, VK_VERTEX_INPUT_RATE_MAX_ENUM = 0x7FFFFFFF } VkVertexInputRate;
+typedef enum VkPrimitiveTopology {
+  VK_PRIMITIVE_TOPOLOGY_POINT_LIST = 0, VK_PRIMITIVE_TOPOLOGY_LINE_LIST = 1, VK_PRIMITIVE_TOPOLOGY_LINE_STRIP = 2,
+  VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST = 3, VK_PRIMITIVE_TOPOLOGY_TRIANGLE_STRIP = 4, VK_PRIMITIVE_TOPOLOGY_TRIANGLE_FAN = 5,
+  VK_PRIMITIVE_TOPOLOGY_MAX_ENUM = 0x7FFFFFFF
+} VkPrimitiveTopology;
+typedef enum VkPolygonMode { VK_POLYGON_MODE_FILL = 0, VK_POLYGON_MODE_LINE = 1, VK_POLYGON_MODE_POINT = 2, VK_POLYGON_MODE_MAX_ENUM = 0x7FFFFFFF } VkPolygonMode;
+typedef enum VkFrontFace { VK_FRONT_FACE_COUNTER_CLOCKWISE = 0, VK_FRONT_FACE_CLOCKWISE = 1, VK_FRONT_FACE_MAX_ENUM = 0x7FFFFFFF } VkFrontFace;
+typedef enum VkCompareOp {
+  VK_COMPARE_OP_NEVER = 0, VK_COMPARE_OP_LESS = 1, VK_COMPARE_OP_EQUAL = 2, VK_COMPARE_OP_LESS_OR_EQUAL = 3,
+  VK_COMPARE_OP_GREATER = 4, VK_COMPARE_OP_NOT_EQUAL = 5, VK_COMPARE_OP_GREATER_OR_EQUAL = 6, VK_COMPARE_OP_ALWAYS = 7,
+  VK_COMPARE_OP_MAX_ENUM = 0x7FFFFFFF
+} VkCompareOp;
+typedef enum VkStencilOp {
+  VK_STENCIL_OP_KEEP = 0, VK_STENCIL_OP_ZERO = 1, VK_STENCIL_OP_REPLACE = 2, VK_STENCIL_OP_INCREMENT_AND_CLAMP = 3,
+  VK_STENCIL_OP_DECREMENT_AND_CLAMP = 4, VK_STENCIL_OP_INVERT = 5, VK_STENCIL_OP_INCREMENT_AND_WRAP = 6,
+  VK_STENCIL_OP_DECREMENT_AND_WRAP = 7, VK_STENCIL_OP_MAX_ENUM = 0x7FFFFFFF
+} VkStencilOp;
+typedef enum VkLogicOp { VK_LOGIC_OP_CLEAR = 0, VK_LOGIC_OP_COPY = 3, VK_LOGIC_OP_MAX_ENUM = 0x7FFFFFFF } VkLogicOp;
+typedef enum VkBlendFactor {
+  VK_BLEND_FACTOR_ZERO = 0, VK_BLEND_FACTOR_ONE = 1, VK_BLEND_FACTOR_SRC_COLOR = 2, VK_BLEND_FACTOR_ONE_MINUS_SRC_COLOR = 3,
+  VK_BLEND_FACTOR_DST_COLOR = 4, VK_BLEND_FACTOR_ONE_MINUS_DST_COLOR = 5, VK_BLEND_FACTOR_SRC_ALPHA = 6,
+  VK_BLEND_FACTOR_ONE_MINUS_SRC_ALPHA = 7, VK_BLEND_FACTOR_DST_ALPHA = 8, VK_BLEND_FACTOR_ONE_MINUS_DST_ALPHA = 9,
+  VK_BLEND_FACTOR_CONSTANT_COLOR = 10, VK_BLEND_FACTOR_ONE_MINUS_CONSTANT_COLOR = 11, VK_BLEND_FACTOR_CONSTANT_ALPHA = 12,
+  VK_BLEND_FACTOR_ONE_MINUS_CONSTANT_ALPHA = 13, VK_BLEND_FACTOR_SRC_ALPHA_SATURATE = 14,
+  VK_BLEND_FACTOR_MAX_ENUM = 0x7FFFFFFF
+} VkBlendFactor;
+typedef enum VkBlendOp {
+  VK_BLEND_OP_ADD = 0, VK_BLEND_OP_SUBTRACT = 1, VK_BLEND_OP_REVERSE_SUBTRACT = 2, VK_BLEND_OP_MIN = 3, VK_BLEND_OP_MAX = 4,
+  VK_BLEND_OP_MAX_ENUM = 0x7FFFFFFF
+} VkBlendOp;
+typedef enum VkDynamicState {
+  VK_DYNAMIC_STATE_VIEWPORT = 0, VK_DYNAMIC_STATE_SCISSOR = 1, VK_DYNAMIC_STATE_LINE_WIDTH = 2, VK_DYNAMIC_STATE_DEPTH_BIAS = 3,
+  VK_DYNAMIC_STATE_BLEND_CONSTANTS = 4, VK_DYNAMIC_STATE_DEPTH_BOUNDS = 5, VK_DYNAMIC_STATE_STENCIL_COMPARE_MASK = 6,
+  VK_DYNAMIC_STATE_STENCIL_WRITE_MASK = 7, VK_DYNAMIC_STATE_STENCIL_REFERENCE = 8, VK_DYNAMIC_STATE_MAX_ENUM = 0x7FFFFFFF
+} VkDynamicState;
+typedef enum VkAttachmentLoadOp { VK_ATTACHMENT_LOAD_OP_LOAD = 0, VK_ATTACHMENT_LOAD_OP_CLEAR = 1, VK_ATTACHMENT_LOAD_OP_DONT_CARE = 2, VK_ATTACHMENT_LOAD_OP_MAX_ENUM = 0x7FFFFFFF } VkAttachmentLoadOp;
+typedef enum VkAttachmentStoreOp { VK_ATTACHMENT_STORE_OP_STORE = 0, VK_ATTACHMENT_STORE_OP_DONT_CARE = 1, VK_ATTACHMENT_STORE_OP_MAX_ENUM = 0x7FFFFFFF } VkAttachmentStoreOp;
+typedef enum VkPipelineBindPoint { VK_PIPELINE_BIND_POINT_GRAPHICS = 0, VK_PIPELINE_BIND_POINT_COMPUTE = 1, VK_PIPELINE_BIND_POINT_MAX_ENUM = 0x7FFFFFFF } VkPipelineBindPoint;
+typedef enum VkCommandBufferLevel { VK_COMMAND_BUFFER_LEVEL_PRIMARY = 0, VK_COMMAND_BUFFER_LEVEL_SECONDARY = 1, VK_COMMAND_BUFFER_LEVEL_MAX_ENUM = 0x7FFFFFFF } VkCommandBufferLevel;
+typedef enum VkIndexType { VK_INDEX_TYPE_UINT16 = 0, VK_INDEX_TYPE_UINT32 = 1, VK_INDEX_TYPE_MAX_ENUM = 0x7FFFFFFF } VkIndexType;
+typedef enum VkSubpassContents { VK_SUBPASS_CONTENTS_INLINE = 0, VK_SUBPASS_CONTENTS_SECONDARY_COMMAND_BUFFERS = 1, VK_SUBPASS_CONTENTS_MAX_ENUM = 0x7FFFFFFF } VkSubpassContents;
+typedef enum VkSystemAllocationScope { VK_SYSTEM_ALLOCATION_SCOPE_COMMAND = 0, VK_SYSTEM_ALLOCATION_SCOPE_MAX_ENUM = 0x7FFFFFFF } VkSystemAllocationScope;
+typedef enum VkInternalAllocationType { VK_INTERNAL_ALLOCATION_TYPE_EXECUTABLE = 0, VK_INTERNAL_ALLOCATION_TYPE_MAX_ENUM = 0x7FFFFFFF } VkInternalAllocationType;
+
+/* flag bits */
+typedef VkFlags VkInstanceCreateFlags;
+typedef VkFlags VkDeviceCreateFlags;
+typedef VkFlags VkDeviceQueueCreateFlags;
+typedef VkFlags VkMemoryMapFlags;
+typedef VkFlags VkFenceCreateFlags;
+typedef VkFlags VkSemaphoreCreateFlags;
+typedef VkFlags VkBufferCreateFlags;
+typedef VkFlags VkBufferUsageFlags;
+typedef VkFlags VkImageCreateFlags;
+typedef VkFlags VkImageUsageFlags;
+typedef VkFlags VkImageViewCreateFlags;
+typedef VkFlags VkImageAspectFlags;
+typedef VkFlags VkShaderModuleCreateFlags;
+typedef VkFlags VkPipelineCacheCreateFlags;
+typedef VkFlags VkPipelineCreateFlags;
+typedef VkFlags VkPipelineShaderStageCreateFlags;
+typedef VkFlags VkPipelineVertexInputStateCreateFlags;
+typedef VkFlags VkPipelineInputAssemblyStateCreateFlags;
+typedef VkFlags VkPipelineTessellationStateCreateFlags;
+typedef VkFlags VkPipelineViewportStateCreateFlags;
+typedef VkFlags VkPipelineRasterizationStateCreateFlags;
+typedef VkFlags VkPipelineMultisampleStateCreateFlags;
+typedef VkFlags VkPipelineDepthStencilStateCreateFlags;
+typedef VkFlags VkPipelineColorBlendStateCreateFlags;
+typedef VkFlags VkPipelineDynamicStateCreateFlags;
+typedef VkFlags VkPipelineLayoutCreateFlags;
+typedef VkFlags VkShaderStageFlags;
+typedef VkFlags VkCullModeFlags;
+typedef VkFlags VkColorComponentFlags;
+typedef VkFlags VkSampleCountFlags;
+typedef VkFlags VkFramebufferCreateFlags;
+typedef VkFlags VkRenderPassCreateFlags;
+typedef VkFlags VkAttachmentDescriptionFlags;
+typedef VkFlags VkSubpassDescriptionFlags;
+typedef VkFlags VkPipelineStageFlags;
+typedef VkFlags VkAccessFlags;
+typedef VkFlags VkDependencyFlags;
+typedef VkFlags VkCommandPoolCreateFlags;
+typedef VkFlags VkCommandPoolResetFlags;
+typedef VkFlags VkCommandBufferUsageFlags;
+typedef VkFlags VkCommandBufferResetFlags;
+typedef VkFlags VkQueryControlFlags;
+typedef VkFlags VkQueryPipelineStatisticFlags;
+typedef VkFlags VkQueueFlags;
+typedef VkFlags VkMemoryPropertyFlags;
+typedef VkFlags VkMemoryHeapFlags;
+typedef VkFlags VkFormatFeatureFlags;
+typedef VkFlags VkStencilFaceFlags;
+
+#define VK_QUEUE_GRAPHICS_BIT 0x1u
+#define VK_QUEUE_COMPUTE_BIT 0x2u
+#define VK_QUEUE_TRANSFER_BIT 0x4u
+#define VK_MEMORY_PROPERTY_DEVICE_LOCAL_BIT 0x1u
+#define VK_MEMORY_PROPERTY_HOST_VISIBLE_BIT 0x2u
+#define VK_MEMORY_PROPERTY_HOST_COHERENT_BIT 0x4u
+#define VK_MEMORY_PROPERTY_HOST_CACHED_BIT 0x8u
+#define VK_MEMORY_HEAP_DEVICE_LOCAL_BIT 0x1u
+#define VK_FENCE_CREATE_SIGNALED_BIT 0x1u
+#define VK_BUFFER_USAGE_TRANSFER_SRC_BIT 0x1u
+#define VK_BUFFER_USAGE_TRANSFER_DST_BIT 0x2u
+#define VK_BUFFER_USAGE_UNIFORM_BUFFER_BIT 0x10u
+#define VK_BUFFER_USAGE_STORAGE_BUFFER_BIT 0x20u
+#define VK_BUFFER_USAGE_INDEX_BUFFER_BIT 0x40u
+#define VK_BUFFER_USAGE_VERTEX_BUFFER_BIT 0x80u
+#define VK_BUFFER_USAGE_INDIRECT_BUFFER_BIT 0x100u
+#define VK_IMAGE_USAGE_TRANSFER_SRC_BIT 0x1u
+#define VK_IMAGE_USAGE_TRANSFER_DST_BIT 0x2u
+#define VK_IMAGE_USAGE_SAMPLED_BIT 0x4u
+#define VK_IMAGE_USAGE_STORAGE_BIT 0x8u
+#define VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT 0x10u
+#define VK_IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT_BIT 0x20u
+#define VK_IMAGE_ASPECT_COLOR_BIT 0x1u
+#define VK_IMAGE_ASPECT_DEPTH_BIT 0x2u
+#define VK_IMAGE_ASPECT_STENCIL_BIT 0x4u
+#define VK_SAMPLE_COUNT_1_BIT 0x1u
+#define VK_SAMPLE_COUNT_4_BIT 0x4u
+#define VK_SHADER_STAGE_VERTEX_BIT 0x1u
+#define VK_SHADER_STAGE_FRAGMENT_BIT 0x10u
+#define VK_SHADER_STAGE_COMPUTE_BIT 0x20u
+#define VK_SHADER_STAGE_ALL_GRAPHICS 0x1Fu
+#define VK_CULL_MODE_NONE 0u
+#define VK_CULL_MODE_FRONT_BIT 0x1u
+#define VK_CULL_MODE_BACK_BIT 0x2u
+#define VK_CULL_MODE_FRONT_AND_BACK 0x3u
+#define VK_COLOR_COMPONENT_R_BIT 0x1u
+#define VK_COLOR_COMPONENT_G_BIT 0x2u
+#define VK_COLOR_COMPONENT_B_BIT 0x4u
+#define VK_COLOR_COMPONENT_A_BIT 0x8u
+#define VK_COMMAND_POOL_CREATE_TRANSIENT_BIT 0x1u
+#define VK_COMMAND_POOL_CREATE_RESET_COMMAND_BUFFER_BIT 0x2u
+#define VK_COMMAND_BUFFER_USAGE_ONE_TIME_SUBMIT_BIT 0x1u
+#define VK_COMMAND_BUFFER_USAGE_SIMULTANEOUS_USE_BIT 0x4u
+#define VK_FORMAT_FEATURE_SAMPLED_IMAGE_BIT 0x1u
+#define VK_FORMAT_FEATURE_VERTEX_BUFFER_BIT 0x40u
+#define VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT 0x80u
+#define VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT 0x100u
+#define VK_FORMAT_FEATURE_DEPTH_STENCIL_ATTACHMENT_BIT 0x200u
+#define VK_FORMAT_FEATURE_TRANSFER_SRC_BIT 0x4000u
+#define VK_FORMAT_FEATURE_TRANSFER_DST_BIT 0x8000u
+
+/* callbacks */
+typedef void(VKAPI_PTR* PFN_vkVoidFunction)(void);
+typedef void*(VKAPI_PTR* PFN_vkAllocationFunction)(void* pUserData, size_t size, size_t alignment, VkSystemAllocationScope scope);
+typedef void*(VKAPI_PTR* PFN_vkReallocationFunction)(void* pUserData, void* pOriginal, size_t size, size_t alignment, VkSystemAllocationScope scope);
+typedef void(VKAPI_PTR* PFN_vkFreeFunction)(void* pUserData, void* pMemory);
+typedef void(VKAPI_PTR* PFN_vkInternalAllocationNotification)(void* pUserData, size_t size, VkInternalAllocationType type, VkSystemAllocationScope scope);
+typedef void(VKAPI_PTR* PFN_vkInternalFreeNotification)(void* pUserData, size_t size, VkInternalAllocationType type, VkSystemAllocationScope scope);
+
+typedef struct VkAllocationCallbacks {
+  void* pUserData;
+  PFN_vkAllocationFunction pfnAllocation;
+  PFN_vkReallocationFunction pfnReallocation;
+  PFN_vkFreeFunction pfnFree;
+  PFN_vkInternalAllocationNotification pfnInternalAllocation;
+  PFN_vkInternalFreeNotification pfnInternalFree;
+} VkAllocationCallbacks;
+
+typedef struct VkOffset2D { int32_t x, y; } VkOffset2D;
+typedef struct VkOffset3D { int32_t x, y, z; } VkOffset3D;
+typedef struct VkExtent2D { uint32_t width, height; } VkExtent2D;
+typedef struct VkExtent3D { uint32_t width, height, depth; } VkExtent3D;
+typedef struct VkRect2D { VkOffset2D offset; VkExtent2D extent; } VkRect2D;
+
+typedef struct VkApplicationInfo {
+  VkStructureType sType;
+  const void* pNext;
+  const char* pApplicationName;
+  uint32_t applicationVersion;
+  const char* pEngineName;
+  uint32_t engineVersion;
+  uint32_t apiVersion;
+} VkApplicationInfo;
+
+typedef struct VkInstanceCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkInstanceCreateFlags flags;
+  const VkApplicationInfo* pApplicationInfo;
+  uint32_t enabledLayerCount;
+  const char* const* ppEnabledLayerNames;
+  uint32_t enabledExtensionCount;
+  const char* const* ppEnabledExtensionNames;
+} VkInstanceCreateInfo;
+
+typedef struct VkExtensionProperties { char extensionName[VK_MAX_EXTENSION_NAME_SIZE]; uint32_t specVersion; } VkExtensionProperties;
+typedef struct VkLayerProperties {
+  char layerName[VK_MAX_EXTENSION_NAME_SIZE];
+  uint32_t specVersion;
+  uint32_t implementationVersion;
+  char description[VK_MAX_DESCRIPTION_SIZE];
+} VkLayerProperties;
+
+typedef struct VkPhysicalDeviceFeatures {
+  VkBool32 robustBufferAccess, fullDrawIndexUint32, imageCubeArray, independentBlend, geometryShader,
+      tessellationShader, sampleRateShading, dualSrcBlend, logicOp, multiDrawIndirect, drawIndirectFirstInstance,
+      depthClamp, depthBiasClamp, fillModeNonSolid, depthBounds, wideLines, largePoints, alphaToOne, multiViewport,
+      samplerAnisotropy, textureCompressionETC2, textureCompressionASTC_LDR, textureCompressionBC,
+      occlusionQueryPrecise, pipelineStatisticsQuery, vertexPipelineStoresAndAtomics, fragmentStoresAndAtomics,
+      shaderTessellationAndGeometryPointSize, shaderImageGatherExtended, shaderStorageImageExtendedFormats,
+      shaderStorageImageMultisample, shaderStorageImageReadWithoutFormat, shaderStorageImageWriteWithoutFormat,
+      shaderUniformBufferArrayDynamicIndexing, shaderSampledImageArrayDynamicIndexing,
+      shaderStorageBufferArrayDynamicIndexing, shaderStorageImageArrayDynamicIndexing, shaderClipDistance,
+      shaderCullDistance, shaderFloat64, shaderInt64, shaderInt16, shaderResourceResidency, shaderResourceMinLod,
+      sparseBinding, sparseResidencyBuffer, sparseResidencyImage2D, sparseResidencyImage3D, sparseResidency2Samples,
+      sparseResidency4Samples, sparseResidency8Samples, sparseResidency16Samples, sparseResidencyAliased,
+      variableMultisampleRate, inheritedQueries;
+} VkPhysicalDeviceFeatures;
+
+typedef struct VkPhysicalDeviceLimits {
+  uint32_t maxImageDimension1D;
+  uint32_t maxImageDimension2D;
+  uint32_t maxImageDimension3D;
+  uint32_t maxImageDimensionCube;
+  uint32_t maxImageArrayLayers;
+  uint32_t maxTexelBufferElements;
+  uint32_t maxUniformBufferRange;
+  uint32_t maxStorageBufferRange;
+  uint32_t maxPushConstantsSize;
+  uint32_t maxMemoryAllocationCount;
+  uint32_t maxSamplerAllocationCount;
+  VkDeviceSize bufferImageGranularity;
+  VkDeviceSize sparseAddressSpaceSize;
+  uint32_t maxBoundDescriptorSets;
+  uint32_t maxPerStageDescriptorSamplers;
+  uint32_t maxPerStageDescriptorUniformBuffers;
+  uint32_t maxPerStageDescriptorStorageBuffers;
+  uint32_t maxPerStageDescriptorSampledImages;
+  uint32_t maxPerStageDescriptorStorageImages;
+  uint32_t maxPerStageDescriptorInputAttachments;
+  uint32_t maxPerStageResources;
+  uint32_t maxDescriptorSetSamplers;
+  uint32_t maxDescriptorSetUniformBuffers;
+  uint32_t maxDescriptorSetUniformBuffersDynamic;
+  uint32_t maxDescriptorSetStorageBuffers;
+  uint32_t maxDescriptorSetStorageBuffersDynamic;
+  uint32_t maxDescriptorSetSampledImages;
+  uint32_t maxDescriptorSetStorageImages;
+  uint32_t maxDescriptorSetInputAttachments;
+  uint32_t maxVertexInputAttributes;
+  uint32_t maxVertexInputBindings;
+  uint32_t maxVertexInputAttributeOffset;
+  uint32_t maxVertexInputBindingStride;
+  uint32_t maxVertexOutputComponents;
+  uint32_t maxTessellationGenerationLevel;
+  uint32_t maxTessellationPatchSize;
+  uint32_t maxTessellationControlPerVertexInputComponents;
+  uint32_t maxTessellationControlPerVertexOutputComponents;
+  uint32_t maxTessellationControlPerPatchOutputComponents;
+  uint32_t maxTessellationControlTotalOutputComponents;
+  uint32_t maxTessellationEvaluationInputComponents;
+  uint32_t maxTessellationEvaluationOutputComponents;
+  uint32_t maxGeometryShaderInvocations;
+  uint32_t maxGeometryInputComponents;
+  uint32_t maxGeometryOutputComponents;
+  uint32_t maxGeometryOutputVertices;
+  uint32_t maxGeometryTotalOutputComponents;
+  uint32_t maxFragmentInputComponents;
+  uint32_t maxFragmentOutputAttachments;
+  uint32_t maxFragmentDualSrcAttachments;
+  uint32_t maxFragmentCombinedOutputResources;
+  uint32_t maxComputeSharedMemorySize;
+  uint32_t maxComputeWorkGroupCount[3];
+  uint32_t maxComputeWorkGroupInvocations;
+  uint32_t maxComputeWorkGroupSize[3];
+  uint32_t subPixelPrecisionBits;
+  uint32_t subTexelPrecisionBits;
+  uint32_t mipmapPrecisionBits;
+  uint32_t maxDrawIndexedIndexValue;
+  uint32_t maxDrawIndirectCount;
+  float maxSamplerLodBias;
+  float maxSamplerAnisotropy;
+  uint32_t maxViewports;
+  uint32_t maxViewportDimensions[2];
+  float viewportBoundsRange[2];
+  uint32_t viewportSubPixelBits;
+  size_t minMemoryMapAlignment;
+  VkDeviceSize minTexelBufferOffsetAlignment;
+  VkDeviceSize minUniformBufferOffsetAlignment;
+  VkDeviceSize minStorageBufferOffsetAlignment;
+  int32_t minTexelOffset;
+  uint32_t maxTexelOffset;
+  int32_t minTexelGatherOffset;
+  uint32_t maxTexelGatherOffset;
+  float minInterpolationOffset;
+  float maxInterpolationOffset;
+  uint32_t subPixelInterpolationOffsetBits;
+  uint32_t maxFramebufferWidth;
+  uint32_t maxFramebufferHeight;
+  uint32_t maxFramebufferLayers;
+  VkSampleCountFlags framebufferColorSampleCounts;
+  VkSampleCountFlags framebufferDepthSampleCounts;
+  VkSampleCountFlags framebufferStencilSampleCounts;
+  VkSampleCountFlags framebufferNoAttachmentsSampleCounts;
+  uint32_t maxColorAttachments;
+  VkSampleCountFlags sampledImageColorSampleCounts;
+  VkSampleCountFlags sampledImageIntegerSampleCounts;
+  VkSampleCountFlags sampledImageDepthSampleCounts;
+  VkSampleCountFlags sampledImageStencilSampleCounts;
+  VkSampleCountFlags storageImageSampleCounts;
+  uint32_t maxSampleMaskWords;
+  VkBool32 timestampComputeAndGraphics;
+  float timestampPeriod;
+  uint32_t maxClipDistances;
+  uint32_t maxCullDistances;
+  uint32_t maxCombinedClipAndCullDistances;
+  uint32_t discreteQueuePriorities;
+  float pointSizeRange[2];
+  float lineWidthRange[2];
+  float pointSizeGranularity;
+  float lineWidthGranularity;
+  VkBool32 strictLines;
+  VkBool32 standardSampleLocations;
+  VkDeviceSize optimalBufferCopyOffsetAlignment;
+  VkDeviceSize optimalBufferCopyRowPitchAlignment;
+  VkDeviceSize nonCoherentAtomSize;
+} VkPhysicalDeviceLimits;
+
+typedef struct VkPhysicalDeviceSparseProperties {
+  VkBool32 residencyStandard2DBlockShape, residencyStandard2DMultisampleBlockShape, residencyStandard3DBlockShape,
+      residencyAlignedMipSize, residencyNonResidentStrict;
+} VkPhysicalDeviceSparseProperties;
+
+typedef struct VkPhysicalDeviceProperties {
+  uint32_t apiVersion;
+  uint32_t driverVersion;
+  uint32_t vendorID;
+  uint32_t deviceID;
+  VkPhysicalDeviceType deviceType;
+  char deviceName[VK_MAX_PHYSICAL_DEVICE_NAME_SIZE];
+  uint8_t pipelineCacheUUID[VK_UUID_SIZE];
+  VkPhysicalDeviceLimits limits;
+  VkPhysicalDeviceSparseProperties sparseProperties;
+} VkPhysicalDeviceProperties;
+
+typedef struct VkQueueFamilyProperties {
+  VkQueueFlags queueFlags;
+  uint32_t queueCount;
+  uint32_t timestampValidBits;
+  VkExtent3D minImageTransferGranularity;
+} VkQueueFamilyProperties;
+
+typedef struct VkMemoryType { VkMemoryPropertyFlags propertyFlags; uint32_t heapIndex; } VkMemoryType;
+typedef struct VkMemoryHeap { VkDeviceSize size; VkMemoryHeapFlags flags; } VkMemoryHeap;
+typedef struct VkPhysicalDeviceMemoryProperties {
+  uint32_t memoryTypeCount;
+  VkMemoryType memoryTypes[VK_MAX_MEMORY_TYPES];
+  uint32_t memoryHeapCount;
+  VkMemoryHeap memoryHeaps[VK_MAX_MEMORY_HEAPS];
+} VkPhysicalDeviceMemoryProperties;
+
+typedef struct VkFormatProperties {
+  VkFormatFeatureFlags linearTilingFeatures;
+  VkFormatFeatureFlags optimalTilingFeatures;
+  VkFormatFeatureFlags bufferFeatures;
+} VkFormatProperties;
+
+typedef struct VkImageFormatProperties {
+  VkExtent3D maxExtent;
+  uint32_t maxMipLevels;
+  uint32_t maxArrayLayers;
+  VkSampleCountFlags sampleCounts;
+  VkDeviceSize maxResourceSize;
+} VkImageFormatProperties;
+
+typedef struct VkDeviceQueueCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkDeviceQueueCreateFlags flags;
+  uint32_t queueFamilyIndex;
+  uint32_t queueCount;
+  const float* pQueuePriorities;
+} VkDeviceQueueCreateInfo;
+
+typedef struct VkDeviceCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkDeviceCreateFlags flags;
+  uint32_t queueCreateInfoCount;
+  const VkDeviceQueueCreateInfo* pQueueCreateInfos;
+  uint32_t enabledLayerCount;
+  const char* const* ppEnabledLayerNames;
+  uint32_t enabledExtensionCount;
+  const char* const* ppEnabledExtensionNames;
+  const VkPhysicalDeviceFeatures* pEnabledFeatures;
+} VkDeviceCreateInfo;
+
+typedef struct VkSubmitInfo {
+  VkStructureType sType;
+  const void* pNext;
+  uint32_t waitSemaphoreCount;
+  const VkSemaphore* pWaitSemaphores;
+  const VkPipelineStageFlags* pWaitDstStageMask;
+  uint32_t commandBufferCount;
+  const VkCommandBuffer* pCommandBuffers;
+  uint32_t signalSemaphoreCount;
+  const VkSemaphore* pSignalSemaphores;
+} VkSubmitInfo;
+
+typedef struct VkMemoryAllocateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkDeviceSize allocationSize;
+  uint32_t memoryTypeIndex;
+} VkMemoryAllocateInfo;
+
+typedef struct VkMappedMemoryRange {
+  VkStructureType sType;
+  const void* pNext;
+  VkDeviceMemory memory;
+  VkDeviceSize offset;
+  VkDeviceSize size;
+} VkMappedMemoryRange;
+
+typedef struct VkMemoryRequirements { VkDeviceSize size; VkDeviceSize alignment; uint32_t memoryTypeBits; } VkMemoryRequirements;
+
+typedef struct VkFenceCreateInfo { VkStructureType sType; const void* pNext; VkFenceCreateFlags flags; } VkFenceCreateInfo;
+typedef struct VkSemaphoreCreateInfo { VkStructureType sType; const void* pNext; VkSemaphoreCreateFlags flags; } VkSemaphoreCreateInfo;
+
+typedef struct VkBufferCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkBufferCreateFlags flags;
+  VkDeviceSize size;
+  VkBufferUsageFlags usage;
+  VkSharingMode sharingMode;
+  uint32_t queueFamilyIndexCount;
+  const uint32_t* pQueueFamilyIndices;
+} VkBufferCreateInfo;
+
+typedef struct VkImageCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkImageCreateFlags flags;
+  VkImageType imageType;
+  VkFormat format;
+  VkExtent3D extent;
+  uint32_t mipLevels;
+  uint32_t arrayLayers;
+  VkSampleCountFlags samples;
+  VkImageTiling tiling;
+  VkImageUsageFlags usage;
+  VkSharingMode sharingMode;
+  uint32_t queueFamilyIndexCount;
+  const uint32_t* pQueueFamilyIndices;
+  VkImageLayout initialLayout;
+} VkImageCreateInfo;
+
+typedef struct VkImageSubresource { VkImageAspectFlags aspectMask; uint32_t mipLevel; uint32_t arrayLayer; } VkImageSubresource;
+typedef struct VkSubresourceLayout {
+  VkDeviceSize offset;
+  VkDeviceSize size;
+  VkDeviceSize rowPitch;
+  VkDeviceSize arrayPitch;
+  VkDeviceSize depthPitch;
+} VkSubresourceLayout;
+typedef struct VkComponentMapping { VkComponentSwizzle r, g, b, a; } VkComponentMapping;
+typedef struct VkImageSubresourceRange {
+  VkImageAspectFlags aspectMask;
+  uint32_t baseMipLevel;
+  uint32_t levelCount;
+  uint32_t baseArrayLayer;
+  uint32_t layerCount;
+} VkImageSubresourceRange;
+typedef struct VkImageSubresourceLayers {
+  VkImageAspectFlags aspectMask;
+  uint32_t mipLevel;
+  uint32_t baseArrayLayer;
+  uint32_t layerCount;
+} VkImageSubresourceLayers;
+
+typedef struct VkImageViewCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkImageViewCreateFlags flags;
+  VkImage image;
+  VkImageViewType viewType;
+  VkFormat format;
+  VkComponentMapping components;
+  VkImageSubresourceRange subresourceRange;
+} VkImageViewCreateInfo;
+
+typedef struct VkShaderModuleCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkShaderModuleCreateFlags flags;
+  size_t codeSize;
+  const uint32_t* pCode;
+} VkShaderModuleCreateInfo;
+
+typedef struct VkPipelineCacheCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineCacheCreateFlags flags;
+  size_t initialDataSize;
+  const void* pInitialData;
+} VkPipelineCacheCreateInfo;
+
+typedef struct VkSpecializationMapEntry { uint32_t constantID; uint32_t offset; size_t size; } VkSpecializationMapEntry;
+typedef struct VkSpecializationInfo {
+  uint32_t mapEntryCount;
+  const VkSpecializationMapEntry* pMapEntries;
+  size_t dataSize;
+  const void* pData;
+} VkSpecializationInfo;
+
+typedef struct VkPipelineShaderStageCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineShaderStageCreateFlags flags;
+  VkShaderStageFlags stage; /* a single VkShaderStageFlagBits value */
+  VkShaderModule module;
+  const char* pName;
+  const VkSpecializationInfo* pSpecializationInfo;
+} VkPipelineShaderStageCreateInfo;
+
+typedef struct VkVertexInputBindingDescription { uint32_t binding; uint32_t stride; VkVertexInputRate inputRate; } VkVertexInputBindingDescription;
+typedef struct VkVertexInputAttributeDescription { uint32_t location; uint32_t binding; VkFormat format; uint32_t offset; } VkVertexInputAttributeDescription;
+
+typedef struct VkPipelineVertexInputStateCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineVertexInputStateCreateFlags flags;
+  uint32_t vertexBindingDescriptionCount;
+  const VkVertexInputBindingDescription* pVertexBindingDescriptions;
+  uint32_t vertexAttributeDescriptionCount;
+  const VkVertexInputAttributeDescription* pVertexAttributeDescriptions;
+} VkPipelineVertexInputStateCreateInfo;
+
+typedef struct VkPipelineInputAssemblyStateCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineInputAssemblyStateCreateFlags flags;
+  VkPrimitiveTopology topology;
+  VkBool32 primitiveRestartEnable;
+} VkPipelineInputAssemblyStateCreateInfo;
+
+typedef struct VkPipelineTessellationStateCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineTessellationStateCreateFlags flags;
+  uint32_t patchControlPoints;
+} VkPipelineTessellationStateCreateInfo;
+
+typedef struct VkViewport { float x, y, width, height, minDepth, maxDepth; } VkViewport;
+
+typedef struct VkPipelineViewportStateCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineViewportStateCreateFlags flags;
+  uint32_t viewportCount;
+  const VkViewport* pViewports;
+  uint32_t scissorCount;
+  const VkRect2D* pScissors;
+} VkPipelineViewportStateCreateInfo;
+
+typedef struct VkPipelineRasterizationStateCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineRasterizationStateCreateFlags flags;
+  VkBool32 depthClampEnable;
+  VkBool32 rasterizerDiscardEnable;
+  VkPolygonMode polygonMode;
+  VkCullModeFlags cullMode;
+  VkFrontFace frontFace;
+  VkBool32 depthBiasEnable;
+  float depthBiasConstantFactor;
+  float depthBiasClamp;
+  float depthBiasSlopeFactor;
+  float lineWidth;
+} VkPipelineRasterizationStateCreateInfo;
+
+typedef struct VkPipelineMultisampleStateCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineMultisampleStateCreateFlags flags;
+  VkSampleCountFlags rasterizationSamples;
+  VkBool32 sampleShadingEnable;
+  float minSampleShading;
+  const VkSampleMask* pSampleMask;
+  VkBool32 alphaToCoverageEnable;
+  VkBool32 alphaToOneEnable;
+} VkPipelineMultisampleStateCreateInfo;
+
+typedef struct VkStencilOpState {
+  VkStencilOp failOp;
+  VkStencilOp passOp;
+  VkStencilOp depthFailOp;
+  VkCompareOp compareOp;
+  uint32_t compareMask;
+  uint32_t writeMask;
+  uint32_t reference;
+} VkStencilOpState;
+
+typedef struct VkPipelineDepthStencilStateCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineDepthStencilStateCreateFlags flags;
+  VkBool32 depthTestEnable;
+  VkBool32 depthWriteEnable;
+  VkCompareOp depthCompareOp;
+  VkBool32 depthBoundsTestEnable;
+  VkBool32 stencilTestEnable;
+  VkStencilOpState front;
+  VkStencilOpState back;
+  float minDepthBounds;
+  float maxDepthBounds;
+} VkPipelineDepthStencilStateCreateInfo;
+
+typedef struct VkPipelineColorBlendAttachmentState {
+  VkBool32 blendEnable;
+  VkBlendFactor srcColorBlendFactor;
+  VkBlendFactor dstColorBlendFactor;
+  VkBlendOp colorBlendOp;
+  VkBlendFactor srcAlphaBlendFactor;
+  VkBlendFactor dstAlphaBlendFactor;
+  VkBlendOp alphaBlendOp;
+  VkColorComponentFlags colorWriteMask;
+} VkPipelineColorBlendAttachmentState;
+
+typedef struct VkPipelineColorBlendStateCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineColorBlendStateCreateFlags flags;
+  VkBool32 logicOpEnable;
+  VkLogicOp logicOp;
+  uint32_t attachmentCount;
+  const VkPipelineColorBlendAttachmentState* pAttachments;
+  float blendConstants[4];
+} VkPipelineColorBlendStateCreateInfo;
+
+typedef struct VkPipelineDynamicStateCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineDynamicStateCreateFlags flags;
+  uint32_t dynamicStateCount;
+  const VkDynamicState* pDynamicStates;
+} VkPipelineDynamicStateCreateInfo;
+
+typedef struct VkGraphicsPipelineCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineCreateFlags flags;
+  uint32_t stageCount;
+  const VkPipelineShaderStageCreateInfo* pStages;
+  const VkPipelineVertexInputStateCreateInfo* pVertexInputState;
+  const VkPipelineInputAssemblyStateCreateInfo* pInputAssemblyState;
+  const VkPipelineTessellationStateCreateInfo* pTessellationState;
+  const VkPipelineViewportStateCreateInfo* pViewportState;
+  const VkPipelineRasterizationStateCreateInfo* pRasterizationState;
+  const VkPipelineMultisampleStateCreateInfo* pMultisampleState;
+  const VkPipelineDepthStencilStateCreateInfo* pDepthStencilState;
+  const VkPipelineColorBlendStateCreateInfo* pColorBlendState;
+  const VkPipelineDynamicStateCreateInfo* pDynamicState;
+  VkPipelineLayout layout;
+  VkRenderPass renderPass;
+  uint32_t subpass;
+  VkPipeline basePipelineHandle;
+  int32_t basePipelineIndex;
+} VkGraphicsPipelineCreateInfo;
+
+typedef struct VkPushConstantRange { VkShaderStageFlags stageFlags; uint32_t offset; uint32_t size; } VkPushConstantRange;
+
+typedef struct VkPipelineLayoutCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkPipelineLayoutCreateFlags flags;
+  uint32_t setLayoutCount;
+  const VkDescriptorSetLayout* pSetLayouts;
+  uint32_t pushConstantRangeCount;
+  const VkPushConstantRange* pPushConstantRanges;
+} VkPipelineLayoutCreateInfo;
+
+typedef struct VkAttachmentDescription {
+  VkAttachmentDescriptionFlags flags;
+  VkFormat format;
+  VkSampleCountFlags samples;
+  VkAttachmentLoadOp loadOp;
+  VkAttachmentStoreOp storeOp;
+  VkAttachmentLoadOp stencilLoadOp;
+  VkAttachmentStoreOp stencilStoreOp;
+  VkImageLayout initialLayout;
+  VkImageLayout finalLayout;
+} VkAttachmentDescription;
+
+typedef struct VkAttachmentReference { uint32_t attachment; VkImageLayout layout; } VkAttachmentReference;
+
+typedef struct VkSubpassDescription {
+  VkSubpassDescriptionFlags flags;
+  VkPipelineBindPoint pipelineBindPoint;
+  uint32_t inputAttachmentCount;
+  const VkAttachmentReference* pInputAttachments;
+  uint32_t colorAttachmentCount;
+  const VkAttachmentReference* pColorAttachments;
+  const VkAttachmentReference* pResolveAttachments;
+  const VkAttachmentReference* pDepthStencilAttachment;
+  uint32_t preserveAttachmentCount;
+  const uint32_t* pPreserveAttachments;
+} VkSubpassDescription;
+
+typedef struct VkSubpassDependency {
+  uint32_t srcSubpass;
+  uint32_t dstSubpass;
+  VkPipelineStageFlags srcStageMask;
+  VkPipelineStageFlags dstStageMask;
+  VkAccessFlags srcAccessMask;
+  VkAccessFlags dstAccessMask;
+  VkDependencyFlags dependencyFlags;
+} VkSubpassDependency;
+
+typedef struct VkRenderPassCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkRenderPassCreateFlags flags;
+  uint32_t attachmentCount;
+  const VkAttachmentDescription* pAttachments;
+  uint32_t subpassCount;
+  const VkSubpassDescription* pSubpasses;
+  uint32_t dependencyCount;
+  const VkSubpassDependency* pDependencies;
+} VkRenderPassCreateInfo;
+
+typedef struct VkFramebufferCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkFramebufferCreateFlags flags;
+  VkRenderPass renderPass;
+  uint32_t attachmentCount;
+  const VkImageView* pAttachments;
+  uint32_t width;
+  uint32_t height;
+  uint32_t layers;
+} VkFramebufferCreateInfo;
+
+typedef struct VkCommandPoolCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkCommandPoolCreateFlags flags;
+  uint32_t queueFamilyIndex;
+} VkCommandPoolCreateInfo;
+
+typedef struct VkCommandBufferAllocateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkCommandPool commandPool;
+  VkCommandBufferLevel level;
+  uint32_t commandBufferCount;
+} VkCommandBufferAllocateInfo;
+
+typedef struct VkCommandBufferInheritanceInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkRenderPass renderPass;
+  uint32_t subpass;
+  VkFramebuffer framebuffer;
+  VkBool32 occlusionQueryEnable;
+  VkQueryControlFlags queryFlags;
+  VkQueryPipelineStatisticFlags pipelineStatistics;
+} VkCommandBufferInheritanceInfo;
+
+typedef struct VkCommandBufferBeginInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkCommandBufferUsageFlags flags;
+  const VkCommandBufferInheritanceInfo* pInheritanceInfo;
+} VkCommandBufferBeginInfo;
+
+typedef union VkClearColorValue { float float32[4]; int32_t int32[4]; uint32_t uint32[4]; } VkClearColorValue;
+typedef struct VkClearDepthStencilValue { float depth; uint32_t stencil; } VkClearDepthStencilValue;
+typedef union VkClearValue { VkClearColorValue color; VkClearDepthStencilValue depthStencil; } VkClearValue;
+
+typedef struct VkRenderPassBeginInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkRenderPass renderPass;
+  VkFramebuffer framebuffer;
+  VkRect2D renderArea;
+  uint32_t clearValueCount;
+  const VkClearValue* pClearValues;
+} VkRenderPassBeginInfo;
+
+typedef struct VkBufferCopy { VkDeviceSize srcOffset; VkDeviceSize dstOffset; VkDeviceSize size; } VkBufferCopy;
+typedef struct VkBufferImageCopy {
+  VkDeviceSize bufferOffset;
+  uint32_t bufferRowLength;
+  uint32_t bufferImageHeight;
+  VkImageSubresourceLayers imageSubresource;
+  VkOffset3D imageOffset;
+  VkExtent3D imageExtent;
+} VkBufferImageCopy;
+
+typedef struct VkMemoryBarrier { VkStructureType sType; const void* pNext; VkAccessFlags srcAccessMask; VkAccessFlags dstAccessMask; } VkMemoryBarrier;
+typedef struct VkBufferMemoryBarrier {
+  VkStructureType sType;
+  const void* pNext;
+  VkAccessFlags srcAccessMask;
+  VkAccessFlags dstAccessMask;
+  uint32_t srcQueueFamilyIndex;
+  uint32_t dstQueueFamilyIndex;
+  VkBuffer buffer;
+  VkDeviceSize offset;
+  VkDeviceSize size;
+} VkBufferMemoryBarrier;
+typedef struct VkImageMemoryBarrier {
+  VkStructureType sType;
+  const void* pNext;
+  VkAccessFlags srcAccessMask;
+  VkAccessFlags dstAccessMask;
+  VkImageLayout oldLayout;
+  VkImageLayout newLayout;
+  uint32_t srcQueueFamilyIndex;
+  uint32_t dstQueueFamilyIndex;
+  VkImage image;
+  VkImageSubresourceRange subresourceRange;
+} VkImageMemoryBarrier;
+
+typedef struct VkBindBufferMemoryInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkBuffer buffer;
+  VkDeviceMemory memory;
+  VkDeviceSize memoryOffset;
+} VkBindBufferMemoryInfo;
+typedef struct VkBindImageMemoryInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkImage image;
+  VkDeviceMemory memory;
+  VkDeviceSize memoryOffset;
+} VkBindImageMemoryInfo;
+
+/* loader entry point type */
+typedef PFN_vkVoidFunction(VKAPI_PTR* PFN_vkGetInstanceProcAddr)(VkInstance instance, const char* pName);
+typedef PFN_vkVoidFunction(VKAPI_PTR* PFN_vkGetDeviceProcAddr)(VkDevice device, const char* pName);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KZ_VK_ABI_H */

@@ -1,0 +1,1065 @@
+/*
+ * kz_cmd.cpp - command pools and buffers, recording, lowering, submission and fences.
+ *
+ * The reference declares these entry points and implements none of them
+ * (vulkan-driver/src/api_impl.rs:4436-4970 vkCmd*, :3414 vkQueueSubmit, :3653-3700 fences;
+ * CommandBuffer/Fence are empty structs, handle.rs:315,327).
+ *
+ * Recording resolves all state at the vkCmdDraw* call (device addresses, viewport transform, pixel
+ * rectangle, push-constant snapshot).  vkEndCommandBuffer lowers the recording into device tables
+ * (kz_raster_abi.h: KzDraw / KzPipe / KzChunk / KzSegment), links the pipeline set's shaders into the
+ * pipeline kernels, sizes the scratch (triangle records, tile bins) and, for the persistent and batched
+ * modes, captures the launch sequence as a CUDA graph.  vkQueueSubmit replays that graph on the queue's
+ * stream, bracketed by the host<->device copies that keep HOST_COHERENT memory coherent.
+ */
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <thread>
+
+#include "kazan_driver.h"
+#include "kz_icd.h"
+
+namespace kz {
+
+template <class T>
+static T* H(const void* h) {
+  return reinterpret_cast<T*>(const_cast<void*>(h));
+}
+
+static uint8_t unorm8(float v) {
+  float c = std::fmin(std::fmax(v, 0.0f), 1.0f);
+  return (uint8_t)(int)std::rint(c * 255.0f);
+}
+
+static uint32_t pack_color(VkFormat f, const float* c) {
+  uint8_t r = unorm8(c[0]), g = unorm8(c[1]), b = unorm8(c[2]), a = unorm8(c[3]);
+  if (f == VK_FORMAT_B8G8R8A8_UNORM) return (uint32_t)b | ((uint32_t)g << 8) | ((uint32_t)r << 16) | ((uint32_t)a << 24);
+  return (uint32_t)r | ((uint32_t)g << 8) | ((uint32_t)b << 16) | ((uint32_t)a << 24);
+}
+
+static uint32_t float_bits(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return u;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* recording                                                                                        */
+
+static void draw_rect(const Framebuffer* fb, const int32_t area[4], const VkRect2D& sc, const VkViewport& vp,
+                      int32_t out[4]) {
+  /* framebuffer & render area & scissor & viewport; pixel x is inside the viewport iff x + 0.5 lies in
+   * [x, x + width) (the oracle's kzo_draw_rect uses the same formula) */
+  int32_t x0 = 0, y0 = 0, x1 = (int32_t)fb->width, y1 = (int32_t)fb->height;
+  x0 = std::max(x0, area[0]);
+  y0 = std::max(y0, area[1]);
+  x1 = std::min(x1, area[2]);
+  y1 = std::min(y1, area[3]);
+  x0 = std::max(x0, sc.offset.x);
+  y0 = std::max(y0, sc.offset.y);
+  x1 = std::min(x1, sc.offset.x + (int32_t)sc.extent.width);
+  y1 = std::min(y1, sc.offset.y + (int32_t)sc.extent.height);
+  float ylo = vp.height >= 0.0f ? vp.y : vp.y + vp.height, yhi = vp.height >= 0.0f ? vp.y + vp.height : vp.y;
+  int32_t px0 = (int32_t)std::ceil(vp.x - 0.5f), px1 = (int32_t)std::ceil(vp.x + vp.width - 0.5f);
+  int32_t py0 = (int32_t)std::ceil(ylo - 0.5f), py1 = (int32_t)std::ceil(yhi - 0.5f);
+  out[0] = std::max(x0, px0);
+  out[1] = std::max(y0, py0);
+  out[2] = std::min(x1, px1);
+  out[3] = std::min(y1, py1);
+}
+
+static void record_draw(CommandBuffer* cb, uint32_t tri_count, uint32_t instances, uint32_t first_instance, bool indexed,
+                        uint32_t first_index, int32_t vertex_offset) {
+  if (cb->cur_pass < 0 || !cb->pipe) {
+    log_error("draw outside a render pass or without a bound pipeline");
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
+  Pipeline* p = cb->pipe;
+  if (p->rasterizer_discard || tri_count == 0 || instances == 0) return;
+  PassRec& pass = cb->passes[(size_t)cb->cur_pass];
+  DrawRec dr;
+  std::memset(&dr.d, 0, sizeof dr.d);
+  dr.pipe = p;
+  KzDraw& d = dr.d;
+  int nreads = 0;
+  for (int b = 0; b < KZ_MAX_BINDINGS; b++) {
+    if (cb->vb[b]) {
+      d.vb[b] = (uint64_t)(uintptr_t)(cb->vb[b]->ptr() + cb->vb_off[b]);
+      dr.reads[nreads++] = cb->vb[b]->mem;
+    }
+  }
+  if (indexed) {
+    if (!cb->ib) {
+      log_error("vkCmdDrawIndexed without an index buffer");
+      cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+      return;
+    }
+    uint32_t isz = cb->ib_type == VK_INDEX_TYPE_UINT16 ? 2 : 4;
+    d.ib = (uint64_t)(uintptr_t)(cb->ib->ptr() + cb->ib_off + (VkDeviceSize)first_index * isz);
+    d.indexed = isz == 4 ? 1 : 2;
+    dr.reads[nreads++] = cb->ib->mem;
+  }
+  d.vertex_offset = vertex_offset;
+  d.first_instance = first_instance;
+  d.instance_count = instances;
+  d.tri_count = tri_count;
+  VkViewport vp = p->dyn_viewport ? cb->viewport : p->viewport;
+  VkRect2D sc = p->dyn_scissor ? cb->scissor : p->scissor;
+  d.hx = 0.5f * vp.width;
+  d.ox = vp.x + d.hx;
+  d.hy = 0.5f * vp.height;
+  d.oy = vp.y + d.hy;
+  d.pz = vp.maxDepth - vp.minDepth;
+  d.oz = vp.minDepth;
+  d.zmin = std::fmin(vp.minDepth, vp.maxDepth);
+  d.zmax = std::fmax(vp.minDepth, vp.maxDepth);
+  draw_rect(pass.fb, pass.area, sc, vp, d.rect);
+  std::memcpy(dr.push, cb->push, KZ_PUSH_BYTES);
+  dr.triangles = (uint64_t)tri_count * instances;
+  if (p->dyn_blend && cb->have_blend_const) {
+    /* dynamic blend constants become part of the per-draw pipeline copy at lowering */
+  }
+  pass.draws.push_back(dr);
+}
+
+}  // namespace kz
+
+using namespace kz;
+
+extern "C" {
+
+VkResult VKAPI_CALL kzCreateCommandPool(VkDevice device, const VkCommandPoolCreateInfo* ci, const VkAllocationCallbacks*,
+                                        VkCommandPool* out) {
+  /* api_impl.rs:4436 vkCreateCommandPool */
+  if (!ci || ci->queueFamilyIndex != 0) return VK_ERROR_INITIALIZATION_FAILED;
+  CommandPool* pool = new CommandPool();
+  pool->dev = H<Device>(device);
+  *out = reinterpret_cast<VkCommandPool>(pool);
+  return VK_SUCCESS;
+}
+
+static void destroy_cb(CommandBuffer* cb) {
+  if (cb->low) {
+    cudaStreamSynchronize(cb->dev->queue.stream);
+    free_lowered(cb->low.get());
+  }
+  delete cb;
+}
+
+void VKAPI_CALL kzDestroyCommandPool(VkDevice, VkCommandPool pool_h, const VkAllocationCallbacks*) {
+  CommandPool* pool = H<CommandPool>(pool_h);
+  if (!pool) return;
+  for (CommandBuffer* cb : pool->buffers) destroy_cb(cb);
+  delete pool;
+}
+
+static void reset_cb(CommandBuffer* cb) {
+  if (cb->low) {
+    cudaStreamSynchronize(cb->dev->queue.stream);
+    free_lowered(cb->low.get());
+    cb->low.reset();
+  }
+  cb->recording = false;
+  cb->pipe = nullptr;
+  cb->have_viewport = cb->have_scissor = cb->have_blend_const = false;
+  std::memset(cb->vb, 0, sizeof cb->vb);
+  std::memset(cb->vb_off, 0, sizeof cb->vb_off);
+  cb->ib = nullptr;
+  cb->ib_off = 0;
+  std::memset(cb->push, 0, sizeof cb->push);
+  cb->cur_pass = -1;
+  cb->passes.clear();
+  cb->ops.clear();
+  cb->record_error = VK_SUCCESS;
+}
+
+VkResult VKAPI_CALL kzResetCommandPool(VkDevice, VkCommandPool pool_h, VkCommandPoolResetFlags) {
+  CommandPool* pool = H<CommandPool>(pool_h);
+  for (CommandBuffer* cb : pool->buffers) reset_cb(cb);
+  return VK_SUCCESS;
+}
+
+VkResult VKAPI_CALL kzAllocateCommandBuffers(VkDevice device, const VkCommandBufferAllocateInfo* ai,
+                                             VkCommandBuffer* out) {
+  /* api_impl.rs:4464 vkAllocateCommandBuffers (secondary command buffers are not supported) */
+  if (!ai || ai->level != VK_COMMAND_BUFFER_LEVEL_PRIMARY) return VK_ERROR_FEATURE_NOT_PRESENT;
+  CommandPool* pool = H<CommandPool>(ai->commandPool);
+  for (uint32_t i = 0; i < ai->commandBufferCount; i++) {
+    CommandBuffer* cb = new CommandBuffer();
+    cb->dev = H<Device>(device);
+    cb->pool = pool;
+    pool->buffers.push_back(cb);
+    out[i] = reinterpret_cast<VkCommandBuffer>(cb);
+  }
+  return VK_SUCCESS;
+}
+
+void VKAPI_CALL kzFreeCommandBuffers(VkDevice, VkCommandPool pool_h, uint32_t n, const VkCommandBuffer* cbs) {
+  CommandPool* pool = H<CommandPool>(pool_h);
+  for (uint32_t i = 0; i < n; i++) {
+    CommandBuffer* cb = H<CommandBuffer>(cbs[i]);
+    if (!cb) continue;
+    for (size_t k = 0; k < pool->buffers.size(); k++)
+      if (pool->buffers[k] == cb) {
+        pool->buffers.erase(pool->buffers.begin() + (long)k);
+        break;
+      }
+    destroy_cb(cb);
+  }
+}
+
+VkResult VKAPI_CALL kzBeginCommandBuffer(VkCommandBuffer cbh, const VkCommandBufferBeginInfo*) {
+  /* api_impl.rs:4483 vkBeginCommandBuffer (implicit reset) */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  reset_cb(cb);
+  cb->recording = true;
+  return VK_SUCCESS;
+}
+
+VkResult VKAPI_CALL kzEndCommandBuffer(VkCommandBuffer cbh) {
+  /* api_impl.rs:4491 vkEndCommandBuffer: lower and capture */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  if (!cb->recording) return VK_ERROR_INITIALIZATION_FAILED;
+  cb->recording = false;
+  if (cb->record_error != VK_SUCCESS) return cb->record_error;
+  return lower_command_buffer(cb);
+}
+
+VkResult VKAPI_CALL kzResetCommandBuffer(VkCommandBuffer cbh, VkCommandBufferResetFlags) {
+  reset_cb(H<CommandBuffer>(cbh));
+  return VK_SUCCESS;
+}
+
+void VKAPI_CALL kzCmdBindPipeline(VkCommandBuffer cbh, VkPipelineBindPoint bp, VkPipeline p) {
+  /* api_impl.rs:4506 */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  if (bp != VK_PIPELINE_BIND_POINT_GRAPHICS) {
+    cb->record_error = VK_ERROR_FEATURE_NOT_PRESENT;
+    return;
+  }
+  cb->pipe = H<Pipeline>(p);
+}
+
+void VKAPI_CALL kzCmdSetViewport(VkCommandBuffer cbh, uint32_t first, uint32_t n, const VkViewport* vps) {
+  /* api_impl.rs:4515 */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  if (first == 0 && n >= 1) {
+    cb->viewport = vps[0];
+    cb->have_viewport = true;
+  }
+}
+
+void VKAPI_CALL kzCmdSetScissor(VkCommandBuffer cbh, uint32_t first, uint32_t n, const VkRect2D* sc) {
+  /* api_impl.rs:4525 */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  if (first == 0 && n >= 1) {
+    cb->scissor = sc[0];
+    cb->have_scissor = true;
+  }
+}
+
+void VKAPI_CALL kzCmdSetBlendConstants(VkCommandBuffer cbh, const float c[4]) {
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  std::memcpy(cb->blend_const, c, sizeof cb->blend_const);
+  cb->have_blend_const = true;
+}
+
+void VKAPI_CALL kzCmdBindVertexBuffers(VkCommandBuffer cbh, uint32_t first, uint32_t n, const VkBuffer* bufs,
+                                       const VkDeviceSize* offs) {
+  /* api_impl.rs:4621 */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  for (uint32_t i = 0; i < n && first + i < KZ_MAX_BINDINGS; i++) {
+    cb->vb[first + i] = H<Buffer>(bufs[i]);
+    cb->vb_off[first + i] = offs[i];
+  }
+}
+
+void VKAPI_CALL kzCmdBindIndexBuffer(VkCommandBuffer cbh, VkBuffer buf, VkDeviceSize off, VkIndexType type) {
+  /* api_impl.rs:4611 */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  cb->ib = H<Buffer>(buf);
+  cb->ib_off = off;
+  cb->ib_type = type;
+}
+
+void VKAPI_CALL kzCmdPushConstants(VkCommandBuffer cbh, VkPipelineLayout, VkShaderStageFlags, uint32_t offset,
+                                   uint32_t size, const void* data) {
+  /* api_impl.rs:4932 */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  if (offset + size > KZ_PUSH_BYTES) {
+    cb->record_error = VK_ERROR_FEATURE_NOT_PRESENT;
+    return;
+  }
+  std::memcpy(cb->push + offset, data, size);
+}
+
+void VKAPI_CALL kzCmdDraw(VkCommandBuffer cbh, uint32_t vertexCount, uint32_t instanceCount, uint32_t firstVertex,
+                          uint32_t firstInstance) {
+  /* api_impl.rs:4632 vkCmdDraw: triangle list over vertices firstVertex + k */
+  record_draw(H<CommandBuffer>(cbh), vertexCount / 3, instanceCount, firstInstance, false, 0, (int32_t)firstVertex);
+}
+
+void VKAPI_CALL kzCmdDrawIndexed(VkCommandBuffer cbh, uint32_t indexCount, uint32_t instanceCount, uint32_t firstIndex,
+                                 int32_t vertexOffset, uint32_t firstInstance) {
+  /* api_impl.rs:4643 vkCmdDrawIndexed: vertex = index[firstIndex + k] + vertexOffset */
+  record_draw(H<CommandBuffer>(cbh), indexCount / 3, instanceCount, firstInstance, true, firstIndex, vertexOffset);
+}
+
+void VKAPI_CALL kzCmdBeginRenderPass(VkCommandBuffer cbh, const VkRenderPassBeginInfo* bi, VkSubpassContents) {
+  /* api_impl.rs:4944 */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  PassRec pr;
+  pr.fb = H<Framebuffer>(bi->framebuffer);
+  pr.rp = H<RenderPass>(bi->renderPass);
+  pr.area[0] = bi->renderArea.offset.x;
+  pr.area[1] = bi->renderArea.offset.y;
+  pr.area[2] = bi->renderArea.offset.x + (int32_t)bi->renderArea.extent.width;
+  pr.area[3] = bi->renderArea.offset.y + (int32_t)bi->renderArea.extent.height;
+  if (pr.rp->color_att >= 0 && (uint32_t)pr.rp->color_att < bi->clearValueCount)
+    pr.clear_color = bi->pClearValues[pr.rp->color_att];
+  if (pr.rp->depth_att >= 0 && (uint32_t)pr.rp->depth_att < bi->clearValueCount)
+    pr.clear_depth = bi->pClearValues[pr.rp->depth_att];
+  cb->passes.push_back(pr);
+  cb->cur_pass = (int)cb->passes.size() - 1;
+  RecOp op;
+  op.kind = OpKind::Pass;
+  op.pass = cb->passes.size() - 1;
+  cb->ops.push_back(op);
+}
+
+void VKAPI_CALL kzCmdEndRenderPass(VkCommandBuffer cbh) {
+  /* api_impl.rs:4961 */
+  H<CommandBuffer>(cbh)->cur_pass = -1;
+}
+
+static void clear_image(CommandBuffer* cb, Image* img, uint32_t value) {
+  RecOp op;
+  op.kind = OpKind::Clear;
+  op.base = img->ptr();
+  op.pitch = img->pitch;
+  op.rect[0] = 0;
+  op.rect[1] = 0;
+  op.rect[2] = (int32_t)img->width;
+  op.rect[3] = (int32_t)img->height;
+  op.value = value;
+  op.wmem = img->mem;
+  cb->ops.push_back(op);
+}
+
+void VKAPI_CALL kzCmdClearColorImage(VkCommandBuffer cbh, VkImage image, VkImageLayout, const VkClearColorValue* c,
+                                     uint32_t, const VkImageSubresourceRange*) {
+  /* api_impl.rs:4780 vkCmdClearColorImage: the clear colour converted to the image format (UNORM8, round
+   * to nearest even) fills the single mip level / layer */
+  Image* img = H<Image>(image);
+  clear_image(H<CommandBuffer>(cbh), img, pack_color(img->format, c->float32));
+}
+
+void VKAPI_CALL kzCmdClearDepthStencilImage(VkCommandBuffer cbh, VkImage image, VkImageLayout,
+                                            const VkClearDepthStencilValue* v, uint32_t,
+                                            const VkImageSubresourceRange*) {
+  /* api_impl.rs:4792 */
+  clear_image(H<CommandBuffer>(cbh), H<Image>(image), float_bits(v->depth));
+}
+
+void VKAPI_CALL kzCmdPipelineBarrier(VkCommandBuffer, VkPipelineStageFlags, VkPipelineStageFlags, VkDependencyFlags,
+                                     uint32_t, const VkMemoryBarrier*, uint32_t, const VkBufferMemoryBarrier*,
+                                     uint32_t, const VkImageMemoryBarrier*) {
+  /* api_impl.rs:4863: every command executes in order on one stream, so barriers order nothing new */
+}
+
+void VKAPI_CALL kzCmdCopyBuffer(VkCommandBuffer cbh, VkBuffer src, VkBuffer dst, uint32_t n, const VkBufferCopy* r) {
+  /* api_impl.rs:4696 */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  Buffer* s = H<Buffer>(src);
+  Buffer* d = H<Buffer>(dst);
+  for (uint32_t i = 0; i < n; i++) {
+    RecOp op;
+    op.kind = OpKind::Copy;
+    op.src = s->ptr() + r[i].srcOffset;
+    op.dst = d->ptr() + r[i].dstOffset;
+    op.bytes = (size_t)r[i].size;
+    op.rmem = s->mem;
+    op.wmem = d->mem;
+    cb->ops.push_back(op);
+  }
+}
+
+static void image_buffer_copy(CommandBuffer* cb, Image* img, Buffer* buf, const VkBufferImageCopy& r, bool to_buffer) {
+  RecOp op;
+  op.kind = OpKind::Copy2D;
+  uint32_t row_len = r.bufferRowLength ? r.bufferRowLength : r.imageExtent.width;
+  size_t bpitch = (size_t)row_len * img->bpp;
+  char* ip = img->ptr() + (size_t)r.imageOffset.y * img->pitch + (size_t)r.imageOffset.x * img->bpp;
+  char* bp = buf->ptr() + r.bufferOffset;
+  op.width_bytes = (size_t)r.imageExtent.width * img->bpp;
+  op.rows = r.imageExtent.height;
+  if (to_buffer) {
+    op.dst = bp;
+    op.dpitch = bpitch;
+    op.src = ip;
+    op.spitch = img->pitch;
+    op.rmem = img->mem;
+    op.wmem = buf->mem;
+  } else {
+    op.dst = ip;
+    op.dpitch = img->pitch;
+    op.src = bp;
+    op.spitch = bpitch;
+    op.rmem = buf->mem;
+    op.wmem = img->mem;
+  }
+  cb->ops.push_back(op);
+}
+
+void VKAPI_CALL kzCmdCopyImageToBuffer(VkCommandBuffer cbh, VkImage image, VkImageLayout, VkBuffer buffer, uint32_t n,
+                                       const VkBufferImageCopy* r) {
+  /* api_impl.rs:4746 */
+  for (uint32_t i = 0; i < n; i++) image_buffer_copy(H<CommandBuffer>(cbh), H<Image>(image), H<Buffer>(buffer), r[i], true);
+}
+
+void VKAPI_CALL kzCmdCopyBufferToImage(VkCommandBuffer cbh, VkBuffer buffer, VkImage image, VkImageLayout, uint32_t n,
+                                       const VkBufferImageCopy* r) {
+  for (uint32_t i = 0; i < n; i++) image_buffer_copy(H<CommandBuffer>(cbh), H<Image>(image), H<Buffer>(buffer), r[i], false);
+}
+
+void VKAPI_CALL kzCmdFillBuffer(VkCommandBuffer cbh, VkBuffer buffer, VkDeviceSize off, VkDeviceSize size,
+                                uint32_t data) {
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  Buffer* b = H<Buffer>(buffer);
+  if (size == VK_WHOLE_SIZE) size = (b->size - off) & ~(VkDeviceSize)3;
+  RecOp op;
+  op.kind = OpKind::Fill;
+  op.base = b->ptr() + off;
+  op.pitch = (uint32_t)size;
+  op.rect[0] = 0;
+  op.rect[1] = 0;
+  op.rect[2] = (int32_t)(size / 4);
+  op.rect[3] = 1;
+  op.value = data;
+  op.wmem = b->mem;
+  cb->ops.push_back(op);
+}
+
+}  // extern "C"
+
+namespace kz {
+
+/* ------------------------------------------------------------------------------------------------ */
+/* lowering                                                                                         */
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+void free_lowered(Lowered* low) {
+  if (!low) return;
+  if (low->exec) cudaGraphExecDestroy(low->exec);
+  if (low->graph) cudaGraphDestroy(low->graph);
+  if (low->ev_begin) cudaEventDestroy(low->ev_begin);
+  if (low->ev_end) cudaEventDestroy(low->ev_end);
+  device_free(low->d_tables);
+  device_free(low->d_records);
+  device_free(low->d_bins);
+  device_free(low->d_tiles);
+  if (low->h_status) cudaFreeHost(low->h_status);
+  low->exec = nullptr;
+  low->graph = nullptr;
+  low->d_tables = low->d_records = low->d_bins = nullptr;
+  low->d_tiles = nullptr;
+  low->h_status = nullptr;
+}
+
+static void add_unique(std::vector<DeviceMemory*>& v, DeviceMemory* m) {
+  if (!m) return;
+  for (DeviceMemory* x : v)
+    if (x == m) return;
+  v.push_back(m);
+}
+
+static uint32_t color_format(VkFormat f) {
+  if (f == VK_FORMAT_R8G8B8A8_UNORM) return KZ_CF_RGBA8;
+  if (f == VK_FORMAT_B8G8R8A8_UNORM) return KZ_CF_BGRA8;
+  return KZ_CF_NONE;
+}
+
+/* fill the framebuffer part of a segment from a render pass instance */
+static void segment_target(const PassRec& pr, KzSegment& s, uint32_t tile, bool first, Lowered& low) {
+  const RenderPass* rp = pr.rp;
+  const Framebuffer* fb = pr.fb;
+  s.width = fb->width;
+  s.height = fb->height;
+  s.tile = tile;
+  s.tiles_x = (s.width + tile - 1) / tile;
+  s.tiles_y = (s.height + tile - 1) / tile;
+  s.area[0] = std::max(0, pr.area[0]);
+  s.area[1] = std::max(0, pr.area[1]);
+  s.area[2] = std::min((int32_t)fb->width, pr.area[2]);
+  s.area[3] = std::min((int32_t)fb->height, pr.area[3]);
+  s.color_load = s.depth_load = KZ_LOAD_LOAD;
+  s.color_store = s.depth_store = 1;
+  if (rp->color_att >= 0 && (size_t)rp->color_att < fb->views.size()) {
+    Image* img = fb->views[(size_t)rp->color_att]->image;
+    s.color = (uint64_t)(uintptr_t)img->ptr();
+    s.color_pitch = img->pitch;
+    s.color_format = color_format(img->format);
+    s.width = std::min(s.width, img->width);
+    s.height = std::min(s.height, img->height);
+    const VkAttachmentDescription& a = rp->atts[(size_t)rp->color_att];
+    if (first && a.loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR) s.color_load = KZ_LOAD_CLEAR;
+    s.clear_color = pack_color(img->format, pr.clear_color.color.float32);
+    add_unique(low.writes, img->mem);
+    if (s.color_load == KZ_LOAD_LOAD) add_unique(low.reads, img->mem);
+  }
+  if (rp->depth_att >= 0 && (size_t)rp->depth_att < fb->views.size()) {
+    Image* img = fb->views[(size_t)rp->depth_att]->image;
+    s.depth = (uint64_t)(uintptr_t)img->ptr();
+    s.depth_pitch = img->pitch;
+    s.width = std::min(s.width, img->width);
+    s.height = std::min(s.height, img->height);
+    const VkAttachmentDescription& a = rp->atts[(size_t)rp->depth_att];
+    if (first && a.loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR) s.depth_load = KZ_LOAD_CLEAR;
+    s.clear_depth = pr.clear_depth.depthStencil.depth;
+    add_unique(low.writes, img->mem);
+    if (s.depth_load == KZ_LOAD_LOAD) add_unique(low.reads, img->mem);
+  }
+  s.tiles_x = (s.width + tile - 1) / tile;
+  s.tiles_y = (s.height + tile - 1) / tile;
+  s.area[2] = std::min((int32_t)s.width, s.area[2]);
+  s.area[3] = std::min((int32_t)s.height, s.area[3]);
+}
+
+static int raster_class(const DrawRec& d) {
+  /* draws that share a class can share one segment: visibility mode with the same key and write mask,
+   * or ordered mode */
+  if (d.pipe->vis_key >= 0) return 1 + d.pipe->vis_key + 16 * (int)d.pipe->pipe.write_mask;
+  return 0;
+}
+
+static VkResult size_scratch(Device* dev, Lowered& low, uint32_t rec_cap, uint32_t pair_cap) {
+  cudaSetDevice(dev->pd->cuda_device);
+  device_free(low.d_records);
+  device_free(low.d_bins);
+  low.d_records = low.d_bins = nullptr;
+  void* p = nullptr;
+  VkResult r = device_alloc((size_t)rec_cap * sizeof(KzTriRecord), &p);
+  if (r != VK_SUCCESS) return r;
+  low.d_records = static_cast<char*>(p);
+  r = device_alloc((size_t)pair_cap * 4, &p);
+  if (r != VK_SUCCESS) return r;
+  low.d_bins = static_cast<char*>(p);
+  low.rec_cap = rec_cap;
+  low.pair_cap = pair_cap;
+  for (KzSegment& s : low.segments) {
+    s.records = (uint64_t)(uintptr_t)low.d_records;
+    s.bins = (uint64_t)(uintptr_t)low.d_bins;
+    s.rec_cap = rec_cap;
+    s.pair_cap = pair_cap;
+  }
+  return VK_SUCCESS;
+}
+
+static void upload_tables(Lowered& low) {
+  size_t o_draws = 0;
+  size_t o_pipes = align_up(o_draws + low.draws.size() * sizeof(KzDraw), 256);
+  size_t o_chunks = align_up(o_pipes + low.pipes.size() * sizeof(KzPipe), 256);
+  size_t o_segs = align_up(o_chunks + low.chunks.size() * sizeof(KzChunk), 256);
+  size_t o_push = align_up(o_segs + low.segments.size() * sizeof(KzSegment), 256);
+  std::vector<char> host(low.tables_bytes, 0);
+  if (!low.draws.empty()) std::memcpy(host.data() + o_draws, low.draws.data(), low.draws.size() * sizeof(KzDraw));
+  if (!low.pipes.empty()) std::memcpy(host.data() + o_pipes, low.pipes.data(), low.pipes.size() * sizeof(KzPipe));
+  if (!low.chunks.empty()) std::memcpy(host.data() + o_chunks, low.chunks.data(), low.chunks.size() * sizeof(KzChunk));
+  if (!low.segments.empty())
+    std::memcpy(host.data() + o_segs, low.segments.data(), low.segments.size() * sizeof(KzSegment));
+  if (!low.push.empty()) std::memcpy(host.data() + o_push, low.push.data(), low.push.size());
+  cudaMemcpy(low.d_tables, host.data(), o_push + low.push.size(), cudaMemcpyHostToDevice);
+}
+
+static uint32_t grid_cap(Device* dev) { return (uint32_t)std::max(1, dev->pd->sm_count) * 8u; }
+
+/* enqueue the lowered command buffer from segment `start` on */
+static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, bool capture) {
+  Lowered& low = *cb->low;
+  Device* dev = cb->dev;
+  uint32_t launches = 0;
+  uint32_t nseg = (uint32_t)low.segments.size();
+  cudaMemsetAsync(low.d_status, 0, sizeof(KzStatus), st);
+  if (nseg > start) cudaMemsetAsync(low.d_counters + start, 0, (nseg - start) * sizeof(KzSegCounters), st);
+  if (low.max_tiles) cudaMemsetAsync(low.d_tiles, 0, (size_t)low.max_tiles * 4, st);
+  if (capture) cudaEventRecordWithFlags(low.ev_begin, st, cudaEventRecordExternal);
+  else cudaEventRecord(low.ev_begin, st);
+  KernelSet* ks = low.ks;
+  for (const Lowered::LOp& lop : low.ops) {
+    if (lop.kind == OpKind::Pass) {
+      if (lop.seg_end <= start) continue;
+      uint32_t s0 = std::max(lop.seg_begin, start);
+      if (low.mode == 0) {
+        KzFrame f = low.frame;
+        f.first_segment = s0;
+        f.num_segments = lop.seg_end;
+        void* args[] = {&f};
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)ks->persistent_blocks);
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = KZ_DYN_SMEM;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelExC(&cfg, (const void*)ks->persistent, args);
+        launches++;
+      } else {
+        for (uint32_t s = s0; s < lop.seg_end; s++) {
+          const KzSegment& seg = low.segments[s];
+          KzFrame f = low.frame;
+          void* args[] = {&f, &s};
+          cudaLaunchConfig_t cfg = {};
+          cfg.blockDim = dim3(256);
+          cfg.stream = st;
+          if (seg.num_chunks) {
+            cfg.gridDim = dim3(seg.num_chunks);
+            cudaLaunchKernelExC(&cfg, (const void*)ks->geometry, args);
+            launches++;
+          }
+          cfg.gridDim = dim3(1);
+          cudaLaunchKernelExC(&cfg, (const void*)ks->scan, args);
+          cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (seg.rec_cap + 255) / 256)));
+          cudaLaunchKernelExC(&cfg, (const void*)ks->bin, args);
+          cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, seg.tiles_x * seg.tiles_y)));
+          cfg.dynamicSmemBytes = KZ_DYN_SMEM;
+          cudaLaunchKernelExC(&cfg, (const void*)ks->raster, args);
+          launches += 3;
+        }
+      }
+    } else {
+      if (lop.seg_begin < start) continue;
+      const RecOp& op = lop.op;
+      if (op.kind == OpKind::Clear || op.kind == OpKind::Fill) {
+        uint64_t base = (uint64_t)(uintptr_t)op.base;
+        uint32_t pitch = op.pitch;
+        int32_t x0 = op.rect[0], y0 = op.rect[1], x1 = op.rect[2], y1 = op.rect[3];
+        uint32_t value = op.value;
+        void* args[] = {&base, &pitch, &x0, &y0, &x1, &y1, &value};
+        cudaLaunchConfig_t cfg = {};
+        cfg.blockDim = dim3(256);
+        long long work = (long long)(x1 - x0) * (y1 - y0) / 4 + 1;
+        cfg.gridDim = dim3((unsigned)std::min<long long>(grid_cap(dev), (work + 255) / 256));
+        cfg.stream = st;
+        cudaLaunchKernelExC(&cfg, (const void*)ks->clear, args);
+        launches++;
+      } else if (op.kind == OpKind::Copy) {
+        cudaMemcpyAsync(op.dst, op.src, op.bytes, cudaMemcpyDeviceToDevice, st);
+      } else if (op.kind == OpKind::Copy2D) {
+        cudaMemcpy2DAsync(op.dst, op.dpitch, op.src, op.spitch, op.width_bytes, op.rows, cudaMemcpyDeviceToDevice, st);
+      }
+    }
+  }
+  if (capture) cudaEventRecordWithFlags(low.ev_end, st, cudaEventRecordExternal);
+  else cudaEventRecord(low.ev_end, st);
+  cudaMemcpyAsync(low.h_status, low.d_status, sizeof(KzStatus), cudaMemcpyDeviceToHost, st);
+  return launches;
+}
+
+VkResult lower_command_buffer(CommandBuffer* cb) {
+  Device* dev = cb->dev;
+  std::lock_guard<std::recursive_mutex> lock(dev->mu);
+  cudaSetDevice(dev->pd->cuda_device);
+  cb->low.reset(new Lowered());
+  Lowered& low = *cb->low;
+  low.mode = options().mode;
+  low.tile = options().tile;
+  std::map<Pipeline*, uint32_t> pipe_index;
+  auto pipe_of = [&](Pipeline* p, const float* blend) -> uint32_t {
+    auto it = pipe_index.find(p);
+    if (it != pipe_index.end() && !(p->dyn_blend && blend)) return it->second;
+    KzPipe kp = p->pipe;
+    if (p->dyn_blend && blend) std::memcpy(kp.blend_const, blend, sizeof kp.blend_const);
+    uint32_t idx = (uint32_t)low.pipes.size();
+    low.pipes.push_back(kp);
+    low.pipe_objs.push_back(p);
+    pipe_index[p] = idx;
+    return idx;
+  };
+  for (const RecOp& op : cb->ops) {
+    Lowered::LOp lop;
+    lop.kind = op.kind;
+    lop.op = op;
+    lop.seg_begin = (uint32_t)low.segments.size();
+    if (op.kind != OpKind::Pass) {
+      add_unique(low.writes, op.wmem);
+      add_unique(low.reads, op.rmem);
+      lop.seg_end = lop.seg_begin;
+      low.ops.push_back(lop);
+      continue;
+    }
+    const PassRec& pr = cb->passes[op.pass];
+    /* split the pass into segments */
+    std::vector<std::pair<size_t, size_t>> runs; /* [begin, end) draw indices */
+    if (low.mode == 2) {
+      for (size_t i = 0; i < pr.draws.size(); i++) runs.push_back({i, i + 1});
+    } else {
+      size_t b = 0;
+      for (size_t i = 1; i <= pr.draws.size(); i++)
+        if (i == pr.draws.size() || raster_class(pr.draws[i]) != raster_class(pr.draws[b])) {
+          runs.push_back({b, i});
+          b = i;
+        }
+    }
+    bool needs_clear = false;
+    if (pr.rp->color_att >= 0 && pr.rp->atts[(size_t)pr.rp->color_att].loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR)
+      needs_clear = true;
+    if (pr.rp->depth_att >= 0 && pr.rp->atts[(size_t)pr.rp->depth_att].loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR)
+      needs_clear = true;
+    if (runs.empty() && needs_clear) runs.push_back({0, 0});
+    for (size_t r = 0; r < runs.size(); r++) {
+      KzSegment s;
+      std::memset(&s, 0, sizeof s);
+      segment_target(pr, s, low.tile, r == 0, low);
+      s.segment_index = (uint32_t)low.segments.size();
+      s.first_draw = (uint32_t)low.draws.size();
+      s.first_chunk = (uint32_t)low.chunks.size();
+      s.mode = KZ_MODE_ORDERED;
+      s.vis_key = 0;
+      uint64_t prims = 0;
+      for (size_t i = runs[r].first; i < runs[r].second; i++) {
+        const DrawRec& dr = pr.draws[i];
+        if (i == runs[r].first && dr.pipe->vis_key >= 0) {
+          s.mode = KZ_MODE_VISIBILITY;
+          s.vis_key = (uint32_t)dr.pipe->vis_key;
+        }
+        KzDraw d = dr.d;
+        d.rect[2] = std::min(d.rect[2], (int32_t)s.width);
+        d.rect[3] = std::min(d.rect[3], (int32_t)s.height);
+        d.pipe = pipe_of(dr.pipe, cb->have_blend_const ? cb->blend_const : nullptr);
+        d.prim_base = (uint32_t)prims;
+        d.push_index = (uint32_t)(low.push.size() / KZ_PUSH_BYTES);
+        low.push.insert(low.push.end(), dr.push, dr.push + KZ_PUSH_BYTES);
+        uint32_t di = (uint32_t)low.draws.size();
+        for (uint64_t c = 0; c < dr.triangles; c += KZ_CHUNK) {
+          KzChunk ch;
+          ch.draw = di;
+          ch.first = (uint32_t)c;
+          ch.count = (uint32_t)std::min<uint64_t>(KZ_CHUNK, dr.triangles - c);
+          ch.pad = 0;
+          low.chunks.push_back(ch);
+        }
+        low.draws.push_back(d);
+        for (DeviceMemory* m : dr.reads) add_unique(low.reads, m);
+        prims += dr.triangles;
+      }
+      if (prims >= 0xFFFFFFF0ull) {
+        log_error("a render pass of %llu triangles exceeds the 2^32 primitive limit", (unsigned long long)prims);
+        return VK_ERROR_OUT_OF_DEVICE_MEMORY;
+      }
+      s.num_draws = (uint32_t)(low.draws.size() - s.first_draw);
+      s.num_chunks = (uint32_t)(low.chunks.size() - s.first_chunk);
+      s.num_prims = (uint32_t)prims;
+      low.triangles += prims;
+      low.max_tiles = std::max(low.max_tiles, s.tiles_x * s.tiles_y);
+      low.segments.push_back(s);
+    }
+    lop.seg_end = (uint32_t)low.segments.size();
+    low.ops.push_back(lop);
+  }
+  /* scratch sizing: records for every triangle plus clipping headroom; bins for a few tiles per record */
+  uint64_t max_prims = 0, max_tiles = 0;
+  for (const KzSegment& s : low.segments) {
+    max_prims = std::max<uint64_t>(max_prims, s.num_prims);
+    max_tiles = std::max<uint64_t>(max_tiles, (uint64_t)s.tiles_x * s.tiles_y);
+  }
+  uint64_t rec_cap = (uint64_t)((double)max_prims * options().rec_slack) + 4096;
+  uint64_t pair_cap = rec_cap * 4 + max_tiles * 16 + (1u << 18);
+  rec_cap = std::min<uint64_t>(rec_cap, 0xFFFFFFF0ull);
+  pair_cap = std::min<uint64_t>(pair_cap, 0xFFFFFFF0ull);
+  /* device tables: draws | pipes | chunks | segments | push, then counters and status */
+  size_t o_pipes = align_up(low.draws.size() * sizeof(KzDraw), 256);
+  size_t o_chunks = align_up(o_pipes + low.pipes.size() * sizeof(KzPipe), 256);
+  size_t o_segs = align_up(o_chunks + low.chunks.size() * sizeof(KzChunk), 256);
+  size_t o_push = align_up(o_segs + low.segments.size() * sizeof(KzSegment), 256);
+  size_t o_counters = align_up(o_push + low.push.size(), 256);
+  size_t o_status = align_up(o_counters + low.segments.size() * sizeof(KzSegCounters), 256);
+  low.tables_bytes = o_status + sizeof(KzStatus);
+  void* p = nullptr;
+  VkResult r = device_alloc(low.tables_bytes, &p);
+  if (r != VK_SUCCESS) return r;
+  low.d_tables = static_cast<char*>(p);
+  low.d_counters = reinterpret_cast<KzSegCounters*>(low.d_tables + o_counters);
+  low.d_status = reinterpret_cast<KzStatus*>(low.d_tables + o_status);
+  r = device_alloc(std::max<size_t>(4, (size_t)(low.max_tiles + 1) * 3 * 4), &p);
+  if (r != VK_SUCCESS) return r;
+  low.d_tiles = static_cast<uint32_t*>(p);
+  for (size_t i = 0; i < low.segments.size(); i++) {
+    KzSegment& s = low.segments[i];
+    s.tile_count = (uint64_t)(uintptr_t)low.d_tiles;
+    s.tile_offset = (uint64_t)(uintptr_t)(low.d_tiles + low.max_tiles);
+    s.tile_cursor = (uint64_t)(uintptr_t)(low.d_tiles + 2 * (size_t)low.max_tiles + 1);
+    s.counters = (uint64_t)(uintptr_t)(low.d_counters + i);
+  }
+  r = size_scratch(dev, low, (uint32_t)rec_cap, (uint32_t)pair_cap);
+  if (r != VK_SUCCESS) return r;
+  low.frame.draws = (uint64_t)(uintptr_t)low.d_tables;
+  low.frame.pipes = (uint64_t)(uintptr_t)(low.d_tables + o_pipes);
+  low.frame.chunks = (uint64_t)(uintptr_t)(low.d_tables + o_chunks);
+  low.frame.segments = (uint64_t)(uintptr_t)(low.d_tables + o_segs);
+  low.frame.push = (uint64_t)(uintptr_t)(low.d_tables + o_push);
+  low.frame.status = (uint64_t)(uintptr_t)low.d_status;
+  low.frame.num_segments = (uint32_t)low.segments.size();
+  low.frame.first_segment = 0;
+  upload_tables(low);
+  if (cudaMallocHost((void**)&low.h_status, sizeof(KzStatus)) != cudaSuccess) return VK_ERROR_OUT_OF_HOST_MEMORY;
+  std::memset(low.h_status, 0, sizeof(KzStatus));
+  cudaEventCreate(&low.ev_begin);
+  cudaEventCreate(&low.ev_end);
+  std::string err;
+  low.ks = kernel_set_for(dev, low.pipe_objs, err);
+  if (!low.ks) {
+    log_error("pipeline link failed: %s", err.c_str());
+    return VK_ERROR_INITIALIZATION_FAILED;
+  }
+  if (low.mode != 2) {
+    cudaStream_t cs = dev->capture_stream;
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      log_error("stream capture failed to start: %s", cudaGetErrorString(cudaGetLastError()));
+      return VK_ERROR_INITIALIZATION_FAILED;
+    }
+    launch_ops(cb, cs, 0, true);
+    cudaError_t e = cudaStreamEndCapture(cs, &low.graph);
+    if (e != cudaSuccess || cudaGraphInstantiate(&low.exec, low.graph, 0) != cudaSuccess) {
+      log_error("graph capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : cudaGetLastError()));
+      return VK_ERROR_INITIALIZATION_FAILED;
+    }
+  }
+  if (options().trace)
+    log_error("lowered: %zu draws, %zu segments, %llu triangles, mode %d, tile %u, records %u, pairs %u",
+              low.draws.size(), low.segments.size(), (unsigned long long)low.triangles, low.mode, low.tile,
+              low.rec_cap, low.pair_cap);
+  return VK_SUCCESS;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* submission and completion                                                                        */
+
+static cudaEvent_t pool_event(Device* dev) {
+  if (!dev->event_pool.empty()) {
+    cudaEvent_t e = dev->event_pool.back();
+    dev->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  return e;
+}
+
+static void enqueue(CommandBuffer* cb, cudaStream_t st) {
+  Lowered& low = *cb->low;
+  for (DeviceMemory* m : low.reads)
+    if (m->host && m->mapped) cudaMemcpyAsync(m->dptr, m->host, (size_t)m->size, cudaMemcpyHostToDevice, st);
+  if (low.exec) cudaGraphLaunch(low.exec, st);
+  else launch_ops(cb, st, 0, false);
+  for (DeviceMemory* m : low.writes) {
+    if (m->host && m->mapped) cudaMemcpyAsync(m->host, m->dptr, (size_t)m->size, cudaMemcpyDeviceToHost, st);
+    else m->device_newer = true;
+  }
+}
+
+/* grow the scratch after an overflow and run the command buffer again from the failing segment;
+ * called only when nothing was enqueued after it */
+static bool replay(CommandBuffer* cb, Queue* q) {
+  Lowered& low = *cb->low;
+  for (int attempt = 0; attempt < 4; attempt++) {
+    KzStatus st = *low.h_status;
+    if (!(st.flags & (KZ_STATUS_RECORD_OVERFLOW | KZ_STATUS_PAIR_OVERFLOW))) return !(st.flags & ~0u);
+    uint64_t rec = std::max<uint64_t>(low.rec_cap, (uint64_t)((double)st.need_records * 1.25) + 4096);
+    uint64_t pair = std::max<uint64_t>(low.pair_cap, (uint64_t)((double)st.need_pairs * 1.25) + 65536);
+    if (options().trace) log_error("scratch overflow in segment %u: growing to %llu records, %llu pairs",
+                                   st.failed_segment, (unsigned long long)rec, (unsigned long long)pair);
+    if (rec > 0xFFFFFFF0ull || pair > 0xFFFFFFF0ull) return false;
+    if (size_scratch(cb->dev, low, (uint32_t)rec, (uint32_t)pair) != VK_SUCCESS) return false;
+    upload_tables(low);
+    launch_ops(cb, q->stream, st.failed_segment, false);
+    for (DeviceMemory* m : low.writes)
+      if (m->host && m->mapped) cudaMemcpyAsync(m->host, m->dptr, (size_t)m->size, cudaMemcpyDeviceToHost, q->stream);
+    cudaStreamSynchronize(q->stream);
+  }
+  return false;
+}
+
+static void complete(Queue* q, Submission& s) {
+  Device* dev = q->dev;
+  VkResult err = VK_SUCCESS;
+  if (s.cb && s.cb->low) {
+    CommandBuffer* cb = s.cb;
+    Lowered& low = *cb->low;
+    KzStatus st = *low.h_status;
+    if (st.flags & (KZ_STATUS_RECORD_OVERFLOW | KZ_STATUS_PAIR_OVERFLOW)) {
+      bool last = &s == &q->inflight.back();
+      if (!last || !replay(cb, q)) {
+        log_error("triangle-record or tile-bin capacity exceeded and the submission could not be replayed");
+        err = VK_ERROR_DEVICE_LOST;
+      }
+      st = *low.h_status;
+    }
+    if (st.flags & KZ_STATUS_BARRIER_TIMEOUT) {
+      log_error("persistent kernel barrier timed out");
+      err = VK_ERROR_DEVICE_LOST;
+    }
+    if (st.flags & KZ_STATUS_BIN_TOO_LARGE) {
+      log_error("a tile's bin exceeds the ordered-mode sort capacity; use a smaller tile");
+      err = VK_ERROR_DEVICE_LOST;
+    }
+    cb->last_status = st;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, low.ev_begin, low.ev_end) == cudaSuccess) cb->last_ms = ms;
+    else cudaGetLastError();
+  }
+  if (err != VK_SUCCESS) q->lost = err;
+  if (s.fence) {
+    s.fence->signaled = true;
+    s.fence->pending = false;
+    s.fence->error = err;
+  }
+  dev->event_pool.push_back(s.done);
+}
+
+static void process_completions(Queue* q, bool block_all) {
+  while (!q->inflight.empty()) {
+    Submission& s = q->inflight.front();
+    cudaError_t e = block_all ? cudaEventSynchronize(s.done) : cudaEventQuery(s.done);
+    if (e == cudaErrorNotReady) return;
+    if (e != cudaSuccess) {
+      log_error("device error: %s", cudaGetErrorString(e));
+      q->lost = VK_ERROR_DEVICE_LOST;
+    }
+    complete(q, s);
+    q->inflight.erase(q->inflight.begin());
+  }
+}
+
+VkResult queue_submit(Queue* q, uint32_t count, const VkSubmitInfo* submits, Fence* fence) {
+  Device* dev = q->dev;
+  std::lock_guard<std::recursive_mutex> lock(dev->mu);
+  cudaSetDevice(dev->pd->cuda_device);
+  if (q->lost != VK_SUCCESS) return q->lost;
+  process_completions(q, false);
+  for (uint32_t i = 0; i < count; i++)
+    for (uint32_t k = 0; k < submits[i].commandBufferCount; k++) {
+      CommandBuffer* cb = H<CommandBuffer>(submits[i].pCommandBuffers[k]);
+      if (!cb->low) return VK_ERROR_INITIALIZATION_FAILED;
+    }
+  for (uint32_t i = 0; i < count; i++)
+    for (uint32_t k = 0; k < submits[i].commandBufferCount; k++) {
+      CommandBuffer* cb = H<CommandBuffer>(submits[i].pCommandBuffers[k]);
+      enqueue(cb, q->stream);
+      Submission s;
+      s.cb = cb;
+      s.done = pool_event(dev);
+      cudaEventRecord(s.done, q->stream);
+      q->inflight.push_back(s);
+    }
+  if (fence) {
+    if (q->inflight.empty()) {
+      Submission s;
+      s.done = pool_event(dev);
+      cudaEventRecord(s.done, q->stream);
+      q->inflight.push_back(s);
+    }
+    cudaEventRecord(fence->ev, q->stream);
+    fence->pending = true;
+    fence->signaled = false;
+    fence->error = VK_SUCCESS;
+    q->inflight.back().fence = fence;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    log_error("submission failed: %s", cudaGetErrorString(e));
+    return VK_ERROR_DEVICE_LOST;
+  }
+  return VK_SUCCESS;
+}
+
+VkResult queue_wait_idle(Queue* q) {
+  Device* dev = q->dev;
+  std::lock_guard<std::recursive_mutex> lock(dev->mu);
+  cudaSetDevice(dev->pd->cuda_device);
+  process_completions(q, true);
+  cudaStreamSynchronize(q->stream);
+  return q->lost;
+}
+
+VkResult fence_status(Device* dev, Fence* f) {
+  std::lock_guard<std::recursive_mutex> lock(dev->mu);
+  cudaSetDevice(dev->pd->cuda_device);
+  process_completions(&dev->queue, false);
+  if (f->signaled) return f->error;
+  return VK_NOT_READY;
+}
+
+VkResult wait_fences(Device* dev, uint32_t n, const VkFence* fences, VkBool32 all, uint64_t timeout) {
+  auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    {
+      std::lock_guard<std::recursive_mutex> lock(dev->mu);
+      cudaSetDevice(dev->pd->cuda_device);
+      process_completions(&dev->queue, false);
+      uint32_t done = 0;
+      VkResult err = VK_SUCCESS;
+      for (uint32_t i = 0; i < n; i++) {
+        Fence* f = H<Fence>(fences[i]);
+        if (f->signaled) {
+          done++;
+          if (f->error != VK_SUCCESS) err = f->error;
+        }
+      }
+      if (err != VK_SUCCESS) return err;
+      if ((all && done == n) || (!all && done > 0)) return VK_SUCCESS;
+      if (timeout == 0) return VK_TIMEOUT;
+      /* block on the oldest submission when waiting without a deadline */
+      if (timeout == UINT64_MAX && !dev->queue.inflight.empty()) {
+        cudaEventSynchronize(dev->queue.inflight.front().done);
+        continue;
+      }
+    }
+    auto el = std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+    if ((uint64_t)el >= timeout) return VK_TIMEOUT;
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+}  // namespace kz
+
+extern "C" KZ_API void* kzGetQueueStream(VkQueue queue) {
+  return (void*)kz::H<kz::Queue>(queue)->stream;
+}
+
+extern "C" KZ_API int kzGetCommandBufferStats(VkCommandBuffer cbh, KzCommandBufferStats* out) {
+  kz::CommandBuffer* cb = kz::H<kz::CommandBuffer>(cbh);
+  if (!cb || !out) return -1;
+  std::memset(out, 0, sizeof(*out));
+  if (!cb->low) return -1;
+  const kz::Lowered& low = *cb->low;
+  out->triangles = low.triangles;
+  out->draws = (uint32_t)low.draws.size();
+  out->segments = (uint32_t)low.segments.size();
+  out->mode = (uint32_t)low.mode;
+  out->tile = low.tile;
+  out->status = cb->last_status.flags;
+  out->records = cb->last_status.need_records;
+  out->pairs = cb->last_status.need_pairs;
+  out->fragments = cb->last_status.fragments_lo;
+  out->rec_cap = low.rec_cap;
+  out->pair_cap = low.pair_cap;
+  out->gpu_ms = cb->last_ms;
+  uint32_t launches = 0;
+  for (const auto& op : low.ops) {
+    if (op.kind == kz::OpKind::Pass) {
+      if (low.mode == 0) launches += op.seg_end > op.seg_begin ? 1 : 0;
+      else
+        for (uint32_t s = op.seg_begin; s < op.seg_end; s++) launches += (low.segments[s].num_chunks ? 4 : 3);
+    } else if (op.kind == kz::OpKind::Clear || op.kind == kz::OpKind::Fill) {
+      launches++;
+    }
+  }
+  out->launches = launches;
+  return 0;
+}

@@ -1,0 +1,295 @@
+/*
+ * kz_icd.h - objects of the kazan GB300 Vulkan driver (internal).
+ *
+ * Mirrors the reference driver's object model (vulkan-driver/src/handle.rs, api_impl.rs): dispatchable
+ * handles (instance, physical device, device, queue, command buffer) start with the loader dispatch
+ * word initialised to ICD_LOADER_MAGIC (handle.rs:23-37); every other handle is a pointer to a heap
+ * object owned by the application between vkCreate* and vkDestroy* (handle.rs:121-209).
+ *
+ * Where the reference keeps memory in host RAM (device_memory.rs:206-217) and has no command
+ * execution at all (api_impl.rs:3414, 4436-4970 are `unimplemented!()`), this driver keeps memory in
+ * HBM and executes recorded command buffers with the sm_103a pipeline kernels.
+ */
+#ifndef KZ_ICD_H
+#define KZ_ICD_H
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../kz_raster_abi.h"
+#include "../shader/kz_ir.h"
+#include "kz_vk_abi.h"
+
+namespace kz {
+
+struct Instance;
+struct PhysicalDevice;
+struct Device;
+struct Queue;
+struct CommandBuffer;
+
+struct Dispatchable {
+  uintptr_t loader_magic = ICD_LOADER_MAGIC;
+};
+
+struct PhysicalDevice : Dispatchable {
+  Instance* instance = nullptr;
+  int cuda_device = 0;
+  int sm_count = 0;
+  size_t hbm_bytes = 0;
+  std::string name;
+};
+
+struct Instance : Dispatchable {
+  PhysicalDevice* pd = nullptr;
+  uint32_t api_version = VK_API_VERSION_1_1;
+};
+
+/* memory types: 0 = DEVICE_LOCAL|HOST_VISIBLE|HOST_COHERENT|HOST_CACHED (the reference's single
+ * "Main" type, device_memory.rs:30-38), 1 = DEVICE_LOCAL only */
+struct DeviceMemory {
+  Device* dev = nullptr;
+  VkDeviceSize size = 0;
+  uint32_t type = 0;
+  char* dptr = nullptr;        /* HBM */
+  char* host = nullptr;        /* pinned host shadow behind vkMapMemory (type 0 only) */
+  bool mapped = false;
+  bool device_newer = false;   /* the GPU wrote it since the host shadow was last refreshed */
+};
+
+struct Buffer {
+  VkDeviceSize size = 0;
+  VkBufferUsageFlags usage = 0;
+  DeviceMemory* mem = nullptr;
+  VkDeviceSize offset = 0;
+  char* ptr() const { return mem ? mem->dptr + offset : nullptr; }
+};
+
+struct Image {
+  VkFormat format = VK_FORMAT_UNDEFINED;
+  uint32_t width = 0, height = 0;
+  VkImageTiling tiling = VK_IMAGE_TILING_OPTIMAL;
+  VkImageUsageFlags usage = 0;
+  uint32_t bpp = 4;
+  uint32_t pitch = 0;
+  VkDeviceSize size = 0;
+  DeviceMemory* mem = nullptr;
+  VkDeviceSize offset = 0;
+  char* ptr() const { return mem ? mem->dptr + offset : nullptr; }
+};
+
+struct ImageView {
+  Image* image = nullptr;
+  VkFormat format = VK_FORMAT_UNDEFINED;
+};
+
+struct ShaderModule {
+  std::vector<uint32_t> code;
+};
+
+struct PipelineLayout {
+  uint32_t push_size = 0;
+};
+
+struct RenderPass {
+  std::vector<VkAttachmentDescription> atts;
+  int color_att = -1;
+  int depth_att = -1;
+};
+
+struct Framebuffer {
+  RenderPass* rp = nullptr;
+  std::vector<ImageView*> views;
+  uint32_t width = 0, height = 0;
+};
+
+struct Pipeline {
+  uint64_t uid = 0;
+  KzPipe pipe{};
+  std::shared_ptr<ir::Shader> vs, fs;
+  VkViewport viewport{};
+  VkRect2D scissor{};
+  bool dyn_viewport = false, dyn_scissor = false, dyn_blend = false;
+  bool rasterizer_discard = false;
+  int vis_key = -1; /* KzVisKey when the pipeline can be resolved order-independently, else -1 */
+};
+
+struct Fence {
+  cudaEvent_t ev = nullptr;
+  bool signaled = false;
+  bool pending = false;
+  VkResult error = VK_SUCCESS;
+};
+
+struct Semaphore {};
+struct PipelineCache {};
+
+/* a linked pipeline-kernel module for one pipeline set */
+struct KernelSet {
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t geometry = nullptr, scan = nullptr, bin = nullptr, raster = nullptr, persistent = nullptr,
+               clear = nullptr;
+  int persistent_blocks = 0;
+};
+
+/* ---- recording ---- */
+
+struct DrawRec {
+  Pipeline* pipe = nullptr;
+  KzDraw d{};
+  uint8_t push[KZ_PUSH_BYTES];
+  uint64_t triangles = 0;
+  DeviceMemory* reads[KZ_MAX_BINDINGS + 1] = {};
+};
+
+struct PassRec {
+  Framebuffer* fb = nullptr;
+  RenderPass* rp = nullptr;
+  int32_t area[4] = {0, 0, 0, 0};
+  VkClearValue clear_color{}, clear_depth{};
+  std::vector<DrawRec> draws;
+};
+
+enum class OpKind { Pass, Clear, Copy, Copy2D, Fill };
+
+struct RecOp {
+  OpKind kind = OpKind::Pass;
+  size_t pass = 0;                       /* index into passes for Pass */
+  /* Clear / Fill: rows [y0,y1) x [x0,x1) of a 4-byte-per-pixel surface */
+  char* base = nullptr;
+  uint32_t pitch = 0;
+  int32_t rect[4] = {0, 0, 0, 0};
+  uint32_t value = 0;
+  /* Copy / Copy2D */
+  char* dst = nullptr;
+  const char* src = nullptr;
+  size_t bytes = 0, width_bytes = 0, rows = 0, dpitch = 0, spitch = 0;
+  DeviceMemory* wmem = nullptr;          /* memory the op writes */
+  DeviceMemory* rmem = nullptr;          /* memory the op reads */
+};
+
+/* lowered command buffer */
+struct Lowered {
+  std::vector<KzDraw> draws;
+  std::vector<KzPipe> pipes;
+  std::vector<Pipeline*> pipe_objs;
+  std::vector<KzChunk> chunks;
+  std::vector<KzSegment> segments;
+  std::vector<uint8_t> push;
+  struct LOp {
+    OpKind kind;
+    uint32_t seg_begin = 0, seg_end = 0;  /* Pass: segments [begin, end); others: segments before it */
+    RecOp op;
+  };
+  std::vector<LOp> ops;
+  std::vector<DeviceMemory*> reads, writes;
+  uint64_t triangles = 0;
+  uint32_t max_tiles = 0;
+  /* device memory */
+  char* d_tables = nullptr;
+  size_t tables_bytes = 0;
+  KzFrame frame{};
+  char* d_records = nullptr;
+  char* d_bins = nullptr;
+  uint32_t* d_tiles = nullptr;
+  KzSegCounters* d_counters = nullptr;
+  KzStatus* d_status = nullptr;
+  KzStatus* h_status = nullptr;
+  uint32_t rec_cap = 0, pair_cap = 0;
+  KernelSet* ks = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+  int mode = 0; /* 0 persistent, 1 batched, 2 per-draw */
+  uint32_t tile = 16;
+};
+
+struct CommandPool {
+  Device* dev = nullptr;
+  std::vector<CommandBuffer*> buffers;
+};
+
+struct CommandBuffer : Dispatchable {
+  Device* dev = nullptr;
+  CommandPool* pool = nullptr;
+  bool recording = false;
+  /* recording state */
+  Pipeline* pipe = nullptr;
+  VkViewport viewport{};
+  VkRect2D scissor{};
+  bool have_viewport = false, have_scissor = false;
+  float blend_const[4] = {0, 0, 0, 0};
+  bool have_blend_const = false;
+  Buffer* vb[KZ_MAX_BINDINGS] = {};
+  VkDeviceSize vb_off[KZ_MAX_BINDINGS] = {};
+  Buffer* ib = nullptr;
+  VkDeviceSize ib_off = 0;
+  VkIndexType ib_type = VK_INDEX_TYPE_UINT32;
+  uint8_t push[KZ_PUSH_BYTES] = {};
+  int cur_pass = -1;
+  std::vector<PassRec> passes;
+  std::vector<RecOp> ops;
+  VkResult record_error = VK_SUCCESS;
+  std::unique_ptr<Lowered> low;
+  /* statistics of the last completed execution */
+  KzStatus last_status{};
+  float last_ms = 0.0f;
+};
+
+struct Submission {
+  CommandBuffer* cb = nullptr;
+  cudaEvent_t done = nullptr;
+  Fence* fence = nullptr;
+};
+
+struct Queue : Dispatchable {
+  Device* dev = nullptr;
+  cudaStream_t stream = nullptr;
+  std::vector<Submission> inflight;
+  VkResult lost = VK_SUCCESS;
+};
+
+struct Device : Dispatchable {
+  PhysicalDevice* pd = nullptr;
+  Queue queue;
+  cudaStream_t capture_stream = nullptr;
+  std::recursive_mutex mu;
+  std::map<std::vector<uint64_t>, KernelSet*> kernel_sets;
+  std::vector<cudaEvent_t> event_pool;
+};
+
+/* global options (kzDriverSetOption / KZ_* environment variables) */
+struct Options {
+  int mode = 0;       /* KZ_MODE: persistent (0), batched (1), perdraw (2) */
+  uint32_t tile = 16; /* KZ_TILE */
+  double rec_slack = 1.25;
+  int trace = 0;      /* KZ_TRACE */
+  long fault_alloc = -1; /* KZ_FAULT=alloc:N: the Nth device allocation fails */
+};
+Options& options();
+
+/* internal helpers shared by the translation units */
+VkResult device_alloc(size_t bytes, void** out);
+void device_free(void* p);
+const std::vector<char>& pipeline_object();
+KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std::string& err);
+void log_error(const char* fmt, ...);
+
+/* command buffer / queue entry points implemented in kz_cmd.cpp */
+VkResult lower_command_buffer(CommandBuffer* cb);
+void free_lowered(Lowered* low);
+VkResult queue_submit(Queue* q, uint32_t count, const VkSubmitInfo* submits, Fence* fence);
+VkResult queue_wait_idle(Queue* q);
+VkResult fence_status(Device* dev, Fence* f);
+VkResult wait_fences(Device* dev, uint32_t n, const VkFence* fences, VkBool32 all, uint64_t timeout);
+
+}  // namespace kz
+
+#endif

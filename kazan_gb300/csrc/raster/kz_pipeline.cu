@@ -1,0 +1,1195 @@
+/*
+ * kz_pipeline.cu - sm_103a pipeline kernels of the kazan draw path.
+ *
+ * Compiled once (nvcc -rdc=true -cubin) into a relocatable device object.  The shader stages are not
+ * part of it: kz_vs / kz_vs_pos / kz_fs are resolved when a pipeline set is JIT-linked with the PTX
+ * that the shader backend emits from SPIR-V (see shader/kz_ptx_backend.cpp).  The reference has no
+ * counterpart for any kernel here (vulkan-driver/src/api_impl.rs:4632-4653 are `unimplemented!()`).
+ *
+ * Phases of one raster segment (see kz_raster_abi.h):
+ *   geometry  per triangle: index + attribute fetch, position-only vertex shader, guard-band clip,
+ *             viewport transform, 16.8 snap, facing/cull, bounding box -> KzTriRecord, tile pair counts
+ *   scan      per tile: exclusive prefix of pair counts -> bin offsets; capacity checks
+ *   bin       per record: scatter record index into each overlapped tile's bin
+ *   raster    per tile: visibility mode  - shared-memory 64-bit atomicMin of (depth, primitive) keys,
+ *                                          then one fragment-shader call per pixel for the winner
+ *                       ordered mode     - bin sorted by primitive, per-pixel in-order depth/blend
+ *
+ * Arithmetic follows the rules the CPU oracle restates (every float op an explicit IEEE single op;
+ * the file is built with -fmad=false and uses the __f*_rn intrinsics), so coverage, depth and colour
+ * are bit-identical to it.
+ */
+#include <stdint.h>
+
+#include "../kz_raster_abi.h"
+
+extern "C" __device__ void kz_vs(uint32_t pipe, const KzVsIn* in, const uint8_t* push, KzVsOut* out);
+extern "C" __device__ void kz_vs_pos(uint32_t pipe, const KzVsIn* in, const uint8_t* push, float* pos);
+extern "C" __device__ uint32_t kz_fs(uint32_t pipe, const KzFsIn* in, const uint8_t* push, float* color);
+
+#define KZ_THREADS 256
+#define KZ_SORT_CAP 4096          /* ordered mode: largest bin sorted in shared memory */
+#define KZ_BATCH 32               /* ordered mode: triangles set up per batch */
+#define KZ_BARRIER_NS 4000000000ull /* grid barrier gives up after 4 s */
+
+namespace {
+
+/* ---------------- exact arithmetic ---------------- */
+
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+__device__ __forceinline__ uint8_t unorm8(float v) {
+  float c = fminf(fmaxf(v, 0.0f), 1.0f);
+  return (uint8_t)__float2int_rn(fmul(c, 255.0f));
+}
+__device__ __forceinline__ float u8f(uint32_t u) { return fdiv(__uint2float_rn(u), 255.0f); }
+
+__device__ __forceinline__ int64_t floordiv256(int64_t a) { return a >= 0 ? a / 256 : -((-a + 255) / 256); }
+
+/* ---------------- frame access ---------------- */
+
+struct Ctx {
+  const KzFrame* f;
+  const KzSegment* seg;
+  KzSegCounters* cnt;
+  KzStatus* st;
+  const KzDraw* draws;
+  const KzPipe* pipes;
+};
+
+__device__ __forceinline__ Ctx make_ctx(const KzFrame& f, uint32_t s) {
+  Ctx c;
+  c.f = &f;
+  c.seg = reinterpret_cast<const KzSegment*>(f.segments) + s;
+  c.cnt = reinterpret_cast<KzSegCounters*>(c.seg->counters);
+  c.st = reinterpret_cast<KzStatus*>(f.status);
+  c.draws = reinterpret_cast<const KzDraw*>(f.draws);
+  c.pipes = reinterpret_cast<const KzPipe*>(f.pipes);
+  return c;
+}
+
+__device__ __forceinline__ const uint8_t* push_ptr(const KzFrame& f, const KzDraw& d) {
+  return reinterpret_cast<const uint8_t*>(f.push) + (size_t)d.push_index * KZ_PUSH_BYTES;
+}
+
+/* last draw of the segment whose prim_base <= g */
+__device__ uint32_t find_draw(const KzDraw* draws, uint32_t first, uint32_t count, uint32_t g) {
+  uint32_t lo = first, hi = first + count;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (draws[mid].prim_base <= g) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__device__ void tri_vertices(const KzDraw& d, uint32_t local, uint32_t vid[3], uint32_t& iid) {
+  uint32_t inst = local / d.tri_count;
+  uint32_t t = local - inst * d.tri_count;
+  iid = d.first_instance + inst;
+  if (d.indexed == 1) {
+    const uint32_t* ib = reinterpret_cast<const uint32_t*>(d.ib) + (size_t)3 * t;
+    for (int j = 0; j < 3; j++) vid[j] = __ldg(ib + j) + (uint32_t)d.vertex_offset;
+  } else if (d.indexed == 2) {
+    const uint16_t* ib = reinterpret_cast<const uint16_t*>(d.ib) + (size_t)3 * t;
+    for (int j = 0; j < 3; j++) vid[j] = (uint32_t)__ldg(ib + j) + (uint32_t)d.vertex_offset;
+  } else {
+    for (int j = 0; j < 3; j++) vid[j] = (uint32_t)d.vertex_offset + 3u * t + (uint32_t)j;
+  }
+}
+
+__device__ void fetch_inputs(const KzPipe& p, const KzDraw& d, uint32_t vid, uint32_t iid, uint32_t mask,
+                             KzVsIn& in) {
+  uint32_t na = p.num_attrs;
+  for (uint32_t a = 0; a < na; a++) {
+    KzAttr at = p.attrs[a];
+    if (!((mask >> at.location) & 1u)) continue;
+    uint32_t b = at.binding;
+    uint32_t idx = ((p.binding_instanced >> b) & 1u) ? iid : vid;
+    const char* src = reinterpret_cast<const char*>(d.vb[b]) + (size_t)idx * p.binding_stride[b] + at.offset;
+    float v[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+    uintptr_t addr = reinterpret_cast<uintptr_t>(src);
+    switch (at.format) {
+      case KZ_FMT_F32x4:
+        if ((addr & 15u) == 0) {
+          float4 q = __ldg(reinterpret_cast<const float4*>(src));
+          v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+          break;
+        }
+        v[3] = __ldg(reinterpret_cast<const float*>(src) + 3);
+        /* fall through */
+      case KZ_FMT_F32x3:
+        v[2] = __ldg(reinterpret_cast<const float*>(src) + 2);
+        /* fall through */
+      case KZ_FMT_F32x2:
+        if ((addr & 7u) == 0) {
+          float2 q = __ldg(reinterpret_cast<const float2*>(src));
+          v[0] = q.x; v[1] = q.y;
+          break;
+        }
+        v[1] = __ldg(reinterpret_cast<const float*>(src) + 1);
+        /* fall through */
+      case KZ_FMT_F32x1:
+        v[0] = __ldg(reinterpret_cast<const float*>(src));
+        break;
+      case KZ_FMT_U8x4_UNORM: {
+        uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(src));
+        for (int k = 0; k < 4; k++) v[k] = u8f((w >> (8 * k)) & 0xFFu);
+        break;
+      }
+      case KZ_FMT_U32x4: v[3] = __uint_as_float(__ldg(reinterpret_cast<const uint32_t*>(src) + 3)); /* fall through */
+      case KZ_FMT_U32x3: v[2] = __uint_as_float(__ldg(reinterpret_cast<const uint32_t*>(src) + 2)); /* fall through */
+      case KZ_FMT_U32x2: v[1] = __uint_as_float(__ldg(reinterpret_cast<const uint32_t*>(src) + 1)); /* fall through */
+      case KZ_FMT_U32x1: v[0] = __uint_as_float(__ldg(reinterpret_cast<const uint32_t*>(src))); break;
+      default: break;
+    }
+    in.attr[at.location][0] = v[0];
+    in.attr[at.location][1] = v[1];
+    in.attr[at.location][2] = v[2];
+    in.attr[at.location][3] = v[3];
+  }
+  in.vertex_index = vid;
+  in.instance_index = iid;
+}
+
+/* ---------------- clipping ---------------- */
+
+__device__ __forceinline__ float plane_dist(const float* p, int plane) {
+  switch (plane) {
+    case 0: return p[2];
+    case 1: return fsub(p[3], p[2]);
+    case 2: return fadd(p[0], fmul(KZ_GUARD_BAND, p[3]));
+    case 3: return fsub(fmul(KZ_GUARD_BAND, p[3]), p[0]);
+    case 4: return fadd(p[1], fmul(KZ_GUARD_BAND, p[3]));
+    default: return fsub(fmul(KZ_GUARD_BAND, p[3]), p[1]);
+  }
+}
+
+/* 0: reject, 1: inside the guard band, 2: needs clipping */
+__device__ int classify(const float pos[3][4]) {
+  bool all[6] = {true, true, true, true, true, true};
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (!isfinite(pos[j][k])) return 0;
+    const float* c = pos[j];
+    all[0] &= c[0] > c[3];
+    all[1] &= c[0] < -c[3];
+    all[2] &= c[1] > c[3];
+    all[3] &= c[1] < -c[3];
+    all[4] &= c[2] < 0.0f;
+    all[5] &= c[2] > c[3];
+  }
+  if (all[0] | all[1] | all[2] | all[3] | all[4] | all[5]) return 0;
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+#pragma unroll
+    for (int plane = 0; plane < 6; plane++)
+      if (plane_dist(pos[j], plane) < 0.0f) return 2;
+  return 1;
+}
+
+struct ClipV {
+  float c[4 + KZ_MAX_VARYINGS];
+};
+
+/* Sutherland-Hodgman against z>=0, z<=w, |x|,|y|<=4w; nc varyings ride along.  Returns the polygon
+ * size (0 = rejected). */
+__device__ __noinline__ int clip_polygon(ClipV* a, int nc) {
+  ClipV b[KZ_MAX_CLIP_VERTS];
+  int n = 3;
+  ClipV* cur = a;
+  ClipV* nxt = b;
+  for (int plane = 0; plane < 6; plane++) {
+    bool any_out = false;
+    for (int i = 0; i < n; i++)
+      if (plane_dist(cur[i].c, plane) < 0.0f) any_out = true;
+    if (!any_out) continue;
+    int m = 0;
+    for (int i = 0; i < n; i++) {
+      const ClipV& p = cur[i];
+      const ClipV& q = cur[(i + 1) % n];
+      float dp = plane_dist(p.c, plane), dq = plane_dist(q.c, plane);
+      bool pin = dp >= 0.0f, qin = dq >= 0.0f;
+      if (pin) nxt[m++] = p;
+      if (pin != qin) {
+        const ClipV& vi = pin ? p : q;
+        const ClipV& vo = pin ? q : p;
+        float di = pin ? dp : dq, dout = pin ? dq : dp;
+        float t = fdiv(di, fsub(di, dout));
+        ClipV c;
+        for (int k = 0; k < 4 + nc; k++) c.c[k] = ffma(t, fsub(vo.c[k], vi.c[k]), vi.c[k]);
+        nxt[m++] = c;
+      }
+    }
+    n = m;
+    ClipV* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+    if (n < 3) return 0;
+  }
+  for (int i = 0; i < n; i++) {
+    if (!(cur[i].c[3] > 0.0f)) return 0;
+    if (cur != a) a[i] = cur[i];
+  }
+  return n;
+}
+
+/* ---------------- triangle setup ---------------- */
+
+struct Proj {
+  int32_t X, Y;
+  float z, iw;
+};
+
+__device__ __forceinline__ Proj project(const KzDraw& d, const float* c) {
+  Proj p;
+  float iw = fdiv(1.0f, c[3]);
+  float xd = fmul(c[0], iw), yd = fmul(c[1], iw), zd = fmul(c[2], iw);
+  float xf = ffma(xd, d.hx, d.ox), yf = ffma(yd, d.hy, d.oy);
+  p.z = ffma(zd, d.pz, d.oz);
+  p.X = __float2int_rn(fmul(xf, 256.0f));
+  p.Y = __float2int_rn(fmul(yf, 256.0f));
+  p.iw = iw;
+  return p;
+}
+
+/* Fills the coverage/depth record from three projected vertices; returns false when the triangle can
+ * produce no fragment (degenerate, culled, or no pixel centre in its box). */
+__device__ bool make_record(const KzDraw& d, const KzPipe& pp, Proj v[3], KzTriRecord& r, bool& swapped) {
+  int64_t S = (int64_t)(v[1].X - v[0].X) * (v[2].Y - v[0].Y) - (int64_t)(v[2].X - v[0].X) * (v[1].Y - v[0].Y);
+  if (S == 0) return false;
+  bool front = pp.front_ccw ? (S < 0) : (S > 0);
+  if (((pp.cull_mode & 2u) && !front) || ((pp.cull_mode & 1u) && front)) return false;
+  swapped = S < 0;
+  if (swapped) {
+    Proj t = v[1];
+    v[1] = v[2];
+    v[2] = t;
+    S = -S;
+  }
+  int32_t minx = min(v[0].X, min(v[1].X, v[2].X)), maxx = max(v[0].X, max(v[1].X, v[2].X));
+  int32_t miny = min(v[0].Y, min(v[1].Y, v[2].Y)), maxy = max(v[0].Y, max(v[1].Y, v[2].Y));
+  int64_t bx0 = -floordiv256(-((int64_t)minx - 128));
+  int64_t by0 = -floordiv256(-((int64_t)miny - 128));
+  int64_t bx1 = floordiv256((int64_t)maxx - 128);
+  int64_t by1 = floordiv256((int64_t)maxy - 128);
+  if (bx0 < d.rect[0]) bx0 = d.rect[0];
+  if (by0 < d.rect[1]) by0 = d.rect[1];
+  if (bx1 > d.rect[2] - 1) bx1 = d.rect[2] - 1;
+  if (by1 > d.rect[3] - 1) by1 = d.rect[3] - 1;
+  if (bx0 > bx1 || by0 > by1) return false;
+  uint32_t info = 0;
+#pragma unroll
+  for (int e = 0; e < 3; e++) {
+    int a = (e + 1) % 3, b = (e + 2) % 3;
+    int32_t dx = v[b].X - v[a].X, dy = v[b].Y - v[a].Y;
+    if ((dy < 0) || (dy == 0 && dx > 0)) info |= 1u << e;
+  }
+  if (swapped) info |= 8u;
+  if (front) info |= 256u;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    r.x[i] = v[i].X;
+    r.y[i] = v[i].Y;
+  }
+  r.z0 = v[0].z;
+  r.dz1 = fsub(v[1].z, v[0].z);
+  r.dz2 = fsub(v[2].z, v[0].z);
+  r.inv_s = fdiv(1.0f, __ll2float_rn(S));
+  r.info = info;
+  r.bb0 = (uint32_t)bx0 | ((uint32_t)by0 << 16);
+  r.bb1 = (uint32_t)bx1 | ((uint32_t)by1 << 16);
+  return true;
+}
+
+/* edge e of a record is v(e+1) -> v(e+2); E_e(p) = dx (py - ya) - dy (px - xa) */
+struct Edges {
+  int32_t dx[3], dy[3], xa[3], ya[3];
+  int64_t thr[3];
+};
+
+__device__ __forceinline__ void edges_of(const KzTriRecord& r, Edges& e) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    int a = (k + 1) % 3, b = (k + 2) % 3;
+    e.dx[k] = r.x[b] - r.x[a];
+    e.dy[k] = r.y[b] - r.y[a];
+    e.xa[k] = r.x[a];
+    e.ya[k] = r.y[a];
+    e.thr[k] = ((r.info >> k) & 1u) ? 0 : 1;
+  }
+}
+
+__device__ __forceinline__ int64_t edge_at(const Edges& e, int k, int64_t px, int64_t py) {
+  return (int64_t)e.dx[k] * (py - e.ya[k]) - (int64_t)e.dy[k] * (px - e.xa[k]);
+}
+
+/* ---------------- full setup for shading ---------------- */
+
+struct Shade {
+  KzTriRecord r;      /* coverage + depth */
+  float iw[3];
+  float a[3][KZ_MAX_VARYINGS];
+  uint32_t pipe;
+  uint32_t draw;
+  uint32_t ok;
+};
+
+__device__ void vs_full(const Ctx& c, const KzDraw& d, const KzPipe& p, uint32_t vid, uint32_t iid, KzVsOut& o) {
+  KzVsIn in;
+  fetch_inputs(p, d, vid, iid, p.full_input_mask, in);
+  kz_vs(d.pipe, &in, push_ptr(*c.f, d), &o);
+}
+
+/* Build the shading setup of a (sub-)triangle from three full vertices (clip position + varyings). */
+__device__ bool shade_from_vertices(const KzDraw& d, const KzPipe& p, const ClipV* v, int nc, Shade& s) {
+  Proj pr[3];
+  for (int i = 0; i < 3; i++) pr[i] = project(d, v[i].c);
+  bool swapped = false;
+  if (!make_record(d, p, pr, s.r, swapped)) return false;
+  int order[3] = {0, swapped ? 2 : 1, swapped ? 1 : 2};
+  for (int i = 0; i < 3; i++) {
+    const ClipV& src = v[order[i]];
+    float iw = fdiv(1.0f, src.c[3]);
+    s.iw[i] = iw;
+    for (int k = 0; k < nc; k++) {
+      float val = src.c[4 + k];
+      bool flat = (p.flat_mask >> k) & 1u;
+      if (flat) val = v[0].c[4 + k];
+      s.a[i][k] = (flat || ((p.noperspective_mask >> k) & 1u)) ? val : fmul(val, iw);
+    }
+  }
+  return true;
+}
+
+/* True if pixel (x, y) is covered by the record. */
+__device__ __forceinline__ bool covers(const KzTriRecord& r, int32_t x, int32_t y, int64_t E[3]) {
+  Edges e;
+  edges_of(r, e);
+  int64_t px = (int64_t)x * 256 + 128, py = (int64_t)y * 256 + 128;
+  bool in = true;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    E[k] = edge_at(e, k, px, py);
+    in &= E[k] >= e.thr[k];
+  }
+  return in;
+}
+
+/* Recompute primitive g of the segment for shading at pixel (x, y) (sub-triangle chosen by coverage
+ * when the primitive was clipped, or by `sub` when it is known: sub = clip sub-index + 1, 0 = any). */
+__device__ __noinline__ bool shade_setup(const Ctx& c, uint32_t g, int32_t x, int32_t y, uint32_t sub, Shade& s) {
+  const KzSegment& seg = *c.seg;
+  uint32_t di = find_draw(c.draws, seg.first_draw, seg.num_draws, g);
+  const KzDraw& d = c.draws[di];
+  const KzPipe& p = c.pipes[d.pipe];
+  uint32_t vid[3], iid;
+  tri_vertices(d, g - d.prim_base, vid, iid);
+  int nc = (int)p.num_varyings;
+  ClipV v[KZ_MAX_CLIP_VERTS];
+  for (int j = 0; j < 3; j++) {
+    KzVsOut o;
+    vs_full(c, d, p, vid[j], iid, o);
+    for (int k = 0; k < 4; k++) v[j].c[k] = o.pos[k];
+    for (int k = 0; k < nc; k++) v[j].c[4 + k] = o.var[k];
+  }
+  s.pipe = d.pipe;
+  s.draw = di;
+  float pos[3][4];
+  for (int j = 0; j < 3; j++)
+    for (int k = 0; k < 4; k++) pos[j][k] = v[j].c[k];
+  int cls = classify(pos);
+  if (cls == 0) return false;
+  if (cls == 1) return shade_from_vertices(d, p, v, nc, s);
+  ClipV v0 = v[0];
+  int n = clip_polygon(v, nc);
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < nc; k++)
+      if ((p.flat_mask >> k) & 1u) v[i].c[4 + k] = v0.c[4 + k];
+  for (int i = 1; i + 1 < n; i++) {
+    if (sub != 0 && (uint32_t)i != sub) continue;
+    ClipV tri[3] = {v[0], v[i], v[i + 1]};
+    if (!shade_from_vertices(d, p, tri, nc, s)) continue;
+    if (sub != 0) return true;
+    int64_t E[3];
+    if (covers(s.r, x, y, E)) return true;
+  }
+  return false;
+}
+
+/* interpolate varyings and run the fragment shader */
+__device__ uint32_t shade_pixel(const Ctx& c, const Shade& s, int32_t x, int32_t y, const int64_t E[3], float z,
+                                float col[4]) {
+  const KzPipe& p = c.pipes[s.pipe];
+  const KzDraw& d = c.draws[s.draw];
+  float l0 = fmul(__ll2float_rn(E[0]), s.r.inv_s);
+  float l1 = fmul(__ll2float_rn(E[1]), s.r.inv_s);
+  float l2 = fmul(__ll2float_rn(E[2]), s.r.inv_s);
+  float q = ffma(l2, s.iw[2], ffma(l1, s.iw[1], fmul(l0, s.iw[0])));
+  float rq = fdiv(1.0f, q);
+  KzFsIn in;
+  int nc = (int)p.num_varyings;
+  for (int k = 0; k < nc; k++) {
+    float num = ffma(l2, s.a[2][k], ffma(l1, s.a[1][k], fmul(l0, s.a[0][k])));
+    in.var[k] = ((p.noperspective_mask >> k) & 1u) || ((p.flat_mask >> k) & 1u) ? num : fmul(num, rq);
+    if ((p.flat_mask >> k) & 1u) in.var[k] = s.a[0][k];
+  }
+  in.frag_coord[0] = fadd((float)x, 0.5f);
+  in.frag_coord[1] = fadd((float)y, 0.5f);
+  in.frag_coord[2] = z;
+  in.frag_coord[3] = q;
+  in.front_facing = (s.r.info >> 8) & 1u;
+  if (!p.has_fs) {
+    col[0] = col[1] = col[2] = col[3] = 0.0f;
+    return 0;
+  }
+  return kz_fs(s.pipe, &in, push_ptr(*c.f, d), col);
+}
+
+/* ---------------- fragment operations ---------------- */
+
+__device__ __forceinline__ bool depth_cmp(uint32_t op, float z, float d) {
+  switch (op) {
+    case 0: return false;
+    case 1: return z < d;
+    case 2: return z == d;
+    case 3: return z <= d;
+    case 4: return z > d;
+    case 5: return z != d;
+    case 6: return z >= d;
+    default: return true;
+  }
+}
+
+__device__ float blend_factor(uint32_t f, int ch, const float s[4], const float dst[4], const float k[4]) {
+  switch (f) {
+    case 0: return 0.0f;
+    case 1: return 1.0f;
+    case 2: return s[ch];
+    case 3: return fsub(1.0f, s[ch]);
+    case 4: return dst[ch];
+    case 5: return fsub(1.0f, dst[ch]);
+    case 6: return s[3];
+    case 7: return fsub(1.0f, s[3]);
+    case 8: return dst[3];
+    case 9: return fsub(1.0f, dst[3]);
+    case 10: return k[ch];
+    case 11: return fsub(1.0f, k[ch]);
+    case 12: return k[3];
+    case 13: return fsub(1.0f, k[3]);
+    case 14: return ch < 3 ? fminf(s[3], fsub(1.0f, dst[3])) : 1.0f;
+    default: return 0.0f;
+  }
+}
+
+__device__ __forceinline__ float blend_op(uint32_t op, float s, float sf, float d, float df) {
+  switch (op) {
+    case 0: return ffma(s, sf, fmul(d, df));
+    case 1: return ffma(s, sf, -fmul(d, df));
+    case 2: return ffma(d, df, -fmul(s, sf));
+    case 3: return fminf(s, d);
+    default: return fmaxf(s, d);
+  }
+}
+
+/* colour in attachment byte order -> RGBA channel order */
+__device__ __forceinline__ uint32_t to_rgba(uint32_t px, uint32_t fmt) {
+  if (fmt == KZ_CF_BGRA8) return (px & 0xFF00FF00u) | ((px >> 16) & 0xFFu) | ((px & 0xFFu) << 16);
+  return px;
+}
+__device__ __forceinline__ uint32_t from_rgba(uint32_t px, uint32_t fmt) { return to_rgba(px, fmt); }
+
+/* apply blend + write mask; dst/out packed RGBA (R in the low byte) */
+__device__ uint32_t color_write(const KzPipe& p, uint32_t dst, const float col[4]) {
+  uint32_t out = dst;
+  if (p.blend_enable) {
+    float s[4], dd[4];
+    for (int i = 0; i < 4; i++) {
+      s[i] = fminf(fmaxf(col[i], 0.0f), 1.0f);
+      dd[i] = u8f((dst >> (8 * i)) & 0xFFu);
+    }
+    for (int i = 0; i < 4; i++) {
+      if (!((p.write_mask >> i) & 1u)) continue;
+      float r;
+      if (i < 3)
+        r = blend_op(p.color_op, s[i], blend_factor(p.src_color, i, s, dd, p.blend_const), dd[i],
+                     blend_factor(p.dst_color, i, s, dd, p.blend_const));
+      else
+        r = blend_op(p.alpha_op, s[3], blend_factor(p.src_alpha, 3, s, dd, p.blend_const), dd[3],
+                     blend_factor(p.dst_alpha, 3, s, dd, p.blend_const));
+      out = (out & ~(0xFFu << (8 * i))) | ((uint32_t)unorm8(r) << (8 * i));
+    }
+  } else {
+    for (int i = 0; i < 4; i++)
+      if ((p.write_mask >> i) & 1u) out = (out & ~(0xFFu << (8 * i))) | ((uint32_t)unorm8(col[i]) << (8 * i));
+  }
+  return out;
+}
+
+/* ---------------- visibility keys ---------------- */
+
+__device__ __forceinline__ unsigned long long vis_key(uint32_t mode, float z, uint32_t g) {
+  uint32_t zb = __float_as_uint(z);
+  switch (mode) {
+    case KZ_VIS_LESS: return ((unsigned long long)zb << 32) | (g + 1u);
+    case KZ_VIS_LEQUAL: return ((unsigned long long)zb << 32) | (0xFFFFFFFEu - g);
+    case KZ_VIS_GREATER: return ((unsigned long long)(~zb) << 32) | (g + 1u);
+    case KZ_VIS_GEQUAL: return ((unsigned long long)(~zb) << 32) | (0xFFFFFFFEu - g);
+    default: return (unsigned long long)(0xFFFFFFFEu - g);
+  }
+}
+__device__ __forceinline__ unsigned long long vis_init(uint32_t mode, float d) {
+  uint32_t db = __float_as_uint(d);
+  switch (mode) {
+    case KZ_VIS_LESS: return (unsigned long long)db << 32;
+    case KZ_VIS_LEQUAL: return ((unsigned long long)db << 32) | 0xFFFFFFFFull;
+    case KZ_VIS_GREATER: return (unsigned long long)(~db) << 32;
+    case KZ_VIS_GEQUAL: return ((unsigned long long)(~db) << 32) | 0xFFFFFFFFull;
+    default: return 0xFFFFFFFFull;
+  }
+}
+/* returns true and the primitive when the key holds a fragment */
+__device__ __forceinline__ bool vis_decode(uint32_t mode, unsigned long long k, uint32_t& g, float& z) {
+  uint32_t lo = (uint32_t)k, hi = (uint32_t)(k >> 32);
+  bool frag;
+  if (mode == KZ_VIS_LESS || mode == KZ_VIS_GREATER) {
+    frag = lo != 0;
+    g = lo - 1u;
+  } else {
+    frag = lo != 0xFFFFFFFFu;
+    g = 0xFFFFFFFEu - lo;
+  }
+  z = (mode == KZ_VIS_GREATER || mode == KZ_VIS_GEQUAL) ? __uint_as_float(~hi) : __uint_as_float(hi);
+  return frag;
+}
+
+/* ---------------- status ---------------- */
+
+__device__ __forceinline__ uint32_t status_flags(const KzStatus* st) {
+  return *reinterpret_cast<const volatile uint32_t*>(&st->flags);
+}
+__device__ __forceinline__ bool segment_blocked(const Ctx& c, uint32_t s) {
+  uint32_t f = status_flags(c.st);
+  if (f & KZ_STATUS_BARRIER_TIMEOUT) return true;
+  if (f & (KZ_STATUS_RECORD_OVERFLOW | KZ_STATUS_PAIR_OVERFLOW))
+    return *reinterpret_cast<const volatile uint32_t*>(&c.st->failed_segment) <= s;
+  return false;
+}
+__device__ void mark_failed(KzStatus* st, uint32_t bits, uint32_t s) {
+  atomicMin(&st->failed_segment, s);
+  atomicOr(&st->flags, bits);
+}
+
+/* ---------------- phase: geometry ---------------- */
+
+__device__ __forceinline__ void tile_range(const KzSegment& seg, const KzTriRecord& r, int& tx0, int& ty0, int& tx1,
+                                           int& ty1) {
+  int T = (int)seg.tile;
+  tx0 = (int)(r.bb0 & 0xFFFFu) / T;
+  ty0 = (int)(r.bb0 >> 16) / T;
+  tx1 = (int)(r.bb1 & 0xFFFFu) / T;
+  ty1 = (int)(r.bb1 >> 16) / T;
+}
+
+/* Conservative test: can any pixel centre of tile (tx, ty) be inside the record's three edges? */
+__device__ __forceinline__ bool tile_overlaps(const KzSegment& seg, const Edges& e, int tx, int ty) {
+  int T = (int)seg.tile;
+  int64_t x0 = (int64_t)(tx * T) * 256 + 128, x1 = x0 + (int64_t)(T - 1) * 256;
+  int64_t y0 = (int64_t)(ty * T) * 256 + 128, y1 = y0 + (int64_t)(T - 1) * 256;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    int64_t px = e.dy[k] < 0 ? x1 : x0; /* maximise -dy*px */
+    int64_t py = e.dx[k] > 0 ? y1 : y0; /* maximise dx*py */
+    if (edge_at(e, k, px, py) < e.thr[k]) return false;
+  }
+  return true;
+}
+
+__device__ void count_tiles(const Ctx& c, const KzTriRecord& r) {
+  const KzSegment& seg = *c.seg;
+  int tx0, ty0, tx1, ty1;
+  tile_range(seg, r, tx0, ty0, tx1, ty1);
+  uint32_t* tc = reinterpret_cast<uint32_t*>(seg.tile_count);
+  if (tx0 == tx1 && ty0 == ty1) {
+    atomicAdd(&tc[ty0 * seg.tiles_x + tx0], 1u);
+    return;
+  }
+  Edges e;
+  edges_of(r, e);
+  for (int ty = ty0; ty <= ty1; ty++)
+    for (int tx = tx0; tx <= tx1; tx++)
+      if (tile_overlaps(seg, e, tx, ty)) atomicAdd(&tc[ty * seg.tiles_x + tx], 1u);
+}
+
+__device__ void emit_record(const Ctx& c, KzTriRecord& r) {
+  uint32_t idx = atomicAdd(&c.cnt->rec_count, 1u);
+  if (idx < c.seg->rec_cap) {
+    KzTriRecord* dst = reinterpret_cast<KzTriRecord*>(c.seg->records) + idx;
+    const uint4* s4 = reinterpret_cast<const uint4*>(&r);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    d4[0] = s4[0];
+    d4[1] = s4[1];
+    d4[2] = s4[2];
+    d4[3] = s4[3];
+  }
+  count_tiles(c, r);
+}
+
+__device__ __noinline__ void geometry_clipped(const Ctx& c, const KzDraw& d, const KzPipe& p, float pos[3][4],
+                                              uint32_t g, uint32_t di) {
+  ClipV v[KZ_MAX_CLIP_VERTS];
+  for (int j = 0; j < 3; j++)
+    for (int k = 0; k < 4; k++) v[j].c[k] = pos[j][k];
+  int n = clip_polygon(v, 0);
+  for (int i = 1; i + 1 < n; i++) {
+    Proj pr[3] = {project(d, v[0].c), project(d, v[i].c), project(d, v[i + 1].c)};
+    KzTriRecord r;
+    bool sw;
+    if (!make_record(d, p, pr, r, sw)) continue;
+    r.g = g;
+    r.draw = di;
+    r.pad = 0;
+    r.info |= (uint32_t)i << 4;
+    emit_record(c, r);
+  }
+}
+
+__device__ void geometry_triangle(const Ctx& c, uint32_t di, uint32_t local) {
+  const KzDraw& d = c.draws[di];
+  const KzPipe& p = c.pipes[d.pipe];
+  uint32_t vid[3], iid;
+  tri_vertices(d, local, vid, iid);
+  float pos[3][4];
+  const uint8_t* push = push_ptr(*c.f, d);
+  for (int j = 0; j < 3; j++) {
+    KzVsIn in;
+    fetch_inputs(p, d, vid[j], iid, p.pos_input_mask, in);
+    kz_vs_pos(d.pipe, &in, push, pos[j]);
+  }
+  uint32_t g = d.prim_base + local;
+  int cls = classify(pos);
+  if (cls == 0) return;
+  if (cls == 2) {
+    geometry_clipped(c, d, p, pos, g, di);
+    return;
+  }
+  Proj pr[3] = {project(d, pos[0]), project(d, pos[1]), project(d, pos[2])};
+  KzTriRecord r;
+  bool sw;
+  if (!make_record(d, p, pr, r, sw)) return;
+  r.g = g;
+  r.draw = di;
+  r.pad = 0;
+  emit_record(c, r);
+}
+
+__device__ void geometry_chunk(const Ctx& c, uint32_t chunk) {
+  const KzChunk ch = reinterpret_cast<const KzChunk*>(c.f->chunks)[chunk];
+  if (threadIdx.x < ch.count) geometry_triangle(c, ch.draw, ch.first + threadIdx.x);
+}
+
+/* ---------------- phase: scan (one block) ---------------- */
+
+__device__ void scan_tiles(const Ctx& c, uint32_t s, uint32_t* sh) {
+  const KzSegment& seg = *c.seg;
+  uint32_t n = seg.tiles_x * seg.tiles_y;
+  const uint32_t* tc = reinterpret_cast<const uint32_t*>(seg.tile_count);
+  uint32_t* to = reinterpret_cast<uint32_t*>(seg.tile_offset);
+  uint32_t* cur = reinterpret_cast<uint32_t*>(seg.tile_cursor);
+  uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+  uint32_t b0 = threadIdx.x * per, b1 = min(n, b0 + per);
+  uint32_t sum = 0, mx = 0;
+  for (uint32_t i = b0; i < b1; i++) {
+    uint32_t v = tc[i];
+    sum += v;
+    mx = max(mx, v);
+  }
+  sh[threadIdx.x] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (uint32_t i = 0; i < blockDim.x; i++) {
+      uint32_t v = sh[i];
+      sh[i] = run;
+      run += v;
+    }
+    sh[blockDim.x] = run;
+  }
+  __syncthreads();
+  uint32_t run = sh[threadIdx.x];
+  for (uint32_t i = b0; i < b1; i++) {
+    to[i] = run;
+    cur[i] = 0;
+    run += tc[i];
+  }
+  atomicMax(&c.cnt->max_bin, mx);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t pairs = sh[blockDim.x];
+    to[n] = pairs;
+    c.cnt->pair_count = pairs;
+    uint32_t recs = c.cnt->rec_count;
+    uint32_t bits = 0;
+    if (recs > seg.rec_cap) bits |= KZ_STATUS_RECORD_OVERFLOW;
+    if (pairs > seg.pair_cap) bits |= KZ_STATUS_PAIR_OVERFLOW;
+    atomicMax(&c.st->need_records, recs);
+    atomicMax(&c.st->need_pairs, pairs);
+    if (bits) mark_failed(c.st, bits, s);
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+/* ---------------- phase: bin ---------------- */
+
+__device__ void bin_record(const Ctx& c, uint32_t ri) {
+  const KzSegment& seg = *c.seg;
+  KzTriRecord r = reinterpret_cast<const KzTriRecord*>(seg.records)[ri];
+  int tx0, ty0, tx1, ty1;
+  tile_range(seg, r, tx0, ty0, tx1, ty1);
+  const uint32_t* to = reinterpret_cast<const uint32_t*>(seg.tile_offset);
+  uint32_t* cur = reinterpret_cast<uint32_t*>(seg.tile_cursor);
+  uint32_t* bins = reinterpret_cast<uint32_t*>(seg.bins);
+  if (tx0 == tx1 && ty0 == ty1) {
+    uint32_t t = ty0 * seg.tiles_x + tx0;
+    bins[to[t] + atomicAdd(&cur[t], 1u)] = ri;
+    return;
+  }
+  Edges e;
+  edges_of(r, e);
+  for (int ty = ty0; ty <= ty1; ty++)
+    for (int tx = tx0; tx <= tx1; tx++)
+      if (tile_overlaps(seg, e, tx, ty)) {
+        uint32_t t = ty * seg.tiles_x + tx;
+        bins[to[t] + atomicAdd(&cur[t], 1u)] = ri;
+      }
+}
+
+/* ---------------- phase: raster ---------------- */
+
+struct TileInfo {
+  int32_t x0, y0, x1, y1; /* inclusive pixel bounds of the tile inside the framebuffer and render area */
+  int32_t ox, oy;         /* tile origin */
+  uint32_t n, base;
+};
+
+__device__ __forceinline__ bool tile_info(const KzSegment& seg, uint32_t t, TileInfo& ti) {
+  int T = (int)seg.tile;
+  ti.ox = (int32_t)(t % seg.tiles_x) * T;
+  ti.oy = (int32_t)(t / seg.tiles_x) * T;
+  ti.x0 = max(ti.ox, seg.area[0]);
+  ti.y0 = max(ti.oy, seg.area[1]);
+  ti.x1 = min(ti.ox + T, min((int32_t)seg.width, seg.area[2])) - 1;
+  ti.y1 = min(ti.oy + T, min((int32_t)seg.height, seg.area[3])) - 1;
+  ti.n = reinterpret_cast<const uint32_t*>(seg.tile_count)[t];
+  ti.base = reinterpret_cast<const uint32_t*>(seg.tile_offset)[t];
+  return ti.x0 <= ti.x1 && ti.y0 <= ti.y1;
+}
+
+__device__ __forceinline__ uint32_t* color_px(const KzSegment& seg, int32_t x, int32_t y) {
+  return reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(seg.color) + (size_t)y * seg.color_pitch) + x;
+}
+__device__ __forceinline__ float* depth_px(const KzSegment& seg, int32_t x, int32_t y) {
+  return reinterpret_cast<float*>(reinterpret_cast<char*>(seg.depth) + (size_t)y * seg.depth_pitch) + x;
+}
+
+/* rasterise the part of one record inside the tile into the visibility keys */
+__device__ __forceinline__ uint32_t vis_record(const KzSegment& seg, const KzDraw* draws, const KzTriRecord& r,
+                                               const TileInfo& ti, unsigned long long* keys, int lane0, int step) {
+  int32_t bx0 = max((int32_t)(r.bb0 & 0xFFFFu), ti.x0), by0 = max((int32_t)(r.bb0 >> 16), ti.y0);
+  int32_t bx1 = min((int32_t)(r.bb1 & 0xFFFFu), ti.x1), by1 = min((int32_t)(r.bb1 >> 16), ti.y1);
+  if (bx0 > bx1 || by0 > by1) return 0;
+  const KzDraw& d = draws[r.draw];
+  float zmin = d.zmin, zmax = d.zmax;
+  Edges e;
+  edges_of(r, e);
+  int T = (int)seg.tile;
+  int w = bx1 - bx0 + 1;
+  int npx = w * (by1 - by0 + 1);
+  uint32_t frags = 0;
+  for (int i = lane0; i < npx; i += step) {
+    int32_t x = bx0 + i % w, y = by0 + i / w;
+    int64_t px = (int64_t)x * 256 + 128, py = (int64_t)y * 256 + 128;
+    int64_t E0 = edge_at(e, 0, px, py), E1 = edge_at(e, 1, px, py), E2 = edge_at(e, 2, px, py);
+    if (E0 < e.thr[0] || E1 < e.thr[1] || E2 < e.thr[2]) continue;
+    frags++;
+    float l1 = fmul(__ll2float_rn(E1), r.inv_s), l2 = fmul(__ll2float_rn(E2), r.inv_s);
+    float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
+    z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
+    unsigned long long k = vis_key(seg.vis_key, z, r.g);
+    unsigned long long* slot = &keys[(y - ti.oy) * T + (x - ti.ox)];
+    if (k < *slot) atomicMin(slot, k);
+  }
+  return frags;
+}
+
+__device__ void raster_tile_visibility(const Ctx& c, uint32_t t, unsigned char* smem) {
+  const KzSegment& seg = *c.seg;
+  TileInfo ti;
+  if (!tile_info(seg, t, ti)) return;
+  bool clear_c = seg.color_load == KZ_LOAD_CLEAR, clear_d = seg.depth_load == KZ_LOAD_CLEAR;
+  if (ti.n == 0 && !clear_c && !clear_d) return;
+  int T = (int)seg.tile;
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem);
+  uint32_t* qcount = reinterpret_cast<uint32_t*>(smem + (size_t)T * T * 8);
+  uint32_t* queue = qcount + 1;
+  const bool has_depth = seg.depth != 0;
+  for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
+    int32_t x = ti.ox + i % T, y = ti.oy + i / T;
+    float dv = 1.0f;
+    if (has_depth && x >= ti.x0 && x <= ti.x1 && y >= ti.y0 && y <= ti.y1)
+      dv = clear_d ? seg.clear_depth : *depth_px(seg, x, y);
+    keys[i] = vis_init(seg.vis_key, dv);
+  }
+  if (threadIdx.x == 0) *qcount = 0;
+  __syncthreads();
+  const KzTriRecord* recs = reinterpret_cast<const KzTriRecord*>(seg.records);
+  const uint32_t* bins = reinterpret_cast<const uint32_t*>(seg.bins) + ti.base;
+  uint32_t frags = 0;
+  for (uint32_t e = threadIdx.x; e < ti.n; e += blockDim.x) {
+    uint32_t ri = bins[e];
+    const KzTriRecord& r = recs[ri];
+    int32_t bx0 = max((int32_t)(r.bb0 & 0xFFFFu), ti.x0), by0 = max((int32_t)(r.bb0 >> 16), ti.y0);
+    int32_t bx1 = min((int32_t)(r.bb1 & 0xFFFFu), ti.x1), by1 = min((int32_t)(r.bb1 >> 16), ti.y1);
+    int area = (bx1 - bx0 + 1) * (by1 - by0 + 1);
+    if (area > 48) {
+      uint32_t q = atomicAdd(qcount, 1u);
+      if (q < 1024) {
+        queue[q] = ri;
+        continue;
+      }
+    }
+    KzTriRecord rr = r;
+    frags += vis_record(seg, c.draws, rr, ti, keys, 0, 1);
+  }
+  __syncthreads();
+  uint32_t nq = min(*qcount, 1024u);
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (uint32_t q = warp; q < nq; q += nwarps) {
+    KzTriRecord rr = recs[queue[q]];
+    frags += vis_record(seg, c.draws, rr, ti, keys, lane, 32);
+  }
+  __syncthreads();
+  if (frags) {
+    atomicAdd(&c.cnt->fragments, frags);
+    atomicAdd(&c.st->fragments_lo, frags);
+  }
+  /* resolve: one fragment-shader call per pixel whose key holds a primitive */
+  const bool has_color = seg.color != 0;
+  for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
+    int32_t x = ti.ox + i % T, y = ti.oy + i / T;
+    if (x < ti.x0 || x > ti.x1 || y < ti.y0 || y > ti.y1) continue;
+    uint32_t g;
+    float z;
+    bool frag = vis_decode(seg.vis_key, keys[i], g, z);
+    if (frag) {
+      Shade s;
+      if (shade_setup(c, g, x, y, 0, s)) {
+        int64_t E[3];
+        covers(s.r, x, y, E);
+        float col[4];
+        shade_pixel(c, s, x, y, E, z, col);
+        const KzPipe& p = c.pipes[s.pipe];
+        if (has_color) {
+          uint32_t dst = clear_c ? seg.clear_color : *color_px(seg, x, y);
+          uint32_t out = color_write(p, to_rgba(dst, seg.color_format), col);
+          *color_px(seg, x, y) = from_rgba(out, seg.color_format);
+        }
+        if (has_depth && p.depth_test && p.depth_write) *depth_px(seg, x, y) = z;
+        else if (has_depth && clear_d) *depth_px(seg, x, y) = seg.clear_depth;
+        continue;
+      }
+    }
+    if (has_color && clear_c) *color_px(seg, x, y) = seg.clear_color;
+    if (has_depth && clear_d) *depth_px(seg, x, y) = seg.clear_depth;
+  }
+}
+
+/* ordered mode: per-pixel in-order processing of the tile's bin, sorted by primitive */
+struct BatchEntry {
+  Shade s;
+  uint32_t valid;
+};
+
+__device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* smem, uint32_t s_index) {
+  const KzSegment& seg = *c.seg;
+  TileInfo ti;
+  if (!tile_info(seg, t, ti)) return;
+  bool clear_c = seg.color_load == KZ_LOAD_CLEAR, clear_d = seg.depth_load == KZ_LOAD_CLEAR;
+  if (ti.n == 0 && !clear_c && !clear_d) return;
+  if (ti.n > KZ_SORT_CAP) {
+    if (threadIdx.x == 0) atomicOr(&c.st->flags, KZ_STATUS_BIN_TOO_LARGE);
+    return;
+  }
+  int T = (int)seg.tile;
+  unsigned long long* sk = reinterpret_cast<unsigned long long*>(smem);
+  BatchEntry* batch = reinterpret_cast<BatchEntry*>(smem + KZ_SORT_CAP * 8);
+  const KzTriRecord* recs = reinterpret_cast<const KzTriRecord*>(seg.records);
+  const uint32_t* bins = reinterpret_cast<const uint32_t*>(seg.bins) + ti.base;
+  uint32_t m = 1;
+  while (m < ti.n) m <<= 1;
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+    if (i < ti.n) {
+      uint32_t ri = bins[i];
+      sk[i] = ((unsigned long long)recs[ri].g << 32) | ri;
+    } else {
+      sk[i] = ~0ull;
+    }
+  }
+  __syncthreads();
+  for (uint32_t k = 2; k <= m; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        uint32_t l = i ^ j;
+        if (l > i) {
+          unsigned long long a = sk[i], b = sk[l];
+          bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            sk[i] = b;
+            sk[l] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  /* per-thread pixels (T*T / blockDim.x of them, at most 16) */
+  const int per = (T * T + blockDim.x - 1) / blockDim.x;
+  uint32_t colv[16];
+  float depv[16];
+  const bool has_color = seg.color != 0, has_depth = seg.depth != 0;
+  for (int q = 0; q < per; q++) {
+    int i = threadIdx.x + q * blockDim.x;
+    int32_t x = ti.ox + i % T, y = ti.oy + i / T;
+    colv[q] = 0;
+    depv[q] = 1.0f;
+    if (i >= T * T || x < ti.x0 || x > ti.x1 || y < ti.y0 || y > ti.y1) continue;
+    if (has_color) colv[q] = to_rgba(clear_c ? seg.clear_color : *color_px(seg, x, y), seg.color_format);
+    if (has_depth) depv[q] = clear_d ? seg.clear_depth : *depth_px(seg, x, y);
+  }
+  uint32_t frags = 0;
+  for (uint32_t b0 = 0; b0 < ti.n; b0 += KZ_BATCH) {
+    uint32_t nb = min((uint32_t)KZ_BATCH, ti.n - b0);
+    __syncthreads();
+    if (threadIdx.x < nb) {
+      unsigned long long key = sk[b0 + threadIdx.x];
+      uint32_t ri = (uint32_t)key;
+      const KzTriRecord r = recs[ri];
+      BatchEntry& be = batch[threadIdx.x];
+      be.valid = shade_setup(c, r.g, 0, 0, (r.info >> 4) & 15u, be.s) ? 1u : 0u;
+    }
+    __syncthreads();
+    for (uint32_t j = 0; j < nb; j++) {
+      const BatchEntry& be = batch[j];
+      if (!be.valid) continue;
+      const KzTriRecord& r = be.s.r;
+      int32_t bx0 = (int32_t)(r.bb0 & 0xFFFFu), by0 = (int32_t)(r.bb0 >> 16);
+      int32_t bx1 = (int32_t)(r.bb1 & 0xFFFFu), by1 = (int32_t)(r.bb1 >> 16);
+      const KzPipe& p = c.pipes[be.s.pipe];
+      const KzDraw& d = c.draws[be.s.draw];
+      for (int q = 0; q < per; q++) {
+        int i = threadIdx.x + q * blockDim.x;
+        if (i >= T * T) break;
+        int32_t x = ti.ox + i % T, y = ti.oy + i / T;
+        if (x < bx0 || x > bx1 || y < by0 || y > by1) continue;
+        if (x < ti.x0 || x > ti.x1 || y < ti.y0 || y > ti.y1) continue;
+        int64_t E[3];
+        if (!covers(r, x, y, E)) continue;
+        frags++;
+        float l1 = fmul(__ll2float_rn(E[1]), r.inv_s), l2 = fmul(__ll2float_rn(E[2]), r.inv_s);
+        float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
+        z = fadd(fminf(fmaxf(z, d.zmin), d.zmax), 0.0f);
+        float col[4];
+        uint32_t discard = shade_pixel(c, be.s, x, y, E, z, col);
+        if (discard) continue;
+        if (p.depth_test && has_depth) {
+          if (!depth_cmp(p.depth_compare, z, depv[q])) continue;
+          if (p.depth_write) depv[q] = z;
+        }
+        if (has_color) colv[q] = color_write(p, colv[q], col);
+      }
+    }
+  }
+  if (frags) {
+    atomicAdd(&c.cnt->fragments, frags);
+    atomicAdd(&c.st->fragments_lo, frags);
+  }
+  for (int q = 0; q < per; q++) {
+    int i = threadIdx.x + q * blockDim.x;
+    if (i >= T * T) break;
+    int32_t x = ti.ox + i % T, y = ti.oy + i / T;
+    if (x < ti.x0 || x > ti.x1 || y < ti.y0 || y > ti.y1) continue;
+    if (has_color) *color_px(seg, x, y) = from_rgba(colv[q], seg.color_format);
+    if (has_depth) *depth_px(seg, x, y) = depv[q];
+  }
+  (void)s_index;
+}
+
+__device__ void raster_tile(const Ctx& c, uint32_t t, unsigned char* smem, uint32_t s) {
+  if (c.seg->mode == KZ_MODE_VISIBILITY) raster_tile_visibility(c, t, smem);
+  else raster_tile_ordered(c, t, smem, s);
+  __syncthreads();
+  /* leave the tile counts at zero for the next segment */
+  if (threadIdx.x == 0) reinterpret_cast<uint32_t*>(c.seg->tile_count)[t] = 0;
+}
+
+/* ---------------- grid barrier (persistent kernel) ---------------- */
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+/* Every block arrives once per call.  Gives up after KZ_BARRIER_NS and flags KZ_STATUS_BARRIER_TIMEOUT
+ * so that all blocks leave the kernel instead of spinning. */
+__device__ bool grid_barrier(KzStatus* st) {
+  __syncthreads();
+  __shared__ uint32_t ok;
+  if (threadIdx.x == 0) {
+    volatile uint32_t* genp = &st->barrier_gen;
+    uint32_t gen = *genp;
+    __threadfence();
+    uint32_t arrived = atomicAdd(&st->barrier_arrive, 1u) + 1u;
+    ok = 1;
+    if (arrived == gridDim.x) {
+      atomicExch(&st->barrier_arrive, 0u);
+      __threadfence();
+      atomicAdd(&st->barrier_gen, 1u);
+    } else {
+      unsigned long long t0 = globaltimer();
+      while (*genp == gen) {
+        if (status_flags(st) & KZ_STATUS_BARRIER_TIMEOUT) {
+          ok = 0;
+          break;
+        }
+        if (globaltimer() - t0 > KZ_BARRIER_NS) {
+          atomicOr(&st->flags, KZ_STATUS_BARRIER_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(200);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint32_t grab(uint32_t* counter, uint32_t* sh) {
+  __syncthreads();
+  if (threadIdx.x == 0) *sh = atomicAdd(counter, 1u);
+  __syncthreads();
+  return *sh;
+}
+
+}  // namespace
+
+/* ================= kernels ================= */
+
+extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_geometry(KzFrame f, uint32_t s) {
+  Ctx c = make_ctx(f, s);
+  if (segment_blocked(c, s)) return;
+  if (blockIdx.x < c.seg->num_chunks) geometry_chunk(c, c.seg->first_chunk + blockIdx.x);
+}
+
+extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_scan(KzFrame f, uint32_t s) {
+  __shared__ uint32_t sh[KZ_THREADS + 1];
+  Ctx c = make_ctx(f, s);
+  if (segment_blocked(c, s)) return;
+  scan_tiles(c, s, sh);
+}
+
+extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_bin(KzFrame f, uint32_t s) {
+  Ctx c = make_ctx(f, s);
+  if (segment_blocked(c, s)) return;
+  uint32_t n = min(c.cnt->rec_count, c.seg->rec_cap);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) bin_record(c, i);
+}
+
+extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_raster(KzFrame f, uint32_t s) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Ctx c = make_ctx(f, s);
+  if (segment_blocked(c, s)) return;
+  uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) raster_tile(c, t, smem, s);
+}
+
+/* the whole command buffer in one cooperative launch: phases separated by bounded grid barriers,
+ * work stolen from per-segment counters */
+extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_persistent(KzFrame f) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t item;
+  __shared__ uint32_t scan_sh[KZ_THREADS + 1];
+  KzStatus* st = reinterpret_cast<KzStatus*>(f.status);
+  for (uint32_t s = f.first_segment; s < f.num_segments; s++) {
+    Ctx c = make_ctx(f, s);
+    if (segment_blocked(c, s)) break;
+    for (;;) {
+      uint32_t k = grab(&c.cnt->geom_next, &item);
+      if (k >= c.seg->num_chunks) break;
+      geometry_chunk(c, c.seg->first_chunk + k);
+    }
+    if (!grid_barrier(st)) return;
+    if (blockIdx.x == 0) scan_tiles(c, s, scan_sh);
+    if (!grid_barrier(st)) return;
+    if (segment_blocked(c, s)) break;
+    uint32_t n = min(c.cnt->rec_count, c.seg->rec_cap);
+    for (;;) {
+      uint32_t k = grab(&c.cnt->bin_next, &item);
+      uint32_t i = k * blockDim.x + threadIdx.x;
+      if (k * blockDim.x >= n) break;
+      if (i < n) bin_record(c, i);
+    }
+    if (!grid_barrier(st)) return;
+    uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
+    for (;;) {
+      uint32_t t = grab(&c.cnt->tile_next, &item);
+      if (t >= ntiles) break;
+      raster_tile(c, t, smem, s);
+    }
+    if (!grid_barrier(st)) return;
+  }
+}
+
+/* vkCmdClearColorImage / vkCmdClearDepthStencilImage / render-pass clears outside the raster:
+ * fill rows [y0, y1) x [x0, x1) of a 4-byte-per-pixel image with `value` (16-byte stores where the
+ * row segment is aligned) */
+extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_clear(uint64_t base, uint32_t pitch, int32_t x0,
+                                                                    int32_t y0, int32_t x1, int32_t y1,
+                                                                    uint32_t value) {
+  int32_t w = x1 - x0, h = y1 - y0;
+  if (w <= 0 || h <= 0) return;
+  int32_t lead = (int32_t)((4 - (x0 & 3)) & 3);
+  if (lead > w) lead = w;
+  int32_t body = (w - lead) / 4;
+  int32_t tail = w - lead - body * 4;
+  int32_t per_row = lead + body + tail;
+  long long total = (long long)per_row * h;
+  uint4 v4 = make_uint4(value, value, value, value);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    int32_t y = y0 + (int32_t)(i / per_row);
+    int32_t k = (int32_t)(i % per_row);
+    uint32_t* row = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(base) + (size_t)y * pitch);
+    if (k < lead) {
+      row[x0 + k] = value;
+    } else if (k < lead + body) {
+      int32_t x = x0 + lead + (k - lead) * 4;
+      if ((reinterpret_cast<uintptr_t>(row + x) & 15u) == 0) {
+        *reinterpret_cast<uint4*>(row + x) = v4;
+      } else {
+        row[x] = value; row[x + 1] = value; row[x + 2] = value; row[x + 3] = value;
+      }
+    } else {
+      row[x0 + lead + body * 4 + (k - lead - body)] = value;
+    }
+  }
+}

@@ -1,0 +1,300 @@
+/*
+ * kz_ptx_backend.cpp - shader-compiler-backend-ptx: IR -> PTX device functions -> JIT link.
+ *
+ * Takes the place of the reference's LLVM 7 backend (shader-compiler-backend-llvm-7, LLVM7Compiler::run
+ * at backend.rs:553-690), which JIT-compiles for the host CPU.  Here a pipeline set (the pipelines one
+ * command buffer uses) becomes one PTX module that defines the three functions the pipeline kernels
+ * call (kz_raster_abi.h):
+ *
+ *   .func kz_vs(pipe, KzVsIn* in, push, KzVsOut* out)                 full vertex shader
+ *   .func kz_vs_pos(pipe, KzVsIn* in, push, float* pos)                only gl_Position (dead outputs
+ *                                                                       dropped, ptxas removes their math)
+ *   .func (.b32 discard) kz_fs(pipe, KzFsIn* in, push, float* color)   fragment shader
+ *
+ * Each function branches on `pipe` to the inlined body of that pipeline.  nvJitLink then links the
+ * module with the relocatable sm_103a object holding the kernels (kz_pipeline.cu) into one cubin; the
+ * result plays the role of the reference's `CompiledCode` (shader-compiler-backend/src/lib.rs:200-205),
+ * with kernels looked up by name instead of host function pointers.
+ *
+ * Rounding is explicit in every instruction (add.rn, mul.rn, fma.rn, div.rn, sqrt.rn, cvt.rn...), so
+ * ptxas never contracts or approximates the IEEE operations the CPU oracle restates.  Only the GLSL
+ * transcendental functions (sin, cos, exp2, log2, pow) use the approximate hardware instructions.
+ */
+#include <nvJitLink.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kz_ir.h"
+#include "kz_shader_backend_impl.h"
+
+namespace kz {
+namespace ptx {
+
+using ir::Function;
+using ir::Inst;
+using ir::Op;
+using ir::Ty;
+
+namespace {
+
+struct RegMap {
+  std::vector<std::string> names;
+};
+
+const char* cmp_name(uint32_t c) {
+  static const char* ord[] = {"eq", "ne", "lt", "le", "gt", "ge"};
+  static const char* unord[] = {"equ", "neu", "ltu", "leu", "gtu", "geu"};
+  uint32_t k = c & 7u;
+  if (k > 5) k = 0;
+  return (c & ir::CmpUnordered) ? unord[k] : ord[k];
+}
+
+enum class Kind { VertexFull, VertexPos, Fragment };
+
+class Emitter {
+ public:
+  std::string out;
+  uint32_t nf = 0, nr = 0, np = 0;
+
+  void line(const std::string& s) { out += "  " + s + "\n"; }
+
+  /* body of one pipeline stage; registers numbered from the running counters */
+  void body(const Function& fn, const std::string& pfx, Kind kind) {
+    std::vector<std::string> name(fn.regs.size());
+    for (size_t i = 0; i < fn.regs.size(); i++) {
+      switch (fn.regs[i]) {
+        case Ty::F32: name[i] = "%f" + std::to_string(nf++); break;
+        case Ty::B32: name[i] = "%r" + std::to_string(nr++); break;
+        case Ty::Pred: name[i] = "%p" + std::to_string(np++); break;
+      }
+    }
+    auto R = [&](int32_t r) { return name[(size_t)r]; };
+    auto L = [&](uint32_t l) { return "$" + pfx + "_L" + std::to_string(l); };
+    char buf[160];
+    for (const Inst& i : fn.code) {
+      switch (i.op) {
+        case Op::Const:
+          if (i.ty == Ty::F32) {
+            std::snprintf(buf, sizeof buf, "mov.f32 %s, 0f%08X;", R(i.dst).c_str(), i.imm);
+            line(buf);
+          } else if (i.ty == Ty::B32) {
+            std::snprintf(buf, sizeof buf, "mov.b32 %s, %u;", R(i.dst).c_str(), i.imm);
+            line(buf);
+          } else {
+            std::snprintf(buf, sizeof buf, "mov.b32 %%kzt, %u;", i.imm ? 1u : 0u);
+            line(buf);
+            line("setp.ne.u32 " + R(i.dst) + ", %kzt, 0;");
+          }
+          break;
+        case Op::Mov: {
+          Ty st = fn.regs[(size_t)i.a];
+          if (i.ty == Ty::Pred && st == Ty::Pred) line("mov.pred " + R(i.dst) + ", " + R(i.a) + ";");
+          else if (i.ty == Ty::F32 && st == Ty::F32) line("mov.f32 " + R(i.dst) + ", " + R(i.a) + ";");
+          else if (i.ty == Ty::Pred) line("setp.ne.u32 " + R(i.dst) + ", " + R(i.a) + ", 0;");
+          else if (st == Ty::Pred) line("selp.u32 " + R(i.dst) + ", 1, 0, " + R(i.a) + ";");
+          else line("mov.b32 " + R(i.dst) + ", " + R(i.a) + ";");
+          break;
+        }
+        case Op::LdIn:
+          std::snprintf(buf, sizeof buf, "ld.%s %s, [%%kzin+%u];", i.ty == Ty::F32 ? "f32" : "u32", R(i.dst).c_str(),
+                        i.imm);
+          line(buf);
+          break;
+        case Op::LdPush:
+          std::snprintf(buf, sizeof buf, "ld.global.nc.%s %s, [%%kzpush+%u];", i.ty == Ty::F32 ? "f32" : "u32",
+                        R(i.dst).c_str(), i.imm);
+          line(buf);
+          break;
+        case Op::StOut: {
+          if (kind == Kind::VertexPos && i.imm >= 16) break;
+          std::string v = R(i.a);
+          if (fn.regs[(size_t)i.a] == Ty::Pred) {
+            line("selp.u32 %kzt, 1, 0, " + v + ";");
+            v = "%kzt";
+          }
+          std::snprintf(buf, sizeof buf, "st.%s [%%kzout+%u], %s;",
+                        fn.regs[(size_t)i.a] == Ty::F32 ? "f32" : "u32", i.imm, v.c_str());
+          line(buf);
+          break;
+        }
+        case Op::FAdd: line("add.rn.f32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::FSub: line("sub.rn.f32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::FMul: line("mul.rn.f32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::FDiv: line("div.rn.f32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::FFma: line("fma.rn.f32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ", " + R(i.c) + ";"); break;
+        case Op::FMin: line("min.f32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::FMax: line("max.f32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::FNeg: line("neg.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::FAbs: line("abs.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::FSqrt: line("sqrt.rn.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::FFloor: line("cvt.rmi.f32.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::FCeil: line("cvt.rpi.f32.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::FTrunc: line("cvt.rzi.f32.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::FRoundEven: line("cvt.rni.f32.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::FSin: line("sin.approx.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::FCos: line("cos.approx.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::FEx2: line("ex2.approx.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::FLg2: line("lg2.approx.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::IAdd: line("add.s32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::ISub: line("sub.s32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::IMul: line("mul.lo.s32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::UDiv: line("div.u32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::SDiv: line("div.s32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::URem: line("rem.u32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::SRem: line("rem.s32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::And: line("and.b32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::Or: line("or.b32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::Xor: line("xor.b32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::Not: line("not.b32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::Shl: line("shl.b32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::Shr: line("shr.u32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::Sar: line("shr.s32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::INeg: line("neg.s32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::CvtF2S: line("cvt.rzi.s32.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::CvtF2U: line("cvt.rzi.u32.f32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::CvtS2F: line("cvt.rn.f32.s32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::CvtU2F: line("cvt.rn.f32.u32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::SetpF:
+          line(std::string("setp.") + cmp_name(i.imm) + ".f32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";");
+          break;
+        case Op::SetpS:
+          line(std::string("setp.") + cmp_name(i.imm & 7u) + ".s32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";");
+          break;
+        case Op::SetpU:
+          line(std::string("setp.") + cmp_name(i.imm & 7u) + ".u32 " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";");
+          break;
+        case Op::Selp:
+          line(std::string(i.ty == Ty::F32 ? "selp.f32 " : "selp.b32 ") + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) +
+               ", " + R(i.c) + ";");
+          break;
+        case Op::PAnd: line("and.pred " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::POr: line("or.pred " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::PXor: line("xor.pred " + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ";"); break;
+        case Op::PNot: line("not.pred " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::PToB32: line("selp.u32 " + R(i.dst) + ", 1, 0, " + R(i.a) + ";"); break;
+        case Op::B32ToP: line("setp.ne.u32 " + R(i.dst) + ", " + R(i.a) + ", 0;"); break;
+        case Op::Label: out += L(i.imm) + ":\n"; break;
+        case Op::Bra: line("bra " + L(i.imm) + ";"); break;
+        case Op::BraIf: line("@" + R(i.a) + " bra " + L(i.imm) + ";"); break;
+        case Op::Ret:
+          if (kind == Kind::Fragment) {
+            line("mov.b32 %kzt, 0;");
+            line("st.param.b32 [func_retval0], %kzt;");
+          }
+          line("ret;");
+          break;
+        case Op::Kill:
+          if (kind == Kind::Fragment) {
+            line("mov.b32 %kzt, 1;");
+            line("st.param.b32 [func_retval0], %kzt;");
+          }
+          line("ret;");
+          break;
+      }
+    }
+    /* a body always ends in Ret; keep a fallback for malformed input */
+    if (kind == Kind::Fragment) {
+      line("mov.b32 %kzt, 0;");
+      line("st.param.b32 [func_retval0], %kzt;");
+    }
+    line("ret;");
+  }
+};
+
+std::string function_text(const char* fname, Kind kind, const std::vector<const ir::Shader*>& stages) {
+  Emitter e;
+  std::string bodies;
+  for (size_t p = 0; p < stages.size(); p++) {
+    e.out.clear();
+    std::string pfx = std::string(fname) + "_p" + std::to_string(p);
+    e.out += "$" + pfx + ":\n";
+    if (stages[p]) {
+      e.body(stages[p]->fn, pfx, kind);
+    } else {
+      if (kind == Kind::Fragment) {
+        e.line("mov.b32 %kzt, 0;");
+        e.line("st.param.b32 [func_retval0], %kzt;");
+      }
+      e.line("ret;");
+    }
+    bodies += e.out;
+  }
+  std::string s;
+  char buf[256];
+  if (kind == Kind::Fragment)
+    std::snprintf(buf, sizeof buf, ".visible .func (.param .b32 func_retval0) %s(", fname);
+  else
+    std::snprintf(buf, sizeof buf, ".visible .func %s(", fname);
+  s += buf;
+  std::snprintf(buf, sizeof buf,
+                "\n  .param .b32 %s_pipe,\n  .param .b64 %s_in,\n  .param .b64 %s_push,\n  .param .b64 %s_out\n)\n{\n",
+                fname, fname, fname, fname);
+  s += buf;
+  s += "  .reg .b32 %kzsel, %kzt;\n  .reg .b64 %kzin, %kzpush, %kzout;\n  .reg .pred %kzp;\n";
+  if (e.nf) s += "  .reg .f32 %f<" + std::to_string(e.nf) + ">;\n";
+  if (e.nr) s += "  .reg .b32 %r<" + std::to_string(e.nr) + ">;\n";
+  if (e.np) s += "  .reg .pred %p<" + std::to_string(e.np) + ">;\n";
+  std::snprintf(buf, sizeof buf,
+                "  ld.param.u32 %%kzsel, [%s_pipe];\n  ld.param.u64 %%kzin, [%s_in];\n  ld.param.u64 %%kzpush, [%s_push];\n"
+                "  cvta.to.global.u64 %%kzpush, %%kzpush;\n  ld.param.u64 %%kzout, [%s_out];\n",
+                fname, fname, fname, fname);
+  s += buf;
+  for (size_t p = 0; p + 1 < stages.size(); p++) {
+    std::snprintf(buf, sizeof buf, "  setp.eq.u32 %%kzp, %%kzsel, %zu;\n  @%%kzp bra $%s_p%zu;\n", p, fname, p);
+    s += buf;
+  }
+  std::snprintf(buf, sizeof buf, "  bra $%s_p%zu;\n", fname, stages.empty() ? (size_t)0 : stages.size() - 1);
+  s += buf;
+  if (stages.empty()) {
+    s += "$" + std::string(fname) + "_p0:\n";
+    if (kind == Kind::Fragment) s += "  mov.b32 %kzt, 0;\n  st.param.b32 [func_retval0], %kzt;\n";
+    s += "  ret;\n";
+  }
+  s += bodies;
+  s += "}\n\n";
+  return s;
+}
+
+}  // namespace
+
+std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vector<const ir::Shader*>& fs) {
+  std::string s = ".version 9.0\n.target sm_103a\n.address_size 64\n\n";
+  s += function_text("kz_vs", Kind::VertexFull, vs);
+  s += function_text("kz_vs_pos", Kind::VertexPos, vs);
+  s += function_text("kz_fs", Kind::Fragment, fs);
+  return s;
+}
+
+std::string link(const std::string& ptx, const void* object, size_t object_size, std::vector<char>& cubin) {
+  nvJitLinkHandle h = nullptr;
+  const char* opts[] = {"-arch=sm_103a", "-O3"};
+  std::string err;
+  if (nvJitLinkCreate(&h, 2, opts) != NVJITLINK_SUCCESS) return "nvJitLinkCreate failed";
+  auto log = [&](const char* what) {
+    size_t n = 0;
+    nvJitLinkGetErrorLogSize(h, &n);
+    std::string l(n + 1, '\0');
+    if (n) nvJitLinkGetErrorLog(h, &l[0]);
+    return std::string(what) + ": " + l.c_str();
+  };
+  if (nvJitLinkAddData(h, NVJITLINK_INPUT_CUBIN, object, object_size, "kz_pipeline") != NVJITLINK_SUCCESS) {
+    err = log("adding the pipeline kernels");
+  } else if (nvJitLinkAddData(h, NVJITLINK_INPUT_PTX, ptx.c_str(), ptx.size() + 1, "kz_shaders") != NVJITLINK_SUCCESS) {
+    err = log("adding the shader PTX");
+  } else if (nvJitLinkComplete(h) != NVJITLINK_SUCCESS) {
+    err = log("linking");
+  } else {
+    size_t n = 0;
+    nvJitLinkGetLinkedCubinSize(h, &n);
+    cubin.resize(n);
+    if (nvJitLinkGetLinkedCubin(h, cubin.data()) != NVJITLINK_SUCCESS) err = "fetching the linked cubin failed";
+  }
+  nvJitLinkDestroy(&h);
+  return err;
+}
+
+}  // namespace ptx
+}  // namespace kz

@@ -1,0 +1,25 @@
+/*
+ * kz_shader_backend_impl.h - internal C++ interface of the PTX shader backend (see kz_ptx_backend.cpp).
+ */
+#ifndef KZ_SHADER_BACKEND_IMPL_H
+#define KZ_SHADER_BACKEND_IMPL_H
+
+#include <string>
+#include <vector>
+
+#include "kz_ir.h"
+
+namespace kz {
+namespace ptx {
+
+/* PTX module defining kz_vs / kz_vs_pos / kz_fs for a pipeline set (entry p = pipeline index p;
+ * a null fragment stage yields a fragment function that writes nothing) */
+std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vector<const ir::Shader*>& fs);
+
+/* nvJitLink the relocatable pipeline-kernel object with the shader PTX; returns "" on success */
+std::string link(const std::string& ptx, const void* object, size_t object_size, std::vector<char>& cubin);
+
+}  // namespace ptx
+}  // namespace kz
+
+#endif

@@ -1,0 +1,1504 @@
+/*
+ * kz_spirv_to_ir.cpp - SPIR-V vertex/fragment entry point -> scalar register IR.
+ *
+ * Role of the reference's shader-compiler-translate-spirv-to-ir (TranslatedSPIRVShader::new,
+ * shader-compiler-translate-spirv-to-ir/src/lib.rs:191-214), which today translates only an empty
+ * main (OpLoad/OpStore/OpAccessChain are `todo!()` at parse/memory_instructions.rs:99,124,141 and the
+ * arithmetic opcodes are unimplemented, parse/unimplemented_instructions.rs).  This translator covers
+ * the opcodes vertex and fragment shaders of the draw path use: typed constants and specialisation
+ * constants, interface variables (Location, Component, BuiltIn, Flat, NoPerspective), push-constant
+ * blocks (Offset, MatrixStride, ArrayStride, RowMajor), function/private variables, composites,
+ * float/int/bool arithmetic, matrix products, GLSL.std.450, and unstructured control flow with OpPhi.
+ * Interface variables are laid out in 16-byte locations as the reference's io_layout does
+ * (shader-compiler-translate-spirv-to-ir/src/io_layout.rs:6-13).
+ *
+ * Fixed evaluation order (the CPU oracle restates the same):
+ *   OpDot(a, b)               t = a0*b0; t = fma(ak, bk, t) for k = 1..n-1
+ *   OpMatrixTimesVector(M, v) r_i = M[0][i]*v0, then fma(M[c][i], vc, r_i) for c = 1..C-1
+ *   Normalize(x)              x * (1 / sqrt(dot(x, x)))   (sqrt and divide correctly rounded)
+ *   Length(x)                 sqrt(dot(x, x))
+ *   FMix(x, y, a)             fma(a, y - x, x)
+ */
+#include <cstring>
+#include <map>
+#include <unordered_map>
+
+#include "kz_ir.h"
+#include "kz_spirv.h"
+
+namespace kz {
+namespace ir {
+
+using namespace spv;
+
+namespace {
+
+struct TypeInfo {
+  enum Kind { Void, Bool, Int, Float, Vector, Matrix, Array, RuntimeArray, Struct, Pointer, Function, Other } kind =
+      Other;
+  uint32_t width = 32;
+  bool is_signed = false;
+  uint32_t elem = 0;
+  uint32_t count = 0;
+  uint32_t storage = 0;
+  std::vector<uint32_t> members;
+};
+
+struct DecSet {
+  std::vector<std::pair<uint32_t, std::vector<uint32_t>>> list;
+  bool has(uint32_t d) const {
+    for (auto& e : list)
+      if (e.first == d) return true;
+    return false;
+  }
+  bool get(uint32_t d, uint32_t& v) const {
+    for (auto& e : list)
+      if (e.first == d) {
+        v = e.second.empty() ? 0 : e.second[0];
+        return true;
+      }
+    return false;
+  }
+};
+
+/* per-scalar address of a variable */
+enum class Space : uint8_t { None, In, Out, Push, Reg };
+struct Slot {
+  Space space = Space::None;
+  uint32_t offset = 0;  /* byte offset for In/Out/Push */
+  int32_t reg = -1;     /* shadow register for Out/Reg */
+  bool is_bool_in = false;
+};
+
+struct Var {
+  uint32_t storage = 0;
+  uint32_t type = 0; /* pointee type */
+  std::vector<Slot> slots;
+};
+
+struct Place {
+  uint32_t var = 0;
+  uint32_t type = 0;
+  uint32_t first = 0;
+  uint32_t push_byte = 0; /* unused: push slots carry their own offsets */
+};
+
+struct Val {
+  uint32_t type = 0;
+  std::vector<int32_t> regs;
+};
+
+struct PhiInfo {
+  uint32_t result;
+  uint32_t type;
+  std::vector<std::pair<uint32_t, uint32_t>> incoming; /* (value id, parent label) */
+};
+
+class Translator {
+ public:
+  Translator(const Module& m, Stage stage, const char* entry, const std::vector<std::pair<uint32_t, uint32_t>>& spec,
+             Shader& out)
+      : m_(m), stage_(stage), entry_name_(entry), spec_(spec), out_(out), fn_(out.fn) {}
+
+  std::string run();
+
+ private:
+  const Module& m_;
+  Stage stage_;
+  std::string entry_name_;
+  const std::vector<std::pair<uint32_t, uint32_t>>& spec_;
+  Shader& out_;
+  Function& fn_;
+  std::string err_;
+
+  std::unordered_map<uint32_t, TypeInfo> types_;
+  std::unordered_map<uint32_t, DecSet> decs_;
+  std::map<std::pair<uint32_t, uint32_t>, DecSet> member_decs_;
+  std::unordered_map<uint32_t, std::pair<uint32_t, std::vector<uint32_t>>> consts_; /* id -> (type, bits) */
+  std::unordered_map<uint32_t, Var> vars_;
+  std::unordered_map<uint32_t, Place> places_;
+  std::unordered_map<uint32_t, Val> vals_;
+  std::unordered_map<uint32_t, std::string> ext_sets_;
+  std::unordered_map<uint32_t, uint32_t> labels_; /* SPIR-V label id -> IR label */
+  std::unordered_map<uint32_t, std::vector<PhiInfo>> phis_;
+  uint32_t entry_id_ = 0;
+  std::vector<uint32_t> interface_ids_;
+  uint32_t cur_block_ = 0;
+
+  bool fail(const std::string& s) {
+    if (err_.empty()) err_ = s;
+    return false;
+  }
+
+  /* ---- types ---- */
+  const TypeInfo& ty(uint32_t id) {
+    static TypeInfo none;
+    auto it = types_.find(id);
+    return it == types_.end() ? none : it->second;
+  }
+  uint32_t scalars(uint32_t t) {
+    const TypeInfo& ti = ty(t);
+    switch (ti.kind) {
+      case TypeInfo::Bool:
+      case TypeInfo::Int:
+      case TypeInfo::Float: return 1;
+      case TypeInfo::Vector: return ti.count;
+      case TypeInfo::Matrix: return ti.count * scalars(ti.elem);
+      case TypeInfo::Array: return ti.count * scalars(ti.elem);
+      case TypeInfo::Struct: {
+        uint32_t n = 0;
+        for (uint32_t mbr : ti.members) n += scalars(mbr);
+        return n;
+      }
+      default: return 0;
+    }
+  }
+  void flat_types(uint32_t t, std::vector<Ty>& outv) {
+    const TypeInfo& ti = ty(t);
+    switch (ti.kind) {
+      case TypeInfo::Bool: outv.push_back(Ty::Pred); break;
+      case TypeInfo::Int: outv.push_back(Ty::B32); break;
+      case TypeInfo::Float: outv.push_back(Ty::F32); break;
+      case TypeInfo::Vector:
+      case TypeInfo::Matrix:
+      case TypeInfo::Array:
+        for (uint32_t i = 0; i < ti.count; i++) flat_types(ti.elem, outv);
+        break;
+      case TypeInfo::Struct:
+        for (uint32_t mbr : ti.members) flat_types(mbr, outv);
+        break;
+      default: break;
+    }
+  }
+  /* scalar offset and type of member `idx` inside composite type t */
+  bool member(uint32_t t, uint32_t idx, uint32_t& off, uint32_t& mt) {
+    const TypeInfo& ti = ty(t);
+    switch (ti.kind) {
+      case TypeInfo::Vector:
+      case TypeInfo::Matrix:
+      case TypeInfo::Array:
+        if (ti.count && idx >= ti.count) return fail("composite index out of range");
+        mt = ti.elem;
+        off = idx * scalars(ti.elem);
+        return true;
+      case TypeInfo::Struct: {
+        if (idx >= ti.members.size()) return fail("struct member index out of range");
+        off = 0;
+        for (uint32_t i = 0; i < idx; i++) off += scalars(ti.members[i]);
+        mt = ti.members[idx];
+        return true;
+      }
+      default: return fail("index into a non-composite type");
+    }
+  }
+  bool is_float(uint32_t t) {
+    const TypeInfo& ti = ty(t);
+    if (ti.kind == TypeInfo::Float) return true;
+    if (ti.kind == TypeInfo::Vector || ti.kind == TypeInfo::Matrix) return is_float(ti.elem);
+    return false;
+  }
+  bool is_signed_int(uint32_t t) {
+    const TypeInfo& ti = ty(t);
+    if (ti.kind == TypeInfo::Int) return ti.is_signed;
+    if (ti.kind == TypeInfo::Vector) return is_signed_int(ti.elem);
+    return false;
+  }
+
+  /* ---- emission helpers ---- */
+  int32_t konst(Ty t, uint32_t bits) {
+    int32_t r = fn_.reg(t);
+    Inst i;
+    i.op = Op::Const;
+    i.ty = t;
+    i.dst = r;
+    i.imm = bits;
+    fn_.emit(i);
+    return r;
+  }
+  int32_t op1(Op op, Ty t, int32_t a) {
+    int32_t r = fn_.reg(t);
+    Inst i;
+    i.op = op;
+    i.ty = t;
+    i.dst = r;
+    i.a = a;
+    fn_.emit(i);
+    return r;
+  }
+  int32_t op2(Op op, Ty t, int32_t a, int32_t b, uint32_t imm = 0) {
+    int32_t r = fn_.reg(t);
+    Inst i;
+    i.op = op;
+    i.ty = t;
+    i.dst = r;
+    i.a = a;
+    i.b = b;
+    i.imm = imm;
+    fn_.emit(i);
+    return r;
+  }
+  int32_t op3(Op op, Ty t, int32_t a, int32_t b, int32_t c) {
+    int32_t r = fn_.reg(t);
+    Inst i;
+    i.op = op;
+    i.ty = t;
+    i.dst = r;
+    i.a = a;
+    i.b = b;
+    i.c = c;
+    fn_.emit(i);
+    return r;
+  }
+  void mov(Ty t, int32_t dst, int32_t a) {
+    Inst i;
+    i.op = Op::Mov;
+    i.ty = t;
+    i.dst = dst;
+    i.a = a;
+    fn_.emit(i);
+  }
+  void label(uint32_t l) {
+    Inst i;
+    i.op = Op::Label;
+    i.imm = l;
+    fn_.emit(i);
+  }
+  void bra(uint32_t l) {
+    Inst i;
+    i.op = Op::Bra;
+    i.imm = l;
+    fn_.emit(i);
+  }
+  void bra_if(int32_t p, uint32_t l) {
+    Inst i;
+    i.op = Op::BraIf;
+    i.ty = Ty::Pred;
+    i.a = p;
+    i.imm = l;
+    fn_.emit(i);
+  }
+  Ty reg_ty(int32_t r) { return fn_.regs[(size_t)r]; }
+
+  Val* val(uint32_t id) {
+    auto it = vals_.find(id);
+    if (it == vals_.end()) {
+      fail("use of an undefined value %" + std::to_string(id));
+      return nullptr;
+    }
+    return &it->second;
+  }
+  uint32_t label_of(uint32_t id) {
+    auto it = labels_.find(id);
+    if (it != labels_.end()) return it->second;
+    uint32_t l = fn_.label();
+    labels_[id] = l;
+    return l;
+  }
+
+  /* ---- module scan ---- */
+  bool scan_module();
+  bool eval_spec_op(const Insn& in);
+  bool layout_interface(uint32_t var_id, Var& v);
+  void assign_io(uint32_t t, const DecSet* d, uint32_t struct_type, uint32_t member_idx, uint32_t& location,
+                 std::vector<Slot>& slots, bool is_input);
+  void assign_push(uint32_t t, uint32_t byte, std::vector<Slot>& slots, uint32_t stride_hint, bool row_major);
+
+  /* ---- function body ---- */
+  bool translate_entry();
+  bool do_insn(const Insn& in);
+  bool branch_to(uint32_t target);
+  bool load(const Place& p, Val& v);
+  bool store(const Place& p, const Val& v);
+  bool ext_inst(const Insn& in);
+  void finish_outputs();
+  int32_t dot(const std::vector<int32_t>& a, const std::vector<int32_t>& b, size_t n);
+};
+
+bool Translator::scan_module() {
+  for (const Insn& in : m_.insns) {
+    const auto& o = in.ops;
+    switch (in.opcode) {
+      case OpCapability: {
+        uint32_t c = o.empty() ? 0 : o[0];
+        if (c != 0 && c != 1 && c != 11 && c != 32 && c != 33) {
+          /* Matrix, Shader, Int64 (decode only), ClipDistance, CullDistance */
+        }
+        break;
+      }
+      case OpExtInstImport: {
+        size_t i = 1;
+        ext_sets_[o[0]] = read_string(o, i);
+        break;
+      }
+      case OpEntryPoint: {
+        size_t i = 2;
+        std::string name = read_string(o, i);
+        uint32_t model = o[0];
+        bool want = (stage_ == Stage::Vertex && model == EMVertex) || (stage_ == Stage::Fragment && model == EMFragment);
+        if (want && name == entry_name_) {
+          entry_id_ = o[1];
+          interface_ids_.assign(o.begin() + (long)i, o.end());
+        }
+        break;
+      }
+      case OpExecutionMode:
+        if (o.size() >= 2 && o[1] == ModeOriginLowerLeft && stage_ == Stage::Fragment && o[0] == entry_id_)
+          return fail("OriginLowerLeft is not supported (Vulkan requires OriginUpperLeft)");
+        if (o.size() >= 2 && o[1] == ModeDepthReplacing && o[0] == entry_id_)
+          return fail("fragment depth output is not supported");
+        break;
+      case OpDecorate: {
+        std::vector<uint32_t> rest(o.begin() + 2, o.end());
+        decs_[o[0]].list.push_back({o[1], rest});
+        break;
+      }
+      case OpMemberDecorate: {
+        std::vector<uint32_t> rest(o.begin() + 3, o.end());
+        member_decs_[{o[0], o[1]}].list.push_back({o[2], rest});
+        break;
+      }
+      case OpTypeVoid: types_[o[0]].kind = TypeInfo::Void; break;
+      case OpTypeBool: types_[o[0]].kind = TypeInfo::Bool; break;
+      case OpTypeInt: {
+        TypeInfo& t = types_[o[0]];
+        t.kind = TypeInfo::Int;
+        t.width = o[1];
+        t.is_signed = o[2] != 0;
+        break;
+      }
+      case OpTypeFloat: {
+        TypeInfo& t = types_[o[0]];
+        t.kind = TypeInfo::Float;
+        t.width = o[1];
+        break;
+      }
+      case OpTypeVector:
+      case OpTypeMatrix: {
+        TypeInfo& t = types_[o[0]];
+        t.kind = in.opcode == OpTypeVector ? TypeInfo::Vector : TypeInfo::Matrix;
+        t.elem = o[1];
+        t.count = o[2];
+        break;
+      }
+      case OpTypeArray: {
+        TypeInfo& t = types_[o[0]];
+        t.kind = TypeInfo::Array;
+        t.elem = o[1];
+        auto c = consts_.find(o[2]);
+        t.count = c == consts_.end() || c->second.second.empty() ? 0 : c->second.second[0];
+        break;
+      }
+      case OpTypeRuntimeArray: {
+        TypeInfo& t = types_[o[0]];
+        t.kind = TypeInfo::RuntimeArray;
+        t.elem = o[1];
+        break;
+      }
+      case OpTypeStruct: {
+        TypeInfo& t = types_[o[0]];
+        t.kind = TypeInfo::Struct;
+        t.members.assign(o.begin() + 1, o.end());
+        break;
+      }
+      case OpTypePointer: {
+        TypeInfo& t = types_[o[0]];
+        t.kind = TypeInfo::Pointer;
+        t.storage = o[1];
+        t.elem = o[2];
+        break;
+      }
+      case OpTypeFunction: types_[o[0]].kind = TypeInfo::Function; break;
+      case OpTypeImage:
+      case OpTypeSampler:
+      case OpTypeSampledImage:
+      case OpTypeOpaque: types_[o[0]].kind = TypeInfo::Other; break;
+      case OpConstantTrue:
+      case OpConstantFalse:
+        consts_[o[1]] = {o[0], {in.opcode == OpConstantTrue ? 1u : 0u}};
+        break;
+      case OpSpecConstantTrue:
+      case OpSpecConstantFalse: {
+        uint32_t v = in.opcode == OpSpecConstantTrue ? 1u : 0u, sid;
+        if (decs_[o[1]].get(DecSpecId, sid))
+          for (auto& s : spec_)
+            if (s.first == sid) v = s.second != 0;
+        consts_[o[1]] = {o[0], {v}};
+        break;
+      }
+      case OpConstant:
+      case OpSpecConstant: {
+        if (o.size() < 3) return fail("constant without a value");
+        if (ty(o[0]).width != 32) {
+          consts_[o[1]] = {o[0], {o[2]}}; /* 64-bit constants keep their low word (decode-only support) */
+          break;
+        }
+        uint32_t v = o[2], sid;
+        if (in.opcode == OpSpecConstant && decs_[o[1]].get(DecSpecId, sid))
+          for (auto& s : spec_)
+            if (s.first == sid) v = s.second;
+        consts_[o[1]] = {o[0], {v}};
+        break;
+      }
+      case OpConstantComposite:
+      case OpSpecConstantComposite: {
+        std::vector<uint32_t> bits;
+        for (size_t i = 2; i < o.size(); i++) {
+          auto c = consts_.find(o[i]);
+          if (c == consts_.end()) return fail("composite constant of a non-constant");
+          bits.insert(bits.end(), c->second.second.begin(), c->second.second.end());
+        }
+        consts_[o[1]] = {o[0], bits};
+        break;
+      }
+      case OpConstantNull:
+        consts_[o[1]] = {o[0], std::vector<uint32_t>(scalars(o[0]), 0u)};
+        break;
+      case OpSpecConstantOp:
+        if (!eval_spec_op(in)) return false;
+        break;
+      case OpVariable: {
+        if (o[2] == SCFunction) break; /* handled inside the function */
+        Var v;
+        v.storage = o[2];
+        v.type = ty(o[0]).elem;
+        vars_[o[1]] = v;
+        break;
+      }
+      default: break;
+    }
+  }
+  if (!entry_id_) return fail("entry point \"" + entry_name_ + "\" not found for this stage");
+  return err_.empty();
+}
+
+bool Translator::eval_spec_op(const Insn& in) {
+  const auto& o = in.ops;
+  uint32_t opc = o[2];
+  auto arg = [&](size_t i, uint32_t& v) -> bool {
+    auto c = consts_.find(o[i]);
+    if (c == consts_.end() || c->second.second.empty()) return fail("OpSpecConstantOp operand is not constant");
+    v = c->second.second[0];
+    return true;
+  };
+  uint32_t a = 0, b = 0, r = 0;
+  if (!arg(3, a)) return false;
+  if (o.size() > 4 && !arg(4, b)) return false;
+  switch (opc) {
+    case OpIAdd: r = a + b; break;
+    case OpISub: r = a - b; break;
+    case OpIMul: r = a * b; break;
+    case OpUDiv: r = b ? a / b : 0; break;
+    case OpSDiv: r = b ? (uint32_t)((int32_t)a / (int32_t)b) : 0; break;
+    case OpUMod: r = b ? a % b : 0; break;
+    case OpSRem: r = b ? (uint32_t)((int32_t)a % (int32_t)b) : 0; break;
+    case OpBitwiseAnd: r = a & b; break;
+    case OpBitwiseOr: r = a | b; break;
+    case OpBitwiseXor: r = a ^ b; break;
+    case OpShiftLeftLogical: r = a << (b & 31); break;
+    case OpShiftRightLogical: r = a >> (b & 31); break;
+    case OpShiftRightArithmetic: r = (uint32_t)((int32_t)a >> (b & 31)); break;
+    case OpNot: r = ~a; break;
+    case OpSNegate: r = (uint32_t)(-(int32_t)a); break;
+    case OpIEqual: r = a == b; break;
+    case OpINotEqual: r = a != b; break;
+    case OpLogicalAnd: r = a && b; break;
+    case OpLogicalOr: r = a || b; break;
+    case OpLogicalNot: r = !a; break;
+    default: return fail("unsupported OpSpecConstantOp opcode " + std::to_string(opc));
+  }
+  consts_[o[1]] = {o[0], {r}};
+  return true;
+}
+
+/* interface layout: each location is 16 bytes (four 32-bit components) */
+void Translator::assign_io(uint32_t t, const DecSet* d, uint32_t struct_type, uint32_t member_idx, uint32_t& location,
+                           std::vector<Slot>& slots, bool is_input) {
+  uint32_t loc, comp = 0, bi;
+  DecSet empty;
+  const DecSet& ds = d ? *d : empty;
+  if (ds.get(DecLocation, loc)) location = loc;
+  ds.get(DecComponent, comp);
+  bool flat = ds.has(DecFlat), noper = ds.has(DecNoPerspective);
+  const TypeInfo& ti = ty(t);
+  if (ds.get(DecBuiltIn, bi)) {
+    uint32_t n = scalars(t);
+    for (uint32_t k = 0; k < n; k++) {
+      Slot s;
+      if (is_input) {
+        s.space = Space::In;
+        if (stage_ == Stage::Vertex && (bi == BuiltInVertexIndex || bi == BuiltInVertexId)) s.offset = 128;
+        else if (stage_ == Stage::Vertex && (bi == BuiltInInstanceIndex || bi == BuiltInInstanceId)) s.offset = 132;
+        else if (stage_ == Stage::Fragment && bi == BuiltInFragCoord) s.offset = 64 + 4 * k;
+        else if (stage_ == Stage::Fragment && bi == BuiltInFrontFacing) {
+          s.offset = 80;
+          s.is_bool_in = true;
+        } else {
+          fail("unsupported input built-in " + std::to_string(bi));
+          s.space = Space::None;
+        }
+      } else {
+        s.space = Space::Out;
+        if (stage_ == Stage::Vertex && bi == BuiltInPosition && k < 4) {
+          s.offset = 4 * k;
+          out_.iface.writes_position = true;
+        } else if (stage_ == Stage::Fragment && bi == BuiltInFragDepth) {
+          fail("fragment depth output is not supported");
+        } else {
+          s.space = Space::None; /* PointSize, ClipDistance, CullDistance: accepted and ignored */
+        }
+      }
+      slots.push_back(s);
+    }
+    return;
+  }
+  (void)struct_type;
+  (void)member_idx;
+  switch (ti.kind) {
+    case TypeInfo::Bool:
+    case TypeInfo::Int:
+    case TypeInfo::Float:
+    case TypeInfo::Vector: {
+      uint32_t n = scalars(t);
+      for (uint32_t k = 0; k < n; k++) {
+        Slot s;
+        uint32_t c = comp + k;
+        uint32_t slot = location * 4 + c;
+        if (is_input) {
+          s.space = Space::In;
+          s.offset = location * 16 + c * 4;
+          if (stage_ == Stage::Vertex) {
+            if (location >= 8) fail("vertex input location beyond 7");
+            out_.iface.input_locations |= 1u << location;
+          } else {
+            if (slot >= 16) fail("fragment input beyond 16 scalar varyings");
+            out_.iface.input_slots |= 1u << slot;
+            out_.iface.input_locations |= 1u << location;
+            if (flat) out_.iface.flat_slots |= 1u << slot;
+            if (noper) out_.iface.noperspective_slots |= 1u << slot;
+          }
+        } else {
+          s.space = Space::Out;
+          if (stage_ == Stage::Vertex) {
+            if (slot >= 16) fail("vertex output beyond 16 scalar varyings");
+            s.offset = 16 + slot * 4;
+            out_.iface.output_slots |= 1u << slot;
+            if (flat) out_.iface.flat_slots |= 1u << slot;
+            if (noper) out_.iface.noperspective_slots |= 1u << slot;
+          } else {
+            if (location == 0) {
+              s.offset = c * 4;
+              out_.iface.writes_color = true;
+            } else {
+              s.space = Space::None; /* only one colour attachment */
+            }
+          }
+        }
+        slots.push_back(s);
+      }
+      location++;
+      break;
+    }
+    case TypeInfo::Matrix:
+    case TypeInfo::Array:
+      for (uint32_t i = 0; i < ti.count; i++) assign_io(ti.elem, nullptr, 0, 0, location, slots, is_input);
+      break;
+    case TypeInfo::Struct:
+      for (uint32_t i = 0; i < ti.members.size(); i++) {
+        auto it = member_decs_.find({t, i});
+        const DecSet* md = it == member_decs_.end() ? nullptr : &it->second;
+        uint32_t mloc;
+        if (md && md->get(DecLocation, mloc)) location = mloc;
+        DecSet merged;
+        if (md) merged = *md;
+        if (flat && !merged.has(DecFlat)) merged.list.push_back({DecFlat, {}});
+        if (noper && !merged.has(DecNoPerspective)) merged.list.push_back({DecNoPerspective, {}});
+        assign_io(ti.members[i], &merged, t, i, location, slots, is_input);
+      }
+      break;
+    default: fail("unsupported interface variable type"); break;
+  }
+}
+
+void Translator::assign_push(uint32_t t, uint32_t byte, std::vector<Slot>& slots, uint32_t stride_hint,
+                             bool row_major) {
+  const TypeInfo& ti = ty(t);
+  switch (ti.kind) {
+    case TypeInfo::Bool:
+    case TypeInfo::Int:
+    case TypeInfo::Float: {
+      Slot s;
+      s.space = Space::Push;
+      s.offset = byte;
+      slots.push_back(s);
+      if (byte + 4 > out_.iface.push_bytes) out_.iface.push_bytes = byte + 4;
+      break;
+    }
+    case TypeInfo::Vector:
+      for (uint32_t i = 0; i < ti.count; i++) assign_push(ti.elem, byte + 4 * i, slots, 0, false);
+      break;
+    case TypeInfo::Matrix: {
+      uint32_t rows = ty(ti.elem).count;
+      uint32_t stride = stride_hint ? stride_hint : 16;
+      for (uint32_t c = 0; c < ti.count; c++)
+        for (uint32_t r = 0; r < rows; r++) {
+          uint32_t off = row_major ? byte + r * stride + 4 * c : byte + c * stride + 4 * r;
+          assign_push(ty(ti.elem).elem, off, slots, 0, false);
+        }
+      break;
+    }
+    case TypeInfo::Array: {
+      uint32_t stride = 0;
+      decs_[t].get(DecArrayStride, stride);
+      if (!stride) stride = 4 * scalars(ti.elem);
+      for (uint32_t i = 0; i < ti.count; i++) assign_push(ti.elem, byte + i * stride, slots, stride_hint, row_major);
+      break;
+    }
+    case TypeInfo::Struct:
+      for (uint32_t i = 0; i < ti.members.size(); i++) {
+        auto it = member_decs_.find({t, i});
+        uint32_t off = 0, ms = 0;
+        bool rm = false;
+        if (it != member_decs_.end()) {
+          it->second.get(DecOffset, off);
+          it->second.get(DecMatrixStride, ms);
+          rm = it->second.has(DecRowMajor);
+        }
+        assign_push(ti.members[i], byte + off, slots, ms, rm);
+      }
+      break;
+    default: fail("unsupported push-constant member type"); break;
+  }
+}
+
+bool Translator::layout_interface(uint32_t var_id, Var& v) {
+  v.slots.clear();
+  if (v.storage == SCInput || v.storage == SCOutput) {
+    uint32_t location = 0;
+    auto it = decs_.find(var_id);
+    assign_io(v.type, it == decs_.end() ? nullptr : &it->second, 0, 0, location, v.slots, v.storage == SCInput);
+  } else if (v.storage == SCPushConstant) {
+    assign_push(v.type, 0, v.slots, 0, false);
+  } else if (v.storage == SCPrivate || v.storage == SCFunction) {
+    std::vector<Ty> tys;
+    flat_types(v.type, tys);
+    for (Ty t : tys) {
+      Slot s;
+      s.space = Space::Reg;
+      s.reg = fn_.reg(t);
+      v.slots.push_back(s);
+    }
+  } else {
+    return fail("unsupported variable storage class " + std::to_string(v.storage) +
+                " (descriptor sets are not supported by the draw path)");
+  }
+  if (v.storage == SCOutput) {
+    std::vector<Ty> tys;
+    flat_types(v.type, tys);
+    for (size_t k = 0; k < v.slots.size() && k < tys.size(); k++) v.slots[k].reg = fn_.reg(tys[k]);
+  }
+  return err_.empty();
+}
+
+bool Translator::load(const Place& p, Val& v) {
+  Var& var = vars_[p.var];
+  std::vector<Ty> tys;
+  flat_types(p.type, tys);
+  v.type = p.type;
+  v.regs.clear();
+  for (size_t k = 0; k < tys.size(); k++) {
+    if (p.first + k >= var.slots.size()) return fail("load outside a variable");
+    const Slot& s = var.slots[p.first + k];
+    switch (s.space) {
+      case Space::In: {
+        if (s.is_bool_in) {
+          int32_t r = fn_.reg(Ty::B32);
+          Inst i;
+          i.op = Op::LdIn;
+          i.ty = Ty::B32;
+          i.dst = r;
+          i.imm = s.offset;
+          fn_.emit(i);
+          v.regs.push_back(op1(Op::B32ToP, Ty::Pred, r));
+        } else {
+          int32_t r = fn_.reg(tys[k]);
+          Inst i;
+          i.op = Op::LdIn;
+          i.ty = tys[k];
+          i.dst = r;
+          i.imm = s.offset;
+          fn_.emit(i);
+          v.regs.push_back(r);
+        }
+        break;
+      }
+      case Space::Push: {
+        Ty t = tys[k] == Ty::Pred ? Ty::B32 : tys[k];
+        int32_t r = fn_.reg(t);
+        Inst i;
+        i.op = Op::LdPush;
+        i.ty = t;
+        i.dst = r;
+        i.imm = s.offset;
+        fn_.emit(i);
+        v.regs.push_back(tys[k] == Ty::Pred ? op1(Op::B32ToP, Ty::Pred, r) : r);
+        break;
+      }
+      case Space::Out:
+      case Space::Reg: {
+        int32_t r = fn_.reg(tys[k]);
+        mov(tys[k], r, s.reg);
+        v.regs.push_back(r);
+        break;
+      }
+      default: v.regs.push_back(konst(tys[k], 0)); break;
+    }
+  }
+  return true;
+}
+
+bool Translator::store(const Place& p, const Val& v) {
+  Var& var = vars_[p.var];
+  for (size_t k = 0; k < v.regs.size(); k++) {
+    if (p.first + k >= var.slots.size()) return fail("store outside a variable");
+    const Slot& s = var.slots[p.first + k];
+    if (s.space == Space::Out || s.space == Space::Reg) mov(reg_ty(v.regs[k]), s.reg, v.regs[k]);
+    else if (s.space == Space::None && var.storage == SCOutput) continue;
+    else return fail("store to a read-only variable");
+  }
+  return true;
+}
+
+void Translator::finish_outputs() {
+  for (auto& kv : vars_) {
+    Var& v = kv.second;
+    if (v.storage != SCOutput) continue;
+    for (const Slot& s : v.slots) {
+      if (s.space != Space::Out || s.reg < 0) continue;
+      Inst i;
+      i.op = Op::StOut;
+      i.ty = reg_ty(s.reg);
+      i.a = s.reg;
+      i.imm = s.offset;
+      fn_.emit(i);
+    }
+  }
+}
+
+int32_t Translator::dot(const std::vector<int32_t>& a, const std::vector<int32_t>& b, size_t n) {
+  int32_t t = op2(Op::FMul, Ty::F32, a[0], b[0]);
+  for (size_t k = 1; k < n; k++) t = op3(Op::FFma, Ty::F32, a[k], b[k], t);
+  return t;
+}
+
+bool Translator::branch_to(uint32_t target) {
+  auto it = phis_.find(target);
+  if (it != phis_.end()) {
+    std::vector<std::pair<int32_t, int32_t>> moves; /* (phi reg, temp) */
+    for (const PhiInfo& ph : it->second) {
+      const Val& dst = vals_[ph.result];
+      for (auto& inc : ph.incoming) {
+        if (inc.second != cur_block_) continue;
+        Val* src = nullptr;
+        auto c = vals_.find(inc.first);
+        if (c != vals_.end()) src = &c->second;
+        if (!src) return fail("OpPhi operand %" + std::to_string(inc.first) + " not available");
+        for (size_t k = 0; k < dst.regs.size() && k < src->regs.size(); k++) {
+          int32_t tmp = fn_.reg(reg_ty(dst.regs[k]));
+          mov(reg_ty(dst.regs[k]), tmp, src->regs[k]);
+          moves.push_back({dst.regs[k], tmp});
+        }
+      }
+    }
+    for (auto& mv : moves) mov(reg_ty(mv.first), mv.first, mv.second);
+  }
+  bra(label_of(target));
+  return true;
+}
+
+bool Translator::ext_inst(const Insn& in) {
+  const auto& o = in.ops;
+  uint32_t rt = o[0], res = o[1], set = o[2], num = o[3];
+  if (ext_sets_[set] != "GLSL.std.450") return fail("unsupported extended instruction set");
+  std::vector<Val*> args;
+  for (size_t i = 4; i < o.size(); i++) {
+    Val* v = val(o[i]);
+    if (!v) return false;
+    args.push_back(v);
+  }
+  Val out;
+  out.type = rt;
+  uint32_t n = scalars(rt);
+  auto need = [&](size_t k) { return args.size() >= k || fail("extended instruction with too few operands"); };
+  auto per = [&](Op op) {
+    for (uint32_t k = 0; k < n; k++) out.regs.push_back(op1(op, Ty::F32, args[0]->regs[k]));
+  };
+  auto per2 = [&](Op op, Ty t) {
+    for (uint32_t k = 0; k < n; k++) out.regs.push_back(op2(op, t, args[0]->regs[k], args[1]->regs[k]));
+  };
+  switch (num) {
+    case GFAbs: if (!need(1)) return false; per(Op::FAbs); break;
+    case GFloor: if (!need(1)) return false; per(Op::FFloor); break;
+    case GCeil: if (!need(1)) return false; per(Op::FCeil); break;
+    case GTrunc: if (!need(1)) return false; per(Op::FTrunc); break;
+    case GRoundEven:
+    case GRound: if (!need(1)) return false; per(Op::FRoundEven); break;
+    case GSqrt: if (!need(1)) return false; per(Op::FSqrt); break;
+    case GSin: if (!need(1)) return false; per(Op::FSin); break;
+    case GCos: if (!need(1)) return false; per(Op::FCos); break;
+    case GExp2: if (!need(1)) return false; per(Op::FEx2); break;
+    case GLog2: if (!need(1)) return false; per(Op::FLg2); break;
+    case GInverseSqrt:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++)
+        out.regs.push_back(op2(Op::FDiv, Ty::F32, konst(Ty::F32, 0x3F800000u), op1(Op::FSqrt, Ty::F32, args[0]->regs[k])));
+      break;
+    case GFract:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++)
+        out.regs.push_back(op2(Op::FSub, Ty::F32, args[0]->regs[k], op1(Op::FFloor, Ty::F32, args[0]->regs[k])));
+      break;
+    case GFMin: if (!need(2)) return false; per2(Op::FMin, Ty::F32); break;
+    case GFMax: if (!need(2)) return false; per2(Op::FMax, Ty::F32); break;
+    case GFClamp:
+      if (!need(3)) return false;
+      for (uint32_t k = 0; k < n; k++)
+        out.regs.push_back(op2(Op::FMin, Ty::F32, op2(Op::FMax, Ty::F32, args[0]->regs[k], args[1]->regs[k]),
+                               args[2]->regs[k]));
+      break;
+    case GFMix:
+      if (!need(3)) return false;
+      for (uint32_t k = 0; k < n; k++)
+        out.regs.push_back(op3(Op::FFma, Ty::F32, args[2]->regs[k],
+                               op2(Op::FSub, Ty::F32, args[1]->regs[k], args[0]->regs[k]), args[0]->regs[k]));
+      break;
+    case GFma:
+      if (!need(3)) return false;
+      for (uint32_t k = 0; k < n; k++)
+        out.regs.push_back(op3(Op::FFma, Ty::F32, args[0]->regs[k], args[1]->regs[k], args[2]->regs[k]));
+      break;
+    case GStep:
+      if (!need(2)) return false;
+      /* step(edge, x) = x < edge ? 0 : 1 */
+      for (uint32_t k = 0; k < n; k++) {
+        int32_t p = op2(Op::SetpF, Ty::Pred, args[1]->regs[k], args[0]->regs[k], CmpLt);
+        out.regs.push_back(op3(Op::Selp, Ty::F32, konst(Ty::F32, 0), konst(Ty::F32, 0x3F800000u), p));
+      }
+      break;
+    case GSMin: if (!need(2)) return false; for (uint32_t k = 0; k < n; k++) { int32_t p = op2(Op::SetpS, Ty::Pred, args[0]->regs[k], args[1]->regs[k], CmpLt); out.regs.push_back(op3(Op::Selp, Ty::B32, args[0]->regs[k], args[1]->regs[k], p)); } break;
+    case GSMax: if (!need(2)) return false; for (uint32_t k = 0; k < n; k++) { int32_t p = op2(Op::SetpS, Ty::Pred, args[0]->regs[k], args[1]->regs[k], CmpGt); out.regs.push_back(op3(Op::Selp, Ty::B32, args[0]->regs[k], args[1]->regs[k], p)); } break;
+    case GUMin: if (!need(2)) return false; for (uint32_t k = 0; k < n; k++) { int32_t p = op2(Op::SetpU, Ty::Pred, args[0]->regs[k], args[1]->regs[k], CmpLt); out.regs.push_back(op3(Op::Selp, Ty::B32, args[0]->regs[k], args[1]->regs[k], p)); } break;
+    case GUMax: if (!need(2)) return false; for (uint32_t k = 0; k < n; k++) { int32_t p = op2(Op::SetpU, Ty::Pred, args[0]->regs[k], args[1]->regs[k], CmpGt); out.regs.push_back(op3(Op::Selp, Ty::B32, args[0]->regs[k], args[1]->regs[k], p)); } break;
+    case GLength: {
+      if (!need(1)) return false;
+      size_t m = args[0]->regs.size();
+      out.regs.push_back(op1(Op::FSqrt, Ty::F32, dot(args[0]->regs, args[0]->regs, m)));
+      break;
+    }
+    case GDistance: {
+      if (!need(2)) return false;
+      size_t m = args[0]->regs.size();
+      std::vector<int32_t> d;
+      for (size_t k = 0; k < m; k++) d.push_back(op2(Op::FSub, Ty::F32, args[0]->regs[k], args[1]->regs[k]));
+      out.regs.push_back(op1(Op::FSqrt, Ty::F32, dot(d, d, m)));
+      break;
+    }
+    case GNormalize: {
+      if (!need(1)) return false;
+      size_t m = args[0]->regs.size();
+      int32_t len = op1(Op::FSqrt, Ty::F32, dot(args[0]->regs, args[0]->regs, m));
+      int32_t inv = op2(Op::FDiv, Ty::F32, konst(Ty::F32, 0x3F800000u), len);
+      for (size_t k = 0; k < m; k++) out.regs.push_back(op2(Op::FMul, Ty::F32, args[0]->regs[k], inv));
+      break;
+    }
+    case GCross: {
+      if (!need(2)) return false;
+      const auto& a = args[0]->regs;
+      const auto& b = args[1]->regs;
+      /* cross = a.yzx * b.zxy - a.zxy * b.yzx, each component as fma(a1, b2, -(a2 * b1)) */
+      int idx[3][4] = {{1, 2, 2, 1}, {2, 0, 0, 2}, {0, 1, 1, 0}};
+      for (int k = 0; k < 3; k++) {
+        int32_t t = op1(Op::FNeg, Ty::F32, op2(Op::FMul, Ty::F32, a[idx[k][2]], b[idx[k][3]]));
+        out.regs.push_back(op3(Op::FFma, Ty::F32, a[idx[k][0]], b[idx[k][1]], t));
+      }
+      break;
+    }
+    case GPow: {
+      if (!need(2)) return false;
+      /* pow(x, y) = exp2(y * log2(x)) with the hardware approximations */
+      for (uint32_t k = 0; k < n; k++)
+        out.regs.push_back(op1(Op::FEx2, Ty::F32, op2(Op::FMul, Ty::F32, args[1]->regs[k], op1(Op::FLg2, Ty::F32, args[0]->regs[k]))));
+      break;
+    }
+    default: return fail("unsupported GLSL.std.450 instruction " + std::to_string(num));
+  }
+  vals_[res] = out;
+  return true;
+}
+
+bool Translator::do_insn(const Insn& in) {
+  const auto& o = in.ops;
+  auto unary_f = [&](Op op) {
+    Val* a = val(o[2]);
+    if (!a) return false;
+    Val r;
+    r.type = o[0];
+    for (int32_t x : a->regs) r.regs.push_back(op1(op, Ty::F32, x));
+    vals_[o[1]] = r;
+    return true;
+  };
+  auto binary = [&](Op op, Ty t) {
+    Val* a = val(o[2]);
+    Val* b = val(o[3]);
+    if (!a || !b) return false;
+    Val r;
+    r.type = o[0];
+    for (size_t k = 0; k < a->regs.size() && k < b->regs.size(); k++) r.regs.push_back(op2(op, t, a->regs[k], b->regs[k]));
+    vals_[o[1]] = r;
+    return true;
+  };
+  auto compare = [&](Op op, uint32_t cmp) {
+    Val* a = val(o[2]);
+    Val* b = val(o[3]);
+    if (!a || !b) return false;
+    Val r;
+    r.type = o[0];
+    for (size_t k = 0; k < a->regs.size() && k < b->regs.size(); k++)
+      r.regs.push_back(op2(op, Ty::Pred, a->regs[k], b->regs[k], cmp));
+    vals_[o[1]] = r;
+    return true;
+  };
+  switch (in.opcode) {
+    case OpLine:
+    case OpNop:
+    case OpSelectionMerge:
+    case OpLoopMerge:
+    case OpName:
+    case OpMemberName:
+    case OpPhi: /* registers allocated in the pre-scan; moves emitted on the incoming edges */
+      return true;
+    case OpLabel:
+      cur_block_ = o[0];
+      label(label_of(o[0]));
+      return true;
+    case OpVariable: {
+      Var v;
+      v.storage = SCFunction;
+      v.type = ty(o[0]).elem;
+      if (!layout_interface(o[1], v)) return false;
+      if (o.size() > 3) {
+        Val* init = val(o[3]);
+        if (!init) return false;
+        for (size_t k = 0; k < v.slots.size() && k < init->regs.size(); k++) mov(reg_ty(v.slots[k].reg), v.slots[k].reg, init->regs[k]);
+      }
+      vars_[o[1]] = v;
+      Place p;
+      p.var = o[1];
+      p.type = v.type;
+      places_[o[1]] = p;
+      return true;
+    }
+    case OpAccessChain:
+    case OpInBoundsAccessChain: {
+      auto it = places_.find(o[2]);
+      if (it == places_.end()) return fail("access chain on something that is not a variable");
+      Place p = it->second;
+      for (size_t i = 3; i < o.size(); i++) {
+        auto c = consts_.find(o[i]);
+        if (c == consts_.end() || c->second.second.empty())
+          return fail("dynamic access-chain indices are not supported");
+        uint32_t off, mt;
+        if (!member(p.type, c->second.second[0], off, mt)) return false;
+        p.first += off;
+        p.type = mt;
+      }
+      places_[o[1]] = p;
+      return true;
+    }
+    case OpLoad: {
+      auto it = places_.find(o[2]);
+      if (it == places_.end()) return fail("load through an unknown pointer");
+      Val v;
+      if (!load(it->second, v)) return false;
+      v.type = o[0];
+      vals_[o[1]] = v;
+      return true;
+    }
+    case OpStore: {
+      auto it = places_.find(o[0]);
+      if (it == places_.end()) return fail("store through an unknown pointer");
+      Val* v = val(o[1]);
+      if (!v) return false;
+      return store(it->second, *v);
+    }
+    case OpCopyObject: {
+      Val* a = val(o[2]);
+      if (!a) return false;
+      vals_[o[1]] = *a;
+      return true;
+    }
+    case OpUndef: {
+      std::vector<Ty> tys;
+      flat_types(o[0], tys);
+      Val r;
+      r.type = o[0];
+      for (Ty t : tys) r.regs.push_back(konst(t, 0));
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpCompositeConstruct: {
+      Val r;
+      r.type = o[0];
+      for (size_t i = 2; i < o.size(); i++) {
+        Val* a = val(o[i]);
+        if (!a) return false;
+        r.regs.insert(r.regs.end(), a->regs.begin(), a->regs.end());
+      }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpCompositeExtract: {
+      Val* a = val(o[2]);
+      if (!a) return false;
+      uint32_t t = a->type, first = 0;
+      for (size_t i = 3; i < o.size(); i++) {
+        uint32_t off, mt;
+        if (!member(t, o[i], off, mt)) return false;
+        first += off;
+        t = mt;
+      }
+      Val r;
+      r.type = o[0];
+      uint32_t n = scalars(t);
+      for (uint32_t k = 0; k < n; k++) r.regs.push_back(a->regs[first + k]);
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpCompositeInsert: {
+      Val* obj = val(o[2]);
+      Val* comp = val(o[3]);
+      if (!obj || !comp) return false;
+      uint32_t t = comp->type, first = 0;
+      for (size_t i = 4; i < o.size(); i++) {
+        uint32_t off, mt;
+        if (!member(t, o[i], off, mt)) return false;
+        first += off;
+        t = mt;
+      }
+      Val r = *comp;
+      r.type = o[0];
+      for (size_t k = 0; k < obj->regs.size(); k++) r.regs[first + k] = obj->regs[k];
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpVectorShuffle: {
+      Val* a = val(o[2]);
+      Val* b = val(o[3]);
+      if (!a || !b) return false;
+      Val r;
+      r.type = o[0];
+      for (size_t i = 4; i < o.size(); i++) {
+        uint32_t s = o[i];
+        if (s == 0xFFFFFFFFu) r.regs.push_back(konst(Ty::F32, 0));
+        else if (s < a->regs.size()) r.regs.push_back(a->regs[s]);
+        else r.regs.push_back(b->regs[s - a->regs.size()]);
+      }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpFAdd: return binary(Op::FAdd, Ty::F32);
+    case OpFSub: return binary(Op::FSub, Ty::F32);
+    case OpFMul: return binary(Op::FMul, Ty::F32);
+    case OpFDiv: return binary(Op::FDiv, Ty::F32);
+    case OpFNegate: return unary_f(Op::FNeg);
+    case OpIAdd: return binary(Op::IAdd, Ty::B32);
+    case OpISub: return binary(Op::ISub, Ty::B32);
+    case OpIMul: return binary(Op::IMul, Ty::B32);
+    case OpUDiv: return binary(Op::UDiv, Ty::B32);
+    case OpSDiv: return binary(Op::SDiv, Ty::B32);
+    case OpUMod: return binary(Op::URem, Ty::B32);
+    case OpSRem: return binary(Op::SRem, Ty::B32);
+    case OpBitwiseAnd: return binary(Op::And, Ty::B32);
+    case OpBitwiseOr: return binary(Op::Or, Ty::B32);
+    case OpBitwiseXor: return binary(Op::Xor, Ty::B32);
+    case OpShiftLeftLogical: return binary(Op::Shl, Ty::B32);
+    case OpShiftRightLogical: return binary(Op::Shr, Ty::B32);
+    case OpShiftRightArithmetic: return binary(Op::Sar, Ty::B32);
+    case OpNot:
+    case OpSNegate: {
+      Val* a = val(o[2]);
+      if (!a) return false;
+      Val r;
+      r.type = o[0];
+      for (int32_t x : a->regs) r.regs.push_back(op1(in.opcode == OpNot ? Op::Not : Op::INeg, Ty::B32, x));
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpLogicalAnd: return binary(Op::PAnd, Ty::Pred);
+    case OpLogicalOr: return binary(Op::POr, Ty::Pred);
+    case OpLogicalNotEqual: return binary(Op::PXor, Ty::Pred);
+    case OpLogicalEqual: {
+      if (!binary(Op::PXor, Ty::Pred)) return false;
+      for (int32_t& x : vals_[o[1]].regs) x = op1(Op::PNot, Ty::Pred, x);
+      return true;
+    }
+    case OpLogicalNot: {
+      Val* a = val(o[2]);
+      if (!a) return false;
+      Val r;
+      r.type = o[0];
+      for (int32_t x : a->regs) r.regs.push_back(op1(Op::PNot, Ty::Pred, x));
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpSelect: {
+      Val* c = val(o[2]);
+      Val* a = val(o[3]);
+      Val* b = val(o[4]);
+      if (!c || !a || !b) return false;
+      Val r;
+      r.type = o[0];
+      for (size_t k = 0; k < a->regs.size(); k++) {
+        int32_t p = c->regs.size() == 1 ? c->regs[0] : c->regs[k];
+        Ty t = reg_ty(a->regs[k]);
+        if (t == Ty::Pred) {
+          int32_t x = op2(Op::PAnd, Ty::Pred, p, a->regs[k]);
+          int32_t y = op2(Op::PAnd, Ty::Pred, op1(Op::PNot, Ty::Pred, p), b->regs[k]);
+          r.regs.push_back(op2(Op::POr, Ty::Pred, x, y));
+        } else {
+          r.regs.push_back(op3(Op::Selp, t, a->regs[k], b->regs[k], p));
+        }
+      }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpIEqual: return compare(Op::SetpU, CmpEq);
+    case OpINotEqual: return compare(Op::SetpU, CmpNe);
+    case OpUGreaterThan: return compare(Op::SetpU, CmpGt);
+    case OpSGreaterThan: return compare(Op::SetpS, CmpGt);
+    case OpUGreaterThanEqual: return compare(Op::SetpU, CmpGe);
+    case OpSGreaterThanEqual: return compare(Op::SetpS, CmpGe);
+    case OpULessThan: return compare(Op::SetpU, CmpLt);
+    case OpSLessThan: return compare(Op::SetpS, CmpLt);
+    case OpULessThanEqual: return compare(Op::SetpU, CmpLe);
+    case OpSLessThanEqual: return compare(Op::SetpS, CmpLe);
+    case OpFOrdEqual: return compare(Op::SetpF, CmpEq);
+    case OpFUnordEqual: return compare(Op::SetpF, CmpEq | CmpUnordered);
+    case OpFOrdNotEqual: return compare(Op::SetpF, CmpNe);
+    case OpFUnordNotEqual: return compare(Op::SetpF, CmpNe | CmpUnordered);
+    case OpFOrdLessThan: return compare(Op::SetpF, CmpLt);
+    case OpFUnordLessThan: return compare(Op::SetpF, CmpLt | CmpUnordered);
+    case OpFOrdGreaterThan: return compare(Op::SetpF, CmpGt);
+    case OpFUnordGreaterThan: return compare(Op::SetpF, CmpGt | CmpUnordered);
+    case OpFOrdLessThanEqual: return compare(Op::SetpF, CmpLe);
+    case OpFUnordLessThanEqual: return compare(Op::SetpF, CmpLe | CmpUnordered);
+    case OpFOrdGreaterThanEqual: return compare(Op::SetpF, CmpGe);
+    case OpFUnordGreaterThanEqual: return compare(Op::SetpF, CmpGe | CmpUnordered);
+    case OpIsNan: {
+      Val* a = val(o[2]);
+      if (!a) return false;
+      Val r;
+      r.type = o[0];
+      for (int32_t x : a->regs) r.regs.push_back(op2(Op::SetpF, Ty::Pred, x, x, CmpNe | CmpUnordered));
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpConvertFToS:
+    case OpConvertFToU:
+    case OpConvertSToF:
+    case OpConvertUToF:
+    case OpBitcast:
+    case OpUConvert:
+    case OpSConvert:
+    case OpFConvert: {
+      Val* a = val(o[2]);
+      if (!a) return false;
+      Val r;
+      r.type = o[0];
+      for (int32_t x : a->regs) {
+        switch (in.opcode) {
+          case OpConvertFToS: r.regs.push_back(op1(Op::CvtF2S, Ty::B32, x)); break;
+          case OpConvertFToU: r.regs.push_back(op1(Op::CvtF2U, Ty::B32, x)); break;
+          case OpConvertSToF: r.regs.push_back(op1(Op::CvtS2F, Ty::F32, x)); break;
+          case OpConvertUToF: r.regs.push_back(op1(Op::CvtU2F, Ty::F32, x)); break;
+          case OpBitcast: {
+            Ty t = is_float(o[0]) ? Ty::F32 : Ty::B32;
+            int32_t d = fn_.reg(t);
+            Inst i;
+            i.op = Op::Mov;
+            i.ty = t;
+            i.dst = d;
+            i.a = x;
+            fn_.emit(i);
+            r.regs.push_back(d);
+            break;
+          }
+          default: r.regs.push_back(x); break; /* 32-bit only: width conversions are identities */
+        }
+      }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpVectorTimesScalar:
+    case OpMatrixTimesScalar: {
+      Val* a = val(o[2]);
+      Val* s = val(o[3]);
+      if (!a || !s) return false;
+      Val r;
+      r.type = o[0];
+      for (int32_t x : a->regs) r.regs.push_back(op2(Op::FMul, Ty::F32, x, s->regs[0]));
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpDot: {
+      Val* a = val(o[2]);
+      Val* b = val(o[3]);
+      if (!a || !b) return false;
+      Val r;
+      r.type = o[0];
+      r.regs.push_back(dot(a->regs, b->regs, a->regs.size()));
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpMatrixTimesVector: {
+      Val* mtx = val(o[2]);
+      Val* v = val(o[3]);
+      if (!mtx || !v) return false;
+      const TypeInfo& mt = ty(mtx->type);
+      uint32_t cols = mt.count, rows = ty(mt.elem).count;
+      Val r;
+      r.type = o[0];
+      for (uint32_t i = 0; i < rows; i++) {
+        int32_t t = op2(Op::FMul, Ty::F32, mtx->regs[i], v->regs[0]);
+        for (uint32_t c = 1; c < cols; c++) t = op3(Op::FFma, Ty::F32, mtx->regs[c * rows + i], v->regs[c], t);
+        r.regs.push_back(t);
+      }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpVectorTimesMatrix: {
+      Val* v = val(o[2]);
+      Val* mtx = val(o[3]);
+      if (!v || !mtx) return false;
+      const TypeInfo& mt = ty(mtx->type);
+      uint32_t cols = mt.count, rows = ty(mt.elem).count;
+      Val r;
+      r.type = o[0];
+      for (uint32_t c = 0; c < cols; c++) {
+        std::vector<int32_t> col(mtx->regs.begin() + c * rows, mtx->regs.begin() + (c + 1) * rows);
+        r.regs.push_back(dot(v->regs, col, rows));
+      }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpMatrixTimesMatrix: {
+      Val* a = val(o[2]);
+      Val* b = val(o[3]);
+      if (!a || !b) return false;
+      const TypeInfo& at = ty(a->type);
+      const TypeInfo& bt = ty(b->type);
+      uint32_t k_dim = at.count, rows = ty(at.elem).count, cols = bt.count;
+      Val r;
+      r.type = o[0];
+      for (uint32_t c = 0; c < cols; c++)
+        for (uint32_t i = 0; i < rows; i++) {
+          int32_t t = op2(Op::FMul, Ty::F32, a->regs[i], b->regs[c * k_dim]);
+          for (uint32_t k = 1; k < k_dim; k++) t = op3(Op::FFma, Ty::F32, a->regs[k * rows + i], b->regs[c * k_dim + k], t);
+          r.regs.push_back(t);
+        }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpOuterProduct: {
+      Val* a = val(o[2]);
+      Val* b = val(o[3]);
+      if (!a || !b) return false;
+      Val r;
+      r.type = o[0];
+      for (int32_t y : b->regs)
+        for (int32_t x : a->regs) r.regs.push_back(op2(Op::FMul, Ty::F32, x, y));
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpTranspose: {
+      Val* a = val(o[2]);
+      if (!a) return false;
+      const TypeInfo& at = ty(a->type);
+      uint32_t cols = at.count, rows = ty(at.elem).count;
+      Val r;
+      r.type = o[0];
+      for (uint32_t i = 0; i < rows; i++)
+        for (uint32_t c = 0; c < cols; c++) r.regs.push_back(a->regs[c * rows + i]);
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpExtInst: return ext_inst(in);
+    case OpBranch: return branch_to(o[0]);
+    case OpBranchConditional: {
+      Val* c = val(o[0]);
+      if (!c) return false;
+      uint32_t t_l = fn_.label();
+      bra_if(c->regs[0], t_l);
+      if (!branch_to(o[2])) return false;
+      label(t_l);
+      return branch_to(o[1]);
+    }
+    case OpSwitch: {
+      Val* sel = val(o[0]);
+      if (!sel) return false;
+      std::vector<std::pair<uint32_t, uint32_t>> cases; /* (IR label of the trampoline, target) */
+      for (size_t i = 2; i + 1 < o.size(); i += 2) {
+        int32_t k = konst(Ty::B32, o[i]);
+        int32_t p = op2(Op::SetpU, Ty::Pred, sel->regs[0], k, CmpEq);
+        uint32_t l = fn_.label();
+        bra_if(p, l);
+        cases.push_back({l, o[i + 1]});
+      }
+      if (!branch_to(o[1])) return false;
+      for (auto& cs : cases) {
+        label(cs.first);
+        if (!branch_to(cs.second)) return false;
+      }
+      return true;
+    }
+    case OpReturn: {
+      finish_outputs();
+      Inst i;
+      i.op = Op::Ret;
+      fn_.emit(i);
+      return true;
+    }
+    case OpKill: {
+      out_.iface.discards = true;
+      Inst i;
+      i.op = Op::Kill;
+      fn_.emit(i);
+      return true;
+    }
+    case OpUnreachable: {
+      Inst i;
+      i.op = Op::Ret;
+      fn_.emit(i);
+      return true;
+    }
+    case OpFunctionCall: return fail("function calls are not supported yet (inline helper functions)");
+    default: return fail(std::string("unsupported instruction ") + opcode_name(in.opcode));
+  }
+}
+
+bool Translator::translate_entry() {
+  /* locate the entry function */
+  size_t begin = 0, end = 0;
+  for (size_t i = 0; i < m_.insns.size(); i++) {
+    const Insn& in = m_.insns[i];
+    if (in.opcode == OpFunction && in.ops.size() > 1 && in.ops[1] == entry_id_) begin = i + 1;
+    if (begin && in.opcode == OpFunctionEnd && i >= begin) {
+      end = i;
+      break;
+    }
+  }
+  if (!begin || !end) return fail("entry function body not found");
+  /* constants: materialised once at the top of the function */
+  for (auto& kv : consts_) {
+    std::vector<Ty> tys;
+    flat_types(kv.second.first, tys);
+    Val v;
+    v.type = kv.second.first;
+    for (size_t k = 0; k < tys.size() && k < kv.second.second.size(); k++) v.regs.push_back(konst(tys[k], kv.second.second[k]));
+    vals_[kv.first] = v;
+  }
+  /* module-scope variables */
+  for (auto& kv : vars_) {
+    if (!layout_interface(kv.first, kv.second)) return false;
+    Place p;
+    p.var = kv.first;
+    p.type = kv.second.type;
+    places_[kv.first] = p;
+    for (const Slot& s : kv.second.slots)
+      if (s.reg >= 0) mov(reg_ty(s.reg), s.reg, konst(reg_ty(s.reg), 0));
+  }
+  /* phis: result registers up front, incoming edges recorded per block */
+  uint32_t block = 0;
+  for (size_t i = begin; i < end; i++) {
+    const Insn& in = m_.insns[i];
+    if (in.opcode == OpLabel) block = in.ops[0];
+    if (in.opcode == OpPhi) {
+      PhiInfo ph;
+      ph.type = in.ops[0];
+      ph.result = in.ops[1];
+      for (size_t k = 2; k + 1 < in.ops.size(); k += 2) ph.incoming.push_back({in.ops[k], in.ops[k + 1]});
+      std::vector<Ty> tys;
+      flat_types(ph.type, tys);
+      Val v;
+      v.type = ph.type;
+      for (Ty t : tys) v.regs.push_back(fn_.reg(t));
+      vals_[ph.result] = v;
+      phis_[block].push_back(ph);
+    }
+  }
+  for (size_t i = begin; i < end; i++) {
+    const Insn& in = m_.insns[i];
+    if (in.opcode == OpFunctionParameter) return fail("entry point with parameters");
+    if (!do_insn(in)) return false;
+  }
+  return err_.empty();
+}
+
+std::string Translator::run() {
+  out_.iface.stage = stage_;
+  out_.entry = entry_name_;
+  if (!scan_module()) return err_;
+  if (!translate_entry()) return err_;
+  /* positions-only liveness: which vertex inputs feed gl_Position */
+  if (stage_ == Stage::Vertex) {
+    for (uint32_t off : live_inputs(fn_, 0, 16))
+      if (off < 128) out_.iface.pos_input_locations |= 1u << (off / 16);
+  }
+  return "";
+}
+
+}  // namespace
+
+std::string translate_spirv(const uint32_t* words, size_t count, Stage stage, const char* entry,
+                            const std::vector<std::pair<uint32_t, uint32_t>>& spec, Shader& out) {
+  Module m;
+  std::string e = decode(words, count, m);
+  if (!e.empty()) return e;
+  out = Shader();
+  Translator t(m, stage, entry ? entry : "main", spec, out);
+  return t.run();
+}
+
+std::vector<uint32_t> live_inputs(const Function& fn, uint32_t out_lo, uint32_t out_hi) {
+  std::vector<char> live(fn.regs.size(), 0);
+  bool changed = true;
+  auto mark = [&](int32_t r) {
+    if (r >= 0 && !live[(size_t)r]) {
+      live[(size_t)r] = 1;
+      changed = true;
+    }
+  };
+  while (changed) {
+    changed = false;
+    for (const Inst& i : fn.code) {
+      bool root = false;
+      switch (i.op) {
+        case Op::StOut: root = i.imm >= out_lo && i.imm < out_hi; break;
+        case Op::BraIf:
+        case Op::Kill: root = true; break;
+        default: break;
+      }
+      if (root || (i.dst >= 0 && live[(size_t)i.dst])) {
+        mark(i.a);
+        mark(i.b);
+        mark(i.c);
+      }
+    }
+  }
+  std::vector<uint32_t> offs;
+  for (const Inst& i : fn.code)
+    if (i.op == Op::LdIn && i.dst >= 0 && live[(size_t)i.dst]) offs.push_back(i.imm);
+  return offs;
+}
+
+}  // namespace ir
+}  // namespace kz

@@ -1,0 +1,388 @@
+"""Drive the kazan GB300 driver through its Vulkan entry points: the calls an application (or the Vulkan
+CTS through a loader) would make, issued directly against the ICD library.
+
+  r = Renderer()                          instance, device, queue, command pool
+  run = SceneRun(r, scene)                buffers, images, render pass, framebuffer, pipeline, command buffer
+  run.submit(); color, depth = run.read()
+"""
+import ctypes
+from ctypes import byref, c_float, c_uint32, c_uint64, c_void_p, pointer
+
+import numpy as np
+
+from . import vk
+from .vk import check
+
+
+class Buffer:
+    def __init__(self, handle, memory, size, host_visible):
+        self.handle, self.memory, self.size, self.host_visible = handle, memory, size, host_visible
+        self.mapped = None
+
+
+class Image:
+    def __init__(self, handle, memory, view, width, height, fmt, host_visible, pitch):
+        self.handle, self.memory, self.view = handle, memory, view
+        self.width, self.height, self.format, self.host_visible, self.pitch = width, height, fmt, host_visible, pitch
+        self.mapped = None
+
+
+class Renderer:
+    def __init__(self, driver=None):
+        self.drv = driver or vk.Driver()
+        d = self.drv
+        app = vk.VkApplicationInfo(vk.ST_APPLICATION_INFO, None, b"kazan_gb300", 1, b"kazan_gb300", 1,
+                                   (1 << 22) | (1 << 12))
+        ici = vk.VkInstanceCreateInfo(vk.ST_INSTANCE_CREATE_INFO, None, 0, pointer(app), 0, None, 0, None)
+        self.instance = c_void_p()
+        check("vkCreateInstance", d.vkCreateInstance(byref(ici), None, byref(self.instance)))
+        n = c_uint32(0)
+        check("vkEnumeratePhysicalDevices", d.vkEnumeratePhysicalDevices(self.instance, byref(n), None))
+        if n.value == 0:
+            d.vkDestroyInstance(self.instance, None)
+            raise RuntimeError("no GPU: the driver exposes no physical device")
+        pds = (c_void_p * n.value)()
+        check("vkEnumeratePhysicalDevices", d.vkEnumeratePhysicalDevices(self.instance, byref(n), pds))
+        self.physical = c_void_p(pds[0])
+        self.props = vk.VkPhysicalDeviceProperties()
+        d.vkGetPhysicalDeviceProperties(self.physical, byref(self.props))
+        mp = vk.VkPhysicalDeviceMemoryProperties()
+        d.vkGetPhysicalDeviceMemoryProperties(self.physical, byref(mp))
+        self.host_type = self.device_type = None
+        for i in range(mp.memoryTypeCount):
+            f = mp.memoryTypes[i].propertyFlags
+            if f & vk.MEMORY_PROPERTY_HOST_VISIBLE and self.host_type is None:
+                self.host_type = i
+            if f == vk.MEMORY_PROPERTY_DEVICE_LOCAL and self.device_type is None:
+                self.device_type = i
+        prio = c_float(1.0)
+        qci = vk.VkDeviceQueueCreateInfo(vk.ST_DEVICE_QUEUE_CREATE_INFO, None, 0, 0, 1, pointer(prio))
+        dci = vk.VkDeviceCreateInfo(vk.ST_DEVICE_CREATE_INFO, None, 0, 1, pointer(qci), 0, None, 0, None, None)
+        self.device = c_void_p()
+        check("vkCreateDevice", d.vkCreateDevice(self.physical, byref(dci), None, byref(self.device)))
+        self.queue = c_void_p()
+        d.vkGetDeviceQueue(self.device, 0, 0, byref(self.queue))
+        pci = vk.VkCommandPoolCreateInfo(vk.ST_COMMAND_POOL_CREATE_INFO, None, 0x2, 0)
+        self.pool = c_void_p()
+        check("vkCreateCommandPool", d.vkCreateCommandPool(self.device, byref(pci), None, byref(self.pool)))
+        fci = vk.VkFenceCreateInfo(vk.ST_FENCE_CREATE_INFO, None, 0)
+        self.fence = c_void_p()
+        check("vkCreateFence", d.vkCreateFence(self.device, byref(fci), None, byref(self.fence)))
+        self._objects = []
+
+    # ---------------------------------------------------------------------------------------------
+    def close(self):
+        d = self.drv
+        if self.device:
+            d.vkDeviceWaitIdle(self.device)
+            for kind, h in reversed(self._objects):
+                getattr(d, "vkDestroy" + kind if kind != "Memory" else "vkFreeMemory")(self.device, h, None)
+            self._objects = []
+            d.vkDestroyFence(self.device, self.fence, None)
+            d.vkDestroyCommandPool(self.device, self.pool, None)
+            d.vkDestroyDevice(self.device, None)
+            d.vkDestroyInstance(self.instance, None)
+            self.device = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def stream(self):
+        return self.drv.lib.kzGetQueueStream(self.queue)
+
+    # ---------------------------------------------------------------------------------------------
+    def _alloc(self, req, host_visible):
+        t = self.host_type if host_visible else self.device_type
+        ai = vk.VkMemoryAllocateInfo(vk.ST_MEMORY_ALLOCATE_INFO, None, req.size, t)
+        mem = c_void_p()
+        check("vkAllocateMemory", self.drv.vkAllocateMemory(self.device, byref(ai), None, byref(mem)))
+        self._objects.append(("Memory", mem))
+        return mem
+
+    def create_buffer(self, size, usage, host_visible=True):
+        d = self.drv
+        bci = vk.VkBufferCreateInfo(vk.ST_BUFFER_CREATE_INFO, None, 0, max(int(size), 4),
+                                    usage | vk.BUFFER_USAGE_TRANSFER_SRC | vk.BUFFER_USAGE_TRANSFER_DST, 0, 0, None)
+        h = c_void_p()
+        check("vkCreateBuffer", d.vkCreateBuffer(self.device, byref(bci), None, byref(h)))
+        req = vk.VkMemoryRequirements()
+        d.vkGetBufferMemoryRequirements(self.device, h, byref(req))
+        mem = self._alloc(req, host_visible)
+        check("vkBindBufferMemory", d.vkBindBufferMemory(self.device, h, mem, 0))
+        self._objects.append(("Buffer", h))
+        return Buffer(h, mem, int(size), host_visible)
+
+    def map(self, obj):
+        if obj.mapped is None:
+            p = c_void_p()
+            check("vkMapMemory", self.drv.vkMapMemory(self.device, obj.memory, 0, 0xFFFFFFFFFFFFFFFF, 0, byref(p)))
+            obj.mapped = p.value
+        return obj.mapped
+
+    def unmap(self, obj):
+        if obj.mapped is not None:
+            self.drv.vkUnmapMemory(self.device, obj.memory)
+            obj.mapped = None
+
+    def write_buffer(self, buf, array, keep_mapped=False):
+        a = np.ascontiguousarray(array)
+        if buf.host_visible:
+            p = self.map(buf)
+            ctypes.memmove(p, a.ctypes.data, a.nbytes)
+            if not keep_mapped:
+                self.unmap(buf)
+            return
+        staging = self.create_buffer(a.nbytes, 0, True)
+        self.write_buffer(staging, a)
+        cb = self.begin()
+        region = vk.VkBufferCopy(0, 0, a.nbytes)
+        self.drv.vkCmdCopyBuffer(cb, staging.handle, buf.handle, 1, byref(region))
+        self.end_submit_wait(cb)
+        self.free_command_buffer(cb)
+
+    def create_image(self, width, height, fmt, usage, host_visible=True):
+        d = self.drv
+        ici = vk.VkImageCreateInfo(vk.ST_IMAGE_CREATE_INFO, None, 0, vk.IMAGE_TYPE_2D, fmt,
+                                   vk.VkExtent3D(width, height, 1), 1, 1, vk.SAMPLE_COUNT_1,
+                                   vk.IMAGE_TILING_LINEAR if host_visible else vk.IMAGE_TILING_OPTIMAL,
+                                   usage | vk.IMAGE_USAGE_TRANSFER_SRC | vk.IMAGE_USAGE_TRANSFER_DST, 0, 0, None,
+                                   vk.IMAGE_LAYOUT_UNDEFINED)
+        h = c_void_p()
+        check("vkCreateImage", d.vkCreateImage(self.device, byref(ici), None, byref(h)))
+        req = vk.VkMemoryRequirements()
+        d.vkGetImageMemoryRequirements(self.device, h, byref(req))
+        mem = self._alloc(req, host_visible)
+        check("vkBindImageMemory", d.vkBindImageMemory(self.device, h, mem, 0))
+        self._objects.append(("Image", h))
+        aspect = vk.IMAGE_ASPECT_DEPTH if fmt == vk.FORMAT_D32_SFLOAT else vk.IMAGE_ASPECT_COLOR
+        vci = vk.VkImageViewCreateInfo(vk.ST_IMAGE_VIEW_CREATE_INFO, None, 0, h, vk.IMAGE_VIEW_TYPE_2D, fmt,
+                                       (ctypes.c_int * 4)(0, 0, 0, 0), vk.VkImageSubresourceRange(aspect, 0, 1, 0, 1))
+        view = c_void_p()
+        check("vkCreateImageView", d.vkCreateImageView(self.device, byref(vci), None, byref(view)))
+        self._objects.append(("ImageView", view))
+        sub = vk.VkImageSubresource(aspect, 0, 0)
+        lay = vk.VkSubresourceLayout()
+        d.vkGetImageSubresourceLayout(self.device, h, byref(sub), byref(lay))
+        return Image(h, mem, view, width, height, fmt, host_visible, lay.rowPitch)
+
+    def read_image(self, img):
+        n = img.pitch * img.height
+        if img.host_visible:
+            p = self.map(img)
+            raw = np.ctypeslib.as_array((ctypes.c_uint8 * n).from_address(p)).copy()
+        else:
+            staging = self.create_buffer(n, 0, True)
+            cb = self.begin()
+            aspect = vk.IMAGE_ASPECT_DEPTH if img.format == vk.FORMAT_D32_SFLOAT else vk.IMAGE_ASPECT_COLOR
+            region = vk.VkBufferImageCopy(0, 0, 0, vk.VkImageSubresourceLayers(aspect, 0, 0, 1),
+                                          vk.VkOffset3D(0, 0, 0), vk.VkExtent3D(img.width, img.height, 1))
+            self.drv.vkCmdCopyImageToBuffer(cb, img.handle, vk.IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, staging.handle, 1,
+                                            byref(region))
+            self.end_submit_wait(cb)
+            self.free_command_buffer(cb)
+            p = self.map(staging)
+            raw = np.ctypeslib.as_array((ctypes.c_uint8 * n).from_address(p)).copy()
+            self.unmap(staging)
+        raw = raw.reshape(img.height, img.pitch)
+        if img.format == vk.FORMAT_D32_SFLOAT:
+            return raw[:, :img.width * 4].copy().view(np.float32)
+        return raw[:, :img.width * 4].reshape(img.height, img.width, 4).copy()
+
+    # ---------------------------------------------------------------------------------------------
+    def begin(self):
+        d = self.drv
+        ai = vk.VkCommandBufferAllocateInfo(vk.ST_COMMAND_BUFFER_ALLOCATE_INFO, None, self.pool,
+                                            vk.COMMAND_BUFFER_LEVEL_PRIMARY, 1)
+        cb = c_void_p()
+        check("vkAllocateCommandBuffers", d.vkAllocateCommandBuffers(self.device, byref(ai), byref(cb)))
+        bi = vk.VkCommandBufferBeginInfo(vk.ST_COMMAND_BUFFER_BEGIN_INFO, None, 0, None)
+        check("vkBeginCommandBuffer", d.vkBeginCommandBuffer(cb, byref(bi)))
+        return cb
+
+    def free_command_buffer(self, cb):
+        self.drv.vkFreeCommandBuffers(self.device, self.pool, 1, byref(cb))
+
+    def submit(self, cb, fence=None):
+        arr = (c_void_p * 1)(cb)
+        si = vk.VkSubmitInfo(vk.ST_SUBMIT_INFO, None, 0, None, None, 1, arr, 0, None)
+        check("vkQueueSubmit", self.drv.vkQueueSubmit(self.queue, 1, byref(si), fence))
+
+    def wait(self, timeout_ns=60_000_000_000):
+        f = (c_void_p * 1)(self.fence)
+        check("vkWaitForFences", self.drv.vkWaitForFences(self.device, 1, f, 1, timeout_ns))
+        check("vkResetFences", self.drv.vkResetFences(self.device, 1, f))
+
+    def submit_wait(self, cb):
+        self.submit(cb, self.fence)
+        self.wait()
+
+    def end_submit_wait(self, cb):
+        check("vkEndCommandBuffer", self.drv.vkEndCommandBuffer(cb))
+        self.submit_wait(cb)
+
+    # ---------------------------------------------------------------------------------------------
+    def render_pass(self, color_fmt, depth, color_load=vk.LOAD_OP_CLEAR, depth_load=vk.LOAD_OP_CLEAR):
+        atts = (vk.VkAttachmentDescription * 2)()
+        atts[0] = vk.VkAttachmentDescription(0, color_fmt, 1, color_load, vk.STORE_OP_STORE, 2, 1,
+                                             vk.IMAGE_LAYOUT_UNDEFINED, vk.IMAGE_LAYOUT_GENERAL)
+        atts[1] = vk.VkAttachmentDescription(0, vk.FORMAT_D32_SFLOAT, 1, depth_load, vk.STORE_OP_STORE, 2, 1,
+                                             vk.IMAGE_LAYOUT_UNDEFINED, vk.IMAGE_LAYOUT_GENERAL)
+        cref = vk.VkAttachmentReference(0, vk.IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL)
+        dref = vk.VkAttachmentReference(1, vk.IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL)
+        sp = vk.VkSubpassDescription(0, vk.BIND_POINT_GRAPHICS, 0, None, 1, pointer(cref), None,
+                                     pointer(dref) if depth else None, 0, None)
+        rci = vk.VkRenderPassCreateInfo(vk.ST_RENDER_PASS_CREATE_INFO, None, 0, 2 if depth else 1, atts, 1,
+                                        pointer(sp), 0, None)
+        h = c_void_p()
+        check("vkCreateRenderPass", self.drv.vkCreateRenderPass(self.device, byref(rci), None, byref(h)))
+        self._objects.append(("RenderPass", h))
+        return h
+
+    def framebuffer(self, rp, views, width, height):
+        arr = (c_void_p * len(views))(*[v.value if isinstance(v, c_void_p) else v for v in views])
+        fci = vk.VkFramebufferCreateInfo(vk.ST_FRAMEBUFFER_CREATE_INFO, None, 0, rp, len(views), arr, width, height, 1)
+        h = c_void_p()
+        check("vkCreateFramebuffer", self.drv.vkCreateFramebuffer(self.device, byref(fci), None, byref(h)))
+        self._objects.append(("Framebuffer", h))
+        return h
+
+    def shader_module(self, words):
+        w = np.ascontiguousarray(words, dtype=np.uint32)
+        sci = vk.VkShaderModuleCreateInfo(vk.ST_SHADER_MODULE_CREATE_INFO, None, 0, w.nbytes, w.ctypes.data)
+        h = c_void_p()
+        check("vkCreateShaderModule", self.drv.vkCreateShaderModule(self.device, byref(sci), None, byref(h)))
+        self._objects.append(("ShaderModule", h))
+        return h
+
+    def pipeline_layout(self, push_bytes):
+        rng = vk.VkPushConstantRange(vk.SHADER_STAGE_VERTEX | vk.SHADER_STAGE_FRAGMENT, 0, push_bytes)
+        lci = vk.VkPipelineLayoutCreateInfo(vk.ST_PIPELINE_LAYOUT_CREATE_INFO, None, 0, 0, None,
+                                            1 if push_bytes else 0, pointer(rng) if push_bytes else None)
+        h = c_void_p()
+        check("vkCreatePipelineLayout", self.drv.vkCreatePipelineLayout(self.device, byref(lci), None, byref(h)))
+        self._objects.append(("PipelineLayout", h))
+        return h
+
+    def pipeline(self, scene, rp, layout, vs_words, fs_words):
+        vsm, fsm = self.shader_module(vs_words), self.shader_module(fs_words)
+        stages = (vk.VkPipelineShaderStageCreateInfo * 2)()
+        stages[0] = vk.VkPipelineShaderStageCreateInfo(vk.ST_PIPELINE_SHADER_STAGE_CREATE_INFO, None, 0,
+                                                       vk.SHADER_STAGE_VERTEX, vsm, b"main", None)
+        stages[1] = vk.VkPipelineShaderStageCreateInfo(vk.ST_PIPELINE_SHADER_STAGE_CREATE_INFO, None, 0,
+                                                       vk.SHADER_STAGE_FRAGMENT, fsm, b"main", None)
+        stride = scene.vertex_stride()
+        binding = vk.VkVertexInputBindingDescription(0, stride, vk.VERTEX_INPUT_RATE_VERTEX)
+        attrs = (vk.VkVertexInputAttributeDescription * 2)()
+        if scene.shader == "color":
+            attrs[0] = vk.VkVertexInputAttributeDescription(0, 0, vk.FORMAT_R32G32B32A32_SFLOAT, 0)
+            attrs[1] = vk.VkVertexInputAttributeDescription(1, 0, vk.FORMAT_R32G32B32A32_SFLOAT, 16)
+        else:
+            attrs[0] = vk.VkVertexInputAttributeDescription(0, 0, vk.FORMAT_R32G32B32_SFLOAT, 0)
+            attrs[1] = vk.VkVertexInputAttributeDescription(1, 0, vk.FORMAT_R32G32B32_SFLOAT, 12)
+        vis = vk.VkPipelineVertexInputStateCreateInfo(vk.ST_PIPELINE_VERTEX_INPUT_STATE_CREATE_INFO, None, 0, 1,
+                                                      pointer(binding), 2, attrs)
+        ias = vk.VkPipelineInputAssemblyStateCreateInfo(vk.ST_PIPELINE_INPUT_ASSEMBLY_STATE_CREATE_INFO, None, 0,
+                                                        vk.TOPOLOGY_TRIANGLE_LIST, 0)
+        vp = vk.VkViewport(0.0, 0.0, float(scene.width), float(scene.height), 0.0, 1.0)
+        sc = vk.VkRect2D(vk.VkOffset2D(0, 0), vk.VkExtent2D(scene.width, scene.height))
+        vps = vk.VkPipelineViewportStateCreateInfo(vk.ST_PIPELINE_VIEWPORT_STATE_CREATE_INFO, None, 0, 1,
+                                                   pointer(vp), 1, pointer(sc))
+        rs = vk.VkPipelineRasterizationStateCreateInfo(vk.ST_PIPELINE_RASTERIZATION_STATE_CREATE_INFO, None, 0, 0, 0,
+                                                       vk.POLYGON_MODE_FILL, scene.cull,
+                                                       vk.FRONT_FACE_CCW if scene.front_ccw else vk.FRONT_FACE_CW,
+                                                       0, 0.0, 0.0, 0.0, 1.0)
+        ms = vk.VkPipelineMultisampleStateCreateInfo(vk.ST_PIPELINE_MULTISAMPLE_STATE_CREATE_INFO, None, 0, 1, 0,
+                                                     0.0, None, 0, 0)
+        ds = vk.VkPipelineDepthStencilStateCreateInfo(vk.ST_PIPELINE_DEPTH_STENCIL_STATE_CREATE_INFO, None, 0,
+                                                      int(scene.depth_test), int(scene.depth_write),
+                                                      scene.depth_compare, 0, 0, vk.VkStencilOpState(),
+                                                      vk.VkStencilOpState(), 0.0, 1.0)
+        if scene.blend:
+            att = vk.VkPipelineColorBlendAttachmentState(1, vk.BLEND_SRC_ALPHA, vk.BLEND_ONE_MINUS_SRC_ALPHA,
+                                                         vk.BLEND_OP_ADD, vk.BLEND_SRC_ALPHA,
+                                                         vk.BLEND_ONE_MINUS_SRC_ALPHA, vk.BLEND_OP_ADD,
+                                                         vk.COLOR_MASK_RGBA)
+        else:
+            att = vk.VkPipelineColorBlendAttachmentState(0, vk.BLEND_ONE, vk.BLEND_ZERO, vk.BLEND_OP_ADD,
+                                                         vk.BLEND_ONE, vk.BLEND_ZERO, vk.BLEND_OP_ADD,
+                                                         vk.COLOR_MASK_RGBA)
+        cbs = vk.VkPipelineColorBlendStateCreateInfo(vk.ST_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO, None, 0, 0, 0, 1,
+                                                     pointer(att), (c_float * 4)(0, 0, 0, 0))
+        gci = vk.VkGraphicsPipelineCreateInfo(vk.ST_GRAPHICS_PIPELINE_CREATE_INFO, None, 0, 2, stages, pointer(vis),
+                                              pointer(ias), None, pointer(vps), pointer(rs), pointer(ms), pointer(ds),
+                                              pointer(cbs), None, layout, rp, 0, None, -1)
+        h = c_void_p()
+        check("vkCreateGraphicsPipelines",
+              self.drv.vkCreateGraphicsPipelines(self.device, None, 1, byref(gci), None, byref(h)))
+        self._objects.append(("Pipeline", h))
+        return h
+
+
+class SceneRun:
+    """GPU resources and a recorded command buffer for one scene."""
+
+    def __init__(self, r, scene, host_visible=False, mode=None, tile=None, keep_mapped=False):
+        self.r, self.scene = r, scene
+        d = r.drv
+        if mode is not None:
+            d.set_option("mode", mode)
+        if tile is not None:
+            d.set_option("tile", tile)
+        self.vb = r.create_buffer(scene.vertices.nbytes, vk.BUFFER_USAGE_VERTEX, host_visible)
+        r.write_buffer(self.vb, scene.vertices, keep_mapped=keep_mapped and host_visible)
+        self.ib = None
+        if scene.indexed:
+            self.ib = r.create_buffer(scene.indices.nbytes, vk.BUFFER_USAGE_INDEX, host_visible)
+            r.write_buffer(self.ib, scene.indices, keep_mapped=keep_mapped and host_visible)
+        self.color = r.create_image(scene.width, scene.height, vk.FORMAT_R8G8B8A8_UNORM,
+                                    vk.IMAGE_USAGE_COLOR_ATTACHMENT, host_visible)
+        self.depth = r.create_image(scene.width, scene.height, vk.FORMAT_D32_SFLOAT,
+                                    vk.IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT, host_visible)
+        self.rp = r.render_pass(vk.FORMAT_R8G8B8A8_UNORM, True)
+        self.fb = r.framebuffer(self.rp, [self.color.view, self.depth.view], scene.width, scene.height)
+        self.layout = r.pipeline_layout(64 if scene.shader == "lambert" else 0)
+        vs, fs = scene.shaders()
+        self.pipe = r.pipeline(scene, self.rp, self.layout, vs, fs)
+        self.cb = self.record()
+
+    def record(self):
+        r, s, d = self.r, self.scene, self.r.drv
+        cb = r.begin()
+        clears = (vk.VkClearValue * 2)()
+        clears[0].color.float32[:] = list(s.clear_color)
+        clears[1].depthStencil.depth = s.clear_depth
+        rbi = vk.VkRenderPassBeginInfo(vk.ST_RENDER_PASS_BEGIN_INFO, None, self.rp, self.fb,
+                                       vk.VkRect2D(vk.VkOffset2D(0, 0), vk.VkExtent2D(s.width, s.height)), 2, clears)
+        d.vkCmdBeginRenderPass(cb, byref(rbi), vk.SUBPASS_CONTENTS_INLINE)
+        d.vkCmdBindPipeline(cb, vk.BIND_POINT_GRAPHICS, self.pipe)
+        bufs = (c_void_p * 1)(self.vb.handle.value)
+        offs = (c_uint64 * 1)(0)
+        d.vkCmdBindVertexBuffers(cb, 0, 1, bufs, offs)
+        if self.ib is not None:
+            d.vkCmdBindIndexBuffer(cb, self.ib.handle, 0, vk.INDEX_TYPE_UINT32)
+        for dr in s.draws:
+            if dr.mvp is not None:
+                m = np.ascontiguousarray(dr.mvp, dtype=np.float32)
+                d.vkCmdPushConstants(cb, self.layout, vk.SHADER_STAGE_VERTEX, 0, 64, m.ctypes.data)
+            if s.indexed:
+                d.vkCmdDrawIndexed(cb, 3 * dr.count, 1, dr.first, dr.vertex_offset, 0)
+            else:
+                d.vkCmdDraw(cb, 3 * dr.count, 1, dr.first, 0)
+        d.vkCmdEndRenderPass(cb)
+        check("vkEndCommandBuffer", d.vkEndCommandBuffer(cb))
+        return cb
+
+    def submit(self, wait=True):
+        if wait:
+            self.r.submit_wait(self.cb)
+        else:
+            self.r.submit(self.cb)
+
+    def read(self):
+        return self.r.read_image(self.color), self.r.read_image(self.depth)
+
+    def stats(self):
+        return self.r.drv.stats(self.cb)

@@ -1,0 +1,182 @@
+"""Seeded synthetic scenes of the draw-path workloads (generators in csrc/scene/kz_scene.c).
+
+  small_soup      256x256, 2,048 non-indexed triangles, clip-space positions, pass-through colour shader,
+                  depth LESS with writes, no culling, no blending (seed 1)
+  single_large    1920x1080, 1,000,000 indexed triangles of a jittered latitude/longitude sphere mesh,
+                  MVP push constant, Lambert fragment shader, back-face culling (seed 2)
+  batched         2048x2048, 4,096 indexed draws with log-uniform triangle counts in [16, 65536], each its
+                  own sphere mesh and MVP (random rotation, translation in [-5,5]^3) (seed 3)
+  ordered_blend   1920x1080, 200,000 triangles with log-uniform pixel area in [4, 4096], alpha 0.5,
+                  SRC_ALPHA / ONE_MINUS_SRC_ALPHA blending, depth LESS with writes off (seed 4)
+Each generator takes its size parameters so tests can run the same scene family at smaller sizes.
+"""
+import ctypes
+import os
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import spirv_asm
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+# camera distance of the single-large-draw sphere; puts the mean screen area of all triangles
+# (front and back facing) at about 8 pixels on 1920x1080 (kz_scene.c kz_mvp_single)
+SINGLE_DISTANCE = 1.30
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(PKG, "_build", "libkz_scene.so")
+        if not os.path.exists(path):
+            raise RuntimeError("libkz_scene.so is not built (run __graft_entry__.build())")
+        L = ctypes.CDLL(path)
+        f32p = ctypes.POINTER(ctypes.c_float)
+        u32p = ctypes.POINTER(ctypes.c_uint32)
+        L.kz_scene_soup.argtypes = [ctypes.c_uint64, ctypes.c_uint32, f32p]
+        L.kz_scene_blend.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                     ctypes.c_float, ctypes.c_float, ctypes.c_float, f32p]
+        L.kz_mesh_dims.argtypes = [ctypes.c_uint32, u32p, u32p]
+        L.kz_mesh_vertex_count.argtypes = [ctypes.c_uint32]
+        L.kz_mesh_vertex_count.restype = ctypes.c_uint32
+        L.kz_mesh_sphere.argtypes = [ctypes.c_uint64, ctypes.c_uint32, f32p, u32p]
+        L.kz_mvp_single.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, f32p]
+        L.kz_mvp_batched.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, f32p]
+        L.kz_batched_counts.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, u32p]
+        L.kz_batched_counts.restype = ctypes.c_uint64
+        L.kz_rng_floats.argtypes = [ctypes.c_uint64, ctypes.c_uint32, f32p]
+        L.kz_rng_first.argtypes = [ctypes.c_uint64]
+        L.kz_rng_first.restype = ctypes.c_uint32
+        _LIB = L
+    return _LIB
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _up(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+
+@dataclass
+class Draw:
+    first: int                 # firstVertex (non-indexed) or firstIndex (indexed)
+    count: int                 # triangles
+    vertex_offset: int = 0     # vkCmdDrawIndexed vertexOffset
+    mvp: Optional[np.ndarray] = None  # column-major float32[16] push constant (Lambert)
+
+
+@dataclass
+class Scene:
+    name: str
+    width: int
+    height: int
+    shader: str                # "color" or "lambert"
+    vertices: np.ndarray       # float32 [V, 8] (color) or [V, 6] (lambert)
+    indices: Optional[np.ndarray]
+    draws: List[Draw]
+    cull: int = 0
+    front_ccw: bool = True
+    depth_test: bool = True
+    depth_write: bool = True
+    depth_compare: int = 1     # VK_COMPARE_OP_LESS
+    blend: bool = False
+    clear_color: tuple = (0.0, 0.0, 0.0, 1.0)
+    clear_depth: float = 1.0
+    fs_words: Optional[np.ndarray] = field(default=None, repr=False)  # overrides the default fragment shader
+
+    @property
+    def triangles(self):
+        return sum(d.count for d in self.draws)
+
+    @property
+    def indexed(self):
+        return self.indices is not None
+
+    def vertex_stride(self):
+        return self.vertices.shape[1] * 4
+
+    def shaders(self):
+        if self.shader == "color":
+            vs, fs = spirv_asm.color_vs(), spirv_asm.color_fs()
+        else:
+            vs, fs = spirv_asm.lambert_vs(), spirv_asm.lambert_fs()
+        if self.fs_words is not None:
+            fs = self.fs_words
+        return vs, fs
+
+    def algorithmic_bytes(self):
+        """B = 12 T_indexed + S_v V + 64 draws + W H (colour + depth traffic)"""
+        t_idx = self.triangles if self.indexed else 0
+        v = len(self.vertices) if self.indexed else 3 * self.triangles
+        push = 64 * len(self.draws) if self.shader == "lambert" else 0
+        fb = self.width * self.height * ((4 + 4) * 2 if self.depth_write else (2 * 4 + 4))
+        return 12 * t_idx + self.vertex_stride() * v + push + fb
+
+
+def small_soup(seed=1, n=2048, width=256, height=256):
+    v = np.empty((3 * n, 8), dtype=np.float32)
+    lib().kz_scene_soup(seed, n, _fp(v))
+    return Scene("small_soup", width, height, "color", v, None, [Draw(0, n)], cull=0)
+
+
+def sphere_mesh(seed, tris):
+    nv = lib().kz_mesh_vertex_count(tris)
+    v = np.empty((nv, 6), dtype=np.float32)
+    idx = np.empty(3 * tris, dtype=np.uint32)
+    lib().kz_mesh_sphere(seed, tris, _fp(v), _up(idx))
+    return v, idx
+
+
+def mvp_single(width, height, dist=SINGLE_DISTANCE):
+    m = np.empty(16, dtype=np.float32)
+    lib().kz_mvp_single(width, height, dist, _fp(m))
+    return m
+
+
+def single_large(seed=2, tris=1_000_000, width=1920, height=1080, dist=SINGLE_DISTANCE):
+    v, idx = sphere_mesh(seed, tris)
+    return Scene("single_large", width, height, "lambert", v, idx,
+                 [Draw(0, tris, 0, mvp_single(width, height, dist))], cull=2)
+
+
+def batched_counts(seed=3, ndraws=4096, lo=16, hi=65536):
+    c = np.empty(ndraws, dtype=np.uint32)
+    lib().kz_batched_counts(seed, ndraws, lo, hi, _up(c))
+    return c
+
+
+def batched(seed=3, ndraws=4096, width=2048, height=2048, lo=16, hi=65536):
+    counts = batched_counts(seed, ndraws, lo, hi)
+    verts, inds, draws = [], [], []
+    vbase = ibase = 0
+    for i, t in enumerate(counts):
+        v, idx = sphere_mesh(seed ^ (i + 1), int(t))
+        m = np.empty(16, dtype=np.float32)
+        lib().kz_mvp_batched(seed, i, width, height, _fp(m))
+        verts.append(v)
+        inds.append(idx)
+        draws.append(Draw(ibase, int(t), vbase, m))
+        vbase += len(v)
+        ibase += len(idx)
+    return Scene("batched", width, height, "lambert", np.concatenate(verts), np.concatenate(inds), draws, cull=2)
+
+
+def ordered_blend(seed=4, n=200_000, width=1920, height=1080, amin=4.0, amax=4096.0, alpha=0.5):
+    v = np.empty((3 * n, 8), dtype=np.float32)
+    lib().kz_scene_blend(seed, n, width, height, amin, amax, alpha, _fp(v))
+    return Scene("ordered_blend", width, height, "color", v, None, [Draw(0, n)], cull=0, depth_test=True,
+                 depth_write=False, blend=True)
+
+
+def triangles_from(vertices_xyzw_rgba, width, height, **state):
+    """a hand-made non-indexed colour scene (tests)"""
+    v = np.ascontiguousarray(vertices_xyzw_rgba, dtype=np.float32).reshape(-1, 8)
+    s = Scene("custom", width, height, "color", v, None, [Draw(0, len(v) // 3)])
+    for k, val in state.items():
+        setattr(s, k, val)
+    return s

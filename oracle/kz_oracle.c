@@ -1,0 +1,570 @@
+/*
+ * kz_oracle.c - CPU oracle for the kazan draw path.  TEST INFRASTRUCTURE ONLY (see kz_oracle.h).
+ * PARITY UNPINNED: no reference rasteriser exists (vulkan-driver/src/api_impl.rs:4632-4653 are stubs);
+ * the rules restated here are the Vulkan specification's "Rasterization" and "Fragment operations"
+ * chapters with the open choices fixed as listed in kz_oracle.h.
+ *
+ * Build: gcc -O2 -ffp-contract=off -fPIC -shared -pthread (see oracle/Makefile).
+ */
+#include "kz_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define KZO_MAXK 4        /* varyings per vertex for the two shaders (rgba or normal xyz) */
+#define KZO_G 4.0f        /* guard band factor */
+#define KZO_MAXPOLY 9
+
+/* Vulkan enumerant values used below (from the specification) */
+enum { CMP_NEVER, CMP_LESS, CMP_EQUAL, CMP_LEQUAL, CMP_GREATER, CMP_NOTEQUAL, CMP_GEQUAL, CMP_ALWAYS };
+enum {
+  BF_ZERO, BF_ONE, BF_SRC_COLOR, BF_ONE_MINUS_SRC_COLOR, BF_DST_COLOR, BF_ONE_MINUS_DST_COLOR, BF_SRC_ALPHA,
+  BF_ONE_MINUS_SRC_ALPHA, BF_DST_ALPHA, BF_ONE_MINUS_DST_ALPHA, BF_CONSTANT_COLOR, BF_ONE_MINUS_CONSTANT_COLOR,
+  BF_CONSTANT_ALPHA, BF_ONE_MINUS_CONSTANT_ALPHA, BF_SRC_ALPHA_SATURATE
+};
+enum { BO_ADD, BO_SUBTRACT, BO_REVERSE_SUBTRACT, BO_MIN, BO_MAX };
+
+uint8_t kzo_unorm8(float v) {
+  float c = fminf(fmaxf(v, 0.0f), 1.0f);
+  return (uint8_t)(int)rintf(c * 255.0f);
+}
+
+static float u8_to_f32(uint8_t u) { return (float)u / 255.0f; }
+
+/* ---- shaders (the SPIR-V semantics the PTX backend implements, restated in C) ---- */
+
+typedef struct {
+  float c[4 + KZO_MAXK]; /* clip position x,y,z,w then varyings */
+} cvert;
+
+static int shader_varyings(const kzo_draw* d) { return d->shader == KZO_SHADER_COLOR ? 4 : 3; }
+
+/* vertex shader: COLOR is gl_Position = in0, out0 = in1; LAMBERT is gl_Position = mvp * vec4(in0, 1),
+ * out0 = in1.  OpMatrixTimesVector is r_i = fma(m3i, v3, fma(m2i, v2, fma(m1i, v1, m0i * v0))). */
+static void run_vs(const kzo_draw* d, uint32_t vid, cvert* out) {
+  if (d->shader == KZO_SHADER_COLOR) {
+    const float* v = d->vertices + (size_t)vid * 8;
+    for (int i = 0; i < 8; i++) out->c[i] = v[i];
+  } else {
+    const float* v = d->vertices + (size_t)vid * 6;
+    const float* m = d->mvp;
+    float in[4] = {v[0], v[1], v[2], 1.0f};
+    for (int i = 0; i < 4; i++) {
+      float t = m[0 * 4 + i] * in[0];
+      t = fmaf(m[1 * 4 + i], in[1], t);
+      t = fmaf(m[2 * 4 + i], in[2], t);
+      t = fmaf(m[3 * 4 + i], in[3], t);
+      out->c[i] = t;
+    }
+    out->c[4] = v[3];
+    out->c[5] = v[4];
+    out->c[6] = v[5];
+    out->c[7] = 0.0f;
+  }
+}
+
+/* fragment shader: COLOR writes the varying; LAMBERT writes
+ * vec4(albedo * max(dot(normalize(n), L), 0), 1) with
+ * dot(a, b) = fma(a2, b2, fma(a1, b1, a0 * b0)) and normalize(x) = x * (1 / sqrt(dot(x, x))). */
+static void run_fs(const kzo_draw* d, const float* var, float out[4]) {
+  if (d->shader == KZO_SHADER_COLOR) {
+    for (int i = 0; i < 4; i++) out[i] = var[i];
+  } else {
+    float n0 = var[0], n1 = var[1], n2 = var[2];
+    float dd = fmaf(n2, n2, fmaf(n1, n1, n0 * n0));
+    float len = sqrtf(dd);
+    float inv = 1.0f / len;
+    float m0 = n0 * inv, m1 = n1 * inv, m2 = n2 * inv;
+    float dl = fmaf(m2, d->light[2], fmaf(m1, d->light[1], m0 * d->light[0]));
+    dl = fmaxf(dl, 0.0f);
+    out[0] = d->albedo[0] * dl;
+    out[1] = d->albedo[1] * dl;
+    out[2] = d->albedo[2] * dl;
+    out[3] = 1.0f;
+  }
+}
+
+/* ---- clipping ---- */
+
+static float plane_dist(const float* p, int plane) {
+  switch (plane) {
+    case 0: return p[2];                  /* z >= 0 */
+    case 1: return p[3] - p[2];           /* z <= w */
+    case 2: return p[0] + KZO_G * p[3];   /* x >= -4w */
+    case 3: return KZO_G * p[3] - p[0];   /* x <= 4w */
+    case 4: return p[1] + KZO_G * p[3];   /* y >= -4w */
+    default: return KZO_G * p[3] - p[1];  /* y <= 4w */
+  }
+}
+
+/* returns the number of polygon vertices (0 = rejected) */
+static int clip_polygon(const cvert in[3], int nc, cvert poly[KZO_MAXPOLY]) {
+  cvert a[KZO_MAXPOLY], b[KZO_MAXPOLY];
+  int n = 3;
+  for (int i = 0; i < 3; i++) a[i] = in[i];
+  cvert* cur = a;
+  cvert* nxt = b;
+  for (int plane = 0; plane < 6; plane++) {
+    int any_out = 0;
+    for (int i = 0; i < n; i++)
+      if (plane_dist(cur[i].c, plane) < 0.0f) any_out = 1;
+    if (!any_out) continue;
+    int m = 0;
+    for (int i = 0; i < n; i++) {
+      const cvert* p = &cur[i];
+      const cvert* q = &cur[(i + 1) % n];
+      float dp = plane_dist(p->c, plane), dq = plane_dist(q->c, plane);
+      int pin = dp >= 0.0f, qin = dq >= 0.0f;
+      if (pin) nxt[m++] = *p;
+      if (pin != qin) {
+        const cvert* vi = pin ? p : q;
+        const cvert* vo = pin ? q : p;
+        float di = pin ? dp : dq, dout = pin ? dq : dp;
+        float t = di / (di - dout);
+        cvert c;
+        for (int k = 0; k < 4 + nc; k++) c.c[k] = fmaf(t, vo->c[k] - vi->c[k], vi->c[k]);
+        nxt[m++] = c;
+      }
+    }
+    n = m;
+    cvert* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+    if (n < 3) return 0;
+  }
+  for (int i = 0; i < n; i++) {
+    if (!(cur[i].c[3] > 0.0f)) return 0;
+    poly[i] = cur[i];
+  }
+  return n;
+}
+
+/* ---- prepared (sub-)triangle ---- */
+
+typedef struct {
+  int32_t X[3], Y[3];
+  int64_t S;
+  float inv_s;
+  float z0, dz1, dz2;
+  float iw[3];
+  float a[3][KZO_MAXK]; /* varying * (1/w) */
+  int tl[3];
+  int32_t bx0, by0, bx1, by1; /* inclusive pixel box */
+  int front;
+  uint32_t draw;
+} prep;
+
+typedef struct {
+  prep* v;
+  size_t n, cap;
+  kzo_stats st;
+} prep_list;
+
+static void push_prep(prep_list* l, const prep* p) {
+  if (l->n == l->cap) {
+    l->cap = l->cap ? l->cap * 2 : 1024;
+    l->v = (prep*)realloc(l->v, l->cap * sizeof(prep));
+  }
+  l->v[l->n++] = *p;
+}
+
+static int64_t floordiv256(int64_t a) { return a >= 0 ? a / 256 : -((-a + 255) / 256); }
+
+void kzo_draw_rect(uint32_t width, uint32_t height, const int32_t area[4], const kzo_draw* d, int32_t out[4]) {
+  int32_t x0 = 0, y0 = 0, x1 = (int32_t)width, y1 = (int32_t)height;
+  if (area[0] > x0) x0 = area[0];
+  if (area[1] > y0) y0 = area[1];
+  if (area[2] < x1) x1 = area[2];
+  if (area[3] < y1) y1 = area[3];
+  if (d->scissor[0] > x0) x0 = d->scissor[0];
+  if (d->scissor[1] > y0) y0 = d->scissor[1];
+  if (d->scissor[0] + d->scissor[2] < x1) x1 = d->scissor[0] + d->scissor[2];
+  if (d->scissor[1] + d->scissor[3] < y1) y1 = d->scissor[1] + d->scissor[3];
+  /* pixel x is inside the viewport iff x + 0.5 lies in [vx, vx + vw) */
+  float vx = d->viewport[0], vy = d->viewport[1], vw = d->viewport[2], vh = d->viewport[3];
+  float ylo = vh >= 0.0f ? vy : vy + vh, yhi = vh >= 0.0f ? vy + vh : vy;
+  int32_t px0 = (int32_t)ceilf(vx - 0.5f), px1 = (int32_t)ceilf(vx + vw - 0.5f);
+  int32_t py0 = (int32_t)ceilf(ylo - 0.5f), py1 = (int32_t)ceilf(yhi - 0.5f);
+  if (px0 > x0) x0 = px0;
+  if (py0 > y0) y0 = py0;
+  if (px1 < x1) x1 = px1;
+  if (py1 < y1) y1 = py1;
+  out[0] = x0;
+  out[1] = y0;
+  out[2] = x1;
+  out[3] = y1;
+}
+
+/* project + snap + cull + orient one (sub-)triangle; appends to the list if it can produce fragments */
+static void setup_tri(const kzo_draw* d, uint32_t di, const int32_t rect[4], const cvert v[3], int nc,
+                      prep_list* out) {
+  float hx = 0.5f * d->viewport[2], ox = d->viewport[0] + hx;
+  float hy = 0.5f * d->viewport[3], oy = d->viewport[1] + hy;
+  float pz = d->viewport[5] - d->viewport[4], oz = d->viewport[4];
+  prep p;
+  float zf[3];
+  memset(&p, 0, sizeof(p));
+  for (int i = 0; i < 3; i++) {
+    float iw = 1.0f / v[i].c[3];
+    float xd = v[i].c[0] * iw, yd = v[i].c[1] * iw, zd = v[i].c[2] * iw;
+    float xf = fmaf(xd, hx, ox), yf = fmaf(yd, hy, oy);
+    zf[i] = fmaf(zd, pz, oz);
+    p.X[i] = (int32_t)rintf(xf * 256.0f);
+    p.Y[i] = (int32_t)rintf(yf * 256.0f);
+    p.iw[i] = iw;
+    for (int k = 0; k < nc; k++) p.a[i][k] = v[i].c[4 + k] * iw;
+  }
+  int64_t S = (int64_t)(p.X[1] - p.X[0]) * (p.Y[2] - p.Y[0]) - (int64_t)(p.X[2] - p.X[0]) * (p.Y[1] - p.Y[0]);
+  if (S == 0) {
+    out->st.rejected++;
+    return;
+  }
+  int front = d->front_ccw ? (S < 0) : (S > 0);
+  if (((d->cull_mode & 2u) && !front) || ((d->cull_mode & 1u) && front)) {
+    out->st.rejected++;
+    return;
+  }
+  if (S < 0) {
+    int32_t t;
+    float f;
+    t = p.X[1]; p.X[1] = p.X[2]; p.X[2] = t;
+    t = p.Y[1]; p.Y[1] = p.Y[2]; p.Y[2] = t;
+    f = zf[1]; zf[1] = zf[2]; zf[2] = f;
+    f = p.iw[1]; p.iw[1] = p.iw[2]; p.iw[2] = f;
+    for (int k = 0; k < nc; k++) {
+      f = p.a[1][k];
+      p.a[1][k] = p.a[2][k];
+      p.a[2][k] = f;
+    }
+    S = -S;
+  }
+  int32_t minx = p.X[0], maxx = p.X[0], miny = p.Y[0], maxy = p.Y[0];
+  for (int i = 1; i < 3; i++) {
+    if (p.X[i] < minx) minx = p.X[i];
+    if (p.X[i] > maxx) maxx = p.X[i];
+    if (p.Y[i] < miny) miny = p.Y[i];
+    if (p.Y[i] > maxy) maxy = p.Y[i];
+  }
+  int64_t bx0 = -floordiv256(-((int64_t)minx - 128)); /* ceil((minx - 128) / 256) */
+  int64_t by0 = -floordiv256(-((int64_t)miny - 128));
+  int64_t bx1 = floordiv256((int64_t)maxx - 128);
+  int64_t by1 = floordiv256((int64_t)maxy - 128);
+  if (bx0 < rect[0]) bx0 = rect[0];
+  if (by0 < rect[1]) by0 = rect[1];
+  if (bx1 > rect[2] - 1) bx1 = rect[2] - 1;
+  if (by1 > rect[3] - 1) by1 = rect[3] - 1;
+  if (bx0 > bx1 || by0 > by1) {
+    out->st.rejected++;
+    return;
+  }
+  p.bx0 = (int32_t)bx0;
+  p.by0 = (int32_t)by0;
+  p.bx1 = (int32_t)bx1;
+  p.by1 = (int32_t)by1;
+  for (int e = 0; e < 3; e++) {
+    int a = (e + 1) % 3, b = (e + 2) % 3; /* edge e is opposite vertex e: v(e+1) -> v(e+2) */
+    int32_t dx = p.X[b] - p.X[a], dy = p.Y[b] - p.Y[a];
+    p.tl[e] = (dy < 0) || (dy == 0 && dx > 0);
+  }
+  p.S = S;
+  p.inv_s = 1.0f / (float)S;
+  p.z0 = zf[0];
+  p.dz1 = zf[1] - zf[0];
+  p.dz2 = zf[2] - zf[0];
+  p.front = front;
+  p.draw = di;
+  out->st.subtris++;
+  push_prep(out, &p);
+}
+
+static void process_triangle(const kzo_draw* d, uint32_t di, const int32_t rect[4], uint32_t t, prep_list* out) {
+  uint32_t vid[3];
+  for (int j = 0; j < 3; j++) {
+    if (d->indices)
+      vid[j] = (uint32_t)((int64_t)d->indices[d->first + 3 * t + j] + d->vertex_offset);
+    else
+      vid[j] = d->first + 3 * t + (uint32_t)j;
+  }
+  int nc = shader_varyings(d);
+  cvert v[3];
+  for (int j = 0; j < 3; j++) run_vs(d, vid[j], &v[j]);
+  out->st.tris++;
+  for (int j = 0; j < 3; j++)
+    for (int k = 0; k < 4; k++)
+      if (!isfinite(v[j].c[k])) {
+        out->st.rejected++;
+        return;
+      }
+  /* trivial reject against the view volume -w <= x,y <= w, 0 <= z <= w */
+  int all[6] = {1, 1, 1, 1, 1, 1};
+  for (int j = 0; j < 3; j++) {
+    const float* c = v[j].c;
+    all[0] &= c[0] > c[3];
+    all[1] &= c[0] < -c[3];
+    all[2] &= c[1] > c[3];
+    all[3] &= c[1] < -c[3];
+    all[4] &= c[2] < 0.0f;
+    all[5] &= c[2] > c[3];
+  }
+  if (all[0] | all[1] | all[2] | all[3] | all[4] | all[5]) {
+    out->st.rejected++;
+    return;
+  }
+  int need = 0;
+  for (int j = 0; j < 3; j++)
+    for (int plane = 0; plane < 6; plane++)
+      if (plane_dist(v[j].c, plane) < 0.0f) need = 1;
+  if (!need) {
+    setup_tri(d, di, rect, v, nc, out);
+    return;
+  }
+  out->st.clipped++;
+  cvert poly[KZO_MAXPOLY];
+  int n = clip_polygon(v, nc, poly);
+  if (n == 0) {
+    out->st.rejected++;
+    return;
+  }
+  for (int i = 1; i + 1 < n; i++) {
+    cvert tri[3] = {poly[0], poly[i], poly[i + 1]};
+    setup_tri(d, di, rect, tri, nc, out);
+  }
+}
+
+static int depth_cmp(uint32_t op, float z, float d) {
+  switch (op) {
+    case CMP_NEVER: return 0;
+    case CMP_LESS: return z < d;
+    case CMP_EQUAL: return z == d;
+    case CMP_LEQUAL: return z <= d;
+    case CMP_GREATER: return z > d;
+    case CMP_NOTEQUAL: return z != d;
+    case CMP_GEQUAL: return z >= d;
+    default: return 1;
+  }
+}
+
+static float blend_factor(uint32_t f, int c, const float s[4], const float dst[4], const float k[4]) {
+  switch (f) {
+    case BF_ZERO: return 0.0f;
+    case BF_ONE: return 1.0f;
+    case BF_SRC_COLOR: return s[c];
+    case BF_ONE_MINUS_SRC_COLOR: return 1.0f - s[c];
+    case BF_DST_COLOR: return dst[c];
+    case BF_ONE_MINUS_DST_COLOR: return 1.0f - dst[c];
+    case BF_SRC_ALPHA: return s[3];
+    case BF_ONE_MINUS_SRC_ALPHA: return 1.0f - s[3];
+    case BF_DST_ALPHA: return dst[3];
+    case BF_ONE_MINUS_DST_ALPHA: return 1.0f - dst[3];
+    case BF_CONSTANT_COLOR: return k[c];
+    case BF_ONE_MINUS_CONSTANT_COLOR: return 1.0f - k[c];
+    case BF_CONSTANT_ALPHA: return k[3];
+    case BF_ONE_MINUS_CONSTANT_ALPHA: return 1.0f - k[3];
+    case BF_SRC_ALPHA_SATURATE: return c < 3 ? fminf(s[3], 1.0f - dst[3]) : 1.0f;
+    default: return 0.0f;
+  }
+}
+
+static float blend_op(uint32_t op, float s, float sf, float d, float df) {
+  switch (op) {
+    case BO_ADD: return fmaf(s, sf, d * df);
+    case BO_SUBTRACT: return fmaf(s, sf, -(d * df));
+    case BO_REVERSE_SUBTRACT: return fmaf(d, df, -(s * sf));
+    case BO_MIN: return fminf(s, d);
+    default: return fmaxf(s, d);
+  }
+}
+
+/* rasterise one prepared triangle over rows [ylo, yhi) */
+static void raster_prep(const kzo_draw* draws, const prep* p, uint32_t width, uint8_t* color, float* depth,
+                        int32_t ylo, int32_t yhi, kzo_stats* st) {
+  const kzo_draw* d = &draws[p->draw];
+  int nc = shader_varyings(d);
+  int32_t y0 = p->by0 > ylo ? p->by0 : ylo, y1 = p->by1 < yhi - 1 ? p->by1 : yhi - 1;
+  float zmin = fminf(d->viewport[4], d->viewport[5]), zmax = fmaxf(d->viewport[4], d->viewport[5]);
+  for (int32_t y = y0; y <= y1; y++) {
+    int64_t py = (int64_t)y * 256 + 128;
+    for (int32_t x = p->bx0; x <= p->bx1; x++) {
+      int64_t px = (int64_t)x * 256 + 128;
+      int64_t E[3];
+      int inside = 1;
+      for (int e = 0; e < 3; e++) {
+        int a = (e + 1) % 3, b = (e + 2) % 3;
+        E[e] = (int64_t)(p->X[b] - p->X[a]) * (py - p->Y[a]) - (int64_t)(p->Y[b] - p->Y[a]) * (px - p->X[a]);
+        if (!(E[e] > 0 || (E[e] == 0 && p->tl[e]))) inside = 0;
+      }
+      if (!inside) continue;
+      st->fragments++;
+      float l0 = (float)E[0] * p->inv_s, l1 = (float)E[1] * p->inv_s, l2 = (float)E[2] * p->inv_s;
+      float z = fmaf(l2, p->dz2, fmaf(l1, p->dz1, p->z0));
+      z = fminf(fmaxf(z, zmin), zmax);
+      z = z + 0.0f;
+      size_t pix = (size_t)y * width + (size_t)x;
+      if (d->depth_test && depth) {
+        if (!depth_cmp(d->depth_compare, z, depth[pix])) continue;
+      }
+      st->depth_pass++;
+      float q = fmaf(l2, p->iw[2], fmaf(l1, p->iw[1], l0 * p->iw[0]));
+      float rq = 1.0f / q;
+      float var[KZO_MAXK];
+      for (int k = 0; k < nc; k++) {
+        float num = fmaf(l2, p->a[2][k], fmaf(l1, p->a[1][k], l0 * p->a[0][k]));
+        var[k] = num * rq;
+      }
+      float out[4];
+      run_fs(d, var, out);
+      if (d->depth_test && d->depth_write && depth) depth[pix] = z;
+      uint8_t* c = color + pix * 4;
+      if (d->blend_enable) {
+        float s[4], dst[4];
+        for (int i = 0; i < 4; i++) {
+          s[i] = fminf(fmaxf(out[i], 0.0f), 1.0f);
+          dst[i] = u8_to_f32(c[i]);
+        }
+        for (int i = 0; i < 4; i++) {
+          if (!(d->write_mask & (1u << i))) continue;
+          float r;
+          if (i < 3)
+            r = blend_op(d->color_op, s[i], blend_factor(d->src_color, i, s, dst, d->blend_const), dst[i],
+                         blend_factor(d->dst_color, i, s, dst, d->blend_const));
+          else
+            r = blend_op(d->alpha_op, s[3], blend_factor(d->src_alpha, 3, s, dst, d->blend_const), dst[3],
+                         blend_factor(d->dst_alpha, 3, s, dst, d->blend_const));
+          c[i] = kzo_unorm8(r);
+        }
+      } else {
+        for (int i = 0; i < 4; i++)
+          if (d->write_mask & (1u << i)) c[i] = kzo_unorm8(out[i]);
+      }
+    }
+  }
+}
+
+/* ---- drivers: sequential and banded-parallel ---- */
+
+typedef struct {
+  const kzo_draw* draws;
+  uint32_t num_draws;
+  const int32_t (*rects)[4];
+  const uint64_t* tri_base; /* prefix sums of triangle counts */
+  uint64_t t0, t1;
+  prep_list list;
+} setup_job;
+
+static void* setup_worker(void* arg) {
+  setup_job* j = (setup_job*)arg;
+  uint32_t di = 0;
+  for (uint64_t g = j->t0; g < j->t1; g++) {
+    while (g >= j->tri_base[di + 1]) di++;
+    process_triangle(&j->draws[di], di, j->rects[di], (uint32_t)(g - j->tri_base[di]), &j->list);
+  }
+  return NULL;
+}
+
+typedef struct {
+  const kzo_draw* draws;
+  setup_job* jobs;
+  int njobs;
+  uint32_t width;
+  uint8_t* color;
+  float* depth;
+  int32_t ylo, yhi;
+  kzo_stats st;
+} raster_job;
+
+static void* raster_worker(void* arg) {
+  raster_job* r = (raster_job*)arg;
+  for (int j = 0; j < r->njobs; j++) {
+    const prep_list* l = &r->jobs[j].list;
+    for (size_t i = 0; i < l->n; i++) {
+      const prep* p = &l->v[i];
+      if (p->by1 < r->ylo || p->by0 >= r->yhi) continue;
+      raster_prep(r->draws, p, r->width, r->color, r->depth, r->ylo, r->yhi, &r->st);
+    }
+  }
+  return NULL;
+}
+
+int kzo_render(uint32_t width, uint32_t height, uint8_t* color, float* depth, const int32_t render_area[4],
+               uint32_t num_draws, const kzo_draw* draws, int nthreads, kzo_stats* stats) {
+  if (nthreads < 1) nthreads = 1;
+  uint64_t* base = (uint64_t*)calloc(num_draws + 1, sizeof(uint64_t));
+  int32_t(*rects)[4] = (int32_t(*)[4])calloc(num_draws ? num_draws : 1, sizeof(int32_t[4]));
+  if (!base || !rects) return -1;
+  for (uint32_t i = 0; i < num_draws; i++) {
+    base[i + 1] = base[i] + draws[i].tri_count;
+    kzo_draw_rect(width, height, render_area, &draws[i], rects[i]);
+  }
+  uint64_t total = base[num_draws];
+  int nsetup = nthreads;
+  if ((uint64_t)nsetup > total) nsetup = total ? (int)total : 1;
+  setup_job* jobs = (setup_job*)calloc((size_t)nsetup, sizeof(setup_job));
+  pthread_t* th = (pthread_t*)calloc((size_t)(nthreads > nsetup ? nthreads : nsetup), sizeof(pthread_t));
+  for (int j = 0; j < nsetup; j++) {
+    jobs[j].draws = draws;
+    jobs[j].num_draws = num_draws;
+    jobs[j].rects = (const int32_t(*)[4])rects;
+    jobs[j].tri_base = base;
+    jobs[j].t0 = total * (uint64_t)j / (uint64_t)nsetup;
+    jobs[j].t1 = total * (uint64_t)(j + 1) / (uint64_t)nsetup;
+  }
+  if (nsetup == 1) {
+    setup_worker(&jobs[0]);
+  } else {
+    for (int j = 0; j < nsetup; j++) pthread_create(&th[j], NULL, setup_worker, &jobs[j]);
+    for (int j = 0; j < nsetup; j++) pthread_join(th[j], NULL);
+  }
+  int nbands = nthreads;
+  if ((uint32_t)nbands > height) nbands = height ? (int)height : 1;
+  raster_job* rj = (raster_job*)calloc((size_t)nbands, sizeof(raster_job));
+  for (int b = 0; b < nbands; b++) {
+    rj[b].draws = draws;
+    rj[b].jobs = jobs;
+    rj[b].njobs = nsetup;
+    rj[b].width = width;
+    rj[b].color = color;
+    rj[b].depth = depth;
+    rj[b].ylo = (int32_t)((uint64_t)height * (uint64_t)b / (uint64_t)nbands);
+    rj[b].yhi = (int32_t)((uint64_t)height * (uint64_t)(b + 1) / (uint64_t)nbands);
+  }
+  if (nbands == 1) {
+    raster_worker(&rj[0]);
+  } else {
+    for (int b = 0; b < nbands; b++) pthread_create(&th[b], NULL, raster_worker, &rj[b]);
+    for (int b = 0; b < nbands; b++) pthread_join(th[b], NULL);
+  }
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    for (int j = 0; j < nsetup; j++) {
+      stats->tris += jobs[j].list.st.tris;
+      stats->rejected += jobs[j].list.st.rejected;
+      stats->clipped += jobs[j].list.st.clipped;
+      stats->subtris += jobs[j].list.st.subtris;
+    }
+    for (int b = 0; b < nbands; b++) {
+      stats->fragments += rj[b].st.fragments;
+      stats->depth_pass += rj[b].st.depth_pass;
+    }
+  }
+  for (int j = 0; j < nsetup; j++) free(jobs[j].list.v);
+  free(jobs);
+  free(rj);
+  free(th);
+  free(base);
+  free(rects);
+  return 0;
+}
+
+void kzo_clear_color(uint32_t width, uint8_t* color, const int32_t rect[4], const float rgba[4]) {
+  uint8_t px[4];
+  for (int i = 0; i < 4; i++) px[i] = kzo_unorm8(rgba[i]);
+  for (int32_t y = rect[1]; y < rect[3]; y++)
+    for (int32_t x = rect[0]; x < rect[2]; x++) memcpy(color + ((size_t)y * width + (size_t)x) * 4, px, 4);
+}
+
+void kzo_clear_depth(uint32_t width, float* depth, const int32_t rect[4], float value) {
+  for (int32_t y = rect[1]; y < rect[3]; y++)
+    for (int32_t x = rect[0]; x < rect[2]; x++) depth[(size_t)y * width + (size_t)x] = value;
+}

@@ -1,0 +1,92 @@
+/*
+ * kz_oracle.h - CPU oracle for the kazan draw path.  TEST INFRASTRUCTURE ONLY.
+ *
+ * This is the checker the GPU path is compared against; it is never linked into, called by or
+ * shipped with the driver.  Only the tests, the smoke check and the CPU-baseline leg of the
+ * benchmark load it.
+ *
+ * PARITY UNPINNED: the reference driver has no rasteriser.  vkCmdDraw, vkCmdDrawIndexed and
+ * vkCmdClearColorImage are `unimplemented!()` (vulkan-driver/src/api_impl.rs:4632-4653,4780-4790),
+ * no reference test renders anything (vulkan-driver/src/lib.rs:134-135 is an empty test module), and
+ * the reference cannot be built here (no Rust toolchain).  This oracle therefore restates the
+ * rasterisation rules of the Vulkan specification, with the choices the specification leaves open
+ * fixed as follows (the GPU kernels make the same choices):
+ *   - viewport transform xf = fma(x/w, w/2, x0 + w/2) in f32, with x/w computed as x * (1/w);
+ *   - 8 sub-pixel bits: X = rint(xf * 256) (round to nearest even), int32;
+ *   - samples at pixel centres (x*256+128, y*256+128); exact int64 edge functions;
+ *   - top-left fill rule in framebuffer space (y down): an edge a->b of a triangle with positive
+ *     signed area S is "top-left" iff dy < 0, or dy == 0 and dx > 0;
+ *   - facing per Vulkan: area a = -S/2; VK_FRONT_FACE_COUNTER_CLOCKWISE means a > 0 is front;
+ *   - clipping against z >= 0, z <= w and a guard band |x|,|y| <= 4w (Sutherland-Hodgman, planes in
+ *     that order, new vertices interpolated from the inside vertex towards the outside one);
+ *   - screen-space barycentrics l_i = (float)E_i * (1/(float)S); depth z0 + l1 dz1 + l2 dz2 by fma,
+ *     clamped to the viewport depth range; perspective-correct varyings divided by the interpolated 1/w;
+ *   - UNORM8 stores rint(clamp(c, 0, 1) * 255); blending in f32 with dst = u8 / 255.
+ * Every float operation is an explicit IEEE single operation (built with -ffp-contract=off and fmaf
+ * where the GPU fuses), so results are bit-identical to the kernels.
+ */
+#ifndef KZ_ORACLE_H
+#define KZ_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { KZO_SHADER_COLOR = 0, KZO_SHADER_LAMBERT = 1 };
+
+typedef struct kzo_draw {
+  uint32_t shader;          /* KZO_SHADER_COLOR: pos f32x4 + rgba f32x4 (8 floats per vertex);
+                               KZO_SHADER_LAMBERT: pos f32x3 + normal f32x3 (6 floats per vertex) */
+  const float* vertices;
+  const uint32_t* indices;  /* NULL for vkCmdDraw */
+  uint32_t first;           /* firstVertex (vkCmdDraw) or firstIndex (vkCmdDrawIndexed) */
+  int32_t vertex_offset;    /* vkCmdDrawIndexed vertexOffset */
+  uint32_t tri_count;
+  float mvp[16];            /* column-major, LAMBERT vertex shader */
+  float albedo[3];          /* LAMBERT fragment shader constants */
+  float light[3];
+  uint32_t cull_mode;       /* VkCullModeFlags */
+  uint32_t front_ccw;
+  uint32_t depth_test, depth_write, depth_compare; /* VkCompareOp */
+  uint32_t blend_enable;
+  uint32_t src_color, dst_color, color_op, src_alpha, dst_alpha, alpha_op;
+  uint32_t write_mask;
+  float blend_const[4];
+  float viewport[6];        /* x, y, width, height, minDepth, maxDepth */
+  int32_t scissor[4];       /* x, y, width, height */
+} kzo_draw;
+
+typedef struct kzo_stats {
+  uint64_t tris;            /* triangles submitted */
+  uint64_t rejected;        /* trivially rejected, culled, degenerate or empty */
+  uint64_t clipped;         /* triangles that needed clipping */
+  uint64_t subtris;         /* (sub-)triangles rasterised */
+  uint64_t fragments;       /* covered samples inside the pixel rectangle, before the depth test */
+  uint64_t depth_pass;      /* fragments that passed the depth test */
+} kzo_stats;
+
+/* Render draws in order into an RGBA8 colour image (width*height*4 bytes, row-major) and an optional
+ * D32 depth image.  render_area = x0, y0, x1, y1 (exclusive).  nthreads <= 1 runs the plain in-order
+ * loop; nthreads > 1 runs setup in parallel over triangles and rasterises horizontal bands in parallel
+ * (each band walks the triangles in API order, so the result is identical). */
+int kzo_render(uint32_t width, uint32_t height, uint8_t* color, float* depth, const int32_t render_area[4],
+               uint32_t num_draws, const kzo_draw* draws, int nthreads, kzo_stats* stats);
+
+/* vkCmdClearColorImage / vkCmdClearDepthStencilImage restated for a rectangle */
+void kzo_clear_color(uint32_t width, uint8_t* color, const int32_t rect[4], const float rgba[4]);
+void kzo_clear_depth(uint32_t width, float* depth, const int32_t rect[4], float value);
+
+/* f32 -> UNORM8 as the driver stores it */
+uint8_t kzo_unorm8(float v);
+
+/* pixel rectangle of a draw: framebuffer & render area & scissor & viewport (x0, y0, x1, y1 exclusive) */
+void kzo_draw_rect(uint32_t width, uint32_t height, const int32_t render_area[4], const kzo_draw* d,
+                   int32_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,123 @@
+"""Python binding of the CPU oracle (kz_oracle.c).  TEST INFRASTRUCTURE ONLY.
+
+Used by the tests, the smoke check and the CPU-baseline leg of bench.py as the checker; the driver never
+loads it.  PARITY UNPINNED: the reference driver has no rasteriser (vulkan-driver/src/api_impl.rs:4632-4653
+are `unimplemented!()`), so this oracle restates the Vulkan specification's rules (see kz_oracle.h).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libkz_oracle.so")
+
+SHADER = {"color": 0, "lambert": 1}
+
+
+class KzoDraw(ctypes.Structure):
+    _fields_ = [("shader", ctypes.c_uint32), ("vertices", ctypes.c_void_p), ("indices", ctypes.c_void_p),
+                ("first", ctypes.c_uint32), ("vertex_offset", ctypes.c_int32), ("tri_count", ctypes.c_uint32),
+                ("mvp", ctypes.c_float * 16), ("albedo", ctypes.c_float * 3), ("light", ctypes.c_float * 3),
+                ("cull_mode", ctypes.c_uint32), ("front_ccw", ctypes.c_uint32), ("depth_test", ctypes.c_uint32),
+                ("depth_write", ctypes.c_uint32), ("depth_compare", ctypes.c_uint32),
+                ("blend_enable", ctypes.c_uint32), ("src_color", ctypes.c_uint32), ("dst_color", ctypes.c_uint32),
+                ("color_op", ctypes.c_uint32), ("src_alpha", ctypes.c_uint32), ("dst_alpha", ctypes.c_uint32),
+                ("alpha_op", ctypes.c_uint32), ("write_mask", ctypes.c_uint32), ("blend_const", ctypes.c_float * 4),
+                ("viewport", ctypes.c_float * 6), ("scissor", ctypes.c_int32 * 4)]
+
+
+class KzoStats(ctypes.Structure):
+    _fields_ = [("tris", ctypes.c_uint64), ("rejected", ctypes.c_uint64), ("clipped", ctypes.c_uint64),
+                ("subtris", ctypes.c_uint64), ("fragments", ctypes.c_uint64), ("depth_pass", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+_LIB = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.kzo_render.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                 ctypes.POINTER(ctypes.c_int32), ctypes.c_uint32, ctypes.POINTER(KzoDraw),
+                                 ctypes.c_int, ctypes.POINTER(KzoStats)]
+        L.kzo_render.restype = ctypes.c_int
+        L.kzo_unorm8.argtypes = [ctypes.c_float]
+        L.kzo_unorm8.restype = ctypes.c_uint8
+        L.kzo_clear_color.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                      ctypes.POINTER(ctypes.c_float)]
+        L.kzo_clear_depth.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                      ctypes.c_float]
+        _LIB = L
+    return _LIB
+
+
+def unorm8(v):
+    return int(lib().kzo_unorm8(float(v)))
+
+
+def clear_images(scene):
+    w, h = scene.width, scene.height
+    color = np.empty((h, w, 4), dtype=np.uint8)
+    depth = np.empty((h, w), dtype=np.float32)
+    rect = (ctypes.c_int32 * 4)(0, 0, w, h)
+    lib().kzo_clear_color(w, color.ctypes.data, rect, (ctypes.c_float * 4)(*scene.clear_color))
+    lib().kzo_clear_depth(w, depth.ctypes.data, rect, scene.clear_depth)
+    return color, depth
+
+
+def make_draws(scene, draws=None):
+    from kazan_gb300 import spirv_asm
+    draws = scene.draws if draws is None else draws
+    arr = (KzoDraw * max(1, len(draws)))()
+    for i, d in enumerate(draws):
+        k = arr[i]
+        k.shader = SHADER[scene.shader]
+        k.vertices = scene.vertices.ctypes.data
+        k.indices = scene.indices.ctypes.data if scene.indices is not None else None
+        k.first = d.first
+        k.vertex_offset = d.vertex_offset
+        k.tri_count = d.count
+        if d.mvp is not None:
+            k.mvp[:] = [float(x) for x in d.mvp]
+        k.albedo[:] = [float(x) for x in spirv_asm.ALBEDO]
+        k.light[:] = [float(x) for x in spirv_asm.LIGHT]
+        k.cull_mode = scene.cull
+        k.front_ccw = int(scene.front_ccw)
+        k.depth_test = int(scene.depth_test)
+        k.depth_write = int(scene.depth_write)
+        k.depth_compare = scene.depth_compare
+        k.blend_enable = int(scene.blend)
+        k.src_color, k.dst_color, k.color_op = 6, 7, 0
+        k.src_alpha, k.dst_alpha, k.alpha_op = 6, 7, 0
+        k.write_mask = 0xF
+        k.viewport[:] = [0.0, 0.0, float(scene.width), float(scene.height), 0.0, 1.0]
+        k.scissor[:] = [0, 0, scene.width, scene.height]
+    return arr, len(draws)
+
+
+def render(scene, threads=1, draws=None, color=None, depth=None):
+    """Render `scene` (a kazan_gb300.scenes.Scene) from cleared attachments; returns
+    (color uint8 [H, W, 4], depth float32 [H, W], stats dict)."""
+    if color is None or depth is None:
+        color, depth = clear_images(scene)
+    arr, n = make_draws(scene, draws)
+    st = KzoStats()
+    area = (ctypes.c_int32 * 4)(0, 0, scene.width, scene.height)
+    rc = lib().kzo_render(scene.width, scene.height, color.ctypes.data, depth.ctypes.data, area, n, arr, threads,
+                          ctypes.byref(st))
+    if rc != 0:
+        raise RuntimeError("oracle failed")
+    return color, depth, st.as_dict()
