@@ -46,9 +46,21 @@ KZ_API int kzShaderCompile(const uint32_t* code, size_t word_count, uint32_t sta
 KZ_API void kzShaderInfo(const void* shader, KzShaderInfo* out);
 KZ_API void kzShaderDestroy(void* shader);
 
-/* PTX module for a pipeline set (fs[i] may be NULL).  Returns the size needed including the terminating
- * NUL; writes at most `size` bytes into buf when buf is not NULL. */
-KZ_API size_t kzShaderEmitPtx(const void* const* vs, const void* const* fs, uint32_t count, char* buf, size_t size);
+/* Vertex input state of one pipeline (VkPipelineVertexInputStateCreateInfo in the form the generated
+ * vertex fetch uses).  format: 1..4 = R32..R32G32B32A32_SFLOAT, 5 = R8G8B8A8_UNORM, 6..9 = 1..4 x 32-bit
+ * integers. */
+typedef struct KzVertexInputLayout {
+  uint32_t num_attrs;
+  uint32_t location[8], binding[8], format[8], offset[8];
+  uint32_t stride[8];
+  uint32_t instanced; /* bit b: binding b advances per instance */
+} KzVertexInputLayout;
+
+/* PTX module for a pipeline set (fs[i] may be NULL; layouts may be NULL, then vertex inputs read as 0).
+ * Returns the size needed including the terminating NUL; writes at most `size` bytes into buf when buf
+ * is not NULL. */
+KZ_API size_t kzShaderEmitPtx(const void* const* vs, const void* const* fs, const KzVertexInputLayout* layouts,
+                              uint32_t count, char* buf, size_t size);
 
 /* Link PTX with the relocatable pipeline-kernel object (NULL: the object built next to the library). */
 KZ_API int kzShaderLink(const char* ptx, const void* object, size_t object_size, void** out_code, char* err,

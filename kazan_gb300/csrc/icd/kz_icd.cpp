@@ -109,11 +109,23 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
     return nullptr;
   }
   std::vector<const ir::Shader*> vs, fs;
+  std::vector<ptx::VertexLayout> layouts;
   for (Pipeline* p : pipes) {
     vs.push_back(p->vs.get());
     fs.push_back(p->fs.get());
+    ptx::VertexLayout l;
+    l.num_attrs = p->pipe.num_attrs;
+    for (uint32_t k = 0; k < p->pipe.num_attrs; k++) {
+      l.location[k] = p->pipe.attrs[k].location;
+      l.binding[k] = p->pipe.attrs[k].binding;
+      l.format[k] = p->pipe.attrs[k].format;
+      l.offset[k] = p->pipe.attrs[k].offset;
+    }
+    for (uint32_t b = 0; b < KZ_MAX_BINDINGS; b++) l.stride[b] = p->pipe.binding_stride[b];
+    l.instanced = p->pipe.binding_instanced;
+    layouts.push_back(l);
   }
-  std::string ptx = ptx::module_text(vs, fs);
+  std::string ptx = ptx::module_text(vs, fs, layouts);
   std::vector<char> cubin;
   err = ptx::link(ptx, obj.data(), obj.size(), cubin);
   if (!err.empty()) return nullptr;

@@ -23,8 +23,11 @@
 
 #include "../kz_raster_abi.h"
 
-extern "C" __device__ void kz_vs(uint32_t pipe, const KzVsIn* in, const uint8_t* push, KzVsOut* out);
-extern "C" __device__ void kz_vs_pos(uint32_t pipe, const KzVsIn* in, const uint8_t* push, float* pos);
+/* vertex shader functions fetch their own attributes from the draw's vertex buffers */
+extern "C" __device__ void kz_vs(uint32_t pipe, const KzDraw* draw, uint32_t vid, uint32_t iid, const uint8_t* push,
+                                 KzVsOut* out);
+extern "C" __device__ float4 kz_vs_pos(uint32_t pipe, const KzDraw* draw, uint32_t vid, uint32_t iid,
+                                       const uint8_t* push);
 extern "C" __device__ uint32_t kz_fs(uint32_t pipe, const KzFsIn* in, const uint8_t* push, float* color);
 
 #define KZ_THREADS 256
@@ -100,60 +103,6 @@ __device__ void tri_vertices(const KzDraw& d, uint32_t local, uint32_t vid[3], u
   } else {
     for (int j = 0; j < 3; j++) vid[j] = (uint32_t)d.vertex_offset + 3u * t + (uint32_t)j;
   }
-}
-
-__device__ void fetch_inputs(const KzPipe& p, const KzDraw& d, uint32_t vid, uint32_t iid, uint32_t mask,
-                             KzVsIn& in) {
-  uint32_t na = p.num_attrs;
-  for (uint32_t a = 0; a < na; a++) {
-    KzAttr at = p.attrs[a];
-    if (!((mask >> at.location) & 1u)) continue;
-    uint32_t b = at.binding;
-    uint32_t idx = ((p.binding_instanced >> b) & 1u) ? iid : vid;
-    const char* src = reinterpret_cast<const char*>(d.vb[b]) + (size_t)idx * p.binding_stride[b] + at.offset;
-    float v[4] = {0.0f, 0.0f, 0.0f, 1.0f};
-    uintptr_t addr = reinterpret_cast<uintptr_t>(src);
-    switch (at.format) {
-      case KZ_FMT_F32x4:
-        if ((addr & 15u) == 0) {
-          float4 q = __ldg(reinterpret_cast<const float4*>(src));
-          v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-          break;
-        }
-        v[3] = __ldg(reinterpret_cast<const float*>(src) + 3);
-        /* fall through */
-      case KZ_FMT_F32x3:
-        v[2] = __ldg(reinterpret_cast<const float*>(src) + 2);
-        /* fall through */
-      case KZ_FMT_F32x2:
-        if ((addr & 7u) == 0) {
-          float2 q = __ldg(reinterpret_cast<const float2*>(src));
-          v[0] = q.x; v[1] = q.y;
-          break;
-        }
-        v[1] = __ldg(reinterpret_cast<const float*>(src) + 1);
-        /* fall through */
-      case KZ_FMT_F32x1:
-        v[0] = __ldg(reinterpret_cast<const float*>(src));
-        break;
-      case KZ_FMT_U8x4_UNORM: {
-        uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(src));
-        for (int k = 0; k < 4; k++) v[k] = u8f((w >> (8 * k)) & 0xFFu);
-        break;
-      }
-      case KZ_FMT_U32x4: v[3] = __uint_as_float(__ldg(reinterpret_cast<const uint32_t*>(src) + 3)); /* fall through */
-      case KZ_FMT_U32x3: v[2] = __uint_as_float(__ldg(reinterpret_cast<const uint32_t*>(src) + 2)); /* fall through */
-      case KZ_FMT_U32x2: v[1] = __uint_as_float(__ldg(reinterpret_cast<const uint32_t*>(src) + 1)); /* fall through */
-      case KZ_FMT_U32x1: v[0] = __uint_as_float(__ldg(reinterpret_cast<const uint32_t*>(src))); break;
-      default: break;
-    }
-    in.attr[at.location][0] = v[0];
-    in.attr[at.location][1] = v[1];
-    in.attr[at.location][2] = v[2];
-    in.attr[at.location][3] = v[3];
-  }
-  in.vertex_index = vid;
-  in.instance_index = iid;
 }
 
 /* ---------------- clipping ---------------- */
@@ -341,10 +290,9 @@ struct Shade {
   uint32_t ok;
 };
 
-__device__ void vs_full(const Ctx& c, const KzDraw& d, const KzPipe& p, uint32_t vid, uint32_t iid, KzVsOut& o) {
-  KzVsIn in;
-  fetch_inputs(p, d, vid, iid, p.full_input_mask, in);
-  kz_vs(d.pipe, &in, push_ptr(*c.f, d), &o);
+__device__ __forceinline__ void vs_full(const Ctx& c, const KzDraw& d, const KzPipe&, uint32_t vid, uint32_t iid,
+                                        KzVsOut& o) {
+  kz_vs(d.pipe, &d, vid, iid, push_ptr(*c.f, d), &o);
 }
 
 /* Build the shading setup of a (sub-)triangle from three full vertices (clip position + varyings). */
@@ -382,31 +330,15 @@ __device__ __forceinline__ bool covers(const KzTriRecord& r, int32_t x, int32_t 
   return in;
 }
 
-/* Recompute primitive g of the segment for shading at pixel (x, y) (sub-triangle chosen by coverage
- * when the primitive was clipped, or by `sub` when it is known: sub = clip sub-index + 1, 0 = any). */
-__device__ __noinline__ bool shade_setup(const Ctx& c, uint32_t g, int32_t x, int32_t y, uint32_t sub, Shade& s) {
-  const KzSegment& seg = *c.seg;
-  uint32_t di = find_draw(c.draws, seg.first_draw, seg.num_draws, g);
-  const KzDraw& d = c.draws[di];
-  const KzPipe& p = c.pipes[d.pipe];
-  uint32_t vid[3], iid;
-  tri_vertices(d, g - d.prim_base, vid, iid);
-  int nc = (int)p.num_varyings;
+/* clipped primitive: redo the clip with varyings and pick the sub-triangle (by index, or by coverage
+ * of pixel (x, y) when sub == 0) */
+__device__ __noinline__ bool shade_clipped(const KzDraw& d, const KzPipe& p, const KzVsOut* o, int nc, int32_t x,
+                                           int32_t y, uint32_t sub, Shade& s) {
   ClipV v[KZ_MAX_CLIP_VERTS];
   for (int j = 0; j < 3; j++) {
-    KzVsOut o;
-    vs_full(c, d, p, vid[j], iid, o);
-    for (int k = 0; k < 4; k++) v[j].c[k] = o.pos[k];
-    for (int k = 0; k < nc; k++) v[j].c[4 + k] = o.var[k];
+    for (int k = 0; k < 4; k++) v[j].c[k] = o[j].pos[k];
+    for (int k = 0; k < nc; k++) v[j].c[4 + k] = o[j].var[k];
   }
-  s.pipe = d.pipe;
-  s.draw = di;
-  float pos[3][4];
-  for (int j = 0; j < 3; j++)
-    for (int k = 0; k < 4; k++) pos[j][k] = v[j].c[k];
-  int cls = classify(pos);
-  if (cls == 0) return false;
-  if (cls == 1) return shade_from_vertices(d, p, v, nc, s);
   ClipV v0 = v[0];
   int n = clip_polygon(v, nc);
   for (int i = 0; i < n; i++)
@@ -421,6 +353,49 @@ __device__ __noinline__ bool shade_setup(const Ctx& c, uint32_t g, int32_t x, in
     if (covers(s.r, x, y, E)) return true;
   }
   return false;
+}
+
+/* setup of an unclipped triangle straight from the vertex-shader outputs */
+__device__ __forceinline__ bool shade_direct(const KzDraw& d, const KzPipe& p, const KzVsOut* o, int nc, Shade& s) {
+  Proj pr[3];
+  for (int i = 0; i < 3; i++) pr[i] = project(d, o[i].pos);
+  bool swapped = false;
+  if (!make_record(d, p, pr, s.r, swapped)) return false;
+  int order[3] = {0, swapped ? 2 : 1, swapped ? 1 : 2};
+  for (int i = 0; i < 3; i++) {
+    const KzVsOut& src = o[order[i]];
+    float iw = fdiv(1.0f, src.pos[3]);
+    s.iw[i] = iw;
+    for (int k = 0; k < nc; k++) {
+      bool flat = (p.flat_mask >> k) & 1u;
+      float val = flat ? o[0].var[k] : src.var[k];
+      s.a[i][k] = (flat || ((p.noperspective_mask >> k) & 1u)) ? val : fmul(val, iw);
+    }
+  }
+  return true;
+}
+
+/* Recompute primitive g of the segment for shading at pixel (x, y) (sub-triangle chosen by coverage
+ * when the primitive was clipped, or by `sub` when it is known: sub = clip sub-index, 0 = any). */
+__device__ bool shade_setup(const Ctx& c, uint32_t g, int32_t x, int32_t y, uint32_t sub, Shade& s) {
+  const KzSegment& seg = *c.seg;
+  uint32_t di = find_draw(c.draws, seg.first_draw, seg.num_draws, g);
+  const KzDraw& d = c.draws[di];
+  const KzPipe& p = c.pipes[d.pipe];
+  uint32_t vid[3], iid;
+  tri_vertices(d, g - d.prim_base, vid, iid);
+  int nc = (int)p.num_varyings;
+  KzVsOut o[3];
+  for (int j = 0; j < 3; j++) vs_full(c, d, p, vid[j], iid, o[j]);
+  s.pipe = d.pipe;
+  s.draw = di;
+  float pos[3][4];
+  for (int j = 0; j < 3; j++)
+    for (int k = 0; k < 4; k++) pos[j][k] = o[j].pos[k];
+  int cls = classify(pos);
+  if (cls == 0) return false;
+  if (cls == 1) return shade_direct(d, p, o, nc, s);
+  return shade_clipped(d, p, o, nc, x, y, sub, s);
 }
 
 /* interpolate varyings and run the fragment shader */
@@ -611,15 +586,23 @@ __device__ __forceinline__ bool tile_overlaps(const KzSegment& seg, const Edges&
   return true;
 }
 
-__device__ void count_tiles(const Ctx& c, const KzTriRecord& r) {
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+/* tile counts of a record; single-tile records (the common case) are aggregated per warp */
+__device__ void count_tiles(const Ctx& c, const KzTriRecord& r, bool active) {
   const KzSegment& seg = *c.seg;
-  int tx0, ty0, tx1, ty1;
-  tile_range(seg, r, tx0, ty0, tx1, ty1);
+  int tx0 = 0, ty0 = 0, tx1 = -1, ty1 = -1;
+  if (active) tile_range(seg, r, tx0, ty0, tx1, ty1);
+  bool single = active && tx0 == tx1 && ty0 == ty1;
   uint32_t* tc = reinterpret_cast<uint32_t*>(seg.tile_count);
-  if (tx0 == tx1 && ty0 == ty1) {
-    atomicAdd(&tc[ty0 * seg.tiles_x + tx0], 1u);
-    return;
-  }
+  uint32_t t = single ? (uint32_t)(ty0 * (int)seg.tiles_x + tx0) : 0xFFFFFFFFu;
+  uint32_t peers = __match_any_sync(0xFFFFFFFFu, t);
+  if (single && (__ffs(peers) - 1) == (int)(threadIdx.x & 31)) atomicAdd(&tc[t], (uint32_t)__popc(peers));
+  if (!active || single) return;
   Edges e;
   edges_of(r, e);
   for (int ty = ty0; ty <= ty1; ty++)
@@ -627,8 +610,7 @@ __device__ void count_tiles(const Ctx& c, const KzTriRecord& r) {
       if (tile_overlaps(seg, e, tx, ty)) atomicAdd(&tc[ty * seg.tiles_x + tx], 1u);
 }
 
-__device__ void emit_record(const Ctx& c, KzTriRecord& r) {
-  uint32_t idx = atomicAdd(&c.cnt->rec_count, 1u);
+__device__ void store_record(const Ctx& c, uint32_t idx, const KzTriRecord& r) {
   if (idx < c.seg->rec_cap) {
     KzTriRecord* dst = reinterpret_cast<KzTriRecord*>(c.seg->records) + idx;
     const uint4* s4 = reinterpret_cast<const uint4*>(&r);
@@ -638,7 +620,21 @@ __device__ void emit_record(const Ctx& c, KzTriRecord& r) {
     d4[2] = s4[2];
     d4[3] = s4[3];
   }
-  count_tiles(c, r);
+}
+
+/* slow path (clipped primitives): one record at a time */
+__device__ void emit_record(const Ctx& c, KzTriRecord& r) {
+  uint32_t idx = atomicAdd(&c.cnt->rec_count, 1u);
+  store_record(c, idx, r);
+  const KzSegment& seg = *c.seg;
+  int tx0, ty0, tx1, ty1;
+  tile_range(seg, r, tx0, ty0, tx1, ty1);
+  uint32_t* tc = reinterpret_cast<uint32_t*>(seg.tile_count);
+  Edges e;
+  edges_of(r, e);
+  for (int ty = ty0; ty <= ty1; ty++)
+    for (int tx = tx0; tx <= tx1; tx++)
+      if (tile_overlaps(seg, e, tx, ty)) atomicAdd(&tc[ty * seg.tiles_x + tx], 1u);
 }
 
 __device__ __noinline__ void geometry_clipped(const Ctx& c, const KzDraw& d, const KzPipe& p, float pos[3][4],
@@ -660,7 +656,8 @@ __device__ __noinline__ void geometry_clipped(const Ctx& c, const KzDraw& d, con
   }
 }
 
-__device__ void geometry_triangle(const Ctx& c, uint32_t di, uint32_t local) {
+/* returns true with the record of an unclipped visible triangle; clipped triangles are emitted here */
+__device__ bool geometry_triangle(const Ctx& c, uint32_t di, uint32_t local, KzTriRecord& r) {
   const KzDraw& d = c.draws[di];
   const KzPipe& p = c.pipes[d.pipe];
   uint32_t vid[3], iid;
@@ -668,30 +665,52 @@ __device__ void geometry_triangle(const Ctx& c, uint32_t di, uint32_t local) {
   float pos[3][4];
   const uint8_t* push = push_ptr(*c.f, d);
   for (int j = 0; j < 3; j++) {
-    KzVsIn in;
-    fetch_inputs(p, d, vid[j], iid, p.pos_input_mask, in);
-    kz_vs_pos(d.pipe, &in, push, pos[j]);
+    float4 q = kz_vs_pos(d.pipe, &d, vid[j], iid, push);
+    pos[j][0] = q.x;
+    pos[j][1] = q.y;
+    pos[j][2] = q.z;
+    pos[j][3] = q.w;
   }
   uint32_t g = d.prim_base + local;
   int cls = classify(pos);
-  if (cls == 0) return;
+  if (cls == 0) return false;
   if (cls == 2) {
     geometry_clipped(c, d, p, pos, g, di);
-    return;
+    return false;
   }
   Proj pr[3] = {project(d, pos[0]), project(d, pos[1]), project(d, pos[2])};
-  KzTriRecord r;
   bool sw;
-  if (!make_record(d, p, pr, r, sw)) return;
+  if (!make_record(d, p, pr, r, sw)) return false;
   r.g = g;
   r.draw = di;
   r.pad = 0;
-  emit_record(c, r);
+  return true;
 }
 
-__device__ void geometry_chunk(const Ctx& c, uint32_t chunk) {
+/* one chunk per block: records are allocated with one atomic per block */
+__device__ void geometry_chunk(const Ctx& c, uint32_t chunk, uint32_t* sh) {
   const KzChunk ch = reinterpret_cast<const KzChunk*>(c.f->chunks)[chunk];
-  if (threadIdx.x < ch.count) geometry_triangle(c, ch.draw, ch.first + threadIdx.x);
+  KzTriRecord r;
+  bool have = false;
+  if (threadIdx.x < ch.count) have = geometry_triangle(c, ch.draw, ch.first + threadIdx.x, r);
+  uint32_t ballot = __ballot_sync(0xFFFFFFFFu, have);
+  uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) sh[warp] = (uint32_t)__popc(ballot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (uint32_t w = 0; w < (blockDim.x >> 5); w++) {
+      uint32_t v = sh[w];
+      sh[w] = run;
+      run += v;
+    }
+    sh[32] = run ? atomicAdd(&c.cnt->rec_count, run) : 0u;
+  }
+  __syncthreads();
+  uint32_t idx = sh[32] + sh[warp] + (uint32_t)__popc(ballot & lanemask_lt());
+  if (have) store_record(c, idx, r);
+  count_tiles(c, r, have);
+  __syncthreads();
 }
 
 /* ---------------- phase: scan (one block) ---------------- */
@@ -748,30 +767,48 @@ __device__ void scan_tiles(const Ctx& c, uint32_t s, uint32_t* sh) {
 
 /* ---------------- phase: bin ---------------- */
 
-__device__ void bin_record(const Ctx& c, uint32_t ri) {
+__device__ void bin_record(const Ctx& c, uint32_t ri, bool active) {
   const KzSegment& seg = *c.seg;
-  KzTriRecord r = reinterpret_cast<const KzTriRecord*>(seg.records)[ri];
-  int tx0, ty0, tx1, ty1;
-  tile_range(seg, r, tx0, ty0, tx1, ty1);
+  KzTriRecord r;
+  int tx0 = 0, ty0 = 0, tx1 = -1, ty1 = -1;
+  if (active) {
+    r = reinterpret_cast<const KzTriRecord*>(seg.records)[ri];
+    tile_range(seg, r, tx0, ty0, tx1, ty1);
+  }
   const uint32_t* to = reinterpret_cast<const uint32_t*>(seg.tile_offset);
   uint32_t* cur = reinterpret_cast<uint32_t*>(seg.tile_cursor);
   uint32_t* bins = reinterpret_cast<uint32_t*>(seg.bins);
-  if (tx0 == tx1 && ty0 == ty1) {
-    uint32_t t = ty0 * seg.tiles_x + tx0;
-    bins[to[t] + atomicAdd(&cur[t], 1u)] = ri;
-    return;
-  }
+  bool single = active && tx0 == tx1 && ty0 == ty1;
+  uint32_t t = single ? (uint32_t)(ty0 * (int)seg.tiles_x + tx0) : 0xFFFFFFFFu;
+  uint32_t peers = __match_any_sync(0xFFFFFFFFu, t);
+  int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (single && leader == (int)(threadIdx.x & 31)) base = to[t] + atomicAdd(&cur[t], (uint32_t)__popc(peers));
+  base = __shfl_sync(0xFFFFFFFFu, base, leader);
+  if (single) bins[base + __popc(peers & lanemask_lt())] = ri;
+  if (!active || single) return;
   Edges e;
   edges_of(r, e);
   for (int ty = ty0; ty <= ty1; ty++)
     for (int tx = tx0; tx <= tx1; tx++)
       if (tile_overlaps(seg, e, tx, ty)) {
-        uint32_t t = ty * seg.tiles_x + tx;
-        bins[to[t] + atomicAdd(&cur[t], 1u)] = ri;
+        uint32_t tt = ty * seg.tiles_x + tx;
+        bins[to[tt] + atomicAdd(&cur[tt], 1u)] = ri;
       }
 }
 
 /* ---------------- phase: raster ---------------- */
+
+__device__ __forceinline__ KzTriRecord load_record(const KzSegment& seg, uint32_t ri) {
+  const uint4* src = reinterpret_cast<const uint4*>(reinterpret_cast<const KzTriRecord*>(seg.records) + ri);
+  KzTriRecord r;
+  uint4* d = reinterpret_cast<uint4*>(&r);
+  d[0] = __ldg(src);
+  d[1] = __ldg(src + 1);
+  d[2] = __ldg(src + 2);
+  d[3] = __ldg(src + 3);
+  return r;
+}
 
 struct TileInfo {
   int32_t x0, y0, x1, y1; /* inclusive pixel bounds of the tile inside the framebuffer and render area */
@@ -799,9 +836,20 @@ __device__ __forceinline__ float* depth_px(const KzSegment& seg, int32_t x, int3
   return reinterpret_cast<float*>(reinterpret_cast<char*>(seg.depth) + (size_t)y * seg.depth_pitch) + x;
 }
 
-/* rasterise the part of one record inside the tile into the visibility keys */
-__device__ __forceinline__ uint32_t vis_record(const KzSegment& seg, const KzDraw* draws, const KzTriRecord& r,
-                                               const TileInfo& ti, unsigned long long* keys, int lane0, int step) {
+__device__ __forceinline__ void vis_fragment(const KzSegment& seg, const KzTriRecord& r, float zmin, float zmax,
+                                             const TileInfo& ti, unsigned long long* keys, int32_t x, int32_t y,
+                                             int64_t E1, int64_t E2) {
+  float l1 = fmul(__ll2float_rn(E1), r.inv_s), l2 = fmul(__ll2float_rn(E2), r.inv_s);
+  float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
+  z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
+  unsigned long long k = vis_key(seg.vis_key, z, r.g);
+  unsigned long long* slot = &keys[(y - ti.oy) * (int)seg.tile + (x - ti.ox)];
+  if (k < *slot) atomicMin(slot, k);
+}
+
+/* one thread walks the record's box inside the tile with incrementally stepped edge functions */
+__device__ uint32_t vis_record_thread(const KzSegment& seg, const KzDraw* draws, const KzTriRecord& r,
+                                      const TileInfo& ti, unsigned long long* keys) {
   int32_t bx0 = max((int32_t)(r.bb0 & 0xFFFFu), ti.x0), by0 = max((int32_t)(r.bb0 >> 16), ti.y0);
   int32_t bx1 = min((int32_t)(r.bb1 & 0xFFFFu), ti.x1), by1 = min((int32_t)(r.bb1 >> 16), ti.y1);
   if (bx0 > bx1 || by0 > by1) return 0;
@@ -809,22 +857,47 @@ __device__ __forceinline__ uint32_t vis_record(const KzSegment& seg, const KzDra
   float zmin = d.zmin, zmax = d.zmax;
   Edges e;
   edges_of(r, e);
-  int T = (int)seg.tile;
-  int w = bx1 - bx0 + 1;
-  int npx = w * (by1 - by0 + 1);
+  int64_t sx0 = -(int64_t)e.dy[0] * 256, sx1 = -(int64_t)e.dy[1] * 256, sx2 = -(int64_t)e.dy[2] * 256;
+  int64_t px0 = (int64_t)bx0 * 256 + 128;
   uint32_t frags = 0;
-  for (int i = lane0; i < npx; i += step) {
-    int32_t x = bx0 + i % w, y = by0 + i / w;
-    int64_t px = (int64_t)x * 256 + 128, py = (int64_t)y * 256 + 128;
-    int64_t E0 = edge_at(e, 0, px, py), E1 = edge_at(e, 1, px, py), E2 = edge_at(e, 2, px, py);
-    if (E0 < e.thr[0] || E1 < e.thr[1] || E2 < e.thr[2]) continue;
-    frags++;
-    float l1 = fmul(__ll2float_rn(E1), r.inv_s), l2 = fmul(__ll2float_rn(E2), r.inv_s);
-    float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
-    z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
-    unsigned long long k = vis_key(seg.vis_key, z, r.g);
-    unsigned long long* slot = &keys[(y - ti.oy) * T + (x - ti.ox)];
-    if (k < *slot) atomicMin(slot, k);
+  for (int32_t y = by0; y <= by1; y++) {
+    int64_t py = (int64_t)y * 256 + 128;
+    int64_t E0 = edge_at(e, 0, px0, py), E1 = edge_at(e, 1, px0, py), E2 = edge_at(e, 2, px0, py);
+    for (int32_t x = bx0; x <= bx1; x++) {
+      if (E0 >= e.thr[0] && E1 >= e.thr[1] && E2 >= e.thr[2]) {
+        frags++;
+        vis_fragment(seg, r, zmin, zmax, ti, keys, x, y, E1, E2);
+      }
+      E0 += sx0;
+      E1 += sx1;
+      E2 += sx2;
+    }
+  }
+  return frags;
+}
+
+/* one warp covers the record's box in 8x4 pixel blocks */
+__device__ uint32_t vis_record_warp(const KzSegment& seg, const KzDraw* draws, const KzTriRecord& r,
+                                    const TileInfo& ti, unsigned long long* keys, int lane) {
+  int32_t bx0 = max((int32_t)(r.bb0 & 0xFFFFu), ti.x0), by0 = max((int32_t)(r.bb0 >> 16), ti.y0);
+  int32_t bx1 = min((int32_t)(r.bb1 & 0xFFFFu), ti.x1), by1 = min((int32_t)(r.bb1 >> 16), ti.y1);
+  if (bx0 > bx1 || by0 > by1) return 0;
+  const KzDraw& d = draws[r.draw];
+  float zmin = d.zmin, zmax = d.zmax;
+  Edges e;
+  edges_of(r, e);
+  int lx = lane & 7, ly = lane >> 3;
+  uint32_t frags = 0;
+  for (int32_t yb = by0; yb <= by1; yb += 4) {
+    for (int32_t xb = bx0; xb <= bx1; xb += 8) {
+      int32_t x = xb + lx, y = yb + ly;
+      if (x > bx1 || y > by1) continue;
+      int64_t px = (int64_t)x * 256 + 128, py = (int64_t)y * 256 + 128;
+      int64_t E0 = edge_at(e, 0, px, py), E1 = edge_at(e, 1, px, py), E2 = edge_at(e, 2, px, py);
+      if (E0 < e.thr[0] || E1 < e.thr[1] || E2 < e.thr[2]) continue;
+      frags++;
+      vis_fragment(seg, r, zmin, zmax, ti, keys, x, y, E1, E2);
+    }
   }
   return frags;
 }
@@ -849,12 +922,11 @@ __device__ void raster_tile_visibility(const Ctx& c, uint32_t t, unsigned char* 
   }
   if (threadIdx.x == 0) *qcount = 0;
   __syncthreads();
-  const KzTriRecord* recs = reinterpret_cast<const KzTriRecord*>(seg.records);
   const uint32_t* bins = reinterpret_cast<const uint32_t*>(seg.bins) + ti.base;
   uint32_t frags = 0;
   for (uint32_t e = threadIdx.x; e < ti.n; e += blockDim.x) {
     uint32_t ri = bins[e];
-    const KzTriRecord& r = recs[ri];
+    const KzTriRecord r = load_record(seg, ri);
     int32_t bx0 = max((int32_t)(r.bb0 & 0xFFFFu), ti.x0), by0 = max((int32_t)(r.bb0 >> 16), ti.y0);
     int32_t bx1 = min((int32_t)(r.bb1 & 0xFFFFu), ti.x1), by1 = min((int32_t)(r.bb1 >> 16), ti.y1);
     int area = (bx1 - bx0 + 1) * (by1 - by0 + 1);
@@ -865,15 +937,14 @@ __device__ void raster_tile_visibility(const Ctx& c, uint32_t t, unsigned char* 
         continue;
       }
     }
-    KzTriRecord rr = r;
-    frags += vis_record(seg, c.draws, rr, ti, keys, 0, 1);
+    frags += vis_record_thread(seg, c.draws, r, ti, keys);
   }
   __syncthreads();
   uint32_t nq = min(*qcount, 1024u);
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (uint32_t q = warp; q < nq; q += nwarps) {
-    KzTriRecord rr = recs[queue[q]];
-    frags += vis_record(seg, c.draws, rr, ti, keys, lane, 32);
+    const KzTriRecord rr = load_record(seg, queue[q]);
+    frags += vis_record_warp(seg, c.draws, rr, ti, keys, lane);
   }
   __syncthreads();
   if (frags) {
@@ -1095,9 +1166,10 @@ __device__ __forceinline__ uint32_t grab(uint32_t* counter, uint32_t* sh) {
 /* ================= kernels ================= */
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_geometry(KzFrame f, uint32_t s) {
+  __shared__ uint32_t sh[40];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
-  if (blockIdx.x < c.seg->num_chunks) geometry_chunk(c, c.seg->first_chunk + blockIdx.x);
+  if (blockIdx.x < c.seg->num_chunks) geometry_chunk(c, c.seg->first_chunk + blockIdx.x, sh);
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_scan(KzFrame f, uint32_t s) {
@@ -1111,10 +1183,13 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_bin(KzFrame f, uin
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
   uint32_t n = min(c.cnt->rec_count, c.seg->rec_cap);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) bin_record(c, i);
+  for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    uint32_t i = i0 + threadIdx.x;
+    bin_record(c, i, i < n);
+  }
 }
 
-extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_raster(KzFrame f, uint32_t s) {
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 2) kz_k_raster(KzFrame f, uint32_t s) {
   extern __shared__ __align__(16) unsigned char smem[];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
@@ -1124,10 +1199,11 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_raster(KzFrame f, 
 
 /* the whole command buffer in one cooperative launch: phases separated by bounded grid barriers,
  * work stolen from per-segment counters */
-extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_persistent(KzFrame f) {
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 2) kz_k_persistent(KzFrame f) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t item;
   __shared__ uint32_t scan_sh[KZ_THREADS + 1];
+  __shared__ uint32_t geo_sh[40];
   KzStatus* st = reinterpret_cast<KzStatus*>(f.status);
   for (uint32_t s = f.first_segment; s < f.num_segments; s++) {
     Ctx c = make_ctx(f, s);
@@ -1135,7 +1211,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_persistent(KzFrame
     for (;;) {
       uint32_t k = grab(&c.cnt->geom_next, &item);
       if (k >= c.seg->num_chunks) break;
-      geometry_chunk(c, c.seg->first_chunk + k);
+      geometry_chunk(c, c.seg->first_chunk + k, geo_sh);
     }
     if (!grid_barrier(st)) return;
     if (blockIdx.x == 0) scan_tiles(c, s, scan_sh);
@@ -1146,7 +1222,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_persistent(KzFrame
       uint32_t k = grab(&c.cnt->bin_next, &item);
       uint32_t i = k * blockDim.x + threadIdx.x;
       if (k * blockDim.x >= n) break;
-      if (i < n) bin_record(c, i);
+      bin_record(c, i, i < n);
     }
     if (!grid_barrier(st)) return;
     uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;

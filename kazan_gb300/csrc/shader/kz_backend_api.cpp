@@ -72,14 +72,29 @@ extern "C" KZ_API void kzShaderInfo(const void* shader, KzShaderInfo* out) {
 
 extern "C" KZ_API void kzShaderDestroy(void* shader) { delete static_cast<kz::ir::Shader*>(shader); }
 
-extern "C" KZ_API size_t kzShaderEmitPtx(const void* const* vs, const void* const* fs, uint32_t count, char* buf,
-                                         size_t size) {
+extern "C" KZ_API size_t kzShaderEmitPtx(const void* const* vs, const void* const* fs,
+                                         const KzVertexInputLayout* layouts, uint32_t count, char* buf, size_t size) {
   std::vector<const kz::ir::Shader*> v, f;
+  std::vector<kz::ptx::VertexLayout> lay;
   for (uint32_t i = 0; i < count; i++) {
     v.push_back(static_cast<const kz::ir::Shader*>(vs[i]));
     f.push_back(fs ? static_cast<const kz::ir::Shader*>(fs[i]) : nullptr);
+    kz::ptx::VertexLayout l;
+    if (layouts) {
+      const KzVertexInputLayout& src = layouts[i];
+      l.num_attrs = src.num_attrs < 8 ? src.num_attrs : 8;
+      for (uint32_t k = 0; k < 8; k++) {
+        l.location[k] = src.location[k];
+        l.binding[k] = src.binding[k] & 7u;
+        l.format[k] = src.format[k];
+        l.offset[k] = src.offset[k];
+        l.stride[k] = src.stride[k];
+      }
+      l.instanced = src.instanced;
+    }
+    lay.push_back(l);
   }
-  std::string ptx = kz::ptx::module_text(v, f);
+  std::string ptx = kz::ptx::module_text(v, f, lay);
   if (buf && size) {
     size_t n = ptx.size() + 1 < size ? ptx.size() + 1 : size;
     std::memcpy(buf, ptx.c_str(), n - 1);

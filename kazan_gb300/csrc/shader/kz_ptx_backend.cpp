@@ -6,10 +6,15 @@
  * command buffer uses) becomes one PTX module that defines the three functions the pipeline kernels
  * call (kz_raster_abi.h):
  *
- *   .func kz_vs(pipe, KzVsIn* in, push, KzVsOut* out)                 full vertex shader
- *   .func kz_vs_pos(pipe, KzVsIn* in, push, float* pos)                only gl_Position (dead outputs
- *                                                                       dropped, ptxas removes their math)
+ *   .func kz_vs(pipe, KzDraw* draw, vid, iid, push, KzVsOut* out)        full vertex shader
+ *   .func (.b8[16] pos) kz_vs_pos(pipe, KzDraw* draw, vid, iid, push)  only gl_Position, returned by value
+ *                                                                       (dead outputs dropped, ptxas removes
+ *                                                                       their math)
  *   .func (.b32 discard) kz_fs(pipe, KzFsIn* in, push, float* color)   fragment shader
+ *
+ * The vertex functions fetch their own attributes: the pipeline's vertex input state (binding, format,
+ * offset, stride, input rate) is compiled into direct loads from the draw's vertex buffers, so no
+ * attribute block passes through local memory.
  *
  * Each function branches on `pipe` to the inlined body of that pipeline.  nvJitLink then links the
  * module with the relocatable sm_103a object holding the kernels (kz_pipeline.cu) into one cubin; the
@@ -61,8 +66,62 @@ class Emitter {
 
   void line(const std::string& s) { out += "  " + s + "\n"; }
 
+  /* load of vertex input (location, component) for the generated fetch */
+  void vertex_load(const VertexLayout* lay, uint32_t off, Ty ty, const std::string& dst) {
+    char buf[160];
+    if (off == 128 || off == 132) {
+      line("mov.b32 " + dst + ", " + (off == 128 ? "%kzvid" : "%kziid") + ";");
+      return;
+    }
+    uint32_t loc = off / 16, comp = (off % 16) / 4;
+    int a = -1;
+    for (uint32_t i = 0; lay && i < lay->num_attrs; i++)
+      if (lay->location[i] == loc) a = (int)i;
+    uint32_t fmt = a >= 0 ? lay->format[a] : 0;
+    uint32_t ncomp = (fmt >= 1 && fmt <= 4) ? fmt : (fmt == 5 ? 4u : (fmt >= 6 && fmt <= 9) ? fmt - 5 : 0u);
+    if (a < 0 || comp >= ncomp) {
+      uint32_t bits = comp == 3 ? (ty == Ty::F32 ? 0x3F800000u : 1u) : 0u;
+      std::snprintf(buf, sizeof buf, ty == Ty::F32 ? "mov.f32 %s, 0f%08X;" : "mov.b32 %s, %u;", dst.c_str(), bits);
+      line(buf);
+      return;
+    }
+    uint32_t b = lay->binding[a];
+    if (fmt == 5) { /* R8G8B8A8_UNORM: byte / 255, correctly rounded */
+      std::snprintf(buf, sizeof buf, "ld.global.nc.u32 %%kzt, [%%kzvb%u+%u];", b, lay->offset[a]);
+      line(buf);
+      std::snprintf(buf, sizeof buf, "bfe.u32 %%kzt, %%kzt, %u, 8;", 8 * comp);
+      line(buf);
+      if (ty == Ty::F32) {
+        line("cvt.rn.f32.u32 " + dst + ", %kzt;");
+        line("div.rn.f32 " + dst + ", " + dst + ", 0f437F0000;");
+      } else {
+        line("mov.b32 " + dst + ", %kzt;");
+      }
+      return;
+    }
+    std::snprintf(buf, sizeof buf, "ld.global.nc.%s %s, [%%kzvb%u+%u];", ty == Ty::F32 ? "f32" : "u32", dst.c_str(), b,
+                  lay->offset[a] + 4 * comp);
+    line(buf);
+  }
+
+  /* per-vertex base address of each binding the layout uses */
+  void vertex_prologue(const VertexLayout* lay) {
+    if (!lay) return;
+    uint32_t used = 0;
+    for (uint32_t i = 0; i < lay->num_attrs; i++) used |= 1u << lay->binding[i];
+    char buf[200];
+    for (uint32_t b = 0; b < 8; b++) {
+      if (!(used & (1u << b))) continue;
+      std::snprintf(buf, sizeof buf,
+                    "ld.global.nc.u64 %%kzvb%u, [%%kzdraw+%u];\n  mul.wide.u32 %%kzoff, %s, %u;\n"
+                    "  add.s64 %%kzvb%u, %%kzvb%u, %%kzoff;\n  cvta.to.global.u64 %%kzvb%u, %%kzvb%u;",
+                    b, 8 * b, ((lay->instanced >> b) & 1u) ? "%kziid" : "%kzvid", lay->stride[b], b, b, b, b);
+      line(buf);
+    }
+  }
+
   /* body of one pipeline stage; registers numbered from the running counters */
-  void body(const Function& fn, const std::string& pfx, Kind kind) {
+  void body(const Function& fn, const std::string& pfx, Kind kind, const VertexLayout* lay = nullptr) {
     std::vector<std::string> name(fn.regs.size());
     for (size_t i = 0; i < fn.regs.size(); i++) {
       switch (fn.regs[i]) {
@@ -74,6 +133,8 @@ class Emitter {
     auto R = [&](int32_t r) { return name[(size_t)r]; };
     auto L = [&](uint32_t l) { return "$" + pfx + "_L" + std::to_string(l); };
     char buf[160];
+    bool vertex = kind != Kind::Fragment;
+    if (vertex) vertex_prologue(lay);
     for (const Inst& i : fn.code) {
       switch (i.op) {
         case Op::Const:
@@ -99,6 +160,10 @@ class Emitter {
           break;
         }
         case Op::LdIn:
+          if (vertex) {
+            vertex_load(lay, i.imm, i.ty, R(i.dst));
+            break;
+          }
           std::snprintf(buf, sizeof buf, "ld.%s %s, [%%kzin+%u];", i.ty == Ty::F32 ? "f32" : "u32", R(i.dst).c_str(),
                         i.imm);
           line(buf);
@@ -115,8 +180,12 @@ class Emitter {
             line("selp.u32 %kzt, 1, 0, " + v + ";");
             v = "%kzt";
           }
-          std::snprintf(buf, sizeof buf, "st.%s [%%kzout+%u], %s;",
-                        fn.regs[(size_t)i.a] == Ty::F32 ? "f32" : "u32", i.imm, v.c_str());
+          if (kind == Kind::VertexPos)
+            std::snprintf(buf, sizeof buf, "st.param.%s [func_retval0+%u], %s;",
+                          fn.regs[(size_t)i.a] == Ty::F32 ? "f32" : "b32", i.imm, v.c_str());
+          else
+            std::snprintf(buf, sizeof buf, "st.%s [%%kzout+%u], %s;",
+                          fn.regs[(size_t)i.a] == Ty::F32 ? "f32" : "u32", i.imm, v.c_str());
           line(buf);
           break;
         }
@@ -204,7 +273,8 @@ class Emitter {
   }
 };
 
-std::string function_text(const char* fname, Kind kind, const std::vector<const ir::Shader*>& stages) {
+std::string function_text(const char* fname, Kind kind, const std::vector<const ir::Shader*>& stages,
+                          const std::vector<VertexLayout>& layouts) {
   Emitter e;
   std::string bodies;
   for (size_t p = 0; p < stages.size(); p++) {
@@ -212,7 +282,7 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
     std::string pfx = std::string(fname) + "_p" + std::to_string(p);
     e.out += "$" + pfx + ":\n";
     if (stages[p]) {
-      e.body(stages[p]->fn, pfx, kind);
+      e.body(stages[p]->fn, pfx, kind, p < layouts.size() ? &layouts[p] : nullptr);
     } else {
       if (kind == Kind::Fragment) {
         e.line("mov.b32 %kzt, 0;");
@@ -223,24 +293,43 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
     bodies += e.out;
   }
   std::string s;
-  char buf[256];
-  if (kind == Kind::Fragment)
-    std::snprintf(buf, sizeof buf, ".visible .func (.param .b32 func_retval0) %s(", fname);
-  else
-    std::snprintf(buf, sizeof buf, ".visible .func %s(", fname);
+  char buf[512];
+  if (kind == Kind::Fragment) {
+    std::snprintf(buf, sizeof buf,
+                  ".visible .func (.param .b32 func_retval0) %s(\n  .param .b32 %s_pipe,\n  .param .b64 %s_in,\n"
+                  "  .param .b64 %s_push,\n  .param .b64 %s_out\n)\n{\n",
+                  fname, fname, fname, fname, fname);
+  } else if (kind == Kind::VertexPos) {
+    std::snprintf(buf, sizeof buf,
+                  ".visible .func (.param .align 16 .b8 func_retval0[16]) %s(\n  .param .b32 %s_pipe,\n"
+                  "  .param .b64 %s_draw,\n  .param .b32 %s_vid,\n  .param .b32 %s_iid,\n  .param .b64 %s_push\n)\n{\n",
+                  fname, fname, fname, fname, fname, fname);
+  } else {
+    std::snprintf(buf, sizeof buf,
+                  ".visible .func %s(\n  .param .b32 %s_pipe,\n  .param .b64 %s_draw,\n  .param .b32 %s_vid,\n"
+                  "  .param .b32 %s_iid,\n  .param .b64 %s_push,\n  .param .b64 %s_out\n)\n{\n",
+                  fname, fname, fname, fname, fname, fname, fname);
+  }
   s += buf;
-  std::snprintf(buf, sizeof buf,
-                "\n  .param .b32 %s_pipe,\n  .param .b64 %s_in,\n  .param .b64 %s_push,\n  .param .b64 %s_out\n)\n{\n",
-                fname, fname, fname, fname);
-  s += buf;
-  s += "  .reg .b32 %kzsel, %kzt;\n  .reg .b64 %kzin, %kzpush, %kzout;\n  .reg .pred %kzp;\n";
+  s += "  .reg .b32 %kzsel, %kzt, %kzvid, %kziid;\n  .reg .b64 %kzin, %kzpush, %kzout, %kzdraw, %kzoff;\n"
+       "  .reg .b64 %kzvb<8>;\n  .reg .pred %kzp;\n";
   if (e.nf) s += "  .reg .f32 %f<" + std::to_string(e.nf) + ">;\n";
   if (e.nr) s += "  .reg .b32 %r<" + std::to_string(e.nr) + ">;\n";
   if (e.np) s += "  .reg .pred %p<" + std::to_string(e.np) + ">;\n";
-  std::snprintf(buf, sizeof buf,
-                "  ld.param.u32 %%kzsel, [%s_pipe];\n  ld.param.u64 %%kzin, [%s_in];\n  ld.param.u64 %%kzpush, [%s_push];\n"
-                "  cvta.to.global.u64 %%kzpush, %%kzpush;\n  ld.param.u64 %%kzout, [%s_out];\n",
-                fname, fname, fname, fname);
+  std::snprintf(buf, sizeof buf, "  ld.param.u32 %%kzsel, [%s_pipe];\n  ld.param.u64 %%kzpush, [%s_push];\n"
+                                 "  cvta.to.global.u64 %%kzpush, %%kzpush;\n", fname, fname);
+  s += buf;
+  if (kind == Kind::Fragment) {
+    std::snprintf(buf, sizeof buf, "  ld.param.u64 %%kzin, [%s_in];\n  ld.param.u64 %%kzout, [%s_out];\n", fname, fname);
+  } else {
+    std::snprintf(buf, sizeof buf,
+                  "  ld.param.u64 %%kzdraw, [%s_draw];\n  cvta.to.global.u64 %%kzdraw, %%kzdraw;\n"
+                  "  ld.param.u32 %%kzvid, [%s_vid];\n  ld.param.u32 %%kziid, [%s_iid];\n",
+                  fname, fname, fname);
+    s += buf;
+    if (kind == Kind::VertexFull) std::snprintf(buf, sizeof buf, "  ld.param.u64 %%kzout, [%s_out];\n", fname);
+    else buf[0] = 0;
+  }
   s += buf;
   for (size_t p = 0; p + 1 < stages.size(); p++) {
     std::snprintf(buf, sizeof buf, "  setp.eq.u32 %%kzp, %%kzsel, %zu;\n  @%%kzp bra $%s_p%zu;\n", p, fname, p);
@@ -260,11 +349,12 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
 
 }  // namespace
 
-std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vector<const ir::Shader*>& fs) {
+std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vector<const ir::Shader*>& fs,
+                        const std::vector<VertexLayout>& layouts) {
   std::string s = ".version 9.0\n.target sm_103a\n.address_size 64\n\n";
-  s += function_text("kz_vs", Kind::VertexFull, vs);
-  s += function_text("kz_vs_pos", Kind::VertexPos, vs);
-  s += function_text("kz_fs", Kind::Fragment, fs);
+  s += function_text("kz_vs", Kind::VertexFull, vs, layouts);
+  s += function_text("kz_vs_pos", Kind::VertexPos, vs, layouts);
+  s += function_text("kz_fs", Kind::Fragment, fs, {});
   return s;
 }
 

@@ -12,9 +12,18 @@
 namespace kz {
 namespace ptx {
 
+/* vertex input state of a pipeline, as the generated vertex-shader code fetches it */
+struct VertexLayout {
+  uint32_t num_attrs = 0;
+  uint32_t location[8] = {}, binding[8] = {}, format[8] = {}, offset[8] = {}; /* format: KzAttrFormat */
+  uint32_t stride[8] = {};
+  uint32_t instanced = 0; /* bit b: binding b advances per instance */
+};
+
 /* PTX module defining kz_vs / kz_vs_pos / kz_fs for a pipeline set (entry p = pipeline index p;
  * a null fragment stage yields a fragment function that writes nothing) */
-std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vector<const ir::Shader*>& fs);
+std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vector<const ir::Shader*>& fs,
+                        const std::vector<VertexLayout>& layouts);
 
 /* nvJitLink the relocatable pipeline-kernel object with the shader PTX; returns "" on success */
 std::string link(const std::string& ptx, const void* object, size_t object_size, std::vector<char>& cubin);

@@ -1346,12 +1346,16 @@ bool Translator::do_insn(const Insn& in) {
       Val* sel = val(o[0]);
       if (!sel) return false;
       std::vector<std::pair<uint32_t, uint32_t>> cases; /* (IR label of the trampoline, target) */
-      for (size_t i = 2; i + 1 < o.size(); i += 2) {
+      /* literals are as wide as the selector; 64-bit selectors are carried in 32 bits, so a case
+       * matches on its low word only when its high word is zero */
+      size_t lw = ty(sel->type).width > 32 ? 2 : 1;
+      for (size_t i = 2; i + lw < o.size(); i += lw + 1) {
+        if (lw == 2 && o[i + 1] != 0) continue;
         int32_t k = konst(Ty::B32, o[i]);
         int32_t p = op2(Op::SetpU, Ty::Pred, sel->regs[0], k, CmpEq);
         uint32_t l = fn_.label();
         bra_if(p, l);
-        cases.push_back({l, o[i + 1]});
+        cases.push_back({l, o[i + lw]});
       }
       if (!branch_to(o[1])) return false;
       for (auto& cs : cases) {
