@@ -461,6 +461,8 @@ void free_lowered(Lowered* low) {
   device_free(low->d_records);
   device_free(low->d_bins);
   device_free(low->d_tiles);
+  device_free(low->d_vis);
+  low->d_vis = nullptr;
   if (low->h_status) cudaFreeHost(low->h_status);
   low->exec = nullptr;
   low->graph = nullptr;
@@ -617,6 +619,21 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
           cudaLaunchConfig_t cfg = {};
           cfg.blockDim = dim3(256);
           cfg.stream = st;
+          if (seg.mode == KZ_MODE_VISIBILITY) {
+            cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (seg.width * seg.height + 255) / 256)));
+            cudaLaunchKernelExC(&cfg, (const void*)ks->vis_init, args);
+            if (seg.num_chunks) {
+              cfg.gridDim = dim3(seg.num_chunks);
+              cudaLaunchKernelExC(&cfg, (const void*)ks->vis_geometry, args);
+              cfg.gridDim = dim3(grid_cap(dev));
+              cudaLaunchKernelExC(&cfg, (const void*)ks->vis_large, args);
+              launches += 2;
+            }
+            cfg.gridDim = dim3(grid_cap(dev));
+            cudaLaunchKernelExC(&cfg, (const void*)ks->vis_resolve, args);
+            launches += 2;
+            continue;
+          }
           if (seg.num_chunks) {
             cfg.gridDim = dim3(seg.num_chunks);
             cudaLaunchKernelExC(&cfg, (const void*)ks->geometry, args);
@@ -789,12 +806,21 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   r = device_alloc(std::max<size_t>(4, (size_t)(low.max_tiles + 1) * 3 * 4), &p);
   if (r != VK_SUCCESS) return r;
   low.d_tiles = static_cast<uint32_t*>(p);
+  size_t vis_px = 0;
+  for (const KzSegment& sg : low.segments)
+    if (sg.mode == KZ_MODE_VISIBILITY) vis_px = std::max(vis_px, (size_t)sg.width * sg.height);
+  if (vis_px) {
+    r = device_alloc(vis_px * 8, &p);
+    if (r != VK_SUCCESS) return r;
+    low.d_vis = static_cast<char*>(p);
+  }
   for (size_t i = 0; i < low.segments.size(); i++) {
     KzSegment& s = low.segments[i];
     s.tile_count = (uint64_t)(uintptr_t)low.d_tiles;
     s.tile_offset = (uint64_t)(uintptr_t)(low.d_tiles + low.max_tiles);
     s.tile_cursor = (uint64_t)(uintptr_t)(low.d_tiles + 2 * (size_t)low.max_tiles + 1);
     s.counters = (uint64_t)(uintptr_t)(low.d_counters + i);
+    s.vis = s.mode == KZ_MODE_VISIBILITY ? (uint64_t)(uintptr_t)low.d_vis : 0;
   }
   r = size_scratch(dev, low, (uint32_t)rec_cap, (uint32_t)pair_cap);
   if (r != VK_SUCCESS) return r;
@@ -1055,7 +1081,7 @@ extern "C" KZ_API int kzGetCommandBufferStats(VkCommandBuffer cbh, KzCommandBuff
     if (op.kind == kz::OpKind::Pass) {
       if (low.mode == 0) launches += op.seg_end > op.seg_begin ? 1 : 0;
       else
-        for (uint32_t s = op.seg_begin; s < op.seg_end; s++) launches += (low.segments[s].num_chunks ? 4 : 3);
+        for (uint32_t s = op.seg_begin; s < op.seg_end; s++) launches += (low.segments[s].num_chunks ? 4 : 2);
     } else if (op.kind == kz::OpKind::Clear || op.kind == kz::OpKind::Fill) {
       launches++;
     }

@@ -141,7 +141,9 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
     cudaKernel_t* k;
   } names[] = {{"kz_k_geometry", &ks->geometry}, {"kz_k_scan", &ks->scan},
                {"kz_k_bin", &ks->bin},           {"kz_k_raster", &ks->raster},
-               {"kz_k_persistent", &ks->persistent}, {"kz_k_clear", &ks->clear}};
+               {"kz_k_persistent", &ks->persistent}, {"kz_k_clear", &ks->clear},
+               {"kz_k_vis_init", &ks->vis_init}, {"kz_k_vis_geometry", &ks->vis_geometry},
+               {"kz_k_vis_large", &ks->vis_large}, {"kz_k_vis_resolve", &ks->vis_resolve}};
   for (auto& n : names) {
     if (cudaLibraryGetKernel(n.k, ks->lib, n.name) != cudaSuccess) {
       err = std::string("kernel ") + n.name + " missing from the linked module";

@@ -135,7 +135,8 @@ struct PipelineCache {};
 struct KernelSet {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t geometry = nullptr, scan = nullptr, bin = nullptr, raster = nullptr, persistent = nullptr,
-               clear = nullptr;
+               clear = nullptr, vis_init = nullptr, vis_geometry = nullptr, vis_large = nullptr,
+               vis_resolve = nullptr;
   int persistent_blocks = 0;
 };
 
@@ -199,6 +200,7 @@ struct Lowered {
   char* d_records = nullptr;
   char* d_bins = nullptr;
   uint32_t* d_tiles = nullptr;
+  char* d_vis = nullptr;
   KzSegCounters* d_counters = nullptr;
   KzStatus* d_status = nullptr;
   KzStatus* h_status = nullptr;

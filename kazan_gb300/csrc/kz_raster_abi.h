@@ -5,11 +5,20 @@
  * list of raster segments (KzSegment).  A segment is a run of draws that render into one framebuffer
  * with a single raster mode; the kernels process one segment at a time:
  *
- *   geometry  : per triangle  -> vertex fetch + position-only vertex shader, clip, project, 16.8 snap,
- *                                cull, bounding box; writes a KzTriRecord and counts screen-tile pairs
+ * Opaque segments (visibility mode) resolve depth order-independently through a per-pixel 64-bit key
+ * (depth, primitive sequence number) in HBM/L2:
+ *   vis init  : per pixel     -> key of the loaded or cleared depth
+ *   geometry  : per triangle  -> index fetch, position-only vertex shader (each vertex of a 256-triangle
+ *                                chunk shaded once), clip, project, 16.8 snap, cull; small triangles are
+ *                                rasterised on the spot into the keys (atomicMin), large ones become
+ *                                records split into 8x8-pixel jobs
+ *   large     : per job       -> warp-wide edge tests of one record over up to 16 blocks
+ *   resolve   : per pixel     -> one fragment-shader call for the key's primitive, framebuffer store
+ * Ordered segments (blending, discard, other compare ops) keep primitive order through screen tiles:
+ *   geometry  : per triangle  -> KzTriRecord + screen-tile pair counts
  *   tile scan : per tile      -> exclusive prefix sum of the pair counts (bin offsets)
  *   bin       : per record    -> scatter the record index into every overlapped tile's bin
- *   raster    : per tile      -> exact edge tests, depth, fragment shader, blend, framebuffer store
+ *   raster    : per tile      -> bin sorted by primitive, per-pixel in-order depth test, blend, store
  *
  * The reference driver declares the entry points of this path but implements none of them
  * (vulkan-driver/src/api_impl.rs:4632-4653 vkCmdDraw/vkCmdDrawIndexed, :4780 vkCmdClearColorImage,
@@ -136,8 +145,8 @@ typedef struct KzTriRecord {
 
 /* per-segment scratch counters (zeroed before the segment runs) */
 typedef struct KzSegCounters {
-  uint32_t rec_count;   /* records written */
-  uint32_t pair_count;  /* (tile, record) pairs */
+  uint32_t rec_count;   /* records written (visibility mode: large triangles only) */
+  uint32_t pair_count;  /* (tile, record) pairs (visibility mode: large-triangle jobs) */
   uint32_t geom_next;   /* work-stealing cursor over chunks */
   uint32_t bin_next;    /* work-stealing cursor over records */
   uint32_t tile_next;   /* work-stealing cursor over tiles */
@@ -173,6 +182,7 @@ typedef struct KzSegment {
   uint64_t tile_cursor;      /* u32[tiles] */
   uint64_t bins;             /* u32[pair_cap] */
   uint64_t counters;         /* KzSegCounters* */
+  uint64_t vis;              /* visibility mode: u64 (depth, primitive) key per pixel, width * height */
   uint32_t rec_cap, pair_cap;
   uint32_t segment_index;
   uint32_t pad;

@@ -22,6 +22,7 @@
 #include <stdint.h>
 
 #include "../kz_raster_abi.h"
+#include "kz_exact.h"
 
 /* vertex shader functions fetch their own attributes from the draw's vertex buffers */
 extern "C" __device__ void kz_vs(uint32_t pipe, const KzDraw* draw, uint32_t vid, uint32_t iid, const uint8_t* push,
@@ -250,7 +251,7 @@ __device__ bool make_record(const KzDraw& d, const KzPipe& pp, Proj v[3], KzTriR
   r.z0 = v[0].z;
   r.dz1 = fsub(v[1].z, v[0].z);
   r.dz2 = fsub(v[2].z, v[0].z);
-  r.inv_s = fdiv(1.0f, __ll2float_rn(S));
+  r.inv_s = fdiv(1.0f, kz_i64_to_f32(S));
   r.info = info;
   r.bb0 = (uint32_t)bx0 | ((uint32_t)by0 << 16);
   r.bb1 = (uint32_t)bx1 | ((uint32_t)by1 << 16);
@@ -403,9 +404,9 @@ __device__ uint32_t shade_pixel(const Ctx& c, const Shade& s, int32_t x, int32_t
                                 float col[4]) {
   const KzPipe& p = c.pipes[s.pipe];
   const KzDraw& d = c.draws[s.draw];
-  float l0 = fmul(__ll2float_rn(E[0]), s.r.inv_s);
-  float l1 = fmul(__ll2float_rn(E[1]), s.r.inv_s);
-  float l2 = fmul(__ll2float_rn(E[2]), s.r.inv_s);
+  float l0 = fmul(kz_i64_to_f32(E[0]), s.r.inv_s);
+  float l1 = fmul(kz_i64_to_f32(E[1]), s.r.inv_s);
+  float l2 = fmul(kz_i64_to_f32(E[2]), s.r.inv_s);
   float q = ffma(l2, s.iw[2], ffma(l1, s.iw[1], fmul(l0, s.iw[0])));
   float rq = fdiv(1.0f, q);
   KzFsIn in;
@@ -836,150 +837,363 @@ __device__ __forceinline__ float* depth_px(const KzSegment& seg, int32_t x, int3
   return reinterpret_cast<float*>(reinterpret_cast<char*>(seg.depth) + (size_t)y * seg.depth_pitch) + x;
 }
 
-__device__ __forceinline__ void vis_fragment(const KzSegment& seg, const KzTriRecord& r, float zmin, float zmax,
-                                             const TileInfo& ti, unsigned long long* keys, int32_t x, int32_t y,
-                                             int64_t E1, int64_t E2) {
-  float l1 = fmul(__ll2float_rn(E1), r.inv_s), l2 = fmul(__ll2float_rn(E2), r.inv_s);
-  float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
-  z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
-  unsigned long long k = vis_key(seg.vis_key, z, r.g);
-  unsigned long long* slot = &keys[(y - ti.oy) * (int)seg.tile + (x - ti.ox)];
-  if (k < *slot) atomicMin(slot, k);
+/* ================= visibility-buffer path (opaque segments) ================= */
+
+#define KZ_SMALL_PX 32      /* boxes of at most this many pixels are rasterised by their geometry thread */
+#define KZ_JOB_BLOCKS 16    /* 8x8 pixel blocks per large-triangle job */
+#define KZ_VCACHE 1024      /* vertex-cache slots per 256-triangle chunk */
+
+__device__ __forceinline__ unsigned long long* vis_px(const KzSegment& seg, int32_t x, int32_t y) {
+  return reinterpret_cast<unsigned long long*>(seg.vis) + (size_t)y * seg.width + x;
 }
 
-/* one thread walks the record's box inside the tile with incrementally stepped edge functions */
-__device__ uint32_t vis_record_thread(const KzSegment& seg, const KzDraw* draws, const KzTriRecord& r,
-                                      const TileInfo& ti, unsigned long long* keys) {
-  int32_t bx0 = max((int32_t)(r.bb0 & 0xFFFFu), ti.x0), by0 = max((int32_t)(r.bb0 >> 16), ti.y0);
-  int32_t bx1 = min((int32_t)(r.bb1 & 0xFFFFu), ti.x1), by1 = min((int32_t)(r.bb1 >> 16), ti.y1);
-  if (bx0 > bx1 || by0 > by1) return 0;
-  const KzDraw& d = draws[r.draw];
-  float zmin = d.zmin, zmax = d.zmax;
+/* keep the smaller key: a fire-and-forget 64-bit min reduction at L2 (the result is unused, so the
+ * issuing thread never waits for it) */
+__device__ __forceinline__ void vis_store(const KzSegment& seg, unsigned long long k, int32_t x, int32_t y) {
+  atomicMin(vis_px(seg, x, y), k);
+}
+
+__device__ __forceinline__ unsigned long long frag_key(const KzSegment& seg, const KzTriRecord& r, float zmin,
+                                                       float zmax, float fE1, float fE2) {
+  float l1 = fmul(fE1, r.inv_s), l2 = fmul(fE2, r.inv_s);
+  float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
+  z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
+  return vis_key(seg.vis_key, z, r.g);
+}
+
+/* rasterise a small record (box of at most KZ_SMALL_PX pixels) into the keys, one thread */
+__device__ uint32_t vis_small(const KzSegment& seg, const KzTriRecord& r, float zmin, float zmax) {
+  int32_t bx0 = (int32_t)(r.bb0 & 0xFFFFu), by0 = (int32_t)(r.bb0 >> 16);
+  int32_t bx1 = (int32_t)(r.bb1 & 0xFFFFu), by1 = (int32_t)(r.bb1 >> 16);
+  int32_t ox = bx0 * 256 + 128, oy = by0 * 256 + 128;
+  int32_t xr[3], yr[3];
+  bool near = true;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    xr[i] = r.x[i] - ox;
+    yr[i] = r.y[i] - oy;
+    near &= (xr[i] > -8192 && xr[i] < 8192 && yr[i] > -8192 && yr[i] < 8192);
+  }
+  uint32_t frags = 0;
+  if (near) {
+    /* every vertex and pixel centre lies within 32 pixels of the box origin: each product of the edge
+     * function is below 2^28, so 32-bit arithmetic is exact (same integers as the 64-bit form) */
+    int32_t dx[3], dy[3], xa[3], ya[3], thr[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      int a = (k + 1) % 3, b = (k + 2) % 3;
+      dx[k] = xr[b] - xr[a];
+      dy[k] = yr[b] - yr[a];
+      xa[k] = xr[a];
+      ya[k] = yr[a];
+      thr[k] = ((r.info >> k) & 1u) ? 0 : 1;
+    }
+    for (int32_t y = by0; y <= by1; y++) {
+      int32_t py = (y - by0) * 256;
+      int32_t E0 = dx[0] * (py - ya[0]) + dy[0] * xa[0];
+      int32_t E1 = dx[1] * (py - ya[1]) + dy[1] * xa[1];
+      int32_t E2 = dx[2] * (py - ya[2]) + dy[2] * xa[2];
+      for (int32_t x = bx0; x <= bx1; x++) {
+        if (E0 >= thr[0] && E1 >= thr[1] && E2 >= thr[2]) {
+          frags++;
+          vis_store(seg, frag_key(seg, r, zmin, zmax, __int2float_rn(E1), __int2float_rn(E2)), x, y);
+        }
+        E0 -= dy[0] * 256;
+        E1 -= dy[1] * 256;
+        E2 -= dy[2] * 256;
+      }
+    }
+    return frags;
+  }
   Edges e;
   edges_of(r, e);
-  int64_t sx0 = -(int64_t)e.dy[0] * 256, sx1 = -(int64_t)e.dy[1] * 256, sx2 = -(int64_t)e.dy[2] * 256;
   int64_t px0 = (int64_t)bx0 * 256 + 128;
-  uint32_t frags = 0;
   for (int32_t y = by0; y <= by1; y++) {
     int64_t py = (int64_t)y * 256 + 128;
     int64_t E0 = edge_at(e, 0, px0, py), E1 = edge_at(e, 1, px0, py), E2 = edge_at(e, 2, px0, py);
     for (int32_t x = bx0; x <= bx1; x++) {
       if (E0 >= e.thr[0] && E1 >= e.thr[1] && E2 >= e.thr[2]) {
         frags++;
-        vis_fragment(seg, r, zmin, zmax, ti, keys, x, y, E1, E2);
+        vis_store(seg, frag_key(seg, r, zmin, zmax, kz_i64_to_f32(E1), kz_i64_to_f32(E2)), x, y);
       }
-      E0 += sx0;
-      E1 += sx1;
-      E2 += sx2;
+      E0 -= (int64_t)e.dy[0] * 256;
+      E1 -= (int64_t)e.dy[1] * 256;
+      E2 -= (int64_t)e.dy[2] * 256;
     }
   }
   return frags;
 }
 
-/* one warp covers the record's box in 8x4 pixel blocks */
-__device__ uint32_t vis_record_warp(const KzSegment& seg, const KzDraw* draws, const KzTriRecord& r,
-                                    const TileInfo& ti, unsigned long long* keys, int lane) {
-  int32_t bx0 = max((int32_t)(r.bb0 & 0xFFFFu), ti.x0), by0 = max((int32_t)(r.bb0 >> 16), ti.y0);
-  int32_t bx1 = min((int32_t)(r.bb1 & 0xFFFFu), ti.x1), by1 = min((int32_t)(r.bb1 >> 16), ti.y1);
-  if (bx0 > bx1 || by0 > by1) return 0;
-  const KzDraw& d = draws[r.draw];
+__device__ __forceinline__ uint32_t box_area(const KzTriRecord& r) {
+  return ((r.bb1 & 0xFFFFu) - (r.bb0 & 0xFFFFu) + 1) * ((r.bb1 >> 16) - (r.bb0 >> 16) + 1);
+}
+
+__device__ __forceinline__ uint32_t box_blocks(const KzTriRecord& r, uint32_t& nbx) {
+  nbx = ((r.bb1 & 0xFFFFu) - (r.bb0 & 0xFFFFu) + 8) / 8;
+  uint32_t nby = ((r.bb1 >> 16) - (r.bb0 >> 16) + 8) / 8;
+  return nbx * nby;
+}
+
+/* emit a large record and its jobs (job = record index, first block) */
+__device__ void vis_emit_large(const Ctx& c, const KzTriRecord& r) {
+  uint32_t idx = atomicAdd(&c.cnt->rec_count, 1u);
+  store_record(c, idx, r);
+  uint32_t nbx, nb = box_blocks(r, nbx);
+  uint32_t njobs = (nb + KZ_JOB_BLOCKS - 1) / KZ_JOB_BLOCKS;
+  uint32_t j0 = atomicAdd(&c.cnt->pair_count, njobs);
+  uint32_t cap = c.seg->pair_cap / 2;
+  if (idx >= c.seg->rec_cap) return;
+  uint2* jobs = reinterpret_cast<uint2*>(c.seg->bins);
+  for (uint32_t j = 0; j < njobs && j0 + j < cap; j++) jobs[j0 + j] = make_uint2(idx, j * KZ_JOB_BLOCKS);
+}
+
+/* one record: small -> rasterise now, large -> jobs */
+__device__ uint32_t vis_record(const Ctx& c, const KzTriRecord& r) {
+  const KzDraw& d = c.draws[r.draw];
+  if (box_area(r) <= KZ_SMALL_PX) return vis_small(*c.seg, r, d.zmin, d.zmax);
+  vis_emit_large(c, r);
+  return 0;
+}
+
+__device__ __noinline__ uint32_t vis_clipped(const Ctx& c, const KzDraw& d, const KzPipe& p, float pos[3][4],
+                                             uint32_t g, uint32_t di) {
+  ClipV v[KZ_MAX_CLIP_VERTS];
+  for (int j = 0; j < 3; j++)
+    for (int k = 0; k < 4; k++) v[j].c[k] = pos[j][k];
+  int n = clip_polygon(v, 0);
+  uint32_t frags = 0;
+  for (int i = 1; i + 1 < n; i++) {
+    Proj pr[3] = {project(d, v[0].c), project(d, v[i].c), project(d, v[i + 1].c)};
+    KzTriRecord r;
+    bool sw;
+    if (!make_record(d, p, pr, r, sw)) continue;
+    r.g = g;
+    r.draw = di;
+    r.pad = 0;
+    r.info |= (uint32_t)i << 4;
+    frags += vis_record(c, r);
+  }
+  return frags;
+}
+
+/* a shaded vertex as the triangles of a chunk need it: clip position, clip outcode and (when inside
+ * the guard band) its projected 16.8 position and depth */
+struct VEntry {
+  float4 clip;
+  int32_t X, Y;
+  float z;
+  uint32_t code; /* bits 0-5 outside the view volume (x>w, x<-w, y>w, y<-w, z<0, z>w); bits 6-11 outside
+                    a clip plane (near, far, guard band); bit 12 non-finite */
+};
+
+__device__ __forceinline__ VEntry shade_vertex(const KzDraw& d, uint32_t vid, uint32_t iid, const uint8_t* push) {
+  VEntry e;
+  e.clip = kz_vs_pos(d.pipe, &d, vid, iid, push);
+  const float c[4] = {e.clip.x, e.clip.y, e.clip.z, e.clip.w};
+  uint32_t code = 0;
+  if (!(isfinite(c[0]) && isfinite(c[1]) && isfinite(c[2]) && isfinite(c[3]))) {
+    code = 1u << 12;
+  } else {
+    code |= (c[0] > c[3]) ? 1u : 0u;
+    code |= (c[0] < -c[3]) ? 2u : 0u;
+    code |= (c[1] > c[3]) ? 4u : 0u;
+    code |= (c[1] < -c[3]) ? 8u : 0u;
+    code |= (c[2] < 0.0f) ? 16u : 0u;
+    code |= (c[2] > c[3]) ? 32u : 0u;
+#pragma unroll
+    for (int plane = 0; plane < 6; plane++) code |= plane_dist(c, plane) < 0.0f ? (64u << plane) : 0u;
+  }
+  e.X = e.Y = 0;
+  e.z = 0.0f;
+  if (!(code & ((63u << 6) | (1u << 12)))) {
+    Proj p = project(d, c);
+    e.X = p.X;
+    e.Y = p.Y;
+    e.z = p.z;
+  }
+  e.code = code;
+  return e;
+}
+
+/* set up and rasterise (small) or emit (large) the triangle of three shaded vertices */
+__device__ uint32_t vis_triangle(const Ctx& c, const KzDraw& d, const KzPipe& p, uint32_t di, uint32_t g,
+                                 const VEntry* v[3]) {
+  uint32_t any = v[0]->code | v[1]->code | v[2]->code;
+  if (any & (1u << 12)) return 0;
+  if (v[0]->code & v[1]->code & v[2]->code & 63u) return 0; /* outside one view-volume plane */
+  if (any & (63u << 6)) {
+    float pos[3][4];
+    for (int j = 0; j < 3; j++) {
+      pos[j][0] = v[j]->clip.x;
+      pos[j][1] = v[j]->clip.y;
+      pos[j][2] = v[j]->clip.z;
+      pos[j][3] = v[j]->clip.w;
+    }
+    return vis_clipped(c, d, p, pos, g, di);
+  }
+  Proj pr[3];
+  for (int j = 0; j < 3; j++) {
+    pr[j].X = v[j]->X;
+    pr[j].Y = v[j]->Y;
+    pr[j].z = v[j]->z;
+    pr[j].iw = 0.0f;
+  }
+  KzTriRecord r;
+  bool sw;
+  if (!make_record(d, p, pr, r, sw)) return 0;
+  r.g = g;
+  r.draw = di;
+  r.pad = 0;
+  if (box_area(r) <= KZ_SMALL_PX) return vis_small(*c.seg, r, d.zmin, d.zmax);
+  vis_emit_large(c, r);
+  return 0;
+}
+
+/* geometry of one 256-triangle chunk: the chunk's vertices are shaded and projected once each through a
+ * shared-memory cache keyed by vertex index (single-instance draws), then every thread sets up its
+ * triangle.  `reuse`: the block goes on to another chunk and must not overwrite the cache early. */
+__device__ void vis_geometry_chunk(const Ctx& c, uint32_t chunk, unsigned char* smem, bool reuse) {
+  const KzChunk ch = reinterpret_cast<const KzChunk*>(c.f->chunks)[chunk];
+  const KzDraw& d = c.draws[ch.draw];
+  const KzPipe& p = c.pipes[d.pipe];
+  const uint8_t* push = push_ptr(*c.f, d);
+  bool active = threadIdx.x < ch.count;
+  uint32_t local = ch.first + threadIdx.x;
+  uint32_t vid[3] = {0, 0, 0}, iid = 0;
+  if (active) tri_vertices(d, local, vid, iid);
+  uint32_t g = d.prim_base + local;
+  uint32_t frags = 0;
+  if (d.instance_count == 1) {
+    uint32_t* keys = reinterpret_cast<uint32_t*>(smem);
+    VEntry* cache = reinterpret_cast<VEntry*>(smem + KZ_VCACHE * 4);
+    for (int i = threadIdx.x; i < KZ_VCACHE; i += blockDim.x) keys[i] = 0xFFFFFFFFu;
+    __syncthreads();
+    uint32_t slot[3] = {0, 0, 0};
+    uint32_t owned = 0;
+    if (active) {
+      for (int j = 0; j < 3; j++) {
+        uint32_t vv = vid[j];
+        uint32_t h = (vv * 2654435761u) >> 22;
+        /* at most 768 keys in 1024 slots: the probe always ends */
+        for (;;) {
+          uint32_t old = atomicCAS(&keys[h], 0xFFFFFFFFu, vv);
+          if (old == 0xFFFFFFFFu) {
+            owned |= 1u << j;
+            break;
+          }
+          if (old == vv) break;
+          h = (h + 1) & (KZ_VCACHE - 1);
+        }
+        slot[j] = h;
+      }
+    }
+    __syncthreads();
+    for (int j = 0; j < 3; j++)
+      if (owned & (1u << j)) cache[slot[j]] = shade_vertex(d, vid[j], iid, push);
+    __syncthreads();
+    if (active) {
+      const VEntry* v[3] = {&cache[slot[0]], &cache[slot[1]], &cache[slot[2]]};
+      frags = vis_triangle(c, d, p, ch.draw, g, v);
+    }
+    if (reuse) __syncthreads();
+  } else if (active) {
+    VEntry e[3];
+    for (int j = 0; j < 3; j++) e[j] = shade_vertex(d, vid[j], iid, push);
+    const VEntry* v[3] = {&e[0], &e[1], &e[2]};
+    frags = vis_triangle(c, d, p, ch.draw, g, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
+  if ((threadIdx.x & 31) == 0 && frags) {
+    atomicAdd(&c.cnt->fragments, frags);
+    atomicAdd(&c.st->fragments_lo, frags);
+  }
+}
+
+/* one large-triangle job, one warp: up to KZ_JOB_BLOCKS 8x8 blocks of the record's box */
+__device__ uint32_t vis_large_job(const Ctx& c, uint2 job, int lane) {
+  const KzSegment& seg = *c.seg;
+  const KzTriRecord r = load_record(seg, job.x);
+  const KzDraw& d = c.draws[r.draw];
   float zmin = d.zmin, zmax = d.zmax;
   Edges e;
   edges_of(r, e);
+  int32_t bx0 = (int32_t)(r.bb0 & 0xFFFFu), by0 = (int32_t)(r.bb0 >> 16);
+  int32_t bx1 = (int32_t)(r.bb1 & 0xFFFFu), by1 = (int32_t)(r.bb1 >> 16);
+  uint32_t nbx, nb = box_blocks(r, nbx);
+  uint32_t b1 = min(nb, job.y + KZ_JOB_BLOCKS);
   int lx = lane & 7, ly = lane >> 3;
   uint32_t frags = 0;
-  for (int32_t yb = by0; yb <= by1; yb += 4) {
-    for (int32_t xb = bx0; xb <= bx1; xb += 8) {
-      int32_t x = xb + lx, y = yb + ly;
+  for (uint32_t b = job.y; b < b1; b++) {
+    int32_t x0 = bx0 + (int32_t)(b % nbx) * 8, y0 = by0 + (int32_t)(b / nbx) * 8;
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+      int32_t x = x0 + lx, y = y0 + ly + 4 * half;
       if (x > bx1 || y > by1) continue;
       int64_t px = (int64_t)x * 256 + 128, py = (int64_t)y * 256 + 128;
       int64_t E0 = edge_at(e, 0, px, py), E1 = edge_at(e, 1, px, py), E2 = edge_at(e, 2, px, py);
       if (E0 < e.thr[0] || E1 < e.thr[1] || E2 < e.thr[2]) continue;
       frags++;
-      vis_fragment(seg, r, zmin, zmax, ti, keys, x, y, E1, E2);
+      vis_store(seg, frag_key(seg, r, zmin, zmax, kz_i64_to_f32(E1), kz_i64_to_f32(E2)), x, y);
     }
   }
   return frags;
 }
 
-__device__ void raster_tile_visibility(const Ctx& c, uint32_t t, unsigned char* smem) {
-  const KzSegment& seg = *c.seg;
-  TileInfo ti;
-  if (!tile_info(seg, t, ti)) return;
-  bool clear_c = seg.color_load == KZ_LOAD_CLEAR, clear_d = seg.depth_load == KZ_LOAD_CLEAR;
-  if (ti.n == 0 && !clear_c && !clear_d) return;
-  int T = (int)seg.tile;
-  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem);
-  uint32_t* qcount = reinterpret_cast<uint32_t*>(smem + (size_t)T * T * 8);
-  uint32_t* queue = qcount + 1;
-  const bool has_depth = seg.depth != 0;
-  for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
-    int32_t x = ti.ox + i % T, y = ti.oy + i / T;
+__device__ void vis_init_range(const KzSegment& seg, size_t i0, size_t stride) {
+  size_t n = (size_t)seg.width * seg.height;
+  bool clear_d = seg.depth_load == KZ_LOAD_CLEAR;
+  for (size_t i = i0; i < n; i += stride) {
+    int32_t x = (int32_t)(i % seg.width), y = (int32_t)(i / seg.width);
     float dv = 1.0f;
-    if (has_depth && x >= ti.x0 && x <= ti.x1 && y >= ti.y0 && y <= ti.y1)
-      dv = clear_d ? seg.clear_depth : *depth_px(seg, x, y);
-    keys[i] = vis_init(seg.vis_key, dv);
+    if (seg.depth) dv = clear_d ? seg.clear_depth : *depth_px(seg, x, y);
+    reinterpret_cast<unsigned long long*>(seg.vis)[i] = vis_init(seg.vis_key, dv);
   }
-  if (threadIdx.x == 0) *qcount = 0;
-  __syncthreads();
-  const uint32_t* bins = reinterpret_cast<const uint32_t*>(seg.bins) + ti.base;
-  uint32_t frags = 0;
-  for (uint32_t e = threadIdx.x; e < ti.n; e += blockDim.x) {
-    uint32_t ri = bins[e];
-    const KzTriRecord r = load_record(seg, ri);
-    int32_t bx0 = max((int32_t)(r.bb0 & 0xFFFFu), ti.x0), by0 = max((int32_t)(r.bb0 >> 16), ti.y0);
-    int32_t bx1 = min((int32_t)(r.bb1 & 0xFFFFu), ti.x1), by1 = min((int32_t)(r.bb1 >> 16), ti.y1);
-    int area = (bx1 - bx0 + 1) * (by1 - by0 + 1);
-    if (area > 48) {
-      uint32_t q = atomicAdd(qcount, 1u);
-      if (q < 1024) {
-        queue[q] = ri;
-        continue;
+}
+
+/* resolve 32 consecutive pixels of one row, one warp */
+__device__ void vis_resolve_run(const Ctx& c, uint32_t item) {
+  const KzSegment& seg = *c.seg;
+  uint32_t runs = (seg.width + 31) / 32;
+  int32_t y = (int32_t)(item / runs), x = (int32_t)(item % runs) * 32 + (int32_t)(threadIdx.x & 31);
+  if (x >= (int32_t)seg.width || x < seg.area[0] || x >= seg.area[2] || y < seg.area[1] || y >= seg.area[3]) return;
+  bool clear_c = seg.color_load == KZ_LOAD_CLEAR, clear_d = seg.depth_load == KZ_LOAD_CLEAR;
+  const bool has_color = seg.color != 0, has_depth = seg.depth != 0;
+  uint32_t g;
+  float z;
+  if (vis_decode(seg.vis_key, *vis_px(seg, x, y), g, z)) {
+    Shade s;
+    if (shade_setup(c, g, x, y, 0, s)) {
+      int64_t E[3];
+      covers(s.r, x, y, E);
+      float col[4];
+      shade_pixel(c, s, x, y, E, z, col);
+      const KzPipe& p = c.pipes[s.pipe];
+      if (has_color) {
+        uint32_t dst = clear_c ? seg.clear_color : *color_px(seg, x, y);
+        *color_px(seg, x, y) = from_rgba(color_write(p, to_rgba(dst, seg.color_format), col), seg.color_format);
       }
+      if (has_depth && p.depth_test && p.depth_write) *depth_px(seg, x, y) = z;
+      else if (has_depth && clear_d) *depth_px(seg, x, y) = seg.clear_depth;
+      return;
     }
-    frags += vis_record_thread(seg, c.draws, r, ti, keys);
   }
-  __syncthreads();
-  uint32_t nq = min(*qcount, 1024u);
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  for (uint32_t q = warp; q < nq; q += nwarps) {
-    const KzTriRecord rr = load_record(seg, queue[q]);
-    frags += vis_record_warp(seg, c.draws, rr, ti, keys, lane);
+  if (has_color && clear_c) *color_px(seg, x, y) = seg.clear_color;
+  if (has_depth && clear_d) *depth_px(seg, x, y) = seg.clear_depth;
+}
+
+/* after geometry: large-triangle scratch overflow check (every block reads the same final counts) */
+__device__ bool vis_check(const Ctx& c, uint32_t s) {
+  uint32_t recs = *reinterpret_cast<volatile uint32_t*>(&c.cnt->rec_count);
+  uint32_t jobs = *reinterpret_cast<volatile uint32_t*>(&c.cnt->pair_count);
+  uint32_t bits = 0;
+  if (recs > c.seg->rec_cap) bits |= KZ_STATUS_RECORD_OVERFLOW;
+  if (jobs > c.seg->pair_cap / 2) bits |= KZ_STATUS_PAIR_OVERFLOW;
+  if (bits && threadIdx.x == 0 && blockIdx.x == 0) {
+    atomicMax(&c.st->need_records, recs);
+    atomicMax(&c.st->need_pairs, jobs * 2);
+    mark_failed(c.st, bits, s);
   }
-  __syncthreads();
-  if (frags) {
-    atomicAdd(&c.cnt->fragments, frags);
-    atomicAdd(&c.st->fragments_lo, frags);
-  }
-  /* resolve: one fragment-shader call per pixel whose key holds a primitive */
-  const bool has_color = seg.color != 0;
-  for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
-    int32_t x = ti.ox + i % T, y = ti.oy + i / T;
-    if (x < ti.x0 || x > ti.x1 || y < ti.y0 || y > ti.y1) continue;
-    uint32_t g;
-    float z;
-    bool frag = vis_decode(seg.vis_key, keys[i], g, z);
-    if (frag) {
-      Shade s;
-      if (shade_setup(c, g, x, y, 0, s)) {
-        int64_t E[3];
-        covers(s.r, x, y, E);
-        float col[4];
-        shade_pixel(c, s, x, y, E, z, col);
-        const KzPipe& p = c.pipes[s.pipe];
-        if (has_color) {
-          uint32_t dst = clear_c ? seg.clear_color : *color_px(seg, x, y);
-          uint32_t out = color_write(p, to_rgba(dst, seg.color_format), col);
-          *color_px(seg, x, y) = from_rgba(out, seg.color_format);
-        }
-        if (has_depth && p.depth_test && p.depth_write) *depth_px(seg, x, y) = z;
-        else if (has_depth && clear_d) *depth_px(seg, x, y) = seg.clear_depth;
-        continue;
-      }
-    }
-    if (has_color && clear_c) *color_px(seg, x, y) = seg.clear_color;
-    if (has_depth && clear_d) *depth_px(seg, x, y) = seg.clear_depth;
-  }
+  return bits == 0;
 }
 
 /* ordered mode: per-pixel in-order processing of the tile's bin, sorted by primitive */
@@ -1073,7 +1287,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
         int64_t E[3];
         if (!covers(r, x, y, E)) continue;
         frags++;
-        float l1 = fmul(__ll2float_rn(E[1]), r.inv_s), l2 = fmul(__ll2float_rn(E[2]), r.inv_s);
+        float l1 = fmul(kz_i64_to_f32(E[1]), r.inv_s), l2 = fmul(kz_i64_to_f32(E[2]), r.inv_s);
         float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
         z = fadd(fminf(fmaxf(z, d.zmin), d.zmax), 0.0f);
         float col[4];
@@ -1103,8 +1317,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
 }
 
 __device__ void raster_tile(const Ctx& c, uint32_t t, unsigned char* smem, uint32_t s) {
-  if (c.seg->mode == KZ_MODE_VISIBILITY) raster_tile_visibility(c, t, smem);
-  else raster_tile_ordered(c, t, smem, s);
+  raster_tile_ordered(c, t, smem, s);
   __syncthreads();
   /* leave the tile counts at zero for the next segment */
   if (threadIdx.x == 0) reinterpret_cast<uint32_t*>(c.seg->tile_count)[t] = 0;
@@ -1197,9 +1410,45 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 2) kz_k_raster(KzFrame 
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) raster_tile(c, t, smem, s);
 }
 
+extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_vis_init(KzFrame f, uint32_t s) {
+  Ctx c = make_ctx(f, s);
+  if (segment_blocked(c, s)) return;
+  vis_init_range(*c.seg, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+}
+
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_vis_geometry(KzFrame f, uint32_t s) {
+  __shared__ __align__(16) unsigned char cache[KZ_VCACHE * (4 + sizeof(VEntry))];
+  Ctx c = make_ctx(f, s);
+  if (segment_blocked(c, s)) return;
+  if (blockIdx.x < c.seg->num_chunks) vis_geometry_chunk(c, c.seg->first_chunk + blockIdx.x, cache, false);
+}
+
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_vis_large(KzFrame f, uint32_t s) {
+  Ctx c = make_ctx(f, s);
+  if (segment_blocked(c, s) || !vis_check(c, s)) return;
+  uint32_t njobs = c.cnt->pair_count;
+  const uint2* jobs = reinterpret_cast<const uint2*>(c.seg->bins);
+  uint32_t warps = gridDim.x * (blockDim.x >> 5), w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  uint32_t frags = 0;
+  for (uint32_t j = w; j < njobs; j += warps) frags += vis_large_job(c, jobs[j], threadIdx.x & 31);
+  for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
+  if ((threadIdx.x & 31) == 0 && frags) {
+    atomicAdd(&c.cnt->fragments, frags);
+    atomicAdd(&c.st->fragments_lo, frags);
+  }
+}
+
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 2) kz_k_vis_resolve(KzFrame f, uint32_t s) {
+  Ctx c = make_ctx(f, s);
+  if (segment_blocked(c, s)) return;
+  uint32_t items = ((c.seg->width + 31) / 32) * c.seg->height;
+  uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < items; i += warps) vis_resolve_run(c, i);
+}
+
 /* the whole command buffer in one cooperative launch: phases separated by bounded grid barriers,
  * work stolen from per-segment counters */
-extern "C" __global__ void __launch_bounds__(KZ_THREADS, 2) kz_k_persistent(KzFrame f) {
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFrame f) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t item;
   __shared__ uint32_t scan_sh[KZ_THREADS + 1];
@@ -1208,6 +1457,44 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 2) kz_k_persistent(KzFr
   for (uint32_t s = f.first_segment; s < f.num_segments; s++) {
     Ctx c = make_ctx(f, s);
     if (segment_blocked(c, s)) break;
+    if (c.seg->mode == KZ_MODE_VISIBILITY) {
+      vis_init_range(*c.seg, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+      if (!grid_barrier(st)) return;
+      for (;;) {
+        uint32_t k = grab(&c.cnt->geom_next, &item);
+        if (k >= c.seg->num_chunks) break;
+        vis_geometry_chunk(c, c.seg->first_chunk + k, smem, true);
+      }
+      if (!grid_barrier(st)) return;
+      if (!vis_check(c, s)) break;
+      uint32_t njobs = c.cnt->pair_count;
+      const uint2* jobs = reinterpret_cast<const uint2*>(c.seg->bins);
+      uint32_t frags = 0;
+      int lane = threadIdx.x & 31;
+      for (;;) {
+        uint32_t j = 0;
+        if (lane == 0) j = atomicAdd(&c.cnt->bin_next, 1u);
+        j = __shfl_sync(0xFFFFFFFFu, j, 0);
+        if (j >= njobs) break;
+        frags += vis_large_job(c, jobs[j], lane);
+      }
+      for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
+      if (lane == 0 && frags) {
+        atomicAdd(&c.cnt->fragments, frags);
+        atomicAdd(&c.st->fragments_lo, frags);
+      }
+      if (!grid_barrier(st)) return;
+      uint32_t items = ((c.seg->width + 31) / 32) * c.seg->height;
+      for (;;) {
+        uint32_t i = 0;
+        if (lane == 0) i = atomicAdd(&c.cnt->tile_next, 1u);
+        i = __shfl_sync(0xFFFFFFFFu, i, 0);
+        if (i >= items) break;
+        vis_resolve_run(c, i);
+      }
+      if (!grid_barrier(st)) return;
+      continue;
+    }
     for (;;) {
       uint32_t k = grab(&c.cnt->geom_next, &item);
       if (k >= c.seg->num_chunks) break;
