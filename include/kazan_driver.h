@@ -70,6 +70,29 @@ typedef struct KzCommandBufferStats {
 /* Statistics of a command buffer's lowering and last completed execution (0 = success). */
 KZ_API int kzGetCommandBufferStats(VkCommandBuffer commandBuffer, KzCommandBufferStats* out);
 
+/* No counterpart in the reference.  Renders without allocating device memory, for callers that cannot
+ * call cudaMalloc when they draw: code running while a stream is captured into a CUDA graph (an allocation
+ * breaks the capture), serving loops that must not take the synchronisation an allocation or free may
+ * cause, and programs whose own pool owns all device memory.  The Vulkan path allocates its scratch at
+ * vkEndCommandBuffer; this call uses one fixed scratch array inside the library (about 24 MiB, held on
+ * every GPU that loads the library until the process exits).
+ *
+ * Draws `triangleCount` triangles (non-indexed list, 8 floats per vertex: clip-space x, y, z, w, then
+ * colour r, g, b, a) into a width x height RGBA8 image and D32 depth image (tight rows), both cleared
+ * first: full viewport, depth range [0, 1], depth test LESS with writes, no culling, no blending -- the
+ * same pixels the Vulkan path gives for that pipeline.  Pointers are device pointers owned by the caller;
+ * `stream` is a cudaStream_t (NULL: legacy default stream); the call returns once the work has finished.
+ * Limits: width * height <= 1048576, triangleCount <= 65536, at most 2^20 8x8-block jobs for triangles
+ * larger than 32 pixels.  Returns 0; -1 for arguments beyond the limits (no GPU work); -2 for a CUDA
+ * error; -3 when the large-triangle jobs overflow the scratch.
+ *
+ * The first call on a device looks up the scratch array's device address: make it before any stream
+ * capture.  All calls share the scratch; each call re-initialises what it reads, but calls whose work
+ * overlaps on the GPU (other streams, other threads) race. */
+KZ_API int kzRasterTrianglesNoAlloc(const float* vertices, uint32_t triangleCount, uint32_t width, uint32_t height,
+                                    uint32_t* color, float* depth, const float clearColor[4], float clearDepth,
+                                    void* stream);
+
 #ifdef __cplusplus
 }
 #endif

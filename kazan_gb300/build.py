@@ -4,7 +4,9 @@
                        driver JIT-links it with each pipeline set's shader PTX at run time
   libkazan_driver.so   the Vulkan driver (ICD) + shader compiler + PTX backend, C ABI
                        (include/kazan_driver.h, include/kz_shader_backend.h); CUDA runtime linked
-                       statically, so the library loads on a machine without a GPU driver
+                       statically, so the library loads on a machine without a GPU driver; it also
+                       carries kz_noalloc.o, the allocation-free entry point (pipeline kernels compiled
+                       with a fixed pass-through colour stage)
   libkz_scene.so       seeded synthetic scene generators
 
 Host code is plain C/C++17 with no architecture-specific flags (it builds on x86_64 and aarch64).
@@ -80,11 +82,23 @@ def _compile_cpp(src):
     return obj
 
 
+def _compile_noalloc():
+    src = os.path.join(CSRC, "raster", "kz_noalloc.cu")
+    obj = os.path.join(OUT, "obj", "kz_noalloc.o")
+    deps = [src, os.path.join(CSRC, "raster", "kz_pipeline.cu"), os.path.join(CSRC, "raster", "kz_exact.h"),
+            os.path.join(CSRC, "kz_raster_abi.h"), os.path.join(ROOT, "include", "kazan_driver.h")]
+    if _newer(obj, deps):
+        _run([NVCC, "-c", "-std=c++17"] + ARCH + ["-O3", "-lineinfo", "-fmad=false", "-I", os.path.join(ROOT, "include"),
+             "-Xcompiler", "-fPIC,-fvisibility=hidden", "-o", obj, src])
+    return obj
+
+
 def driver_library():
     os.makedirs(os.path.join(OUT, "obj"), exist_ok=True)
     srcs = [os.path.join(CSRC, s) for s in DRIVER_SOURCES]
-    with concurrent.futures.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
-        objs = list(ex.map(_compile_cpp, srcs))
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(srcs) + 1) as ex:
+        noalloc = ex.submit(_compile_noalloc)
+        objs = list(ex.map(_compile_cpp, srcs)) + [noalloc.result()]
     out = os.path.join(OUT, "libkazan_driver.so")
     if _newer(out, objs):
         lib = os.path.join(CUDA, "lib64")
