@@ -4,7 +4,10 @@
 Workload (default): the batched command buffer - 4,096 vkCmdDrawIndexed draws (log-uniform triangle
 counts in [16, 65536], each its own sphere mesh and MVP push constant, Lambert VS/FS) into a 2048x2048
 RGBA8 + D32 target, seeded synthetic scene (seed 3).  One step = one vkQueueSubmit of the recorded command
-buffer (graph-captured persistent form), i.e. one full render of the scene.
+buffer (--mode batched: one launch per pipeline phase), i.e. one full render of the scene.  The timed
+command buffer is recorded with the driver's kernel timing on, so every kernel launch inside the timed
+region is bracketed by CUDA events on the queue stream; the roofline uses the dominant kernel's mean
+duration from those events.
 
 Printed JSON line (rank 0):
   value      Mtris/s with vertex/index buffers and attachments resident in HBM (device-local memory),
@@ -33,13 +36,13 @@ sys.path.insert(0, ROOT)
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched", choices=["batched", "single", "soup", "blend"])
     ap.add_argument("--ndraws", type=int, default=4096)
     ap.add_argument("--tile", type=int, default=16)
-    ap.add_argument("--mode", default="persistent", choices=["persistent", "batched", "perdraw"])
+    ap.add_argument("--mode", default="batched", choices=["persistent", "batched", "perdraw"])
     ap.add_argument("--no-perdraw", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -70,20 +73,32 @@ class Clocks:
         self.lines = []
 
     def start(self):
+        """start sampling every 20 ms; returns once the first sample has arrived (or after 5 s)"""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
             self.proc = None
+            return
+        t0 = time.monotonic()
+        while not self.lines and time.monotonic() - t0 < 5.0 and self.proc.poll() is None:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
 
-    def stop(self):
+    def window(self, t0, t1):
+        """keep only the samples taken between t0 and t1 (monotonic seconds), plus the first one after t1
+        so that a short timed region still has a sample that covers its end"""
+        inside = [x for x in self.lines if t0 <= x[0] <= t1]
+        after = [x for x in self.lines if x[0] > t1][:1]
+        self.lines = inside + after
+
+    def stop(self, t0=None, t1=None):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -91,9 +106,12 @@ class Clocks:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        self.t.join(timeout=2)
+        if t0 is not None:
+            self.window(t0, t1)
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        for _, line in self.lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -118,21 +136,43 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(workload):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary (None if absent)"""
+def profiled_traffic(workload, kernel):
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu summary (None if absent)"""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(workload)
-    except (OSError, ValueError):
+            return json.load(f).get(workload, {}).get(kernel)
+    except (OSError, ValueError, AttributeError):
         return None
+
+
+def kernel_bytes(scene, kernel):
+    """algorithmic HBM bytes of one launch of `kernel` over the whole scene (one segment):
+      kz_k_persistent            the whole path: 12 T_indexed + S_v V + 64 draws + framebuffer traffic
+      kz_k_vis_geometry / geometry  index + vertex-position bytes + push constants: 12 T_indexed + P V + 64 draws
+                                 (P = 12 B position of the Lambert layout, 16 B of the colour layout)
+      kz_k_vis_resolve           colour + depth stores: W H (4 + 4)
+      kz_k_raster                framebuffer read + write (depth written or not)
+    returns (bytes, formula)"""
+    t_idx = scene.triangles if scene.indexed else 0
+    v = len(scene.vertices) if scene.indexed else 3 * scene.triangles
+    push = 64 * len(scene.draws) if scene.shader == "lambert" else 0
+    pos = 12 if scene.shader == "lambert" else 16
+    wh = scene.width * scene.height
+    if kernel in ("kz_k_vis_geometry", "kz_k_geometry"):
+        return 12 * t_idx + pos * v + push, "12*T_indexed + %d*V + 64*draws" % pos
+    if kernel == "kz_k_vis_resolve":
+        return wh * 8, "W*H*(4+4)"
+    if kernel == "kz_k_raster":
+        return wh * ((4 + 4) * 2 if scene.depth_write else (2 * 4 + 4)), "W*H*framebuffer read+write"
+    return scene.algorithmic_bytes(), "12*T_indexed + S_v*V + 64*draws + W*H*(4+4)*2"
 
 
 def cpu_baseline(scene, budget_s=4.0):
     """the CPU oracle on a bounded prefix of the draws with all host threads; returns Mtris/s and sample"""
     from oracle import kz_oracle
     threads = os.cpu_count() or 1
-    n = 1 if len(scene.draws) > 1 else 1
+    n = 1
     tri, el = 0, 0.0
     while True:
         draws = scene.draws[:n]
@@ -163,11 +203,13 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
     from kazan_gb300 import render
     scene, cfg = make_scene(args)
     r = render.Renderer()
+    # the timed command buffer launches its kernels at submit with timing events around each launch
+    r.drv.set_option("kernel_timing", 1)
     run = render.SceneRun(r, scene, host_visible=False, mode=args.mode, tile=args.tile)
+    r.drv.set_option("kernel_timing", 0)
     stream = torch.cuda.ExternalStream(r.stream())
 
     def barrier():
@@ -177,19 +219,21 @@ def main():
 
     for _ in range(max(3, args.warmup)):
         run.submit()
-    st = run.stats()
+    r.drv.kernel_times(run.cb, reset=True)
     barrier()
     torch.cuda.synchronize()
     clocks = Clocks(local)
     clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0 = time.monotonic()
     e0.record(stream)
     for _ in range(args.steps):
         run.submit(wait=False)
     e1.record(stream)
     e1.synchronize()
+    w1 = time.monotonic()
     r.drv.vkQueueWaitIdle(r.queue)
-    ck = clocks.stop()
+    ck = clocks.stop(w0, w1)
     torch.cuda.synchronize()
     barrier()
     ms = e0.elapsed_time(e1) / args.steps
@@ -198,33 +242,36 @@ def main():
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    # kernel-only device time (CUDA events around the kernels inside the captured graph)
-    kms = []
-    for _ in range(min(3, args.steps)):
-        run.submit()
-        kms.append(run.stats().gpu_ms)
-    kernel_ms = sorted(kms)[len(kms) // 2]
+    # per-kernel device time over the timed submissions (events on the queue stream around each launch)
+    ktimes = r.drv.kernel_times(run.cb)
+    kernels = {k: {"launches": n, "ms_per_launch": round(t / max(n, 1), 4),
+                   "share": round(t / max(sum(x[0] for x in ktimes.values()), 1e-9), 4)}
+               for k, (t, n) in ktimes.items()}
+    dom = max(ktimes, key=lambda k: ktimes[k][0])
+    dom_ms = ktimes[dom][0] / ktimes[dom][1]
     st = run.stats()
     tris = scene.triangles
     value = tris * world / (ms / 1e3) / 1e6
     peak, peak_kind = measured_peak()
-    B = scene.algorithmic_bytes()
-    traffic = profiled_traffic(args.workload)
+    kb, kformula = kernel_bytes(scene, dom)
+    achieved = kb / (dom_ms / 1e3) / 1e9
     out = {"metric": "Mtris/s (batched command buffer, exact coverage)", "value": round(value, 2),
            "unit": "Mtris/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
            "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32+int64 (16.8 fixed-point edges)", "data": "synthetic (seeded scene generator)",
-           "config": dict(cfg, tile=st.tile, mode=args.mode + (" graph-captured" if args.mode != "perdraw" else ""), triangles=tris,
+           "config": dict(cfg, tile=st.tile, mode=args.mode, triangles=tris,
                           l2="inputs larger than L2 (%.0f MB vertex+index per step)" % (
                               (scene.vertices.nbytes + (scene.indices.nbytes if scene.indices is not None else 0))
                               / 1e6), parallelism="replicas" if world > 1 else "single GPU"),
            "gfrag_per_s": round(st.fragments / (ms / 1e3) / 1e9, 3),
            "fragments": int(st.fragments),
-           "roofline": {"bound": "hbm", "achieved": round(B / (kernel_ms / 1e3) / 1e9, 1), "peak": peak,
-                        "unit": "GB/s", "frac": round(B / (kernel_ms / 1e3) / 1e9 / peak, 4),
-                        "traffic": traffic, "algorithmic_bytes": B, "kernel": "kz_k_persistent",
-                        "kernel_ms": round(kernel_ms, 4), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"},
-           "clocks": ck, "gpu_launches": int(st.launches) * args.steps}
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.workload, dom),
+                        "kernel": dom, "kernel_ms": round(dom_ms, 4), "algorithmic_bytes": kb,
+                        "bytes_formula": kformula,
+                        "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"},
+           "kernels": kernels,
+           "clocks": ck, "gpu_launches": int(sum(n for _, n in ktimes.values()))}
     if not args.no_perdraw:
         pd = render.SceneRun(r, scene, host_visible=False, mode="perdraw", tile=args.tile)
         pd.submit()
@@ -244,7 +291,7 @@ def main():
         out["batched_vs_per_draw"] = round(out["value"] / world / out["per_draw"]["value"], 2)
     if not args.no_e2e:
         import numpy as np
-        e2 = render.SceneRun(r, scene, host_visible=True, mode="persistent", tile=args.tile, keep_mapped=True)
+        e2 = render.SceneRun(r, scene, host_visible=True, mode=args.mode, tile=args.tile, keep_mapped=True)
         e2.submit()
         p = r.map(e2.color)
         nbytes = e2.color.pitch * scene.height

@@ -44,8 +44,10 @@ KZ_API PFN_vkVoidFunction vk_icdGetPhysicalDeviceProcAddr(VkInstance instance, c
  *   "tile"  screen-tile side in pixels: "8", "16", "32" or "64"
  *   "trace" "0" / "1": log lowering and linking decisions to stderr
  *   "fault_alloc" "N": the Nth device allocation from now fails with VK_ERROR_OUT_OF_DEVICE_MEMORY
- * Returns 0, or -1 for an unknown key or value.  The KZ_MODE, KZ_TILE, KZ_TRACE and KZ_FAULT=alloc:N
- * environment variables set the initial values. */
+ *   "kernel_timing" "0" / "1": command buffers ended while it is on launch their kernels at each submit
+ *           (no graph capture) with a pair of timing events around every launch; see kzGetKernelTimes
+ * Returns 0, or -1 for an unknown key or value.  The KZ_MODE, KZ_TILE, KZ_TRACE, KZ_KERNEL_TIMING and
+ * KZ_FAULT=alloc:N environment variables set the initial values. */
 KZ_API int kzDriverSetOption(const char* key, const char* value);
 
 /* The CUDA stream (cudaStream_t) a queue executes on, for callers that time submissions with CUDA
@@ -69,6 +71,20 @@ typedef struct KzCommandBufferStats {
 
 /* Statistics of a command buffer's lowering and last completed execution (0 = success). */
 KZ_API int kzGetCommandBufferStats(VkCommandBuffer commandBuffer, KzCommandBufferStats* out);
+
+/* Kernel kinds of kzGetKernelTimes, in array order. */
+#define KZ_KERNEL_KIND_NAMES                                                                          \
+  {"kz_k_persistent", "kz_k_vis_init", "kz_k_vis_geometry", "kz_k_vis_large", "kz_k_vis_resolve",      \
+   "kz_k_geometry",   "kz_k_scan",     "kz_k_bin",          "kz_k_raster",    "kz_k_clear"}
+#define KZ_KERNEL_KINDS 10
+
+/* Device time of a command buffer recorded with "kernel_timing" on: for each kernel kind, the summed
+ * durations (CUDA events on the queue stream around each launch) and the number of launches over all
+ * submissions completed since the last reset.  Fills the first `count` entries of either array (either
+ * may be NULL), resets the sums when `reset` is non-zero, and returns KZ_KERNEL_KINDS (-1 for a bad
+ * handle).  Submissions complete at vkQueueWaitIdle, vkWaitForFences and vkGetFenceStatus. */
+KZ_API int kzGetKernelTimes(VkCommandBuffer commandBuffer, double* totalMs, uint32_t* launches, uint32_t count,
+                            int reset);
 
 /* No counterpart in the reference.  Renders without allocating device memory, for callers that cannot
  * call cudaMalloc when they draw: code running while a stream is captured into a CUDA graph (an allocation

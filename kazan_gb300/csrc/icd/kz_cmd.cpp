@@ -578,8 +578,37 @@ static void upload_tables(Lowered& low) {
 
 static uint32_t grid_cap(Device* dev) { return (uint32_t)std::max(1, dev->pd->sm_count) * 8u; }
 
+static cudaEvent_t timing_event(Device* dev) {
+  if (!dev->timing_pool.empty()) {
+    cudaEvent_t e = dev->timing_pool.back();
+    dev->timing_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+/* one kernel launch; with `timing` set, bracketed by a pair of timing events on the same stream */
+static void launch(Device* dev, std::vector<TimedLaunch>* timing, int kind, const cudaLaunchConfig_t& cfg,
+                   cudaKernel_t fn, void** args) {
+  TimedLaunch t;
+  if (timing) {
+    t.kind = kind;
+    t.before = timing_event(dev);
+    t.after = timing_event(dev);
+    cudaEventRecord(t.before, cfg.stream);
+  }
+  cudaLaunchKernelExC(&cfg, (const void*)fn, args);
+  if (timing) {
+    cudaEventRecord(t.after, cfg.stream);
+    timing->push_back(t);
+  }
+}
+
 /* enqueue the lowered command buffer from segment `start` on */
-static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, bool capture) {
+static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, bool capture,
+                           std::vector<TimedLaunch>* timing = nullptr) {
   Lowered& low = *cb->low;
   Device* dev = cb->dev;
   uint32_t launches = 0;
@@ -609,7 +638,7 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
         at[0].val.cooperative = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        cudaLaunchKernelExC(&cfg, (const void*)ks->persistent, args);
+        launch(dev, timing, KK_PERSISTENT, cfg, ks->persistent, args);
         launches++;
       } else {
         for (uint32_t s = s0; s < lop.seg_end; s++) {
@@ -621,31 +650,31 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
           cfg.stream = st;
           if (seg.mode == KZ_MODE_VISIBILITY) {
             cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (seg.width * seg.height + 255) / 256)));
-            cudaLaunchKernelExC(&cfg, (const void*)ks->vis_init, args);
+            launch(dev, timing, KK_VIS_INIT, cfg, ks->vis_init, args);
             if (seg.num_chunks) {
               cfg.gridDim = dim3(seg.num_chunks);
-              cudaLaunchKernelExC(&cfg, (const void*)ks->vis_geometry, args);
+              launch(dev, timing, KK_VIS_GEOMETRY, cfg, ks->vis_geometry, args);
               cfg.gridDim = dim3(grid_cap(dev));
-              cudaLaunchKernelExC(&cfg, (const void*)ks->vis_large, args);
+              launch(dev, timing, KK_VIS_LARGE, cfg, ks->vis_large, args);
               launches += 2;
             }
             cfg.gridDim = dim3(grid_cap(dev));
-            cudaLaunchKernelExC(&cfg, (const void*)ks->vis_resolve, args);
+            launch(dev, timing, KK_VIS_RESOLVE, cfg, ks->vis_resolve, args);
             launches += 2;
             continue;
           }
           if (seg.num_chunks) {
             cfg.gridDim = dim3(seg.num_chunks);
-            cudaLaunchKernelExC(&cfg, (const void*)ks->geometry, args);
+            launch(dev, timing, KK_GEOMETRY, cfg, ks->geometry, args);
             launches++;
           }
           cfg.gridDim = dim3(1);
-          cudaLaunchKernelExC(&cfg, (const void*)ks->scan, args);
+          launch(dev, timing, KK_SCAN, cfg, ks->scan, args);
           cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (seg.rec_cap + 255) / 256)));
-          cudaLaunchKernelExC(&cfg, (const void*)ks->bin, args);
+          launch(dev, timing, KK_BIN, cfg, ks->bin, args);
           cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, seg.tiles_x * seg.tiles_y)));
           cfg.dynamicSmemBytes = KZ_DYN_SMEM;
-          cudaLaunchKernelExC(&cfg, (const void*)ks->raster, args);
+          launch(dev, timing, KK_RASTER, cfg, ks->raster, args);
           launches += 3;
         }
       }
@@ -663,7 +692,7 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
         long long work = (long long)(x1 - x0) * (y1 - y0) / 4 + 1;
         cfg.gridDim = dim3((unsigned)std::min<long long>(grid_cap(dev), (work + 255) / 256));
         cfg.stream = st;
-        cudaLaunchKernelExC(&cfg, (const void*)ks->clear, args);
+        launch(dev, timing, KK_CLEAR, cfg, ks->clear, args);
         launches++;
       } else if (op.kind == OpKind::Copy) {
         cudaMemcpyAsync(op.dst, op.src, op.bytes, cudaMemcpyDeviceToDevice, st);
@@ -686,6 +715,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   Lowered& low = *cb->low;
   low.mode = options().mode;
   low.tile = options().tile;
+  low.timed = options().kernel_timing != 0;
   std::map<Pipeline*, uint32_t> pipe_index;
   auto pipe_of = [&](Pipeline* p, const float* blend) -> uint32_t {
     auto it = pipe_index.find(p);
@@ -843,7 +873,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
     log_error("pipeline link failed: %s", err.c_str());
     return VK_ERROR_INITIALIZATION_FAILED;
   }
-  if (low.mode != 2) {
+  if (low.mode != 2 && !low.timed) {
     cudaStream_t cs = dev->capture_stream;
     if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
       log_error("stream capture failed to start: %s", cudaGetErrorString(cudaGetLastError()));
@@ -882,7 +912,7 @@ static void enqueue(CommandBuffer* cb, cudaStream_t st) {
   for (DeviceMemory* m : low.reads)
     if (m->host && m->mapped) cudaMemcpyAsync(m->dptr, m->host, (size_t)m->size, cudaMemcpyHostToDevice, st);
   if (low.exec) cudaGraphLaunch(low.exec, st);
-  else launch_ops(cb, st, 0, false);
+  else launch_ops(cb, st, 0, false, low.timed ? &cb->timing : nullptr);
   for (DeviceMemory* m : low.writes) {
     if (m->host && m->mapped) cudaMemcpyAsync(m->host, m->dptr, (size_t)m->size, cudaMemcpyDeviceToHost, st);
     else m->device_newer = true;
@@ -938,7 +968,21 @@ static void complete(Queue* q, Submission& s) {
     float ms = 0.0f;
     if (cudaEventElapsedTime(&ms, low.ev_begin, low.ev_end) == cudaSuccess) cb->last_ms = ms;
     else cudaGetLastError();
+    for (const TimedLaunch& t : s.timing) {
+      float kms = 0.0f;
+      if (cudaEventElapsedTime(&kms, t.before, t.after) == cudaSuccess) {
+        cb->kernel_ms[t.kind] += kms;
+        cb->kernel_launches[t.kind]++;
+      } else {
+        cudaGetLastError();
+      }
+    }
   }
+  for (const TimedLaunch& t : s.timing) {
+    dev->timing_pool.push_back(t.before);
+    dev->timing_pool.push_back(t.after);
+  }
+  s.timing.clear();
   if (err != VK_SUCCESS) q->lost = err;
   if (s.fence) {
     s.fence->signaled = true;
@@ -979,6 +1023,7 @@ VkResult queue_submit(Queue* q, uint32_t count, const VkSubmitInfo* submits, Fen
       enqueue(cb, q->stream);
       Submission s;
       s.cb = cb;
+      s.timing.swap(cb->timing);
       s.done = pool_event(dev);
       cudaEventRecord(s.done, q->stream);
       q->inflight.push_back(s);
@@ -1056,6 +1101,24 @@ VkResult wait_fences(Device* dev, uint32_t n, const VkFence* fences, VkBool32 al
 
 extern "C" KZ_API void* kzGetQueueStream(VkQueue queue) {
   return (void*)kz::H<kz::Queue>(queue)->stream;
+}
+
+extern "C" KZ_API int kzGetKernelTimes(VkCommandBuffer cbh, double* total_ms, uint32_t* launches, uint32_t count,
+                                       int reset) {
+  kz::CommandBuffer* cb = kz::H<kz::CommandBuffer>(cbh);
+  if (!cb) return -1;
+  std::lock_guard<std::recursive_mutex> lock(cb->dev->mu);
+  for (uint32_t k = 0; k < count && k < (uint32_t)kz::KK_COUNT; k++) {
+    if (total_ms) total_ms[k] = cb->kernel_ms[k];
+    if (launches) launches[k] = cb->kernel_launches[k];
+  }
+  if (reset) {
+    for (int k = 0; k < kz::KK_COUNT; k++) {
+      cb->kernel_ms[k] = 0.0;
+      cb->kernel_launches[k] = 0;
+    }
+  }
+  return (int)kz::KK_COUNT;
 }
 
 extern "C" KZ_API int kzGetCommandBufferStats(VkCommandBuffer cbh, KzCommandBufferStats* out) {

@@ -41,6 +41,8 @@ Options& options() {
     if (tr) r.trace = std::atoi(tr);
     const char* f = std::getenv("KZ_FAULT");
     if (f && !std::strncmp(f, "alloc:", 6)) r.fault_alloc = std::atol(f + 6);
+    const char* kt = std::getenv("KZ_KERNEL_TIMING");
+    if (kt) r.kernel_timing = std::atoi(kt);
     return r;
   }();
   return o;
@@ -1249,6 +1251,11 @@ extern "C" KZ_API int kzDriverSetOption(const char* key, const char* value) {
   }
   if (!std::strcmp(key, "trace")) {
     o.trace = std::atoi(value);
+    return 0;
+  }
+  if (!std::strcmp(key, "kernel_timing")) {
+    if (std::strcmp(value, "0") && std::strcmp(value, "1")) return -1;
+    o.kernel_timing = value[0] == '1';
     return 0;
   }
   if (!std::strcmp(key, "fault_alloc")) {

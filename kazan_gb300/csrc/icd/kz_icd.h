@@ -129,6 +129,27 @@ struct Fence {
 };
 
 struct Semaphore {};
+
+/* kinds of kernel launch, as reported by kzGetKernelTimes */
+enum KernelKind {
+  KK_PERSISTENT = 0,
+  KK_VIS_INIT,
+  KK_VIS_GEOMETRY,
+  KK_VIS_LARGE,
+  KK_VIS_RESOLVE,
+  KK_GEOMETRY,
+  KK_SCAN,
+  KK_BIN,
+  KK_RASTER,
+  KK_CLEAR,
+  KK_COUNT
+};
+
+/* one timed kernel launch: events recorded right before and right after it on the queue stream */
+struct TimedLaunch {
+  int kind = 0;
+  cudaEvent_t before = nullptr, after = nullptr;
+};
 struct PipelineCache {};
 
 /* a linked pipeline-kernel module for one pipeline set */
@@ -211,6 +232,7 @@ struct Lowered {
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
   int mode = 0; /* 0 persistent, 1 batched, 2 per-draw */
   uint32_t tile = 16;
+  bool timed = false; /* kernel timing: launched at submit with an event pair around each kernel */
 };
 
 struct CommandPool {
@@ -243,12 +265,17 @@ struct CommandBuffer : Dispatchable {
   /* statistics of the last completed execution */
   KzStatus last_status{};
   float last_ms = 0.0f;
+  /* kernel timing: device time and launches per KernelKind, summed over completed submissions */
+  double kernel_ms[KK_COUNT] = {};
+  uint32_t kernel_launches[KK_COUNT] = {};
+  std::vector<TimedLaunch> timing; /* launches of the submission being enqueued */
 };
 
 struct Submission {
   CommandBuffer* cb = nullptr;
   cudaEvent_t done = nullptr;
   Fence* fence = nullptr;
+  std::vector<TimedLaunch> timing;
 };
 
 struct Queue : Dispatchable {
@@ -265,6 +292,7 @@ struct Device : Dispatchable {
   std::recursive_mutex mu;
   std::map<std::vector<uint64_t>, KernelSet*> kernel_sets;
   std::vector<cudaEvent_t> event_pool;
+  std::vector<cudaEvent_t> timing_pool; /* events with timing enabled */
 };
 
 /* global options (kzDriverSetOption / KZ_* environment variables) */
@@ -274,6 +302,7 @@ struct Options {
   double rec_slack = 1.25;
   int trace = 0;      /* KZ_TRACE */
   long fault_alloc = -1; /* KZ_FAULT=alloc:N: the Nth device allocation fails */
+  int kernel_timing = 0; /* KZ_KERNEL_TIMING */
 };
 Options& options();
 

@@ -491,6 +491,11 @@ class VkBufferImageCopy(Structure):
                 ("imageExtent", VkExtent3D)]
 
 
+# kernel kinds of kzGetKernelTimes (KZ_KERNEL_KIND_NAMES)
+KERNEL_KINDS = ["kz_k_persistent", "kz_k_vis_init", "kz_k_vis_geometry", "kz_k_vis_large", "kz_k_vis_resolve",
+                "kz_k_geometry", "kz_k_scan", "kz_k_bin", "kz_k_raster", "kz_k_clear"]
+
+
 class KzCommandBufferStats(Structure):
     _fields_ = [("triangles", c_uint64), ("draws", c_uint32), ("segments", c_uint32), ("mode", c_uint32),
                 ("tile", c_uint32), ("status", c_uint32), ("records", c_uint32), ("pairs", c_uint32),
@@ -590,6 +595,9 @@ class Driver:
         self.lib.kzGetQueueStream.argtypes = [c_void_p]
         self.lib.kzGetCommandBufferStats.restype = c_int
         self.lib.kzGetCommandBufferStats.argtypes = [c_void_p, POINTER(KzCommandBufferStats)]
+        self.lib.kzGetKernelTimes.restype = c_int
+        self.lib.kzGetKernelTimes.argtypes = [c_void_p, POINTER(ctypes.c_double), POINTER(c_uint32), c_uint32,
+                                              c_int]
         for name, (res, args) in _PROTOS.items():
             addr = self.lib.vk_icdGetInstanceProcAddr(None, name.encode())
             if not addr:
@@ -604,3 +612,11 @@ class Driver:
         s = KzCommandBufferStats()
         check("kzGetCommandBufferStats", self.lib.kzGetCommandBufferStats(cb, ctypes.byref(s)))
         return s
+
+    def kernel_times(self, cb, reset=False):
+        """{kernel name: (summed ms, launches)} of a command buffer recorded with kernel_timing on"""
+        ms = (ctypes.c_double * len(KERNEL_KINDS))()
+        n = (c_uint32 * len(KERNEL_KINDS))()
+        if self.lib.kzGetKernelTimes(cb, ms, n, len(KERNEL_KINDS), int(reset)) < 0:
+            raise VkError("kzGetKernelTimes", -1)
+        return {k: (ms[i], n[i]) for i, k in enumerate(KERNEL_KINDS) if n[i]}

@@ -58,3 +58,25 @@ def test_resubmit_is_stable(renderer):
         outs.append(run.read())
     for c, d in outs[1:]:
         assert np.array_equal(c, outs[0][0]) and np.array_equal(d, outs[0][1])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["persistent", "batched"])
+def test_kernel_timing_keeps_parity_and_counts_launches(driver, renderer, mode):
+    """kernel timing launches at submit instead of through a graph: same pixels, one timed entry per launch"""
+    scene = CASES["batched"]
+    driver.set_option("kernel_timing", 1)
+    try:
+        run = render.SceneRun(renderer, scene, mode=mode, tile=16)
+    finally:
+        driver.set_option("kernel_timing", 0)
+    for _ in range(2):
+        run.submit()
+    color, depth = run.read()
+    _check(scene, color, depth, run.stats())
+    times = driver.kernel_times(run.cb, reset=True)
+    assert sum(n for _, n in times.values()) == 2 * run.stats().launches
+    assert all(ms > 0 for ms, _ in times.values())
+    if mode == "persistent":
+        assert "kz_k_persistent" in times and "kz_k_vis_geometry" not in times
+    assert driver.kernel_times(run.cb) == {}
