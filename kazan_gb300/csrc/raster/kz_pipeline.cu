@@ -211,7 +211,7 @@ __device__ __forceinline__ Proj project(const KzDraw& d, const float* c) {
 
 /* Fills the coverage/depth record from three projected vertices; returns false when the triangle can
  * produce no fragment (degenerate, culled, or no pixel centre in its box). */
-__device__ bool make_record(const KzDraw& d, const KzPipe& pp, Proj v[3], KzTriRecord& r, bool& swapped) {
+__device__ __forceinline__ bool make_record(const KzDraw& d, const KzPipe& pp, Proj v[3], KzTriRecord& r, bool& swapped) {
   int64_t S = (int64_t)(v[1].X - v[0].X) * (v[2].Y - v[0].Y) - (int64_t)(v[2].X - v[0].X) * (v[1].Y - v[0].Y);
   if (S == 0) return false;
   bool front = pp.front_ccw ? (S < 0) : (S > 0);
@@ -225,10 +225,12 @@ __device__ bool make_record(const KzDraw& d, const KzPipe& pp, Proj v[3], KzTriR
   }
   int32_t minx = min(v[0].X, min(v[1].X, v[2].X)), maxx = max(v[0].X, max(v[1].X, v[2].X));
   int32_t miny = min(v[0].Y, min(v[1].Y, v[2].Y)), maxy = max(v[0].Y, max(v[1].Y, v[2].Y));
-  int64_t bx0 = -floordiv256(-((int64_t)minx - 128));
-  int64_t by0 = -floordiv256(-((int64_t)miny - 128));
-  int64_t bx1 = floordiv256((int64_t)maxx - 128);
-  int64_t by1 = floordiv256((int64_t)maxy - 128);
+  /* pixels whose centre (p * 256 + 128) lies in [min, max]: ceil((min - 128) / 256) .. floor((max - 128) / 256);
+   * snapped coordinates stay within the guard band (|X| < 2^23), so 32-bit arithmetic shifts are exact */
+  int32_t bx0 = (minx + 127) >> 8;
+  int32_t by0 = (miny + 127) >> 8;
+  int32_t bx1 = (maxx - 128) >> 8;
+  int32_t by1 = (maxy - 128) >> 8;
   if (bx0 < d.rect[0]) bx0 = d.rect[0];
   if (by0 < d.rect[1]) by0 = d.rect[1];
   if (bx1 > d.rect[2] - 1) bx1 = d.rect[2] - 1;
@@ -839,9 +841,11 @@ __device__ __forceinline__ float* depth_px(const KzSegment& seg, int32_t x, int3
 
 /* ================= visibility-buffer path (opaque segments) ================= */
 
-#define KZ_SMALL_PX 32      /* boxes of at most this many pixels are rasterised by their geometry thread */
+#define KZ_SMALL_PX 32      /* clipped sub-triangles with boxes of at most this many pixels are rasterised by
+                               their geometry thread */
+#define KZ_WARP_PX 256      /* unclipped triangles with boxes of at most this many pixels are rasterised by
+                               their geometry warp (vis_warp_raster); larger ones become jobs */
 #define KZ_JOB_BLOCKS 16    /* 8x8 pixel blocks per large-triangle job */
-#define KZ_VCACHE 1024      /* vertex-cache slots per 256-triangle chunk */
 
 __device__ __forceinline__ unsigned long long* vis_px(const KzSegment& seg, int32_t x, int32_t y) {
   return reinterpret_cast<unsigned long long*>(seg.vis) + (size_t)y * seg.width + x;
@@ -1015,93 +1019,161 @@ __device__ __forceinline__ VEntry shade_vertex(const KzDraw& d, uint32_t vid, ui
   return e;
 }
 
-/* set up and rasterise (small) or emit (large) the triangle of three shaded vertices */
-__device__ uint32_t vis_triangle(const Ctx& c, const KzDraw& d, const KzPipe& p, uint32_t di, uint32_t g,
-                                 const VEntry* v[3]) {
-  uint32_t any = v[0]->code | v[1]->code | v[2]->code;
-  if (any & (1u << 12)) return 0;
-  if (v[0]->code & v[1]->code & v[2]->code & 63u) return 0; /* outside one view-volume plane */
+/* set up the triangle of three shaded vertices.  Returns true with `out` set when the triangle's box
+ * holds at most KZ_WARP_PX pixels (the warp rasterises it, vis_warp_raster); clipped triangles are
+ * rasterised here (their fragments are added to `frags`) and larger ones are emitted as jobs. */
+__device__ __forceinline__ bool vis_triangle(const Ctx& c, const KzDraw& d, const KzPipe& p, uint32_t di, uint32_t g,
+                             const VEntry (&v)[3], KzTriRecord& out, uint32_t& frags) {
+  uint32_t any = v[0].code | v[1].code | v[2].code;
+  if (any & (1u << 12)) return false;
+  if (v[0].code & v[1].code & v[2].code & 63u) return false; /* outside one view-volume plane */
   if (any & (63u << 6)) {
     float pos[3][4];
     for (int j = 0; j < 3; j++) {
-      pos[j][0] = v[j]->clip.x;
-      pos[j][1] = v[j]->clip.y;
-      pos[j][2] = v[j]->clip.z;
-      pos[j][3] = v[j]->clip.w;
+      pos[j][0] = v[j].clip.x;
+      pos[j][1] = v[j].clip.y;
+      pos[j][2] = v[j].clip.z;
+      pos[j][3] = v[j].clip.w;
     }
-    return vis_clipped(c, d, p, pos, g, di);
+    frags += vis_clipped(c, d, p, pos, g, di);
+    return false;
   }
   Proj pr[3];
   for (int j = 0; j < 3; j++) {
-    pr[j].X = v[j]->X;
-    pr[j].Y = v[j]->Y;
-    pr[j].z = v[j]->z;
+    pr[j].X = v[j].X;
+    pr[j].Y = v[j].Y;
+    pr[j].z = v[j].z;
     pr[j].iw = 0.0f;
   }
-  KzTriRecord r;
   bool sw;
-  if (!make_record(d, p, pr, r, sw)) return 0;
-  r.g = g;
-  r.draw = di;
-  r.pad = 0;
-  if (box_area(r) <= KZ_SMALL_PX) return vis_small(*c.seg, r, d.zmin, d.zmax);
-  vis_emit_large(c, r);
-  return 0;
+  if (!make_record(d, p, pr, out, sw)) return false;
+  out.g = g;
+  out.draw = di;
+  out.pad = 0;
+  if (box_area(out) <= KZ_WARP_PX) return true;
+  vis_emit_large(c, out);
+  return false;
 }
 
-/* geometry of one 256-triangle chunk: the chunk's vertices are shaded and projected once each through a
- * shared-memory cache keyed by vertex index (single-instance draws), then every thread sets up its
- * triangle.  `reuse`: the block goes on to another chunk and must not overwrite the cache early. */
-__device__ void vis_geometry_chunk(const Ctx& c, uint32_t chunk, unsigned char* smem, bool reuse) {
+#define KZ_GEO_SMEM (KZ_THREADS * (96 + 1))
+
+/* what the warp raster keeps of a record, in shared memory (one slot per lane) */
+struct WarpTri {
+  int64_t e[3];       /* edge functions at the centre of the box's first pixel, minus the edge's threshold
+                         (1 unless top-left): covered iff all three are >= 0 */
+  int32_t ex[3];      /* edge function step per pixel in x (-dy * 256) */
+  int32_t ey[3];      /* ... and in y (dx * 256) */
+  int32_t ox, oy;     /* first pixel of the box */
+  uint32_t w, magic;  /* box width; umulhi(i, magic) = i / w for i < 2^16 (w > 1) */
+  uint32_t start, thr;/* number of the box's first pixel in the warp's list; bit k: edge k's threshold is 1 */
+  float z0, dz1, dz2, inv_s;
+  uint32_t g, pad;    /* primitive number */
+};                    /* 96 bytes */
+static_assert(sizeof(WarpTri) == 96, "WarpTri layout");
+
+/* rasterise every lane's record (valid where `have`) into the keys with the whole warp.  The boxes'
+ * pixels are numbered consecutively across the lanes and the warp takes 32 consecutive pixels per step,
+ * so lanes stay busy however unequal the boxes are and neighbouring lanes write neighbouring keys.  In a
+ * step, each triangle whose pixels meet the step's window writes its lane into `owner` at the window
+ * position of its first pixel there; lane l's triangle is the one marked at the highest position <= l.
+ * `slots`: this warp's 32 WarpTri, `owner`: its 32-entry table, both in shared memory. */
+__device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const KzTriRecord& r, bool have, float zmin,
+                                                    float zmax, WarpTri* slots, uint8_t* owner) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t n = have ? box_area(r) : 0u;
+  uint32_t incl = n;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  if (total == 0) return 0;
+  const uint32_t start = incl - n;
+  if (have) {
+    WarpTri& t = slots[lane];
+    Edges e;
+    edges_of(r, e);
+    t.ox = (int32_t)(r.bb0 & 0xFFFFu);
+    t.oy = (int32_t)(r.bb0 >> 16);
+    t.w = (r.bb1 & 0xFFFFu) - (r.bb0 & 0xFFFFu) + 1;
+    /* floor((2^32 - 1) / w) + 1: the rounded-up reciprocal for every w > 1 (exact when w is a power of two) */
+    t.magic = t.w > 1 ? 0xFFFFFFFFu / t.w + 1u : 0u;
+    t.start = start;
+    int64_t px = (int64_t)t.ox * 256 + 128, py = (int64_t)t.oy * 256 + 128;
+    uint32_t thr = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      t.e[k] = edge_at(e, k, px, py) - e.thr[k];
+      t.ex[k] = -e.dy[k] * 256;
+      t.ey[k] = e.dx[k] * 256;
+      thr |= (uint32_t)e.thr[k] << k;
+    }
+    t.thr = thr;
+    t.z0 = r.z0;
+    t.dz1 = r.dz1;
+    t.dz2 = r.dz2;
+    t.inv_s = r.inv_s;
+    t.g = r.g;
+  }
+  uint32_t frags = 0;
+  const uint32_t upto = 0xFFFFFFFFu >> (31 - lane); /* window positions 0..lane */
+  for (uint32_t base = 0; base < total; base += 32) {
+    bool meets = n != 0 && start < base + 32 && start + n > base;
+    uint32_t pos = start > base ? start - base : 0u;
+    if (meets) owner[pos] = (uint8_t)lane;
+    uint32_t marks = __reduce_or_sync(0xFFFFFFFFu, meets ? 1u << pos : 0u);
+    __syncwarp();
+    uint32_t o = owner[31 - __clz(marks & upto)];
+    __syncwarp();
+    uint32_t idx = base + (uint32_t)lane;
+    if (idx >= total) continue;
+    const WarpTri& t = slots[o];
+    uint32_t local = idx - t.start;
+    uint32_t w = t.w;
+    uint32_t y = w > 1 ? __umulhi(local, t.magic) : local;
+    int32_t x = (int32_t)(local - y * w);
+    int64_t e0 = t.e[0] + (int64_t)t.ex[0] * x + (int64_t)t.ey[0] * (int32_t)y;
+    int64_t e1 = t.e[1] + (int64_t)t.ex[1] * x + (int64_t)t.ey[1] * (int32_t)y;
+    int64_t e2 = t.e[2] + (int64_t)t.ex[2] * x + (int64_t)t.ey[2] * (int32_t)y;
+    if ((e0 | e1 | e2) < 0) continue;
+    frags++;
+    uint32_t thr = t.thr;
+    float l1 = fmul(kz_i64_to_f32(e1 + (int64_t)((thr >> 1) & 1u)), t.inv_s);
+    float l2 = fmul(kz_i64_to_f32(e2 + (int64_t)(thr >> 2)), t.inv_s);
+    float z = ffma(l2, t.dz2, ffma(l1, t.dz1, t.z0));
+    z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
+    vis_store(seg, vis_key(seg.vis_key, z, t.g), t.ox + x, t.oy + (int32_t)y);
+  }
+  __syncwarp();
+  return frags;
+}
+
+/* geometry of one chunk of at most 256 triangles of one draw, one thread per triangle: the thread shades
+ * its three vertices (position-only vertex shader), clips, projects and sets up its triangle; each warp
+ * then rasterises its lanes' small and medium triangles together (vis_warp_raster).  `smem`: 8 warps x 32
+ * WarpTri, then 8 warps x 32 owner bytes (KZ_GEO_SMEM bytes). */
+__device__ void vis_geometry_chunk(const Ctx& c, uint32_t chunk, unsigned char* smem) {
   const KzChunk ch = reinterpret_cast<const KzChunk*>(c.f->chunks)[chunk];
   const KzDraw& d = c.draws[ch.draw];
   const KzPipe& p = c.pipes[d.pipe];
   const uint8_t* push = push_ptr(*c.f, d);
   bool active = threadIdx.x < ch.count;
   uint32_t local = ch.first + threadIdx.x;
-  uint32_t vid[3] = {0, 0, 0}, iid = 0;
-  if (active) tri_vertices(d, local, vid, iid);
-  uint32_t g = d.prim_base + local;
   uint32_t frags = 0;
-  if (d.instance_count == 1) {
-    uint32_t* keys = reinterpret_cast<uint32_t*>(smem);
-    VEntry* cache = reinterpret_cast<VEntry*>(smem + KZ_VCACHE * 4);
-    for (int i = threadIdx.x; i < KZ_VCACHE; i += blockDim.x) keys[i] = 0xFFFFFFFFu;
-    __syncthreads();
-    uint32_t slot[3] = {0, 0, 0};
-    uint32_t owned = 0;
-    if (active) {
-      for (int j = 0; j < 3; j++) {
-        uint32_t vv = vid[j];
-        uint32_t h = (vv * 2654435761u) >> 22;
-        /* at most 768 keys in 1024 slots: the probe always ends */
-        for (;;) {
-          uint32_t old = atomicCAS(&keys[h], 0xFFFFFFFFu, vv);
-          if (old == 0xFFFFFFFFu) {
-            owned |= 1u << j;
-            break;
-          }
-          if (old == vv) break;
-          h = (h + 1) & (KZ_VCACHE - 1);
-        }
-        slot[j] = h;
-      }
-    }
-    __syncthreads();
-    for (int j = 0; j < 3; j++)
-      if (owned & (1u << j)) cache[slot[j]] = shade_vertex(d, vid[j], iid, push);
-    __syncthreads();
-    if (active) {
-      const VEntry* v[3] = {&cache[slot[0]], &cache[slot[1]], &cache[slot[2]]};
-      frags = vis_triangle(c, d, p, ch.draw, g, v);
-    }
-    if (reuse) __syncthreads();
-  } else if (active) {
+  KzTriRecord r;
+  bool have = false;
+  if (active) {
+    uint32_t vid[3], iid;
+    tri_vertices(d, local, vid, iid);
     VEntry e[3];
+#pragma unroll
     for (int j = 0; j < 3; j++) e[j] = shade_vertex(d, vid[j], iid, push);
-    const VEntry* v[3] = {&e[0], &e[1], &e[2]};
-    frags = vis_triangle(c, d, p, ch.draw, g, v);
+    have = vis_triangle(c, d, p, ch.draw, d.prim_base + local, e, r, frags);
   }
+  WarpTri* slots = reinterpret_cast<WarpTri*>(smem) + (threadIdx.x & ~31u);
+  uint8_t* owner = smem + KZ_THREADS * sizeof(WarpTri) + (threadIdx.x & ~31u);
+  frags += vis_warp_raster(*c.seg, r, have, d.zmin, d.zmax, slots, owner);
   for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
   if ((threadIdx.x & 31) == 0 && frags) {
     atomicAdd(&c.cnt->fragments, frags);
@@ -1109,7 +1181,12 @@ __device__ void vis_geometry_chunk(const Ctx& c, uint32_t chunk, unsigned char* 
   }
 }
 
-/* one large-triangle job, one warp: up to KZ_JOB_BLOCKS 8x8 blocks of the record's box */
+/* one large-triangle job, one warp: up to KZ_JOB_BLOCKS 8x8 blocks of the record's box.
+ * Lane b < KZ_JOB_BLOCKS first evaluates the three edge functions at block b's first pixel centre and
+ * drops the block when, for some edge, even the block's largest value (at the corner the edge's
+ * gradient points to) is below the threshold.  The warp then walks the remaining blocks: each lane adds
+ * its fixed offset within the block to the block's edge values (the same int64 integers as evaluating the
+ * edge functions at the pixel directly). */
 __device__ uint32_t vis_large_job(const Ctx& c, uint2 job, int lane) {
   const KzSegment& seg = *c.seg;
   const KzTriRecord r = load_record(seg, job.x);
@@ -1120,20 +1197,55 @@ __device__ uint32_t vis_large_job(const Ctx& c, uint2 job, int lane) {
   int32_t bx0 = (int32_t)(r.bb0 & 0xFFFFu), by0 = (int32_t)(r.bb0 >> 16);
   int32_t bx1 = (int32_t)(r.bb1 & 0xFFFFu), by1 = (int32_t)(r.bb1 >> 16);
   uint32_t nbx, nb = box_blocks(r, nbx);
-  uint32_t b1 = min(nb, job.y + KZ_JOB_BLOCKS);
-  int lx = lane & 7, ly = lane >> 3;
-  uint32_t frags = 0;
-  for (uint32_t b = job.y; b < b1; b++) {
-    int32_t x0 = bx0 + (int32_t)(b % nbx) * 8, y0 = by0 + (int32_t)(b / nbx) * 8;
+  /* block test, one block per lane */
+  uint32_t b = job.y + (uint32_t)lane;
+  bool live = lane < KZ_JOB_BLOCKS && b < nb;
+  int32_t ox = 0, oy = 0;
+  int64_t E0 = 0, E1 = 0, E2 = 0;
+  if (live) {
+    uint32_t row = b / nbx;
+    ox = bx0 + (int32_t)(b - row * nbx) * 8;
+    oy = by0 + (int32_t)row * 8;
+    int64_t px = (int64_t)ox * 256 + 128, py = (int64_t)oy * 256 + 128;
+    E0 = edge_at(e, 0, px, py);
+    E1 = edge_at(e, 1, px, py);
+    E2 = edge_at(e, 2, px, py);
 #pragma unroll
-    for (int half = 0; half < 2; half++) {
-      int32_t x = x0 + lx, y = y0 + ly + 4 * half;
-      if (x > bx1 || y > by1) continue;
-      int64_t px = (int64_t)x * 256 + 128, py = (int64_t)y * 256 + 128;
-      int64_t E0 = edge_at(e, 0, px, py), E1 = edge_at(e, 1, px, py), E2 = edge_at(e, 2, px, py);
-      if (E0 < e.thr[0] || E1 < e.thr[1] || E2 < e.thr[2]) continue;
-      frags++;
-      vis_store(seg, frag_key(seg, r, zmin, zmax, kz_i64_to_f32(E1), kz_i64_to_f32(E2)), x, y);
+    for (int k = 0; k < 3; k++) {
+      int64_t ek = k == 0 ? E0 : (k == 1 ? E1 : E2);
+      int64_t mx = ek + (e.dy[k] < 0 ? -(int64_t)e.dy[k] * (7 * 256) : 0) + (e.dx[k] > 0 ? (int64_t)e.dx[k] * (7 * 256) : 0);
+      live = live && mx >= e.thr[k];
+    }
+  }
+  uint32_t mask = __ballot_sync(0xFFFFFFFFu, live);
+  /* this lane's offset inside a block: column lx, rows ly and ly + 4 */
+  int lx = lane & 7, ly = lane >> 3;
+  int64_t inc[3], half[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    inc[k] = (int64_t)e.dx[k] * (ly * 256) - (int64_t)e.dy[k] * (lx * 256);
+    half[k] = (int64_t)e.dx[k] * (4 * 256);
+  }
+  uint32_t frags = 0;
+  while (mask) {
+    int src = __ffs(mask) - 1;
+    mask &= mask - 1;
+    int32_t bxo = __shfl_sync(0xFFFFFFFFu, ox, src), byo = __shfl_sync(0xFFFFFFFFu, oy, src);
+    int64_t e0 = __shfl_sync(0xFFFFFFFFu, E0, src) + inc[0];
+    int64_t e1 = __shfl_sync(0xFFFFFFFFu, E1, src) + inc[1];
+    int64_t e2 = __shfl_sync(0xFFFFFFFFu, E2, src) + inc[2];
+    int32_t x = bxo + lx;
+    if (x > bx1) continue;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      int32_t y = byo + ly + 4 * h;
+      if (y <= by1 && e0 >= e.thr[0] && e1 >= e.thr[1] && e2 >= e.thr[2]) {
+        frags++;
+        vis_store(seg, frag_key(seg, r, zmin, zmax, kz_i64_to_f32(e1), kz_i64_to_f32(e2)), x, y);
+      }
+      e0 += half[0];
+      e1 += half[1];
+      e2 += half[2];
     }
   }
   return frags;
@@ -1416,11 +1528,11 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_vis_init(KzFrame f
   vis_init_range(*c.seg, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
 }
 
-extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_vis_geometry(KzFrame f, uint32_t s) {
-  __shared__ __align__(16) unsigned char cache[KZ_VCACHE * (4 + sizeof(VEntry))];
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_geometry(KzFrame f, uint32_t s) {
+  __shared__ __align__(16) unsigned char slots[KZ_GEO_SMEM];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
-  if (blockIdx.x < c.seg->num_chunks) vis_geometry_chunk(c, c.seg->first_chunk + blockIdx.x, cache, false);
+  if (blockIdx.x < c.seg->num_chunks) vis_geometry_chunk(c, c.seg->first_chunk + blockIdx.x, slots);
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_vis_large(KzFrame f, uint32_t s) {
@@ -1463,7 +1575,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
       for (;;) {
         uint32_t k = grab(&c.cnt->geom_next, &item);
         if (k >= c.seg->num_chunks) break;
-        vis_geometry_chunk(c, c.seg->first_chunk + k, smem, true);
+        vis_geometry_chunk(c, c.seg->first_chunk + k, smem);
       }
       if (!grid_barrier(st)) return;
       if (!vis_check(c, s)) break;
