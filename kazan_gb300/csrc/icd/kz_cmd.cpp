@@ -652,7 +652,7 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
             cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (seg.width * seg.height + 255) / 256)));
             launch(dev, timing, KK_VIS_INIT, cfg, ks->vis_init, args);
             if (seg.num_chunks) {
-              cfg.gridDim = dim3(seg.num_chunks);
+              cfg.gridDim = dim3(std::min<uint32_t>(seg.num_chunks, (uint32_t)std::max(1, ks->geometry_blocks)));
               launch(dev, timing, KK_VIS_GEOMETRY, cfg, ks->vis_geometry, args);
               cfg.gridDim = dim3(grid_cap(dev));
               launch(dev, timing, KK_VIS_LARGE, cfg, ks->vis_large, args);

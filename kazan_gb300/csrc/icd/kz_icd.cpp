@@ -162,6 +162,13 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
     per_sm = 1;
   }
   ks->persistent_blocks = per_sm * dev->pd->sm_count;
+  int geo_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&geo_sm, (const void*)ks->vis_geometry, 256, 0) != cudaSuccess ||
+      geo_sm < 1) {
+    cudaGetLastError();
+    geo_sm = 1;
+  }
+  ks->geometry_blocks = geo_sm * dev->pd->sm_count;
   if (options().trace) log_error("kernel set linked: %zu pipelines, persistent grid %d", pipes.size(), ks->persistent_blocks);
   dev->kernel_sets[key] = ks;
   return ks;

@@ -159,6 +159,7 @@ struct KernelSet {
                clear = nullptr, vis_init = nullptr, vis_geometry = nullptr, vis_large = nullptr,
                vis_resolve = nullptr;
   int persistent_blocks = 0;
+  int geometry_blocks = 0; /* resident blocks of kz_k_vis_geometry on the whole GPU */
 };
 
 /* ---- recording ---- */

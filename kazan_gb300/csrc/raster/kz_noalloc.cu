@@ -58,6 +58,15 @@ extern "C" __device__ float4 kz_vs_pos(uint32_t, const KzDraw* d, uint32_t vid, 
   return make_float4(v[0], v[1], v[2], v[3]);
 }
 
+extern "C" __device__ KzPos3 kz_vs_pos3(uint32_t pipe, const KzDraw* d, uint32_t v0, uint32_t v1, uint32_t v2,
+                                        uint32_t iid, const uint8_t* push) {
+  KzPos3 r;
+  r.p[0] = kz_vs_pos(pipe, d, v0, iid, push);
+  r.p[1] = kz_vs_pos(pipe, d, v1, iid, push);
+  r.p[2] = kz_vs_pos(pipe, d, v2, iid, push);
+  return r;
+}
+
 extern "C" __device__ void kz_vs(uint32_t, const KzDraw* d, uint32_t vid, uint32_t, const uint8_t*, KzVsOut* out) {
   const float* v = reinterpret_cast<const float*>(d->vb[0]) + (size_t)vid * 8;
   for (int k = 0; k < 4; k++) out->pos[k] = v[k];

@@ -30,6 +30,12 @@ extern "C" __device__ void kz_vs(uint32_t pipe, const KzDraw* draw, uint32_t vid
 extern "C" __device__ float4 kz_vs_pos(uint32_t pipe, const KzDraw* draw, uint32_t vid, uint32_t iid,
                                        const uint8_t* push);
 extern "C" __device__ uint32_t kz_fs(uint32_t pipe, const KzFsIn* in, const uint8_t* push, float* color);
+/* gl_Position of the three vertices of one triangle in one call (push constants read once) */
+struct KzPos3 {
+  float4 p[3];
+};
+extern "C" __device__ KzPos3 kz_vs_pos3(uint32_t pipe, const KzDraw* draw, uint32_t vid0, uint32_t vid1, uint32_t vid2,
+                                        uint32_t iid, const uint8_t* push);
 
 #define KZ_THREADS 256
 #define KZ_SORT_CAP 4096          /* ordered mode: largest bin sorted in shared memory */
@@ -52,7 +58,6 @@ __device__ __forceinline__ uint8_t unorm8(float v) {
 }
 __device__ __forceinline__ float u8f(uint32_t u) { return fdiv(__uint2float_rn(u), 255.0f); }
 
-__device__ __forceinline__ int64_t floordiv256(int64_t a) { return a >= 0 ? a / 256 : -((-a + 255) / 256); }
 
 /* ---------------- frame access ---------------- */
 
@@ -951,6 +956,38 @@ __device__ void vis_emit_large(const Ctx& c, const KzTriRecord& r) {
   for (uint32_t j = 0; j < njobs && j0 + j < cap; j++) jobs[j0 + j] = make_uint2(idx, j * KZ_JOB_BLOCKS);
 }
 
+/* emit the records of the lanes where `large` holds (their boxes exceed KZ_WARP_PX pixels) with one
+ * record and one job reservation for the whole warp (all lanes call it) */
+__device__ __forceinline__ void vis_emit_large_warp(const Ctx& c, const KzTriRecord& r, bool large) {
+  const uint32_t m = __ballot_sync(0xFFFFFFFFu, large);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  uint32_t nbx = 0, njobs = 0;
+  if (large) njobs = (box_blocks(r, nbx) + KZ_JOB_BLOCKS - 1) / KZ_JOB_BLOCKS;
+  uint32_t jincl = njobs;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xFFFFFFFFu, jincl, o);
+    if (lane >= o) jincl += t;
+  }
+  const uint32_t jtotal = __shfl_sync(0xFFFFFFFFu, jincl, 31);
+  const int leader = __ffs(m) - 1;
+  uint32_t rbase = 0, jbase = 0;
+  if (lane == leader) {
+    rbase = atomicAdd(&c.cnt->rec_count, (uint32_t)__popc(m));
+    jbase = atomicAdd(&c.cnt->pair_count, jtotal);
+  }
+  rbase = __shfl_sync(0xFFFFFFFFu, rbase, leader);
+  jbase = __shfl_sync(0xFFFFFFFFu, jbase, leader);
+  if (!large) return;
+  uint32_t idx = rbase + (uint32_t)__popc(m & lanemask_lt());
+  store_record(c, idx, r);
+  if (idx >= c.seg->rec_cap) return;
+  uint32_t j0 = jbase + jincl - njobs, cap = c.seg->pair_cap / 2;
+  uint2* jobs = reinterpret_cast<uint2*>(c.seg->bins);
+  for (uint32_t j = 0; j < njobs && j0 + j < cap; j++) jobs[j0 + j] = make_uint2(idx, j * KZ_JOB_BLOCKS);
+}
+
 /* one record: small -> rasterise now, large -> jobs */
 __device__ uint32_t vis_record(const Ctx& c, const KzTriRecord& r) {
   const KzDraw& d = c.draws[r.draw];
@@ -990,9 +1027,9 @@ struct VEntry {
                     a clip plane (near, far, guard band); bit 12 non-finite */
 };
 
-__device__ __forceinline__ VEntry shade_vertex(const KzDraw& d, uint32_t vid, uint32_t iid, const uint8_t* push) {
+__device__ __forceinline__ VEntry vertex_entry(const KzDraw& d, float4 clip) {
   VEntry e;
-  e.clip = kz_vs_pos(d.pipe, &d, vid, iid, push);
+  e.clip = clip;
   const float c[4] = {e.clip.x, e.clip.y, e.clip.z, e.clip.w};
   uint32_t code = 0;
   if (!(isfinite(c[0]) && isfinite(c[1]) && isfinite(c[2]) && isfinite(c[3]))) {
@@ -1019,14 +1056,15 @@ __device__ __forceinline__ VEntry shade_vertex(const KzDraw& d, uint32_t vid, ui
   return e;
 }
 
-/* set up the triangle of three shaded vertices.  Returns true with `out` set when the triangle's box
- * holds at most KZ_WARP_PX pixels (the warp rasterises it, vis_warp_raster); clipped triangles are
- * rasterised here (their fragments are added to `frags`) and larger ones are emitted as jobs. */
-__device__ __forceinline__ bool vis_triangle(const Ctx& c, const KzDraw& d, const KzPipe& p, uint32_t di, uint32_t g,
+/* set up the triangle of three shaded vertices.  Returns 1 with `out` set when the triangle's box holds
+ * at most KZ_WARP_PX pixels (the warp rasterises it, vis_warp_raster), 2 with `out` set when it is larger
+ * (jobs, vis_emit_large_warp), 0 otherwise; clipped triangles are rasterised here (their fragments are
+ * added to `frags`). */
+__device__ __forceinline__ int vis_triangle(const Ctx& c, const KzDraw& d, const KzPipe& p, uint32_t di, uint32_t g,
                              const VEntry (&v)[3], KzTriRecord& out, uint32_t& frags) {
   uint32_t any = v[0].code | v[1].code | v[2].code;
-  if (any & (1u << 12)) return false;
-  if (v[0].code & v[1].code & v[2].code & 63u) return false; /* outside one view-volume plane */
+  if (any & (1u << 12)) return 0;
+  if (v[0].code & v[1].code & v[2].code & 63u) return 0; /* outside one view-volume plane */
   if (any & (63u << 6)) {
     float pos[3][4];
     for (int j = 0; j < 3; j++) {
@@ -1036,7 +1074,7 @@ __device__ __forceinline__ bool vis_triangle(const Ctx& c, const KzDraw& d, cons
       pos[j][3] = v[j].clip.w;
     }
     frags += vis_clipped(c, d, p, pos, g, di);
-    return false;
+    return 0;
   }
   Proj pr[3];
   for (int j = 0; j < 3; j++) {
@@ -1046,13 +1084,11 @@ __device__ __forceinline__ bool vis_triangle(const Ctx& c, const KzDraw& d, cons
     pr[j].iw = 0.0f;
   }
   bool sw;
-  if (!make_record(d, p, pr, out, sw)) return false;
+  if (!make_record(d, p, pr, out, sw)) return 0;
   out.g = g;
   out.draw = di;
   out.pad = 0;
-  if (box_area(out) <= KZ_WARP_PX) return true;
-  vis_emit_large(c, out);
-  return false;
+  return box_area(out) <= KZ_WARP_PX ? 1 : 2;
 }
 
 #define KZ_GEO_SMEM (KZ_THREADS * (96 + 1))
@@ -1064,23 +1100,39 @@ struct WarpTri {
   int32_t ex[3];      /* edge function step per pixel in x (-dy * 256) */
   int32_t ey[3];      /* ... and in y (dx * 256) */
   int32_t ox, oy;     /* first pixel of the box */
-  uint32_t w, magic;  /* box width; umulhi(i, magic) = i / w for i < 2^16 (w > 1) */
-  uint32_t start, thr;/* number of the box's first pixel in the warp's list; bit k: edge k's threshold is 1 */
+  uint32_t pw, magic; /* pixel pairs per box row, ceil(w / 2); umulhi(i, magic) = i / pw for i < 2^16 */
+  uint32_t start, w;  /* number of the box's first pair in the warp's list; box width */
   float z0, dz1, dz2, inv_s;
-  uint32_t g, pad;    /* primitive number */
+  uint32_t g, thr;    /* primitive number; bit k: edge k's threshold is 1 */
 };                    /* 96 bytes */
 static_assert(sizeof(WarpTri) == 96, "WarpTri layout");
 
-/* rasterise every lane's record (valid where `have`) into the keys with the whole warp.  The boxes'
- * pixels are numbered consecutively across the lanes and the warp takes 32 consecutive pixels per step,
- * so lanes stay busy however unequal the boxes are and neighbouring lanes write neighbouring keys.  In a
- * step, each triangle whose pixels meet the step's window writes its lane into `owner` at the window
- * position of its first pixel there; lane l's triangle is the one marked at the highest position <= l.
- * `slots`: this warp's 32 WarpTri, `owner`: its 32-entry table, both in shared memory. */
+/* one covered pixel of a warp-rasterised triangle: its depth key into the visibility buffer */
+__device__ __forceinline__ void warp_fragment(const KzSegment& seg, const WarpTri& t, int64_t e1, int64_t e2, float zmin,
+                                              float zmax, int32_t x, int32_t y) {
+  uint32_t thr = t.thr;
+  float l1 = fmul(kz_i64_to_f32(e1 + (int64_t)((thr >> 1) & 1u)), t.inv_s);
+  float l2 = fmul(kz_i64_to_f32(e2 + (int64_t)(thr >> 2)), t.inv_s);
+  float z = ffma(l2, t.dz2, ffma(l1, t.dz1, t.z0));
+  z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
+  vis_store(seg, vis_key(seg.vis_key, z, t.g), x, y);
+}
+
+/* rasterise every lane's record (valid where `have`) into the keys with the whole warp.  Each box row is
+ * cut into pairs of horizontally adjacent pixels; the pairs of all lanes' boxes are numbered consecutively
+ * and the warp takes 32 consecutive pairs per step, so lanes stay busy however unequal the boxes are and
+ * neighbouring lanes write neighbouring keys.  In a step, each triangle whose pairs meet the step's window
+ * writes its lane into `owner` at the window position of its first pair there; lane l's triangle is the
+ * one marked at the highest position <= l.  `slots`: this warp's 32 WarpTri, `owner`: its 32-entry table,
+ * both in shared memory. */
 __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const KzTriRecord& r, bool have, float zmin,
                                                     float zmax, WarpTri* slots, uint8_t* owner) {
   const int lane = threadIdx.x & 31;
-  const uint32_t n = have ? box_area(r) : 0u;
+  uint32_t n = 0;
+  if (have) {
+    uint32_t w = (r.bb1 & 0xFFFFu) - (r.bb0 & 0xFFFFu) + 1;
+    n = ((r.bb1 >> 16) - (r.bb0 >> 16) + 1) * ((w + 1) >> 1);
+  }
   uint32_t incl = n;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -1097,8 +1149,9 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
     t.ox = (int32_t)(r.bb0 & 0xFFFFu);
     t.oy = (int32_t)(r.bb0 >> 16);
     t.w = (r.bb1 & 0xFFFFu) - (r.bb0 & 0xFFFFu) + 1;
-    /* floor((2^32 - 1) / w) + 1: the rounded-up reciprocal for every w > 1 (exact when w is a power of two) */
-    t.magic = t.w > 1 ? 0xFFFFFFFFu / t.w + 1u : 0u;
+    t.pw = (t.w + 1) >> 1;
+    /* floor((2^32 - 1) / pw) + 1: the rounded-up reciprocal for every pw > 1 (exact when pw is a power of 2) */
+    t.magic = t.pw > 1 ? 0xFFFFFFFFu / t.pw + 1u : 0u;
     t.start = start;
     int64_t px = (int64_t)t.ox * 256 + 128, py = (int64_t)t.oy * 256 + 128;
     uint32_t thr = 0;
@@ -1130,50 +1183,72 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
     if (idx >= total) continue;
     const WarpTri& t = slots[o];
     uint32_t local = idx - t.start;
-    uint32_t w = t.w;
-    uint32_t y = w > 1 ? __umulhi(local, t.magic) : local;
-    int32_t x = (int32_t)(local - y * w);
-    int64_t e0 = t.e[0] + (int64_t)t.ex[0] * x + (int64_t)t.ey[0] * (int32_t)y;
-    int64_t e1 = t.e[1] + (int64_t)t.ex[1] * x + (int64_t)t.ey[1] * (int32_t)y;
-    int64_t e2 = t.e[2] + (int64_t)t.ex[2] * x + (int64_t)t.ey[2] * (int32_t)y;
-    if ((e0 | e1 | e2) < 0) continue;
-    frags++;
-    uint32_t thr = t.thr;
-    float l1 = fmul(kz_i64_to_f32(e1 + (int64_t)((thr >> 1) & 1u)), t.inv_s);
-    float l2 = fmul(kz_i64_to_f32(e2 + (int64_t)(thr >> 2)), t.inv_s);
-    float z = ffma(l2, t.dz2, ffma(l1, t.dz1, t.z0));
-    z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
-    vis_store(seg, vis_key(seg.vis_key, z, t.g), t.ox + x, t.oy + (int32_t)y);
+    uint32_t pw = t.pw;
+    uint32_t y = pw > 1 ? __umulhi(local, t.magic) : local;
+    int32_t x = (int32_t)(local - y * pw) * 2;
+    int32_t sx0 = t.ex[0], sx1 = t.ex[1], sx2 = t.ex[2];
+    int64_t e0 = t.e[0] + (int64_t)sx0 * x + (int64_t)t.ey[0] * (int32_t)y;
+    int64_t e1 = t.e[1] + (int64_t)sx1 * x + (int64_t)t.ey[1] * (int32_t)y;
+    int64_t e2 = t.e[2] + (int64_t)sx2 * x + (int64_t)t.ey[2] * (int32_t)y;
+    int32_t px = t.ox + x, py = t.oy + (int32_t)y;
+    if ((e0 | e1 | e2) >= 0) {
+      frags++;
+      warp_fragment(seg, t, e1, e2, zmin, zmax, px, py);
+    }
+    if ((uint32_t)x + 1 < t.w) {
+      e0 += sx0;
+      e1 += sx1;
+      e2 += sx2;
+      if ((e0 | e1 | e2) >= 0) {
+        frags++;
+        warp_fragment(seg, t, e1, e2, zmin, zmax, px + 1, py);
+      }
+    }
   }
   __syncwarp();
   return frags;
 }
 
-/* geometry of one chunk of at most 256 triangles of one draw, one thread per triangle: the thread shades
- * its three vertices (position-only vertex shader), clips, projects and sets up its triangle; each warp
- * then rasterises its lanes' small and medium triangles together (vis_warp_raster).  `smem`: 8 warps x 32
- * WarpTri, then 8 warps x 32 owner bytes (KZ_GEO_SMEM bytes). */
-__device__ void vis_geometry_chunk(const Ctx& c, uint32_t chunk, unsigned char* smem) {
+/* geometry of the 32 triangles [32 sub, 32 sub + 32) of one chunk, one warp, one lane per triangle: the
+ * lane shades its three vertices (position-only vertex shader), clips, projects and sets up its triangle;
+ * the warp then emits its large triangles together and rasterises the small and medium ones together
+ * (vis_warp_raster).  Returns the lane's fragment count. */
+__device__ __forceinline__ uint32_t vis_geometry_warp(const Ctx& c, uint32_t chunk, uint32_t sub, WarpTri* slots,
+                                                      uint8_t* owner) {
   const KzChunk ch = reinterpret_cast<const KzChunk*>(c.f->chunks)[chunk];
+  if (sub * 32 >= ch.count) return 0;
   const KzDraw& d = c.draws[ch.draw];
   const KzPipe& p = c.pipes[d.pipe];
   const uint8_t* push = push_ptr(*c.f, d);
-  bool active = threadIdx.x < ch.count;
-  uint32_t local = ch.first + threadIdx.x;
+  uint32_t off = sub * 32 + (threadIdx.x & 31);
+  uint32_t local = ch.first + off;
   uint32_t frags = 0;
   KzTriRecord r;
-  bool have = false;
-  if (active) {
+  int kind = 0;
+  if (off < ch.count) {
     uint32_t vid[3], iid;
     tri_vertices(d, local, vid, iid);
+    const KzPos3 q = kz_vs_pos3(d.pipe, &d, vid[0], vid[1], vid[2], iid, push);
     VEntry e[3];
 #pragma unroll
-    for (int j = 0; j < 3; j++) e[j] = shade_vertex(d, vid[j], iid, push);
-    have = vis_triangle(c, d, p, ch.draw, d.prim_base + local, e, r, frags);
+    for (int j = 0; j < 3; j++) e[j] = vertex_entry(d, q.p[j]);
+    kind = vis_triangle(c, d, p, ch.draw, d.prim_base + local, e, r, frags);
   }
-  WarpTri* slots = reinterpret_cast<WarpTri*>(smem) + (threadIdx.x & ~31u);
-  uint8_t* owner = smem + KZ_THREADS * sizeof(WarpTri) + (threadIdx.x & ~31u);
-  frags += vis_warp_raster(*c.seg, r, have, d.zmin, d.zmax, slots, owner);
+  vis_emit_large_warp(c, r, kind == 2);
+  frags += vis_warp_raster(*c.seg, r, kind == 1, d.zmin, d.zmax, slots, owner);
+  return frags;
+}
+
+/* the geometry of a segment by warps: warp w of `warps` takes the 32-triangle groups w, w + warps, ...
+ * (8 groups per chunk), then adds its fragment count to the statistics.  `smem`: 8 warps x 32 WarpTri,
+ * then 8 warps x 32 owner bytes (KZ_GEO_SMEM bytes). */
+__device__ void vis_geometry_warps(const Ctx& c, unsigned char* smem, uint32_t w, uint32_t warps) {
+  const uint32_t wib = threadIdx.x >> 5;
+  WarpTri* slots = reinterpret_cast<WarpTri*>(smem) + wib * 32;
+  uint8_t* owner = smem + KZ_THREADS * sizeof(WarpTri) + wib * 32;
+  const uint32_t groups = c.seg->num_chunks * 8;
+  uint32_t frags = 0;
+  for (uint32_t i = w; i < groups; i += warps) frags += vis_geometry_warp(c, c.seg->first_chunk + i / 8, i % 8, slots, owner);
   for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
   if ((threadIdx.x & 31) == 0 && frags) {
     atomicAdd(&c.cnt->fragments, frags);
@@ -1532,7 +1607,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_geometry(Kz
   __shared__ __align__(16) unsigned char slots[KZ_GEO_SMEM];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
-  if (blockIdx.x < c.seg->num_chunks) vis_geometry_chunk(c, c.seg->first_chunk + blockIdx.x, slots);
+  vis_geometry_warps(c, slots, blockIdx.x * (KZ_THREADS / 32) + (threadIdx.x >> 5), gridDim.x * (KZ_THREADS / 32));
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_vis_large(KzFrame f, uint32_t s) {
@@ -1572,11 +1647,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
     if (c.seg->mode == KZ_MODE_VISIBILITY) {
       vis_init_range(*c.seg, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
       if (!grid_barrier(st)) return;
-      for (;;) {
-        uint32_t k = grab(&c.cnt->geom_next, &item);
-        if (k >= c.seg->num_chunks) break;
-        vis_geometry_chunk(c, c.seg->first_chunk + k, smem);
-      }
+      vis_geometry_warps(c, smem, blockIdx.x * (KZ_THREADS / 32) + (threadIdx.x >> 5), gridDim.x * (KZ_THREADS / 32));
       if (!grid_barrier(st)) return;
       if (!vis_check(c, s)) break;
       uint32_t njobs = c.cnt->pair_count;

@@ -10,6 +10,9 @@
  *   .func (.b8[16] pos) kz_vs_pos(pipe, KzDraw* draw, vid, iid, push)  only gl_Position, returned by value
  *                                                                       (dead outputs dropped, ptxas removes
  *                                                                       their math)
+ *   .func (.b8[48] pos) kz_vs_pos3(pipe, draw, vid0, vid1, vid2, iid, push)  gl_Position of a triangle's three
+ *                                                                       vertices: push constants loaded once,
+ *                                                                       three straight copies of the body
  *   .func (.b32 discard) kz_fs(pipe, KzFsIn* in, push, float* color)   fragment shader
  *
  * The vertex functions fetch their own attributes: the pipeline's vertex input state (binding, format,
@@ -29,10 +32,12 @@
 
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
 #include "kz_ir.h"
+#include "kz_raster_abi.h"
 #include "kz_shader_backend_impl.h"
 
 namespace kz {
@@ -57,12 +62,43 @@ const char* cmp_name(uint32_t c) {
   return (c & ir::CmpUnordered) ? unord[k] : ord[k];
 }
 
-enum class Kind { VertexFull, VertexPos, Fragment };
+enum class Kind { VertexFull, VertexPos, VertexPos3, Fragment };
 
 class Emitter {
  public:
   std::string out;
-  uint32_t nf = 0, nr = 0, np = 0;
+  uint32_t nf = 0, nr = 0, np = 0, nk = 0;
+  std::map<uint32_t, std::string> push_regs; /* push-constant word (byte offset) -> register loaded up front */
+  uint32_t copy = 0;                          /* VertexPos3: which vertex the body computes */
+
+  /* load every push-constant word `fn` reads once, as 16-byte vectors where an aligned group is used twice
+   * or more (the push block is 16-byte aligned and KZ_PUSH_BYTES long) */
+  void preload_push(const Function& fn) {
+    push_regs.clear();
+    std::map<uint32_t, uint32_t> groups; /* 16-byte group -> mask of words read */
+    for (const Inst& i : fn.code)
+      if (i.op == Op::LdPush && i.imm % 4 == 0) groups[i.imm / 16] |= 1u << ((i.imm % 16) / 4);
+    char buf[200];
+    for (const auto& g : groups) {
+      uint32_t base = g.first * 16;
+      if (__builtin_popcount(g.second) >= 2 && base + 16 <= KZ_PUSH_BYTES) {
+        uint32_t r0 = nk;
+        nk += 4;
+        std::snprintf(buf, sizeof buf, "ld.global.nc.v4.b32 {%%kp%u, %%kp%u, %%kp%u, %%kp%u}, [%%kzpush+%u];", r0,
+                      r0 + 1, r0 + 2, r0 + 3, base);
+        line(buf);
+        for (uint32_t w = 0; w < 4; w++) push_regs[base + 4 * w] = "%kp" + std::to_string(r0 + w);
+      } else {
+        for (uint32_t w = 0; w < 4; w++) {
+          if (!(g.second & (1u << w))) continue;
+          std::string r = "%kp" + std::to_string(nk++);
+          std::snprintf(buf, sizeof buf, "ld.global.nc.b32 %s, [%%kzpush+%u];", r.c_str(), base + 4 * w);
+          line(buf);
+          push_regs[base + 4 * w] = r;
+        }
+      }
+    }
+  }
 
   void line(const std::string& s) { out += "  " + s + "\n"; }
 
@@ -168,13 +204,30 @@ class Emitter {
                         i.imm);
           line(buf);
           break;
-        case Op::LdPush:
+        case Op::LdPush: {
+          auto pr = push_regs.find(i.imm);
+          if (pr != push_regs.end()) {
+            line("mov.b32 " + R(i.dst) + ", " + pr->second + ";");
+            break;
+          }
           std::snprintf(buf, sizeof buf, "ld.global.nc.%s %s, [%%kzpush+%u];", i.ty == Ty::F32 ? "f32" : "u32",
                         R(i.dst).c_str(), i.imm);
           line(buf);
           break;
+        }
         case Op::StOut: {
-          if (kind == Kind::VertexPos && i.imm >= 16) break;
+          if ((kind == Kind::VertexPos || kind == Kind::VertexPos3) && i.imm >= 16) break;
+          if (kind == Kind::VertexPos3) {
+            std::string v3 = R(i.a);
+            if (fn.regs[(size_t)i.a] == Ty::Pred) {
+              line("selp.u32 %kzt, 1, 0, " + v3 + ";");
+              v3 = "%kzt";
+            }
+            std::snprintf(buf, sizeof buf, "st.param.%s [func_retval0+%u], %s;",
+                          fn.regs[(size_t)i.a] == Ty::F32 ? "f32" : "b32", 16 * copy + i.imm, v3.c_str());
+            line(buf);
+            break;
+          }
           std::string v = R(i.a);
           if (fn.regs[(size_t)i.a] == Ty::Pred) {
             line("selp.u32 %kzt, 1, 0, " + v + ";");
@@ -249,6 +302,10 @@ class Emitter {
         case Op::Bra: line("bra " + L(i.imm) + ";"); break;
         case Op::BraIf: line("@" + R(i.a) + " bra " + L(i.imm) + ";"); break;
         case Op::Ret:
+          if (kind == Kind::VertexPos3) {
+            line("bra $" + pfx + "_end;");
+            break;
+          }
           if (kind == Kind::Fragment) {
             line("mov.b32 %kzt, 0;");
             line("st.param.b32 [func_retval0], %kzt;");
@@ -263,6 +320,10 @@ class Emitter {
           line("ret;");
           break;
       }
+    }
+    if (kind == Kind::VertexPos3) { /* the next vertex's copy follows */
+      out += "$" + pfx + "_end:\n";
+      return;
     }
     /* a body always ends in Ret; keep a fallback for malformed input */
     if (kind == Kind::Fragment) {
@@ -281,7 +342,16 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
     e.out.clear();
     std::string pfx = std::string(fname) + "_p" + std::to_string(p);
     e.out += "$" + pfx + ":\n";
-    if (stages[p]) {
+    if (stages[p] && kind == Kind::VertexPos3) {
+      e.preload_push(stages[p]->fn);
+      for (uint32_t k = 0; k < 3; k++) {
+        e.copy = k;
+        e.line("mov.b32 %kzvid, %kzv" + std::to_string(k) + ";");
+        e.body(stages[p]->fn, pfx + "_v" + std::to_string(k), kind, p < layouts.size() ? &layouts[p] : nullptr);
+      }
+      e.push_regs.clear();
+      e.line("ret;");
+    } else if (stages[p]) {
       e.body(stages[p]->fn, pfx, kind, p < layouts.size() ? &layouts[p] : nullptr);
     } else {
       if (kind == Kind::Fragment) {
@@ -299,6 +369,12 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
                   ".visible .func (.param .b32 func_retval0) %s(\n  .param .b32 %s_pipe,\n  .param .b64 %s_in,\n"
                   "  .param .b64 %s_push,\n  .param .b64 %s_out\n)\n{\n",
                   fname, fname, fname, fname, fname);
+  } else if (kind == Kind::VertexPos3) {
+    std::snprintf(buf, sizeof buf,
+                  ".visible .func (.param .align 16 .b8 func_retval0[48]) %s(\n  .param .b32 %s_pipe,\n"
+                  "  .param .b64 %s_draw,\n  .param .b32 %s_vid0,\n  .param .b32 %s_vid1,\n  .param .b32 %s_vid2,\n"
+                  "  .param .b32 %s_iid,\n  .param .b64 %s_push\n)\n{\n",
+                  fname, fname, fname, fname, fname, fname, fname, fname);
   } else if (kind == Kind::VertexPos) {
     std::snprintf(buf, sizeof buf,
                   ".visible .func (.param .align 16 .b8 func_retval0[16]) %s(\n  .param .b32 %s_pipe,\n"
@@ -311,8 +387,9 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
                   fname, fname, fname, fname, fname, fname, fname);
   }
   s += buf;
-  s += "  .reg .b32 %kzsel, %kzt, %kzvid, %kziid;\n  .reg .b64 %kzin, %kzpush, %kzout, %kzdraw, %kzoff;\n"
-       "  .reg .b64 %kzvb<8>;\n  .reg .pred %kzp;\n";
+  s += "  .reg .b32 %kzsel, %kzt, %kzvid, %kziid, %kzv0, %kzv1, %kzv2;\n"
+       "  .reg .b64 %kzin, %kzpush, %kzout, %kzdraw, %kzoff;\n  .reg .b64 %kzvb<8>;\n  .reg .pred %kzp;\n";
+  if (e.nk) s += "  .reg .b32 %kp<" + std::to_string(e.nk) + ">;\n";
   if (e.nf) s += "  .reg .f32 %f<" + std::to_string(e.nf) + ">;\n";
   if (e.nr) s += "  .reg .b32 %r<" + std::to_string(e.nr) + ">;\n";
   if (e.np) s += "  .reg .pred %p<" + std::to_string(e.np) + ">;\n";
@@ -321,6 +398,14 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
   s += buf;
   if (kind == Kind::Fragment) {
     std::snprintf(buf, sizeof buf, "  ld.param.u64 %%kzin, [%s_in];\n  ld.param.u64 %%kzout, [%s_out];\n", fname, fname);
+  } else if (kind == Kind::VertexPos3) {
+    std::snprintf(buf, sizeof buf,
+                  "  ld.param.u64 %%kzdraw, [%s_draw];\n  cvta.to.global.u64 %%kzdraw, %%kzdraw;\n"
+                  "  ld.param.u32 %%kzv0, [%s_vid0];\n  ld.param.u32 %%kzv1, [%s_vid1];\n"
+                  "  ld.param.u32 %%kzv2, [%s_vid2];\n  ld.param.u32 %%kziid, [%s_iid];\n",
+                  fname, fname, fname, fname, fname);
+    s += buf;
+    buf[0] = 0;
   } else {
     std::snprintf(buf, sizeof buf,
                   "  ld.param.u64 %%kzdraw, [%s_draw];\n  cvta.to.global.u64 %%kzdraw, %%kzdraw;\n"
@@ -354,6 +439,7 @@ std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vec
   std::string s = ".version 9.0\n.target sm_103a\n.address_size 64\n\n";
   s += function_text("kz_vs", Kind::VertexFull, vs, layouts);
   s += function_text("kz_vs_pos", Kind::VertexPos, vs, layouts);
+  s += function_text("kz_vs_pos3", Kind::VertexPos3, vs, layouts);
   s += function_text("kz_fs", Kind::Fragment, fs, {});
   return s;
 }
