@@ -190,19 +190,17 @@ def cpu_baseline(scene, budget_s=4.0):
 
 def main():
     args = parse()
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from kazan_gb300 import replicas
+    rk = replicas.from_env()
+    rank, world, local = rk.rank, rk.world, rk.local
     if args.impl == "reference":
-        if rank != 0:
+        if not rk.leader:
             return 0
         scene, cfg = make_scene(args)
         return reference_arm(args, scene, cfg)
     import torch
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    replicas.init(rk, "nccl", torch.device("cuda", local))
     from kazan_gb300 import render
     scene, cfg = make_scene(args)
     r = render.Renderer()
@@ -213,9 +211,7 @@ def main():
     stream = torch.cuda.ExternalStream(r.stream())
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        replicas.barrier(rk)
 
     for _ in range(max(3, args.warmup)):
         run.submit()
@@ -236,12 +232,7 @@ def main():
     ck = clocks.stop(w0, w1)
     torch.cuda.synchronize()
     barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(rk, e0.elapsed_time(e1) / args.steps, device="cuda")
     # per-kernel device time over the timed submissions (events on the queue stream around each launch)
     ktimes = r.drv.kernel_times(run.cb)
     kernels = {k: {"launches": n, "ms_per_launch": round(t / max(n, 1), 4),
@@ -251,7 +242,7 @@ def main():
     dom_ms = ktimes[dom][0] / ktimes[dom][1]
     st = run.stats()
     tris = scene.triangles
-    value = tris * world / (ms / 1e3) / 1e6
+    value = replicas.aggregate_rate(rk, tris, ms) / 1e6
     peak, peak_kind = measured_peak()
     kb, kformula = kernel_bytes(scene, dom)
     achieved = kb / (dom_ms / 1e3) / 1e9
@@ -303,7 +294,7 @@ def main():
         for _ in range(steps):
             e2.submit()
             ctypes.memmove(host.ctypes.data, p, nbytes)
-        el = (time.perf_counter() - t0) / steps
+        el = replicas.max_over_ranks(rk, (time.perf_counter() - t0) / steps, device="cuda")
         h2d = scene.vertices.nbytes + (scene.indices.nbytes if scene.indices is not None else 0)
         out["e2e"] = {"value": round(tris * world / el / 1e6, 2), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d),
                       "d2h_bytes_per_step": int(nbytes), "ms_per_step": round(el * 1e3, 3), "steps": steps}
@@ -312,9 +303,7 @@ def main():
     if rank == 0:
         print(json.dumps(out), flush=True)
     r.close()
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    replicas.finish(rk)
     return 0
 
 

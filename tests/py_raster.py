@@ -1,0 +1,132 @@
+"""A second, independent restatement of the draw path's rules in pure Python, for tiny scenes only.
+
+It is test infrastructure: it checks the C oracle (oracle/kz_oracle.c) on hand-sized cases, using exact
+rational arithmetic with one explicit round-to-nearest-even to binary32 per operation, so every fma is a
+true single-rounding fma.  Coverage: colour pipeline (pass-through vertex shader, colour fragment shader),
+non-indexed triangle lists with no clipping needed (0 <= z <= w, inside the guard band), full-framebuffer
+viewport with depth range [0, 1], no culling, depth test LESS with writes, no blending.
+
+Rules (Vulkan specification, with the choices the spec leaves open fixed as the GPU path fixes them):
+viewport x_f = fma(x * (1/w), W/2, W/2), snapped to 16.8 fixed point with round-to-nearest-even; signed
+area S of the snapped vertices decides orientation; pixel (x, y) is sampled at (256 x + 128, 256 y + 128);
+edge e runs from vertex e+1 to vertex e+2 and a pixel is covered when every edge function is > 0, or
+== 0 on a top or left edge; depth z = fma(l2, z2 - z0, fma(l1, z1 - z0, z0)) with l_i = E_i * (1 / S);
+colour = perspective-correct interpolation q = fma(l2, 1/w2, fma(l1, 1/w1, l0 * 1/w0)),
+c = fma(l2, c2/w2, fma(l1, c1/w1, l0 * c0/w0)) * (1 / q), stored as round(clamp(c, 0, 1) * 255).
+"""
+from fractions import Fraction
+import math
+
+import numpy as np
+
+HALF = Fraction(1, 2)
+
+
+def f32(q):
+    """round an exact rational to the nearest binary32 value, ties to even (no overflow handling)"""
+    q = Fraction(q)
+    if q == 0:
+        return Fraction(0)
+    sign = -1 if q < 0 else 1
+    a = abs(q)
+    e = a.numerator.bit_length() - a.denominator.bit_length()
+    while Fraction(2) ** e > a:
+        e -= 1
+    while Fraction(2) ** (e + 1) <= a:
+        e += 1
+    e = max(e, -126)
+    ulp = Fraction(2) ** (e - 23)
+    m = a / ulp
+    n = math.floor(m)
+    r = m - n
+    if r > HALF or (r == HALF and n % 2 == 1):
+        n += 1
+    return sign * n * ulp
+
+
+def mul(a, b):
+    return f32(a * b)
+
+
+def fma(a, b, c):
+    return f32(a * b + c)
+
+
+def div(a, b):
+    return f32(Fraction(a) / Fraction(b))
+
+
+def rne(q):
+    """round to the nearest integer, ties to even"""
+    return round(Fraction(q))
+
+
+def unorm8(v):
+    c = min(max(v, Fraction(0)), Fraction(1))
+    return int(rne(mul(c, Fraction(255))))
+
+
+def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_depth=1.0):
+    """vertices: float32 [3T, 8] (x, y, z, w, r, g, b, a); returns (colour uint8 [H, W, 4], depth float32
+    [H, W], fragment count)"""
+    v = np.asarray(vertices, dtype=np.float32).reshape(-1, 8)
+    color = np.empty((height, width, 4), dtype=np.uint8)
+    color[:] = [unorm8(Fraction(float(np.float32(c)))) for c in clear_color]
+    depth = [[Fraction(float(np.float32(clear_depth)))] * width for _ in range(height)]
+    hx, hy = f32(Fraction(width) / 2), f32(Fraction(height) / 2)
+    frags = 0
+    for t in range(len(v) // 3):
+        P = [[Fraction(float(c)) for c in v[3 * t + j]] for j in range(3)]
+        X, Y, Z, IW, A = [], [], [], [], []
+        for p in P:
+            x, y, z, w = p[:4]
+            assert w > 0 and 0 <= z <= w and abs(x) <= 4 * w and abs(y) <= 4 * w, "case needs clipping"
+            iw = div(1, w)
+            X.append(int(rne(mul(fma(mul(x, iw), hx, hx), 256))))
+            Y.append(int(rne(mul(fma(mul(y, iw), hy, hy), 256))))
+            Z.append(fma(mul(z, iw), Fraction(1), Fraction(0)))
+            IW.append(iw)
+            A.append([mul(c, iw) for c in p[4:8]])
+        S = (X[1] - X[0]) * (Y[2] - Y[0]) - (X[2] - X[0]) * (Y[1] - Y[0])
+        if S == 0:
+            continue
+        if S < 0:
+            for arr in (X, Y, Z, IW, A):
+                arr[1], arr[2] = arr[2], arr[1]
+            S = -S
+        bx0 = max(0, -((-(min(X) - 128)) // 256))
+        by0 = max(0, -((-(min(Y) - 128)) // 256))
+        bx1 = min(width - 1, (max(X) - 128) // 256)
+        by1 = min(height - 1, (max(Y) - 128) // 256)
+        inv_s = div(1, f32(S))
+        z0, dz1, dz2 = Z[0], f32(Z[1] - Z[0]), f32(Z[2] - Z[0])
+        tl, dxs, dys = [], [], []
+        for e in range(3):
+            a, b = (e + 1) % 3, (e + 2) % 3
+            dx, dy = X[b] - X[a], Y[b] - Y[a]
+            dxs.append(dx)
+            dys.append(dy)
+            tl.append(dy < 0 or (dy == 0 and dx > 0))
+        for py in range(by0, by1 + 1):
+            for px in range(bx0, bx1 + 1):
+                sx, sy = 256 * px + 128, 256 * py + 128
+                E = []
+                for e in range(3):
+                    a = (e + 1) % 3
+                    E.append(dxs[e] * (sy - Y[a]) - dys[e] * (sx - X[a]))
+                if not all(E[e] > 0 or (E[e] == 0 and tl[e]) for e in range(3)):
+                    continue
+                frags += 1
+                l = [mul(f32(E[e]), inv_s) for e in range(3)]
+                z = fma(l[2], dz2, fma(l[1], dz1, z0))
+                z = min(max(z, Fraction(0)), Fraction(1))
+                if not z < depth[py][px]:
+                    continue
+                depth[py][px] = z
+                q = fma(l[2], IW[2], fma(l[1], IW[1], mul(l[0], IW[0])))
+                rq = div(1, q)
+                for k in range(4):
+                    num = fma(l[2], A[2][k], fma(l[1], A[1][k], mul(l[0], A[0][k])))
+                    color[py, px, k] = unorm8(mul(num, rq))
+    dep = np.array([[float(d) for d in row] for row in depth], dtype=np.float32)
+    return color, dep, frags

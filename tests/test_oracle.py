@@ -1,0 +1,175 @@
+"""The CPU oracle (oracle/kz_oracle.c) on the CPU: checked against an independent pure-Python restatement
+of the rules (tests/py_raster.py, exact rational arithmetic) on small scenes, against properties that
+follow from the rules by hand (watertight tessellations, no double coverage at shared vertices, invariance
+under vertex rotation, UNORM8 rounding), and against its own committed golden digests.
+
+The reference driver has no rasteriser to pin against (vulkan-driver/src/api_impl.rs:4632-4653 are
+`unimplemented!()`); these checks are what pins the oracle."""
+import hashlib
+import json
+import os
+import struct
+
+import numpy as np
+import pytest
+
+import py_raster
+from kazan_gb300 import scenes
+from oracle import kz_oracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _pix_to_ndc(px, size):
+    return 2.0 * px / size - 1.0
+
+
+def _tri(points, size, z=0.5, w=1.0, rgba=(1.0, 0.5, 0.25, 1.0)):
+    """three vertices given in pixel coordinates (x right, y down) -> clip-space rows"""
+    rows = []
+    for (x, y) in points:
+        rows.append([_pix_to_ndc(x, size) * w, _pix_to_ndc(y, size) * w, z * w, w] + list(rgba))
+    return rows
+
+
+def _scene(rows, size):
+    return scenes.triangles_from(np.array(rows, dtype=np.float32), size, size, clear_color=(0.0, 0.0, 0.0, 0.0))
+
+
+def _both(rows, size):
+    sc = _scene(rows, size)
+    oc, od, st = kz_oracle.render(sc, threads=1)
+    pc, pd, pf = py_raster.render(sc.vertices, size, size, clear_color=sc.clear_color)
+    return sc, (oc, od, st["fragments"]), (pc, pd, pf)
+
+
+def _random_rows(seed, n, size, perspective):
+    rng = np.random.default_rng(seed)
+    rows = []
+    for _ in range(n):
+        c = rng.uniform(-2, size + 2, 2)
+        pts = [tuple(c + rng.normal(0, size / 5, 2)) for _ in range(3)]
+        z = [float(rng.uniform(0.05, 0.95)) for _ in range(3)]
+        w = [float(rng.uniform(0.5, 2.0)) if perspective else 1.0 for _ in range(3)]
+        col = rng.uniform(0, 1, (3, 4))
+        for j in range(3):
+            x, y = pts[j]
+            rows.append([_pix_to_ndc(x, size) * w[j], _pix_to_ndc(y, size) * w[j], z[j] * w[j], w[j]] + list(col[j]))
+    return rows
+
+
+@pytest.mark.parametrize("seed,perspective", [(1, False), (2, False), (3, True), (4, True)])
+def test_oracle_matches_python_restatement(built, seed, perspective):
+    size = 24
+    _, (oc, od, of), (pc, pd, pf) = _both(_random_rows(seed, 12, size, perspective), size)
+    assert of == pf
+    assert np.array_equal(od.view(np.uint32), pd.view(np.uint32))
+    assert np.array_equal(oc, pc)
+
+
+def test_watertight_tessellation(built):
+    """an 8x8 grid of cells over a 16-pixel square, each cell split in two: every pixel of the square is
+    covered exactly once (no gaps, no double hits on shared edges)"""
+    size, n, x0, s = 24, 8, 4.0, 2.0
+    rows = []
+    for i in range(n):
+        for j in range(n):
+            a, b = (x0 + i * s, x0 + j * s), (x0 + (i + 1) * s, x0 + j * s)
+            c, d = (x0 + (i + 1) * s, x0 + (j + 1) * s), (x0 + i * s, x0 + (j + 1) * s)
+            rows += _tri([a, b, c], size) + _tri([a, c, d], size)
+    sc, (oc, od, of), (pc, pd, pf) = _both(rows, size)
+    assert of == pf == 16 * 16
+    covered = oc[..., 3] > 0
+    assert covered[4:20, 4:20].all() and covered.sum() == 256
+    assert np.array_equal(oc, pc)
+
+
+def test_shared_vertex_on_pixel_centre(built):
+    """a fan of 8 triangles around a pixel centre: the centre pixel is covered by exactly one of them"""
+    size = 16
+    cx, cy = 8.5, 8.5
+    ring = [(cx + 5 * np.cos(a), cy + 5 * np.sin(a)) for a in np.linspace(0, 2 * np.pi, 9)[:-1]]
+    rows = []
+    for k in range(8):
+        rows += _tri([(cx, cy), ring[k], ring[(k + 1) % 8]], size, z=0.1 + 0.1 * k)
+    sc, (oc, od, of), (pc, pd, pf) = _both(rows, size)
+    assert of == pf
+    # count how many fan triangles cover the centre pixel with the oracle, one triangle at a time
+    hits = 0
+    for k in range(8):
+        one = _scene(rows[3 * k:3 * k + 3], size)
+        c, _, _ = kz_oracle.render(one)
+        hits += int(c[8, 8, 3] > 0)
+    assert hits == 1
+
+
+def test_vertex_rotation_keeps_coverage(built):
+    size = 24
+    rows = _random_rows(7, 10, size, False)
+    rot = []
+    for t in range(len(rows) // 3):
+        a, b, c = rows[3 * t:3 * t + 3]
+        rot += [b, c, a]
+    _, _, st1 = kz_oracle.render(_scene(rows, size))
+    _, _, st2 = kz_oracle.render(_scene(rot, size))
+    assert st1["fragments"] == st2["fragments"]
+    # flat triangles (equal z, equal colour) give the same image under rotation
+    flat = [r[:2] + [0.25 * r[3], r[3]] + [0.2, 0.4, 0.6, 1.0] for r in rows]
+    flat_rot = [r[:2] + [0.25 * r[3], r[3]] + [0.2, 0.4, 0.6, 1.0] for r in rot]
+    c1, d1, _ = kz_oracle.render(_scene(flat, size))
+    c2, d2, _ = kz_oracle.render(_scene(flat_rot, size))
+    assert np.array_equal(c1[..., 3] > 0, c2[..., 3] > 0)
+
+
+def test_degenerate_and_offscreen_produce_nothing(built):
+    size = 16
+    rows = _tri([(2, 2), (6, 6), (10, 10)], size)            # collinear
+    rows += _tri([(3, 3), (3, 3), (3, 3)], size)             # a point
+    rows += _tri([(-20, 2), (-10, 2), (-15, 8)], size)       # left of the framebuffer
+    rows += _tri([(2.6, 2.6), (2.9, 2.6), (2.6, 2.9)], size)  # misses every pixel centre
+    _, _, st = kz_oracle.render(_scene(rows, size))
+    assert st["fragments"] == 0
+
+
+def _f32(x):
+    return struct.unpack("<f", struct.pack("<f", x))[0]
+
+
+def test_unorm8_rounding_boundaries(built):
+    for k in range(0, 255):
+        mid = _f32((k + 0.5) / 255.0)
+        for v in (mid, np.nextafter(np.float32(mid), np.float32(0)), np.nextafter(np.float32(mid), np.float32(1))):
+            v = float(np.float32(v))
+            assert kz_oracle.unorm8(v) == py_raster.unorm8(py_raster.Fraction(v)), v
+    assert kz_oracle.unorm8(-1.0) == 0 and kz_oracle.unorm8(2.0) == 255 and kz_oracle.unorm8(float("nan")) in (0, 255)
+
+
+def _digest(color, depth):
+    return hashlib.sha256(color.tobytes()).hexdigest()[:32], hashlib.sha256(depth.tobytes()).hexdigest()[:32]
+
+
+def test_oracle_golden_digests(built):
+    """tests/golden/oracle_digests.json (made by tests/golden/make_oracle_golden.py) fixes the oracle's
+    output on the small workloads, so a change to the oracle cannot pass silently"""
+    with open(os.path.join(GOLDEN, "oracle_digests.json"), encoding="utf-8") as f:
+        gold = json.load(f)
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_oracle_golden
+    for name, scene in make_oracle_golden.cases().items():
+        c, d, st = kz_oracle.render(scene, threads=4)
+        cd, dd = _digest(c, d)
+        assert gold[name] == {"color": cd, "depth": dd, "fragments": st["fragments"]}, name
+
+
+def test_oracle_matches_python_on_plain_draw_prefix(built):
+    """the first 8 triangles of the 2,048-triangle plain draw (seed 1), drawn at 40x40"""
+    soup = scenes.small_soup()
+    rows = soup.vertices[:24]
+    size = 40
+    sc = scenes.triangles_from(rows, size, size)
+    oc, od, st = kz_oracle.render(sc, threads=1)
+    pc, pd, pf = py_raster.render(sc.vertices, size, size, clear_color=sc.clear_color)
+    assert st["fragments"] == pf > 0
+    assert np.array_equal(od.view(np.uint32), pd.view(np.uint32))
+    assert np.array_equal(oc, pc)
