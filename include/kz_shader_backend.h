@@ -5,7 +5,8 @@
  *   kzShaderCompile       front end of Compiler::run (lib.rs:245-257) for one stage: SPIR-V entry point ->
  *                         shader IR (role of TranslatedSPIRVShader::new,
  *                         shader-compiler-translate-spirv-to-ir/src/lib.rs:191-214)
- *   kzShaderEmitPtx       code generation for a pipeline set: PTX device functions kz_vs, kz_vs_pos, kz_fs
+ *   kzShaderEmitPtx       code generation for a pipeline set: PTX device functions kz_vs, kz_vs_pos,
+ *                         kz_vs_pos3, kz_fs
  *   kzShaderLink          JIT link with the pipeline kernels -> CompiledCode (lib.rs:200-205)
  *   kzCompiledCodeImage   the linked sm_103a image; kernels are looked up by name (CompiledCode::get)
  *   kzSpirvDisassemble    text dump of a module in the reference decoder's format

@@ -1103,7 +1103,8 @@ struct WarpTri {
   uint32_t pw, magic; /* pixel pairs per box row, ceil(w / 2); umulhi(i, magic) = i / pw for i < 2^16 */
   uint32_t start, w;  /* number of the box's first pair in the warp's list; box width */
   float z0, dz1, dz2, inv_s;
-  uint32_t g, thr;    /* primitive number; bit k: edge k's threshold is 1 */
+  uint32_t g, thr;    /* primitive number; bit k: edge k's threshold is 1; bit 3: every edge value over the
+                         box fits in 32 bits */
 };                    /* 96 bytes */
 static_assert(sizeof(WarpTri) == 96, "WarpTri layout");
 
@@ -1112,7 +1113,17 @@ __device__ __forceinline__ void warp_fragment(const KzSegment& seg, const WarpTr
                                               float zmax, int32_t x, int32_t y) {
   uint32_t thr = t.thr;
   float l1 = fmul(kz_i64_to_f32(e1 + (int64_t)((thr >> 1) & 1u)), t.inv_s);
-  float l2 = fmul(kz_i64_to_f32(e2 + (int64_t)(thr >> 2)), t.inv_s);
+  float l2 = fmul(kz_i64_to_f32(e2 + (int64_t)((thr >> 2) & 1u)), t.inv_s);
+  float z = ffma(l2, t.dz2, ffma(l1, t.dz1, t.z0));
+  z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
+  vis_store(seg, vis_key(seg.vis_key, z, t.g), x, y);
+}
+
+/* the same for edge values known to fit in 32 bits (E1, E2 with their thresholds added back) */
+__device__ __forceinline__ void warp_fragment32(const KzSegment& seg, const WarpTri& t, int32_t e1, int32_t e2,
+                                                float zmin, float zmax, int32_t x, int32_t y) {
+  float l1 = fmul(__int2float_rn(e1), t.inv_s);
+  float l2 = fmul(__int2float_rn(e2), t.inv_s);
   float z = ffma(l2, t.dz2, ffma(l1, t.dz1, t.z0));
   z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
   vis_store(seg, vis_key(seg.vis_key, z, t.g), x, y);
@@ -1155,14 +1166,20 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
     t.start = start;
     int64_t px = (int64_t)t.ox * 256 + 128, py = (int64_t)t.oy * 256 + 128;
     uint32_t thr = 0;
+    bool fits = true;
+    const int64_t h1 = (int64_t)((r.bb1 >> 16) - (r.bb0 >> 16)), w1 = (int64_t)t.w - 1;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       t.e[k] = edge_at(e, k, px, py) - e.thr[k];
       t.ex[k] = -e.dy[k] * 256;
       t.ey[k] = e.dx[k] * 256;
       thr |= (uint32_t)e.thr[k] << k;
+      /* largest |value| the edge takes over the box (plus one step past its last column) */
+      int64_t ae = t.e[k] < 0 ? -t.e[k] : t.e[k];
+      int64_t bound = ae + (int64_t)abs(t.ex[k]) * (w1 + 1) + (int64_t)abs(t.ey[k]) * h1 + 1;
+      fits = fits && bound < 0x7FFFFFFFll;
     }
-    t.thr = thr;
+    t.thr = thr | (fits ? 8u : 0u);
     t.z0 = r.z0;
     t.dz1 = r.dz1;
     t.dz2 = r.dz2;
@@ -1187,10 +1204,32 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
     uint32_t y = pw > 1 ? __umulhi(local, t.magic) : local;
     int32_t x = (int32_t)(local - y * pw) * 2;
     int32_t sx0 = t.ex[0], sx1 = t.ex[1], sx2 = t.ex[2];
+    int32_t px = t.ox + x, py = t.oy + (int32_t)y;
+    const uint32_t tthr = t.thr;
+    if (tthr & 8u) {
+      /* every edge value of this box fits in 32 bits: the same integers in 32-bit arithmetic */
+      int32_t e0 = (int32_t)t.e[0] + sx0 * x + t.ey[0] * (int32_t)y;
+      int32_t e1 = (int32_t)t.e[1] + sx1 * x + t.ey[1] * (int32_t)y;
+      int32_t e2 = (int32_t)t.e[2] + sx2 * x + t.ey[2] * (int32_t)y;
+      if ((e0 | e1 | e2) >= 0) {
+        frags++;
+        warp_fragment32(seg, t, e1 + (int32_t)((tthr >> 1) & 1u), e2 + (int32_t)((tthr >> 2) & 1u), zmin, zmax, px, py);
+      }
+      if ((uint32_t)x + 1 < t.w) {
+        e0 += sx0;
+        e1 += sx1;
+        e2 += sx2;
+        if ((e0 | e1 | e2) >= 0) {
+          frags++;
+          warp_fragment32(seg, t, e1 + (int32_t)((tthr >> 1) & 1u), e2 + (int32_t)((tthr >> 2) & 1u), zmin, zmax, px + 1,
+                          py);
+        }
+      }
+      continue;
+    }
     int64_t e0 = t.e[0] + (int64_t)sx0 * x + (int64_t)t.ey[0] * (int32_t)y;
     int64_t e1 = t.e[1] + (int64_t)sx1 * x + (int64_t)t.ey[1] * (int32_t)y;
     int64_t e2 = t.e[2] + (int64_t)sx2 * x + (int64_t)t.ey[2] * (int32_t)y;
-    int32_t px = t.ox + x, py = t.oy + (int32_t)y;
     if ((e0 | e1 | e2) >= 0) {
       frags++;
       warp_fragment(seg, t, e1, e2, zmin, zmax, px, py);
