@@ -460,6 +460,8 @@ void free_lowered(Lowered* low) {
   device_free(low->d_tables);
   device_free(low->d_records);
   device_free(low->d_bins);
+  device_free(low->d_shades);
+  low->d_shades = nullptr;
   device_free(low->d_tiles);
   device_free(low->d_vis);
   low->d_vis = nullptr;
@@ -541,7 +543,8 @@ static VkResult size_scratch(Device* dev, Lowered& low, uint32_t rec_cap, uint32
   cudaSetDevice(dev->pd->cuda_device);
   device_free(low.d_records);
   device_free(low.d_bins);
-  low.d_records = low.d_bins = nullptr;
+  device_free(low.d_shades);
+  low.d_records = low.d_bins = low.d_shades = nullptr;
   void* p = nullptr;
   VkResult r = device_alloc((size_t)rec_cap * sizeof(KzTriRecord), &p);
   if (r != VK_SUCCESS) return r;
@@ -549,11 +552,25 @@ static VkResult size_scratch(Device* dev, Lowered& low, uint32_t rec_cap, uint32
   r = device_alloc((size_t)pair_cap * 4, &p);
   if (r != VK_SUCCESS) return r;
   low.d_bins = static_cast<char*>(p);
+  /* ordered segments keep each unclipped record's shading setup beside it: 1/w of the three vertices
+   * (16 bytes) then three vertices' varyings */
+  bool ordered = false;
+  for (const KzSegment& s : low.segments) ordered |= s.mode == KZ_MODE_ORDERED && s.num_chunks > 0;
+  if (ordered) {
+    uint32_t nv = 0;
+    for (const KzPipe& kp : low.pipes) nv = std::max(nv, kp.num_varyings);
+    low.shade_stride = (uint32_t)align_up(16 + 12 * (size_t)nv, 16);
+    r = device_alloc((size_t)rec_cap * low.shade_stride, &p);
+    if (r != VK_SUCCESS) return r;
+    low.d_shades = static_cast<char*>(p);
+  }
   low.rec_cap = rec_cap;
   low.pair_cap = pair_cap;
   for (KzSegment& s : low.segments) {
     s.records = (uint64_t)(uintptr_t)low.d_records;
     s.bins = (uint64_t)(uintptr_t)low.d_bins;
+    s.shades = (uint64_t)(uintptr_t)low.d_shades;
+    s.shade_stride = low.shade_stride;
     s.rec_cap = rec_cap;
     s.pair_cap = pair_cap;
   }

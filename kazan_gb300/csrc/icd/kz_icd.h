@@ -223,6 +223,8 @@ struct Lowered {
   char* d_bins = nullptr;
   uint32_t* d_tiles = nullptr;
   char* d_vis = nullptr;
+  char* d_shades = nullptr;   /* ordered segments: per-record shading setup (KzSegment::shades) */
+  uint32_t shade_stride = 0;
   KzSegCounters* d_counters = nullptr;
   KzStatus* d_status = nullptr;
   KzStatus* h_status = nullptr;

@@ -185,7 +185,10 @@ typedef struct KzSegment {
   uint64_t vis;              /* visibility mode: u64 (depth, primitive) key per pixel, width * height */
   uint32_t rec_cap, pair_cap;
   uint32_t segment_index;
-  uint32_t pad;
+  uint32_t shade_stride;     /* ordered mode: bytes per record in `shades` */
+  uint64_t shades;           /* ordered mode: per record, the shading setup of an unclipped triangle:
+                                float 1/w[3], pad, then varyings (divided by w unless flat/noperspective)
+                                [3][num_varyings] */
 } KzSegment;
 
 /* status words written by the kernels (one per submission) */

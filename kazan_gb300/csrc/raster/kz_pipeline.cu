@@ -488,14 +488,16 @@ __device__ __forceinline__ uint32_t to_rgba(uint32_t px, uint32_t fmt) {
 }
 __device__ __forceinline__ uint32_t from_rgba(uint32_t px, uint32_t fmt) { return to_rgba(px, fmt); }
 
-/* apply blend + write mask; dst/out packed RGBA (R in the low byte) */
-__device__ uint32_t color_write(const KzPipe& p, uint32_t dst, const float col[4]) {
+/* apply blend + write mask; dst/out packed RGBA (R in the low byte).  `u8tab`, when given, holds u8f(k)
+ * for k = 0..255 (the same quotients, read instead of divided). */
+__device__ uint32_t color_write(const KzPipe& p, uint32_t dst, const float col[4], const float* u8tab = nullptr) {
   uint32_t out = dst;
   if (p.blend_enable) {
     float s[4], dd[4];
     for (int i = 0; i < 4; i++) {
       s[i] = fminf(fmaxf(col[i], 0.0f), 1.0f);
-      dd[i] = u8f((dst >> (8 * i)) & 0xFFu);
+      uint32_t u = (dst >> (8 * i)) & 0xFFu;
+      dd[i] = u8tab ? u8tab[u] : u8f(u);
     }
     for (int i = 0; i < 4; i++) {
       if (!((p.write_mask >> i) & 1u)) continue;
@@ -664,11 +666,12 @@ __device__ __noinline__ void geometry_clipped(const Ctx& c, const KzDraw& d, con
   }
 }
 
-/* returns true with the record of an unclipped visible triangle; clipped triangles are emitted here */
-__device__ bool geometry_triangle(const Ctx& c, uint32_t di, uint32_t local, KzTriRecord& r) {
+/* returns true with the record of an unclipped visible triangle (and its vertex indices, instance and
+ * whether setup swapped vertices 1 and 2); clipped triangles are emitted here */
+__device__ bool geometry_triangle(const Ctx& c, uint32_t di, uint32_t local, KzTriRecord& r, uint32_t vid[3],
+                                  uint32_t& iid, bool& sw) {
   const KzDraw& d = c.draws[di];
   const KzPipe& p = c.pipes[d.pipe];
-  uint32_t vid[3], iid;
   tri_vertices(d, local, vid, iid);
   float pos[3][4];
   const uint8_t* push = push_ptr(*c.f, d);
@@ -687,7 +690,6 @@ __device__ bool geometry_triangle(const Ctx& c, uint32_t di, uint32_t local, KzT
     return false;
   }
   Proj pr[3] = {project(d, pos[0]), project(d, pos[1]), project(d, pos[2])};
-  bool sw;
   if (!make_record(d, p, pr, r, sw)) return false;
   r.g = g;
   r.draw = di;
@@ -695,12 +697,37 @@ __device__ bool geometry_triangle(const Ctx& c, uint32_t di, uint32_t local, KzT
   return true;
 }
 
+/* the shading setup of an unclipped record, stored beside it once so that the tiles it overlaps do not
+ * recompute it: full vertex shader of its three vertices, then what shade_direct computes */
+__device__ void write_shade(const Ctx& c, uint32_t idx, uint32_t di, const uint32_t vid[3], uint32_t iid, bool swapped) {
+  const KzSegment& seg = *c.seg;
+  if (idx >= seg.rec_cap || !seg.shades) return;
+  const KzDraw& d = c.draws[di];
+  const KzPipe& p = c.pipes[d.pipe];
+  KzVsOut o[3];
+  for (int j = 0; j < 3; j++) vs_full(c, d, p, vid[j], iid, o[j]);
+  float* dst = reinterpret_cast<float*>(seg.shades + (size_t)idx * seg.shade_stride);
+  const int nc = (int)p.num_varyings;
+  const int order[3] = {0, swapped ? 2 : 1, swapped ? 1 : 2};
+  for (int i = 0; i < 3; i++) {
+    const KzVsOut& src = o[order[i]];
+    float iw = fdiv(1.0f, src.pos[3]);
+    dst[i] = iw;
+    for (int k = 0; k < nc; k++) {
+      bool flat = (p.flat_mask >> k) & 1u;
+      float val = flat ? o[0].var[k] : src.var[k];
+      dst[4 + i * nc + k] = (flat || ((p.noperspective_mask >> k) & 1u)) ? val : fmul(val, iw);
+    }
+  }
+}
+
 /* one chunk per block: records are allocated with one atomic per block */
 __device__ void geometry_chunk(const Ctx& c, uint32_t chunk, uint32_t* sh) {
   const KzChunk ch = reinterpret_cast<const KzChunk*>(c.f->chunks)[chunk];
   KzTriRecord r;
-  bool have = false;
-  if (threadIdx.x < ch.count) have = geometry_triangle(c, ch.draw, ch.first + threadIdx.x, r);
+  bool have = false, sw = false;
+  uint32_t vid[3] = {0, 0, 0}, iid = 0;
+  if (threadIdx.x < ch.count) have = geometry_triangle(c, ch.draw, ch.first + threadIdx.x, r, vid, iid, sw);
   uint32_t ballot = __ballot_sync(0xFFFFFFFFu, have);
   uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) sh[warp] = (uint32_t)__popc(ballot);
@@ -716,7 +743,10 @@ __device__ void geometry_chunk(const Ctx& c, uint32_t chunk, uint32_t* sh) {
   }
   __syncthreads();
   uint32_t idx = sh[32] + sh[warp] + (uint32_t)__popc(ballot & lanemask_lt());
-  if (have) store_record(c, idx, r);
+  if (have) {
+    store_record(c, idx, r);
+    write_shade(c, idx, ch.draw, vid, iid, sw);
+  }
   count_tiles(c, r, have);
   __syncthreads();
 }
@@ -1423,12 +1453,47 @@ __device__ bool vis_check(const Ctx& c, uint32_t s) {
 }
 
 /* ordered mode: per-pixel in-order processing of the tile's bin, sorted by primitive */
+/* one triangle of an ordered tile's batch, as the pixel loop reads it from shared memory */
 struct BatchEntry {
-  Shade s;
+  Shade s;                 /* record, 1/w and varyings, pipeline and draw */
+  int64_t e[3];            /* edge functions at the centre of the tile's first pixel, minus their thresholds */
+  int32_t ex[3], ey[3];    /* edge steps per pixel in x (-dy * 256) and y (dx * 256) */
+  float zmin, zmax;
   uint32_t valid;
+  uint32_t fits;           /* every edge value over the tile fits in 32 bits */
+  uint32_t depth;          /* bit 0 test, bit 1 write, bits 2.. compare op */
+  uint32_t blend;          /* 0 none, 1 straight alpha (SRC_ALPHA, ONE_MINUS_SRC_ALPHA, ADD), 2 any other */
+  uint32_t write_mask;
+  uint32_t thr;            /* bit k: edge k's threshold is 1 */
 };
+static_assert(KZ_SORT_CAP * 8 + KZ_BATCH * sizeof(BatchEntry) <= KZ_DYN_SMEM,
+              "ordered tile raster: sort keys and batch fit the dynamic shared memory");
 
-__device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* smem, uint32_t s_index) {
+/* blend with SRC_ALPHA / ONE_MINUS_SRC_ALPHA and ADD for colour and alpha: the same operations as
+ * color_write's general path for these factors */
+__device__ __forceinline__ uint32_t blend_straight_alpha(uint32_t dst, const float col[4], const float* u8tab,
+                                                         uint32_t wm) {
+  float a = fminf(fmaxf(col[3], 0.0f), 1.0f);
+  float ia = fsub(1.0f, a);
+  uint32_t out = dst;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    if (!((wm >> i) & 1u)) continue;
+    float sv = i == 3 ? a : fminf(fmaxf(col[i], 0.0f), 1.0f);
+    float d = u8tab[(dst >> (8 * i)) & 0xFFu];
+    float r = ffma(sv, a, fmul(d, ia));
+    out = (out & ~(0xFFu << (8 * i))) | ((uint32_t)unorm8(r) << (8 * i));
+  }
+  return out;
+}
+
+/* PER: pixels per thread (1 for tiles up to 16x16, 4 for 32x32), a compile-time constant so that the
+ * tile's colour and depth stay in registers; the call handles the tile's pixels [base, base + PER *
+ * blockDim.x) (64x64 tiles take four calls).  The bin is sorted by primitive number; each batch of
+ * KZ_BATCH triangles is set up in shared memory, then every thread runs its pixels through the batch in
+ * order: coverage, depth test, fragment shader, depth write, blend.  `u8tab`: u8f(k) for k = 0..255. */
+template <int PER>
+__device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* smem, const float* u8tab, int base) {
   const KzSegment& seg = *c.seg;
   TileInfo ti;
   if (!tile_info(seg, t, ti)) return;
@@ -1438,7 +1503,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
     if (threadIdx.x == 0) atomicOr(&c.st->flags, KZ_STATUS_BIN_TOO_LARGE);
     return;
   }
-  int T = (int)seg.tile;
+  const int T = (int)seg.tile;
   unsigned long long* sk = reinterpret_cast<unsigned long long*>(smem);
   BatchEntry* batch = reinterpret_cast<BatchEntry*>(smem + KZ_SORT_CAP * 8);
   const KzTriRecord* recs = reinterpret_cast<const KzTriRecord*>(seg.records);
@@ -1470,20 +1535,26 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
       __syncthreads();
     }
   }
-  /* per-thread pixels (T*T / blockDim.x of them, at most 16) */
-  const int per = (T * T + blockDim.x - 1) / blockDim.x;
-  uint32_t colv[16];
-  float depv[16];
+  /* this thread's pixels: offsets in the tile and whether they lie in the framebuffer and render area */
   const bool has_color = seg.color != 0, has_depth = seg.depth != 0;
-  for (int q = 0; q < per; q++) {
-    int i = threadIdx.x + q * blockDim.x;
-    int32_t x = ti.ox + i % T, y = ti.oy + i / T;
+  int lx[PER], ly[PER];
+  bool in[PER];
+  uint32_t colv[PER];
+  float depv[PER];
+#pragma unroll
+  for (int q = 0; q < PER; q++) {
+    int i = base + (int)threadIdx.x + q * (int)blockDim.x;
+    lx[q] = i % T;
+    ly[q] = i / T;
+    int32_t x = ti.ox + lx[q], y = ti.oy + ly[q];
+    in[q] = i < T * T && x >= ti.x0 && x <= ti.x1 && y >= ti.y0 && y <= ti.y1;
     colv[q] = 0;
     depv[q] = 1.0f;
-    if (i >= T * T || x < ti.x0 || x > ti.x1 || y < ti.y0 || y > ti.y1) continue;
+    if (!in[q]) continue;
     if (has_color) colv[q] = to_rgba(clear_c ? seg.clear_color : *color_px(seg, x, y), seg.color_format);
     if (has_depth) depv[q] = clear_d ? seg.clear_depth : *depth_px(seg, x, y);
   }
+  const int64_t tpx = (int64_t)ti.ox * 256 + 128, tpy = (int64_t)ti.oy * 256 + 128;
   uint32_t frags = 0;
   for (uint32_t b0 = 0; b0 < ti.n; b0 += KZ_BATCH) {
     uint32_t nb = min((uint32_t)KZ_BATCH, ti.n - b0);
@@ -1493,37 +1564,91 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
       uint32_t ri = (uint32_t)key;
       const KzTriRecord r = recs[ri];
       BatchEntry& be = batch[threadIdx.x];
-      be.valid = shade_setup(c, r.g, 0, 0, (r.info >> 4) & 15u, be.s) ? 1u : 0u;
+      uint32_t sub = (r.info >> 4) & 15u;
+      if (sub == 0 && seg.shades) {
+        /* unclipped: the setup the geometry phase stored beside the record */
+        be.s.r = r;
+        be.s.draw = r.draw;
+        be.s.pipe = c.draws[r.draw].pipe;
+        const int nc = (int)c.pipes[be.s.pipe].num_varyings;
+        const float* src = reinterpret_cast<const float*>(seg.shades + (size_t)ri * seg.shade_stride);
+        for (int i = 0; i < 3; i++) {
+          be.s.iw[i] = __ldg(src + i);
+          for (int k = 0; k < nc; k++) be.s.a[i][k] = __ldg(src + 4 + i * nc + k);
+        }
+        be.valid = 1u;
+      } else {
+        be.valid = shade_setup(c, r.g, 0, 0, sub, be.s) ? 1u : 0u;
+      }
+      const KzDraw& bd = c.draws[r.draw];
+      const KzPipe& bp = c.pipes[bd.pipe];
+      be.zmin = bd.zmin;
+      be.zmax = bd.zmax;
+      be.depth = (bp.depth_test ? 1u : 0u) | (bp.depth_write ? 2u : 0u) | (bp.depth_compare << 2);
+      bool straight = bp.src_color == 6 && bp.dst_color == 7 && bp.color_op == 0 && bp.src_alpha == 6 &&
+                      bp.dst_alpha == 7 && bp.alpha_op == 0;
+      be.blend = bp.blend_enable ? (straight ? 1u : 2u) : 0u;
+      be.write_mask = bp.write_mask;
+      /* edge values at the tile's first pixel centre, from the record that shading uses */
+      Edges ed;
+      edges_of(be.s.r, ed);
+      bool fits = true;
+      uint32_t thr = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        be.e[k] = edge_at(ed, k, tpx, tpy) - ed.thr[k];
+        be.ex[k] = -ed.dy[k] * 256;
+        be.ey[k] = ed.dx[k] * 256;
+        thr |= (uint32_t)ed.thr[k] << k;
+        int64_t ae = be.e[k] < 0 ? -be.e[k] : be.e[k];
+        fits = fits && ae + ((int64_t)abs(be.ex[k]) + (int64_t)abs(be.ey[k])) * (T - 1) + 1 < 0x7FFFFFFFll;
+      }
+      be.thr = thr;
+      be.fits = fits ? 1u : 0u;
     }
     __syncthreads();
     for (uint32_t j = 0; j < nb; j++) {
       const BatchEntry& be = batch[j];
       if (!be.valid) continue;
-      const KzTriRecord& r = be.s.r;
-      int32_t bx0 = (int32_t)(r.bb0 & 0xFFFFu), by0 = (int32_t)(r.bb0 >> 16);
-      int32_t bx1 = (int32_t)(r.bb1 & 0xFFFFu), by1 = (int32_t)(r.bb1 >> 16);
-      const KzPipe& p = c.pipes[be.s.pipe];
-      const KzDraw& d = c.draws[be.s.draw];
-      for (int q = 0; q < per; q++) {
-        int i = threadIdx.x + q * blockDim.x;
-        if (i >= T * T) break;
-        int32_t x = ti.ox + i % T, y = ti.oy + i / T;
-        if (x < bx0 || x > bx1 || y < by0 || y > by1) continue;
-        if (x < ti.x0 || x > ti.x1 || y < ti.y0 || y > ti.y1) continue;
+#pragma unroll
+      for (int q = 0; q < PER; q++) {
+        if (!in[q]) continue;
         int64_t E[3];
-        if (!covers(r, x, y, E)) continue;
+        if (be.fits) {
+          /* the same integers in 32-bit arithmetic (bounded over the tile) */
+          int32_t e0 = (int32_t)be.e[0] + be.ex[0] * lx[q] + be.ey[0] * ly[q];
+          int32_t e1 = (int32_t)be.e[1] + be.ex[1] * lx[q] + be.ey[1] * ly[q];
+          int32_t e2 = (int32_t)be.e[2] + be.ex[2] * lx[q] + be.ey[2] * ly[q];
+          if ((e0 | e1 | e2) < 0) continue;
+          E[0] = e0;
+          E[1] = e1;
+          E[2] = e2;
+        } else {
+          int64_t e0 = be.e[0] + (int64_t)be.ex[0] * lx[q] + (int64_t)be.ey[0] * ly[q];
+          int64_t e1 = be.e[1] + (int64_t)be.ex[1] * lx[q] + (int64_t)be.ey[1] * ly[q];
+          int64_t e2 = be.e[2] + (int64_t)be.ex[2] * lx[q] + (int64_t)be.ey[2] * ly[q];
+          if ((e0 | e1 | e2) < 0) continue;
+          E[0] = e0;
+          E[1] = e1;
+          E[2] = e2;
+        }
+        E[0] += (int64_t)(be.thr & 1u);
+        E[1] += (int64_t)((be.thr >> 1) & 1u);
+        E[2] += (int64_t)(be.thr >> 2);
         frags++;
+        const KzTriRecord& r = be.s.r;
         float l1 = fmul(kz_i64_to_f32(E[1]), r.inv_s), l2 = fmul(kz_i64_to_f32(E[2]), r.inv_s);
         float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
-        z = fadd(fminf(fmaxf(z, d.zmin), d.zmax), 0.0f);
+        z = fadd(fminf(fmaxf(z, be.zmin), be.zmax), 0.0f);
+        const bool dtest = (be.depth & 1u) && has_depth;
+        if (dtest && !depth_cmp(be.depth >> 2, z, depv[q])) continue;
+        int32_t x = ti.ox + lx[q], y = ti.oy + ly[q];
         float col[4];
-        uint32_t discard = shade_pixel(c, be.s, x, y, E, z, col);
-        if (discard) continue;
-        if (p.depth_test && has_depth) {
-          if (!depth_cmp(p.depth_compare, z, depv[q])) continue;
-          if (p.depth_write) depv[q] = z;
-        }
-        if (has_color) colv[q] = color_write(p, colv[q], col);
+        if (shade_pixel(c, be.s, x, y, E, z, col)) continue;
+        if (dtest && (be.depth & 2u)) depv[q] = z;
+        if (!has_color) continue;
+        if (be.blend == 1u) colv[q] = blend_straight_alpha(colv[q], col, u8tab, be.write_mask);
+        else colv[q] = color_write(c.pipes[be.s.pipe], colv[q], col, u8tab);
       }
     }
   }
@@ -1531,19 +1656,25 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
     atomicAdd(&c.cnt->fragments, frags);
     atomicAdd(&c.st->fragments_lo, frags);
   }
-  for (int q = 0; q < per; q++) {
-    int i = threadIdx.x + q * blockDim.x;
-    if (i >= T * T) break;
-    int32_t x = ti.ox + i % T, y = ti.oy + i / T;
-    if (x < ti.x0 || x > ti.x1 || y < ti.y0 || y > ti.y1) continue;
+#pragma unroll
+  for (int q = 0; q < PER; q++) {
+    if (!in[q]) continue;
+    int32_t x = ti.ox + lx[q], y = ti.oy + ly[q];
     if (has_color) *color_px(seg, x, y) = from_rgba(colv[q], seg.color_format);
     if (has_depth) *depth_px(seg, x, y) = depv[q];
   }
-  (void)s_index;
 }
 
-__device__ void raster_tile(const Ctx& c, uint32_t t, unsigned char* smem, uint32_t s) {
-  raster_tile_ordered(c, t, smem, s);
+__device__ void raster_tile(const Ctx& c, uint32_t t, unsigned char* smem, const float* u8tab) {
+  const uint32_t T = c.seg->tile;
+  if (T <= 16) {
+    raster_tile_ordered<1>(c, t, smem, u8tab, 0);
+  } else {
+    for (int base = 0; base < (int)(T * T); base += 4 * KZ_THREADS) {
+      __syncthreads();
+      raster_tile_ordered<4>(c, t, smem, u8tab, base);
+    }
+  }
   __syncthreads();
   /* leave the tile counts at zero for the next segment */
   if (threadIdx.x == 0) reinterpret_cast<uint32_t*>(c.seg->tile_count)[t] = 0;
@@ -1630,10 +1761,12 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_bin(KzFrame f, uin
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 2) kz_k_raster(KzFrame f, uint32_t s) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float u8tab[256];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
+  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) u8tab[i] = u8f(i);
   uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) raster_tile(c, t, smem, s);
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) raster_tile(c, t, smem, u8tab);
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_vis_init(KzFrame f, uint32_t s) {
@@ -1679,6 +1812,8 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
   __shared__ uint32_t item;
   __shared__ uint32_t scan_sh[KZ_THREADS + 1];
   __shared__ uint32_t geo_sh[40];
+  __shared__ float u8tab[256];
+  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) u8tab[i] = u8f(i);
   KzStatus* st = reinterpret_cast<KzStatus*>(f.status);
   for (uint32_t s = f.first_segment; s < f.num_segments; s++) {
     Ctx c = make_ctx(f, s);
@@ -1738,7 +1873,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
     for (;;) {
       uint32_t t = grab(&c.cnt->tile_next, &item);
       if (t >= ntiles) break;
-      raster_tile(c, t, smem, s);
+      raster_tile(c, t, smem, u8tab);
     }
     if (!grid_barrier(st)) return;
   }
