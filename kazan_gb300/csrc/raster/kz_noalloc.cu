@@ -78,6 +78,19 @@ extern "C" __device__ uint32_t kz_fs(uint32_t, const KzFsIn* in, const uint8_t*,
   return 0;
 }
 
+extern "C" __device__ KzFsResult kz_fs_r8(uint32_t, const uint8_t*, uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3,
+                                          uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t,
+                                          uint32_t) {
+  KzFsResult r;
+  r.c[0] = __uint_as_float(v0);
+  r.c[1] = __uint_as_float(v1);
+  r.c[2] = __uint_as_float(v2);
+  r.c[3] = __uint_as_float(v3);
+  r.discard = 0;
+  r.pad[0] = r.pad[1] = r.pad[2] = 0;
+  return r;
+}
+
 /* writes the tables of one draw into the scratch and zeroes the counters (one block) */
 extern "C" __global__ void kz_k_noalloc_setup(KzDraw draw, KzPipe pipe, KzSegment seg, unsigned char* base,
                                               uint32_t tri_count) {

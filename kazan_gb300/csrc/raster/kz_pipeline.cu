@@ -30,6 +30,17 @@ extern "C" __device__ void kz_vs(uint32_t pipe, const KzDraw* draw, uint32_t vid
 extern "C" __device__ float4 kz_vs_pos(uint32_t pipe, const KzDraw* draw, uint32_t vid, uint32_t iid,
                                        const uint8_t* push);
 extern "C" __device__ uint32_t kz_fs(uint32_t pipe, const KzFsIn* in, const uint8_t* push, float* color);
+/* the fragment shader with inputs and outputs in registers, for interfaces of at most 8 varyings: varyings
+ * v0..v7, gl_FragCoord, gl_FrontFacing in; colour and the discard flag out (float bits in 32-bit words) */
+struct __align__(16) KzFsResult {
+  float c[4];
+  uint32_t discard;
+  uint32_t pad[3];
+};
+extern "C" __device__ KzFsResult kz_fs_r8(uint32_t pipe, const uint8_t* push, uint32_t v0, uint32_t v1, uint32_t v2,
+                                          uint32_t v3, uint32_t v4, uint32_t v5, uint32_t v6, uint32_t v7,
+                                          uint32_t fc0, uint32_t fc1, uint32_t fc2, uint32_t fc3, uint32_t front);
+
 /* gl_Position of the three vertices of one triangle in one call (push constants read once) */
 struct KzPos3 {
   float4 p[3];
@@ -406,9 +417,12 @@ __device__ bool shade_setup(const Ctx& c, uint32_t g, int32_t x, int32_t y, uint
   return shade_clipped(d, p, o, nc, x, y, sub, s);
 }
 
-/* interpolate varyings and run the fragment shader */
-__device__ uint32_t shade_pixel(const Ctx& c, const Shade& s, int32_t x, int32_t y, const int64_t E[3], float z,
-                                float col[4]) {
+/* interpolate varyings and run the fragment shader.  REGS: pass the inputs in registers (kz_fs_r8) when
+ * the interface has at most 8 varyings; otherwise through a KzFsIn in local memory (kz_fs), which costs
+ * fewer registers in kernels that are already at their register limit. */
+template <bool REGS>
+__device__ __forceinline__ uint32_t shade_pixel(const Ctx& c, const Shade& s, int32_t x, int32_t y, const int64_t E[3],
+                                                float z, float col[4]) {
   const KzPipe& p = c.pipes[s.pipe];
   const KzDraw& d = c.draws[s.draw];
   float l0 = fmul(kz_i64_to_f32(E[0]), s.r.inv_s);
@@ -416,22 +430,46 @@ __device__ uint32_t shade_pixel(const Ctx& c, const Shade& s, int32_t x, int32_t
   float l2 = fmul(kz_i64_to_f32(E[2]), s.r.inv_s);
   float q = ffma(l2, s.iw[2], ffma(l1, s.iw[1], fmul(l0, s.iw[0])));
   float rq = fdiv(1.0f, q);
+  const int nc = (int)p.num_varyings;
+  const float fx = fadd((float)x, 0.5f), fy = fadd((float)y, 0.5f);
+  const uint32_t front = (s.r.info >> 8) & 1u;
+  if (!p.has_fs) {
+    col[0] = col[1] = col[2] = col[3] = 0.0f;
+    return 0;
+  }
+  if (REGS && nc <= 8) {
+    uint32_t v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      float val = 0.0f;
+      if (k < nc) {
+        float num = ffma(l2, s.a[2][k], ffma(l1, s.a[1][k], fmul(l0, s.a[0][k])));
+        const bool flat = (p.flat_mask >> k) & 1u;
+        val = ((p.noperspective_mask >> k) & 1u) || flat ? num : fmul(num, rq);
+        if (flat) val = s.a[0][k];
+      }
+      v[k] = __float_as_uint(val);
+    }
+    const KzFsResult rr = kz_fs_r8(s.pipe, push_ptr(*c.f, d), v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7],
+                                   __float_as_uint(fx), __float_as_uint(fy), __float_as_uint(z), __float_as_uint(q),
+                                   front);
+    col[0] = rr.c[0];
+    col[1] = rr.c[1];
+    col[2] = rr.c[2];
+    col[3] = rr.c[3];
+    return rr.discard;
+  }
   KzFsIn in;
-  int nc = (int)p.num_varyings;
   for (int k = 0; k < nc; k++) {
     float num = ffma(l2, s.a[2][k], ffma(l1, s.a[1][k], fmul(l0, s.a[0][k])));
     in.var[k] = ((p.noperspective_mask >> k) & 1u) || ((p.flat_mask >> k) & 1u) ? num : fmul(num, rq);
     if ((p.flat_mask >> k) & 1u) in.var[k] = s.a[0][k];
   }
-  in.frag_coord[0] = fadd((float)x, 0.5f);
-  in.frag_coord[1] = fadd((float)y, 0.5f);
+  in.frag_coord[0] = fx;
+  in.frag_coord[1] = fy;
   in.frag_coord[2] = z;
   in.frag_coord[3] = q;
-  in.front_facing = (s.r.info >> 8) & 1u;
-  if (!p.has_fs) {
-    col[0] = col[1] = col[2] = col[3] = 0.0f;
-    return 0;
-  }
+  in.front_facing = front;
   return kz_fs(s.pipe, &in, push_ptr(*c.f, d), col);
 }
 
@@ -1422,7 +1460,7 @@ __device__ void vis_resolve_run(const Ctx& c, uint32_t item) {
       int64_t E[3];
       covers(s.r, x, y, E);
       float col[4];
-      shade_pixel(c, s, x, y, E, z, col);
+      shade_pixel<true>(c, s, x, y, E, z, col);
       const KzPipe& p = c.pipes[s.pipe];
       if (has_color) {
         uint32_t dst = clear_c ? seg.clear_color : *color_px(seg, x, y);
@@ -1644,7 +1682,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
         if (dtest && !depth_cmp(be.depth >> 2, z, depv[q])) continue;
         int32_t x = ti.ox + lx[q], y = ti.oy + ly[q];
         float col[4];
-        if (shade_pixel(c, be.s, x, y, E, z, col)) continue;
+        if (shade_pixel<false>(c, be.s, x, y, E, z, col)) continue;
         if (dtest && (be.depth & 2u)) depv[q] = z;
         if (!has_color) continue;
         if (be.blend == 1u) colv[q] = blend_straight_alpha(colv[q], col, u8tab, be.write_mask);

@@ -14,6 +14,9 @@
  *                                                                       vertices: push constants loaded once,
  *                                                                       three straight copies of the body
  *   .func (.b32 discard) kz_fs(pipe, KzFsIn* in, push, float* color)   fragment shader
+ *   .func (.b8[32] colour, discard) kz_fs_r8(pipe, push, v0..v7, fc0..fc3, front)  the same for
+ *                                                                       interfaces of at most 8 varyings,
+ *                                                                       inputs and outputs in registers
  *
  * The vertex functions fetch their own attributes: the pipeline's vertex input state (binding, format,
  * offset, stride, input rate) is compiled into direct loads from the draw's vertex buffers, so no
@@ -62,7 +65,7 @@ const char* cmp_name(uint32_t c) {
   return (c & ir::CmpUnordered) ? unord[k] : ord[k];
 }
 
-enum class Kind { VertexFull, VertexPos, VertexPos3, Fragment };
+enum class Kind { VertexFull, VertexPos, VertexPos3, Fragment, FragmentRegs };
 
 class Emitter {
  public:
@@ -169,7 +172,7 @@ class Emitter {
     auto R = [&](int32_t r) { return name[(size_t)r]; };
     auto L = [&](uint32_t l) { return "$" + pfx + "_L" + std::to_string(l); };
     char buf[160];
-    bool vertex = kind != Kind::Fragment;
+    bool vertex = kind != Kind::Fragment && kind != Kind::FragmentRegs;
     if (vertex) vertex_prologue(lay);
     for (const Inst& i : fn.code) {
       switch (i.op) {
@@ -198,6 +201,20 @@ class Emitter {
         case Op::LdIn:
           if (vertex) {
             vertex_load(lay, i.imm, i.ty, R(i.dst));
+            break;
+          }
+          if (kind == Kind::FragmentRegs) {
+            /* inputs arrive as scalar parameters: varyings 0..7, FragCoord, FrontFacing */
+            const char* t = i.ty == Ty::F32 ? "f32" : "b32";
+            if (i.imm < 32 && i.imm % 4 == 0)
+              std::snprintf(buf, sizeof buf, "ld.param.%s %s, [kz_fs_r8_v%u];", t, R(i.dst).c_str(), i.imm / 4);
+            else if (i.imm >= 64 && i.imm < 80 && i.imm % 4 == 0)
+              std::snprintf(buf, sizeof buf, "ld.param.%s %s, [kz_fs_r8_fc%u];", t, R(i.dst).c_str(), (i.imm - 64) / 4);
+            else if (i.imm == 80)
+              std::snprintf(buf, sizeof buf, "ld.param.%s %s, [kz_fs_r8_front];", t, R(i.dst).c_str());
+            else
+              std::snprintf(buf, sizeof buf, "mov.b32 %s, 0;", R(i.dst).c_str());
+            line(buf);
             break;
           }
           std::snprintf(buf, sizeof buf, "ld.%s %s, [%%kzin+%u];", i.ty == Ty::F32 ? "f32" : "u32", R(i.dst).c_str(),
@@ -232,6 +249,13 @@ class Emitter {
           if (fn.regs[(size_t)i.a] == Ty::Pred) {
             line("selp.u32 %kzt, 1, 0, " + v + ";");
             v = "%kzt";
+          }
+          if (kind == Kind::FragmentRegs) {
+            if (i.imm >= 16) break;
+            std::snprintf(buf, sizeof buf, "st.param.%s [func_retval0+%u], %s;",
+                          fn.regs[(size_t)i.a] == Ty::F32 ? "f32" : "b32", i.imm, v.c_str());
+            line(buf);
+            break;
           }
           if (kind == Kind::VertexPos)
             std::snprintf(buf, sizeof buf, "st.param.%s [func_retval0+%u], %s;",
@@ -310,12 +334,20 @@ class Emitter {
             line("mov.b32 %kzt, 0;");
             line("st.param.b32 [func_retval0], %kzt;");
           }
+          if (kind == Kind::FragmentRegs) {
+            line("mov.b32 %kzt, 0;");
+            line("st.param.b32 [func_retval0+16], %kzt;");
+          }
           line("ret;");
           break;
         case Op::Kill:
           if (kind == Kind::Fragment) {
             line("mov.b32 %kzt, 1;");
             line("st.param.b32 [func_retval0], %kzt;");
+          }
+          if (kind == Kind::FragmentRegs) {
+            line("mov.b32 %kzt, 1;");
+            line("st.param.b32 [func_retval0+16], %kzt;");
           }
           line("ret;");
           break;
@@ -329,6 +361,10 @@ class Emitter {
     if (kind == Kind::Fragment) {
       line("mov.b32 %kzt, 0;");
       line("st.param.b32 [func_retval0], %kzt;");
+    }
+    if (kind == Kind::FragmentRegs) {
+      line("mov.b32 %kzt, 0;");
+      line("st.param.b32 [func_retval0+16], %kzt;");
     }
     line("ret;");
   }
@@ -352,11 +388,17 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
       e.push_regs.clear();
       e.line("ret;");
     } else if (stages[p]) {
+      if (kind == Kind::FragmentRegs) /* colour components the shader does not write read as 0 */
+        for (uint32_t k = 0; k < 4; k++) e.line("st.param.b32 [func_retval0+" + std::to_string(4 * k) + "], 0;");
       e.body(stages[p]->fn, pfx, kind, p < layouts.size() ? &layouts[p] : nullptr);
     } else {
       if (kind == Kind::Fragment) {
         e.line("mov.b32 %kzt, 0;");
         e.line("st.param.b32 [func_retval0], %kzt;");
+      }
+      if (kind == Kind::FragmentRegs) {
+        for (uint32_t k = 0; k < 4; k++) e.line("st.param.b32 [func_retval0+" + std::to_string(4 * k) + "], 0;");
+        e.line("st.param.b32 [func_retval0+16], 0;");
       }
       e.line("ret;");
     }
@@ -369,6 +411,13 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
                   ".visible .func (.param .b32 func_retval0) %s(\n  .param .b32 %s_pipe,\n  .param .b64 %s_in,\n"
                   "  .param .b64 %s_push,\n  .param .b64 %s_out\n)\n{\n",
                   fname, fname, fname, fname, fname);
+  } else if (kind == Kind::FragmentRegs) {
+    std::string h = ".visible .func (.param .align 16 .b8 func_retval0[32]) " + std::string(fname) + "(\n  .param .b32 " +
+                    fname + "_pipe,\n  .param .b64 " + fname + "_push";
+    for (int k = 0; k < 8; k++) h += ",\n  .param .b32 " + std::string(fname) + "_v" + std::to_string(k);
+    for (int k = 0; k < 4; k++) h += ",\n  .param .b32 " + std::string(fname) + "_fc" + std::to_string(k);
+    h += ",\n  .param .b32 " + std::string(fname) + "_front\n)\n{\n";
+    std::snprintf(buf, sizeof buf, "%s", h.c_str());
   } else if (kind == Kind::VertexPos3) {
     std::snprintf(buf, sizeof buf,
                   ".visible .func (.param .align 16 .b8 func_retval0[48]) %s(\n  .param .b32 %s_pipe,\n"
@@ -398,6 +447,8 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
   s += buf;
   if (kind == Kind::Fragment) {
     std::snprintf(buf, sizeof buf, "  ld.param.u64 %%kzin, [%s_in];\n  ld.param.u64 %%kzout, [%s_out];\n", fname, fname);
+  } else if (kind == Kind::FragmentRegs) {
+    buf[0] = 0;
   } else if (kind == Kind::VertexPos3) {
     std::snprintf(buf, sizeof buf,
                   "  ld.param.u64 %%kzdraw, [%s_draw];\n  cvta.to.global.u64 %%kzdraw, %%kzdraw;\n"
@@ -425,6 +476,7 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
   if (stages.empty()) {
     s += "$" + std::string(fname) + "_p0:\n";
     if (kind == Kind::Fragment) s += "  mov.b32 %kzt, 0;\n  st.param.b32 [func_retval0], %kzt;\n";
+    if (kind == Kind::FragmentRegs) s += "  st.param.b32 [func_retval0+16], 0;\n";
     s += "  ret;\n";
   }
   s += bodies;
@@ -441,6 +493,7 @@ std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vec
   s += function_text("kz_vs_pos", Kind::VertexPos, vs, layouts);
   s += function_text("kz_vs_pos3", Kind::VertexPos3, vs, layouts);
   s += function_text("kz_fs", Kind::Fragment, fs, {});
+  s += function_text("kz_fs_r8", Kind::FragmentRegs, fs, {});
   return s;
 }
 
