@@ -128,6 +128,13 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
     layouts.push_back(l);
   }
   std::string ptx = ptx::module_text(vs, fs, layouts);
+  /* pipelines that differ only in fixed-function state (viewport, depth, blend: data in KzPipe) give the
+   * same PTX and share one linked image */
+  auto same = dev->kernel_sets_by_ptx.find(ptx);
+  if (same != dev->kernel_sets_by_ptx.end()) {
+    dev->kernel_sets[key] = same->second;
+    return same->second;
+  }
   std::vector<char> cubin;
   err = ptx::link(ptx, obj.data(), obj.size(), cubin);
   if (!err.empty()) return nullptr;
@@ -171,6 +178,7 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
   ks->geometry_blocks = geo_sm * dev->pd->sm_count;
   if (options().trace) log_error("kernel set linked: %zu pipelines, persistent grid %d", pipes.size(), ks->persistent_blocks);
   dev->kernel_sets[key] = ks;
+  dev->kernel_sets_by_ptx[ptx] = ks;
   return ks;
 }
 
@@ -483,11 +491,14 @@ static void VKAPI_CALL kzDestroyDevice(VkDevice device, const VkAllocationCallba
   if (!dev) return;
   cudaSetDevice(dev->pd->cuda_device);
   cudaStreamSynchronize(dev->queue.stream);
-  for (auto& kv : dev->kernel_sets) {
+  for (auto& kv : dev->kernel_sets_by_ptx) {
     if (kv.second->lib) cudaLibraryUnload(kv.second->lib);
     delete kv.second;
   }
+  dev->kernel_sets.clear();
+  dev->kernel_sets_by_ptx.clear();
   for (cudaEvent_t e : dev->event_pool) cudaEventDestroy(e);
+  for (cudaEvent_t e : dev->timing_pool) cudaEventDestroy(e);
   cudaStreamDestroy(dev->queue.stream);
   cudaStreamDestroy(dev->capture_stream);
   delete dev;

@@ -293,7 +293,8 @@ struct Device : Dispatchable {
   Queue queue;
   cudaStream_t capture_stream = nullptr;
   std::recursive_mutex mu;
-  std::map<std::vector<uint64_t>, KernelSet*> kernel_sets;
+  std::map<std::vector<uint64_t>, KernelSet*> kernel_sets;        /* by pipeline ids (not owning) */
+  std::unordered_map<std::string, KernelSet*> kernel_sets_by_ptx; /* by generated PTX (owning) */
   std::vector<cudaEvent_t> event_pool;
   std::vector<cudaEvent_t> timing_pool; /* events with timing enabled */
 };
