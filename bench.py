@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-perdraw", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use --mode / --tile as given)")
     return ap.parse_args()
 
 
@@ -207,9 +208,25 @@ def main():
     from kazan_gb300 import render
     scene, cfg = make_scene(args)
     r = render.Renderer()
-    # the timed command buffer launches its kernels at submit with timing events around each launch
-    r.drv.set_option("kernel_timing", 1)
     run = render.SceneRun(r, scene, host_visible=False, mode=args.mode, tile=args.tile)
+    mode, tile, tuning = args.mode, args.tile, None
+    if not args.no_tune:
+        # launch schedule and tile side from the autotuner (measured here unless cached for this workload)
+        from kazan_gb300 import autotune
+        gpu = r.props.deviceName.decode(errors="replace")
+        sig = autotune.signature(gpu, scene.blend, len(scene.draws), scene.triangles, scene.width, scene.height)
+        best, table = autotune.Tuner().choose(sig, autotune.scene_timer(run),
+                                              autotune.candidates(ordered=scene.blend))
+        mode, tile = best.mode, best.tile
+        tuning = {"signature": sig, "chosen": {"mode": mode, "tile": tile},
+                  "ms": None if table is None else {"%s/%d" % (c.mode, c.tile): round(v, 4) for c, v in table.items()}}
+    # the timed command buffer launches its kernels at submit with timing events around each launch
+    r.drv.set_option("mode", mode)
+    r.drv.set_option("tile", tile)
+    r.drv.set_option("kernel_timing", 1)
+    old_cb = run.cb
+    run.cb = run.record()
+    r.free_command_buffer(old_cb)
     r.drv.set_option("kernel_timing", 0)
     stream = torch.cuda.ExternalStream(r.stream())
 
@@ -253,7 +270,7 @@ def main():
            "unit": "Mtris/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
            "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32+int64 (16.8 fixed-point edges)", "data": "synthetic (seeded scene generator)",
-           "config": dict(cfg, tile=st.tile, mode=args.mode, triangles=tris,
+           "config": dict(cfg, tile=st.tile, mode=mode, triangles=tris,
                           l2="inputs larger than L2 (%.0f MB vertex+index per step)" % (
                               (scene.vertices.nbytes + (scene.indices.nbytes if scene.indices is not None else 0))
                               / 1e6), parallelism="replicas" if world > 1 else "single GPU"),
@@ -265,7 +282,7 @@ def main():
                         "bytes_formula": kformula,
                         "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"},
            "kernels": kernels,
-           "clocks": ck, "gpu_launches": int(sum(n for _, n in ktimes.values()))}
+           "clocks": ck, "gpu_launches": int(sum(n for _, n in ktimes.values())), "autotune": tuning}
     if not args.no_perdraw:
         pd = render.SceneRun(r, scene, host_visible=False, mode="perdraw", tile=args.tile)
         pd.submit()
@@ -285,7 +302,7 @@ def main():
         out["batched_vs_per_draw"] = round(out["value"] / world / out["per_draw"]["value"], 2)
     if not args.no_e2e:
         import numpy as np
-        e2 = render.SceneRun(r, scene, host_visible=True, mode=args.mode, tile=args.tile, keep_mapped=True)
+        e2 = render.SceneRun(r, scene, host_visible=True, mode=mode, tile=tile, keep_mapped=True)
         e2.submit()
         p = r.map(e2.color)
         nbytes = e2.color.pitch * scene.height

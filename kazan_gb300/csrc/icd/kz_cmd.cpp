@@ -140,9 +140,22 @@ VkResult VKAPI_CALL kzCreateCommandPool(VkDevice device, const VkCommandPoolCrea
   return VK_SUCCESS;
 }
 
+namespace kz {
+static void process_completions(Queue* q, bool block_all);
+}
+
+/* finish and retire every submission on the device's queue, so that none refers to a command buffer that
+ * is about to be freed or re-recorded */
+static void drain_queue(Device* dev) {
+  std::lock_guard<std::recursive_mutex> lock(dev->mu);
+  cudaSetDevice(dev->pd->cuda_device);
+  process_completions(&dev->queue, true);
+  cudaStreamSynchronize(dev->queue.stream);
+}
+
 static void destroy_cb(CommandBuffer* cb) {
   if (cb->low) {
-    cudaStreamSynchronize(cb->dev->queue.stream);
+    drain_queue(cb->dev);
     free_lowered(cb->low.get());
   }
   delete cb;
@@ -157,7 +170,7 @@ void VKAPI_CALL kzDestroyCommandPool(VkDevice, VkCommandPool pool_h, const VkAll
 
 static void reset_cb(CommandBuffer* cb) {
   if (cb->low) {
-    cudaStreamSynchronize(cb->dev->queue.stream);
+    drain_queue(cb->dev);
     free_lowered(cb->low.get());
     cb->low.reset();
   }
