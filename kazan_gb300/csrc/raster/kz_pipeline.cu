@@ -1367,8 +1367,8 @@ __device__ void vis_geometry_warps(const Ctx& c, unsigned char* smem, uint32_t w
  * Lane b < KZ_JOB_BLOCKS first evaluates the three edge functions at block b's first pixel centre and
  * drops the block when, for some edge, even the block's largest value (at the corner the edge's
  * gradient points to) is below the threshold.  The warp then walks the remaining blocks: each lane adds
- * its fixed offset within the block to the block's edge values (the same int64 integers as evaluating the
- * edge functions at the pixel directly). */
+ * its fixed offset within the block to the block's edge values (the same integers as evaluating the edge
+ * functions at the pixel directly; in 32-bit arithmetic when every value over the box fits). */
 __device__ uint32_t vis_large_job(const Ctx& c, uint2 job, int lane) {
   const KzSegment& seg = *c.seg;
   const KzTriRecord r = load_record(seg, job.x);
@@ -1379,7 +1379,7 @@ __device__ uint32_t vis_large_job(const Ctx& c, uint2 job, int lane) {
   int32_t bx0 = (int32_t)(r.bb0 & 0xFFFFu), by0 = (int32_t)(r.bb0 >> 16);
   int32_t bx1 = (int32_t)(r.bb1 & 0xFFFFu), by1 = (int32_t)(r.bb1 >> 16);
   uint32_t nbx, nb = box_blocks(r, nbx);
-  /* block test, one block per lane */
+  /* block test, one block per lane; E* hold the edge values minus their thresholds (covered iff all >= 0) */
   uint32_t b = job.y + (uint32_t)lane;
   bool live = lane < KZ_JOB_BLOCKS && b < nb;
   int32_t ox = 0, oy = 0;
@@ -1389,26 +1389,72 @@ __device__ uint32_t vis_large_job(const Ctx& c, uint2 job, int lane) {
     ox = bx0 + (int32_t)(b - row * nbx) * 8;
     oy = by0 + (int32_t)row * 8;
     int64_t px = (int64_t)ox * 256 + 128, py = (int64_t)oy * 256 + 128;
-    E0 = edge_at(e, 0, px, py);
-    E1 = edge_at(e, 1, px, py);
-    E2 = edge_at(e, 2, px, py);
+    E0 = edge_at(e, 0, px, py) - e.thr[0];
+    E1 = edge_at(e, 1, px, py) - e.thr[1];
+    E2 = edge_at(e, 2, px, py) - e.thr[2];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       int64_t ek = k == 0 ? E0 : (k == 1 ? E1 : E2);
       int64_t mx = ek + (e.dy[k] < 0 ? -(int64_t)e.dy[k] * (7 * 256) : 0) + (e.dx[k] > 0 ? (int64_t)e.dx[k] * (7 * 256) : 0);
-      live = live && mx >= e.thr[k];
+      live = live && mx >= 0;
     }
   }
   uint32_t mask = __ballot_sync(0xFFFFFFFFu, live);
+  /* every edge value over the box (blocks reach 7 pixels past its last row and column) fits in 32 bits? */
+  bool fits = true;
+  {
+    const int64_t wx = (int64_t)(bx1 - bx0) + 8, wy = (int64_t)(by1 - by0) + 8;
+    const int64_t px = (int64_t)bx0 * 256 + 128, py = (int64_t)by0 * 256 + 128;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      int64_t ek = edge_at(e, k, px, py);
+      int64_t ae = ek < 0 ? -ek : ek;
+      fits = fits && ae + (int64_t)abs(e.dy[k]) * 256 * wx + (int64_t)abs(e.dx[k]) * 256 * wy + 2 < 0x7FFFFFFFll;
+    }
+  }
   /* this lane's offset inside a block: column lx, rows ly and ly + 4 */
-  int lx = lane & 7, ly = lane >> 3;
+  const int lx = lane & 7, ly = lane >> 3;
+  uint32_t frags = 0;
+  if (fits) {
+    int32_t inc[3], half[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      inc[k] = e.dx[k] * (ly * 256) - e.dy[k] * (lx * 256);
+      half[k] = e.dx[k] * (4 * 256);
+    }
+    const int32_t th1 = (int32_t)e.thr[1], th2 = (int32_t)e.thr[2];
+    while (mask) {
+      int src = __ffs(mask) - 1;
+      mask &= mask - 1;
+      int32_t bxo = __shfl_sync(0xFFFFFFFFu, ox, src), byo = __shfl_sync(0xFFFFFFFFu, oy, src);
+      int32_t e0 = __shfl_sync(0xFFFFFFFFu, (int32_t)E0, src) + inc[0];
+      int32_t e1 = __shfl_sync(0xFFFFFFFFu, (int32_t)E1, src) + inc[1];
+      int32_t e2 = __shfl_sync(0xFFFFFFFFu, (int32_t)E2, src) + inc[2];
+      int32_t x = bxo + lx;
+      if (x > bx1) continue;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        int32_t y = byo + ly + 4 * h;
+        if (y <= by1 && (e0 | e1 | e2) >= 0) {
+          frags++;
+          float l1 = fmul(__int2float_rn(e1 + th1), r.inv_s), l2 = fmul(__int2float_rn(e2 + th2), r.inv_s);
+          float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
+          z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
+          vis_store(seg, vis_key(seg.vis_key, z, r.g), x, y);
+        }
+        e0 += half[0];
+        e1 += half[1];
+        e2 += half[2];
+      }
+    }
+    return frags;
+  }
   int64_t inc[3], half[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     inc[k] = (int64_t)e.dx[k] * (ly * 256) - (int64_t)e.dy[k] * (lx * 256);
     half[k] = (int64_t)e.dx[k] * (4 * 256);
   }
-  uint32_t frags = 0;
   while (mask) {
     int src = __ffs(mask) - 1;
     mask &= mask - 1;
@@ -1421,9 +1467,12 @@ __device__ uint32_t vis_large_job(const Ctx& c, uint2 job, int lane) {
 #pragma unroll
     for (int h = 0; h < 2; h++) {
       int32_t y = byo + ly + 4 * h;
-      if (y <= by1 && e0 >= e.thr[0] && e1 >= e.thr[1] && e2 >= e.thr[2]) {
+      if (y <= by1 && (e0 | e1 | e2) >= 0) {
         frags++;
-        vis_store(seg, frag_key(seg, r, zmin, zmax, kz_i64_to_f32(e1), kz_i64_to_f32(e2)), x, y);
+        float l1 = fmul(kz_i64_to_f32(e1 + e.thr[1]), r.inv_s), l2 = fmul(kz_i64_to_f32(e2 + e.thr[2]), r.inv_s);
+        float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
+        z = fadd(fminf(fmaxf(z, zmin), zmax), 0.0f);
+        vis_store(seg, vis_key(seg.vis_key, z, r.g), x, y);
       }
       e0 += half[0];
       e1 += half[1];
