@@ -1109,8 +1109,15 @@ __device__ __forceinline__ VEntry vertex_entry(const KzDraw& d, float4 clip) {
     code |= (c[1] < -c[3]) ? 8u : 0u;
     code |= (c[2] < 0.0f) ? 16u : 0u;
     code |= (c[2] > c[3]) ? 32u : 0u;
-#pragma unroll
-    for (int plane = 0; plane < 6; plane++) code |= plane_dist(c, plane) < 0.0f ? (64u << plane) : 0u;
+    /* outside a clip plane: plane_dist(c, p) < 0 for near, far and the four guard-band planes.  The
+     * signs of those float sums equal these comparisons (4w is an exact scaling, and a rounded sum of two
+     * floats has the sign of the exact sum), so the codes are the same */
+    const float gw = fmul(KZ_GUARD_BAND, c[3]);
+    code |= (code & 48u) << 2; /* near z < 0, far z > w */
+    code |= (c[0] < -gw) ? 256u : 0u;
+    code |= (c[0] > gw) ? 512u : 0u;
+    code |= (c[1] < -gw) ? 1024u : 0u;
+    code |= (c[1] > gw) ? 2048u : 0u;
   }
   e.X = e.Y = 0;
   e.z = 0.0f;
@@ -1160,6 +1167,12 @@ __device__ __forceinline__ int vis_triangle(const Ctx& c, const KzDraw& d, const
 }
 
 #define KZ_GEO_SMEM (KZ_THREADS * (96 + 1))
+#define KZ_MAGIC_MAX 128 /* pixel pairs per row of a warp-rasterised box: ceil(w / 2) with w * h <= KZ_WARP_PX */
+
+/* table[pw] = floor((2^32 - 1) / pw) + 1 for pw in [2, KZ_MAGIC_MAX] (0 for 0 and 1), filled by the block */
+__device__ __forceinline__ void fill_magic(uint32_t* table) {
+  for (uint32_t i = threadIdx.x; i <= KZ_MAGIC_MAX; i += blockDim.x) table[i] = i > 1 ? 0xFFFFFFFFu / i + 1u : 0u;
+}
 
 /* what the warp raster keeps of a record, in shared memory (one slot per lane) */
 struct WarpTri {
@@ -1205,7 +1218,8 @@ __device__ __forceinline__ void warp_fragment32(const KzSegment& seg, const Warp
  * one marked at the highest position <= l.  `slots`: this warp's 32 WarpTri, `owner`: its 32-entry table,
  * both in shared memory. */
 __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const KzTriRecord& r, bool have, float zmin,
-                                                    float zmax, WarpTri* slots, uint8_t* owner) {
+                                                    float zmax, WarpTri* slots, uint8_t* owner,
+                                                    const uint32_t* magic_tab) {
   const int lane = threadIdx.x & 31;
   uint32_t n = 0;
   if (have) {
@@ -1229,8 +1243,9 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
     t.oy = (int32_t)(r.bb0 >> 16);
     t.w = (r.bb1 & 0xFFFFu) - (r.bb0 & 0xFFFFu) + 1;
     t.pw = (t.w + 1) >> 1;
-    /* floor((2^32 - 1) / pw) + 1: the rounded-up reciprocal for every pw > 1 (exact when pw is a power of 2) */
-    t.magic = t.pw > 1 ? 0xFFFFFFFFu / t.pw + 1u : 0u;
+    /* floor((2^32 - 1) / pw) + 1: the rounded-up reciprocal for every pw > 1 (exact when pw is a power of 2);
+     * from the block's table for the widths warp-rasterised boxes have */
+    t.magic = t.pw <= KZ_MAGIC_MAX ? magic_tab[t.pw] : 0xFFFFFFFFu / t.pw + 1u;
     t.start = start;
     int64_t px = (int64_t)t.ox * 256 + 128, py = (int64_t)t.oy * 256 + 128;
     uint32_t thr = 0;
@@ -1321,7 +1336,7 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
  * the warp then emits its large triangles together and rasterises the small and medium ones together
  * (vis_warp_raster).  Returns the lane's fragment count. */
 __device__ __forceinline__ uint32_t vis_geometry_warp(const Ctx& c, uint32_t chunk, uint32_t sub, WarpTri* slots,
-                                                      uint8_t* owner) {
+                                                      uint8_t* owner, const uint32_t* magic_tab) {
   const KzChunk ch = reinterpret_cast<const KzChunk*>(c.f->chunks)[chunk];
   if (sub * 32 >= ch.count) return 0;
   const KzDraw& d = c.draws[ch.draw];
@@ -1342,20 +1357,22 @@ __device__ __forceinline__ uint32_t vis_geometry_warp(const Ctx& c, uint32_t chu
     kind = vis_triangle(c, d, p, ch.draw, d.prim_base + local, e, r, frags);
   }
   vis_emit_large_warp(c, r, kind == 2);
-  frags += vis_warp_raster(*c.seg, r, kind == 1, d.zmin, d.zmax, slots, owner);
+  frags += vis_warp_raster(*c.seg, r, kind == 1, d.zmin, d.zmax, slots, owner, magic_tab);
   return frags;
 }
 
 /* the geometry of a segment by warps: warp w of `warps` takes the 32-triangle groups w, w + warps, ...
  * (8 groups per chunk), then adds its fragment count to the statistics.  `smem`: 8 warps x 32 WarpTri,
  * then 8 warps x 32 owner bytes (KZ_GEO_SMEM bytes). */
-__device__ void vis_geometry_warps(const Ctx& c, unsigned char* smem, uint32_t w, uint32_t warps) {
+__device__ void vis_geometry_warps(const Ctx& c, unsigned char* smem, const uint32_t* magic_tab, uint32_t w,
+                                   uint32_t warps) {
   const uint32_t wib = threadIdx.x >> 5;
   WarpTri* slots = reinterpret_cast<WarpTri*>(smem) + wib * 32;
   uint8_t* owner = smem + KZ_THREADS * sizeof(WarpTri) + wib * 32;
   const uint32_t groups = c.seg->num_chunks * 8;
   uint32_t frags = 0;
-  for (uint32_t i = w; i < groups; i += warps) frags += vis_geometry_warp(c, c.seg->first_chunk + i / 8, i % 8, slots, owner);
+  for (uint32_t i = w; i < groups; i += warps)
+    frags += vis_geometry_warp(c, c.seg->first_chunk + i / 8, i % 8, slots, owner, magic_tab);
   for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
   if ((threadIdx.x & 31) == 0 && frags) {
     atomicAdd(&c.cnt->fragments, frags);
@@ -1864,9 +1881,13 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_vis_init(KzFrame f
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_geometry(KzFrame f, uint32_t s) {
   __shared__ __align__(16) unsigned char slots[KZ_GEO_SMEM];
+  __shared__ uint32_t magic_tab[KZ_MAGIC_MAX + 1];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
-  vis_geometry_warps(c, slots, blockIdx.x * (KZ_THREADS / 32) + (threadIdx.x >> 5), gridDim.x * (KZ_THREADS / 32));
+  fill_magic(magic_tab);
+  __syncthreads();
+  vis_geometry_warps(c, slots, magic_tab, blockIdx.x * (KZ_THREADS / 32) + (threadIdx.x >> 5),
+                     gridDim.x * (KZ_THREADS / 32));
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_vis_large(KzFrame f, uint32_t s) {
@@ -1900,7 +1921,9 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
   __shared__ uint32_t scan_sh[KZ_THREADS + 1];
   __shared__ uint32_t geo_sh[40];
   __shared__ float u8tab[256];
+  __shared__ uint32_t magic_tab[KZ_MAGIC_MAX + 1];
   for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) u8tab[i] = u8f(i);
+  fill_magic(magic_tab);
   KzStatus* st = reinterpret_cast<KzStatus*>(f.status);
   for (uint32_t s = f.first_segment; s < f.num_segments; s++) {
     Ctx c = make_ctx(f, s);
@@ -1908,7 +1931,8 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
     if (c.seg->mode == KZ_MODE_VISIBILITY) {
       vis_init_range(*c.seg, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
       if (!grid_barrier(st)) return;
-      vis_geometry_warps(c, smem, blockIdx.x * (KZ_THREADS / 32) + (threadIdx.x >> 5), gridDim.x * (KZ_THREADS / 32));
+      vis_geometry_warps(c, smem, magic_tab, blockIdx.x * (KZ_THREADS / 32) + (threadIdx.x >> 5),
+                         gridDim.x * (KZ_THREADS / 32));
       if (!grid_barrier(st)) return;
       if (!vis_check(c, s)) break;
       uint32_t njobs = c.cnt->pair_count;
