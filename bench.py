@@ -302,7 +302,10 @@ def main():
         out["batched_vs_per_draw"] = round(out["value"] / world / out["per_draw"]["value"], 2)
     if not args.no_e2e:
         import numpy as np
-        e2 = render.SceneRun(r, scene, host_visible=True, mode=mode, tile=tile, keep_mapped=True)
+        # vertex/index buffers and the colour image host-visible (uploaded / downloaded by every submission);
+        # depth is scratch of the step and stays device-local
+        e2 = render.SceneRun(r, scene, host_visible=True, mode=mode, tile=tile, keep_mapped=True,
+                             depth_host_visible=False)
         e2.submit()
         p = r.map(e2.color)
         nbytes = e2.color.pitch * scene.height

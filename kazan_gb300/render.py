@@ -324,7 +324,7 @@ class Renderer:
 class SceneRun:
     """GPU resources and a recorded command buffer for one scene."""
 
-    def __init__(self, r, scene, host_visible=False, mode=None, tile=None, keep_mapped=False):
+    def __init__(self, r, scene, host_visible=False, mode=None, tile=None, keep_mapped=False, depth_host_visible=None):
         self.r, self.scene = r, scene
         d = r.drv
         if mode is not None:
@@ -340,7 +340,8 @@ class SceneRun:
         self.color = r.create_image(scene.width, scene.height, vk.FORMAT_R8G8B8A8_UNORM,
                                     vk.IMAGE_USAGE_COLOR_ATTACHMENT, host_visible)
         self.depth = r.create_image(scene.width, scene.height, vk.FORMAT_D32_SFLOAT,
-                                    vk.IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT, host_visible)
+                                    vk.IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT,
+                                    host_visible if depth_host_visible is None else depth_host_visible)
         self.rp = r.render_pass(vk.FORMAT_R8G8B8A8_UNORM, True)
         self.fb = r.framebuffer(self.rp, [self.color.view, self.depth.view], scene.width, scene.height)
         self.layout = r.pipeline_layout(64 if scene.shader == "lambert" else 0)
