@@ -937,16 +937,39 @@ static cudaEvent_t pool_event(Device* dev) {
   return e;
 }
 
+/* Host-visible memory the command buffer reads is uploaded from its pinned shadow on the device's copy
+ * stream, after the queue's last use of that memory; the queue waits for the uploads before it launches.
+ * So the upload of one submission overlaps the kernels of the submissions before it whenever they use
+ * other memory (double-buffered inputs), and never overwrites memory they still read or write. */
 static void enqueue(CommandBuffer* cb, cudaStream_t st) {
   Lowered& low = *cb->low;
-  for (DeviceMemory* m : low.reads)
-    if (m->host && m->mapped) cudaMemcpyAsync(m->dptr, m->host, (size_t)m->size, cudaMemcpyHostToDevice, st);
+  Device* dev = cb->dev;
+  bool uploaded = false;
+  for (DeviceMemory* m : low.reads) {
+    if (!(m->host && m->mapped)) continue;
+    if (m->last_use) cudaStreamWaitEvent(dev->copy_stream, m->last_use, 0);
+    cudaMemcpyAsync(m->dptr, m->host, (size_t)m->size, cudaMemcpyHostToDevice, dev->copy_stream);
+    uploaded = true;
+  }
+  if (uploaded) {
+    cudaEvent_t ev = pool_event(dev);
+    cudaEventRecord(ev, dev->copy_stream);
+    cudaStreamWaitEvent(st, ev, 0);
+    dev->event_pool.push_back(ev); /* a recorded event can be re-recorded once the wait is enqueued */
+  }
   if (low.exec) cudaGraphLaunch(low.exec, st);
   else launch_ops(cb, st, 0, false, low.timed ? &cb->timing : nullptr);
   for (DeviceMemory* m : low.writes) {
     if (m->host && m->mapped) cudaMemcpyAsync(m->host, m->dptr, (size_t)m->size, cudaMemcpyDeviceToHost, st);
     else m->device_newer = true;
   }
+  auto mark = [&](DeviceMemory* m) {
+    if (!m) return;
+    if (!m->last_use) cudaEventCreateWithFlags(&m->last_use, cudaEventDisableTiming);
+    cudaEventRecord(m->last_use, st);
+  };
+  for (DeviceMemory* m : low.reads) mark(m);
+  for (DeviceMemory* m : low.writes) mark(m);
 }
 
 /* grow the scratch after an overflow and run the command buffer again from the failing segment;

@@ -477,7 +477,8 @@ static VkResult VKAPI_CALL kzCreateDevice(VkPhysicalDevice physicalDevice, const
   dev->pd = pd;
   dev->queue.dev = dev;
   if (cudaStreamCreateWithFlags(&dev->queue.stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&dev->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaStreamCreateWithFlags(&dev->capture_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&dev->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     delete dev;
     return VK_ERROR_INITIALIZATION_FAILED;
@@ -501,6 +502,7 @@ static void VKAPI_CALL kzDestroyDevice(VkDevice device, const VkAllocationCallba
   for (cudaEvent_t e : dev->timing_pool) cudaEventDestroy(e);
   cudaStreamDestroy(dev->queue.stream);
   cudaStreamDestroy(dev->capture_stream);
+  cudaStreamDestroy(dev->copy_stream);
   delete dev;
 }
 
@@ -554,9 +556,11 @@ static void VKAPI_CALL kzFreeMemory(VkDevice device, VkDeviceMemory memory, cons
   if (!m) return;
   Device* dev = from_handle<Device>(device);
   cudaSetDevice(dev->pd->cuda_device);
+  cudaStreamSynchronize(dev->copy_stream);
   cudaStreamSynchronize(dev->queue.stream);
   device_free(m->dptr);
   if (m->host) cudaFreeHost(m->host);
+  if (m->last_use) cudaEventDestroy(m->last_use);
   delete m;
 }
 

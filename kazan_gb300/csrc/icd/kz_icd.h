@@ -62,6 +62,7 @@ struct DeviceMemory {
   char* host = nullptr;        /* pinned host shadow behind vkMapMemory (type 0 only) */
   bool mapped = false;
   bool device_newer = false;   /* the GPU wrote it since the host shadow was last refreshed */
+  cudaEvent_t last_use = nullptr; /* recorded on the queue stream after the last submission that used it */
 };
 
 struct Buffer {
@@ -292,6 +293,7 @@ struct Device : Dispatchable {
   PhysicalDevice* pd = nullptr;
   Queue queue;
   cudaStream_t capture_stream = nullptr;
+  cudaStream_t copy_stream = nullptr;   /* uploads of host-visible memory (a copy engine beside the queue) */
   std::recursive_mutex mu;
   std::map<std::vector<uint64_t>, KernelSet*> kernel_sets;        /* by pipeline ids (not owning) */
   std::unordered_map<std::string, KernelSet*> kernel_sets_by_ptx; /* by generated PTX (owning) */
