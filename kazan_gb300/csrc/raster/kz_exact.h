@@ -1,5 +1,5 @@
 /*
- * kz_exact.h - exact integer helpers shared by the pipeline kernels and their CPU unit test.
+ * kz_exact.h - exact integer helpers shared by the pipeline kernels and their CPU test (tests/test_exact.py).
  *
  * kz_i64_to_f32: round-to-nearest-even conversion of a 64-bit integer to binary32, computed with integer
  * operations only.  It returns the same bits as the IEEE conversion (C's (float)x under the default
@@ -23,31 +23,6 @@ KZ_HD int kz_clz64(uint64_t a) {
 #else
   return a ? __builtin_clzll(a) : 64;
 #endif
-}
-
-KZ_HD uint32_t kz_u32_to_f32_bits(uint32_t a) {
-  /* exact for a < 2^24; rounds to nearest even above */
-  if (a == 0) return 0;
-  int msb = 31 - kz_clz64((uint64_t)a) + 32;
-  msb -= 32;
-  uint32_t mant, exp;
-  if (msb <= 23) {
-    mant = a << (23 - msb);
-    exp = (uint32_t)msb;
-  } else {
-    int shift = msb - 23;
-    uint32_t m = a >> shift;
-    uint32_t rem = a & ((1u << shift) - 1u);
-    uint32_t half = 1u << (shift - 1);
-    if (rem > half || (rem == half && (m & 1u))) m++;
-    if (m == (1u << 24)) {
-      m >>= 1;
-      msb++;
-    }
-    mant = m;
-    exp = (uint32_t)msb;
-  }
-  return ((exp + 127u) << 23) | (mant & 0x7FFFFFu);
 }
 
 KZ_HD uint32_t kz_i64_to_f32_bits(int64_t v) {
