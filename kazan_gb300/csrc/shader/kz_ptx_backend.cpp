@@ -499,9 +499,12 @@ std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vec
 
 std::string link(const std::string& ptx, const void* object, size_t object_size, std::vector<char>& cubin) {
   nvJitLinkHandle h = nullptr;
-  const char* opts[] = {"-arch=sm_103a", "-O3"};
+  /* shader functions are called from kernels launched with at most 64 registers per thread (the geometry
+   * kernel runs 4 blocks of 256 per SM); the linker rejects a callee that needs more than its caller's
+   * limit, so the shader PTX is compiled within 64 registers (a heavy shader spills instead) */
+  const char* opts[] = {"-arch=sm_103a", "-O3", "-maxrregcount=64"};
   std::string err;
-  if (nvJitLinkCreate(&h, 2, opts) != NVJITLINK_SUCCESS) return "nvJitLinkCreate failed";
+  if (nvJitLinkCreate(&h, 3, opts) != NVJITLINK_SUCCESS) return "nvJitLinkCreate failed";
   auto log = [&](const char* what) {
     size_t n = 0;
     nvJitLinkGetErrorLogSize(h, &n);

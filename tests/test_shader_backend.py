@@ -80,3 +80,51 @@ def test_link_pipeline_set(built):
     ptx = shader.emit_ptx([(cvs, cfs), (lvs, lfs), (cvs, tfs), (cvs, None)], list(_layouts()) + list(_layouts()))
     img = shader.link(ptx)
     assert len(img) > 100_000 and img[:4] == b"\x7fELF"
+
+
+def _heavy_vs():
+    """a vertex shader with many live values: two push-constant matrices and a chain of products"""
+    from kazan_gb300.spirv_asm import (Module, CapShader, DecOffset, DecColMajor, DecMatrixStride, DecBlock,
+                                       SCPushConstant, SCInput, SCOutput, OpAccessChain, OpLoad, OpStore,
+                                       OpMatrixTimesVector, OpFAdd, OpFMul, ExecVertex, _per_vertex, _io,
+                                       _begin_main, _end_main)
+    m = Module()
+    m.capability(CapShader)
+    f32 = m.f32()
+    v4 = m.vec(f32, 4)
+    m4 = m.mat(v4, 4)
+    blk = m.struct(m4, m4)
+    for i in range(2):
+        m.member_decorate(blk, i, DecOffset, 64 * i)
+        m.member_decorate(blk, i, DecColMajor)
+        m.member_decorate(blk, i, DecMatrixStride, 16)
+    m.decorate(blk, DecBlock)
+    pc = m.variable(SCPushConstant, m.ptr(SCPushConstant, blk))
+    pv = _per_vertex(m)
+    in_pos = _io(m, SCInput, v4, 0)
+    in_col = _io(m, SCInput, v4, 1)
+    out_col = _io(m, SCOutput, v4, 0)
+    fn = _begin_main(m)
+    a = m.res(OpLoad, m4, m.res(OpAccessChain, m.ptr(SCPushConstant, m4), pc, m.ci(0)))
+    b = m.res(OpLoad, m4, m.res(OpAccessChain, m.ptr(SCPushConstant, m4), pc, m.ci(1)))
+    p = m.res(OpLoad, v4, in_pos)
+    q = [m.res(OpMatrixTimesVector, v4, a, p), m.res(OpMatrixTimesVector, v4, b, p)]
+    for i in range(6):
+        q.append(m.res(OpMatrixTimesVector, v4, a if i % 2 else b, m.res(OpFAdd, v4, q[-1], q[-2])))
+    acc = q[0]
+    for v in q[1:]:
+        acc = m.res(OpFMul, v4, acc, v)
+    m.op(OpStore, m.res(OpAccessChain, m.ptr(SCOutput, v4), pv, m.ci(0)), acc)
+    m.op(OpStore, out_col, m.res(OpLoad, v4, in_col))
+    _end_main(m)
+    m.entry(ExecVertex, fn, "main", [pc, pv, in_pos, in_col, out_col])
+    return m.to_words()
+
+
+def test_register_heavy_shader_links(built):
+    """shader functions are compiled within the kernels' 64-register limit, so a heavy vertex shader (whose
+    three-vertex function would need more) still links, spilling instead of failing"""
+    vs = shader.Shader(_heavy_vs(), shader.VERTEX)
+    fs = shader.Shader(spirv_asm.color_fs(), shader.FRAGMENT)
+    img = shader.link(shader.emit_ptx([(vs, fs)], [_layouts()[0]]))
+    assert img[:4] == b"\x7fELF"
