@@ -37,6 +37,7 @@ typedef struct KzShaderInfo {
   uint32_t writes_position, writes_color, discards;
   uint32_t push_bytes;          /* bytes of the push-constant block read */
   uint32_t ir_instructions, ir_registers;
+  uint32_t color_passthrough;   /* fragment: colour component k = input varying k (k = 0..3), nothing else */
 } KzShaderInfo;
 
 /* Translate one entry point.  stage: 0 vertex or 4 fragment.  spec_ids/spec_values: specialisation

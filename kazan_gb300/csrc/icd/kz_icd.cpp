@@ -971,6 +971,7 @@ static VkResult create_graphics_pipeline(const VkGraphicsPipelineCreateInfo& ci,
     kp.flat_mask = fif.flat_slots;
     kp.noperspective_mask = fif.noperspective_slots;
     kp.fs_discards = fif.discards;
+    kp.fs_passthrough = ir::color_passthrough(p->fs->fn) ? 1u : 0u;
     kp.has_fs = 1;
     if (!fif.writes_color) kp.write_mask = 0;
   }

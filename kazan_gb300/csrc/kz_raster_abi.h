@@ -101,6 +101,8 @@ typedef struct KzPipe {
   uint32_t fs_discards;
   uint32_t has_fs;
   float blend_const[4];
+  uint32_t fs_passthrough;    /* the fragment shader only copies varyings 0..3 to colour components 0..3 */
+  uint32_t pad;
 } KzPipe;
 
 /* one recorded draw (instances expanded by the kernels) */

@@ -437,6 +437,18 @@ __device__ __forceinline__ uint32_t shade_pixel(const Ctx& c, const Shade& s, in
     col[0] = col[1] = col[2] = col[3] = 0.0f;
     return 0;
   }
+  if (p.fs_passthrough) {
+    /* the shader only copies varyings 0..3 to the colour: the same values without the call */
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      float num = ffma(l2, s.a[2][k], ffma(l1, s.a[1][k], fmul(l0, s.a[0][k])));
+      const bool flat = (p.flat_mask >> k) & 1u;
+      float val = ((p.noperspective_mask >> k) & 1u) || flat ? num : fmul(num, rq);
+      if (flat) val = s.a[0][k];
+      col[k] = val;
+    }
+    return 0;
+  }
   if (REGS && nc <= 8) {
     uint32_t v[8];
 #pragma unroll

@@ -67,6 +67,7 @@ extern "C" KZ_API void kzShaderInfo(const void* shader, KzShaderInfo* out) {
   out->discards = i.discards;
   out->push_bytes = i.push_bytes;
   out->ir_instructions = (uint32_t)s->fn.code.size();
+  out->color_passthrough = i.stage == kz::ir::Stage::Fragment && kz::ir::color_passthrough(s->fn) ? 1u : 0u;
   out->ir_registers = (uint32_t)s->fn.regs.size();
 }
 

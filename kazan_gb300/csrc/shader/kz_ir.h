@@ -98,6 +98,10 @@ std::string translate_spirv(const uint32_t* words, size_t count, Stage stage, co
  * returns the input byte offsets (LdIn imm) that are live */
 std::vector<uint32_t> live_inputs(const Function& fn, uint32_t out_lo, uint32_t out_hi);
 
+/* a fragment shader whose only effect is colour component k = input varying k for k = 0..3 (no other
+ * instruction than loads of those inputs, the four stores and the return) */
+bool color_passthrough(const Function& fn);
+
 }  // namespace ir
 }  // namespace kz
 

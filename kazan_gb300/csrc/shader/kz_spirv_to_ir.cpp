@@ -1504,5 +1504,40 @@ std::vector<uint32_t> live_inputs(const Function& fn, uint32_t out_lo, uint32_t 
   return offs;
 }
 
+/* the pipeline kernels write the interpolated varyings directly for such a shader, with the same values
+ * the call would return */
+bool color_passthrough(const Function& fn) {
+  /* straight-line code only (labels but no branches): follow each register to the input word it holds */
+  std::vector<int64_t> held(fn.regs.size(), -1);
+  uint32_t stored = 0;
+  for (const Inst& i : fn.code) {
+    switch (i.op) {
+      case Op::LdIn:
+        if (i.dst < 0) return false;
+        held[(size_t)i.dst] = (i.ty == Ty::F32 && i.imm < 16 && i.imm % 4 == 0) ? (int64_t)i.imm : -1;
+        break;
+      case Op::Mov:
+        if (i.dst < 0 || i.a < 0) return false;
+        held[(size_t)i.dst] = (i.ty == Ty::F32 && fn.regs[(size_t)i.a] == Ty::F32) ? held[(size_t)i.a] : -1;
+        break;
+      case Op::Const:
+        if (i.dst < 0) return false;
+        held[(size_t)i.dst] = -1;
+        break;
+      case Op::StOut:
+        if (i.imm >= 16 || i.imm % 4 != 0 || i.a < 0 || held[(size_t)i.a] != (int64_t)i.imm) return false;
+        stored |= 1u << (i.imm / 4);
+        break;
+      case Op::Label:
+        break;
+      case Op::Ret: /* what follows is unreachable */
+        return stored == 0xFu;
+      default:
+        return false;
+    }
+  }
+  return stored == 0xFu;
+}
+
 }  // namespace ir
 }  // namespace kz

@@ -15,7 +15,7 @@ class KzShaderInfo(ctypes.Structure):
     _fields_ = [(n, c_uint32) for n in ("stage", "input_locations", "pos_input_locations", "output_slots",
                                         "input_slots", "flat_slots", "noperspective_slots", "writes_position",
                                         "writes_color", "discards", "push_bytes", "ir_instructions",
-                                        "ir_registers")]
+                                        "ir_registers", "color_passthrough")]
 
 
 class KzVertexInputLayout(ctypes.Structure):

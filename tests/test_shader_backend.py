@@ -48,6 +48,9 @@ def test_workload_shader_interfaces(built):
     assert lfs["input_slots"] == 0x7 and lfs["writes_color"]
     tfs = shader.Shader(spirv_asm.threshold_fs(), shader.FRAGMENT).info()
     assert tfs["discards"] == 1
+    # only the colour shader is a pure copy of varyings 0..3 to the colour (the kernels skip its call)
+    assert cfs["color_passthrough"] == 1
+    assert lfs["color_passthrough"] == 0 and tfs["color_passthrough"] == 0 and cvs["color_passthrough"] == 0
 
 
 def test_wrong_stage_entry_point_is_rejected(built):
