@@ -596,14 +596,17 @@ static void upload_tables(Lowered& low) {
   size_t o_chunks = align_up(o_pipes + low.pipes.size() * sizeof(KzPipe), 256);
   size_t o_segs = align_up(o_chunks + low.chunks.size() * sizeof(KzChunk), 256);
   size_t o_push = align_up(o_segs + low.segments.size() * sizeof(KzSegment), 256);
+  size_t o_lut = align_up(o_push + low.push.size(), 256);
   std::vector<char> host(low.tables_bytes, 0);
+  if (!low.draw_lut.empty())
+    std::memcpy(host.data() + o_lut, low.draw_lut.data(), low.draw_lut.size() * sizeof(uint32_t));
   if (!low.draws.empty()) std::memcpy(host.data() + o_draws, low.draws.data(), low.draws.size() * sizeof(KzDraw));
   if (!low.pipes.empty()) std::memcpy(host.data() + o_pipes, low.pipes.data(), low.pipes.size() * sizeof(KzPipe));
   if (!low.chunks.empty()) std::memcpy(host.data() + o_chunks, low.chunks.data(), low.chunks.size() * sizeof(KzChunk));
   if (!low.segments.empty())
     std::memcpy(host.data() + o_segs, low.segments.data(), low.segments.size() * sizeof(KzSegment));
   if (!low.push.empty()) std::memcpy(host.data() + o_push, low.push.data(), low.push.size());
-  cudaMemcpy(low.d_tables, host.data(), o_push + low.push.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(low.d_tables, host.data(), o_lut + low.draw_lut.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
 }
 
 static uint32_t grid_cap(Device* dev) { return (uint32_t)std::max(1, dev->pd->sm_count) * 8u; }
@@ -849,12 +852,25 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   uint64_t pair_cap = rec_cap * 4 + max_tiles * 16 + (1u << 18);
   rec_cap = std::min<uint64_t>(rec_cap, 0xFFFFFFF0ull);
   pair_cap = std::min<uint64_t>(pair_cap, 0xFFFFFFF0ull);
-  /* device tables: draws | pipes | chunks | segments | push, then counters and status */
+  /* per segment, the draw holding every 256th primitive (shading finds a primitive's draw from it) */
+  low.draw_lut.clear();
+  low.draw_lut_offset.assign(low.segments.size(), 0);
+  for (size_t i = 0; i < low.segments.size(); i++) {
+    const KzSegment& sg = low.segments[i];
+    low.draw_lut_offset[i] = low.draw_lut.size();
+    uint32_t d = sg.first_draw;
+    for (uint64_t g = 0; g < sg.num_prims; g += 256) {
+      while (d + 1 < sg.first_draw + sg.num_draws && low.draws[d + 1].prim_base <= g) d++;
+      low.draw_lut.push_back(d);
+    }
+  }
+  /* device tables: draws | pipes | chunks | segments | push | draw lookup, then counters and status */
   size_t o_pipes = align_up(low.draws.size() * sizeof(KzDraw), 256);
   size_t o_chunks = align_up(o_pipes + low.pipes.size() * sizeof(KzPipe), 256);
   size_t o_segs = align_up(o_chunks + low.chunks.size() * sizeof(KzChunk), 256);
   size_t o_push = align_up(o_segs + low.segments.size() * sizeof(KzSegment), 256);
-  size_t o_counters = align_up(o_push + low.push.size(), 256);
+  size_t o_lut = align_up(o_push + low.push.size(), 256);
+  size_t o_counters = align_up(o_lut + low.draw_lut.size() * sizeof(uint32_t), 256);
   size_t o_status = align_up(o_counters + low.segments.size() * sizeof(KzSegCounters), 256);
   low.tables_bytes = o_status + sizeof(KzStatus);
   void* p = nullptr;
@@ -880,6 +896,8 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
     s.tile_offset = (uint64_t)(uintptr_t)(low.d_tiles + low.max_tiles);
     s.tile_cursor = (uint64_t)(uintptr_t)(low.d_tiles + 2 * (size_t)low.max_tiles + 1);
     s.counters = (uint64_t)(uintptr_t)(low.d_counters + i);
+    s.draw_lut = s.num_prims ? (uint64_t)(uintptr_t)(low.d_tables + o_lut + low.draw_lut_offset[i] * sizeof(uint32_t))
+                             : 0;
     s.vis = s.mode == KZ_MODE_VISIBILITY ? (uint64_t)(uintptr_t)low.d_vis : 0;
   }
   r = size_scratch(dev, low, (uint32_t)rec_cap, (uint32_t)pair_cap);

@@ -207,6 +207,8 @@ struct Lowered {
   std::vector<KzChunk> chunks;
   std::vector<KzSegment> segments;
   std::vector<uint8_t> push;
+  std::vector<uint32_t> draw_lut;          /* all segments' draw lookup tables, back to back */
+  std::vector<size_t> draw_lut_offset;     /* per segment: first entry in draw_lut */
   struct LOp {
     OpKind kind;
     uint32_t seg_begin = 0, seg_end = 0;  /* Pass: segments [begin, end); others: segments before it */

@@ -191,6 +191,7 @@ typedef struct KzSegment {
   uint64_t shades;           /* ordered mode: per record, the shading setup of an unclipped triangle:
                                 float 1/w[3], pad, then varyings (divided by w unless flat/noperspective)
                                 [3][num_varyings] */
+  uint64_t draw_lut;         /* u32 per 256 primitives: the draw holding primitive 256 i (0: search) */
 } KzSegment;
 
 /* status words written by the kernels (one per submission) */

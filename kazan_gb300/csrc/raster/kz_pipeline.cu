@@ -398,7 +398,14 @@ __device__ __forceinline__ bool shade_direct(const KzDraw& d, const KzPipe& p, c
  * when the primitive was clipped, or by `sub` when it is known: sub = clip sub-index, 0 = any). */
 __device__ bool shade_setup(const Ctx& c, uint32_t g, int32_t x, int32_t y, uint32_t sub, Shade& s) {
   const KzSegment& seg = *c.seg;
-  uint32_t di = find_draw(c.draws, seg.first_draw, seg.num_draws, g);
+  uint32_t di;
+  if (seg.draw_lut) {
+    /* the draw holding primitive 256 (g / 256), then forward to the draw holding g */
+    di = __ldg(reinterpret_cast<const uint32_t*>(seg.draw_lut) + (g >> 8));
+    while (di + 1 < seg.first_draw + seg.num_draws && c.draws[di + 1].prim_base <= g) di++;
+  } else {
+    di = find_draw(c.draws, seg.first_draw, seg.num_draws, g);
+  }
   const KzDraw& d = c.draws[di];
   const KzPipe& p = c.pipes[d.pipe];
   uint32_t vid[3], iid;
