@@ -935,7 +935,7 @@ __device__ __forceinline__ float* depth_px(const KzSegment& seg, int32_t x, int3
 
 #define KZ_SMALL_PX 32      /* clipped sub-triangles with boxes of at most this many pixels are rasterised by
                                their geometry thread */
-#define KZ_WARP_PX 256      /* unclipped triangles with boxes of at most this many pixels are rasterised by
+#define KZ_WARP_PX 192      /* unclipped triangles with boxes of at most this many pixels are rasterised by
                                their geometry warp (vis_warp_raster); larger ones become jobs */
 #define KZ_JOB_BLOCKS 16    /* 8x8 pixel blocks per large-triangle job */
 
@@ -1186,7 +1186,8 @@ __device__ __forceinline__ int vis_triangle(const Ctx& c, const KzDraw& d, const
 }
 
 #define KZ_GEO_SMEM (KZ_THREADS * (96 + 1))
-#define KZ_MAGIC_MAX 128 /* pixel pairs per row of a warp-rasterised box: ceil(w / 2) with w * h <= KZ_WARP_PX */
+#define KZ_MAGIC_MAX 128 /* at least the pixel pairs per row of a warp-rasterised box: ceil(w / 2), w * h <= KZ_WARP_PX */
+static_assert((KZ_WARP_PX + 1) / 2 <= KZ_MAGIC_MAX, "the divisor table covers every warp-rasterised box width");
 
 /* table[pw] = floor((2^32 - 1) / pw) + 1 for pw in [2, KZ_MAGIC_MAX] (0 for 0 and 1), filled by the block */
 __device__ __forceinline__ void fill_magic(uint32_t* table) {
