@@ -124,6 +124,15 @@ class Translator {
   uint32_t entry_id_ = 0;
   std::vector<uint32_t> interface_ids_;
   uint32_t cur_block_ = 0;
+  /* function calls are inlined: each function's body [begin, end) in m_.insns, and the frames of the
+   * calls being translated (where the callee returns to, and the registers of its result) */
+  std::unordered_map<uint32_t, std::pair<size_t, size_t>> fn_ranges_;
+  struct Frame {
+    uint32_t ret_label = 0;
+    Val result;
+    bool has_result = false;
+  };
+  std::vector<Frame> frames_;
 
   bool fail(const std::string& s) {
     if (err_.empty()) err_ = s;
@@ -305,6 +314,8 @@ class Translator {
 
   /* ---- function body ---- */
   bool translate_entry();
+  void prescan_phis(size_t begin, size_t end);
+  bool inline_call(const Insn& in);
   bool do_insn(const Insn& in);
   bool branch_to(uint32_t target);
   bool load(const Place& p, Val& v);
@@ -1365,10 +1376,24 @@ bool Translator::do_insn(const Insn& in) {
       return true;
     }
     case OpReturn: {
+      if (!frames_.empty()) { /* end of an inlined call */
+        bra(frames_.back().ret_label);
+        return true;
+      }
       finish_outputs();
       Inst i;
       i.op = Op::Ret;
       fn_.emit(i);
+      return true;
+    }
+    case OpReturnValue: {
+      if (frames_.empty()) return fail("OpReturnValue in the entry point");
+      Frame& f = frames_.back();
+      Val* v = val(o[0]);
+      if (!v) return false;
+      for (size_t k = 0; k < f.result.regs.size() && k < v->regs.size(); k++)
+        mov(reg_ty(f.result.regs[k]), f.result.regs[k], v->regs[k]);
+      bra(f.ret_label);
       return true;
     }
     case OpKill: {
@@ -1379,14 +1404,94 @@ bool Translator::do_insn(const Insn& in) {
       return true;
     }
     case OpUnreachable: {
+      if (!frames_.empty()) {
+        bra(frames_.back().ret_label);
+        return true;
+      }
       Inst i;
       i.op = Op::Ret;
       fn_.emit(i);
       return true;
     }
-    case OpFunctionCall: return fail("function calls are not supported yet (inline helper functions)");
+    case OpFunctionCall: return inline_call(in);
     default: return fail(std::string("unsupported instruction ") + opcode_name(in.opcode));
   }
+}
+
+/* phis of the blocks in [begin, end): result registers up front, incoming edges recorded per block */
+void Translator::prescan_phis(size_t begin, size_t end) {
+  uint32_t block = 0;
+  for (size_t i = begin; i < end; i++) {
+    const Insn& in = m_.insns[i];
+    if (in.opcode == OpLabel) {
+      block = in.ops[0];
+      phis_.erase(block);
+    }
+    if (in.opcode == OpPhi) {
+      PhiInfo ph;
+      ph.type = in.ops[0];
+      ph.result = in.ops[1];
+      for (size_t k = 2; k + 1 < in.ops.size(); k += 2) ph.incoming.push_back({in.ops[k], in.ops[k + 1]});
+      std::vector<Ty> tys;
+      flat_types(ph.type, tys);
+      Val v;
+      v.type = ph.type;
+      for (Ty t : tys) v.regs.push_back(fn_.reg(t));
+      vals_[ph.result] = v;
+      phis_[block].push_back(ph);
+    }
+  }
+}
+
+/* OpFunctionCall: the callee's body is translated in place.  Its parameters name the arguments (pointer
+ * arguments name the same variable), its labels and phi registers are fresh for this call, and its returns
+ * become moves into the call's result registers and a branch past the body.  Shaders cannot recurse. */
+bool Translator::inline_call(const Insn& in) {
+  const auto& o = in.ops;
+  if (o.size() < 3) return fail("malformed OpFunctionCall");
+  auto fr = fn_ranges_.find(o[2]);
+  if (fr == fn_ranges_.end()) return fail("call of an unknown function %" + std::to_string(o[2]));
+  if (frames_.size() >= 32) return fail("function calls nested deeper than 32 (recursion is not allowed)");
+  const size_t begin = fr->second.first, end = fr->second.second;
+  Frame f;
+  f.ret_label = fn_.label();
+  if (ty(o[0]).kind != TypeInfo::Void) {
+    std::vector<Ty> tys;
+    flat_types(o[0], tys);
+    f.result.type = o[0];
+    for (Ty t : tys) f.result.regs.push_back(fn_.reg(t));
+    f.has_result = true;
+  }
+  size_t arg = 3;
+  for (size_t i = begin; i < end; i++) {
+    const Insn& p = m_.insns[i];
+    if (p.opcode == OpLabel) labels_.erase(p.ops[0]);
+    if (p.opcode != OpFunctionParameter) continue;
+    if (arg >= o.size()) return fail("OpFunctionCall with too few arguments");
+    uint32_t a = o[arg++];
+    auto pl = places_.find(a);
+    if (pl != places_.end()) {
+      places_[p.ops[1]] = pl->second;
+    } else {
+      Val* v = val(a);
+      if (!v) return false;
+      vals_[p.ops[1]] = *v;
+    }
+  }
+  prescan_phis(begin, end);
+  const uint32_t caller_block = cur_block_;
+  frames_.push_back(f);
+  for (size_t i = begin; i < end; i++) {
+    const Insn& b = m_.insns[i];
+    if (b.opcode == OpFunctionParameter) continue;
+    if (!do_insn(b)) return false;
+  }
+  Frame done = frames_.back();
+  frames_.pop_back();
+  label(done.ret_label);
+  cur_block_ = caller_block;
+  if (done.has_result) vals_[o[1]] = done.result;
+  return true;
 }
 
 bool Translator::translate_entry() {
@@ -1420,25 +1525,15 @@ bool Translator::translate_entry() {
     for (const Slot& s : kv.second.slots)
       if (s.reg >= 0) mov(reg_ty(s.reg), s.reg, konst(reg_ty(s.reg), 0));
   }
-  /* phis: result registers up front, incoming edges recorded per block */
-  uint32_t block = 0;
-  for (size_t i = begin; i < end; i++) {
+  /* every function's body, for inlining calls */
+  for (size_t i = 0; i < m_.insns.size(); i++) {
     const Insn& in = m_.insns[i];
-    if (in.opcode == OpLabel) block = in.ops[0];
-    if (in.opcode == OpPhi) {
-      PhiInfo ph;
-      ph.type = in.ops[0];
-      ph.result = in.ops[1];
-      for (size_t k = 2; k + 1 < in.ops.size(); k += 2) ph.incoming.push_back({in.ops[k], in.ops[k + 1]});
-      std::vector<Ty> tys;
-      flat_types(ph.type, tys);
-      Val v;
-      v.type = ph.type;
-      for (Ty t : tys) v.regs.push_back(fn_.reg(t));
-      vals_[ph.result] = v;
-      phis_[block].push_back(ph);
-    }
+    if (in.opcode != OpFunction || in.ops.size() < 2) continue;
+    size_t j = i + 1;
+    while (j < m_.insns.size() && m_.insns[j].opcode != OpFunctionEnd) j++;
+    fn_ranges_[in.ops[1]] = {i + 1, j};
   }
+  prescan_phis(begin, end);
   for (size_t i = begin; i < end; i++) {
     const Insn& in = m_.insns[i];
     if (in.opcode == OpFunctionParameter) return fail("entry point with parameters");

@@ -88,6 +88,7 @@ class Scene:
     clear_color: tuple = (0.0, 0.0, 0.0, 1.0)
     clear_depth: float = 1.0
     fs_words: Optional[np.ndarray] = field(default=None, repr=False)  # overrides the default fragment shader
+    vs_words: Optional[np.ndarray] = field(default=None, repr=False)  # overrides the default vertex shader
 
     @property
     def triangles(self):
@@ -107,6 +108,8 @@ class Scene:
             vs, fs = spirv_asm.lambert_vs(), spirv_asm.lambert_fs()
         if self.fs_words is not None:
             fs = self.fs_words
+        if self.vs_words is not None:
+            vs = self.vs_words
         return vs, fs
 
     def algorithmic_bytes(self):

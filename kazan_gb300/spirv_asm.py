@@ -39,6 +39,8 @@ OpConstantComposite = 44
 OpSpecConstant = 50
 OpFunction = 54
 OpFunctionEnd = 56
+OpFunctionParameter = 55
+OpFunctionCall = 57
 OpVariable = 59
 OpLoad = 61
 OpStore = 62
@@ -74,6 +76,7 @@ OpBranch = 249
 OpBranchConditional = 250
 OpKill = 252
 OpReturn = 253
+OpReturnValue = 254
 
 # enumerants
 CapShader = 1
@@ -270,6 +273,23 @@ def _begin_main(m):
 
 def _end_main(m):
     m.op(OpReturn)
+    m._ins(m.functions, OpFunctionEnd, ())
+
+
+def begin_function(m, ret_type, param_types):
+    """a helper function: returns (function id, parameter ids); its first block is open"""
+    fn = m.new_id()
+    m._ins(m.functions, OpFunction, (ret_type, fn, 0, m.fn_type(ret_type, *param_types)))
+    params = []
+    for t in param_types:
+        pid = m.new_id()
+        m._ins(m.functions, OpFunctionParameter, (t, pid))
+        params.append(pid)
+    m.op(OpLabel, m.new_id())
+    return fn, params
+
+
+def end_function(m):
     m._ins(m.functions, OpFunctionEnd, ())
 
 

@@ -114,3 +114,16 @@ def test_double_buffered_submissions_in_flight(renderer):
         for s, r in zip(sc, runs):
             color, depth = r.read()
             assert _oracle_equal(s, color, depth)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["batched", "persistent", "perdraw"])
+def test_shaders_with_function_calls(renderer, mode):
+    """shaders whose helpers are inlined by the translator render exactly what the call-free shaders do"""
+    import dataclasses
+    import call_shaders
+    soup = dataclasses.replace(CASES["soup"], fs_words=call_shaders.color_fs_calls())
+    lam = dataclasses.replace(CASES["batched"], vs_words=call_shaders.lambert_vs_calls())
+    for scene in (soup, lam):
+        color, depth, stats = _render(renderer, scene, mode, 16)
+        _check(scene, color, depth, stats)

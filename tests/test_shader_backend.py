@@ -131,3 +131,16 @@ def test_register_heavy_shader_links(built):
     fs = shader.Shader(spirv_asm.color_fs(), shader.FRAGMENT)
     img = shader.link(shader.emit_ptx([(vs, fs)], [_layouts()[0]]))
     assert img[:4] == b"\x7fELF"
+
+
+def test_function_calls_are_inlined(built):
+    """helper functions (value and pointer parameters, returns from two branches, four call sites of the same
+    function) translate, keep the interfaces of the call-free shaders and link"""
+    import call_shaders
+    fs = shader.Shader(call_shaders.color_fs_calls(), shader.FRAGMENT)
+    vs = shader.Shader(call_shaders.lambert_vs_calls(), shader.VERTEX)
+    fi, vi = fs.info(), vs.info()
+    assert fi["input_slots"] == 0xF and fi["writes_color"] and not fi["discards"]
+    assert vi["input_locations"] == 0b11 and vi["pos_input_locations"] == 0b1 and vi["push_bytes"] == 64
+    img = shader.link(shader.emit_ptx([(vs, fs)], [_layouts()[1]]))
+    assert img[:4] == b"\x7fELF"
