@@ -81,6 +81,10 @@ struct Place {
   uint32_t type = 0;
   uint32_t first = 0;
   uint32_t push_byte = 0; /* unused: push slots carry their own offsets */
+  /* one index known only at run time: element dyn of dyn_count, each dyn_stride slots, starts at slot
+   * first + dyn * dyn_stride (constant indices after it are already in `first`) */
+  int32_t dyn = -1;
+  uint32_t dyn_stride = 0, dyn_count = 0;
 };
 
 struct Val {
@@ -711,6 +715,32 @@ bool Translator::layout_interface(uint32_t var_id, Var& v) {
 }
 
 bool Translator::load(const Place& p, Val& v) {
+  if (p.dyn >= 0) {
+    /* run-time index: load every candidate element and select the one the index names (an index out of
+     * range reads element 0) */
+    Place e = p;
+    e.dyn = -1;
+    Val acc;
+    if (!load(e, acc)) return false;
+    for (uint32_t k = 1; k < p.dyn_count; k++) {
+      e.first = p.first + k * p.dyn_stride;
+      Val cand;
+      if (!load(e, cand)) return false;
+      int32_t hit = op2(Op::SetpU, Ty::Pred, p.dyn, konst(Ty::B32, k), CmpEq);
+      for (size_t c = 0; c < acc.regs.size(); c++) {
+        Ty t = reg_ty(acc.regs[c]);
+        if (t == Ty::Pred) {
+          acc.regs[c] = op2(Op::POr, Ty::Pred, op2(Op::PAnd, Ty::Pred, hit, cand.regs[c]),
+                            op2(Op::PAnd, Ty::Pred, op1(Op::PNot, Ty::Pred, hit), acc.regs[c]));
+        } else {
+          acc.regs[c] = op3(Op::Selp, t, cand.regs[c], acc.regs[c], hit);
+        }
+      }
+    }
+    v = acc;
+    v.type = p.type;
+    return true;
+  }
   Var& var = vars_[p.var];
   std::vector<Ty> tys;
   flat_types(p.type, tys);
@@ -769,6 +799,30 @@ bool Translator::load(const Place& p, Val& v) {
 
 bool Translator::store(const Place& p, const Val& v) {
   Var& var = vars_[p.var];
+  if (p.dyn >= 0) {
+    /* run-time index: every candidate element keeps its value unless the index names it */
+    for (uint32_t e = 0; e < p.dyn_count; e++) {
+      int32_t hit = op2(Op::SetpU, Ty::Pred, p.dyn, konst(Ty::B32, e), CmpEq);
+      for (size_t k = 0; k < v.regs.size(); k++) {
+        size_t idx = p.first + e * p.dyn_stride + k;
+        if (idx >= var.slots.size()) return fail("store outside a variable");
+        const Slot& s = var.slots[idx];
+        if (!(s.space == Space::Out || s.space == Space::Reg)) {
+          if (s.space == Space::None && var.storage == SCOutput) continue;
+          return fail("store to a read-only variable");
+        }
+        Ty t = reg_ty(s.reg);
+        int32_t nv;
+        if (t == Ty::Pred)
+          nv = op2(Op::POr, Ty::Pred, op2(Op::PAnd, Ty::Pred, hit, v.regs[k]),
+                   op2(Op::PAnd, Ty::Pred, op1(Op::PNot, Ty::Pred, hit), s.reg));
+        else
+          nv = op3(Op::Selp, t, v.regs[k], s.reg, hit);
+        mov(t, s.reg, nv);
+      }
+    }
+    return true;
+  }
   for (size_t k = 0; k < v.regs.size(); k++) {
     if (p.first + k >= var.slots.size()) return fail("store outside a variable");
     const Slot& s = var.slots[p.first + k];
@@ -1015,8 +1069,21 @@ bool Translator::do_insn(const Insn& in) {
       Place p = it->second;
       for (size_t i = 3; i < o.size(); i++) {
         auto c = consts_.find(o[i]);
-        if (c == consts_.end() || c->second.second.empty())
-          return fail("dynamic access-chain indices are not supported");
+        if (c == consts_.end() || c->second.second.empty()) {
+          /* an index known at run time: into an array, matrix or vector (one such index per chain) */
+          const TypeInfo& ti = ty(p.type);
+          if (ti.kind != TypeInfo::Array && ti.kind != TypeInfo::Matrix && ti.kind != TypeInfo::Vector)
+            return fail("run-time index into a struct");
+          if (!ti.count) return fail("run-time index into a runtime-sized array");
+          if (p.dyn >= 0) return fail("more than one run-time index in an access chain");
+          Val* iv = val(o[i]);
+          if (!iv || iv->regs.empty() || reg_ty(iv->regs[0]) != Ty::B32) return fail("bad run-time index");
+          p.dyn = iv->regs[0];
+          p.dyn_stride = scalars(ti.elem);
+          p.dyn_count = ti.count;
+          p.type = ti.elem;
+          continue;
+        }
         uint32_t off, mt;
         if (!member(p.type, c->second.second[0], off, mt)) return false;
         p.first += off;
@@ -1040,6 +1107,35 @@ bool Translator::do_insn(const Insn& in) {
       Val* v = val(o[1]);
       if (!v) return false;
       return store(it->second, *v);
+    }
+    case OpVectorExtractDynamic: { /* component `index` of a vector (out of range: component 0) */
+      Val* vec = val(o[2]);
+      Val* ix = val(o[3]);
+      if (!vec || !ix || vec->regs.empty() || ix->regs.empty()) return false;
+      int32_t acc = vec->regs[0];
+      for (uint32_t k = 1; k < vec->regs.size(); k++) {
+        int32_t hit = op2(Op::SetpU, Ty::Pred, ix->regs[0], konst(Ty::B32, k), CmpEq);
+        acc = op3(Op::Selp, reg_ty(acc), vec->regs[k], acc, hit);
+      }
+      Val r;
+      r.type = o[0];
+      r.regs.push_back(acc);
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpVectorInsertDynamic: { /* the vector with component `index` replaced */
+      Val* vec = val(o[2]);
+      Val* comp = val(o[3]);
+      Val* ix = val(o[4]);
+      if (!vec || !comp || !ix || comp->regs.empty() || ix->regs.empty()) return false;
+      Val r;
+      r.type = o[0];
+      for (uint32_t k = 0; k < vec->regs.size(); k++) {
+        int32_t hit = op2(Op::SetpU, Ty::Pred, ix->regs[0], konst(Ty::B32, k), CmpEq);
+        r.regs.push_back(op3(Op::Selp, reg_ty(vec->regs[k]), comp->regs[0], vec->regs[k], hit));
+      }
+      vals_[o[1]] = r;
+      return true;
     }
     case OpCopyObject: {
       Val* a = val(o[2]);

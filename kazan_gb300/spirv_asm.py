@@ -29,6 +29,7 @@ OpTypeInt = 21
 OpTypeFloat = 22
 OpTypeVector = 23
 OpTypeMatrix = 24
+OpTypeArray = 28
 OpTypeStruct = 30
 OpTypePointer = 32
 OpTypeFunction = 33
@@ -47,6 +48,8 @@ OpStore = 62
 OpAccessChain = 65
 OpDecorate = 71
 OpMemberDecorate = 72
+OpVectorExtractDynamic = 77
+OpVectorInsertDynamic = 78
 OpVectorShuffle = 79
 OpCompositeConstruct = 80
 OpCompositeExtract = 81
@@ -70,6 +73,8 @@ OpFOrdLessThan = 184
 OpFOrdGreaterThan = 186
 OpBitwiseAnd = 199
 OpPhi = 245
+OpSLessThan = 177
+OpLoopMerge = 246
 OpSelectionMerge = 247
 OpLabel = 248
 OpBranch = 249
@@ -191,6 +196,9 @@ class Module:
 
     def fn_type(self, ret, *params):
         return self._type(("fn", ret) + params, OpTypeFunction, ret, *params)
+
+    def array(self, elem, length):
+        return self._type(("array", elem, length), OpTypeArray, elem, self.ci(length, 0))
 
     def struct(self, *members):
         r = self.new_id()

@@ -84,3 +84,65 @@ def lambert_vs_calls():
     _end_main(m)
     m.entry(ExecVertex, fn, "main", [pc, pv, in_pos, in_nrm, out_nrm])
     return m.to_words()
+
+
+def color_fs_loops():
+    """colour = interpolated in0, copied component by component into a local float[4] in a loop (run-time
+    index into the array, OpVectorExtractDynamic), then read back in a second loop (run-time index loads,
+    OpVectorInsertDynamic into a vec4 phi)"""
+    from kazan_gb300.spirv_asm import (OpPhi, OpLoopMerge, OpBranch, OpSLessThan, OpIAdd,
+                                       OpVectorExtractDynamic, OpVectorInsertDynamic)
+    m = Module()
+    m.capability(CapShader)
+    f32, i32 = m.f32(), m.i32()
+    v4 = m.vec(f32, 4)
+    arr = m.array(f32, 4)
+    v_col = _io(m, SCInput, v4, 0)
+    o = _io(m, SCOutput, v4, 0)
+    fn = _begin_main(m)
+    local = m.res(OpVariable, m.ptr(SCFunction, arr), SCFunction)   # variables live in the first block
+    entry_l = m.new_id()
+    m.op(OpBranch, entry_l)
+    m.op(OpLabel, entry_l)
+    c = m.res(OpLoad, v4, v_col)
+    zero, one, four = m.ci(0), m.ci(1), m.ci(4)
+    # loop 1: for (i = 0; i < 4; i++) local[i] = c[i];
+    h1, b1, k1, e1 = m.new_id(), m.new_id(), m.new_id(), m.new_id()
+    m.op(OpBranch, h1)
+    m.op(OpLabel, h1)
+    i = m.new_id()
+    i_next = m.new_id()
+    m._ins(m.functions, OpPhi, (i32, i, zero, entry_l, i_next, k1))
+    m.op(OpLoopMerge, e1, k1, 0)
+    m.op(OpBranchConditional, m.res(OpSLessThan, m.bool(), i, four), b1, e1)
+    m.op(OpLabel, b1)
+    comp = m.res(OpVectorExtractDynamic, f32, c, i)
+    m.op(OpStore, m.res(OpAccessChain, m.ptr(SCFunction, f32), local, i), comp)
+    m.op(OpBranch, k1)
+    m.op(OpLabel, k1)
+    m._ins(m.functions, OpIAdd, (i32, i_next, i, one))
+    m.op(OpBranch, h1)
+    m.op(OpLabel, e1)
+    # loop 2: r = vec4(0); for (j = 0; j < 4; j++) r[j] = local[j];
+    h2, b2, k2, e2 = m.new_id(), m.new_id(), m.new_id(), m.new_id()
+    zero4 = m.res(OpCompositeConstruct, v4, m.cf(0.0), m.cf(0.0), m.cf(0.0), m.cf(0.0))
+    m.op(OpBranch, h2)
+    m.op(OpLabel, h2)
+    j, j_next, r, r_next = m.new_id(), m.new_id(), m.new_id(), m.new_id()
+    m._ins(m.functions, OpPhi, (i32, j, zero, e1, j_next, k2))
+    m._ins(m.functions, OpPhi, (v4, r, zero4, e1, r_next, k2))
+    m.op(OpLoopMerge, e2, k2, 0)
+    m.op(OpBranchConditional, m.res(OpSLessThan, m.bool(), j, four), b2, e2)
+    m.op(OpLabel, b2)
+    x = m.res(OpLoad, f32, m.res(OpAccessChain, m.ptr(SCFunction, f32), local, j))
+    m._ins(m.functions, OpVectorInsertDynamic, (v4, r_next, r, x, j))
+    m.op(OpBranch, k2)
+    m.op(OpLabel, k2)
+    m._ins(m.functions, OpIAdd, (i32, j_next, j, one))
+    m.op(OpBranch, h2)
+    m.op(OpLabel, e2)
+    m.op(OpStore, o, r)
+    _end_main(m)
+    m.entry(ExecFragment, fn, "main", [v_col, o])
+    m.mode(fn, ModeOriginUpperLeft)
+    return m.to_words()

@@ -119,11 +119,13 @@ def test_double_buffered_submissions_in_flight(renderer):
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["batched", "persistent", "perdraw"])
 def test_shaders_with_function_calls(renderer, mode):
-    """shaders whose helpers are inlined by the translator render exactly what the call-free shaders do"""
+    """shaders whose helpers are inlined by the translator, or that loop over a local array with run-time
+    indices, render exactly what the straight-line shaders do"""
     import dataclasses
     import call_shaders
     soup = dataclasses.replace(CASES["soup"], fs_words=call_shaders.color_fs_calls())
+    loops = dataclasses.replace(CASES["soup"], fs_words=call_shaders.color_fs_loops())
     lam = dataclasses.replace(CASES["batched"], vs_words=call_shaders.lambert_vs_calls())
-    for scene in (soup, lam):
+    for scene in (soup, loops, lam):
         color, depth, stats = _render(renderer, scene, mode, 16)
         _check(scene, color, depth, stats)

@@ -144,3 +144,13 @@ def test_function_calls_are_inlined(built):
     assert vi["input_locations"] == 0b11 and vi["pos_input_locations"] == 0b1 and vi["push_bytes"] == 64
     img = shader.link(shader.emit_ptx([(vs, fs)], [_layouts()[1]]))
     assert img[:4] == b"\x7fELF"
+
+
+def test_run_time_indices_translate(built):
+    """loops with run-time indices into a local array and into vectors translate and link"""
+    import call_shaders
+    fs = shader.Shader(call_shaders.color_fs_loops(), shader.FRAGMENT)
+    assert fs.info()["input_slots"] == 0xF and fs.info()["writes_color"]
+    vs = shader.Shader(spirv_asm.color_vs(), shader.VERTEX)
+    img = shader.link(shader.emit_ptx([(vs, fs)], [_layouts()[0]]))
+    assert img[:4] == b"\x7fELF"
