@@ -69,21 +69,31 @@ static void draw_rect(const Framebuffer* fb, const int32_t area[4], const VkRect
   out[3] = std::min(y1, py1);
 }
 
-static void record_draw(CommandBuffer* cb, uint32_t tri_count, uint32_t instances, uint32_t first_instance, bool indexed,
-                        uint32_t first_index, int32_t vertex_offset) {
+/* a draw needs a render pass and a bound pipeline (else a recording error) */
+static bool draw_state_ok(CommandBuffer* cb) {
   if (cb->cur_pass < 0 || !cb->pipe) {
     log_error("draw outside a render pass or without a bound pipeline");
     cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
-    return;
+    return false;
+  }
+  return true;
+}
+
+/* the state every draw resolves at recording: vertex buffers, index buffer, viewport transform, pixel
+ * rectangle and push-constant snapshot.  False (and a recording error) for an indexed draw without an
+ * index buffer. */
+static bool begin_draw(CommandBuffer* cb, bool indexed, DrawRec& dr, int& nreads) {
+  if (indexed && !cb->ib) {
+    log_error("indexed draw without an index buffer");
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return false;
   }
   Pipeline* p = cb->pipe;
-  if (p->rasterizer_discard || tri_count == 0 || instances == 0) return;
   PassRec& pass = cb->passes[(size_t)cb->cur_pass];
-  DrawRec dr;
   std::memset(&dr.d, 0, sizeof dr.d);
   dr.pipe = p;
   KzDraw& d = dr.d;
-  int nreads = 0;
+  nreads = 0;
   for (int b = 0; b < KZ_MAX_BINDINGS; b++) {
     if (cb->vb[b]) {
       d.vb[b] = (uint64_t)(uintptr_t)(cb->vb[b]->ptr() + cb->vb_off[b]);
@@ -91,20 +101,11 @@ static void record_draw(CommandBuffer* cb, uint32_t tri_count, uint32_t instance
     }
   }
   if (indexed) {
-    if (!cb->ib) {
-      log_error("vkCmdDrawIndexed without an index buffer");
-      cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
-      return;
-    }
-    uint32_t isz = cb->ib_type == VK_INDEX_TYPE_UINT16 ? 2 : 4;
-    d.ib = (uint64_t)(uintptr_t)(cb->ib->ptr() + cb->ib_off + (VkDeviceSize)first_index * isz);
-    d.indexed = isz == 4 ? 1 : 2;
+    d.indexed = cb->ib_type == VK_INDEX_TYPE_UINT16 ? 2 : 1;
+    d.ib_base = (uint64_t)(uintptr_t)(cb->ib->ptr() + cb->ib_off);
+    d.ib = d.ib_base;
     dr.reads[nreads++] = cb->ib->mem;
   }
-  d.vertex_offset = vertex_offset;
-  d.first_instance = first_instance;
-  d.instance_count = instances;
-  d.tri_count = tri_count;
   VkViewport vp = p->dyn_viewport ? cb->viewport : p->viewport;
   VkRect2D sc = p->dyn_scissor ? cb->scissor : p->scissor;
   d.hx = 0.5f * vp.width;
@@ -117,11 +118,88 @@ static void record_draw(CommandBuffer* cb, uint32_t tri_count, uint32_t instance
   d.zmax = std::fmax(vp.minDepth, vp.maxDepth);
   draw_rect(pass.fb, pass.area, sc, vp, d.rect);
   std::memcpy(dr.push, cb->push, KZ_PUSH_BYTES);
+  return true;
+}
+
+static void record_draw(CommandBuffer* cb, uint32_t tri_count, uint32_t instances, uint32_t first_instance, bool indexed,
+                        uint32_t first_index, int32_t vertex_offset) {
+  if (!draw_state_ok(cb) || cb->pipe->rasterizer_discard || tri_count == 0 || instances == 0) return;
+  DrawRec dr;
+  int nreads = 0;
+  if (!begin_draw(cb, indexed, dr, nreads)) return;
+  KzDraw& d = dr.d;
+  if (indexed) d.ib = d.ib_base + (uint64_t)first_index * (d.indexed == 1 ? 4u : 2u);
+  d.vertex_offset = vertex_offset;
+  d.first_instance = first_instance;
+  d.instance_count = instances;
+  d.tri_count = tri_count;
   dr.triangles = (uint64_t)tri_count * instances;
-  if (p->dyn_blend && cb->have_blend_const) {
-    /* dynamic blend constants become part of the per-draw pipeline copy at lowering */
+  cb->passes[(size_t)cb->cur_pass].draws.push_back(dr);
+}
+
+static uint32_t attr_bytes(uint32_t fmt) {
+  switch (fmt) {
+    case KZ_FMT_F32x1: case KZ_FMT_U32x1: case KZ_FMT_U8x4_UNORM: return 4;
+    case KZ_FMT_F32x2: case KZ_FMT_U32x2: return 8;
+    case KZ_FMT_F32x3: case KZ_FMT_U32x3: return 12;
+    default: return 16;
   }
-  pass.draws.push_back(dr);
+}
+
+/* how many vertices (per_instance false) or instances (true) every attribute the shaders read can fetch
+ * from its bound vertex buffer; UINT32_MAX when no such attribute */
+static uint32_t fetch_limit(const CommandBuffer* cb, const KzPipe& kp, bool per_instance) {
+  uint64_t lim = 0xFFFFFFFFull;
+  uint32_t used = kp.pos_input_mask | kp.full_input_mask;
+  for (uint32_t i = 0; i < kp.num_attrs && i < KZ_MAX_VS_INPUTS; i++) {
+    const KzAttr& a = kp.attrs[i];
+    if (!((used >> a.location) & 1u) || (((kp.binding_instanced >> a.binding) & 1u) != 0) != per_instance) continue;
+    const Buffer* b = cb->vb[a.binding];
+    uint64_t avail = b && cb->vb_off[a.binding] < b->size ? b->size - cb->vb_off[a.binding] : 0;
+    uint64_t need = (uint64_t)a.offset + attr_bytes(a.format), stride = kp.binding_stride[a.binding];
+    uint64_t n = avail < need ? 0 : stride == 0 ? 0xFFFFFFFFull : (avail - need) / stride + 1;
+    lim = std::min(lim, n);
+  }
+  return (uint32_t)lim;
+}
+
+/* vkCmdDrawIndirect / vkCmdDrawIndexedIndirect: one KzDraw per command, whose counts kz_k_indirect reads
+ * from the buffer when the command buffer executes (so the buffer may be written by earlier commands or by
+ * the host between submissions) */
+static void record_indirect(CommandBuffer* cb, VkBuffer buffer, VkDeviceSize offset, uint32_t draw_count,
+                            uint32_t stride, bool indexed) {
+  if (!draw_state_ok(cb) || cb->pipe->rasterizer_discard || draw_count == 0) return;
+  const Buffer* buf = H<Buffer>(buffer);
+  uint32_t cmd_bytes = indexed ? 20u : 16u;
+  if (draw_count == 1) stride = cmd_bytes;
+  if (!buf || (offset & 3) || (stride & 3) || stride < cmd_bytes ||
+      offset + (VkDeviceSize)(draw_count - 1) * stride + cmd_bytes > buf->size) {
+    log_error("indirect draw: offset %llu, stride %u, %u commands do not fit the buffer",
+              (unsigned long long)offset, stride, draw_count);
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
+  DrawRec dr;
+  int nreads = 0;
+  if (!begin_draw(cb, indexed, dr, nreads)) return;
+  dr.reads[nreads++] = buf->mem;
+  KzDraw& d = dr.d;
+  const KzPipe& kp = cb->pipe->pipe;
+  if (indexed) {
+    uint32_t isz = d.indexed == 1 ? 4u : 2u;
+    d.elem_limit = (uint32_t)std::min<uint64_t>(cb->ib_off < cb->ib->size ? (cb->ib->size - cb->ib_off) / isz : 0,
+                                                0xFFFFFFFFull);
+  } else {
+    d.elem_limit = fetch_limit(cb, kp, false);
+  }
+  d.instance_limit = fetch_limit(cb, kp, true);
+  dr.triangles = 0;
+  dr.indirect = true;
+  PassRec& pass = cb->passes[(size_t)cb->cur_pass];
+  for (uint32_t i = 0; i < draw_count; i++) {
+    d.indirect = (uint64_t)(uintptr_t)(buf->ptr() + offset + (VkDeviceSize)i * stride);
+    pass.draws.push_back(dr);
+  }
 }
 
 }  // namespace kz
@@ -318,6 +396,18 @@ void VKAPI_CALL kzCmdDrawIndexed(VkCommandBuffer cbh, uint32_t indexCount, uint3
                                  int32_t vertexOffset, uint32_t firstInstance) {
   /* api_impl.rs:4643 vkCmdDrawIndexed: vertex = index[firstIndex + k] + vertexOffset */
   record_draw(H<CommandBuffer>(cbh), indexCount / 3, instanceCount, firstInstance, true, firstIndex, vertexOffset);
+}
+
+void VKAPI_CALL kzCmdDrawIndirect(VkCommandBuffer cbh, VkBuffer buffer, VkDeviceSize offset, uint32_t drawCount,
+                                  uint32_t stride) {
+  /* api_impl.rs:4655 vkCmdDrawIndirect: drawCount VkDrawIndirectCommand structs, `stride` bytes apart */
+  record_indirect(H<CommandBuffer>(cbh), buffer, offset, drawCount, stride, false);
+}
+
+void VKAPI_CALL kzCmdDrawIndexedIndirect(VkCommandBuffer cbh, VkBuffer buffer, VkDeviceSize offset,
+                                         uint32_t drawCount, uint32_t stride) {
+  /* api_impl.rs:4666 vkCmdDrawIndexedIndirect: drawCount VkDrawIndexedIndirectCommand structs */
+  record_indirect(H<CommandBuffer>(cbh), buffer, offset, drawCount, stride, true);
 }
 
 void VKAPI_CALL kzCmdBeginRenderPass(VkCommandBuffer cbh, const VkRenderPassBeginInfo* bi, VkSubpassContents) {
@@ -547,9 +637,9 @@ static void segment_target(const PassRec& pr, KzSegment& s, uint32_t tile, bool 
 
 static int raster_class(const DrawRec& d) {
   /* draws that share a class can share one segment: visibility mode with the same key and write mask,
-   * or ordered mode */
-  if (d.pipe->vis_key >= 0) return 1 + d.pipe->vis_key + 16 * (int)d.pipe->pipe.write_mask;
-  return 0;
+   * or ordered mode; indirect draws never share a segment with direct ones */
+  int k = d.pipe->vis_key >= 0 ? 1 + d.pipe->vis_key + 16 * (int)d.pipe->pipe.write_mask : 0;
+  return d.indirect ? k + 1024 : k;
 }
 
 static VkResult size_scratch(Device* dev, Lowered& low, uint32_t rec_cap, uint32_t pair_cap) {
@@ -568,7 +658,7 @@ static VkResult size_scratch(Device* dev, Lowered& low, uint32_t rec_cap, uint32
   /* ordered segments keep each unclipped record's shading setup beside it: 1/w of the three vertices
    * (16 bytes) then three vertices' varyings */
   bool ordered = false;
-  for (const KzSegment& s : low.segments) ordered |= s.mode == KZ_MODE_ORDERED && s.num_chunks > 0;
+  for (const KzSegment& s : low.segments) ordered |= s.mode == KZ_MODE_ORDERED && (s.num_chunks > 0 || s.indirect);
   if (ordered) {
     uint32_t nv = 0;
     for (const KzPipe& kp : low.pipes) nv = std::max(nv, kp.num_varyings);
@@ -656,6 +746,18 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
     if (lop.kind == OpKind::Pass) {
       if (lop.seg_end <= start) continue;
       uint32_t s0 = std::max(lop.seg_begin, start);
+      /* indirect segments first read their commands: nothing inside a render pass writes the buffers */
+      for (uint32_t s = s0; s < lop.seg_end; s++) {
+        if (!low.segments[s].indirect) continue;
+        KzFrame f = low.frame;
+        void* args[] = {&f, &s};
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(1);
+        cfg.blockDim = dim3(256);
+        cfg.stream = st;
+        launch(dev, timing, KK_INDIRECT, cfg, ks->indirect, args);
+        launches++;
+      }
       if (low.mode == 0) {
         KzFrame f = low.frame;
         f.first_segment = s0;
@@ -684,8 +786,9 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
           if (seg.mode == KZ_MODE_VISIBILITY) {
             cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (seg.width * seg.height + 255) / 256)));
             launch(dev, timing, KK_VIS_INIT, cfg, ks->vis_init, args);
-            if (seg.num_chunks) {
-              cfg.gridDim = dim3(std::min<uint32_t>(seg.num_chunks, (uint32_t)std::max(1, ks->geometry_blocks)));
+            if (seg.num_chunks || seg.indirect) {
+              uint32_t gb = (uint32_t)std::max(1, ks->geometry_blocks);
+              cfg.gridDim = dim3(seg.indirect ? gb : std::min<uint32_t>(seg.num_chunks, gb));
               launch(dev, timing, KK_VIS_GEOMETRY, cfg, ks->vis_geometry, args);
               cfg.gridDim = dim3(grid_cap(dev));
               launch(dev, timing, KK_VIS_LARGE, cfg, ks->vis_large, args);
@@ -696,8 +799,8 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
             launches += 2;
             continue;
           }
-          if (seg.num_chunks) {
-            cfg.gridDim = dim3(seg.num_chunks);
+          if (seg.num_chunks || seg.indirect) {
+            cfg.gridDim = dim3(seg.indirect ? grid_cap(dev) : seg.num_chunks);
             launch(dev, timing, KK_GEOMETRY, cfg, ks->geometry, args);
             launches++;
           }
@@ -801,9 +904,15 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
       s.first_chunk = (uint32_t)low.chunks.size();
       s.mode = KZ_MODE_ORDERED;
       s.vis_key = 0;
-      uint64_t prims = 0;
+      uint64_t prims = 0, guess = 0;
       for (size_t i = runs[r].first; i < runs[r].second; i++) {
         const DrawRec& dr = pr.draws[i];
+        if (dr.indirect) {
+          /* sizing guess: the draws together cover their bound buffers about once; an overflow grows the
+           * scratch and replays */
+          s.indirect = 1;
+          guess = std::max<uint64_t>(guess, std::min<uint64_t>(dr.d.elem_limit / 3, 1u << 22));
+        }
         if (i == runs[r].first && dr.pipe->vis_key >= 0) {
           s.mode = KZ_MODE_VISIBILITY;
           s.vis_key = (uint32_t)dr.pipe->vis_key;
@@ -816,7 +925,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
         d.push_index = (uint32_t)(low.push.size() / KZ_PUSH_BYTES);
         low.push.insert(low.push.end(), dr.push, dr.push + KZ_PUSH_BYTES);
         uint32_t di = (uint32_t)low.draws.size();
-        for (uint64_t c = 0; c < dr.triangles; c += KZ_CHUNK) {
+        for (uint64_t c = 0; !dr.indirect && c < dr.triangles; c += KZ_CHUNK) {
           KzChunk ch;
           ch.draw = di;
           ch.first = (uint32_t)c;
@@ -838,14 +947,16 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
       low.triangles += prims;
       low.max_tiles = std::max(low.max_tiles, s.tiles_x * s.tiles_y);
       low.segments.push_back(s);
+      low.prims_guess.push_back(s.indirect ? guess : prims);
     }
     lop.seg_end = (uint32_t)low.segments.size();
     low.ops.push_back(lop);
   }
   /* scratch sizing: records for every triangle plus clipping headroom; bins for a few tiles per record */
   uint64_t max_prims = 0, max_tiles = 0;
-  for (const KzSegment& s : low.segments) {
-    max_prims = std::max<uint64_t>(max_prims, s.num_prims);
+  for (size_t i = 0; i < low.segments.size(); i++) {
+    const KzSegment& s = low.segments[i];
+    max_prims = std::max<uint64_t>(max_prims, low.prims_guess[i]);
     max_tiles = std::max<uint64_t>(max_tiles, (uint64_t)s.tiles_x * s.tiles_y);
   }
   uint64_t rec_cap = (uint64_t)((double)max_prims * options().rec_slack) + 4096;
@@ -996,7 +1107,7 @@ static bool replay(CommandBuffer* cb, Queue* q) {
   Lowered& low = *cb->low;
   for (int attempt = 0; attempt < 4; attempt++) {
     KzStatus st = *low.h_status;
-    if (!(st.flags & (KZ_STATUS_RECORD_OVERFLOW | KZ_STATUS_PAIR_OVERFLOW))) return !(st.flags & ~0u);
+    if (!(st.flags & (KZ_STATUS_RECORD_OVERFLOW | KZ_STATUS_PAIR_OVERFLOW))) return true; /* others: complete() */
     uint64_t rec = std::max<uint64_t>(low.rec_cap, (uint64_t)((double)st.need_records * 1.25) + 4096);
     uint64_t pair = std::max<uint64_t>(low.pair_cap, (uint64_t)((double)st.need_pairs * 1.25) + 65536);
     if (options().trace) log_error("scratch overflow in segment %u: growing to %llu records, %llu pairs",
@@ -1033,6 +1144,13 @@ static void complete(Queue* q, Submission& s) {
     }
     if (st.flags & KZ_STATUS_BIN_TOO_LARGE) {
       log_error("a tile's bin exceeds the ordered-mode sort capacity; use a smaller tile");
+      err = VK_ERROR_DEVICE_LOST;
+    }
+    /* out-of-range indirect commands are skipped, as robust buffer access would leave them without
+     * effect; the status word keeps the bit for the application */
+    if (st.flags & KZ_STATUS_INDIRECT_RANGE) log_error("an indirect command reads past its bound buffers: skipped");
+    if (st.flags & KZ_STATUS_INDIRECT_LIMIT) {
+      log_error("an indirect segment reaches 2^32 triangles: skipped");
       err = VK_ERROR_DEVICE_LOST;
     }
     cb->last_status = st;

@@ -152,7 +152,8 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
                {"kz_k_bin", &ks->bin},           {"kz_k_raster", &ks->raster},
                {"kz_k_persistent", &ks->persistent}, {"kz_k_clear", &ks->clear},
                {"kz_k_vis_init", &ks->vis_init}, {"kz_k_vis_geometry", &ks->vis_geometry},
-               {"kz_k_vis_large", &ks->vis_large}, {"kz_k_vis_resolve", &ks->vis_resolve}};
+               {"kz_k_vis_large", &ks->vis_large}, {"kz_k_vis_resolve", &ks->vis_resolve},
+               {"kz_k_indirect", &ks->indirect}};
   for (auto& n : names) {
     if (cudaLibraryGetKernel(n.k, ks->lib, n.name) != cudaSuccess) {
       err = std::string("kernel ") + n.name + " missing from the linked module";
@@ -1092,6 +1093,8 @@ void VKAPI_CALL kzCmdBindIndexBuffer(VkCommandBuffer, VkBuffer, VkDeviceSize, Vk
 void VKAPI_CALL kzCmdPushConstants(VkCommandBuffer, VkPipelineLayout, VkShaderStageFlags, uint32_t, uint32_t,
                                    const void*);
 void VKAPI_CALL kzCmdDraw(VkCommandBuffer, uint32_t, uint32_t, uint32_t, uint32_t);
+void VKAPI_CALL kzCmdDrawIndirect(VkCommandBuffer, VkBuffer, VkDeviceSize, uint32_t, uint32_t);
+void VKAPI_CALL kzCmdDrawIndexedIndirect(VkCommandBuffer, VkBuffer, VkDeviceSize, uint32_t, uint32_t);
 void VKAPI_CALL kzCmdDrawIndexed(VkCommandBuffer, uint32_t, uint32_t, uint32_t, int32_t, uint32_t);
 void VKAPI_CALL kzCmdBeginRenderPass(VkCommandBuffer, const VkRenderPassBeginInfo*, VkSubpassContents);
 void VKAPI_CALL kzCmdEndRenderPass(VkCommandBuffer);
@@ -1202,6 +1205,8 @@ static const ProcEntry kProcs[] = {
     KZ_PROC("vkCmdBindIndexBuffer", kzCmdBindIndexBuffer),
     KZ_PROC("vkCmdPushConstants", kzCmdPushConstants),
     KZ_PROC("vkCmdDraw", kzCmdDraw),
+    KZ_PROC("vkCmdDrawIndirect", kzCmdDrawIndirect),
+    KZ_PROC("vkCmdDrawIndexedIndirect", kzCmdDrawIndexedIndirect),
     KZ_PROC("vkCmdDrawIndexed", kzCmdDrawIndexed),
     KZ_PROC("vkCmdBeginRenderPass", kzCmdBeginRenderPass),
     KZ_PROC("vkCmdEndRenderPass", kzCmdEndRenderPass),

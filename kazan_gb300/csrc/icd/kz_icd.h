@@ -143,6 +143,7 @@ enum KernelKind {
   KK_BIN,
   KK_RASTER,
   KK_CLEAR,
+  KK_INDIRECT,
   KK_COUNT
 };
 
@@ -158,7 +159,7 @@ struct KernelSet {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t geometry = nullptr, scan = nullptr, bin = nullptr, raster = nullptr, persistent = nullptr,
                clear = nullptr, vis_init = nullptr, vis_geometry = nullptr, vis_large = nullptr,
-               vis_resolve = nullptr;
+               vis_resolve = nullptr, indirect = nullptr;
   int persistent_blocks = 0;
   int geometry_blocks = 0; /* resident blocks of kz_k_vis_geometry on the whole GPU */
 };
@@ -169,8 +170,9 @@ struct DrawRec {
   Pipeline* pipe = nullptr;
   KzDraw d{};
   uint8_t push[KZ_PUSH_BYTES];
-  uint64_t triangles = 0;
-  DeviceMemory* reads[KZ_MAX_BINDINGS + 1] = {};
+  uint64_t triangles = 0;  /* direct draws; indirect draws count theirs on the device */
+  bool indirect = false;
+  DeviceMemory* reads[KZ_MAX_BINDINGS + 2] = {};
 };
 
 struct PassRec {
@@ -206,6 +208,7 @@ struct Lowered {
   std::vector<Pipeline*> pipe_objs;
   std::vector<KzChunk> chunks;
   std::vector<KzSegment> segments;
+  std::vector<uint64_t> prims_guess;       /* per segment: triangles the scratch is first sized for */
   std::vector<uint8_t> push;
   std::vector<uint32_t> draw_lut;          /* all segments' draw lookup tables, back to back */
   std::vector<size_t> draw_lut_offset;     /* per segment: first entry in draw_lut */

@@ -120,6 +120,16 @@ typedef struct KzDraw {
   /* viewport transform constants: xf = fma(xd, hx, ox), yf = fma(yd, hy, oy), zf = fma(zd, pz, oz) */
   float hx, ox, hy, oy, pz, oz, zmin, zmax;
   int32_t rect[4];              /* pixel rectangle x0,y0,x1,y1 (exclusive): fb & render area & scissor & viewport */
+  /* indirect draws (vkCmdDrawIndirect / vkCmdDrawIndexedIndirect): kz_k_indirect reads the command at
+   * `indirect` and writes ib, vertex_offset, first_instance, instance_count, tri_count, prim_base and
+   * chunk_base before the segment runs */
+  uint64_t indirect;            /* device address of a VkDrawIndirectCommand / VkDrawIndexedIndirectCommand; 0: direct */
+  uint64_t ib_base;             /* indexed: device address of index 0 of the bound index buffer (buffer + offset) */
+  uint32_t elem_limit;          /* indices the bound index buffer holds past ib_base (indexed), or vertices every
+                                   per-vertex binding holds (non-indexed); a command beyond it is skipped */
+  uint32_t instance_limit;      /* instances every per-instance binding holds */
+  uint32_t chunk_base;          /* first chunk of the draw within its segment */
+  uint32_t pad;
 } KzDraw;
 
 /* geometry work unit: a contiguous run of at most KZ_CHUNK triangles of one draw */
@@ -192,6 +202,9 @@ typedef struct KzSegment {
                                 float 1/w[3], pad, then varyings (divided by w unless flat/noperspective)
                                 [3][num_varyings] */
   uint64_t draw_lut;         /* u32 per 256 primitives: the draw holding primitive 256 i (0: search) */
+  uint32_t indirect;         /* 1: every draw is indirect; kz_k_indirect writes num_chunks and num_prims, and
+                                chunk k belongs to the last draw whose chunk_base <= k (no KzChunk entries) */
+  uint32_t pad;
 } KzSegment;
 
 /* status words written by the kernels (one per submission) */
@@ -200,7 +213,9 @@ enum KzStatusBits {
   KZ_STATUS_RECORD_OVERFLOW = 1,
   KZ_STATUS_PAIR_OVERFLOW = 2,
   KZ_STATUS_BARRIER_TIMEOUT = 4,
-  KZ_STATUS_BIN_TOO_LARGE = 8
+  KZ_STATUS_BIN_TOO_LARGE = 8,
+  KZ_STATUS_INDIRECT_RANGE = 16,  /* an indirect command reads past its bound buffers: that draw was skipped */
+  KZ_STATUS_INDIRECT_LIMIT = 32   /* an indirect segment's triangles reach 2^32: the segment was skipped */
 };
 
 typedef struct KzStatus {

@@ -107,6 +107,26 @@ __device__ uint32_t find_draw(const KzDraw* draws, uint32_t first, uint32_t coun
   return lo;
 }
 
+/* chunk k of a segment: a table entry, or, for indirect segments, the last draw whose chunk_base <= k
+ * (draws without triangles share the chunk_base of the next draw, so they are never chosen) */
+__device__ __forceinline__ KzChunk chunk_at(const Ctx& c, uint32_t k) {
+  const KzSegment& seg = *c.seg;
+  if (!seg.indirect) return reinterpret_cast<const KzChunk*>(c.f->chunks)[seg.first_chunk + k];
+  uint32_t lo = seg.first_draw, hi = seg.first_draw + seg.num_draws;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (c.draws[mid].chunk_base <= k) lo = mid;
+    else hi = mid;
+  }
+  const KzDraw& d = c.draws[lo];
+  KzChunk ch;
+  ch.draw = lo;
+  ch.first = (k - d.chunk_base) * KZ_CHUNK;
+  ch.count = min((uint32_t)KZ_CHUNK, d.tri_count * d.instance_count - ch.first);
+  ch.pad = 0;
+  return ch;
+}
+
 __device__ void tri_vertices(const KzDraw& d, uint32_t local, uint32_t vid[3], uint32_t& iid) {
   uint32_t inst = local / d.tri_count;
   uint32_t t = local - inst * d.tri_count;
@@ -780,7 +800,7 @@ __device__ void write_shade(const Ctx& c, uint32_t idx, uint32_t di, const uint3
 
 /* one chunk per block: records are allocated with one atomic per block */
 __device__ void geometry_chunk(const Ctx& c, uint32_t chunk, uint32_t* sh) {
-  const KzChunk ch = reinterpret_cast<const KzChunk*>(c.f->chunks)[chunk];
+  const KzChunk ch = chunk_at(c, chunk);
   KzTriRecord r;
   bool have = false, sw = false;
   uint32_t vid[3] = {0, 0, 0}, iid = 0;
@@ -1357,7 +1377,7 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
  * (vis_warp_raster).  Returns the lane's fragment count. */
 __device__ __forceinline__ uint32_t vis_geometry_warp(const Ctx& c, uint32_t chunk, uint32_t sub, WarpTri* slots,
                                                       uint8_t* owner, const uint32_t* magic_tab) {
-  const KzChunk ch = reinterpret_cast<const KzChunk*>(c.f->chunks)[chunk];
+  const KzChunk ch = chunk_at(c, chunk);
   if (sub * 32 >= ch.count) return 0;
   const KzDraw& d = c.draws[ch.draw];
   const KzPipe& p = c.pipes[d.pipe];
@@ -1392,7 +1412,7 @@ __device__ void vis_geometry_warps(const Ctx& c, unsigned char* smem, const uint
   const uint32_t groups = c.seg->num_chunks * 8;
   uint32_t frags = 0;
   for (uint32_t i = w; i < groups; i += warps)
-    frags += vis_geometry_warp(c, c.seg->first_chunk + i / 8, i % 8, slots, owner, magic_tab);
+    frags += vis_geometry_warp(c, i / 8, i % 8, slots, owner, magic_tab);
   for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
   if ((threadIdx.x & 31) == 0 && frags) {
     atomicAdd(&c.cnt->fragments, frags);
@@ -1863,7 +1883,96 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_geometry(KzFrame f
   __shared__ uint32_t sh[40];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
-  if (blockIdx.x < c.seg->num_chunks) geometry_chunk(c, c.seg->first_chunk + blockIdx.x, sh);
+  for (uint32_t k = blockIdx.x; k < c.seg->num_chunks; k += gridDim.x) geometry_chunk(c, k, sh);
+}
+
+/* the indirect draws of segment s (one block, before the segment's other kernels): read each draw's
+ * VkDrawIndirectCommand {vertexCount, instanceCount, firstVertex, firstInstance} or
+ * VkDrawIndexedIndirectCommand {indexCount, instanceCount, firstIndex, vertexOffset, firstInstance}, skip a
+ * command whose vertices, indices or instances lie past the bound buffers (status KZ_STATUS_INDIRECT_RANGE),
+ * write the draw's counts and index address, then prim_base and chunk_base as exclusive prefix sums over
+ * the segment in draw order (a chunk never spans two draws, as in the chunk table of direct draws), and
+ * the segment's num_prims and num_chunks. */
+extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_indirect(KzFrame f, uint32_t s) {
+  __shared__ unsigned long long warp_prims[KZ_THREADS / 32], warp_chunks[KZ_THREADS / 32];
+  KzSegment* seg = reinterpret_cast<KzSegment*>(f.segments) + s;
+  KzDraw* draws = reinterpret_cast<KzDraw*>(f.draws);
+  KzStatus* st = reinterpret_cast<KzStatus*>(f.status);
+  const uint32_t n = seg->num_draws, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long prim_run = 0, chunk_run = 0;
+  bool bad = false;
+  for (uint32_t base = 0; base < n; base += KZ_THREADS) {
+    const uint32_t i = base + threadIdx.x;
+    KzDraw* d = i < n ? draws + seg->first_draw + i : nullptr;
+    unsigned long long prims = 0;
+    if (d) {
+      const uint32_t* cmd = reinterpret_cast<const uint32_t*>(d->indirect);
+      uint32_t tri = cmd[0] / 3, inst = cmd[1], first = cmd[2], first_inst;
+      int32_t voff;
+      if (d->indexed) {
+        voff = (int32_t)cmd[3];
+        first_inst = cmd[4];
+      } else {
+        voff = (int32_t)first;
+        first_inst = cmd[3];
+      }
+      bool ok = (unsigned long long)first + 3ull * tri <= d->elem_limit &&
+                (unsigned long long)first_inst + inst <= d->instance_limit;
+      if (!ok) {
+        bad |= tri != 0 && inst != 0;
+        inst = 0;
+      }
+      d->tri_count = tri;
+      d->instance_count = inst;
+      d->vertex_offset = voff;
+      d->first_instance = first_inst;
+      if (d->indexed) d->ib = d->ib_base + (unsigned long long)first * (d->indexed == 1 ? 4u : 2u);
+      prims = (unsigned long long)tri * inst;
+    }
+    const unsigned long long chunks = (prims + KZ_CHUNK - 1) / KZ_CHUNK;
+    unsigned long long ip = prims, ic = chunks;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long a = __shfl_up_sync(0xFFFFFFFFu, ip, o), b = __shfl_up_sync(0xFFFFFFFFu, ic, o);
+      if (lane >= (uint32_t)o) {
+        ip += a;
+        ic += b;
+      }
+    }
+    if (lane == 31) {
+      warp_prims[warp] = ip;
+      warp_chunks[warp] = ic;
+    }
+    __syncthreads();
+    unsigned long long wp = 0, wc = 0, tp = 0, tc = 0;
+    for (uint32_t w = 0; w < KZ_THREADS / 32; w++) {
+      if (w < warp) {
+        wp += warp_prims[w];
+        wc += warp_chunks[w];
+      }
+      tp += warp_prims[w];
+      tc += warp_chunks[w];
+    }
+    if (d) {
+      d->prim_base = (uint32_t)min(prim_run + wp + ip - prims, 0xFFFFFFFFull);
+      d->chunk_base = (uint32_t)min(chunk_run + wc + ic - chunks, 0xFFFFFFFFull);
+    }
+    prim_run += tp;
+    chunk_run += tc;
+    __syncthreads();
+  }
+  bad = __syncthreads_or(bad) != 0;
+  if (threadIdx.x == 0) {
+    if (prim_run >= 0xFFFFFFF0ull) {
+      seg->num_prims = 0;
+      seg->num_chunks = 0;
+      atomicOr(&st->flags, (uint32_t)KZ_STATUS_INDIRECT_LIMIT);
+    } else {
+      seg->num_prims = (uint32_t)prim_run;
+      seg->num_chunks = (uint32_t)chunk_run;
+    }
+    if (bad) atomicOr(&st->flags, (uint32_t)KZ_STATUS_INDIRECT_RANGE);
+  }
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_scan(KzFrame f, uint32_t s) {
@@ -1986,7 +2095,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
     for (;;) {
       uint32_t k = grab(&c.cnt->geom_next, &item);
       if (k >= c.seg->num_chunks) break;
-      geometry_chunk(c, c.seg->first_chunk + k, geo_sh);
+      geometry_chunk(c, k, geo_sh);
     }
     if (!grid_barrier(st)) return;
     if (blockIdx.x == 0) scan_tiles(c, s, scan_sh);

@@ -321,11 +321,34 @@ class Renderer:
         return h
 
 
-class SceneRun:
-    """GPU resources and a recorded command buffer for one scene."""
+INDIRECT_STRIDE = 32  # bytes between the indirect commands of a SceneRun (larger than either command)
 
-    def __init__(self, r, scene, host_visible=False, mode=None, tile=None, keep_mapped=False, depth_host_visible=None):
+
+def indirect_commands(scene, instances=1):
+    """the scene's draws as VkDrawIndirectCommand {vertexCount, instanceCount, firstVertex, firstInstance} or
+    VkDrawIndexedIndirectCommand {indexCount, instanceCount, firstIndex, vertexOffset, firstInstance} words,
+    one row of INDIRECT_STRIDE bytes per draw"""
+    cmds = np.zeros((len(scene.draws), INDIRECT_STRIDE // 4), dtype=np.uint32)
+    for i, dr in enumerate(scene.draws):
+        if scene.indexed:
+            cmds[i, :5] = [3 * dr.count, instances, dr.first, dr.vertex_offset & 0xFFFFFFFF, 0]
+        else:
+            cmds[i, :4] = [3 * dr.count, instances, dr.first, 0]
+    return cmds
+
+
+class SceneRun:
+    """GPU resources and a recorded command buffer for one scene.
+
+    indirect: None records vkCmdDraw / vkCmdDrawIndexed; "host" records the indirect variants over a
+    host-visible buffer of commands written by the host; "device" over a device-local buffer that the same
+    command buffer fills with vkCmdCopyBuffer before the render pass.  Draws with their own push constants
+    become one indirect call each, the others one call of drawCount = len(draws)."""
+
+    def __init__(self, r, scene, host_visible=False, mode=None, tile=None, keep_mapped=False, depth_host_visible=None,
+                 indirect=None):
         self.r, self.scene = r, scene
+        self.indirect = indirect
         d = r.drv
         if mode is not None:
             d.set_option("mode", mode)
@@ -347,11 +370,23 @@ class SceneRun:
         self.layout = r.pipeline_layout(64 if scene.shader == "lambert" else 0)
         vs, fs = scene.shaders()
         self.pipe = r.pipeline(scene, self.rp, self.layout, vs, fs)
+        self.cmds = self.cmd_staging = None
+        if indirect is not None:
+            words = indirect_commands(scene)
+            self.cmds = r.create_buffer(words.nbytes, vk.BUFFER_USAGE_INDIRECT, indirect == "host")
+            if indirect == "host":
+                r.write_buffer(self.cmds, words)
+            else:
+                self.cmd_staging = r.create_buffer(words.nbytes, vk.BUFFER_USAGE_TRANSFER_SRC, True)
+                r.write_buffer(self.cmd_staging, words)
         self.cb = self.record()
 
     def record(self):
         r, s, d = self.r, self.scene, self.r.drv
         cb = r.begin()
+        if self.cmd_staging is not None:
+            region = vk.VkBufferCopy(0, 0, self.cmds.size)
+            d.vkCmdCopyBuffer(cb, self.cmd_staging.handle, self.cmds.handle, 1, byref(region))
         clears = (vk.VkClearValue * 2)()
         clears[0].color.float32[:] = list(s.clear_color)
         clears[1].depthStencil.depth = s.clear_depth
@@ -364,11 +399,20 @@ class SceneRun:
         d.vkCmdBindVertexBuffers(cb, 0, 1, bufs, offs)
         if self.ib is not None:
             d.vkCmdBindIndexBuffer(cb, self.ib.handle, 0, vk.INDEX_TYPE_UINT32)
-        for dr in s.draws:
+        per_draw_push = any(dr.mvp is not None for dr in s.draws)
+        if self.indirect is not None and not per_draw_push:
+            call = d.vkCmdDrawIndexedIndirect if s.indexed else d.vkCmdDrawIndirect
+            call(cb, self.cmds.handle, 0, len(s.draws), INDIRECT_STRIDE)
+        for i, dr in enumerate(s.draws):
+            if self.indirect is not None and not per_draw_push:
+                break
             if dr.mvp is not None:
                 m = np.ascontiguousarray(dr.mvp, dtype=np.float32)
                 d.vkCmdPushConstants(cb, self.layout, vk.SHADER_STAGE_VERTEX, 0, 64, m.ctypes.data)
-            if s.indexed:
+            if self.indirect is not None:
+                call = d.vkCmdDrawIndexedIndirect if s.indexed else d.vkCmdDrawIndirect
+                call(cb, self.cmds.handle, i * INDIRECT_STRIDE, 1, INDIRECT_STRIDE)
+            elif s.indexed:
                 d.vkCmdDrawIndexed(cb, 3 * dr.count, 1, dr.first, dr.vertex_offset, 0)
             else:
                 d.vkCmdDraw(cb, 3 * dr.count, 1, dr.first, 0)

@@ -76,6 +76,7 @@ BUFFER_USAGE_TRANSFER_SRC = 0x1
 BUFFER_USAGE_TRANSFER_DST = 0x2
 BUFFER_USAGE_INDEX = 0x40
 BUFFER_USAGE_VERTEX = 0x80
+BUFFER_USAGE_INDIRECT = 0x100
 IMAGE_USAGE_TRANSFER_SRC = 0x1
 IMAGE_USAGE_TRANSFER_DST = 0x2
 IMAGE_USAGE_COLOR_ATTACHMENT = 0x10
@@ -493,7 +494,7 @@ class VkBufferImageCopy(Structure):
 
 # kernel kinds of kzGetKernelTimes (KZ_KERNEL_KIND_NAMES)
 KERNEL_KINDS = ["kz_k_persistent", "kz_k_vis_init", "kz_k_vis_geometry", "kz_k_vis_large", "kz_k_vis_resolve",
-                "kz_k_geometry", "kz_k_scan", "kz_k_bin", "kz_k_raster", "kz_k_clear"]
+                "kz_k_geometry", "kz_k_scan", "kz_k_bin", "kz_k_raster", "kz_k_clear", "kz_k_indirect"]
 
 
 class KzCommandBufferStats(Structure):
@@ -557,6 +558,8 @@ _PROTOS = {
     "vkCmdPushConstants": (None, [H, H, c_uint32, c_uint32, c_uint32, c_void_p]),
     "vkCmdDraw": (None, [H, c_uint32, c_uint32, c_uint32, c_uint32]),
     "vkCmdDrawIndexed": (None, [H, c_uint32, c_uint32, c_uint32, c_int32, c_uint32]),
+    "vkCmdDrawIndirect": (None, [H, H, c_uint64, c_uint32, c_uint32]),
+    "vkCmdDrawIndexedIndirect": (None, [H, H, c_uint64, c_uint32, c_uint32]),
     "vkCmdBeginRenderPass": (None, [H, P(VkRenderPassBeginInfo), c_int]),
     "vkCmdEndRenderPass": (None, [H]),
     "vkCmdClearColorImage": (None, [H, H, c_int, P(VkClearColorValue), c_uint32, P(VkImageSubresourceRange)]),
