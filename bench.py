@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--ndraws", type=int, default=4096)
     ap.add_argument("--tile", type=int, default=16)
     ap.add_argument("--mode", default="batched", choices=["persistent", "batched", "perdraw"])
+    ap.add_argument("--indirect", default="none", choices=["none", "host", "device"],
+                    help="record the draws as vkCmdDraw*Indirect over commands in host-visible memory, or in "
+                         "device memory written by a vkCmdCopyBuffer in the same command buffer")
     ap.add_argument("--no-perdraw", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -207,14 +210,19 @@ def main():
         return serve_main(args, rk)
     from kazan_gb300 import render
     scene, cfg = make_scene(args)
+    indirect = None if args.indirect == "none" else args.indirect
+    if indirect:
+        cfg["workload"] = cfg["workload"].replace("vkCmdDrawIndexed", "vkCmdDrawIndexedIndirect") + \
+            ", indirect commands in %s memory" % indirect
     r = render.Renderer()
-    run = render.SceneRun(r, scene, host_visible=False, mode=args.mode, tile=args.tile)
+    run = render.SceneRun(r, scene, host_visible=False, mode=args.mode, tile=args.tile, indirect=indirect)
     mode, tile, tuning = args.mode, args.tile, None
     if not args.no_tune:
         # launch schedule and tile side from the autotuner (measured here unless cached for this workload)
         from kazan_gb300 import autotune
         gpu = r.props.deviceName.decode(errors="replace")
         sig = autotune.signature(gpu, scene.blend, len(scene.draws), scene.triangles, scene.width, scene.height)
+        sig += "|indirect" if indirect else ""
         best, table = autotune.Tuner().choose(sig, autotune.scene_timer(run),
                                               autotune.candidates(ordered=scene.blend))
         mode, tile = best.mode, best.tile
@@ -284,7 +292,7 @@ def main():
            "kernels": kernels,
            "clocks": ck, "gpu_launches": int(sum(n for _, n in ktimes.values())), "autotune": tuning}
     if not args.no_perdraw:
-        pd = render.SceneRun(r, scene, host_visible=False, mode="perdraw", tile=args.tile)
+        pd = render.SceneRun(r, scene, host_visible=False, mode="perdraw", tile=args.tile, indirect=indirect)
         pd.submit()
         steps = 2
         p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -309,7 +317,7 @@ def main():
         # downloads its colour image and reads it on the host; the driver uploads on a copy engine, so one
         # step's upload overlaps the previous step's kernels.  Depth is scratch of the step (device-local).
         sets = [render.SceneRun(r, scene, host_visible=True, mode=mode, tile=tile, keep_mapped=True,
-                                depth_host_visible=False) for _ in range(2)]
+                                depth_host_visible=False, indirect=indirect) for _ in range(2)]
         fences = []
         for _ in range(2):
             f = ctypes.c_void_p()

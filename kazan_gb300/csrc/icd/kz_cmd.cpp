@@ -753,10 +753,14 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
         void* args[] = {&f, &s};
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(1);
-        cfg.blockDim = dim3(256);
+        cfg.blockDim = dim3(1024);
         cfg.stream = st;
         launch(dev, timing, KK_INDIRECT, cfg, ks->indirect, args);
-        launches++;
+        const KzSegment& sg = low.segments[s];
+        cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (std::max(sg.chunk_cap, sg.lut_cap) + 255) / 256)));
+        cfg.blockDim = dim3(256);
+        launch(dev, timing, KK_INDIRECT_TABLES, cfg, ks->indirect_tables, args);
+        launches += 2;
       }
       if (low.mode == 0) {
         KzFrame f = low.frame;
@@ -911,7 +915,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
           /* sizing guess: the draws together cover their bound buffers about once; an overflow grows the
            * scratch and replays */
           s.indirect = 1;
-          guess = std::max<uint64_t>(guess, std::min<uint64_t>(dr.d.elem_limit / 3, 1u << 22));
+          guess = std::max<uint64_t>(guess, dr.d.elem_limit / 3);
         }
         if (i == runs[r].first && dr.pipe->vis_key >= 0) {
           s.mode = KZ_MODE_VISIBILITY;
@@ -947,7 +951,10 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
       low.triangles += prims;
       low.max_tiles = std::max(low.max_tiles, s.tiles_x * s.tiles_y);
       low.segments.push_back(s);
-      low.prims_guess.push_back(s.indirect ? guess : prims);
+      /* scratch records for at most 4M guessed triangles (an overflow grows them); the chunk table and draw
+       * lookup, 4 bytes per 256 triangles, take the whole guess */
+      low.prims_guess.push_back(s.indirect ? std::min<uint64_t>(guess, 1u << 22) : prims);
+      low.table_guess.push_back(s.indirect ? guess : 0);
     }
     lop.seg_end = (uint32_t)low.segments.size();
     low.ops.push_back(lop);
@@ -975,13 +982,28 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
       low.draw_lut.push_back(d);
     }
   }
-  /* device tables: draws | pipes | chunks | segments | push | draw lookup, then counters and status */
+  /* indirect segments: room for the chunk table and the draw lookup that kz_k_indirect_tables fills, sized
+   * from the guess (a segment that outgrows them searches the draws instead) */
+  std::vector<size_t> ind_off(low.segments.size(), 0);
+  size_t ind_words = 0;
+  for (size_t i = 0; i < low.segments.size(); i++) {
+    KzSegment& sg = low.segments[i];
+    if (!sg.indirect) continue;
+    uint64_t g = low.table_guess[i] / KZ_CHUNK;
+    sg.chunk_cap = (uint32_t)std::min<uint64_t>(g + sg.num_draws + 1024, 1u << 24);
+    sg.lut_cap = (uint32_t)std::min<uint64_t>(g + 1024, 1u << 24);
+    ind_off[i] = ind_words;
+    ind_words += (size_t)sg.chunk_cap * (sizeof(KzChunk) / 4) + sg.lut_cap;
+  }
+  /* device tables: draws | pipes | chunks | segments | push | draw lookup | indirect tables, then counters
+   * and status */
   size_t o_pipes = align_up(low.draws.size() * sizeof(KzDraw), 256);
   size_t o_chunks = align_up(o_pipes + low.pipes.size() * sizeof(KzPipe), 256);
   size_t o_segs = align_up(o_chunks + low.chunks.size() * sizeof(KzChunk), 256);
   size_t o_push = align_up(o_segs + low.segments.size() * sizeof(KzSegment), 256);
   size_t o_lut = align_up(o_push + low.push.size(), 256);
-  size_t o_counters = align_up(o_lut + low.draw_lut.size() * sizeof(uint32_t), 256);
+  size_t o_ind = align_up(o_lut + low.draw_lut.size() * sizeof(uint32_t), 256);
+  size_t o_counters = align_up(o_ind + ind_words * sizeof(uint32_t), 256);
   size_t o_status = align_up(o_counters + low.segments.size() * sizeof(KzSegCounters), 256);
   low.tables_bytes = o_status + sizeof(KzStatus);
   void* p = nullptr;
@@ -1010,6 +1032,10 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
     s.draw_lut = s.num_prims ? (uint64_t)(uintptr_t)(low.d_tables + o_lut + low.draw_lut_offset[i] * sizeof(uint32_t))
                              : 0;
     s.vis = s.mode == KZ_MODE_VISIBILITY ? (uint64_t)(uintptr_t)low.d_vis : 0;
+    if (s.indirect) {
+      s.chunk_table = (uint64_t)(uintptr_t)(low.d_tables + o_ind + ind_off[i] * sizeof(uint32_t));
+      s.lut_table = s.chunk_table + (uint64_t)s.chunk_cap * sizeof(KzChunk);
+    }
   }
   r = size_scratch(dev, low, (uint32_t)rec_cap, (uint32_t)pair_cap);
   if (r != VK_SUCCESS) return r;

@@ -153,7 +153,7 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
                {"kz_k_persistent", &ks->persistent}, {"kz_k_clear", &ks->clear},
                {"kz_k_vis_init", &ks->vis_init}, {"kz_k_vis_geometry", &ks->vis_geometry},
                {"kz_k_vis_large", &ks->vis_large}, {"kz_k_vis_resolve", &ks->vis_resolve},
-               {"kz_k_indirect", &ks->indirect}};
+               {"kz_k_indirect", &ks->indirect}, {"kz_k_indirect_tables", &ks->indirect_tables}};
   for (auto& n : names) {
     if (cudaLibraryGetKernel(n.k, ks->lib, n.name) != cudaSuccess) {
       err = std::string("kernel ") + n.name + " missing from the linked module";

@@ -144,6 +144,7 @@ enum KernelKind {
   KK_RASTER,
   KK_CLEAR,
   KK_INDIRECT,
+  KK_INDIRECT_TABLES,
   KK_COUNT
 };
 
@@ -159,7 +160,7 @@ struct KernelSet {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t geometry = nullptr, scan = nullptr, bin = nullptr, raster = nullptr, persistent = nullptr,
                clear = nullptr, vis_init = nullptr, vis_geometry = nullptr, vis_large = nullptr,
-               vis_resolve = nullptr, indirect = nullptr;
+               vis_resolve = nullptr, indirect = nullptr, indirect_tables = nullptr;
   int persistent_blocks = 0;
   int geometry_blocks = 0; /* resident blocks of kz_k_vis_geometry on the whole GPU */
 };
@@ -209,6 +210,7 @@ struct Lowered {
   std::vector<KzChunk> chunks;
   std::vector<KzSegment> segments;
   std::vector<uint64_t> prims_guess;       /* per segment: triangles the scratch is first sized for */
+  std::vector<uint64_t> table_guess;       /* per indirect segment: triangles its device tables have room for */
   std::vector<uint8_t> push;
   std::vector<uint32_t> draw_lut;          /* all segments' draw lookup tables, back to back */
   std::vector<size_t> draw_lut_offset;     /* per segment: first entry in draw_lut */

@@ -204,6 +204,12 @@ typedef struct KzSegment {
   uint64_t draw_lut;         /* u32 per 256 primitives: the draw holding primitive 256 i (0: search) */
   uint32_t indirect;         /* 1: every draw is indirect; kz_k_indirect writes num_chunks and num_prims, and
                                 chunk k belongs to the last draw whose chunk_base <= k (no KzChunk entries) */
+  uint32_t chunk_cap;        /* indirect: entries of chunk_table */
+  uint64_t chunk_table;      /* indirect: KzChunk per chunk (kz_k_indirect_tables); used when
+                                num_chunks <= chunk_cap, else chunk_at searches the draws */
+  uint64_t lut_table;        /* indirect: room for the draw lookup; kz_k_indirect points draw_lut at it when
+                                the segment's primitives need at most lut_cap entries, else sets it to 0 */
+  uint32_t lut_cap;
   uint32_t pad;
 } KzSegment;
 

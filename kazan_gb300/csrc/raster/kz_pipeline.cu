@@ -107,17 +107,25 @@ __device__ uint32_t find_draw(const KzDraw* draws, uint32_t first, uint32_t coun
   return lo;
 }
 
-/* chunk k of a segment: a table entry, or, for indirect segments, the last draw whose chunk_base <= k
- * (draws without triangles share the chunk_base of the next draw, so they are never chosen) */
+/* the last draw of [first, first + count) whose chunk_base <= k (draws without triangles share the
+ * chunk_base of the next draw, so they are never chosen) */
+__device__ __forceinline__ uint32_t draw_of_chunk(const KzDraw* draws, uint32_t first, uint32_t count, uint32_t k) {
+  uint32_t lo = first, hi = first + count;
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (draws[mid].chunk_base <= k) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+/* chunk k of a segment: a table entry; for indirect segments, the draw from the chunk table built on the
+ * device, or from a search when the table was too small */
 __device__ __forceinline__ KzChunk chunk_at(const Ctx& c, uint32_t k) {
   const KzSegment& seg = *c.seg;
   if (!seg.indirect) return reinterpret_cast<const KzChunk*>(c.f->chunks)[seg.first_chunk + k];
-  uint32_t lo = seg.first_draw, hi = seg.first_draw + seg.num_draws;
-  while (hi - lo > 1) {
-    uint32_t mid = (lo + hi) >> 1;
-    if (c.draws[mid].chunk_base <= k) lo = mid;
-    else hi = mid;
-  }
+  if (seg.num_chunks <= seg.chunk_cap) return reinterpret_cast<const KzChunk*>(seg.chunk_table)[k];
+  const uint32_t lo = draw_of_chunk(c.draws, seg.first_draw, seg.num_draws, k);
   const KzDraw& d = c.draws[lo];
   KzChunk ch;
   ch.draw = lo;
@@ -1886,51 +1894,74 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_geometry(KzFrame f
   for (uint32_t k = blockIdx.x; k < c.seg->num_chunks; k += gridDim.x) geometry_chunk(c, k, sh);
 }
 
-/* the indirect draws of segment s (one block, before the segment's other kernels): read each draw's
- * VkDrawIndirectCommand {vertexCount, instanceCount, firstVertex, firstInstance} or
- * VkDrawIndexedIndirectCommand {indexCount, instanceCount, firstIndex, vertexOffset, firstInstance}, skip a
- * command whose vertices, indices or instances lie past the bound buffers (status KZ_STATUS_INDIRECT_RANGE),
- * write the draw's counts and index address, then prim_base and chunk_base as exclusive prefix sums over
- * the segment in draw order (a chunk never spans two draws, as in the chunk table of direct draws), and
- * the segment's num_prims and num_chunks. */
-extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_indirect(KzFrame f, uint32_t s) {
-  __shared__ unsigned long long warp_prims[KZ_THREADS / 32], warp_chunks[KZ_THREADS / 32];
+#define KZ_IND_THREADS 1024
+#define KZ_IND_ITEMS 4
+
+/* one indirect command as read: VkDrawIndirectCommand {vertexCount, instanceCount, firstVertex,
+ * firstInstance} or VkDrawIndexedIndirectCommand {indexCount, instanceCount, firstIndex, vertexOffset,
+ * firstInstance}, with the draw's limits */
+struct IndirectCmd {
+  uint32_t tri, inst, first, first_inst;
+  int32_t voff;
+  uint32_t indexed;
+  unsigned long long ib_base;
+};
+
+/* loads only (read-only path), so that the loads of several commands overlap; a command whose vertices,
+ * indices or instances lie past the bound buffers gets no instances (`bad` set when it would have drawn) */
+__device__ __forceinline__ IndirectCmd load_indirect(const KzDraw& d, bool& bad) {
+  IndirectCmd c;
+  const uint32_t* cmd = reinterpret_cast<const uint32_t*>(__ldg(&d.indirect));
+  c.indexed = __ldg(&d.indexed);
+  c.tri = __ldg(cmd) / 3;
+  c.inst = __ldg(cmd + 1);
+  c.first = __ldg(cmd + 2);
+  if (c.indexed) {
+    c.voff = (int32_t)__ldg(cmd + 3);
+    c.first_inst = __ldg(cmd + 4);
+  } else {
+    c.voff = (int32_t)c.first;
+    c.first_inst = __ldg(cmd + 3);
+  }
+  c.ib_base = __ldg(&d.ib_base);
+  bool ok = (unsigned long long)c.first + 3ull * c.tri <= __ldg(&d.elem_limit) &&
+            (unsigned long long)c.first_inst + c.inst <= __ldg(&d.instance_limit);
+  if (!ok) {
+    bad |= c.tri != 0 && c.inst != 0;
+    c.inst = 0;
+  }
+  return c;
+}
+
+/* the indirect draws of segment s (one block, before the segment's other kernels): each thread reads
+ * KZ_IND_ITEMS consecutive commands (load_indirect), the block scans their triangle and chunk counts, then
+ * each thread writes its draws' counts and index address, and prim_base and chunk_base as exclusive prefix
+ * sums over the segment in draw order (a chunk never spans two draws, as in the chunk table of direct
+ * draws); finally the segment's num_prims, num_chunks and draw lookup pointer. */
+extern "C" __global__ void __launch_bounds__(KZ_IND_THREADS) kz_k_indirect(KzFrame f, uint32_t s) {
+  __shared__ unsigned long long warp_p[KZ_IND_THREADS / 32], warp_c[KZ_IND_THREADS / 32];
   KzSegment* seg = reinterpret_cast<KzSegment*>(f.segments) + s;
-  KzDraw* draws = reinterpret_cast<KzDraw*>(f.draws);
+  KzDraw* draws = reinterpret_cast<KzDraw*>(f.draws) + seg->first_draw;
   KzStatus* st = reinterpret_cast<KzStatus*>(f.status);
   const uint32_t n = seg->num_draws, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long prim_run = 0, chunk_run = 0;
   bool bad = false;
-  for (uint32_t base = 0; base < n; base += KZ_THREADS) {
-    const uint32_t i = base + threadIdx.x;
-    KzDraw* d = i < n ? draws + seg->first_draw + i : nullptr;
-    unsigned long long prims = 0;
-    if (d) {
-      const uint32_t* cmd = reinterpret_cast<const uint32_t*>(d->indirect);
-      uint32_t tri = cmd[0] / 3, inst = cmd[1], first = cmd[2], first_inst;
-      int32_t voff;
-      if (d->indexed) {
-        voff = (int32_t)cmd[3];
-        first_inst = cmd[4];
-      } else {
-        voff = (int32_t)first;
-        first_inst = cmd[3];
-      }
-      bool ok = (unsigned long long)first + 3ull * tri <= d->elem_limit &&
-                (unsigned long long)first_inst + inst <= d->instance_limit;
-      if (!ok) {
-        bad |= tri != 0 && inst != 0;
-        inst = 0;
-      }
-      d->tri_count = tri;
-      d->instance_count = inst;
-      d->vertex_offset = voff;
-      d->first_instance = first_inst;
-      if (d->indexed) d->ib = d->ib_base + (unsigned long long)first * (d->indexed == 1 ? 4u : 2u);
-      prims = (unsigned long long)tri * inst;
+  for (uint32_t base = 0; base < n; base += KZ_IND_THREADS * KZ_IND_ITEMS) {
+    const uint32_t i0 = base + threadIdx.x * KZ_IND_ITEMS;
+    IndirectCmd cmd[KZ_IND_ITEMS];
+#pragma unroll
+    for (int j = 0; j < KZ_IND_ITEMS; j++) {
+      if (i0 + j < n) cmd[j] = load_indirect(draws[i0 + j], bad);
+      else cmd[j].tri = cmd[j].inst = 0;
     }
-    const unsigned long long chunks = (prims + KZ_CHUNK - 1) / KZ_CHUNK;
-    unsigned long long ip = prims, ic = chunks;
+    unsigned long long tp = 0, tc = 0;
+#pragma unroll
+    for (int j = 0; j < KZ_IND_ITEMS; j++) {
+      unsigned long long p = (unsigned long long)cmd[j].tri * cmd[j].inst;
+      tp += p;
+      tc += (p + KZ_CHUNK - 1) / KZ_CHUNK;
+    }
+    unsigned long long ip = tp, ic = tc;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       unsigned long long a = __shfl_up_sync(0xFFFFFFFFu, ip, o), b = __shfl_up_sync(0xFFFFFFFFu, ic, o);
@@ -1940,38 +1971,74 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_indirect(KzFrame f
       }
     }
     if (lane == 31) {
-      warp_prims[warp] = ip;
-      warp_chunks[warp] = ic;
+      warp_p[warp] = ip;
+      warp_c[warp] = ic;
     }
     __syncthreads();
-    unsigned long long wp = 0, wc = 0, tp = 0, tc = 0;
-    for (uint32_t w = 0; w < KZ_THREADS / 32; w++) {
+    unsigned long long wp = 0, wc = 0, bp = 0, bc = 0;
+    for (uint32_t w = 0; w < KZ_IND_THREADS / 32; w++) {
       if (w < warp) {
-        wp += warp_prims[w];
-        wc += warp_chunks[w];
+        wp += warp_p[w];
+        wc += warp_c[w];
       }
-      tp += warp_prims[w];
-      tc += warp_chunks[w];
+      bp += warp_p[w];
+      bc += warp_c[w];
     }
-    if (d) {
-      d->prim_base = (uint32_t)min(prim_run + wp + ip - prims, 0xFFFFFFFFull);
-      d->chunk_base = (uint32_t)min(chunk_run + wc + ic - chunks, 0xFFFFFFFFull);
+    unsigned long long pb = prim_run + wp + ip - tp, cb = chunk_run + wc + ic - tc;
+#pragma unroll
+    for (int j = 0; j < KZ_IND_ITEMS; j++) {
+      if (i0 + j >= n) break;
+      KzDraw& d = draws[i0 + j];
+      const IndirectCmd& c = cmd[j];
+      unsigned long long p = (unsigned long long)c.tri * c.inst;
+      d.tri_count = c.tri;
+      d.instance_count = c.inst;
+      d.vertex_offset = c.voff;
+      d.first_instance = c.first_inst;
+      if (c.indexed) d.ib = c.ib_base + (unsigned long long)c.first * (c.indexed == 1 ? 4u : 2u);
+      d.prim_base = (uint32_t)min(pb, 0xFFFFFFFFull);
+      d.chunk_base = (uint32_t)min(cb, 0xFFFFFFFFull);
+      pb += p;
+      cb += (p + KZ_CHUNK - 1) / KZ_CHUNK;
     }
-    prim_run += tp;
-    chunk_run += tc;
+    prim_run += bp;
+    chunk_run += bc;
     __syncthreads();
   }
   bad = __syncthreads_or(bad) != 0;
   if (threadIdx.x == 0) {
     if (prim_run >= 0xFFFFFFF0ull) {
-      seg->num_prims = 0;
-      seg->num_chunks = 0;
+      prim_run = chunk_run = 0;
       atomicOr(&st->flags, (uint32_t)KZ_STATUS_INDIRECT_LIMIT);
-    } else {
-      seg->num_prims = (uint32_t)prim_run;
-      seg->num_chunks = (uint32_t)chunk_run;
     }
+    seg->num_prims = (uint32_t)prim_run;
+    seg->num_chunks = (uint32_t)chunk_run;
+    seg->draw_lut = (prim_run + 255) / 256 <= seg->lut_cap ? seg->lut_table : 0ull;
     if (bad) atomicOr(&st->flags, (uint32_t)KZ_STATUS_INDIRECT_RANGE);
+  }
+}
+
+/* after kz_k_indirect, every thread of the grid: the chunk table (KzChunk per chunk, as for direct draws)
+ * and the draw lookup (draw holding primitive 256 i) of an indirect segment, where they fit their room */
+extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_indirect_tables(KzFrame f, uint32_t s) {
+  const KzSegment& seg = reinterpret_cast<const KzSegment*>(f.segments)[s];
+  const KzDraw* draws = reinterpret_cast<const KzDraw*>(f.draws);
+  const uint32_t nc = seg.num_chunks <= seg.chunk_cap ? seg.num_chunks : 0u;
+  const uint32_t nl = seg.draw_lut ? (seg.num_prims + 255) / 256 : 0u;
+  KzChunk* chunk_table = reinterpret_cast<KzChunk*>(seg.chunk_table);
+  uint32_t* lut = reinterpret_cast<uint32_t*>(seg.draw_lut);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < max(nc, nl); k += gridDim.x * blockDim.x) {
+    if (k < nc) {
+      const uint32_t di = draw_of_chunk(draws, seg.first_draw, seg.num_draws, k);
+      const KzDraw& d = draws[di];
+      KzChunk ch;
+      ch.draw = di;
+      ch.first = (k - d.chunk_base) * KZ_CHUNK;
+      ch.count = min((uint32_t)KZ_CHUNK, d.tri_count * d.instance_count - ch.first);
+      ch.pad = 0;
+      chunk_table[k] = ch;
+    }
+    if (k < nl) lut[k] = find_draw(draws, seg.first_draw, seg.num_draws, k * 256u);
   }
 }
 

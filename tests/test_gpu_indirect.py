@@ -120,3 +120,17 @@ def test_indirect_full_size_equals_direct(renderer, name):
     assert s0.status == 0 and s1.status == 0
     assert np.array_equal(c0, c1) and np.array_equal(d0.view(np.uint32), d1.view(np.uint32))
     assert s0.fragments == s1.fragments
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["persistent", "batched"])
+def test_indirect_beyond_table_room(renderer, mode):
+    """instanceCount 8 on the 60K-triangle sphere: 480K triangles outgrow the chunk table and draw lookup
+    sized at recording from the bound index buffer, so chunks and primitives find their draw by searching;
+    the image equals the draw recorded eight times"""
+    scene = CASES["sphere"]
+    run = render.SceneRun(renderer, scene, mode=mode, tile=16, indirect="host")
+    renderer.write_buffer(run.cmds, render.indirect_commands(scene, instances=8))
+    eight = dataclasses.replace(scene, draws=[scene.draws[0]] * 8)
+    _check(eight, *_submit(run))
+    renderer.free_command_buffer(run.cb)
