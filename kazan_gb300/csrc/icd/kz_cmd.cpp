@@ -167,9 +167,16 @@ static uint32_t fetch_limit(const CommandBuffer* cb, const KzPipe& kp, bool per_
  * from the buffer when the command buffer executes (so the buffer may be written by earlier commands or by
  * the host between submissions) */
 static void record_indirect(CommandBuffer* cb, VkBuffer buffer, VkDeviceSize offset, uint32_t draw_count,
-                            uint32_t stride, bool indexed) {
+                            uint32_t stride, bool indexed, VkBuffer count_buffer = nullptr,
+                            VkDeviceSize count_offset = 0) {
   if (!draw_state_ok(cb) || cb->pipe->rasterizer_discard || draw_count == 0) return;
   const Buffer* buf = H<Buffer>(buffer);
+  const Buffer* cbuf = H<Buffer>(count_buffer);
+  if (count_buffer && (!cbuf || (count_offset & 3) || count_offset + 4 > cbuf->size)) {
+    log_error("indirect draw count: offset %llu does not fit the count buffer", (unsigned long long)count_offset);
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
   uint32_t cmd_bytes = indexed ? 20u : 16u;
   if (draw_count == 1) stride = cmd_bytes;
   if (!buf || (offset & 3) || (stride & 3) || stride < cmd_bytes ||
@@ -183,7 +190,9 @@ static void record_indirect(CommandBuffer* cb, VkBuffer buffer, VkDeviceSize off
   int nreads = 0;
   if (!begin_draw(cb, indexed, dr, nreads)) return;
   dr.reads[nreads++] = buf->mem;
+  if (cbuf) dr.reads[nreads++] = cbuf->mem;
   KzDraw& d = dr.d;
+  if (cbuf) d.count_addr = (uint64_t)(uintptr_t)(cbuf->ptr() + count_offset);
   const KzPipe& kp = cb->pipe->pipe;
   if (indexed) {
     uint32_t isz = d.indexed == 1 ? 4u : 2u;
@@ -198,6 +207,7 @@ static void record_indirect(CommandBuffer* cb, VkBuffer buffer, VkDeviceSize off
   PassRec& pass = cb->passes[(size_t)cb->cur_pass];
   for (uint32_t i = 0; i < draw_count; i++) {
     d.indirect = (uint64_t)(uintptr_t)(buf->ptr() + offset + (VkDeviceSize)i * stride);
+    d.call_index = i;
     pass.draws.push_back(dr);
   }
 }
@@ -408,6 +418,20 @@ void VKAPI_CALL kzCmdDrawIndexedIndirect(VkCommandBuffer cbh, VkBuffer buffer, V
                                          uint32_t drawCount, uint32_t stride) {
   /* api_impl.rs:4666 vkCmdDrawIndexedIndirect: drawCount VkDrawIndexedIndirectCommand structs */
   record_indirect(H<CommandBuffer>(cbh), buffer, offset, drawCount, stride, true);
+}
+
+void VKAPI_CALL kzCmdDrawIndirectCount(VkCommandBuffer cbh, VkBuffer buffer, VkDeviceSize offset, VkBuffer countBuffer,
+                                       VkDeviceSize countBufferOffset, uint32_t maxDrawCount, uint32_t stride) {
+  /* api_impl.rs:6025 vkCmdDrawIndirectCountKHR: min(count, maxDrawCount) commands, the count read from
+   * countBuffer when the command buffer executes */
+  record_indirect(H<CommandBuffer>(cbh), buffer, offset, maxDrawCount, stride, false, countBuffer, countBufferOffset);
+}
+
+void VKAPI_CALL kzCmdDrawIndexedIndirectCount(VkCommandBuffer cbh, VkBuffer buffer, VkDeviceSize offset,
+                                              VkBuffer countBuffer, VkDeviceSize countBufferOffset,
+                                              uint32_t maxDrawCount, uint32_t stride) {
+  /* api_impl.rs:6039 vkCmdDrawIndexedIndirectCountKHR */
+  record_indirect(H<CommandBuffer>(cbh), buffer, offset, maxDrawCount, stride, true, countBuffer, countBufferOffset);
 }
 
 void VKAPI_CALL kzCmdBeginRenderPass(VkCommandBuffer cbh, const VkRenderPassBeginInfo* bi, VkSubpassContents) {

@@ -344,7 +344,7 @@ static void VKAPI_CALL kzGetPhysicalDeviceProperties(VkPhysicalDevice physicalDe
   l.subTexelPrecisionBits = 0;
   l.mipmapPrecisionBits = 0;
   l.maxDrawIndexedIndexValue = 0xFFFFFFFFu;
-  l.maxDrawIndirectCount = 1;
+  l.maxDrawIndirectCount = 0xFFFFFFFFu;
   l.maxViewports = 1;
   l.maxViewportDimensions[0] = l.maxViewportDimensions[1] = 8192;
   l.viewportBoundsRange[0] = -16384.0f;
@@ -383,6 +383,8 @@ static void VKAPI_CALL kzGetPhysicalDeviceProperties(VkPhysicalDevice physicalDe
 static void VKAPI_CALL kzGetPhysicalDeviceFeatures(VkPhysicalDevice, VkPhysicalDeviceFeatures* f) {
   std::memset(f, 0, sizeof(*f));
   f->fullDrawIndexUint32 = VK_TRUE;
+  f->multiDrawIndirect = VK_TRUE;
+  f->drawIndirectFirstInstance = VK_TRUE;
 }
 
 static void VKAPI_CALL kzGetPhysicalDeviceQueueFamilyProperties(VkPhysicalDevice, uint32_t* count,
@@ -444,11 +446,25 @@ static VkResult VKAPI_CALL kzGetPhysicalDeviceImageFormatProperties(VkPhysicalDe
   return VK_SUCCESS;
 }
 
+/* the one device extension: VK_KHR_draw_indirect_count (vkCmdDraw*IndirectCountKHR) */
+static const char* const kDeviceExtensions[] = {"VK_KHR_draw_indirect_count"};
+
 static VkResult VKAPI_CALL kzEnumerateDeviceExtensionProperties(VkPhysicalDevice, const char* layer, uint32_t* count,
-                                                                VkExtensionProperties*) {
+                                                                VkExtensionProperties* out) {
   if (layer) return VK_ERROR_LAYER_NOT_PRESENT;
-  *count = 0;
-  return VK_SUCCESS;
+  const uint32_t n = (uint32_t)(sizeof kDeviceExtensions / sizeof kDeviceExtensions[0]);
+  if (!out) {
+    *count = n;
+    return VK_SUCCESS;
+  }
+  uint32_t k = std::min(*count, n);
+  for (uint32_t i = 0; i < k; i++) {
+    std::memset(&out[i], 0, sizeof out[i]);
+    std::strncpy(out[i].extensionName, kDeviceExtensions[i], VK_MAX_EXTENSION_NAME_SIZE - 1);
+    out[i].specVersion = 1;
+  }
+  *count = k;
+  return k < n ? VK_INCOMPLETE : VK_SUCCESS;
 }
 
 static VkResult VKAPI_CALL kzEnumerateDeviceLayerProperties(VkPhysicalDevice, uint32_t* count, VkLayerProperties*) {
@@ -463,11 +479,16 @@ static VkResult VKAPI_CALL kzCreateDevice(VkPhysicalDevice physicalDevice, const
                                           const VkAllocationCallbacks*, VkDevice* out) {
   PhysicalDevice* pd = from_handle<PhysicalDevice>(physicalDevice);
   if (!ci || ci->sType != VK_STRUCTURE_TYPE_DEVICE_CREATE_INFO) return VK_ERROR_INITIALIZATION_FAILED;
-  if (ci->enabledExtensionCount) return VK_ERROR_EXTENSION_NOT_PRESENT;
+  for (uint32_t i = 0; i < ci->enabledExtensionCount; i++) {
+    bool known = false;
+    for (const char* e : kDeviceExtensions) known |= std::strcmp(ci->ppEnabledExtensionNames[i], e) == 0;
+    if (!known) return VK_ERROR_EXTENSION_NOT_PRESENT;
+  }
   if (ci->pEnabledFeatures) {
     const VkBool32* f = reinterpret_cast<const VkBool32*>(ci->pEnabledFeatures);
     for (size_t i = 0; i < sizeof(VkPhysicalDeviceFeatures) / sizeof(VkBool32); i++)
-      if (f[i] && i != 1) return VK_ERROR_FEATURE_NOT_PRESENT; /* only fullDrawIndexUint32 */
+      if (f[i] && i != 1 && i != 9 && i != 10)
+        return VK_ERROR_FEATURE_NOT_PRESENT; /* fullDrawIndexUint32, multiDrawIndirect, drawIndirectFirstInstance */
   }
   for (uint32_t i = 0; i < ci->queueCreateInfoCount; i++) {
     const VkDeviceQueueCreateInfo& q = ci->pQueueCreateInfos[i];
@@ -1095,6 +1116,10 @@ void VKAPI_CALL kzCmdPushConstants(VkCommandBuffer, VkPipelineLayout, VkShaderSt
 void VKAPI_CALL kzCmdDraw(VkCommandBuffer, uint32_t, uint32_t, uint32_t, uint32_t);
 void VKAPI_CALL kzCmdDrawIndirect(VkCommandBuffer, VkBuffer, VkDeviceSize, uint32_t, uint32_t);
 void VKAPI_CALL kzCmdDrawIndexedIndirect(VkCommandBuffer, VkBuffer, VkDeviceSize, uint32_t, uint32_t);
+void VKAPI_CALL kzCmdDrawIndirectCount(VkCommandBuffer, VkBuffer, VkDeviceSize, VkBuffer, VkDeviceSize, uint32_t,
+                                       uint32_t);
+void VKAPI_CALL kzCmdDrawIndexedIndirectCount(VkCommandBuffer, VkBuffer, VkDeviceSize, VkBuffer, VkDeviceSize,
+                                              uint32_t, uint32_t);
 void VKAPI_CALL kzCmdDrawIndexed(VkCommandBuffer, uint32_t, uint32_t, uint32_t, int32_t, uint32_t);
 void VKAPI_CALL kzCmdBeginRenderPass(VkCommandBuffer, const VkRenderPassBeginInfo*, VkSubpassContents);
 void VKAPI_CALL kzCmdEndRenderPass(VkCommandBuffer);
@@ -1207,6 +1232,10 @@ static const ProcEntry kProcs[] = {
     KZ_PROC("vkCmdDraw", kzCmdDraw),
     KZ_PROC("vkCmdDrawIndirect", kzCmdDrawIndirect),
     KZ_PROC("vkCmdDrawIndexedIndirect", kzCmdDrawIndexedIndirect),
+    KZ_PROC("vkCmdDrawIndirectCountKHR", kzCmdDrawIndirectCount),
+    KZ_PROC("vkCmdDrawIndexedIndirectCountKHR", kzCmdDrawIndexedIndirectCount),
+    KZ_PROC("vkCmdDrawIndirectCount", kzCmdDrawIndirectCount),
+    KZ_PROC("vkCmdDrawIndexedIndirectCount", kzCmdDrawIndexedIndirectCount),
     KZ_PROC("vkCmdDrawIndexed", kzCmdDrawIndexed),
     KZ_PROC("vkCmdBeginRenderPass", kzCmdBeginRenderPass),
     KZ_PROC("vkCmdEndRenderPass", kzCmdEndRenderPass),

@@ -173,7 +173,7 @@ struct DrawRec {
   uint8_t push[KZ_PUSH_BYTES];
   uint64_t triangles = 0;  /* direct draws; indirect draws count theirs on the device */
   bool indirect = false;
-  DeviceMemory* reads[KZ_MAX_BINDINGS + 2] = {};
+  DeviceMemory* reads[KZ_MAX_BINDINGS + 3] = {};
 };
 
 struct PassRec {

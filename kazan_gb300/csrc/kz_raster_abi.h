@@ -129,7 +129,9 @@ typedef struct KzDraw {
                                    per-vertex binding holds (non-indexed); a command beyond it is skipped */
   uint32_t instance_limit;      /* instances every per-instance binding holds */
   uint32_t chunk_base;          /* first chunk of the draw within its segment */
-  uint32_t pad;
+  uint32_t call_index;          /* position of the command within its vkCmdDraw*Indirect*Count call */
+  uint64_t count_addr;          /* vkCmdDraw*IndirectCount: device address of the u32 draw count (the draw is
+                                   skipped when call_index >= count); 0: every recorded command draws */
 } KzDraw;
 
 /* geometry work unit: a contiguous run of at most KZ_CHUNK triangles of one draw */

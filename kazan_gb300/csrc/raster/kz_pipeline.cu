@@ -1907,8 +1907,9 @@ struct IndirectCmd {
   unsigned long long ib_base;
 };
 
-/* loads only (read-only path), so that the loads of several commands overlap; a command whose vertices,
- * indices or instances lie past the bound buffers gets no instances (`bad` set when it would have drawn) */
+/* loads only (read-only path), so that the loads of several commands overlap; a command at or past the
+ * count of a vkCmdDraw*IndirectCount call draws nothing; a command whose vertices, indices or instances lie
+ * past the bound buffers gets no instances (`bad` set when it would have drawn) */
 __device__ __forceinline__ IndirectCmd load_indirect(const KzDraw& d, bool& bad) {
   IndirectCmd c;
   const uint32_t* cmd = reinterpret_cast<const uint32_t*>(__ldg(&d.indirect));
@@ -1924,6 +1925,8 @@ __device__ __forceinline__ IndirectCmd load_indirect(const KzDraw& d, bool& bad)
     c.first_inst = __ldg(cmd + 3);
   }
   c.ib_base = __ldg(&d.ib_base);
+  const uint32_t* count = reinterpret_cast<const uint32_t*>(__ldg(&d.count_addr));
+  if (count && __ldg(&d.call_index) >= __ldg(count)) c.tri = c.inst = 0;
   bool ok = (unsigned long long)c.first + 3ull * c.tri <= __ldg(&d.elem_limit) &&
             (unsigned long long)c.first_inst + c.inst <= __ldg(&d.instance_limit);
   if (!ok) {

@@ -343,10 +343,13 @@ class SceneRun:
     indirect: None records vkCmdDraw / vkCmdDrawIndexed; "host" records the indirect variants over a
     host-visible buffer of commands written by the host; "device" over a device-local buffer that the same
     command buffer fills with vkCmdCopyBuffer before the render pass.  Draws with their own push constants
-    become one indirect call each, the others one call of drawCount = len(draws)."""
+    become one indirect call each, the others one call of drawCount = len(draws).
+    counts: with indirect, record the vkCmdDraw*IndirectCountKHR variants instead, with maxDrawCount as
+    above and each call's draw count read from a host-visible buffer of one u32 per call (`counts` gives
+    the initial words; the test rewrites them with write_buffer(run.count_buf, ...))."""
 
     def __init__(self, r, scene, host_visible=False, mode=None, tile=None, keep_mapped=False, depth_host_visible=None,
-                 indirect=None):
+                 indirect=None, counts=None):
         self.r, self.scene = r, scene
         self.indirect = indirect
         d = r.drv
@@ -370,7 +373,11 @@ class SceneRun:
         self.layout = r.pipeline_layout(64 if scene.shader == "lambert" else 0)
         vs, fs = scene.shaders()
         self.pipe = r.pipeline(scene, self.rp, self.layout, vs, fs)
-        self.cmds = self.cmd_staging = None
+        self.cmds = self.cmd_staging = self.count_buf = None
+        if indirect is not None and counts is not None:
+            words = np.ascontiguousarray(counts, dtype=np.uint32).ravel()
+            self.count_buf = r.create_buffer(words.nbytes, vk.BUFFER_USAGE_INDIRECT, True)
+            r.write_buffer(self.count_buf, words)
         if indirect is not None:
             words = indirect_commands(scene)
             self.cmds = r.create_buffer(words.nbytes, vk.BUFFER_USAGE_INDIRECT, indirect == "host")
@@ -401,8 +408,7 @@ class SceneRun:
             d.vkCmdBindIndexBuffer(cb, self.ib.handle, 0, vk.INDEX_TYPE_UINT32)
         per_draw_push = any(dr.mvp is not None for dr in s.draws)
         if self.indirect is not None and not per_draw_push:
-            call = d.vkCmdDrawIndexedIndirect if s.indexed else d.vkCmdDrawIndirect
-            call(cb, self.cmds.handle, 0, len(s.draws), INDIRECT_STRIDE)
+            self._indirect_call(cb, 0, 0, len(s.draws))
         for i, dr in enumerate(s.draws):
             if self.indirect is not None and not per_draw_push:
                 break
@@ -410,8 +416,7 @@ class SceneRun:
                 m = np.ascontiguousarray(dr.mvp, dtype=np.float32)
                 d.vkCmdPushConstants(cb, self.layout, vk.SHADER_STAGE_VERTEX, 0, 64, m.ctypes.data)
             if self.indirect is not None:
-                call = d.vkCmdDrawIndexedIndirect if s.indexed else d.vkCmdDrawIndirect
-                call(cb, self.cmds.handle, i * INDIRECT_STRIDE, 1, INDIRECT_STRIDE)
+                self._indirect_call(cb, i, i * INDIRECT_STRIDE, 1)
             elif s.indexed:
                 d.vkCmdDrawIndexed(cb, 3 * dr.count, 1, dr.first, dr.vertex_offset, 0)
             else:
@@ -419,6 +424,15 @@ class SceneRun:
         d.vkCmdEndRenderPass(cb)
         check("vkEndCommandBuffer", d.vkEndCommandBuffer(cb))
         return cb
+
+    def _indirect_call(self, cb, call, offset, draws):
+        d, s = self.r.drv, self.scene
+        if self.count_buf is None:
+            fn = d.vkCmdDrawIndexedIndirect if s.indexed else d.vkCmdDrawIndirect
+            fn(cb, self.cmds.handle, offset, draws, INDIRECT_STRIDE)
+        else:
+            fn = d.vkCmdDrawIndexedIndirectCountKHR if s.indexed else d.vkCmdDrawIndirectCountKHR
+            fn(cb, self.cmds.handle, offset, self.count_buf.handle, 4 * call, draws, INDIRECT_STRIDE)
 
     def submit(self, wait=True):
         if wait:

@@ -482,6 +482,10 @@ class VkRenderPassBeginInfo(Structure):
                 ("renderArea", VkRect2D), ("clearValueCount", c_uint32), ("pClearValues", POINTER(VkClearValue))]
 
 
+class VkExtensionProperties(Structure):
+    _fields_ = [("extensionName", ctypes.c_char * 256), ("specVersion", c_uint32)]
+
+
 class VkBufferCopy(Structure):
     _fields_ = [("srcOffset", c_uint64), ("dstOffset", c_uint64), ("size", c_uint64)]
 
@@ -561,6 +565,10 @@ _PROTOS = {
     "vkCmdDrawIndexed": (None, [H, c_uint32, c_uint32, c_uint32, c_int32, c_uint32]),
     "vkCmdDrawIndirect": (None, [H, H, c_uint64, c_uint32, c_uint32]),
     "vkCmdDrawIndexedIndirect": (None, [H, H, c_uint64, c_uint32, c_uint32]),
+    "vkEnumerateDeviceExtensionProperties": (c_int, [H, ctypes.c_char_p, P(c_uint32), P(VkExtensionProperties)]),
+    "vkGetPhysicalDeviceFeatures": (None, [H, P(c_uint32)]),
+    "vkCmdDrawIndirectCountKHR": (None, [H, H, c_uint64, H, c_uint64, c_uint32, c_uint32]),
+    "vkCmdDrawIndexedIndirectCountKHR": (None, [H, H, c_uint64, H, c_uint64, c_uint32, c_uint32]),
     "vkCmdBeginRenderPass": (None, [H, P(VkRenderPassBeginInfo), c_int]),
     "vkCmdEndRenderPass": (None, [H]),
     "vkCmdClearColorImage": (None, [H, H, c_int, P(VkClearColorValue), c_uint32, P(VkImageSubresourceRange)]),

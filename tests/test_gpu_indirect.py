@@ -4,12 +4,13 @@ the same draws bit for bit, whether the commands were written by the host or by 
 the same command buffer, in every launch schedule; rewriting the commands between submissions changes the
 image accordingly; and a command that reaches past its bound buffers is skipped with a status bit instead of
 being read."""
+import ctypes
 import dataclasses
 
 import numpy as np
 import pytest
 
-from kazan_gb300 import render, scenes
+from kazan_gb300 import render, scenes, vk
 from oracle import kz_oracle
 
 from scene_cases import guard_band_and_near, equal_depth_ties, small_cases
@@ -134,3 +135,40 @@ def test_indirect_beyond_table_room(renderer, mode):
     eight = dataclasses.replace(scene, draws=[scene.draws[0]] * 8)
     _check(eight, *_submit(run))
     renderer.free_command_buffer(run.cb)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["persistent", "batched"])
+def test_indirect_count_from_buffer(renderer, mode):
+    """vkCmdDraw*IndirectCountKHR: the draw count is read from a buffer at execution and capped by
+    maxDrawCount; one call of three non-indexed draws, then 48 indexed calls of at most one draw each"""
+    scene = CASES["soup_split"]
+    run = render.SceneRun(renderer, scene, mode=mode, tile=16, indirect="host", counts=[2])
+    _check(dataclasses.replace(scene, draws=scene.draws[:2]), *_submit(run))
+    for count, keep in ((0, 0), (7, 3), (3, 3), (1, 1)):
+        renderer.write_buffer(run.count_buf, np.array([count], dtype=np.uint32))
+        _check(dataclasses.replace(scene, draws=scene.draws[:keep]), *_submit(run))
+    renderer.free_command_buffer(run.cb)
+
+    scene = CASES["batched"]
+    counts = np.arange(len(scene.draws), dtype=np.uint32) % 2 == 0
+    run = render.SceneRun(renderer, scene, mode=mode, tile=16, indirect="device", counts=counts.astype(np.uint32))
+    _check(dataclasses.replace(scene, draws=scene.draws[0::2]), *_submit(run))
+    renderer.write_buffer(run.count_buf, np.full(len(scene.draws), 5, dtype=np.uint32))
+    _check(scene, *_submit(run))
+    renderer.free_command_buffer(run.cb)
+
+
+@pytest.mark.gpu
+def test_device_advertises_indirect_draws(renderer):
+    """VK_KHR_draw_indirect_count is listed (count query, then fill), and multiDrawIndirect and
+    drawIndirectFirstInstance are reported as features"""
+    d = renderer.drv
+    n = ctypes.c_uint32(0)
+    assert d.vkEnumerateDeviceExtensionProperties(renderer.physical, None, ctypes.byref(n), None) == vk.VK_SUCCESS
+    props = (vk.VkExtensionProperties * n.value)()
+    assert d.vkEnumerateDeviceExtensionProperties(renderer.physical, None, ctypes.byref(n), props) == vk.VK_SUCCESS
+    assert b"VK_KHR_draw_indirect_count" in [p.extensionName for p in props]
+    feats = (ctypes.c_uint32 * 55)()
+    d.vkGetPhysicalDeviceFeatures(renderer.physical, feats)
+    assert feats[1] == 1 and feats[9] == 1 and feats[10] == 1
