@@ -15,7 +15,10 @@
  *   vkBeginCommandBuffer :4483, vkEndCommandBuffer :4491, vkQueueSubmit :3414, vkQueueWaitIdle :3424,
  *   vkCreateFence :3653, vkWaitForFences :3689, vkCreateGraphicsPipelines :4018,
  *   vkCreatePipelineLayout :4061, vkCreateShaderModule :3946, vkAllocateMemory :3434, vkMapMemory :3488,
- *   vkCreateBuffer :3795, vkCreateImage :3851, vkBindBufferMemory2 :4975, vkBindImageMemory2 :5013.
+ *   vkCreateBuffer :3795, vkCreateImage :3851, vkBindBufferMemory2 :4975, vkBindImageMemory2 :5013,
+ *   vkCmdDrawIndirect :4655, vkCmdDrawIndexedIndirect :4666, vkCmdDrawIndirectCountKHR :6025,
+ *   vkCmdDrawIndexedIndirectCountKHR :6039 (also under the core names vkCmdDraw*IndirectCount), and
+ *   vkEnumerateDeviceExtensionProperties, which lists VK_KHR_draw_indirect_count.
  *
  * The kz* functions below have no counterpart in the reference: they expose the driver's execution
  * options and statistics to the benchmark and tests without a Vulkan extension.
