@@ -64,6 +64,27 @@ typedef struct KzVertexInputLayout {
 KZ_API size_t kzShaderEmitPtx(const void* const* vs, const void* const* fs, const KzVertexInputLayout* layouts,
                               uint32_t count, char* buf, size_t size);
 
+/* Descriptor bindings a compiled stage declares (module-scope Uniform / UniformConstant variables). */
+typedef struct KzShaderBinding {
+  uint32_t set, binding;
+  uint32_t kind;   /* 0 uniform buffer, 1 combined image sampler */
+  uint32_t count;  /* array elements */
+  uint32_t bytes;  /* uniform buffer: bytes of the block */
+} KzShaderBinding;
+/* Writes at most `max` bindings into out (may be NULL) and returns how many the stage declares. */
+KZ_API uint32_t kzShaderBindings(const void* shader, KzShaderBinding* out, uint32_t max);
+
+/* Descriptor slots of one pipeline layout: slot[set][binding] is the slot of the binding's first array
+ * element in a draw's snapshot (byte KZ_DESC_OFFSET + 32 * slot after the push constants, one 32-byte
+ * KzDescriptor per slot, kz_raster_abi.h), ~0u where the layout has no such binding. */
+typedef struct KzDescriptorSlots {
+  uint32_t slot[4][16];
+} KzDescriptorSlots;
+/* kzShaderEmitPtx for stages that read descriptors: slots[i] belongs to pipeline i (slots may be NULL). */
+KZ_API size_t kzShaderEmitPtxDescriptors(const void* const* vs, const void* const* fs,
+                                         const KzVertexInputLayout* layouts, const KzDescriptorSlots* slots,
+                                         uint32_t count, char* buf, size_t size);
+
 /* Link PTX with the relocatable pipeline-kernel object (NULL: the object built next to the library). */
 KZ_API int kzShaderLink(const char* ptx, const void* object, size_t object_size, void** out_code, char* err,
                         size_t err_size);

@@ -100,6 +100,7 @@ typedef enum VkResult {
   VK_ERROR_FORMAT_NOT_SUPPORTED = -11,
   VK_ERROR_FRAGMENTED_POOL = -12,
   VK_ERROR_UNKNOWN = -13,
+  VK_ERROR_OUT_OF_POOL_MEMORY = -1000069000,
   VK_ERROR_INVALID_SHADER_NV = -1000012000,
   VK_RESULT_MAX_ENUM = 0x7FFFFFFF
 } VkResult;
@@ -351,6 +352,7 @@ typedef VkFlags VkStencilFaceFlags;
 #define VK_COMMAND_BUFFER_USAGE_ONE_TIME_SUBMIT_BIT 0x1u
 #define VK_COMMAND_BUFFER_USAGE_SIMULTANEOUS_USE_BIT 0x4u
 #define VK_FORMAT_FEATURE_SAMPLED_IMAGE_BIT 0x1u
+#define VK_FORMAT_FEATURE_SAMPLED_IMAGE_FILTER_LINEAR_BIT 0x1000u
 #define VK_FORMAT_FEATURE_VERTEX_BUFFER_BIT 0x40u
 #define VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT 0x80u
 #define VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT 0x100u
@@ -1047,6 +1049,131 @@ typedef struct VkBindImageMemoryInfo {
   VkDeviceMemory memory;
   VkDeviceSize memoryOffset;
 } VkBindImageMemoryInfo;
+
+/* descriptor sets and samplers (vulkan-driver/src/descriptor_set.rs, sampler.rs) */
+typedef enum VkDescriptorType {
+  VK_DESCRIPTOR_TYPE_SAMPLER = 0,
+  VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER = 1,
+  VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE = 2,
+  VK_DESCRIPTOR_TYPE_STORAGE_IMAGE = 3,
+  VK_DESCRIPTOR_TYPE_UNIFORM_TEXEL_BUFFER = 4,
+  VK_DESCRIPTOR_TYPE_STORAGE_TEXEL_BUFFER = 5,
+  VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER = 6,
+  VK_DESCRIPTOR_TYPE_STORAGE_BUFFER = 7,
+  VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC = 8,
+  VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC = 9,
+  VK_DESCRIPTOR_TYPE_INPUT_ATTACHMENT = 10,
+  VK_DESCRIPTOR_TYPE_MAX_ENUM = 0x7FFFFFFF
+} VkDescriptorType;
+typedef enum VkFilter { VK_FILTER_NEAREST = 0, VK_FILTER_LINEAR = 1, VK_FILTER_MAX_ENUM = 0x7FFFFFFF } VkFilter;
+typedef enum VkSamplerMipmapMode {
+  VK_SAMPLER_MIPMAP_MODE_NEAREST = 0,
+  VK_SAMPLER_MIPMAP_MODE_LINEAR = 1,
+  VK_SAMPLER_MIPMAP_MODE_MAX_ENUM = 0x7FFFFFFF
+} VkSamplerMipmapMode;
+typedef enum VkSamplerAddressMode {
+  VK_SAMPLER_ADDRESS_MODE_REPEAT = 0,
+  VK_SAMPLER_ADDRESS_MODE_MIRRORED_REPEAT = 1,
+  VK_SAMPLER_ADDRESS_MODE_CLAMP_TO_EDGE = 2,
+  VK_SAMPLER_ADDRESS_MODE_CLAMP_TO_BORDER = 3,
+  VK_SAMPLER_ADDRESS_MODE_MIRROR_CLAMP_TO_EDGE = 4,
+  VK_SAMPLER_ADDRESS_MODE_MAX_ENUM = 0x7FFFFFFF
+} VkSamplerAddressMode;
+typedef enum VkBorderColor {
+  VK_BORDER_COLOR_FLOAT_TRANSPARENT_BLACK = 0,
+  VK_BORDER_COLOR_INT_TRANSPARENT_BLACK = 1,
+  VK_BORDER_COLOR_FLOAT_OPAQUE_BLACK = 2,
+  VK_BORDER_COLOR_INT_OPAQUE_BLACK = 3,
+  VK_BORDER_COLOR_FLOAT_OPAQUE_WHITE = 4,
+  VK_BORDER_COLOR_INT_OPAQUE_WHITE = 5,
+  VK_BORDER_COLOR_MAX_ENUM = 0x7FFFFFFF
+} VkBorderColor;
+typedef struct VkSamplerCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkFlags flags;
+  VkFilter magFilter;
+  VkFilter minFilter;
+  VkSamplerMipmapMode mipmapMode;
+  VkSamplerAddressMode addressModeU;
+  VkSamplerAddressMode addressModeV;
+  VkSamplerAddressMode addressModeW;
+  float mipLodBias;
+  VkBool32 anisotropyEnable;
+  float maxAnisotropy;
+  VkBool32 compareEnable;
+  VkCompareOp compareOp;
+  float minLod;
+  float maxLod;
+  VkBorderColor borderColor;
+  VkBool32 unnormalizedCoordinates;
+} VkSamplerCreateInfo;
+typedef struct VkDescriptorSetLayoutBinding {
+  uint32_t binding;
+  VkDescriptorType descriptorType;
+  uint32_t descriptorCount;
+  VkFlags stageFlags;
+  const VkSampler* pImmutableSamplers;
+} VkDescriptorSetLayoutBinding;
+typedef struct VkDescriptorSetLayoutCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkFlags flags;
+  uint32_t bindingCount;
+  const VkDescriptorSetLayoutBinding* pBindings;
+} VkDescriptorSetLayoutCreateInfo;
+typedef struct VkDescriptorPoolSize {
+  VkDescriptorType type;
+  uint32_t descriptorCount;
+} VkDescriptorPoolSize;
+typedef struct VkDescriptorPoolCreateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkFlags flags;
+  uint32_t maxSets;
+  uint32_t poolSizeCount;
+  const VkDescriptorPoolSize* pPoolSizes;
+} VkDescriptorPoolCreateInfo;
+typedef struct VkDescriptorSetAllocateInfo {
+  VkStructureType sType;
+  const void* pNext;
+  VkDescriptorPool descriptorPool;
+  uint32_t descriptorSetCount;
+  const VkDescriptorSetLayout* pSetLayouts;
+} VkDescriptorSetAllocateInfo;
+typedef struct VkDescriptorImageInfo {
+  VkSampler sampler;
+  VkImageView imageView;
+  VkImageLayout imageLayout;
+} VkDescriptorImageInfo;
+typedef struct VkDescriptorBufferInfo {
+  VkBuffer buffer;
+  VkDeviceSize offset;
+  VkDeviceSize range;
+} VkDescriptorBufferInfo;
+typedef struct VkWriteDescriptorSet {
+  VkStructureType sType;
+  const void* pNext;
+  VkDescriptorSet dstSet;
+  uint32_t dstBinding;
+  uint32_t dstArrayElement;
+  uint32_t descriptorCount;
+  VkDescriptorType descriptorType;
+  const VkDescriptorImageInfo* pImageInfo;
+  const VkDescriptorBufferInfo* pBufferInfo;
+  const VkBufferView* pTexelBufferView;
+} VkWriteDescriptorSet;
+typedef struct VkCopyDescriptorSet {
+  VkStructureType sType;
+  const void* pNext;
+  VkDescriptorSet srcSet;
+  uint32_t srcBinding;
+  uint32_t srcArrayElement;
+  VkDescriptorSet dstSet;
+  uint32_t dstBinding;
+  uint32_t dstArrayElement;
+  uint32_t descriptorCount;
+} VkCopyDescriptorSet;
 
 /* loader entry point type */
 typedef PFN_vkVoidFunction(VKAPI_PTR* PFN_vkGetInstanceProcAddr)(VkInstance instance, const char* pName);

@@ -79,6 +79,70 @@ static bool draw_state_ok(CommandBuffer* cb) {
   return true;
 }
 
+static uint32_t color_format(VkFormat f);
+
+/* the pipeline layout's descriptor slots from the bound sets, resolved to device addresses (dynamic offsets
+ * applied to dynamic uniform buffers, in binding order); every descriptor the shaders declare must be
+ * written: a combined image sampler with an RGBA8/BGRA8 image, a uniform buffer with a range that covers
+ * the block.  Otherwise a recording error, so that no kernel reads through an unset descriptor. */
+static bool snapshot_descriptors(CommandBuffer* cb, const Pipeline* p, DrawRec& dr) {
+  const PipelineLayoutInfo& L = *p->layout;
+  dr.desc.assign(L.slots, KzDescriptor{});
+  for (uint32_t s = 0; s < L.sets.size(); s++) {
+    const DescriptorSet* ds = cb->sets[s];
+    if (!ds) continue;
+    uint32_t dyn = 0;
+    for (const SetBinding& lb : L.sets[s]->bindings) {
+      const SetBinding* sb = ds->layout->find(lb.binding);
+      for (uint32_t e = 0; e < lb.count; e++) {
+        if (!sb || e >= sb->count) continue;
+        const DescriptorEntry& de = ds->entries[sb->first + e];
+        uint32_t dyn_off = 0;
+        if (sb->type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC) {
+          const std::vector<uint32_t>& offs = cb->dyn_offsets[s];
+          dyn_off = dyn < offs.size() ? offs[dyn] : 0;
+          dyn++;
+        }
+        if (!de.written) continue;
+        KzDescriptor& d = dr.desc[L.slot_base[s] + lb.first + e];
+        if (sb->type == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER) {
+          if (!de.view || !de.view->image || !de.view->image->mem) continue;
+          const Image* img = de.view->image;
+          d.addr = (uint64_t)(uintptr_t)img->ptr();
+          d.width = img->width;
+          d.height = img->height;
+          d.pitch = img->pitch;
+          d.format = color_format(img->format);
+          d.sampler = de.sampler;
+          dr.desc_reads.push_back(img->mem);
+        } else {
+          if (!de.buffer || !de.buffer->mem) continue;
+          VkDeviceSize off = de.offset + dyn_off;
+          VkDeviceSize range = de.range == VK_WHOLE_SIZE ? (off < de.buffer->size ? de.buffer->size - off : 0) : de.range;
+          if (off + range > de.buffer->size) continue;
+          d.addr = (uint64_t)(uintptr_t)(de.buffer->ptr() + off);
+          d.range = (uint32_t)std::min<VkDeviceSize>(range, 0xFFFFFFFFu);
+          dr.desc_reads.push_back(de.buffer->mem);
+        }
+      }
+    }
+  }
+  for (const ir::Interface::Binding& b : p->bindings) {
+    const SetBinding* lb = b.set < L.sets.size() ? L.sets[b.set]->find(b.binding) : nullptr;
+    for (uint32_t e = 0; lb && e < b.count; e++) {
+      const KzDescriptor& d = dr.desc[L.slot_base[b.set] + lb->first + e];
+      bool ok = b.kind == 1 ? d.addr && d.width && d.height && d.format != KZ_CF_NONE : d.addr && d.range >= b.bytes;
+      if (!ok) {
+        log_error("draw: set %u binding %u element %u is not bound or not written with a %s", b.set, b.binding, e,
+                  b.kind == 1 ? "RGBA8/BGRA8 image" : "buffer range covering the uniform block");
+        cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+        return false;
+      }
+    }
+  }
+  return true;
+}
+
 /* the state every draw resolves at recording: vertex buffers, index buffer, viewport transform, pixel
  * rectangle and push-constant snapshot.  False (and a recording error) for an indexed draw without an
  * index buffer. */
@@ -118,6 +182,7 @@ static bool begin_draw(CommandBuffer* cb, bool indexed, DrawRec& dr, int& nreads
   d.zmax = std::fmax(vp.minDepth, vp.maxDepth);
   draw_rect(pass.fb, pass.area, sc, vp, d.rect);
   std::memcpy(dr.push, cb->push, KZ_PUSH_BYTES);
+  if (p->layout && !snapshot_descriptors(cb, p, dr)) return false;
   return true;
 }
 
@@ -270,6 +335,10 @@ static void reset_cb(CommandBuffer* cb) {
   cb->ib = nullptr;
   cb->ib_off = 0;
   std::memset(cb->push, 0, sizeof cb->push);
+  for (int s = 0; s < KZ_MAX_DESC_SETS; s++) {
+    cb->sets[s] = nullptr;
+    cb->dyn_offsets[s].clear();
+  }
   cb->cur_pass = -1;
   cb->passes.clear();
   cb->ops.clear();
@@ -406,6 +475,26 @@ void VKAPI_CALL kzCmdDrawIndexed(VkCommandBuffer cbh, uint32_t indexCount, uint3
                                  int32_t vertexOffset, uint32_t firstInstance) {
   /* api_impl.rs:4643 vkCmdDrawIndexed: vertex = index[firstIndex + k] + vertexOffset */
   record_draw(H<CommandBuffer>(cbh), indexCount / 3, instanceCount, firstInstance, true, firstIndex, vertexOffset);
+}
+
+void VKAPI_CALL kzCmdBindDescriptorSets(VkCommandBuffer cbh, VkPipelineBindPoint bp, VkPipelineLayout,
+                                        uint32_t firstSet, uint32_t count, const VkDescriptorSet* sets,
+                                        uint32_t dynCount, const uint32_t* dynOffsets) {
+  /* api_impl.rs:4597 vkCmdBindDescriptorSets: each set consumes as many dynamic offsets as it has dynamic
+   * uniform buffers, in order */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  if (bp != VK_PIPELINE_BIND_POINT_GRAPHICS || firstSet + count > KZ_MAX_DESC_SETS) {
+    cb->record_error = VK_ERROR_FEATURE_NOT_PRESENT;
+    return;
+  }
+  uint32_t used = 0;
+  for (uint32_t i = 0; i < count; i++) {
+    DescriptorSet* s = H<DescriptorSet>(sets[i]);
+    cb->sets[firstSet + i] = s;
+    std::vector<uint32_t>& offs = cb->dyn_offsets[firstSet + i];
+    offs.clear();
+    for (uint32_t k = 0; s && k < s->layout->dynamic && used < dynCount; k++) offs.push_back(dynOffsets[used++]);
+  }
 }
 
 void VKAPI_CALL kzCmdDrawIndirect(VkCommandBuffer cbh, VkBuffer buffer, VkDeviceSize offset, uint32_t drawCount,
@@ -950,8 +1039,15 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
         d.rect[3] = std::min(d.rect[3], (int32_t)s.height);
         d.pipe = pipe_of(dr.pipe, cb->have_blend_const ? cb->blend_const : nullptr);
         d.prim_base = (uint32_t)prims;
+        /* the draw's snapshot: push constants, then its descriptors, padded to whole KZ_PUSH_BYTES units */
         d.push_index = (uint32_t)(low.push.size() / KZ_PUSH_BYTES);
         low.push.insert(low.push.end(), dr.push, dr.push + KZ_PUSH_BYTES);
+        if (!dr.desc.empty()) {
+          const uint8_t* db = reinterpret_cast<const uint8_t*>(dr.desc.data());
+          low.push.insert(low.push.end(), db, db + dr.desc.size() * sizeof(KzDescriptor));
+          low.push.resize(align_up(low.push.size(), KZ_PUSH_BYTES), 0);
+        }
+        for (DeviceMemory* m : dr.desc_reads) add_unique(low.reads, m);
         uint32_t di = (uint32_t)low.draws.size();
         for (uint64_t c = 0; !dr.indirect && c < dr.triangles; c += KZ_CHUNK) {
           KzChunk ch;

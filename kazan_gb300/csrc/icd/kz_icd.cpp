@@ -7,6 +7,7 @@
  * Invalid usage that the reference answers with a panic is answered here with a VkResult error and a
  * message on stderr, never with an abort of the host process.
  */
+#include <algorithm>
 #include "kz_icd.h"
 
 #include <dlfcn.h>
@@ -125,6 +126,10 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
     }
     for (uint32_t b = 0; b < KZ_MAX_BINDINGS; b++) l.stride[b] = p->pipe.binding_stride[b];
     l.instanced = p->pipe.binding_instanced;
+    if (p->layout)
+      for (size_t s = 0; s < p->layout->sets.size(); s++)
+        for (const SetBinding& b : p->layout->sets[s]->bindings)
+          l.desc_slot[s][b.binding] = p->layout->slot_base[s] + b.first;
     layouts.push_back(l);
   }
   std::string ptx = ptx::module_text(vs, fs, layouts);
@@ -325,13 +330,19 @@ static void VKAPI_CALL kzGetPhysicalDeviceProperties(VkPhysicalDevice physicalDe
   l.maxImageDimensionCube = 1;
   l.maxImageArrayLayers = 1;
   l.maxTexelBufferElements = 0;
-  l.maxUniformBufferRange = 0;
+  l.maxUniformBufferRange = 65536;
   l.maxStorageBufferRange = 0;
   l.maxPushConstantsSize = KZ_PUSH_BYTES;
   l.maxMemoryAllocationCount = 1u << 20;
-  l.maxSamplerAllocationCount = 0;
+  l.maxSamplerAllocationCount = 1u << 16;
   l.bufferImageGranularity = 1;
-  l.maxBoundDescriptorSets = 0;
+  l.maxBoundDescriptorSets = KZ_MAX_DESC_SETS;
+  l.maxPerStageDescriptorSamplers = l.maxPerStageDescriptorSampledImages = KZ_MAX_DESC_SLOTS;
+  l.maxPerStageDescriptorUniformBuffers = KZ_MAX_DESC_SLOTS;
+  l.maxPerStageResources = KZ_MAX_DESC_SLOTS;
+  l.maxDescriptorSetSamplers = l.maxDescriptorSetSampledImages = KZ_MAX_DESC_SLOTS;
+  l.maxDescriptorSetUniformBuffers = KZ_MAX_DESC_SLOTS;
+  l.maxDescriptorSetUniformBuffersDynamic = KZ_MAX_DESC_SLOTS;
   l.maxVertexInputAttributes = KZ_MAX_VS_INPUTS;
   l.maxVertexInputBindings = KZ_MAX_BINDINGS;
   l.maxVertexInputAttributeOffset = 2047;
@@ -352,7 +363,7 @@ static void VKAPI_CALL kzGetPhysicalDeviceProperties(VkPhysicalDevice physicalDe
   l.viewportSubPixelBits = 0;
   l.minMemoryMapAlignment = 128;
   l.minTexelBufferOffsetAlignment = 64;
-  l.minUniformBufferOffsetAlignment = 64;
+  l.minUniformBufferOffsetAlignment = 16;
   l.minStorageBufferOffsetAlignment = 64;
   l.maxFramebufferWidth = 8192;
   l.maxFramebufferHeight = 8192;
@@ -422,7 +433,8 @@ static void VKAPI_CALL kzGetPhysicalDeviceFormatProperties(VkPhysicalDevice, VkF
       /* fall through */
     case VK_FORMAT_B8G8R8A8_UNORM:
       p->optimalTilingFeatures = p->linearTilingFeatures =
-          VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT | VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT | xfer;
+          VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT | VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT | xfer |
+          VK_FORMAT_FEATURE_SAMPLED_IMAGE_BIT | VK_FORMAT_FEATURE_SAMPLED_IMAGE_FILTER_LINEAR_BIT;
       break;
     case VK_FORMAT_D32_SFLOAT:
       p->optimalTilingFeatures = p->linearTilingFeatures = VK_FORMAT_FEATURE_DEPTH_STENCIL_ATTACHMENT_BIT | xfer;
@@ -843,12 +855,213 @@ static void VKAPI_CALL kzDestroyPipelineCache(VkDevice, VkPipelineCache c, const
   delete from_handle<PipelineCache>(c);
 }
 
+/* ------------------------------------------------------------------------------------------------ */
+/* samplers and descriptor sets (api_impl.rs:4165-4339, descriptor_set.rs, sampler.rs)               */
+
+static VkResult VKAPI_CALL kzCreateSampler(VkDevice, const VkSamplerCreateInfo* ci, const VkAllocationCallbacks*,
+                                           VkSampler* out) {
+  /* api_impl.rs:4165 vkCreateSampler.  Images have one mip level, so the level of detail selects only
+   * between the min and mag filters: the driver takes samplers whose two filters agree, without
+   * anisotropy or depth compare */
+  if (!ci || ci->sType != VK_STRUCTURE_TYPE_SAMPLER_CREATE_INFO) return VK_ERROR_INITIALIZATION_FAILED;
+  if (ci->magFilter != ci->minFilter || ci->anisotropyEnable || ci->compareEnable || ci->addressModeU > 4 ||
+      ci->addressModeV > 4 || ci->borderColor > 5) {
+    log_error("sampler: min and mag filters must agree; anisotropy and compare are not supported");
+    return VK_ERROR_FEATURE_NOT_PRESENT;
+  }
+  Sampler* s = new Sampler();
+  s->bits = (ci->magFilter == VK_FILTER_LINEAR ? (uint32_t)KZ_SAMP_LINEAR : 0u) |
+            (ci->unnormalizedCoordinates ? (uint32_t)KZ_SAMP_UNNORMALIZED : 0u) |
+            ((uint32_t)ci->addressModeU << KZ_SAMP_ADDR_U_SHIFT) | ((uint32_t)ci->addressModeV << KZ_SAMP_ADDR_V_SHIFT) |
+            (((uint32_t)ci->borderColor / 2u) << KZ_SAMP_BORDER_SHIFT);
+  *out = to_handle<VkSampler>(s);
+  return VK_SUCCESS;
+}
+
+static void VKAPI_CALL kzDestroySampler(VkDevice, VkSampler s, const VkAllocationCallbacks*) {
+  delete from_handle<Sampler>(s);
+}
+
+static VkResult VKAPI_CALL kzCreateDescriptorSetLayout(VkDevice, const VkDescriptorSetLayoutCreateInfo* ci,
+                                                       const VkAllocationCallbacks*, VkDescriptorSetLayout* out) {
+  /* api_impl.rs:4218; uniform buffers (plain and dynamic) and combined image samplers */
+  if (!ci || ci->sType != VK_STRUCTURE_TYPE_DESCRIPTOR_SET_LAYOUT_CREATE_INFO) return VK_ERROR_INITIALIZATION_FAILED;
+  auto info = std::make_shared<SetLayoutInfo>();
+  for (uint32_t i = 0; i < ci->bindingCount; i++) {
+    const VkDescriptorSetLayoutBinding& b = ci->pBindings[i];
+    if (b.descriptorType != VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER &&
+        b.descriptorType != VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC &&
+        b.descriptorType != VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER) {
+      log_error("descriptor type %d is not supported (uniform buffers and combined image samplers are)",
+                (int)b.descriptorType);
+      return VK_ERROR_FEATURE_NOT_PRESENT;
+    }
+    if (b.binding >= KZ_MAX_DESC_BINDINGS) return VK_ERROR_FEATURE_NOT_PRESENT;
+    SetBinding sb;
+    sb.binding = b.binding;
+    sb.type = b.descriptorType;
+    sb.count = b.descriptorCount;
+    if (b.descriptorType == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER && b.pImmutableSamplers)
+      for (uint32_t k = 0; k < b.descriptorCount; k++) sb.immutable.push_back(from_handle<Sampler>(b.pImmutableSamplers[k])->bits);
+    info->bindings.push_back(sb);
+  }
+  std::sort(info->bindings.begin(), info->bindings.end(),
+            [](const SetBinding& a, const SetBinding& b) { return a.binding < b.binding; });
+  for (SetBinding& b : info->bindings) {
+    b.first = info->descriptors;
+    info->descriptors += b.count;
+    if (b.type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC) info->dynamic += b.count;
+  }
+  if (info->descriptors > KZ_MAX_DESC_SLOTS) return VK_ERROR_FEATURE_NOT_PRESENT;
+  DescriptorSetLayout* l = new DescriptorSetLayout();
+  l->info = info;
+  *out = to_handle<VkDescriptorSetLayout>(l);
+  return VK_SUCCESS;
+}
+
+static void VKAPI_CALL kzDestroyDescriptorSetLayout(VkDevice, VkDescriptorSetLayout l, const VkAllocationCallbacks*) {
+  delete from_handle<DescriptorSetLayout>(l);
+}
+
+static VkResult VKAPI_CALL kzCreateDescriptorPool(VkDevice, const VkDescriptorPoolCreateInfo* ci,
+                                                  const VkAllocationCallbacks*, VkDescriptorPool* out) {
+  /* api_impl.rs:4258 */
+  if (!ci || ci->sType != VK_STRUCTURE_TYPE_DESCRIPTOR_POOL_CREATE_INFO) return VK_ERROR_INITIALIZATION_FAILED;
+  DescriptorPool* p = new DescriptorPool();
+  p->max_sets = ci->maxSets;
+  *out = to_handle<VkDescriptorPool>(p);
+  return VK_SUCCESS;
+}
+
+static void free_pool_sets(DescriptorPool* p) {
+  for (DescriptorSet* s : p->sets) delete s;
+  p->sets.clear();
+}
+
+static void VKAPI_CALL kzDestroyDescriptorPool(VkDevice, VkDescriptorPool h, const VkAllocationCallbacks*) {
+  DescriptorPool* p = from_handle<DescriptorPool>(h);
+  if (!p) return;
+  free_pool_sets(p);
+  delete p;
+}
+
+static VkResult VKAPI_CALL kzResetDescriptorPool(VkDevice, VkDescriptorPool h, VkFlags) {
+  /* api_impl.rs:4282 */
+  free_pool_sets(from_handle<DescriptorPool>(h));
+  return VK_SUCCESS;
+}
+
+static VkResult VKAPI_CALL kzAllocateDescriptorSets(VkDevice, const VkDescriptorSetAllocateInfo* ai,
+                                                    VkDescriptorSet* out) {
+  /* api_impl.rs:4292: every set or none */
+  if (!ai || ai->sType != VK_STRUCTURE_TYPE_DESCRIPTOR_SET_ALLOCATE_INFO) return VK_ERROR_INITIALIZATION_FAILED;
+  DescriptorPool* p = from_handle<DescriptorPool>(ai->descriptorPool);
+  if (p->sets.size() + ai->descriptorSetCount > p->max_sets) {
+    for (uint32_t i = 0; i < ai->descriptorSetCount; i++) out[i] = nullptr;
+    return VK_ERROR_OUT_OF_POOL_MEMORY;
+  }
+  for (uint32_t i = 0; i < ai->descriptorSetCount; i++) {
+    DescriptorSet* s = new DescriptorSet();
+    s->layout = from_handle<DescriptorSetLayout>(ai->pSetLayouts[i])->info;
+    s->entries.resize(s->layout->descriptors);
+    for (const SetBinding& b : s->layout->bindings)
+      for (uint32_t k = 0; k < b.count && k < b.immutable.size(); k++) s->entries[b.first + k].sampler = b.immutable[k];
+    s->pool = p;
+    p->sets.push_back(s);
+    out[i] = to_handle<VkDescriptorSet>(s);
+  }
+  return VK_SUCCESS;
+}
+
+static VkResult VKAPI_CALL kzFreeDescriptorSets(VkDevice, VkDescriptorPool h, uint32_t n, const VkDescriptorSet* sets) {
+  /* api_impl.rs:4326 */
+  DescriptorPool* p = from_handle<DescriptorPool>(h);
+  for (uint32_t i = 0; i < n; i++) {
+    DescriptorSet* s = from_handle<DescriptorSet>(sets[i]);
+    if (!s) continue;
+    p->sets.erase(std::remove(p->sets.begin(), p->sets.end(), s), p->sets.end());
+    delete s;
+  }
+  return VK_SUCCESS;
+}
+
+/* the descriptors [element, element + count) of `binding` and, past its end, of the following bindings
+ * (array element 0 on), as vkUpdateDescriptorSets (api_impl.rs:4339-4370) walks them; calls f(entry index) */
+template <class F>
+static bool walk_descriptors(const SetLayoutInfo& L, uint32_t binding, uint32_t element, uint32_t count, F f) {
+  size_t bi = 0;
+  while (bi < L.bindings.size() && L.bindings[bi].binding != binding) bi++;
+  while (count) {
+    if (bi >= L.bindings.size()) return false;
+    const SetBinding& b = L.bindings[bi];
+    if (element >= b.count) {
+      element -= b.count;
+      bi++;
+      continue;
+    }
+    uint32_t n = std::min(count, b.count - element);
+    for (uint32_t k = 0; k < n; k++) f(b.first + element + k, b);
+    count -= n;
+    element = 0;
+    bi++;
+  }
+  return true;
+}
+
+static void VKAPI_CALL kzUpdateDescriptorSets(VkDevice, uint32_t nw, const VkWriteDescriptorSet* writes, uint32_t nc,
+                                              const VkCopyDescriptorSet* copies) {
+  for (uint32_t i = 0; i < nw; i++) {
+    const VkWriteDescriptorSet& w = writes[i];
+    DescriptorSet* s = from_handle<DescriptorSet>(w.dstSet);
+    uint32_t k = 0;
+    bool ok = walk_descriptors(*s->layout, w.dstBinding, w.dstArrayElement, w.descriptorCount,
+                               [&](uint32_t e, const SetBinding& b) {
+                                 DescriptorEntry& d = s->entries[e];
+                                 if (b.type != w.descriptorType) return;
+                                 d.written = true;
+                                 if (w.descriptorType == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER) {
+                                   d.view = from_handle<ImageView>(w.pImageInfo[k].imageView);
+                                   if (b.immutable.empty())
+                                     d.sampler = from_handle<Sampler>(w.pImageInfo[k].sampler)->bits;
+                                 } else {
+                                   d.buffer = from_handle<Buffer>(w.pBufferInfo[k].buffer);
+                                   d.offset = w.pBufferInfo[k].offset;
+                                   d.range = w.pBufferInfo[k].range;
+                                 }
+                                 k++;
+                               });
+    if (!ok) log_error("vkUpdateDescriptorSets: write past the last binding of the set");
+  }
+  for (uint32_t i = 0; i < nc; i++) {
+    const VkCopyDescriptorSet& c = copies[i];
+    DescriptorSet* src = from_handle<DescriptorSet>(c.srcSet);
+    DescriptorSet* dst = from_handle<DescriptorSet>(c.dstSet);
+    std::vector<DescriptorEntry> tmp;
+    walk_descriptors(*src->layout, c.srcBinding, c.srcArrayElement, c.descriptorCount,
+                     [&](uint32_t e, const SetBinding&) { tmp.push_back(src->entries[e]); });
+    size_t k = 0;
+    walk_descriptors(*dst->layout, c.dstBinding, c.dstArrayElement, c.descriptorCount,
+                     [&](uint32_t e, const SetBinding&) {
+                       if (k < tmp.size()) dst->entries[e] = tmp[k++];
+                     });
+  }
+}
+
 static VkResult VKAPI_CALL kzCreatePipelineLayout(VkDevice, const VkPipelineLayoutCreateInfo* ci,
                                                   const VkAllocationCallbacks*, VkPipelineLayout* out) {
-  /* api_impl.rs:4061 vkCreatePipelineLayout; push_constants_size (:4076-4080) = end of the last range */
+  /* api_impl.rs:4061 vkCreatePipelineLayout; push_constants_size (:4076-4080) = end of the last range;
+   * descriptor slots numbered set by set (sets in order, each set's descriptors in binding order) */
   if (!ci || ci->sType != VK_STRUCTURE_TYPE_PIPELINE_LAYOUT_CREATE_INFO) return VK_ERROR_INITIALIZATION_FAILED;
-  if (ci->setLayoutCount) return VK_ERROR_FEATURE_NOT_PRESENT;
+  if (ci->setLayoutCount > KZ_MAX_DESC_SETS) return VK_ERROR_FEATURE_NOT_PRESENT;
+  auto info = std::make_shared<PipelineLayoutInfo>();
+  for (uint32_t i = 0; i < ci->setLayoutCount; i++) {
+    info->slot_base[i] = info->slots;
+    info->sets.push_back(from_handle<DescriptorSetLayout>(ci->pSetLayouts[i])->info);
+    info->slots += info->sets.back()->descriptors;
+  }
+  if (info->slots > KZ_MAX_DESC_SLOTS) return VK_ERROR_FEATURE_NOT_PRESENT;
   PipelineLayout* l = new PipelineLayout();
+  if (info->slots) l->info = info;
   for (uint32_t i = 0; i < ci->pushConstantRangeCount; i++) {
     uint32_t end = ci->pPushConstantRanges[i].offset + ci->pPushConstantRanges[i].size;
     if (end > l->push_size) l->push_size = end;
@@ -980,6 +1193,27 @@ static VkResult create_graphics_pipeline(const VkGraphicsPipelineCreateInfo& ci,
       kp.write_mask = a.colorWriteMask;
     }
     for (int k = 0; k < 4; k++) kp.blend_const[k] = cb.blendConstants[k];
+  }
+  /* descriptor bindings the stages declare: each must be in the layout with a matching type and at least
+   * as many array elements */
+  PipelineLayout* pl = from_handle<PipelineLayout>(ci.layout);
+  if (pl) p->layout = pl->info;
+  for (const ir::Shader* sh : {p->vs.get(), p->fs.get()}) {
+    if (!sh) continue;
+    for (const ir::Interface::Binding& b : sh->iface.bindings) {
+      const SetBinding* sb = p->layout && b.set < p->layout->sets.size() ? p->layout->sets[b.set]->find(b.binding)
+                                                                         : nullptr;
+      bool ok = sb && sb->count >= b.count &&
+                (b.kind == 1 ? sb->type == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER
+                             : (sb->type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER ||
+                                sb->type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC));
+      if (!ok) {
+        log_error("pipeline: set %u binding %u of the shaders is missing from the pipeline layout or has another type",
+                  b.set, b.binding);
+        r = VK_ERROR_INITIALIZATION_FAILED;
+      }
+      p->bindings.push_back(b);
+    }
   }
   /* interface between the stages */
   const ir::Interface& vif = p->vs->iface;
@@ -1115,6 +1349,8 @@ void VKAPI_CALL kzCmdPushConstants(VkCommandBuffer, VkPipelineLayout, VkShaderSt
                                    const void*);
 void VKAPI_CALL kzCmdDraw(VkCommandBuffer, uint32_t, uint32_t, uint32_t, uint32_t);
 void VKAPI_CALL kzCmdDrawIndirect(VkCommandBuffer, VkBuffer, VkDeviceSize, uint32_t, uint32_t);
+void VKAPI_CALL kzCmdBindDescriptorSets(VkCommandBuffer, VkPipelineBindPoint, VkPipelineLayout, uint32_t, uint32_t,
+                                        const VkDescriptorSet*, uint32_t, const uint32_t*);
 void VKAPI_CALL kzCmdDrawIndexedIndirect(VkCommandBuffer, VkBuffer, VkDeviceSize, uint32_t, uint32_t);
 void VKAPI_CALL kzCmdDrawIndirectCount(VkCommandBuffer, VkBuffer, VkDeviceSize, VkBuffer, VkDeviceSize, uint32_t,
                                        uint32_t);
@@ -1204,6 +1440,17 @@ static const ProcEntry kProcs[] = {
     KZ_PROC("vkCreatePipelineCache", kzCreatePipelineCache),
     KZ_PROC("vkDestroyPipelineCache", kzDestroyPipelineCache),
     KZ_PROC("vkCreatePipelineLayout", kzCreatePipelineLayout),
+    KZ_PROC("vkCreateSampler", kzCreateSampler),
+    KZ_PROC("vkDestroySampler", kzDestroySampler),
+    KZ_PROC("vkCreateDescriptorSetLayout", kzCreateDescriptorSetLayout),
+    KZ_PROC("vkDestroyDescriptorSetLayout", kzDestroyDescriptorSetLayout),
+    KZ_PROC("vkCreateDescriptorPool", kzCreateDescriptorPool),
+    KZ_PROC("vkDestroyDescriptorPool", kzDestroyDescriptorPool),
+    KZ_PROC("vkResetDescriptorPool", kzResetDescriptorPool),
+    KZ_PROC("vkAllocateDescriptorSets", kzAllocateDescriptorSets),
+    KZ_PROC("vkFreeDescriptorSets", kzFreeDescriptorSets),
+    KZ_PROC("vkUpdateDescriptorSets", kzUpdateDescriptorSets),
+    KZ_PROC("vkCmdBindDescriptorSets", kzCmdBindDescriptorSets),
     KZ_PROC("vkDestroyPipelineLayout", kzDestroyPipelineLayout),
     KZ_PROC("vkCreateGraphicsPipelines", kzCreateGraphicsPipelines),
     KZ_PROC("vkDestroyPipeline", kzDestroyPipeline),

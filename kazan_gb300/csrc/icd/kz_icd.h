@@ -95,8 +95,67 @@ struct ShaderModule {
   std::vector<uint32_t> code;
 };
 
+/* ---- descriptor sets (vulkan-driver/src/descriptor_set.rs, sampler.rs) ---- */
+
+struct Sampler {
+  uint32_t bits = 0; /* KzSamplerBits */
+};
+
+/* one binding of a descriptor set layout */
+struct SetBinding {
+  uint32_t binding = 0;
+  VkDescriptorType type = VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER;
+  uint32_t count = 0;
+  uint32_t first = 0;              /* index of its first descriptor within a set */
+  std::vector<uint32_t> immutable; /* KzSamplerBits of its immutable samplers (empty: none) */
+};
+
+struct SetLayoutInfo {
+  std::vector<SetBinding> bindings; /* sorted by binding number */
+  uint32_t descriptors = 0;
+  uint32_t dynamic = 0;             /* UNIFORM_BUFFER_DYNAMIC descriptors (dynamic offsets a bind consumes) */
+  const SetBinding* find(uint32_t binding) const {
+    for (const SetBinding& b : bindings)
+      if (b.binding == binding) return &b;
+    return nullptr;
+  }
+};
+
+struct DescriptorSetLayout {
+  std::shared_ptr<SetLayoutInfo> info;
+};
+
+/* a descriptor as written; device addresses are resolved when a draw is recorded */
+struct DescriptorEntry {
+  bool written = false;
+  Buffer* buffer = nullptr;
+  VkDeviceSize offset = 0, range = 0;
+  ImageView* view = nullptr;
+  uint32_t sampler = 0; /* KzSamplerBits */
+};
+
+struct DescriptorPool;
+struct DescriptorSet {
+  std::shared_ptr<SetLayoutInfo> layout;
+  std::vector<DescriptorEntry> entries;
+  DescriptorPool* pool = nullptr;
+};
+
+struct DescriptorPool {
+  uint32_t max_sets = 0;
+  std::vector<DescriptorSet*> sets;
+};
+
+/* the descriptor slots of a pipeline layout: set s's descriptor k is slot slot_base[s] + k */
+struct PipelineLayoutInfo {
+  std::vector<std::shared_ptr<SetLayoutInfo>> sets;
+  uint32_t slot_base[KZ_MAX_DESC_SETS] = {};
+  uint32_t slots = 0;
+};
+
 struct PipelineLayout {
   uint32_t push_size = 0;
+  std::shared_ptr<PipelineLayoutInfo> info;
 };
 
 struct RenderPass {
@@ -120,6 +179,8 @@ struct Pipeline {
   bool dyn_viewport = false, dyn_scissor = false, dyn_blend = false;
   bool rasterizer_discard = false;
   int vis_key = -1; /* KzVisKey when the pipeline can be resolved order-independently, else -1 */
+  std::shared_ptr<PipelineLayoutInfo> layout;   /* descriptor slots (null: no descriptor sets) */
+  std::vector<ir::Interface::Binding> bindings; /* what the stages declare (checked at each draw) */
 };
 
 struct Fence {
@@ -174,6 +235,8 @@ struct DrawRec {
   uint64_t triangles = 0;  /* direct draws; indirect draws count theirs on the device */
   bool indirect = false;
   DeviceMemory* reads[KZ_MAX_BINDINGS + 3] = {};
+  std::vector<KzDescriptor> desc;          /* the pipeline layout's descriptor slots, resolved */
+  std::vector<DeviceMemory*> desc_reads;   /* memory behind them */
 };
 
 struct PassRec {
@@ -268,6 +331,8 @@ struct CommandBuffer : Dispatchable {
   VkDeviceSize ib_off = 0;
   VkIndexType ib_type = VK_INDEX_TYPE_UINT32;
   uint8_t push[KZ_PUSH_BYTES] = {};
+  DescriptorSet* sets[KZ_MAX_DESC_SETS] = {};
+  std::vector<uint32_t> dyn_offsets[KZ_MAX_DESC_SETS]; /* per bound set, its dynamic offsets */
   int cur_pass = -1;
   std::vector<PassRec> passes;
   std::vector<RecOp> ops;

@@ -276,4 +276,32 @@ typedef struct KzFsOut {
   uint32_t pad[3];
 } KzFsOut; /* 32 bytes */
 
+/* --- descriptors (vkUpdateDescriptorSets / vkCmdBindDescriptorSets) ---
+ * A draw's snapshot in the push area is its KZ_PUSH_BYTES of push constants followed by one KzDescriptor
+ * per descriptor slot of its pipeline layout (sets in order, bindings in increasing binding number, array
+ * elements in order), so every shader function reaches them through its `push` argument. */
+#define KZ_DESC_OFFSET KZ_PUSH_BYTES  /* byte offset of slot 0 within a draw's snapshot */
+#define KZ_MAX_DESC_SETS 4
+#define KZ_MAX_DESC_BINDINGS 16       /* binding numbers 0..15 in each set */
+#define KZ_MAX_DESC_SLOTS 64          /* descriptor slots of one pipeline layout */
+
+typedef struct KzDescriptor {
+  uint64_t addr;     /* uniform buffer: device address of the bound range (offset and dynamic offset applied);
+                        combined image sampler: device address of texel (0, 0) */
+  uint32_t range;    /* uniform buffer: bytes of the bound range */
+  uint32_t width, height;
+  uint32_t pitch;    /* image: bytes per row */
+  uint32_t format;   /* image: KzColorFormat of the texels (RGBA8 or BGRA8, UNORM) */
+  uint32_t sampler;  /* KzSamplerBits */
+} KzDescriptor;      /* 32 bytes */
+
+/* sampler state packed into KzDescriptor::sampler */
+enum KzSamplerBits {
+  KZ_SAMP_LINEAR = 1u,         /* VK_FILTER_LINEAR (else NEAREST); the sampler's min and mag filters agree */
+  KZ_SAMP_UNNORMALIZED = 2u,   /* unnormalizedCoordinates */
+  KZ_SAMP_ADDR_U_SHIFT = 4,    /* bits 4..6: VkSamplerAddressMode for u */
+  KZ_SAMP_ADDR_V_SHIFT = 8,    /* bits 8..10: for v */
+  KZ_SAMP_BORDER_SHIFT = 12    /* bits 12..13: 0 transparent black, 1 opaque black, 2 opaque white */
+};
+
 #endif /* KZ_RASTER_ABI_H */

@@ -73,8 +73,27 @@ extern "C" KZ_API void kzShaderInfo(const void* shader, KzShaderInfo* out) {
 
 extern "C" KZ_API void kzShaderDestroy(void* shader) { delete static_cast<kz::ir::Shader*>(shader); }
 
+extern "C" KZ_API uint32_t kzShaderBindings(const void* shader, KzShaderBinding* out, uint32_t max) {
+  const kz::ir::Shader* s = static_cast<const kz::ir::Shader*>(shader);
+  const auto& b = s->iface.bindings;
+  for (uint32_t i = 0; out && i < max && i < b.size(); i++) {
+    out[i].set = b[i].set;
+    out[i].binding = b[i].binding;
+    out[i].kind = b[i].kind;
+    out[i].count = b[i].count;
+    out[i].bytes = b[i].bytes;
+  }
+  return (uint32_t)b.size();
+}
+
 extern "C" KZ_API size_t kzShaderEmitPtx(const void* const* vs, const void* const* fs,
                                          const KzVertexInputLayout* layouts, uint32_t count, char* buf, size_t size) {
+  return kzShaderEmitPtxDescriptors(vs, fs, layouts, nullptr, count, buf, size);
+}
+
+extern "C" KZ_API size_t kzShaderEmitPtxDescriptors(const void* const* vs, const void* const* fs,
+                                                    const KzVertexInputLayout* layouts, const KzDescriptorSlots* slots,
+                                                    uint32_t count, char* buf, size_t size) {
   std::vector<const kz::ir::Shader*> v, f;
   std::vector<kz::ptx::VertexLayout> lay;
   for (uint32_t i = 0; i < count; i++) {
@@ -93,6 +112,9 @@ extern "C" KZ_API size_t kzShaderEmitPtx(const void* const* vs, const void* cons
       }
       l.instanced = src.instanced;
     }
+    if (slots)
+      for (uint32_t s = 0; s < 4; s++)
+        for (uint32_t b = 0; b < 16; b++) l.desc_slot[s][b] = slots[i].slot[s][b];
     lay.push_back(l);
   }
   std::string ptx = kz::ptx::module_text(v, f, lay);

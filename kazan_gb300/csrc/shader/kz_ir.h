@@ -16,6 +16,11 @@
 #include <string>
 #include <vector>
 
+#include "../kz_raster_abi.h"
+
+#define KZ_IR_MAX_SETS KZ_MAX_DESC_SETS
+#define KZ_IR_MAX_BINDINGS KZ_MAX_DESC_BINDINGS
+
 namespace kz {
 namespace ir {
 
@@ -27,6 +32,11 @@ enum class Op : uint8_t {
   LdIn,    /* dst = 32-bit load from the stage input block at byte offset imm */
   LdPush,  /* dst = 32-bit load from the push-constant block at byte offset imm */
   StOut,   /* 32-bit store of a to the stage output block at byte offset imm */
+  LdUbo,   /* dst = 32-bit load from the uniform buffer of binding imm2 (set << 16 | binding) at byte offset
+              imm, plus the byte offset in register a when a >= 0 */
+  Tex,     /* dst..dst+3 (f32 registers allocated in a row) = the combined image sampler of binding imm2,
+              array element imm (plus register c when c >= 0), sampled at (a, b) */
+  TexFetch,/* dst..dst+3 = texel (a, b) (integers; outside the image: 0) of binding imm2, element imm (+ c) */
   FAdd, FSub, FMul, FDiv, FFma, FMin, FMax, FNeg, FAbs, FSqrt, FFloor, FCeil, FTrunc, FRoundEven,
   FSin, FCos, FEx2, FLg2,
   IAdd, ISub, IMul, UDiv, SDiv, URem, SRem, And, Or, Xor, Not, Shl, Shr, Sar, INeg,
@@ -52,6 +62,7 @@ struct Inst {
   Ty ty = Ty::F32;  /* type of dst (or of the operands for stores/compares) */
   int32_t dst = -1, a = -1, b = -1, c = -1;
   uint32_t imm = 0;
+  uint32_t imm2 = 0;
 };
 
 struct Function {
@@ -82,6 +93,14 @@ struct Interface {
   bool writes_color = false;     /* fragment: location 0 written */
   bool discards = false;
   uint32_t push_bytes = 0;       /* highest push-constant byte read */
+  /* descriptor bindings the stage declares (every module-scope Uniform / UniformConstant variable) */
+  struct Binding {
+    uint32_t set = 0, binding = 0;
+    uint32_t kind = 0;   /* 0 uniform buffer, 1 combined image sampler */
+    uint32_t count = 1;  /* array elements */
+    uint32_t bytes = 0;  /* uniform buffer: bytes of the block (the range a descriptor must cover) */
+  };
+  std::vector<Binding> bindings;
 };
 
 struct Shader {

@@ -72,7 +72,35 @@ class Emitter {
   std::string out;
   uint32_t nf = 0, nr = 0, np = 0, nk = 0;
   std::map<uint32_t, std::string> push_regs; /* push-constant word (byte offset) -> register loaded up front */
+  std::map<uint32_t, std::string> ubo_regs;  /* uniform-buffer binding -> register holding its address */
+  uint32_t nu = 0;                            /* %kzu registers */
+  bool uses_tex = false, uses_fetch = false;  /* calls kz_tex2d / kz_tex_fetch */
   uint32_t copy = 0;                          /* VertexPos3: which vertex the body computes */
+
+  static uint32_t slot_of(const VertexLayout* lay, uint32_t key) {
+    uint32_t set = key >> 16, binding = key & 0xFFFFu;
+    if (!lay || set >= KZ_MAX_DESC_SETS || binding >= KZ_MAX_DESC_BINDINGS) return ~0u;
+    return lay->desc_slot[set][binding];
+  }
+
+  /* the address of every uniform buffer `fn` reads, loaded once from the draw's descriptor slots */
+  void preload_ubo(const Function& fn, const VertexLayout* lay) {
+    ubo_regs.clear();
+    char buf[200];
+    for (const Inst& i : fn.code) {
+      if (i.op != Op::LdUbo || ubo_regs.count(i.imm2)) continue;
+      uint32_t slot = slot_of(lay, i.imm2);
+      std::string r = "%kzu" + std::to_string(nu++);
+      ubo_regs[i.imm2] = r;
+      if (slot == ~0u) { /* not in the layout (pipeline creation rejects this): reads as address 0 */
+        line("mov.b64 " + r + ", 0;");
+        continue;
+      }
+      std::snprintf(buf, sizeof buf, "ld.global.nc.u64 %s, [%%kzpush+%u];\n  cvta.to.global.u64 %s, %s;", r.c_str(),
+                    KZ_DESC_OFFSET + 32u * slot, r.c_str(), r.c_str());
+      line(buf);
+    }
+  }
 
   /* load every push-constant word `fn` reads once, as 16-byte vectors where an aligned group is used twice
    * or more (the push block is 16-byte aligned and KZ_PUSH_BYTES long) */
@@ -232,6 +260,49 @@ class Emitter {
           line(buf);
           break;
         }
+        case Op::LdUbo: {
+          auto ur = ubo_regs.find(i.imm2);
+          std::string base = ur != ubo_regs.end() ? ur->second : std::string("%kzub");
+          if (ur == ubo_regs.end()) line("mov.b64 %kzub, 0;");
+          if (i.a >= 0) {
+            line("cvt.u64.u32 %kzoff, " + R(i.a) + ";");
+            line("add.s64 %kzub, " + base + ", %kzoff;");
+            base = "%kzub";
+          }
+          std::snprintf(buf, sizeof buf, "ld.global.nc.%s %s, [%s+%u];", i.ty == Ty::F32 ? "f32" : "u32",
+                        R(i.dst).c_str(), base.c_str(), i.imm);
+          line(buf);
+          break;
+        }
+        case Op::Tex:
+        case Op::TexFetch: {
+          /* descriptor address (generic): push + KZ_DESC_OFFSET + 32 * (slot + element) */
+          uint32_t slot = slot_of(lay, i.imm2);
+          if (slot == ~0u) { /* not in the layout (pipeline creation rejects this) */
+            for (int k = 0; k < 4; k++) line("mov.f32 " + R(i.dst + k) + ", 0f00000000;");
+            break;
+          }
+          std::snprintf(buf, sizeof buf, "add.s64 %%kzd, %%kzpg, %u;", KZ_DESC_OFFSET + 32u * (slot + i.imm));
+          line(buf);
+          if (i.c >= 0) {
+            line("mul.wide.u32 %kzoff, " + R(i.c) + ", 32;");
+            line("add.s64 %kzd, %kzd, %kzoff;");
+          }
+          const char* fnn = i.op == Op::Tex ? "kz_tex2d" : "kz_tex_fetch";
+          const char* at = i.op == Op::Tex ? "f32" : "b32";
+          line("{");
+          line(".param .b64 kzt_p0;");
+          line(std::string(".param .b32 kzt_p1;\n  .param .b32 kzt_p2;\n  .param .align 16 .b8 kzt_r[16];"));
+          line("st.param.b64 [kzt_p0], %kzd;");
+          line(std::string("st.param.") + at + " [kzt_p1], " + R(i.a) + ";");
+          line(std::string("st.param.") + at + " [kzt_p2], " + R(i.b) + ";");
+          line(std::string("call (kzt_r), ") + fnn + ", (kzt_p0, kzt_p1, kzt_p2);");
+          for (int k = 0; k < 4; k++) line("ld.param.f32 " + R(i.dst + k) + ", [kzt_r+" + std::to_string(4 * k) + "];");
+          line("}");
+          uses_tex |= i.op == Op::Tex;
+          uses_fetch |= i.op == Op::TexFetch;
+          break;
+        }
         case Op::StOut: {
           if ((kind == Kind::VertexPos || kind == Kind::VertexPos3) && i.imm >= 16) break;
           if (kind == Kind::VertexPos3) {
@@ -371,13 +442,14 @@ class Emitter {
 };
 
 std::string function_text(const char* fname, Kind kind, const std::vector<const ir::Shader*>& stages,
-                          const std::vector<VertexLayout>& layouts) {
+                          const std::vector<VertexLayout>& layouts, bool& uses_tex, bool& uses_fetch) {
   Emitter e;
   std::string bodies;
   for (size_t p = 0; p < stages.size(); p++) {
     e.out.clear();
     std::string pfx = std::string(fname) + "_p" + std::to_string(p);
     e.out += "$" + pfx + ":\n";
+    if (stages[p]) e.preload_ubo(stages[p]->fn, p < layouts.size() ? &layouts[p] : nullptr);
     if (stages[p] && kind == Kind::VertexPos3) {
       e.preload_push(stages[p]->fn);
       for (uint32_t k = 0; k < 3; k++) {
@@ -437,13 +509,17 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
   }
   s += buf;
   s += "  .reg .b32 %kzsel, %kzt, %kzvid, %kziid, %kzv0, %kzv1, %kzv2;\n"
-       "  .reg .b64 %kzin, %kzpush, %kzout, %kzdraw, %kzoff;\n  .reg .b64 %kzvb<8>;\n  .reg .pred %kzp;\n";
+       "  .reg .b64 %kzin, %kzpush, %kzout, %kzdraw, %kzoff, %kzpg, %kzub, %kzd;\n  .reg .b64 %kzvb<8>;\n"
+       "  .reg .pred %kzp;\n";
+  if (e.nu) s += "  .reg .b64 %kzu<" + std::to_string(e.nu) + ">;\n";
+  uses_tex |= e.uses_tex;
+  uses_fetch |= e.uses_fetch;
   if (e.nk) s += "  .reg .b32 %kp<" + std::to_string(e.nk) + ">;\n";
   if (e.nf) s += "  .reg .f32 %f<" + std::to_string(e.nf) + ">;\n";
   if (e.nr) s += "  .reg .b32 %r<" + std::to_string(e.nr) + ">;\n";
   if (e.np) s += "  .reg .pred %p<" + std::to_string(e.np) + ">;\n";
   std::snprintf(buf, sizeof buf, "  ld.param.u32 %%kzsel, [%s_pipe];\n  ld.param.u64 %%kzpush, [%s_push];\n"
-                                 "  cvta.to.global.u64 %%kzpush, %%kzpush;\n", fname, fname);
+                                 "  mov.b64 %%kzpg, %%kzpush;\n  cvta.to.global.u64 %%kzpush, %%kzpush;\n", fname, fname);
   s += buf;
   if (kind == Kind::Fragment) {
     std::snprintf(buf, sizeof buf, "  ld.param.u64 %%kzin, [%s_in];\n  ld.param.u64 %%kzout, [%s_out];\n", fname, fname);
@@ -488,13 +564,22 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
 
 std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vector<const ir::Shader*>& fs,
                         const std::vector<VertexLayout>& layouts) {
+  bool tex = false, fetch = false;
+  std::string body;
+  body += function_text("kz_vs", Kind::VertexFull, vs, layouts, tex, fetch);
+  body += function_text("kz_vs_pos", Kind::VertexPos, vs, layouts, tex, fetch);
+  body += function_text("kz_vs_pos3", Kind::VertexPos3, vs, layouts, tex, fetch);
+  body += function_text("kz_fs", Kind::Fragment, fs, layouts, tex, fetch);
+  body += function_text("kz_fs_r8", Kind::FragmentRegs, fs, layouts, tex, fetch);
   std::string s = ".version 9.0\n.target sm_103a\n.address_size 64\n\n";
-  s += function_text("kz_vs", Kind::VertexFull, vs, layouts);
-  s += function_text("kz_vs_pos", Kind::VertexPos, vs, layouts);
-  s += function_text("kz_vs_pos3", Kind::VertexPos3, vs, layouts);
-  s += function_text("kz_fs", Kind::Fragment, fs, {});
-  s += function_text("kz_fs_r8", Kind::FragmentRegs, fs, {});
-  return s;
+  /* sampling functions defined in the pipeline-kernel object (kz_pipeline.cu) */
+  if (tex)
+    s += ".extern .func (.param .align 16 .b8 func_retval0[16]) kz_tex2d(.param .b64 kz_tex2d_param_0, "
+         ".param .b32 kz_tex2d_param_1, .param .b32 kz_tex2d_param_2);\n\n";
+  if (fetch)
+    s += ".extern .func (.param .align 16 .b8 func_retval0[16]) kz_tex_fetch(.param .b64 kz_tex_fetch_param_0, "
+         ".param .b32 kz_tex_fetch_param_1, .param .b32 kz_tex_fetch_param_2);\n\n";
+  return s + body;
 }
 
 std::string link(const std::string& ptx, const void* object, size_t object_size, std::vector<char>& cubin) {

@@ -18,6 +18,13 @@ struct VertexLayout {
   uint32_t location[8] = {}, binding[8] = {}, format[8] = {}, offset[8] = {}; /* format: KzAttrFormat */
   uint32_t stride[8] = {};
   uint32_t instanced = 0; /* bit b: binding b advances per instance */
+  /* descriptor slot of the first array element of (set, binding) in the pipeline layout (KZ_DESC_OFFSET +
+   * 32 * slot bytes into a draw's push snapshot); ~0u for bindings the layout does not have */
+  uint32_t desc_slot[KZ_MAX_DESC_SETS][KZ_MAX_DESC_BINDINGS];
+  VertexLayout() {
+    for (auto& s : desc_slot)
+      for (auto& b : s) b = ~0u;
+  }
 };
 
 /* PTX module defining kz_vs / kz_vs_pos / kz_fs for a pipeline set (entry p = pipeline index p;

@@ -34,8 +34,10 @@ using namespace spv;
 namespace {
 
 struct TypeInfo {
-  enum Kind { Void, Bool, Int, Float, Vector, Matrix, Array, RuntimeArray, Struct, Pointer, Function, Other } kind =
-      Other;
+  enum Kind {
+    Void, Bool, Int, Float, Vector, Matrix, Array, RuntimeArray, Struct, Pointer, Function, Image, SampledImage,
+    Sampler, Other
+  } kind = Other;
   uint32_t width = 32;
   bool is_signed = false;
   uint32_t elem = 0;
@@ -61,13 +63,14 @@ struct DecSet {
   }
 };
 
-/* per-scalar address of a variable */
-enum class Space : uint8_t { None, In, Out, Push, Reg };
+/* per-scalar address of a variable; a combined image sampler is one Tex slot per array element */
+enum class Space : uint8_t { None, In, Out, Push, Reg, Ubo, Tex };
 struct Slot {
   Space space = Space::None;
-  uint32_t offset = 0;  /* byte offset for In/Out/Push */
+  uint32_t offset = 0;  /* byte offset for In/Out/Push/Ubo; array element for Tex */
   int32_t reg = -1;     /* shadow register for Out/Reg */
   bool is_bool_in = false;
+  uint32_t key = 0;     /* Ubo/Tex: descriptor binding, set << 16 | binding */
 };
 
 struct Var {
@@ -90,6 +93,10 @@ struct Place {
 struct Val {
   uint32_t type = 0;
   std::vector<int32_t> regs;
+  /* a combined image sampler (or its image) of binding tex_key: array element tex_elem, or, when
+   * tex_dyn, the element in regs[0] */
+  bool is_tex = false, tex_dyn = false;
+  uint32_t tex_key = 0, tex_elem = 0;
 };
 
 struct PhiInfo {
@@ -158,6 +165,9 @@ class Translator {
       case TypeInfo::Vector: return ti.count;
       case TypeInfo::Matrix: return ti.count * scalars(ti.elem);
       case TypeInfo::Array: return ti.count * scalars(ti.elem);
+      case TypeInfo::Image:
+      case TypeInfo::SampledImage:
+      case TypeInfo::Sampler: return 1; /* one Tex slot */
       case TypeInfo::Struct: {
         uint32_t n = 0;
         for (uint32_t mbr : ti.members) n += scalars(mbr);
@@ -315,6 +325,11 @@ class Translator {
   void assign_io(uint32_t t, const DecSet* d, uint32_t struct_type, uint32_t member_idx, uint32_t& location,
                  std::vector<Slot>& slots, bool is_input);
   void assign_push(uint32_t t, uint32_t byte, std::vector<Slot>& slots, uint32_t stride_hint, bool row_major);
+  bool layout_descriptor(uint32_t var_id, Var& v);
+  bool image_sample(const Insn& in);
+  Space block_space_ = Space::Push; /* what assign_push lays out: push constants or a uniform block */
+  uint32_t block_key_ = 0;
+  uint32_t block_bytes_ = 0;
 
   /* ---- function body ---- */
   bool translate_entry();
@@ -423,9 +438,19 @@ bool Translator::scan_module() {
         break;
       }
       case OpTypeFunction: types_[o[0]].kind = TypeInfo::Function; break;
-      case OpTypeImage:
-      case OpTypeSampler:
-      case OpTypeSampledImage:
+      case OpTypeImage: {
+        TypeInfo& t = types_[o[0]];
+        t.kind = TypeInfo::Image;
+        t.count = o.size() > 2 ? o[2] : 0; /* Dim */
+        break;
+      }
+      case OpTypeSampler: types_[o[0]].kind = TypeInfo::Sampler; break;
+      case OpTypeSampledImage: {
+        TypeInfo& t = types_[o[0]];
+        t.kind = TypeInfo::SampledImage;
+        t.elem = o[1];
+        break;
+      }
       case OpTypeOpaque: types_[o[0]].kind = TypeInfo::Other; break;
       case OpConstantTrue:
       case OpConstantFalse:
@@ -642,10 +667,12 @@ void Translator::assign_push(uint32_t t, uint32_t byte, std::vector<Slot>& slots
     case TypeInfo::Int:
     case TypeInfo::Float: {
       Slot s;
-      s.space = Space::Push;
+      s.space = block_space_;
       s.offset = byte;
+      s.key = block_key_;
       slots.push_back(s);
-      if (byte + 4 > out_.iface.push_bytes) out_.iface.push_bytes = byte + 4;
+      if (block_space_ == Space::Push && byte + 4 > out_.iface.push_bytes) out_.iface.push_bytes = byte + 4;
+      if (block_space_ == Space::Ubo && byte + 4 > block_bytes_) block_bytes_ = byte + 4;
       break;
     }
     case TypeInfo::Vector:
@@ -692,7 +719,10 @@ bool Translator::layout_interface(uint32_t var_id, Var& v) {
     auto it = decs_.find(var_id);
     assign_io(v.type, it == decs_.end() ? nullptr : &it->second, 0, 0, location, v.slots, v.storage == SCInput);
   } else if (v.storage == SCPushConstant) {
+    block_space_ = Space::Push;
     assign_push(v.type, 0, v.slots, 0, false);
+  } else if (v.storage == SCUniform || v.storage == SCUniformConstant) {
+    if (!layout_descriptor(var_id, v)) return false;
   } else if (v.storage == SCPrivate || v.storage == SCFunction) {
     std::vector<Ty> tys;
     flat_types(v.type, tys);
@@ -703,8 +733,7 @@ bool Translator::layout_interface(uint32_t var_id, Var& v) {
       v.slots.push_back(s);
     }
   } else {
-    return fail("unsupported variable storage class " + std::to_string(v.storage) +
-                " (descriptor sets are not supported by the draw path)");
+    return fail("unsupported variable storage class " + std::to_string(v.storage));
   }
   if (v.storage == SCOutput) {
     std::vector<Ty> tys;
@@ -714,7 +743,139 @@ bool Translator::layout_interface(uint32_t var_id, Var& v) {
   return err_.empty();
 }
 
+/* OpImageSample[Proj]{Implicit,Explicit}Lod and OpImageFetch on a combined image sampler of one mip
+ * level: level-of-detail operands (Bias, Lod, Grad, MinLod) select nothing; Proj divides s and t by the
+ * last coordinate component */
+bool Translator::image_sample(const Insn& in) {
+  const auto& o = in.ops;
+  if (o.size() < 4) return fail("image instruction with too few operands");
+  Val* img = val(o[2]);
+  Val* coord = val(o[3]);
+  if (!img || !coord) return false;
+  if (!img->is_tex) return fail("image operand is not a combined image sampler variable");
+  const bool fetch = in.opcode == OpImageFetch;
+  const bool proj = in.opcode == OpImageSampleProjImplicitLod || in.opcode == OpImageSampleProjExplicitLod;
+  if (o.size() > 4) {
+    const uint32_t allowed = fetch ? 0x2u : (0x1u | 0x2u | 0x4u | 0x80u);
+    if (o[4] & ~allowed) return fail("image operands other than Bias, Lod, Grad and MinLod are not supported");
+  }
+  if (coord->regs.size() < 2) return fail("image coordinate with fewer than two components");
+  const TypeInfo& rt = ty(o[0]);
+  if (rt.kind != TypeInfo::Vector || rt.count != 4 || ty(rt.elem).kind != TypeInfo::Float)
+    return fail("image results other than vec4 are not supported (UNORM images)");
+  int32_t s = coord->regs[0], t = coord->regs[1];
+  if (proj) {
+    int32_t q = coord->regs.back();
+    s = op2(Op::FDiv, Ty::F32, s, q);
+    t = op2(Op::FDiv, Ty::F32, t, q);
+  }
+  Inst i;
+  i.op = fetch ? Op::TexFetch : Op::Tex;
+  i.ty = Ty::F32;
+  i.dst = fn_.reg(Ty::F32);
+  for (int k = 1; k < 4; k++) fn_.reg(Ty::F32);
+  i.a = s;
+  i.b = t;
+  i.c = img->tex_dyn ? img->regs[0] : -1;
+  i.imm = img->tex_dyn ? 0u : img->tex_elem;
+  i.imm2 = img->tex_key;
+  fn_.emit(i);
+  Val r;
+  r.type = o[0];
+  for (int k = 0; k < 4; k++) r.regs.push_back(i.dst + k);
+  vals_[o[1]] = r;
+  return true;
+}
+
+bool Translator::layout_descriptor(uint32_t var_id, Var& v) {
+  uint32_t set = 0, binding = 0;
+  auto it = decs_.find(var_id);
+  if (it != decs_.end()) {
+    it->second.get(DecDescriptorSet, set);
+    it->second.get(DecBinding, binding);
+  }
+  if (set >= KZ_IR_MAX_SETS || binding >= KZ_IR_MAX_BINDINGS)
+    return fail("descriptor set " + std::to_string(set) + " binding " + std::to_string(binding) +
+                " is beyond the driver's limits (sets 0..3, bindings 0..15)");
+  Interface::Binding b;
+  b.set = set;
+  b.binding = binding;
+  const uint32_t key = set << 16 | binding;
+  uint32_t t = v.type, count = 1;
+  if (ty(t).kind == TypeInfo::Array) {
+    count = ty(t).count;
+    t = ty(t).elem;
+  }
+  const TypeInfo& ti = ty(t);
+  if (v.storage == SCUniformConstant) {
+    if (ti.kind == TypeInfo::Image || ti.kind == TypeInfo::Sampler)
+      return fail("separate images and samplers are not supported (combined image samplers are)");
+    if (ti.kind != TypeInfo::SampledImage || !count) return fail("unsupported UniformConstant variable");
+    if (ty(ti.elem).count != 1) return fail("only 2D images are supported");
+    b.kind = 1;
+    b.count = count;
+    for (uint32_t k = 0; k < count; k++) {
+      Slot s;
+      s.space = Space::Tex;
+      s.offset = k;
+      s.key = key;
+      v.slots.push_back(s);
+    }
+  } else {
+    if (t != v.type) return fail("arrays of uniform blocks are not supported");
+    if (decs_[t].has(DecBufferBlock)) return fail("storage buffers are not supported");
+    if (ti.kind != TypeInfo::Struct) return fail("a Uniform variable that is not a block");
+    block_space_ = Space::Ubo;
+    block_key_ = key;
+    block_bytes_ = 0;
+    assign_push(t, 0, v.slots, 0, false);
+    block_space_ = Space::Push;
+    b.kind = 0;
+    b.bytes = block_bytes_;
+  }
+  out_.iface.bindings.push_back(b);
+  return err_.empty();
+}
+
 bool Translator::load(const Place& p, Val& v) {
+  if (p.dyn >= 0 && !vars_[p.var].slots.empty() && p.first < vars_[p.var].slots.size() &&
+      (vars_[p.var].slots[p.first].space == Space::Ubo || vars_[p.var].slots[p.first].space == Space::Tex)) {
+    /* run-time index into a uniform block's array or an array of combined image samplers: clamped to the
+     * array, then addressed directly */
+    const Var& var = vars_[p.var];
+    const Slot& s0 = var.slots[p.first];
+    int32_t lim = konst(Ty::B32, p.dyn_count - 1);
+    int32_t idx = op3(Op::Selp, Ty::B32, lim, p.dyn, op2(Op::SetpU, Ty::Pred, p.dyn, lim, CmpGt));
+    v.type = p.type;
+    v.regs.clear();
+    if (s0.space == Space::Tex) {
+      v.is_tex = v.tex_dyn = true;
+      v.tex_key = s0.key;
+      v.regs.push_back(op2(Op::IAdd, Ty::B32, idx, konst(Ty::B32, s0.offset)));
+      return true;
+    }
+    uint32_t stride = p.dyn_count > 1 && p.first + p.dyn_stride < var.slots.size()
+                          ? var.slots[p.first + p.dyn_stride].offset - s0.offset
+                          : 0;
+    int32_t boff = op2(Op::IMul, Ty::B32, idx, konst(Ty::B32, stride));
+    std::vector<Ty> tys;
+    flat_types(p.type, tys);
+    for (size_t k = 0; k < tys.size(); k++) {
+      if (p.first + k >= var.slots.size()) return fail("load outside a variable");
+      const Slot& s = var.slots[p.first + k];
+      Ty t = tys[k] == Ty::Pred ? Ty::B32 : tys[k];
+      Inst i;
+      i.op = Op::LdUbo;
+      i.ty = t;
+      i.dst = fn_.reg(t);
+      i.a = boff;
+      i.imm = s.offset;
+      i.imm2 = s.key;
+      fn_.emit(i);
+      v.regs.push_back(tys[k] == Ty::Pred ? op1(Op::B32ToP, Ty::Pred, i.dst) : i.dst);
+    }
+    return true;
+  }
   if (p.dyn >= 0) {
     /* run-time index: load every candidate element and select the one the index names (an index out of
      * range reads element 0) */
@@ -746,6 +907,15 @@ bool Translator::load(const Place& p, Val& v) {
   flat_types(p.type, tys);
   v.type = p.type;
   v.regs.clear();
+  if (p.first < var.slots.size() && var.slots[p.first].space == Space::Tex) {
+    const TypeInfo& ti = ty(p.type);
+    if (ti.kind != TypeInfo::SampledImage && ti.kind != TypeInfo::Image)
+      return fail("load of a whole array of combined image samplers");
+    v.is_tex = true;
+    v.tex_key = var.slots[p.first].key;
+    v.tex_elem = var.slots[p.first].offset;
+    return true;
+  }
   for (size_t k = 0; k < tys.size(); k++) {
     if (p.first + k >= var.slots.size()) return fail("load outside a variable");
     const Slot& s = var.slots[p.first + k];
@@ -772,14 +942,16 @@ bool Translator::load(const Place& p, Val& v) {
         }
         break;
       }
-      case Space::Push: {
+      case Space::Push:
+      case Space::Ubo: {
         Ty t = tys[k] == Ty::Pred ? Ty::B32 : tys[k];
         int32_t r = fn_.reg(t);
         Inst i;
-        i.op = Op::LdPush;
+        i.op = s.space == Space::Push ? Op::LdPush : Op::LdUbo;
         i.ty = t;
         i.dst = r;
         i.imm = s.offset;
+        i.imm2 = s.key;
         fn_.emit(i);
         v.regs.push_back(tys[k] == Ty::Pred ? op1(Op::B32ToP, Ty::Pred, r) : r);
         break;
@@ -1137,12 +1309,22 @@ bool Translator::do_insn(const Insn& in) {
       vals_[o[1]] = r;
       return true;
     }
-    case OpCopyObject: {
+    case OpCopyObject:
+    case OpImage: { /* the image of a combined image sampler: the same binding and element */
       Val* a = val(o[2]);
       if (!a) return false;
       vals_[o[1]] = *a;
+      vals_[o[1]].type = o[0];
       return true;
     }
+    case OpSampledImage:
+      return fail("OpSampledImage: separate images and samplers are not supported (combined image samplers are)");
+    case OpImageSampleImplicitLod:
+    case OpImageSampleExplicitLod:
+    case OpImageSampleProjImplicitLod:
+    case OpImageSampleProjExplicitLod:
+    case OpImageFetch:
+      return image_sample(in);
     case OpUndef: {
       std::vector<Ty> tys;
       flat_types(o[0], tys);
@@ -1682,7 +1864,10 @@ std::vector<uint32_t> live_inputs(const Function& fn, uint32_t out_lo, uint32_t 
         case Op::Kill: root = true; break;
         default: break;
       }
-      if (root || (i.dst >= 0 && live[(size_t)i.dst])) {
+      bool live_dst = i.dst >= 0 && live[(size_t)i.dst];
+      if ((i.op == Op::Tex || i.op == Op::TexFetch) && i.dst >= 0)
+        for (int k = 1; k < 4; k++) live_dst |= live[(size_t)i.dst + k] != 0;
+      if (root || live_dst) {
         mark(i.a);
         mark(i.b);
         mark(i.c);

@@ -257,9 +257,71 @@ class Renderer:
         self._objects.append(("ShaderModule", h))
         return h
 
-    def pipeline_layout(self, push_bytes):
+    def write_image(self, img, texels):
+        """copy uint8 [h, w, 4] texels into a host-visible linear image, row by row at its pitch"""
+        a = np.ascontiguousarray(texels, dtype=np.uint8)
+        p = self.map(img)
+        row = img.width * 4
+        for y in range(img.height):
+            ctypes.memmove(p + y * img.pitch, a[y].ctypes.data, row)
+        self.unmap(img)
+
+    # ---- samplers and descriptor sets ----
+    def sampler(self, tex):
+        """a VkSampler for scenes.Texture `tex` (min filter = mag filter)"""
+        f = vk.FILTER_LINEAR if tex.linear else vk.FILTER_NEAREST
+        ci = vk.VkSamplerCreateInfo(vk.ST_SAMPLER_CREATE_INFO, None, 0, f, f, 0, tex.address_u, tex.address_v,
+                                    vk.ADDRESS_CLAMP_TO_EDGE, 0.0, 0, 1.0, 0, 0, 0.0, 0.0, 2 * tex.border,
+                                    int(tex.unnormalized))
+        h = c_void_p()
+        check("vkCreateSampler", self.drv.vkCreateSampler(self.device, byref(ci), None, byref(h)))
+        self._objects.append(("Sampler", h))
+        return h
+
+    def set_layout(self, bindings):
+        """a descriptor set layout from [(binding, descriptor type, count)]"""
+        arr = (vk.VkDescriptorSetLayoutBinding * len(bindings))(
+            *[vk.VkDescriptorSetLayoutBinding(b, t, n, vk.SHADER_STAGE_VERTEX | vk.SHADER_STAGE_FRAGMENT, None)
+              for b, t, n in bindings])
+        ci = vk.VkDescriptorSetLayoutCreateInfo(vk.ST_DESCRIPTOR_SET_LAYOUT_CREATE_INFO, None, 0, len(bindings), arr)
+        h = c_void_p()
+        check("vkCreateDescriptorSetLayout", self.drv.vkCreateDescriptorSetLayout(self.device, byref(ci), None,
+                                                                                  byref(h)))
+        self._objects.append(("DescriptorSetLayout", h))
+        return h
+
+    def descriptor_sets(self, layout, n=1):
+        """a pool holding `n` sets of `layout`; returns the sets"""
+        sizes = (vk.VkDescriptorPoolSize * 3)(vk.VkDescriptorPoolSize(vk.DESCRIPTOR_COMBINED_IMAGE_SAMPLER, 64 * n),
+                                              vk.VkDescriptorPoolSize(vk.DESCRIPTOR_UNIFORM_BUFFER, 64 * n),
+                                              vk.VkDescriptorPoolSize(vk.DESCRIPTOR_UNIFORM_BUFFER_DYNAMIC, 64 * n))
+        pci = vk.VkDescriptorPoolCreateInfo(vk.ST_DESCRIPTOR_POOL_CREATE_INFO, None, 0, n, 3, sizes)
+        pool = c_void_p()
+        check("vkCreateDescriptorPool", self.drv.vkCreateDescriptorPool(self.device, byref(pci), None, byref(pool)))
+        self._objects.append(("DescriptorPool", pool))
+        layouts = (c_void_p * n)(*([layout.value] * n))
+        ai = vk.VkDescriptorSetAllocateInfo(vk.ST_DESCRIPTOR_SET_ALLOCATE_INFO, None, pool, n, layouts)
+        sets = (c_void_p * n)()
+        check("vkAllocateDescriptorSets", self.drv.vkAllocateDescriptorSets(self.device, byref(ai), sets))
+        return [c_void_p(s) for s in sets]
+
+    def write_image_descriptor(self, dset, binding, element, sampler, image):
+        ii = vk.VkDescriptorImageInfo(sampler, image.view, vk.IMAGE_LAYOUT_GENERAL)
+        w = vk.VkWriteDescriptorSet(vk.ST_WRITE_DESCRIPTOR_SET, None, dset, binding, element, 1,
+                                    vk.DESCRIPTOR_COMBINED_IMAGE_SAMPLER, pointer(ii), None, None)
+        self.drv.vkUpdateDescriptorSets(self.device, 1, byref(w), 0, None)
+
+    def write_buffer_descriptor(self, dset, binding, buf, offset, size, dtype=vk.DESCRIPTOR_UNIFORM_BUFFER):
+        bi = vk.VkDescriptorBufferInfo(buf.handle, offset, size)
+        w = vk.VkWriteDescriptorSet(vk.ST_WRITE_DESCRIPTOR_SET, None, dset, binding, 0, 1, dtype, None, pointer(bi),
+                                    None)
+        self.drv.vkUpdateDescriptorSets(self.device, 1, byref(w), 0, None)
+
+    def pipeline_layout(self, push_bytes, set_layouts=()):
         rng = vk.VkPushConstantRange(vk.SHADER_STAGE_VERTEX | vk.SHADER_STAGE_FRAGMENT, 0, push_bytes)
-        lci = vk.VkPipelineLayoutCreateInfo(vk.ST_PIPELINE_LAYOUT_CREATE_INFO, None, 0, 0, None,
+        sl = (c_void_p * max(1, len(set_layouts)))(*[s.value for s in set_layouts])
+        lci = vk.VkPipelineLayoutCreateInfo(vk.ST_PIPELINE_LAYOUT_CREATE_INFO, None, 0, len(set_layouts),
+                                            ctypes.cast(sl, c_void_p) if set_layouts else None,
                                             1 if push_bytes else 0, pointer(rng) if push_bytes else None)
         h = c_void_p()
         check("vkCreatePipelineLayout", self.drv.vkCreatePipelineLayout(self.device, byref(lci), None, byref(h)))
@@ -279,6 +341,9 @@ class Renderer:
         if scene.shader == "color":
             attrs[0] = vk.VkVertexInputAttributeDescription(0, 0, vk.FORMAT_R32G32B32A32_SFLOAT, 0)
             attrs[1] = vk.VkVertexInputAttributeDescription(1, 0, vk.FORMAT_R32G32B32A32_SFLOAT, 16)
+        elif scene.shader == "textured":
+            attrs[0] = vk.VkVertexInputAttributeDescription(0, 0, vk.FORMAT_R32G32B32A32_SFLOAT, 0)
+            attrs[1] = vk.VkVertexInputAttributeDescription(1, 0, vk.FORMAT_R32G32_SFLOAT, 16)
         else:
             attrs[0] = vk.VkVertexInputAttributeDescription(0, 0, vk.FORMAT_R32G32B32_SFLOAT, 0)
             attrs[1] = vk.VkVertexInputAttributeDescription(1, 0, vk.FORMAT_R32G32B32_SFLOAT, 12)
@@ -370,7 +435,30 @@ class SceneRun:
                                     host_visible if depth_host_visible is None else depth_host_visible)
         self.rp = r.render_pass(vk.FORMAT_R8G8B8A8_UNORM, True)
         self.fb = r.framebuffer(self.rp, [self.color.view, self.depth.view], scene.width, scene.height)
-        self.layout = r.pipeline_layout(64 if scene.shader == "lambert" else 0)
+        # descriptor sets: the textured scene's sampler2D, or the Lambert matrices in a uniform buffer (one
+        # 256-byte slot per draw, selected by a dynamic offset)
+        self.set_layouts, self.dsets, self.ubo_buf, self.tex_image = [], [], None, None
+        if scene.texture is not None:
+            t = scene.texture
+            th, tw = t.texels.shape[:2]
+            self.tex_image = r.create_image(tw, th, vk.FORMAT_B8G8R8A8_UNORM if t.bgra else vk.FORMAT_R8G8B8A8_UNORM,
+                                            vk.IMAGE_USAGE_SAMPLED, True)
+            r.write_image(self.tex_image, t.texels)
+            self.set_layouts = [r.set_layout([(0, vk.DESCRIPTOR_COMBINED_IMAGE_SAMPLER, 1)])]
+            self.dsets = r.descriptor_sets(self.set_layouts[0])
+            r.write_image_descriptor(self.dsets[0], 0, 0, r.sampler(t), self.tex_image)
+        elif scene.ubo:
+            mats = np.zeros((max(1, len(scene.draws)), 64), dtype=np.float32)
+            for i, dr in enumerate(scene.draws):
+                if dr.mvp is not None:
+                    mats[i, :16] = dr.mvp
+            self.ubo_buf = r.create_buffer(mats.nbytes, vk.BUFFER_USAGE_UNIFORM, host_visible)
+            r.write_buffer(self.ubo_buf, mats)
+            self.set_layouts = [r.set_layout([(0, vk.DESCRIPTOR_UNIFORM_BUFFER_DYNAMIC, 1)])]
+            self.dsets = r.descriptor_sets(self.set_layouts[0])
+            r.write_buffer_descriptor(self.dsets[0], 0, self.ubo_buf, 0, 64, vk.DESCRIPTOR_UNIFORM_BUFFER_DYNAMIC)
+        push = 64 if scene.shader == "lambert" and not scene.ubo else 0
+        self.layout = r.pipeline_layout(push, self.set_layouts)
         vs, fs = scene.shaders()
         self.pipe = r.pipeline(scene, self.rp, self.layout, vs, fs)
         self.cmds = self.cmd_staging = self.count_buf = None
@@ -401,6 +489,9 @@ class SceneRun:
                                        vk.VkRect2D(vk.VkOffset2D(0, 0), vk.VkExtent2D(s.width, s.height)), 2, clears)
         d.vkCmdBeginRenderPass(cb, byref(rbi), vk.SUBPASS_CONTENTS_INLINE)
         d.vkCmdBindPipeline(cb, vk.BIND_POINT_GRAPHICS, self.pipe)
+        if self.dsets and not s.ubo:
+            sets = (c_void_p * 1)(self.dsets[0].value)
+            d.vkCmdBindDescriptorSets(cb, vk.BIND_POINT_GRAPHICS, self.layout, 0, 1, sets, 0, None)
         bufs = (c_void_p * 1)(self.vb.handle.value)
         offs = (c_uint64 * 1)(0)
         d.vkCmdBindVertexBuffers(cb, 0, 1, bufs, offs)
@@ -412,7 +503,11 @@ class SceneRun:
         for i, dr in enumerate(s.draws):
             if self.indirect is not None and not per_draw_push:
                 break
-            if dr.mvp is not None:
+            if dr.mvp is not None and s.ubo:
+                sets = (c_void_p * 1)(self.dsets[0].value)
+                offs = (c_uint32 * 1)(256 * i)
+                d.vkCmdBindDescriptorSets(cb, vk.BIND_POINT_GRAPHICS, self.layout, 0, 1, sets, 1, offs)
+            elif dr.mvp is not None:
                 m = np.ascontiguousarray(dr.mvp, dtype=np.float32)
                 d.vkCmdPushConstants(cb, self.layout, vk.SHADER_STAGE_VERTEX, 0, 64, m.ctypes.data)
             if self.indirect is not None:

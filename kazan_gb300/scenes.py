@@ -71,11 +71,28 @@ class Draw:
 
 
 @dataclass
+class Texture:
+    """a combined image sampler of one mip level: texels uint8 [h, w, 4] in the image's byte order"""
+    texels: np.ndarray
+    bgra: bool = False            # VK_FORMAT_B8G8R8A8_UNORM (else R8G8B8A8_UNORM)
+    linear: bool = False          # VK_FILTER_LINEAR for both min and mag (else NEAREST)
+    address_u: int = 0            # VkSamplerAddressMode
+    address_v: int = 0
+    border: int = 0               # 0 transparent black, 1 opaque black, 2 opaque white
+    unnormalized: bool = False
+
+    def sampler_bits(self):
+        """KzSamplerBits (kz_raster_abi.h)"""
+        return (int(self.linear) | (int(self.unnormalized) << 1) | (self.address_u << 4) | (self.address_v << 8) |
+                (self.border << 12))
+
+
+@dataclass
 class Scene:
     name: str
     width: int
     height: int
-    shader: str                # "color" or "lambert"
+    shader: str                # "color", "lambert" or "textured"
     vertices: np.ndarray       # float32 [V, 8] (color) or [V, 6] (lambert)
     indices: Optional[np.ndarray]
     draws: List[Draw]
@@ -89,6 +106,9 @@ class Scene:
     clear_depth: float = 1.0
     fs_words: Optional[np.ndarray] = field(default=None, repr=False)  # overrides the default fragment shader
     vs_words: Optional[np.ndarray] = field(default=None, repr=False)  # overrides the default vertex shader
+    texture: Optional[Texture] = None  # "textured": the fragment shader's sampler2D (set 0, binding 0)
+    ubo: bool = False          # "lambert": the matrices come from a uniform buffer (set 0, binding 0, dynamic
+                               # offset per draw) instead of push constants
 
     @property
     def triangles(self):
@@ -104,8 +124,10 @@ class Scene:
     def shaders(self):
         if self.shader == "color":
             vs, fs = spirv_asm.color_vs(), spirv_asm.color_fs()
+        elif self.shader == "textured":
+            vs, fs = spirv_asm.textured_vs(), spirv_asm.textured_fs()
         else:
-            vs, fs = spirv_asm.lambert_vs(), spirv_asm.lambert_fs()
+            vs, fs = spirv_asm.lambert_ubo_vs() if self.ubo else spirv_asm.lambert_vs(), spirv_asm.lambert_fs()
         if self.fs_words is not None:
             fs = self.fs_words
         if self.vs_words is not None:
@@ -174,6 +196,31 @@ def ordered_blend(seed=4, n=200_000, width=1920, height=1080, amin=4.0, amax=409
     lib().kz_scene_blend(seed, n, width, height, amin, amax, alpha, _fp(v))
     return Scene("ordered_blend", width, height, "color", v, None, [Draw(0, n)], cull=0, depth_test=True,
                  depth_write=False, blend=True)
+
+
+def textured(seed=6, n=4000, width=640, height=360, tex_w=61, tex_h=37, uv_lo=-1.5, uv_hi=2.5, **sampler):
+    """n random triangles with per-vertex w in [0.5, 2] (perspective-correct texture coordinates) and
+    coordinates in [uv_lo, uv_hi] (every address mode is exercised), over a random RGBA8 texture of
+    tex_w x tex_h; `sampler` sets the Texture's filter and address fields"""
+    rng = np.random.default_rng(seed)
+    v = np.empty((3 * n, 6), dtype=np.float32)
+    cx = rng.uniform(-1.1, 1.1, n)
+    cy = rng.uniform(-1.1, 1.1, n)
+    size = np.exp(rng.uniform(np.log(0.01), np.log(0.6), n))
+    for k in range(3):
+        ang = rng.uniform(0, 2 * np.pi, n)
+        w = rng.uniform(0.5, 2.0, n)
+        x = cx + size * np.cos(ang)
+        y = cy + size * np.sin(ang)
+        v[k::3, 0] = x * w
+        v[k::3, 1] = y * w
+        v[k::3, 2] = rng.uniform(0.05, 0.95, n) * w
+        v[k::3, 3] = w
+        v[k::3, 4] = rng.uniform(uv_lo, uv_hi, n)
+        v[k::3, 5] = rng.uniform(uv_lo, uv_hi, n)
+    texels = rng.integers(0, 256, (tex_h, tex_w, 4), dtype=np.uint8)
+    return Scene("textured", width, height, "textured", v, None, [Draw(0, n)], cull=0,
+                 texture=Texture(texels, **sampler))
 
 
 def triangles_from(vertices_xyzw_rgba, width, height, **state):

@@ -23,6 +23,14 @@ class KzVertexInputLayout(ctypes.Structure):
                 ("format", c_uint32 * 8), ("offset", c_uint32 * 8), ("stride", c_uint32 * 8), ("instanced", c_uint32)]
 
 
+class KzShaderBinding(ctypes.Structure):
+    _fields_ = [(n, c_uint32) for n in ("set", "binding", "kind", "count", "bytes")]
+
+
+class KzDescriptorSlots(ctypes.Structure):
+    _fields_ = [("slot", (c_uint32 * 16) * 4)]
+
+
 class ShaderError(RuntimeError):
     pass
 
@@ -42,6 +50,11 @@ def lib(path=None):
         L.kzShaderEmitPtx.argtypes = [POINTER(c_void_p), POINTER(c_void_p), POINTER(KzVertexInputLayout), c_uint32,
                                       c_char_p, c_size_t]
         L.kzShaderEmitPtx.restype = c_size_t
+        L.kzShaderEmitPtxDescriptors.argtypes = [POINTER(c_void_p), POINTER(c_void_p), POINTER(KzVertexInputLayout),
+                                                 POINTER(KzDescriptorSlots), c_uint32, c_char_p, c_size_t]
+        L.kzShaderEmitPtxDescriptors.restype = c_size_t
+        L.kzShaderBindings.argtypes = [c_void_p, POINTER(KzShaderBinding), c_uint32]
+        L.kzShaderBindings.restype = c_uint32
         L.kzShaderLink.argtypes = [c_char_p, c_void_p, c_size_t, POINTER(c_void_p), c_char_p, c_size_t]
         L.kzShaderLink.restype = ctypes.c_int
         L.kzCompiledCodeImage.argtypes = [c_void_p, POINTER(c_size_t)]
@@ -67,6 +80,13 @@ class Shader:
             raise ShaderError(err.value.decode())
         self.handle = h
 
+    def bindings(self):
+        """[(set, binding, kind, count, bytes)] of the descriptors the stage declares"""
+        n = lib().kzShaderBindings(self.handle, None, 0)
+        arr = (KzShaderBinding * max(1, n))()
+        lib().kzShaderBindings(self.handle, arr, n)
+        return [(b.set, b.binding, b.kind, b.count, b.bytes) for b in arr[:n]]
+
     def info(self):
         i = KzShaderInfo()
         lib().kzShaderInfo(self.handle, ctypes.byref(i))
@@ -90,15 +110,25 @@ def layout(attrs, strides, instanced=0):
     return lay
 
 
-def emit_ptx(pairs, layouts=None):
-    """pairs: list of (vertex Shader, fragment Shader or None)"""
+def descriptor_slots(mapping):
+    """KzDescriptorSlots from {(set, binding): slot}"""
+    d = KzDescriptorSlots()
+    for s in range(4):
+        for b in range(16):
+            d.slot[s][b] = mapping.get((s, b), 0xFFFFFFFF)
+    return d
+
+
+def emit_ptx(pairs, layouts=None, slots=None):
+    """pairs: list of (vertex Shader, fragment Shader or None); slots: per pair, {(set, binding): slot}"""
     n = len(pairs)
     vs = (c_void_p * n)(*[p[0].handle.value for p in pairs])
     fs = (c_void_p * n)(*[(p[1].handle.value if p[1] is not None else None) for p in pairs])
     lays = (KzVertexInputLayout * n)(*layouts) if layouts else None
-    size = lib().kzShaderEmitPtx(vs, fs, lays, n, None, 0)
+    ds = (KzDescriptorSlots * n)(*[descriptor_slots(m) for m in slots]) if slots else None
+    size = lib().kzShaderEmitPtxDescriptors(vs, fs, lays, ds, n, None, 0)
     buf = ctypes.create_string_buffer(size)
-    lib().kzShaderEmitPtx(vs, fs, lays, n, buf, size)
+    lib().kzShaderEmitPtxDescriptors(vs, fs, lays, ds, n, buf, size)
     return buf.value.decode()
 
 

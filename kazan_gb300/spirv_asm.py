@@ -11,6 +11,9 @@ The workload shaders:
   * lambert_vs / lambert_fs  gl_Position = mvp * vec4(in0.xyz, 1) with mvp a column-major mat4 push
                            constant; out0 = in1.xyz (normal); fragment colour
                            = vec4(ALBEDO * max(dot(normalize(n), LIGHT), 0), 1)
+  * lambert_ubo_vs         the same with mvp in a uniform buffer (set 0, binding 0)
+  * textured_vs / textured_fs  gl_Position = in0 (vec4), out0 = in1 (vec2 uv); fragment colour
+                           = texture(sampler2D at set 0 binding 0, uv)
 """
 import struct
 
@@ -29,6 +32,8 @@ OpTypeInt = 21
 OpTypeFloat = 22
 OpTypeVector = 23
 OpTypeMatrix = 24
+OpTypeImage = 25
+OpTypeSampledImage = 27
 OpTypeArray = 28
 OpTypeStruct = 30
 OpTypePointer = 32
@@ -48,6 +53,11 @@ OpStore = 62
 OpAccessChain = 65
 OpDecorate = 71
 OpMemberDecorate = 72
+OpImageSampleImplicitLod = 87
+OpImageSampleExplicitLod = 88
+OpImageSampleProjImplicitLod = 91
+OpImageFetch = 95
+OpImage = 100
 OpVectorExtractDynamic = 77
 OpVectorInsertDynamic = 78
 OpVectorShuffle = 79
@@ -90,7 +100,9 @@ MemoryGLSL450 = 1
 ExecVertex = 0
 ExecFragment = 4
 ModeOriginUpperLeft = 7
+SCUniformConstant = 0
 SCInput = 1
+SCUniform = 2
 SCOutput = 3
 SCPushConstant = 9
 SCFunction = 7
@@ -102,6 +114,9 @@ DecBuiltIn = 11
 DecNoPerspective = 13
 DecFlat = 14
 DecLocation = 30
+DecBinding = 33
+DecDescriptorSet = 34
+ImageOperandsLod = 0x2
 DecOffset = 35
 BuiltInPosition = 0
 BuiltInFragCoord = 15
@@ -390,6 +405,129 @@ def lambert_vs():
     m.op(OpStore, out_nrm, n)
     _end_main(m)
     m.entry(ExecVertex, fn, "main", [pc, pv, in_pos, in_nrm, out_nrm])
+    return m.to_words()
+
+
+def lambert_ubo_vs(set_=0, binding=0):
+    """lambert_vs with mvp read from a uniform block { mat4 mvp; } at (set_, binding)"""
+    m = Module()
+    m.capability(CapShader)
+    f32 = m.f32()
+    v3, v4 = m.vec(f32, 3), m.vec(f32, 4)
+    m4 = m.mat(v4, 4)
+    blk = m.struct(m4)
+    m.member_decorate(blk, 0, DecOffset, 0)
+    m.member_decorate(blk, 0, DecColMajor)
+    m.member_decorate(blk, 0, DecMatrixStride, 16)
+    m.decorate(blk, DecBlock)
+    ubo = m.variable(SCUniform, m.ptr(SCUniform, blk))
+    m.decorate(ubo, DecDescriptorSet, set_)
+    m.decorate(ubo, DecBinding, binding)
+    pv = _per_vertex(m)
+    in_pos = _io(m, SCInput, v3, 0)
+    in_nrm = _io(m, SCInput, v3, 1)
+    out_nrm = _io(m, SCOutput, v3, 0)
+    one = m.cf(1.0)
+    fn = _begin_main(m)
+    mp = m.res(OpAccessChain, m.ptr(SCUniform, m4), ubo, m.ci(0))
+    mvp = m.res(OpLoad, m4, mp)
+    p = m.res(OpLoad, v3, in_pos)
+    x = m.res(OpCompositeExtract, f32, p, 0)
+    y = m.res(OpCompositeExtract, f32, p, 1)
+    z = m.res(OpCompositeExtract, f32, p, 2)
+    p4 = m.res(OpCompositeConstruct, v4, x, y, z, one)
+    clip = m.res(OpMatrixTimesVector, v4, mvp, p4)
+    dst = m.res(OpAccessChain, m.ptr(SCOutput, v4), pv, m.ci(0))
+    m.op(OpStore, dst, clip)
+    n = m.res(OpLoad, v3, in_nrm)
+    m.op(OpStore, out_nrm, n)
+    _end_main(m)
+    m.entry(ExecVertex, fn, "main", [ubo, pv, in_pos, in_nrm, out_nrm])
+    return m.to_words()
+
+
+def textured_vs():
+    """gl_Position = in0 (vec4); out0 = in1 (vec2 texture coordinates)"""
+    m = Module()
+    m.capability(CapShader)
+    f32 = m.f32()
+    v2, v4 = m.vec(f32, 2), m.vec(f32, 4)
+    pv = _per_vertex(m)
+    in_pos = _io(m, SCInput, v4, 0)
+    in_uv = _io(m, SCInput, v2, 1)
+    out_uv = _io(m, SCOutput, v2, 0)
+    fn = _begin_main(m)
+    p = m.res(OpLoad, v4, in_pos)
+    dst = m.res(OpAccessChain, m.ptr(SCOutput, v4), pv, m.ci(0))
+    m.op(OpStore, dst, p)
+    uv = m.res(OpLoad, v2, in_uv)
+    m.op(OpStore, out_uv, uv)
+    _end_main(m)
+    m.entry(ExecVertex, fn, "main", [pv, in_pos, in_uv, out_uv])
+    return m.to_words()
+
+
+def _sampler2d(m, set_, binding, count=None):
+    """a UniformConstant sampler2D variable (an array of `count` when given); returns (var, sampled image type)"""
+    f32 = m.f32()
+    img = m._type(("image2d",), OpTypeImage, f32, 1, 0, 0, 0, 1, 0)   # Dim 2D, sampled, Unknown format
+    simg = m._type(("sampledimage", img), OpTypeSampledImage, img)
+    t = simg if count is None else m.array(simg, count)
+    var = m.variable(SCUniformConstant, m.ptr(SCUniformConstant, t))
+    m.decorate(var, DecDescriptorSet, set_)
+    m.decorate(var, DecBinding, binding)
+    return var, simg
+
+
+def textured_fs(set_=0, binding=0, explicit_lod=False):
+    """colour = texture(tex, uv) (OpImageSampleImplicitLod; OpImageSampleExplicitLod with Lod 0 when
+    `explicit_lod`)"""
+    m = Module()
+    m.capability(CapShader)
+    f32 = m.f32()
+    v2, v4 = m.vec(f32, 2), m.vec(f32, 4)
+    tex, simg = _sampler2d(m, set_, binding)
+    v_uv = _io(m, SCInput, v2, 0)
+    o = _io(m, SCOutput, v4, 0)
+    zero = m.cf(0.0)
+    fn = _begin_main(m)
+    si = m.res(OpLoad, simg, tex)
+    uv = m.res(OpLoad, v2, v_uv)
+    if explicit_lod:
+        c = m.res(OpImageSampleExplicitLod, v4, si, uv, ImageOperandsLod, zero)
+    else:
+        c = m.res(OpImageSampleImplicitLod, v4, si, uv)
+    m.op(OpStore, o, c)
+    _end_main(m)
+    m.entry(ExecFragment, fn, "main", [tex, v_uv, o])
+    m.mode(fn, ModeOriginUpperLeft)
+    return m.to_words()
+
+
+def textured_array_fs(count=2, set_=0, binding=0):
+    """colour = texture(tex[i], uv) with i = 1 where uv.x >= 0.5, else 0: a run-time index into an array of
+    combined image samplers"""
+    m = Module()
+    m.capability(CapShader)
+    f32 = m.f32()
+    i32 = m.i32()
+    v2, v4 = m.vec(f32, 2), m.vec(f32, 4)
+    tex, simg = _sampler2d(m, set_, binding, count)
+    v_uv = _io(m, SCInput, v2, 0)
+    o = _io(m, SCOutput, v4, 0)
+    half = m.cf(0.5)
+    fn = _begin_main(m)
+    uv = m.res(OpLoad, v2, v_uv)
+    u = m.res(OpCompositeExtract, f32, uv, 0)
+    lt = m.res(OpFOrdLessThan, m.bool(), u, half)
+    idx = m.res(OpSelect, i32, lt, m.ci(0), m.ci(1))
+    ptr = m.res(OpAccessChain, m.ptr(SCUniformConstant, simg), tex, idx)
+    si = m.res(OpLoad, simg, ptr)
+    c = m.res(OpImageSampleImplicitLod, v4, si, uv)
+    m.op(OpStore, o, c)
+    _end_main(m)
+    m.entry(ExecFragment, fn, "main", [tex, v_uv, o])
+    m.mode(fn, ModeOriginUpperLeft)
     return m.to_words()
 
 

@@ -47,6 +47,18 @@ ST_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO = 26
 ST_PIPELINE_DYNAMIC_STATE_CREATE_INFO = 27
 ST_GRAPHICS_PIPELINE_CREATE_INFO = 28
 ST_PIPELINE_LAYOUT_CREATE_INFO = 30
+ST_SAMPLER_CREATE_INFO = 31
+ST_DESCRIPTOR_SET_LAYOUT_CREATE_INFO = 32
+ST_DESCRIPTOR_POOL_CREATE_INFO = 33
+ST_DESCRIPTOR_SET_ALLOCATE_INFO = 34
+ST_WRITE_DESCRIPTOR_SET = 35
+ST_COPY_DESCRIPTOR_SET = 36
+DESCRIPTOR_COMBINED_IMAGE_SAMPLER = 1
+DESCRIPTOR_UNIFORM_BUFFER = 6
+DESCRIPTOR_UNIFORM_BUFFER_DYNAMIC = 8
+FILTER_NEAREST, FILTER_LINEAR = 0, 1
+ADDRESS_REPEAT, ADDRESS_MIRRORED_REPEAT, ADDRESS_CLAMP_TO_EDGE, ADDRESS_CLAMP_TO_BORDER, ADDRESS_MIRROR_CLAMP = 0, 1, 2, 3, 4
+VK_ERROR_OUT_OF_POOL_MEMORY = -1000069000
 ST_FRAMEBUFFER_CREATE_INFO = 37
 ST_RENDER_PASS_CREATE_INFO = 38
 ST_COMMAND_POOL_CREATE_INFO = 39
@@ -74,11 +86,13 @@ IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL = 7
 
 BUFFER_USAGE_TRANSFER_SRC = 0x1
 BUFFER_USAGE_TRANSFER_DST = 0x2
+BUFFER_USAGE_UNIFORM = 0x10
 BUFFER_USAGE_INDEX = 0x40
 BUFFER_USAGE_VERTEX = 0x80
 BUFFER_USAGE_INDIRECT = 0x100
 IMAGE_USAGE_TRANSFER_SRC = 0x1
 IMAGE_USAGE_TRANSFER_DST = 0x2
+IMAGE_USAGE_SAMPLED = 0x4
 IMAGE_USAGE_COLOR_ATTACHMENT = 0x10
 IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT = 0x20
 IMAGE_ASPECT_COLOR = 0x1
@@ -482,6 +496,59 @@ class VkRenderPassBeginInfo(Structure):
                 ("renderArea", VkRect2D), ("clearValueCount", c_uint32), ("pClearValues", POINTER(VkClearValue))]
 
 
+class VkSamplerCreateInfo(Structure):
+    _fields_ = [("sType", c_int), ("pNext", c_void_p), ("flags", c_uint32), ("magFilter", c_int),
+                ("minFilter", c_int), ("mipmapMode", c_int), ("addressModeU", c_int), ("addressModeV", c_int),
+                ("addressModeW", c_int), ("mipLodBias", c_float), ("anisotropyEnable", c_uint32),
+                ("maxAnisotropy", c_float), ("compareEnable", c_uint32), ("compareOp", c_int), ("minLod", c_float),
+                ("maxLod", c_float), ("borderColor", c_int), ("unnormalizedCoordinates", c_uint32)]
+
+
+class VkDescriptorSetLayoutBinding(Structure):
+    _fields_ = [("binding", c_uint32), ("descriptorType", c_int), ("descriptorCount", c_uint32),
+                ("stageFlags", c_uint32), ("pImmutableSamplers", c_void_p)]
+
+
+class VkDescriptorSetLayoutCreateInfo(Structure):
+    _fields_ = [("sType", c_int), ("pNext", c_void_p), ("flags", c_uint32), ("bindingCount", c_uint32),
+                ("pBindings", POINTER(VkDescriptorSetLayoutBinding))]
+
+
+class VkDescriptorPoolSize(Structure):
+    _fields_ = [("type", c_int), ("descriptorCount", c_uint32)]
+
+
+class VkDescriptorPoolCreateInfo(Structure):
+    _fields_ = [("sType", c_int), ("pNext", c_void_p), ("flags", c_uint32), ("maxSets", c_uint32),
+                ("poolSizeCount", c_uint32), ("pPoolSizes", POINTER(VkDescriptorPoolSize))]
+
+
+class VkDescriptorSetAllocateInfo(Structure):
+    _fields_ = [("sType", c_int), ("pNext", c_void_p), ("descriptorPool", c_void_p), ("descriptorSetCount", c_uint32),
+                ("pSetLayouts", POINTER(c_void_p))]
+
+
+class VkDescriptorImageInfo(Structure):
+    _fields_ = [("sampler", c_void_p), ("imageView", c_void_p), ("imageLayout", c_int)]
+
+
+class VkDescriptorBufferInfo(Structure):
+    _fields_ = [("buffer", c_void_p), ("offset", c_uint64), ("range", c_uint64)]
+
+
+class VkWriteDescriptorSet(Structure):
+    _fields_ = [("sType", c_int), ("pNext", c_void_p), ("dstSet", c_void_p), ("dstBinding", c_uint32),
+                ("dstArrayElement", c_uint32), ("descriptorCount", c_uint32), ("descriptorType", c_int),
+                ("pImageInfo", POINTER(VkDescriptorImageInfo)), ("pBufferInfo", POINTER(VkDescriptorBufferInfo)),
+                ("pTexelBufferView", c_void_p)]
+
+
+class VkCopyDescriptorSet(Structure):
+    _fields_ = [("sType", c_int), ("pNext", c_void_p), ("srcSet", c_void_p), ("srcBinding", c_uint32),
+                ("srcArrayElement", c_uint32), ("dstSet", c_void_p), ("dstBinding", c_uint32),
+                ("dstArrayElement", c_uint32), ("descriptorCount", c_uint32)]
+
+
 class VkExtensionProperties(Structure):
     _fields_ = [("extensionName", ctypes.c_char * 256), ("specVersion", c_uint32)]
 
@@ -567,6 +634,17 @@ _PROTOS = {
     "vkCmdDrawIndexedIndirect": (None, [H, H, c_uint64, c_uint32, c_uint32]),
     "vkEnumerateDeviceExtensionProperties": (c_int, [H, ctypes.c_char_p, P(c_uint32), P(VkExtensionProperties)]),
     "vkGetPhysicalDeviceFeatures": (None, [H, P(c_uint32)]),
+    "vkCreateSampler": (c_int, [H, P(VkSamplerCreateInfo), c_void_p, P(H)]),
+    "vkDestroySampler": (None, [H, H, c_void_p]),
+    "vkCreateDescriptorSetLayout": (c_int, [H, P(VkDescriptorSetLayoutCreateInfo), c_void_p, P(H)]),
+    "vkDestroyDescriptorSetLayout": (None, [H, H, c_void_p]),
+    "vkCreateDescriptorPool": (c_int, [H, P(VkDescriptorPoolCreateInfo), c_void_p, P(H)]),
+    "vkDestroyDescriptorPool": (None, [H, H, c_void_p]),
+    "vkResetDescriptorPool": (c_int, [H, H, c_uint32]),
+    "vkAllocateDescriptorSets": (c_int, [H, P(VkDescriptorSetAllocateInfo), P(H)]),
+    "vkFreeDescriptorSets": (c_int, [H, H, c_uint32, P(H)]),
+    "vkUpdateDescriptorSets": (None, [H, c_uint32, P(VkWriteDescriptorSet), c_uint32, P(VkCopyDescriptorSet)]),
+    "vkCmdBindDescriptorSets": (None, [H, c_int, H, c_uint32, c_uint32, P(H), c_uint32, P(c_uint32)]),
     "vkCmdDrawIndirectCountKHR": (None, [H, H, c_uint64, H, c_uint64, c_uint32, c_uint32]),
     "vkCmdDrawIndexedIndirectCountKHR": (None, [H, H, c_uint64, H, c_uint64, c_uint32, c_uint32]),
     "vkCmdBeginRenderPass": (None, [H, P(VkRenderPassBeginInfo), c_int]),

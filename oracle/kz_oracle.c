@@ -39,7 +39,87 @@ typedef struct {
   float c[4 + KZO_MAXK]; /* clip position x,y,z,w then varyings */
 } cvert;
 
-static int shader_varyings(const kzo_draw* d) { return d->shader == KZO_SHADER_COLOR ? 4 : 3; }
+static int shader_varyings(const kzo_draw* d) {
+  return d->shader == KZO_SHADER_COLOR ? 4 : d->shader == KZO_SHADER_TEXTURED ? 2 : 3;
+}
+
+/* ---- texture sampling (kz_pipeline.cu kz_tex2d restated) ---- */
+
+static int32_t tex_wrap(int32_t i, int32_t size, uint32_t mode) {
+  switch (mode) {
+    case 0: { /* REPEAT */
+      int32_t m = i % size;
+      return m < 0 ? m + size : m;
+    }
+    case 1: { /* MIRRORED_REPEAT */
+      int32_t m = i % (2 * size);
+      if (m < 0) m += 2 * size;
+      m -= size;
+      return size - 1 - (m >= 0 ? m : -(1 + m));
+    }
+    case 3: /* CLAMP_TO_BORDER */
+      return i < 0 || i >= size ? -1 : i;
+    case 4: { /* MIRROR_CLAMP_TO_EDGE */
+      int32_t mir = i >= 0 ? i : -(1 + i);
+      return mir < size ? mir : size - 1;
+    }
+    default: /* CLAMP_TO_EDGE */
+      return i < 0 ? 0 : (i >= size ? size - 1 : i);
+  }
+}
+
+static int32_t tex_int(float x) { return (int32_t)fminf(fmaxf(x, -1.0e9f), 1.0e9f); }
+
+static void tex_texel(const kzo_texture* t, int32_t i, int32_t j, float out[4]) {
+  if (i < 0 || j < 0) {
+    uint32_t b = (t->sampler >> 12) & 3u;
+    float c = b == 2 ? 1.0f : 0.0f;
+    out[0] = out[1] = out[2] = c;
+    out[3] = b == 0 ? 0.0f : 1.0f;
+    return;
+  }
+  const uint8_t* p = t->texels + (size_t)j * t->pitch + (size_t)i * 4;
+  float c[4];
+  for (int k = 0; k < 4; k++) c[k] = (float)p[k] / 255.0f;
+  if (t->format == 2) {
+    out[0] = c[2];
+    out[1] = c[1];
+    out[2] = c[0];
+  } else {
+    out[0] = c[0];
+    out[1] = c[1];
+    out[2] = c[2];
+  }
+  out[3] = c[3];
+}
+
+static float tex_lerp(float a, float b, float f) { return a + f * (b - a); }
+
+void kzo_tex2d(const kzo_texture* t, float s, float tc, float out[4]) {
+  const int32_t w = (int32_t)t->width, h = (int32_t)t->height;
+  const uint32_t mu = (t->sampler >> 4) & 7u, mv = (t->sampler >> 8) & 7u;
+  float u = s, v = tc;
+  if (!(t->sampler & 2u)) {
+    u = s * (float)w;
+    v = tc * (float)h;
+  }
+  if (!(t->sampler & 1u)) {
+    tex_texel(t, tex_wrap(tex_int(floorf(u)), w, mu), tex_wrap(tex_int(floorf(v)), h, mv), out);
+    return;
+  }
+  float u0 = u - 0.5f, v0 = v - 0.5f;
+  float fi = floorf(u0), fj = floorf(v0);
+  float a = fminf(fmaxf(u0 - fi, 0.0f), 1.0f), b = fminf(fmaxf(v0 - fj, 0.0f), 1.0f);
+  int32_t i0 = tex_int(fi), j0 = tex_int(fj);
+  int32_t x0 = tex_wrap(i0, w, mu), x1 = tex_wrap(i0 + 1, w, mu);
+  int32_t y0 = tex_wrap(j0, h, mv), y1 = tex_wrap(j0 + 1, h, mv);
+  float t00[4], t10[4], t01[4], t11[4];
+  tex_texel(t, x0, y0, t00);
+  tex_texel(t, x1, y0, t10);
+  tex_texel(t, x0, y1, t01);
+  tex_texel(t, x1, y1, t11);
+  for (int k = 0; k < 4; k++) out[k] = tex_lerp(tex_lerp(t00[k], t10[k], a), tex_lerp(t01[k], t11[k], a), b);
+}
 
 /* vertex shader: COLOR is gl_Position = in0, out0 = in1; LAMBERT is gl_Position = mvp * vec4(in0, 1),
  * out0 = in1.  OpMatrixTimesVector is r_i = fma(m3i, v3, fma(m2i, v2, fma(m1i, v1, m0i * v0))). */
@@ -47,6 +127,10 @@ static void run_vs(const kzo_draw* d, uint32_t vid, cvert* out) {
   if (d->shader == KZO_SHADER_COLOR) {
     const float* v = d->vertices + (size_t)vid * 8;
     for (int i = 0; i < 8; i++) out->c[i] = v[i];
+  } else if (d->shader == KZO_SHADER_TEXTURED) {
+    const float* v = d->vertices + (size_t)vid * 6;
+    for (int i = 0; i < 6; i++) out->c[i] = v[i];
+    out->c[6] = out->c[7] = 0.0f;
   } else {
     const float* v = d->vertices + (size_t)vid * 6;
     const float* m = d->mvp;
@@ -71,6 +155,8 @@ static void run_vs(const kzo_draw* d, uint32_t vid, cvert* out) {
 static void run_fs(const kzo_draw* d, const float* var, float out[4]) {
   if (d->shader == KZO_SHADER_COLOR) {
     for (int i = 0; i < 4; i++) out[i] = var[i];
+  } else if (d->shader == KZO_SHADER_TEXTURED) {
+    kzo_tex2d(&d->tex, var[0], var[1], out);
   } else {
     float n0 = var[0], n1 = var[1], n2 = var[2];
     float dd = fmaf(n2, n2, fmaf(n1, n1, n0 * n0));

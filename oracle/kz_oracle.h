@@ -34,11 +34,23 @@
 extern "C" {
 #endif
 
-enum { KZO_SHADER_COLOR = 0, KZO_SHADER_LAMBERT = 1 };
+enum { KZO_SHADER_COLOR = 0, KZO_SHADER_LAMBERT = 1, KZO_SHADER_TEXTURED = 2 };
+
+/* a combined image sampler of one mip level (the GPU's KzDescriptor): RGBA8 or BGRA8 UNORM texels */
+typedef struct kzo_texture {
+  const uint8_t* texels;    /* texel (0, 0) */
+  uint32_t width, height;
+  uint32_t pitch;           /* bytes per row */
+  uint32_t format;          /* 1: RGBA8, 2: BGRA8 */
+  uint32_t sampler;         /* bit 0 LINEAR, bit 1 unnormalized coordinates, bits 4..6 / 8..10 address mode u / v
+                               (VkSamplerAddressMode), bits 12..13 border (0 transparent black, 1 opaque
+                               black, 2 opaque white) */
+} kzo_texture;
 
 typedef struct kzo_draw {
   uint32_t shader;          /* KZO_SHADER_COLOR: pos f32x4 + rgba f32x4 (8 floats per vertex);
-                               KZO_SHADER_LAMBERT: pos f32x3 + normal f32x3 (6 floats per vertex) */
+                               KZO_SHADER_LAMBERT: pos f32x3 + normal f32x3 (6 floats per vertex);
+                               KZO_SHADER_TEXTURED: pos f32x4 + uv f32x2 (6 floats per vertex) */
   const float* vertices;
   const uint32_t* indices;  /* NULL for vkCmdDraw */
   uint32_t first;           /* firstVertex (vkCmdDraw) or firstIndex (vkCmdDrawIndexed) */
@@ -56,6 +68,7 @@ typedef struct kzo_draw {
   float blend_const[4];
   float viewport[6];        /* x, y, width, height, minDepth, maxDepth */
   int32_t scissor[4];       /* x, y, width, height */
+  kzo_texture tex;          /* TEXTURED fragment shader: colour = texture(tex, uv) */
 } kzo_draw;
 
 typedef struct kzo_stats {
@@ -80,6 +93,12 @@ void kzo_clear_depth(uint32_t width, float* depth, const int32_t rect[4], float 
 
 /* f32 -> UNORM8 as the driver stores it */
 uint8_t kzo_unorm8(float v);
+
+/* OpImageSample* on `t` at (s, t): NEAREST texel (floor u, floor v), or LINEAR
+ * lerp(lerp(t00, t10, a), lerp(t01, t11, a), b) around (u - 0.5, v - 0.5) with lerp(x, y, f) = x + f * (y - x),
+ * each operation rounded separately; u = s * width unless unnormalized; texels c / 255; the Vulkan
+ * specification's wrapping operation per address mode */
+void kzo_tex2d(const kzo_texture* t, float s, float tc, float out[4]);
 
 /* pixel rectangle of a draw: framebuffer & render area & scissor & viewport (x0, y0, x1, y1 exclusive) */
 void kzo_draw_rect(uint32_t width, uint32_t height, const int32_t render_area[4], const kzo_draw* d,

@@ -13,7 +13,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libkz_oracle.so")
 
-SHADER = {"color": 0, "lambert": 1}
+SHADER = {"color": 0, "lambert": 1, "textured": 2}
+
+
+class KzoTexture(ctypes.Structure):
+    _fields_ = [("texels", ctypes.c_void_p), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("pitch", ctypes.c_uint32), ("format", ctypes.c_uint32), ("sampler", ctypes.c_uint32)]
 
 
 class KzoDraw(ctypes.Structure):
@@ -25,7 +30,7 @@ class KzoDraw(ctypes.Structure):
                 ("blend_enable", ctypes.c_uint32), ("src_color", ctypes.c_uint32), ("dst_color", ctypes.c_uint32),
                 ("color_op", ctypes.c_uint32), ("src_alpha", ctypes.c_uint32), ("dst_alpha", ctypes.c_uint32),
                 ("alpha_op", ctypes.c_uint32), ("write_mask", ctypes.c_uint32), ("blend_const", ctypes.c_float * 4),
-                ("viewport", ctypes.c_float * 6), ("scissor", ctypes.c_int32 * 4)]
+                ("viewport", ctypes.c_float * 6), ("scissor", ctypes.c_int32 * 4), ("tex", KzoTexture)]
 
 
 class KzoStats(ctypes.Structure):
@@ -54,6 +59,8 @@ def lib():
                                  ctypes.POINTER(ctypes.c_int32), ctypes.c_uint32, ctypes.POINTER(KzoDraw),
                                  ctypes.c_int, ctypes.POINTER(KzoStats)]
         L.kzo_render.restype = ctypes.c_int
+        L.kzo_tex2d.argtypes = [ctypes.POINTER(KzoTexture), ctypes.c_float, ctypes.c_float,
+                                ctypes.POINTER(ctypes.c_float)]
         L.kzo_unorm8.argtypes = [ctypes.c_float]
         L.kzo_unorm8.restype = ctypes.c_uint8
         L.kzo_clear_color.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
@@ -62,6 +69,21 @@ def lib():
                                       ctypes.c_float]
         _LIB = L
     return _LIB
+
+
+def texture_struct(t):
+    """KzoTexture of a kazan_gb300.scenes.Texture (its texel array must stay alive)"""
+    a = t.texels
+    assert a.dtype == np.uint8 and a.flags.c_contiguous and a.ndim == 3 and a.shape[2] == 4
+    return KzoTexture(a.ctypes.data, a.shape[1], a.shape[0], a.shape[1] * 4, 2 if t.bgra else 1, t.sampler_bits())
+
+
+def tex2d(t, s, tc):
+    """kzo_tex2d: the oracle's sample of Texture t at (s, tc), as float32 [4]"""
+    ts = texture_struct(t)
+    out = (ctypes.c_float * 4)()
+    lib().kzo_tex2d(ctypes.byref(ts), float(s), float(tc), out)
+    return np.array(out[:], dtype=np.float32)
 
 
 def unorm8(v):
@@ -105,6 +127,8 @@ def make_draws(scene, draws=None):
         k.write_mask = 0xF
         k.viewport[:] = [0.0, 0.0, float(scene.width), float(scene.height), 0.0, 1.0]
         k.scissor[:] = [0, 0, scene.width, scene.height]
+        if scene.texture is not None:
+            k.tex = texture_struct(scene.texture)
     return arr, len(draws)
 
 

@@ -154,3 +154,51 @@ def test_run_time_indices_translate(built):
     vs = shader.Shader(spirv_asm.color_vs(), shader.VERTEX)
     img = shader.link(shader.emit_ptx([(vs, fs)], [_layouts()[0]]))
     assert img[:4] == b"\x7fELF"
+
+
+def test_descriptor_bindings_translate_and_link(built):
+    """a uniform block in the vertex shader and combined image samplers in the fragment shader: the stages
+    report their bindings, the PTX reads the block through the draw's descriptor slot and calls the
+    sampling function of the pipeline-kernel object, and the set links"""
+    uvs = shader.Shader(spirv_asm.lambert_ubo_vs(0, 0), shader.VERTEX)
+    assert uvs.bindings() == [(0, 0, 0, 1, 64)]
+    tvs = shader.Shader(spirv_asm.textured_vs(), shader.VERTEX)
+    tfs = shader.Shader(spirv_asm.textured_fs(1, 3), shader.FRAGMENT)
+    assert tfs.bindings() == [(1, 3, 1, 1, 0)]
+    afs = shader.Shader(spirv_asm.textured_array_fs(2, 0, 2), shader.FRAGMENT)
+    assert afs.bindings() == [(0, 2, 1, 2, 0)]
+    efs = shader.Shader(spirv_asm.textured_fs(explicit_lod=True), shader.FRAGMENT)
+    lam = shader.layout([(0, 0, 3, 0), (1, 0, 3, 12)], [24])
+    tex = shader.layout([(0, 0, 4, 0), (1, 0, 2, 16)], [24])
+    slots = [{(0, 0): 0}, {(1, 3): 5}, {(0, 2): 1}, {(0, 0): 0}]
+    ptx = shader.emit_ptx([(uvs, shader.Shader(spirv_asm.lambert_fs(), 4)), (tvs, tfs), (tvs, afs), (tvs, efs)],
+                          [lam, tex, tex, tex], slots)
+    # the block's address from slot 0 (byte 128 of the snapshot), texture descriptor 5 at 128 + 32 * 5
+    assert "[%kzpush+128]" in ptx
+    assert "add.s64 %kzd, %kzpg, 288;" in ptx
+    assert "call (kzt_r), kz_tex2d" in ptx and ".extern .func" in ptx
+    # the run-time array index scales by the descriptor size
+    assert "mul.wide.u32 %kzoff" in ptx
+    img = shader.link(ptx)
+    assert img[:4] == b"\x7fELF"
+
+
+def test_unsupported_descriptor_forms_are_rejected(built):
+    """separate images and samplers and storage buffers are reported, not mistranslated"""
+    from kazan_gb300.spirv_asm import (Module, CapShader, SCUniformConstant, OpTypeImage, ExecFragment,
+                                       ModeOriginUpperLeft, DecDescriptorSet, DecBinding, _begin_main, _end_main,
+                                       _io, SCOutput)
+    m = Module()
+    m.capability(CapShader)
+    f32 = m.f32()
+    img = m._type(("image2d",), OpTypeImage, f32, 1, 0, 0, 0, 1, 0)
+    var = m.variable(SCUniformConstant, m.ptr(SCUniformConstant, img))
+    m.decorate(var, DecDescriptorSet, 0)
+    m.decorate(var, DecBinding, 0)
+    o = _io(m, SCOutput, m.vec(f32, 4), 0)
+    fn = _begin_main(m)
+    _end_main(m)
+    m.entry(ExecFragment, fn, "main", [var, o])
+    m.mode(fn, ModeOriginUpperLeft)
+    with pytest.raises(shader.ShaderError, match="separate images"):
+        shader.Shader(m.to_words(), shader.FRAGMENT)
