@@ -39,7 +39,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "single", "soup", "blend", "serve"])
+    ap.add_argument("--workload", default="batched",
+                    choices=["batched", "single", "soup", "blend", "textured", "serve"])
     ap.add_argument("--budget-gb", type=float, default=40.0, help="serve: HBM admission budget")
     ap.add_argument("--ndraws", type=int, default=4096)
     ap.add_argument("--tile", type=int, default=16)
@@ -63,6 +64,12 @@ def make_scene(args):
         return scenes.single_large(), {"workload": "single large draw: 1M indexed tris, 1920x1080, Lambert, seed 2"}
     if args.workload == "soup":
         return scenes.small_soup(), {"workload": "plain single draw: 2048 tris, 256x256, seed 1"}
+    if args.workload == "textured":
+        return (scenes.textured(seed=6, n=200_000, width=1920, height=1080, tex_w=1024, tex_h=1024, size_lo=0.004,
+                                size_hi=0.08, linear=True),
+                {"workload": "textured: 200K tris (vertex radius log-uniform 0.004-0.08 NDC), 1920x1080, "
+                             "1024x1024 RGBA8 combined image sampler, LINEAR / REPEAT, perspective-correct uv, "
+                             "seed 6"})
     return scenes.ordered_blend(), {"workload": "ordered blend: 200K tris, 1920x1080, SRC_ALPHA blend, seed 4"}
 
 

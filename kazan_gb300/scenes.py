@@ -198,15 +198,17 @@ def ordered_blend(seed=4, n=200_000, width=1920, height=1080, amin=4.0, amax=409
                  depth_write=False, blend=True)
 
 
-def textured(seed=6, n=4000, width=640, height=360, tex_w=61, tex_h=37, uv_lo=-1.5, uv_hi=2.5, **sampler):
-    """n random triangles with per-vertex w in [0.5, 2] (perspective-correct texture coordinates) and
-    coordinates in [uv_lo, uv_hi] (every address mode is exercised), over a random RGBA8 texture of
-    tex_w x tex_h; `sampler` sets the Texture's filter and address fields"""
+def textured(seed=6, n=4000, width=640, height=360, tex_w=61, tex_h=37, uv_lo=-1.5, uv_hi=2.5, size_lo=0.01,
+             size_hi=0.6, **sampler):
+    """n random triangles (vertices at log-uniform distances in [size_lo, size_hi] NDC from a centre) with
+    per-vertex w in [0.5, 2] (perspective-correct texture coordinates) and coordinates in [uv_lo, uv_hi]
+    (every address mode is exercised), over a random RGBA8 texture of tex_w x tex_h; `sampler` sets the
+    Texture's filter and address fields"""
     rng = np.random.default_rng(seed)
     v = np.empty((3 * n, 6), dtype=np.float32)
     cx = rng.uniform(-1.1, 1.1, n)
     cy = rng.uniform(-1.1, 1.1, n)
-    size = np.exp(rng.uniform(np.log(0.01), np.log(0.6), n))
+    size = np.exp(rng.uniform(np.log(size_lo), np.log(size_hi), n))
     for k in range(3):
         ang = rng.uniform(0, 2 * np.pi, n)
         w = rng.uniform(0.5, 2.0, n)
