@@ -573,10 +573,29 @@ void VKAPI_CALL kzCmdClearColorImage(VkCommandBuffer cbh, VkImage image, VkImage
 }
 
 void VKAPI_CALL kzCmdClearDepthStencilImage(VkCommandBuffer cbh, VkImage image, VkImageLayout,
-                                            const VkClearDepthStencilValue* v, uint32_t,
-                                            const VkImageSubresourceRange*) {
-  /* api_impl.rs:4792 */
-  clear_image(H<CommandBuffer>(cbh), H<Image>(image), float_bits(v->depth));
+                                            const VkClearDepthStencilValue* v, uint32_t n,
+                                            const VkImageSubresourceRange* ranges) {
+  /* api_impl.rs:4792: the clear value in the image's format (D16 / D24: rint(depth * (2^bits - 1)), as the
+   * kernels convert fragment depths); a D24S8 image is cleared in both aspects at once */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  Image* img = H<Image>(image);
+  if (img->format == VK_FORMAT_D16_UNORM) {
+    uint32_t q = (uint32_t)std::rint(v->depth * 65535.0f);
+    clear_image(cb, img, q | (q << 16));
+    cb->ops.back().rect[2] = (int32_t)((img->width + 1) / 2); /* two texels per 32-bit word */
+  } else if (img->format == VK_FORMAT_D24_UNORM_S8_UINT) {
+    VkImageAspectFlags aspects = 0;
+    for (uint32_t i = 0; i < n; i++) aspects |= ranges[i].aspectMask;
+    if ((aspects & (VK_IMAGE_ASPECT_DEPTH_BIT | VK_IMAGE_ASPECT_STENCIL_BIT)) !=
+        (VK_IMAGE_ASPECT_DEPTH_BIT | VK_IMAGE_ASPECT_STENCIL_BIT)) {
+      log_error("vkCmdClearDepthStencilImage: a D24S8 image is cleared in both aspects together");
+      cb->record_error = VK_ERROR_FEATURE_NOT_PRESENT;
+      return;
+    }
+    clear_image(cb, img, (uint32_t)std::rint(v->depth * 16777215.0f) | ((v->stencil & 0xFFu) << 24));
+  } else {
+    clear_image(cb, img, float_bits(v->depth));
+  }
 }
 
 void VKAPI_CALL kzCmdPipelineBarrier(VkCommandBuffer, VkPipelineStageFlags, VkPipelineStageFlags, VkDependencyFlags,
@@ -739,6 +758,16 @@ static void segment_target(const PassRec& pr, KzSegment& s, uint32_t tile, bool 
     const VkAttachmentDescription& a = rp->atts[(size_t)rp->depth_att];
     if (first && a.loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR) s.depth_load = KZ_LOAD_CLEAR;
     s.clear_depth = pr.clear_depth.depthStencil.depth;
+    s.stencil_load = KZ_LOAD_LOAD;
+    if (img->format == VK_FORMAT_D16_UNORM) {
+      s.depth_format = KZ_DF_D16;
+      s.clear_depth = std::rint(s.clear_depth * 65535.0f);
+    } else if (img->format == VK_FORMAT_D24_UNORM_S8_UINT) {
+      s.depth_format = KZ_DF_D24S8;
+      s.clear_depth = std::rint(s.clear_depth * 16777215.0f);
+      s.clear_stencil = pr.clear_depth.depthStencil.stencil & 0xFFu;
+      if (first && a.stencilLoadOp == VK_ATTACHMENT_LOAD_OP_CLEAR) s.stencil_load = KZ_LOAD_CLEAR;
+    }
     add_unique(low.writes, img->mem);
     if (s.depth_load == KZ_LOAD_LOAD) add_unique(low.reads, img->mem);
   }
@@ -748,10 +777,11 @@ static void segment_target(const PassRec& pr, KzSegment& s, uint32_t tile, bool 
   s.area[3] = std::min((int32_t)s.height, s.area[3]);
 }
 
-static int raster_class(const DrawRec& d) {
+static int raster_class(const DrawRec& d, bool vis_ok) {
   /* draws that share a class can share one segment: visibility mode with the same key and write mask,
-   * or ordered mode; indirect draws never share a segment with direct ones */
-  int k = d.pipe->vis_key >= 0 ? 1 + d.pipe->vis_key + 16 * (int)d.pipe->pipe.write_mask : 0;
+   * or ordered mode; indirect draws never share a segment with direct ones.  Passes whose depth
+   * attachment is not D32 render in ordered mode only. */
+  int k = vis_ok && d.pipe->vis_key >= 0 ? 1 + d.pipe->vis_key + 16 * (int)d.pipe->pipe.write_mask : 0;
   return d.indirect ? k + 1024 : k;
 }
 
@@ -994,6 +1024,11 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
       continue;
     }
     const PassRec& pr = cb->passes[op.pass];
+    bool vis_ok = true;
+    if (pr.rp->depth_att >= 0 && (size_t)pr.rp->depth_att < pr.fb->views.size()) {
+      VkFormat df = pr.fb->views[(size_t)pr.rp->depth_att]->image->format;
+      vis_ok = df == VK_FORMAT_D32_SFLOAT;
+    }
     /* split the pass into segments */
     std::vector<std::pair<size_t, size_t>> runs; /* [begin, end) draw indices */
     if (low.mode == 2) {
@@ -1001,7 +1036,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
     } else {
       size_t b = 0;
       for (size_t i = 1; i <= pr.draws.size(); i++)
-        if (i == pr.draws.size() || raster_class(pr.draws[i]) != raster_class(pr.draws[b])) {
+        if (i == pr.draws.size() || raster_class(pr.draws[i], vis_ok) != raster_class(pr.draws[b], vis_ok)) {
           runs.push_back({b, i});
           b = i;
         }
@@ -1030,7 +1065,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
           s.indirect = 1;
           guess = std::max<uint64_t>(guess, dr.d.elem_limit / 3);
         }
-        if (i == runs[r].first && dr.pipe->vis_key >= 0) {
+        if (i == runs[r].first && vis_ok && dr.pipe->vis_key >= 0) {
           s.mode = KZ_MODE_VISIBILITY;
           s.vis_key = (uint32_t)dr.pipe->vis_key;
         }

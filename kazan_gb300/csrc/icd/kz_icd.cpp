@@ -216,7 +216,9 @@ static uint32_t format_bpp(VkFormat f) {
   switch (f) {
     case VK_FORMAT_R8G8B8A8_UNORM:
     case VK_FORMAT_B8G8R8A8_UNORM:
-    case VK_FORMAT_D32_SFLOAT: return 4;
+    case VK_FORMAT_D32_SFLOAT:
+    case VK_FORMAT_D24_UNORM_S8_UINT: return 4;
+    case VK_FORMAT_D16_UNORM: return 2;
     default: return 0;
   }
 }
@@ -437,6 +439,8 @@ static void VKAPI_CALL kzGetPhysicalDeviceFormatProperties(VkPhysicalDevice, VkF
           VK_FORMAT_FEATURE_SAMPLED_IMAGE_BIT | VK_FORMAT_FEATURE_SAMPLED_IMAGE_FILTER_LINEAR_BIT;
       break;
     case VK_FORMAT_D32_SFLOAT:
+    case VK_FORMAT_D16_UNORM:
+    case VK_FORMAT_D24_UNORM_S8_UINT:
       p->optimalTilingFeatures = p->linearTilingFeatures = VK_FORMAT_FEATURE_DEPTH_STENCIL_ATTACHMENT_BIT | xfer;
       break;
     default:
@@ -723,7 +727,7 @@ static VkResult VKAPI_CALL kzCreateImage(VkDevice, const VkImageCreateInfo* ci, 
   img->tiling = ci->tiling;
   img->usage = ci->usage;
   img->bpp = bpp;
-  img->pitch = img->width * bpp;
+  img->pitch = (img->width * bpp + 3u) & ~3u; /* whole 32-bit words: a D16 row is cleared two texels per word */
   img->size = (VkDeviceSize)img->pitch * img->height;
   *out = to_handle<VkImage>(img);
   return VK_SUCCESS;
@@ -1172,7 +1176,17 @@ static VkResult create_graphics_pipeline(const VkGraphicsPipelineCreateInfo& ci,
     r = VK_ERROR_FEATURE_NOT_PRESENT;
   if (ci.pDepthStencilState) {
     const VkPipelineDepthStencilStateCreateInfo& ds = *ci.pDepthStencilState;
-    if (ds.stencilTestEnable || ds.depthBoundsTestEnable) r = VK_ERROR_FEATURE_NOT_PRESENT;
+    if (ds.depthBoundsTestEnable) r = VK_ERROR_FEATURE_NOT_PRESENT;
+    if (ds.stencilTestEnable) {
+      kp.stencil_test = 1;
+      const VkStencilOpState* faces[2] = {&ds.front, &ds.back};
+      for (int f = 0; f < 2; f++) {
+        const VkStencilOpState& so = *faces[f];
+        kp.stencil[2 * f] = (uint32_t)so.failOp | ((uint32_t)so.passOp << 3) | ((uint32_t)so.depthFailOp << 6) |
+                            ((uint32_t)so.compareOp << 9);
+        kp.stencil[2 * f + 1] = (so.compareMask & 0xFFu) | ((so.writeMask & 0xFFu) << 8) | ((so.reference & 0xFFu) << 16);
+      }
+    }
     kp.depth_test = ds.depthTestEnable;
     kp.depth_write = ds.depthWriteEnable;
     kp.depth_compare = ds.depthCompareOp;
@@ -1237,7 +1251,7 @@ static VkResult create_graphics_pipeline(const VkGraphicsPipelineCreateInfo& ci,
   }
   /* order-independent visibility resolve: no blending, no discard, and a depth rule that the
    * (depth, primitive) key reproduces */
-  if (!kp.blend_enable && !kp.fs_discards) {
+  if (!kp.blend_enable && !kp.fs_discards && !kp.stencil_test) {
     if (!kp.depth_test) p->vis_key = KZ_VIS_LAST;
     else if (kp.depth_write) {
       switch (kp.depth_compare) {

@@ -74,6 +74,11 @@ enum KzLoad { KZ_LOAD_LOAD = 0, KZ_LOAD_CLEAR = 1, KZ_LOAD_DONT_CARE = 2 };
 /* colour formats the raster stores */
 enum KzColorFormat { KZ_CF_NONE = 0, KZ_CF_RGBA8 = 1, KZ_CF_BGRA8 = 2 };
 
+/* depth attachment formats.  D16 and D24 depths are compared and stored as rint(z * (2^bits - 1)), an
+ * integer the kernels hold in a float (exact below 2^24); D24S8 texels keep the depth in bits 0..23 and
+ * the stencil in bits 24..31.  Only ordered segments render into D16 / D24S8. */
+enum KzDepthFormat { KZ_DF_D32 = 0, KZ_DF_D16 = 1, KZ_DF_D24S8 = 2 };
+
 typedef struct KzAttr {
   uint32_t location;
   uint32_t binding;
@@ -102,6 +107,10 @@ typedef struct KzPipe {
   uint32_t has_fs;
   float blend_const[4];
   uint32_t fs_passthrough;    /* the fragment shader only copies varyings 0..3 to colour components 0..3 */
+  uint32_t stencil_test;      /* VkPipelineDepthStencilStateCreateInfo::stencilTestEnable */
+  /* front and back VkStencilOpState, two words each: failOp | passOp << 3 | depthFailOp << 6 | compareOp << 9,
+   * then compareMask | writeMask << 8 | reference << 16 */
+  uint32_t stencil[4];
   uint32_t pad;
 } KzPipe;
 
@@ -212,7 +221,9 @@ typedef struct KzSegment {
   uint64_t lut_table;        /* indirect: room for the draw lookup; kz_k_indirect points draw_lut at it when
                                 the segment's primitives need at most lut_cap entries, else sets it to 0 */
   uint32_t lut_cap;
-  uint32_t pad;
+  uint32_t depth_format;     /* KzDepthFormat; clear_depth holds the converted value for D16 / D24S8 */
+  uint32_t stencil_load;     /* KzLoad of the stencil aspect (D24S8) */
+  uint32_t clear_stencil;
 } KzSegment;
 
 /* status words written by the kernels (one per submission) */

@@ -1059,6 +1059,67 @@ __device__ __forceinline__ float* depth_px(const KzSegment& seg, int32_t x, int3
   return reinterpret_cast<float*>(reinterpret_cast<char*>(seg.depth) + (size_t)y * seg.depth_pitch) + x;
 }
 
+/* the depth texel at (x, y) as the depth test compares it (D32: the float; D16 / D24: the integer in a
+ * float), and the stencil value of a D24S8 texel */
+__device__ __forceinline__ float load_depth(const KzSegment& seg, int32_t x, int32_t y, uint32_t& stencil) {
+  const char* row = reinterpret_cast<const char*>(seg.depth) + (size_t)y * seg.depth_pitch;
+  stencil = 0;
+  if (seg.depth_format == KZ_DF_D16) return (float)reinterpret_cast<const uint16_t*>(row)[x];
+  if (seg.depth_format == KZ_DF_D24S8) {
+    uint32_t w = reinterpret_cast<const uint32_t*>(row)[x];
+    stencil = w >> 24;
+    return (float)(w & 0xFFFFFFu);
+  }
+  return reinterpret_cast<const float*>(row)[x];
+}
+
+__device__ __forceinline__ void store_depth(const KzSegment& seg, int32_t x, int32_t y, float d, uint32_t stencil) {
+  char* row = reinterpret_cast<char*>(seg.depth) + (size_t)y * seg.depth_pitch;
+  if (seg.depth_format == KZ_DF_D16) reinterpret_cast<uint16_t*>(row)[x] = (uint16_t)d;
+  else if (seg.depth_format == KZ_DF_D24S8) reinterpret_cast<uint32_t*>(row)[x] = (uint32_t)d | (stencil << 24);
+  else reinterpret_cast<float*>(row)[x] = d;
+}
+
+/* a fragment depth z in [0, 1] as the depth format compares and stores it: rint(z * (2^bits - 1)) for
+ * D16 / D24 (the product a correctly rounded single), z itself for D32 */
+__device__ __forceinline__ float depth_value(float z, uint32_t format) {
+  if (format == KZ_DF_D16) return rintf(fmul(z, 65535.0f));
+  if (format == KZ_DF_D24S8) return rintf(fmul(z, 16777215.0f));
+  return z;
+}
+
+/* the stencil test: reference OP stored, both under the compare mask (VkCompareOp) */
+__device__ __forceinline__ bool stencil_cmp(uint32_t op, uint32_t ref, uint32_t val) {
+  switch (op) {
+    case 0: return false;
+    case 1: return ref < val;
+    case 2: return ref == val;
+    case 3: return ref <= val;
+    case 4: return ref > val;
+    case 5: return ref != val;
+    case 6: return ref >= val;
+    default: return true;
+  }
+}
+
+/* VkStencilOp `op` on stored value s through the write mask; w1 = compareMask | writeMask << 8 |
+ * reference << 16 */
+__device__ __forceinline__ uint32_t stencil_apply(uint32_t op, uint32_t s, uint32_t w1) {
+  uint32_t v;
+  switch (op) {
+    case 1: v = 0; break;
+    case 2: v = (w1 >> 16) & 0xFFu; break;
+    case 3: v = s < 255u ? s + 1u : 255u; break;
+    case 4: v = s > 0u ? s - 1u : 0u; break;
+    case 5: v = ~s & 0xFFu; break;
+    case 6: v = (s + 1u) & 0xFFu; break;
+    case 7: v = (s - 1u) & 0xFFu; break;
+    default: v = s; break;
+  }
+  uint32_t wm = (w1 >> 8) & 0xFFu;
+  return (s & ~wm) | (v & wm);
+}
+
 /* ================= visibility-buffer path (opaque segments) ================= */
 
 #define KZ_SMALL_PX 32      /* clipped sub-triangles with boxes of at most this many pixels are rasterised by
@@ -1717,6 +1778,9 @@ struct BatchEntry {
   uint32_t blend;          /* 0 none, 1 straight alpha (SRC_ALPHA, ONE_MINUS_SRC_ALPHA, ADD), 2 any other */
   uint32_t write_mask;
   uint32_t thr;            /* bit k: edge k's threshold is 1 */
+  uint32_t stencil;        /* bit 0 stencil test, bit 1 the fragment shader runs before the tests (it may
+                              discard, and a discarded fragment leaves the stencil alone) */
+  uint32_t st[4];          /* KzPipe::stencil, front then back */
 };
 static_assert(KZ_SORT_CAP * 8 + KZ_BATCH * sizeof(BatchEntry) <= KZ_DYN_SMEM,
               "ordered tile raster: sort keys and batch fit the dynamic shared memory");
@@ -1744,13 +1808,15 @@ __device__ __forceinline__ uint32_t blend_straight_alpha(uint32_t dst, const flo
  * blockDim.x) (64x64 tiles take four calls).  The bin is sorted by primitive number; each batch of
  * KZ_BATCH triangles is set up in shared memory, then every thread runs its pixels through the batch in
  * order: coverage, depth test, fragment shader, depth write, blend.  `u8tab`: u8f(k) for k = 0..255. */
-template <int PER>
+template <int PER, bool DS>
 __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* smem, const float* u8tab, int base) {
   const KzSegment& seg = *c.seg;
   TileInfo ti;
   if (!tile_info(seg, t, ti)) return;
   bool clear_c = seg.color_load == KZ_LOAD_CLEAR, clear_d = seg.depth_load == KZ_LOAD_CLEAR;
-  if (ti.n == 0 && !clear_c && !clear_d) return;
+  /* DS: a D16 / D24S8 attachment (integer depths, stencil); otherwise D32 without stencil */
+  const bool has_st = DS && seg.depth_format == KZ_DF_D24S8, clear_s = has_st && seg.stencil_load == KZ_LOAD_CLEAR;
+  if (ti.n == 0 && !clear_c && !clear_d && !clear_s) return;
   if (ti.n > KZ_SORT_CAP) {
     if (threadIdx.x == 0) atomicOr(&c.st->flags, KZ_STATUS_BIN_TOO_LARGE);
     return;
@@ -1793,6 +1859,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
   bool in[PER];
   uint32_t colv[PER];
   float depv[PER];
+  uint32_t stv[PER];
 #pragma unroll
   for (int q = 0; q < PER; q++) {
     int i = base + (int)threadIdx.x + q * (int)blockDim.x;
@@ -1802,9 +1869,17 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
     in[q] = i < T * T && x >= ti.x0 && x <= ti.x1 && y >= ti.y0 && y <= ti.y1;
     colv[q] = 0;
     depv[q] = 1.0f;
+    stv[q] = 0;
     if (!in[q]) continue;
     if (has_color) colv[q] = to_rgba(clear_c ? seg.clear_color : *color_px(seg, x, y), seg.color_format);
-    if (has_depth) depv[q] = clear_d ? seg.clear_depth : *depth_px(seg, x, y);
+    if (has_depth && DS) {
+      uint32_t s0 = 0;
+      float d0 = clear_d && (clear_s || !has_st) ? 0.0f : load_depth(seg, x, y, s0);
+      depv[q] = clear_d ? seg.clear_depth : d0;
+      stv[q] = clear_s ? seg.clear_stencil : s0;
+    } else if (has_depth) {
+      depv[q] = clear_d ? seg.clear_depth : *depth_px(seg, x, y);
+    }
   }
   const int64_t tpx = (int64_t)ti.ox * 256 + 128, tpy = (int64_t)ti.oy * 256 + 128;
   uint32_t frags = 0;
@@ -1841,6 +1916,9 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
                       bp.dst_alpha == 7 && bp.alpha_op == 0;
       be.blend = bp.blend_enable ? (straight ? 1u : 2u) : 0u;
       be.write_mask = bp.write_mask;
+      be.stencil = bp.stencil_test && has_st ? (1u | (bp.fs_discards ? 2u : 0u)) : 0u;
+#pragma unroll
+      for (int k = 0; k < 4; k++) be.st[k] = bp.stencil[k];
       /* edge values at the tile's first pixel centre, from the record that shading uses */
       Edges ed;
       edges_of(be.s.r, ed);
@@ -1893,11 +1971,28 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
         float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
         z = fadd(fminf(fmaxf(z, be.zmin), be.zmax), 0.0f);
         const bool dtest = (be.depth & 1u) && has_depth;
-        if (dtest && !depth_cmp(be.depth >> 2, z, depv[q])) continue;
+        const float zq = DS ? depth_value(z, seg.depth_format) : z;
         int32_t x = ti.ox + lx[q], y = ti.oy + ly[q];
         float col[4];
-        if (shade_pixel<false>(c, be.s, x, y, E, z, col)) continue;
-        if (dtest && (be.depth & 2u)) depv[q] = z;
+        if (DS && be.stencil) {
+          /* late tests when the shader may discard: a discarded fragment changes nothing */
+          if ((be.stencil & 2u) && shade_pixel<false>(c, be.s, x, y, E, z, col)) continue;
+          const bool dpass = !dtest || depth_cmp(be.depth >> 2, zq, depv[q]);
+          const bool front = (be.s.r.info >> 8) & 1u;
+          const uint32_t w0 = front ? be.st[0] : be.st[2], w1 = front ? be.st[1] : be.st[3];
+          const uint32_t cm = w1 & 0xFFu, sv = stv[q];
+          if (!stencil_cmp((w0 >> 9) & 7u, (w1 >> 16) & cm, sv & cm)) {
+            stv[q] = stencil_apply(w0 & 7u, sv, w1);
+            continue;
+          }
+          stv[q] = stencil_apply(dpass ? (w0 >> 3) & 7u : (w0 >> 6) & 7u, sv, w1);
+          if (!dpass) continue;
+          if (!(be.stencil & 2u) && shade_pixel<false>(c, be.s, x, y, E, z, col)) continue;
+        } else {
+          if (dtest && !depth_cmp(be.depth >> 2, zq, depv[q])) continue;
+          if (shade_pixel<false>(c, be.s, x, y, E, z, col)) continue;
+        }
+        if (dtest && (be.depth & 2u)) depv[q] = zq;
         if (!has_color) continue;
         if (be.blend == 1u) colv[q] = blend_straight_alpha(colv[q], col, u8tab, be.write_mask);
         else colv[q] = color_write(c.pipes[be.s.pipe], colv[q], col, u8tab);
@@ -1913,18 +2008,22 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
     if (!in[q]) continue;
     int32_t x = ti.ox + lx[q], y = ti.oy + ly[q];
     if (has_color) *color_px(seg, x, y) = from_rgba(colv[q], seg.color_format);
-    if (has_depth) *depth_px(seg, x, y) = depv[q];
+    if (has_depth && DS) store_depth(seg, x, y, depv[q], stv[q]);
+    else if (has_depth) *depth_px(seg, x, y) = depv[q];
   }
 }
 
 __device__ void raster_tile(const Ctx& c, uint32_t t, unsigned char* smem, const float* u8tab) {
   const uint32_t T = c.seg->tile;
+  const bool ds = c.seg->depth_format != KZ_DF_D32;
   if (T <= 16) {
-    raster_tile_ordered<1>(c, t, smem, u8tab, 0);
+    if (ds) raster_tile_ordered<1, true>(c, t, smem, u8tab, 0);
+    else raster_tile_ordered<1, false>(c, t, smem, u8tab, 0);
   } else {
     for (int base = 0; base < (int)(T * T); base += 4 * KZ_THREADS) {
       __syncthreads();
-      raster_tile_ordered<4>(c, t, smem, u8tab, base);
+      if (ds) raster_tile_ordered<4, true>(c, t, smem, u8tab, base);
+      else raster_tile_ordered<4, false>(c, t, smem, u8tab, base);
     }
   }
   __syncthreads();

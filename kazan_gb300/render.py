@@ -27,6 +27,14 @@ class Image:
         self.mapped = None
 
 
+def _aspect(fmt):
+    if fmt in (vk.FORMAT_D32_SFLOAT, vk.FORMAT_D16_UNORM):
+        return vk.IMAGE_ASPECT_DEPTH
+    if fmt == vk.FORMAT_D24_UNORM_S8_UINT:
+        return vk.IMAGE_ASPECT_DEPTH | vk.IMAGE_ASPECT_STENCIL
+    return vk.IMAGE_ASPECT_COLOR
+
+
 class Renderer:
     def __init__(self, driver=None):
         self.drv = driver or vk.Driver()
@@ -157,7 +165,7 @@ class Renderer:
         mem = self._alloc(req, host_visible)
         check("vkBindImageMemory", d.vkBindImageMemory(self.device, h, mem, 0))
         self._objects.append(("Image", h))
-        aspect = vk.IMAGE_ASPECT_DEPTH if fmt == vk.FORMAT_D32_SFLOAT else vk.IMAGE_ASPECT_COLOR
+        aspect = _aspect(fmt)
         vci = vk.VkImageViewCreateInfo(vk.ST_IMAGE_VIEW_CREATE_INFO, None, 0, h, vk.IMAGE_VIEW_TYPE_2D, fmt,
                                        (ctypes.c_int * 4)(0, 0, 0, 0), vk.VkImageSubresourceRange(aspect, 0, 1, 0, 1))
         view = c_void_p()
@@ -176,7 +184,7 @@ class Renderer:
         else:
             staging = self.create_buffer(n, 0, True)
             cb = self.begin()
-            aspect = vk.IMAGE_ASPECT_DEPTH if img.format == vk.FORMAT_D32_SFLOAT else vk.IMAGE_ASPECT_COLOR
+            aspect = _aspect(img.format)
             region = vk.VkBufferImageCopy(0, 0, 0, vk.VkImageSubresourceLayers(aspect, 0, 0, 1),
                                           vk.VkOffset3D(0, 0, 0), vk.VkExtent3D(img.width, img.height, 1))
             self.drv.vkCmdCopyImageToBuffer(cb, img.handle, vk.IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, staging.handle, 1,
@@ -186,9 +194,16 @@ class Renderer:
             p = self.map(staging)
             raw = np.ctypeslib.as_array((ctypes.c_uint8 * n).from_address(p)).copy()
             self.unmap(staging)
-        raw = raw.reshape(img.height, img.pitch)
+        # a host-visible image is read at its row pitch; a copy to a buffer packs rows tightly
+        bpp = 2 if img.format == vk.FORMAT_D16_UNORM else 4
+        raw = raw.reshape(img.height, img.pitch) if img.host_visible else raw[:img.height * img.width * bpp].reshape(
+            img.height, img.width * bpp)
         if img.format == vk.FORMAT_D32_SFLOAT:
             return raw[:, :img.width * 4].copy().view(np.float32)
+        if img.format == vk.FORMAT_D16_UNORM:
+            return raw[:, :img.width * 2].copy().view(np.uint16)
+        if img.format == vk.FORMAT_D24_UNORM_S8_UINT:
+            return raw[:, :img.width * 4].copy().view(np.uint32)
         return raw[:, :img.width * 4].reshape(img.height, img.width, 4).copy()
 
     # ---------------------------------------------------------------------------------------------
@@ -224,11 +239,12 @@ class Renderer:
         self.submit_wait(cb)
 
     # ---------------------------------------------------------------------------------------------
-    def render_pass(self, color_fmt, depth, color_load=vk.LOAD_OP_CLEAR, depth_load=vk.LOAD_OP_CLEAR):
+    def render_pass(self, color_fmt, depth, color_load=vk.LOAD_OP_CLEAR, depth_load=vk.LOAD_OP_CLEAR,
+                    depth_fmt=vk.FORMAT_D32_SFLOAT, stencil_load=vk.LOAD_OP_CLEAR):
         atts = (vk.VkAttachmentDescription * 2)()
         atts[0] = vk.VkAttachmentDescription(0, color_fmt, 1, color_load, vk.STORE_OP_STORE, 2, 1,
                                              vk.IMAGE_LAYOUT_UNDEFINED, vk.IMAGE_LAYOUT_GENERAL)
-        atts[1] = vk.VkAttachmentDescription(0, vk.FORMAT_D32_SFLOAT, 1, depth_load, vk.STORE_OP_STORE, 2, 1,
+        atts[1] = vk.VkAttachmentDescription(0, depth_fmt, 1, depth_load, vk.STORE_OP_STORE, stencil_load, 0,
                                              vk.IMAGE_LAYOUT_UNDEFINED, vk.IMAGE_LAYOUT_GENERAL)
         cref = vk.VkAttachmentReference(0, vk.IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL)
         dref = vk.VkAttachmentReference(1, vk.IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL)
@@ -361,10 +377,14 @@ class Renderer:
                                                        0, 0.0, 0.0, 0.0, 1.0)
         ms = vk.VkPipelineMultisampleStateCreateInfo(vk.ST_PIPELINE_MULTISAMPLE_STATE_CREATE_INFO, None, 0, 1, 0,
                                                      0.0, None, 0, 0)
+        faces = [vk.VkStencilOpState(), vk.VkStencilOpState()]
+        if scene.stencil is not None:
+            faces = [vk.VkStencilOpState(so.fail, so.pass_, so.depth_fail, so.compare, so.compare_mask, so.write_mask,
+                                         so.reference) for so in (scene.stencil["front"], scene.stencil["back"])]
         ds = vk.VkPipelineDepthStencilStateCreateInfo(vk.ST_PIPELINE_DEPTH_STENCIL_STATE_CREATE_INFO, None, 0,
                                                       int(scene.depth_test), int(scene.depth_write),
-                                                      scene.depth_compare, 0, 0, vk.VkStencilOpState(),
-                                                      vk.VkStencilOpState(), 0.0, 1.0)
+                                                      scene.depth_compare, 0, int(scene.stencil is not None),
+                                                      faces[0], faces[1], 0.0, 1.0)
         if scene.blend:
             att = vk.VkPipelineColorBlendAttachmentState(1, vk.BLEND_SRC_ALPHA, vk.BLEND_ONE_MINUS_SRC_ALPHA,
                                                          vk.BLEND_OP_ADD, vk.BLEND_SRC_ALPHA,
@@ -430,10 +450,10 @@ class SceneRun:
             r.write_buffer(self.ib, scene.indices, keep_mapped=keep_mapped and host_visible)
         self.color = r.create_image(scene.width, scene.height, vk.FORMAT_R8G8B8A8_UNORM,
                                     vk.IMAGE_USAGE_COLOR_ATTACHMENT, host_visible)
-        self.depth = r.create_image(scene.width, scene.height, vk.FORMAT_D32_SFLOAT,
+        self.depth = r.create_image(scene.width, scene.height, vk.DEPTH_FORMATS[scene.depth_format],
                                     vk.IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT,
                                     host_visible if depth_host_visible is None else depth_host_visible)
-        self.rp = r.render_pass(vk.FORMAT_R8G8B8A8_UNORM, True)
+        self.rp = r.render_pass(vk.FORMAT_R8G8B8A8_UNORM, True, depth_fmt=vk.DEPTH_FORMATS[scene.depth_format])
         self.fb = r.framebuffer(self.rp, [self.color.view, self.depth.view], scene.width, scene.height)
         # descriptor sets: the textured scene's sampler2D, or the Lambert matrices in a uniform buffer (one
         # 256-byte slot per draw, selected by a dynamic offset)
@@ -485,6 +505,7 @@ class SceneRun:
         clears = (vk.VkClearValue * 2)()
         clears[0].color.float32[:] = list(s.clear_color)
         clears[1].depthStencil.depth = s.clear_depth
+        clears[1].depthStencil.stencil = s.clear_stencil
         rbi = vk.VkRenderPassBeginInfo(vk.ST_RENDER_PASS_BEGIN_INFO, None, self.rp, self.fb,
                                        vk.VkRect2D(vk.VkOffset2D(0, 0), vk.VkExtent2D(s.width, s.height)), 2, clears)
         d.vkCmdBeginRenderPass(cb, byref(rbi), vk.SUBPASS_CONTENTS_INLINE)

@@ -71,6 +71,18 @@ class Draw:
 
 
 @dataclass
+class StencilOp:
+    """VkStencilOpState: VkStencilOp values and a VkCompareOp"""
+    fail: int = 0
+    pass_: int = 0
+    depth_fail: int = 0
+    compare: int = 7             # ALWAYS
+    compare_mask: int = 0xFF
+    write_mask: int = 0xFF
+    reference: int = 0
+
+
+@dataclass
 class Texture:
     """a combined image sampler of one mip level: texels uint8 [h, w, 4] in the image's byte order"""
     texels: np.ndarray
@@ -109,6 +121,9 @@ class Scene:
     texture: Optional[Texture] = None  # "textured": the fragment shader's sampler2D (set 0, binding 0)
     ubo: bool = False          # "lambert": the matrices come from a uniform buffer (set 0, binding 0, dynamic
                                # offset per draw) instead of push constants
+    depth_format: str = "d32"  # "d32" (D32_SFLOAT), "d16" (D16_UNORM) or "d24s8" (D24_UNORM_S8_UINT)
+    stencil: Optional[dict] = None  # stencil test: {"front": StencilOp, "back": StencilOp} (d24s8 only)
+    clear_stencil: int = 0
 
     @property
     def triangles(self):

@@ -72,6 +72,9 @@ FORMAT_R32G32_SFLOAT = 103
 FORMAT_R32G32B32_SFLOAT = 106
 FORMAT_R32G32B32A32_SFLOAT = 109
 FORMAT_D32_SFLOAT = 126
+FORMAT_D16_UNORM = 124
+FORMAT_D24_UNORM_S8_UINT = 129
+DEPTH_FORMATS = {"d32": FORMAT_D32_SFLOAT, "d16": FORMAT_D16_UNORM, "d24s8": FORMAT_D24_UNORM_S8_UINT}
 
 IMAGE_TYPE_2D = 1
 IMAGE_TILING_OPTIMAL = 0
@@ -97,6 +100,7 @@ IMAGE_USAGE_COLOR_ATTACHMENT = 0x10
 IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT = 0x20
 IMAGE_ASPECT_COLOR = 0x1
 IMAGE_ASPECT_DEPTH = 0x2
+IMAGE_ASPECT_STENCIL = 0x4
 
 MEMORY_PROPERTY_DEVICE_LOCAL = 0x1
 MEMORY_PROPERTY_HOST_VISIBLE = 0x2

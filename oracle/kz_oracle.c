@@ -432,6 +432,43 @@ static int depth_cmp(uint32_t op, float z, float d) {
   }
 }
 
+float kzo_depth_value(float z, uint32_t depth_format) {
+  if (depth_format == KZO_DEPTH_D16) return rintf(z * 65535.0f);
+  if (depth_format == KZO_DEPTH_D24S8) return rintf(z * 16777215.0f);
+  return z;
+}
+
+/* VkStencilOp applied to the stored value s, through the write mask */
+static uint8_t stencil_apply(uint32_t op, uint8_t s, const kzo_stencil* so) {
+  uint32_t v;
+  switch (op) {
+    case 1: v = 0; break;                                  /* ZERO */
+    case 2: v = so->reference & 0xFFu; break;              /* REPLACE */
+    case 3: v = s < 255 ? s + 1u : 255u; break;            /* INCREMENT_AND_CLAMP */
+    case 4: v = s > 0 ? s - 1u : 0u; break;                /* DECREMENT_AND_CLAMP */
+    case 5: v = ~(uint32_t)s & 0xFFu; break;               /* INVERT */
+    case 6: v = (s + 1u) & 0xFFu; break;                   /* INCREMENT_AND_WRAP */
+    case 7: v = (s - 1u) & 0xFFu; break;                   /* DECREMENT_AND_WRAP */
+    default: v = s; break;                                 /* KEEP */
+  }
+  uint32_t wm = so->write_mask & 0xFFu;
+  return (uint8_t)((s & ~wm) | (v & wm));
+}
+
+/* the stencil comparison: reference OP stored, both under the compare mask */
+static int stencil_cmp(uint32_t op, uint32_t ref, uint32_t val) {
+  switch (op) {
+    case CMP_NEVER: return 0;
+    case CMP_LESS: return ref < val;
+    case CMP_EQUAL: return ref == val;
+    case CMP_LEQUAL: return ref <= val;
+    case CMP_GREATER: return ref > val;
+    case CMP_NOTEQUAL: return ref != val;
+    case CMP_GEQUAL: return ref >= val;
+    default: return 1;
+  }
+}
+
 static float blend_factor(uint32_t f, int c, const float s[4], const float dst[4], const float k[4]) {
   switch (f) {
     case BF_ZERO: return 0.0f;
@@ -465,7 +502,7 @@ static float blend_op(uint32_t op, float s, float sf, float d, float df) {
 
 /* rasterise one prepared triangle over rows [ylo, yhi) */
 static void raster_prep(const kzo_draw* draws, const prep* p, uint32_t width, uint8_t* color, float* depth,
-                        int32_t ylo, int32_t yhi, kzo_stats* st) {
+                        uint8_t* stencil, uint32_t depth_format, int32_t ylo, int32_t yhi, kzo_stats* st) {
   const kzo_draw* d = &draws[p->draw];
   int nc = shader_varyings(d);
   int32_t y0 = p->by0 > ylo ? p->by0 : ylo, y1 = p->by1 < yhi - 1 ? p->by1 : yhi - 1;
@@ -488,9 +525,18 @@ static void raster_prep(const kzo_draw* draws, const prep* p, uint32_t width, ui
       z = fminf(fmaxf(z, zmin), zmax);
       z = z + 0.0f;
       size_t pix = (size_t)y * width + (size_t)x;
-      if (d->depth_test && depth) {
-        if (!depth_cmp(d->depth_compare, z, depth[pix])) continue;
+      const float zc = kzo_depth_value(z, depth_format);
+      const int dpass = !(d->depth_test && depth) || depth_cmp(d->depth_compare, zc, depth[pix]);
+      if (d->stencil_test && stencil) {
+        const kzo_stencil* so = p->front ? &d->front : &d->back;
+        uint8_t sv = stencil[pix];
+        if (!stencil_cmp(so->compare_op, so->reference & so->compare_mask & 0xFFu, sv & so->compare_mask)) {
+          stencil[pix] = stencil_apply(so->fail_op, sv, so);
+          continue;
+        }
+        stencil[pix] = stencil_apply(dpass ? so->pass_op : so->depth_fail_op, sv, so);
       }
+      if (!dpass) continue;
       st->depth_pass++;
       float q = fmaf(l2, p->iw[2], fmaf(l1, p->iw[1], l0 * p->iw[0]));
       float rq = 1.0f / q;
@@ -501,7 +547,7 @@ static void raster_prep(const kzo_draw* draws, const prep* p, uint32_t width, ui
       }
       float out[4];
       run_fs(d, var, out);
-      if (d->depth_test && d->depth_write && depth) depth[pix] = z;
+      if (d->depth_test && d->depth_write && depth) depth[pix] = zc;
       uint8_t* c = color + pix * 4;
       if (d->blend_enable) {
         float s[4], dst[4];
@@ -556,6 +602,8 @@ typedef struct {
   uint32_t width;
   uint8_t* color;
   float* depth;
+  uint8_t* stencil;
+  uint32_t depth_format;
   int32_t ylo, yhi;
   kzo_stats st;
 } raster_job;
@@ -567,7 +615,7 @@ static void* raster_worker(void* arg) {
     for (size_t i = 0; i < l->n; i++) {
       const prep* p = &l->v[i];
       if (p->by1 < r->ylo || p->by0 >= r->yhi) continue;
-      raster_prep(r->draws, p, r->width, r->color, r->depth, r->ylo, r->yhi, &r->st);
+      raster_prep(r->draws, p, r->width, r->color, r->depth, r->stencil, r->depth_format, r->ylo, r->yhi, &r->st);
     }
   }
   return NULL;
@@ -575,6 +623,13 @@ static void* raster_worker(void* arg) {
 
 int kzo_render(uint32_t width, uint32_t height, uint8_t* color, float* depth, const int32_t render_area[4],
                uint32_t num_draws, const kzo_draw* draws, int nthreads, kzo_stats* stats) {
+  return kzo_render_ds(width, height, color, depth, NULL, KZO_DEPTH_D32, render_area, num_draws, draws, nthreads,
+                       stats);
+}
+
+int kzo_render_ds(uint32_t width, uint32_t height, uint8_t* color, float* depth, uint8_t* stencil,
+                  uint32_t depth_format, const int32_t render_area[4], uint32_t num_draws, const kzo_draw* draws,
+                  int nthreads, kzo_stats* stats) {
   if (nthreads < 1) nthreads = 1;
   uint64_t* base = (uint64_t*)calloc(num_draws + 1, sizeof(uint64_t));
   int32_t(*rects)[4] = (int32_t(*)[4])calloc(num_draws ? num_draws : 1, sizeof(int32_t[4]));
@@ -612,6 +667,8 @@ int kzo_render(uint32_t width, uint32_t height, uint8_t* color, float* depth, co
     rj[b].width = width;
     rj[b].color = color;
     rj[b].depth = depth;
+    rj[b].stencil = stencil;
+    rj[b].depth_format = depth_format;
     rj[b].ylo = (int32_t)((uint64_t)height * (uint64_t)b / (uint64_t)nbands);
     rj[b].yhi = (int32_t)((uint64_t)height * (uint64_t)(b + 1) / (uint64_t)nbands);
   }

@@ -36,6 +36,16 @@ extern "C" {
 
 enum { KZO_SHADER_COLOR = 0, KZO_SHADER_LAMBERT = 1, KZO_SHADER_TEXTURED = 2 };
 
+/* depth attachment formats: the depth plane holds what the depth test compares, D32 the float depth,
+ * D16 / D24 the integer rint(z * (2^bits - 1)) (exact in a float) */
+enum { KZO_DEPTH_D32 = 0, KZO_DEPTH_D16 = 1, KZO_DEPTH_D24S8 = 2 };
+
+/* VkStencilOpState */
+typedef struct kzo_stencil {
+  uint32_t fail_op, pass_op, depth_fail_op, compare_op;
+  uint32_t compare_mask, write_mask, reference;
+} kzo_stencil;
+
 /* a combined image sampler of one mip level (the GPU's KzDescriptor): RGBA8 or BGRA8 UNORM texels */
 typedef struct kzo_texture {
   const uint8_t* texels;    /* texel (0, 0) */
@@ -69,6 +79,8 @@ typedef struct kzo_draw {
   float viewport[6];        /* x, y, width, height, minDepth, maxDepth */
   int32_t scissor[4];       /* x, y, width, height */
   kzo_texture tex;          /* TEXTURED fragment shader: colour = texture(tex, uv) */
+  uint32_t stencil_test;    /* stencil test against the stencil plane (D24S8 targets) */
+  kzo_stencil front, back;
 } kzo_draw;
 
 typedef struct kzo_stats {
@@ -86,6 +98,17 @@ typedef struct kzo_stats {
  * (each band walks the triangles in API order, so the result is identical). */
 int kzo_render(uint32_t width, uint32_t height, uint8_t* color, float* depth, const int32_t render_area[4],
                uint32_t num_draws, const kzo_draw* draws, int nthreads, kzo_stats* stats);
+
+/* kzo_render with a depth plane in `depth_format` and an optional 8-bit stencil plane (width * height).
+ * Per fragment, in order: stencil test (reference & compare mask against stored & compare mask; on
+ * failure failOp and the fragment ends), depth test (on failure depthFailOp and the fragment ends),
+ * passOp, fragment shader, depth write, colour; ops write through the write mask. */
+int kzo_render_ds(uint32_t width, uint32_t height, uint8_t* color, float* depth, uint8_t* stencil,
+                  uint32_t depth_format, const int32_t render_area[4], uint32_t num_draws, const kzo_draw* draws,
+                  int nthreads, kzo_stats* stats);
+
+/* the value a depth of z is compared and stored as in `depth_format` */
+float kzo_depth_value(float z, uint32_t depth_format);
 
 /* vkCmdClearColorImage / vkCmdClearDepthStencilImage restated for a rectangle */
 void kzo_clear_color(uint32_t width, uint8_t* color, const int32_t rect[4], const float rgba[4]);

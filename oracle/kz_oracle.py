@@ -21,6 +21,14 @@ class KzoTexture(ctypes.Structure):
                 ("pitch", ctypes.c_uint32), ("format", ctypes.c_uint32), ("sampler", ctypes.c_uint32)]
 
 
+class KzoStencil(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in ("fail_op", "pass_op", "depth_fail_op", "compare_op", "compare_mask",
+                                                "write_mask", "reference")]
+
+
+DEPTH_FORMAT = {"d32": 0, "d16": 1, "d24s8": 2}
+
+
 class KzoDraw(ctypes.Structure):
     _fields_ = [("shader", ctypes.c_uint32), ("vertices", ctypes.c_void_p), ("indices", ctypes.c_void_p),
                 ("first", ctypes.c_uint32), ("vertex_offset", ctypes.c_int32), ("tri_count", ctypes.c_uint32),
@@ -30,7 +38,8 @@ class KzoDraw(ctypes.Structure):
                 ("blend_enable", ctypes.c_uint32), ("src_color", ctypes.c_uint32), ("dst_color", ctypes.c_uint32),
                 ("color_op", ctypes.c_uint32), ("src_alpha", ctypes.c_uint32), ("dst_alpha", ctypes.c_uint32),
                 ("alpha_op", ctypes.c_uint32), ("write_mask", ctypes.c_uint32), ("blend_const", ctypes.c_float * 4),
-                ("viewport", ctypes.c_float * 6), ("scissor", ctypes.c_int32 * 4), ("tex", KzoTexture)]
+                ("viewport", ctypes.c_float * 6), ("scissor", ctypes.c_int32 * 4), ("tex", KzoTexture),
+                ("stencil_test", ctypes.c_uint32), ("front", KzoStencil), ("back", KzoStencil)]
 
 
 class KzoStats(ctypes.Structure):
@@ -61,6 +70,12 @@ def lib():
         L.kzo_render.restype = ctypes.c_int
         L.kzo_tex2d.argtypes = [ctypes.POINTER(KzoTexture), ctypes.c_float, ctypes.c_float,
                                 ctypes.POINTER(ctypes.c_float)]
+        L.kzo_render_ds.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32), ctypes.c_uint32,
+                                    ctypes.POINTER(KzoDraw), ctypes.c_int, ctypes.POINTER(KzoStats)]
+        L.kzo_render_ds.restype = ctypes.c_int
+        L.kzo_depth_value.argtypes = [ctypes.c_float, ctypes.c_uint32]
+        L.kzo_depth_value.restype = ctypes.c_float
         L.kzo_unorm8.argtypes = [ctypes.c_float]
         L.kzo_unorm8.restype = ctypes.c_uint8
         L.kzo_clear_color.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
@@ -91,13 +106,25 @@ def unorm8(v):
 
 
 def clear_images(scene):
+    """cleared colour and depth planes; the depth plane holds what the depth test compares (see kz_oracle.h)"""
     w, h = scene.width, scene.height
     color = np.empty((h, w, 4), dtype=np.uint8)
     depth = np.empty((h, w), dtype=np.float32)
     rect = (ctypes.c_int32 * 4)(0, 0, w, h)
     lib().kzo_clear_color(w, color.ctypes.data, rect, (ctypes.c_float * 4)(*scene.clear_color))
-    lib().kzo_clear_depth(w, depth.ctypes.data, rect, scene.clear_depth)
+    fmt = DEPTH_FORMAT[scene.depth_format]
+    lib().kzo_clear_depth(w, depth.ctypes.data, rect, lib().kzo_depth_value(scene.clear_depth, fmt))
     return color, depth
+
+
+def packed_depth(depth, stencil, depth_format):
+    """the depth attachment's texels from the oracle's planes: float32 (d32), uint16 (d16), or uint32 with the
+    depth in bits 0..23 and the stencil in bits 24..31 (d24s8)"""
+    if depth_format == "d16":
+        return depth.astype(np.uint16)
+    if depth_format == "d24s8":
+        return depth.astype(np.uint32) | (stencil.astype(np.uint32) << 24)
+    return depth
 
 
 def make_draws(scene, draws=None):
@@ -129,19 +156,29 @@ def make_draws(scene, draws=None):
         k.scissor[:] = [0, 0, scene.width, scene.height]
         if scene.texture is not None:
             k.tex = texture_struct(scene.texture)
+        if scene.stencil is not None:
+            k.stencil_test = 1
+            for face in ("front", "back"):
+                so = scene.stencil[face]
+                setattr(k, face, KzoStencil(so.fail, so.pass_, so.depth_fail, so.compare, so.compare_mask,
+                                            so.write_mask, so.reference))
     return arr, len(draws)
 
 
 def render(scene, threads=1, draws=None, color=None, depth=None):
     """Render `scene` (a kazan_gb300.scenes.Scene) from cleared attachments; returns
-    (color uint8 [H, W, 4], depth float32 [H, W], stats dict)."""
+    (color uint8 [H, W, 4], depth attachment texels [H, W] (float32 for d32, see packed_depth), stats dict)."""
     if color is None or depth is None:
         color, depth = clear_images(scene)
     arr, n = make_draws(scene, draws)
     st = KzoStats()
     area = (ctypes.c_int32 * 4)(0, 0, scene.width, scene.height)
-    rc = lib().kzo_render(scene.width, scene.height, color.ctypes.data, depth.ctypes.data, area, n, arr, threads,
-                          ctypes.byref(st))
+    stencil = None
+    if scene.depth_format == "d24s8":
+        stencil = np.full((scene.height, scene.width), scene.clear_stencil & 0xFF, dtype=np.uint8)
+    rc = lib().kzo_render_ds(scene.width, scene.height, color.ctypes.data, depth.ctypes.data,
+                             stencil.ctypes.data if stencil is not None else None, DEPTH_FORMAT[scene.depth_format],
+                             area, n, arr, threads, ctypes.byref(st))
     if rc != 0:
         raise RuntimeError("oracle failed")
-    return color, depth, st.as_dict()
+    return color, packed_depth(depth, stencil, scene.depth_format), st.as_dict()
