@@ -1050,6 +1050,14 @@ typedef struct VkBindImageMemoryInfo {
   VkDeviceSize memoryOffset;
 } VkBindImageMemoryInfo;
 
+typedef struct VkImageResolve {
+  VkImageSubresourceLayers srcSubresource;
+  VkOffset3D srcOffset;
+  VkImageSubresourceLayers dstSubresource;
+  VkOffset3D dstOffset;
+  VkExtent3D extent;
+} VkImageResolve;
+
 /* descriptor sets and samplers (vulkan-driver/src/descriptor_set.rs, sampler.rs) */
 typedef enum VkDescriptorType {
   VK_DESCRIPTOR_TYPE_SAMPLER = 0,

@@ -12,6 +12,7 @@
  * modes, captures the launch sequence as a CUDA graph.  vkQueueSubmit replays that graph on the queue's
  * stream, bracketed by the host<->device copies that keep HOST_COHERENT memory coherent.
  */
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -545,9 +546,64 @@ void VKAPI_CALL kzCmdBeginRenderPass(VkCommandBuffer cbh, const VkRenderPassBegi
   cb->ops.push_back(op);
 }
 
+static void record_resolve(CommandBuffer* cb, Image* src, Image* dst, int32_t sx, int32_t sy, int32_t dx, int32_t dy,
+                           int32_t w, int32_t h) {
+  RecOp op;
+  op.kind = OpKind::Resolve;
+  op.src = src->ptr();
+  op.spitch = src->pitch;
+  op.dst = dst->ptr();
+  op.dpitch = dst->pitch;
+  op.rect[0] = sx;
+  op.rect[1] = sy;
+  op.rect[2] = w;
+  op.rect[3] = h;
+  op.dst_x = dx;
+  op.dst_y = dy;
+  op.rmem = src->mem;
+  op.wmem = dst->mem;
+  cb->ops.push_back(op);
+}
+
 void VKAPI_CALL kzCmdEndRenderPass(VkCommandBuffer cbh) {
-  /* api_impl.rs:4961 */
-  H<CommandBuffer>(cbh)->cur_pass = -1;
+  /* api_impl.rs:4961; a subpass resolve attachment receives the average of the colour attachment's samples
+   * over the render area */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  if (cb->cur_pass >= 0) {
+    const PassRec& pr = cb->passes[(size_t)cb->cur_pass];
+    const RenderPass* rp = pr.rp;
+    if (rp->resolve_att >= 0 && rp->color_att >= 0 && (size_t)rp->resolve_att < pr.fb->views.size() &&
+        (size_t)rp->color_att < pr.fb->views.size()) {
+      Image* src = pr.fb->views[(size_t)rp->color_att]->image;
+      Image* dst = pr.fb->views[(size_t)rp->resolve_att]->image;
+      int32_t x0 = std::max(0, pr.area[0]), y0 = std::max(0, pr.area[1]);
+      int32_t x1 = std::min({pr.area[2], (int32_t)src->width, (int32_t)dst->width});
+      int32_t y1 = std::min({pr.area[3], (int32_t)src->height, (int32_t)dst->height});
+      if (src->samples > 1 && dst->samples == 1 && x1 > x0 && y1 > y0)
+        record_resolve(cb, src, dst, x0, y0, x0, y0, x1 - x0, y1 - y0);
+    }
+  }
+  cb->cur_pass = -1;
+}
+
+void VKAPI_CALL kzCmdResolveImage(VkCommandBuffer cbh, VkImage srcImage, VkImageLayout, VkImage dstImage,
+                                  VkImageLayout, uint32_t n, const VkImageResolve* regions) {
+  /* vkCmdResolveImage: each region's samples averaged into the single-sample image, clipped to both images */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  Image* src = H<Image>(srcImage);
+  Image* dst = H<Image>(dstImage);
+  if (src->samples <= 1 || dst->samples != 1) {
+    cb->record_error = VK_ERROR_FEATURE_NOT_PRESENT;
+    return;
+  }
+  for (uint32_t i = 0; i < n; i++) {
+    const VkImageResolve& r = regions[i];
+    int32_t w = (int32_t)r.extent.width, h = (int32_t)r.extent.height;
+    w = std::min({w, (int32_t)src->width - r.srcOffset.x, (int32_t)dst->width - r.dstOffset.x});
+    h = std::min({h, (int32_t)src->height - r.srcOffset.y, (int32_t)dst->height - r.dstOffset.y});
+    if (w <= 0 || h <= 0 || r.srcOffset.x < 0 || r.srcOffset.y < 0 || r.dstOffset.x < 0 || r.dstOffset.y < 0) continue;
+    record_resolve(cb, src, dst, r.srcOffset.x, r.srcOffset.y, r.dstOffset.x, r.dstOffset.y, w, h);
+  }
 }
 
 static void clear_image(CommandBuffer* cb, Image* img, uint32_t value) {
@@ -736,6 +792,15 @@ static void segment_target(const PassRec& pr, KzSegment& s, uint32_t tile, bool 
   s.area[3] = std::min((int32_t)fb->height, pr.area[3]);
   s.color_load = s.depth_load = KZ_LOAD_LOAD;
   s.color_store = s.depth_store = 1;
+  s.samples = 1;
+  /* multisampled passes render through tiles of at most 16 x 16 (the ordered raster keeps a pixel's four
+   * samples in registers) */
+  int ca = rp->color_att >= 0 && (size_t)rp->color_att < fb->views.size() ? rp->color_att : rp->depth_att;
+  if (ca >= 0 && (size_t)ca < fb->views.size() && fb->views[(size_t)ca]->image->samples > 1) {
+    s.samples = fb->views[(size_t)ca]->image->samples;
+    if (tile > 16) tile = 16;
+    s.tile = tile;
+  }
   if (rp->color_att >= 0 && (size_t)rp->color_att < fb->views.size()) {
     Image* img = fb->views[(size_t)rp->color_att]->image;
     s.color = (uint64_t)(uintptr_t)img->ptr();
@@ -770,6 +835,12 @@ static void segment_target(const PassRec& pr, KzSegment& s, uint32_t tile, bool 
     }
     add_unique(low.writes, img->mem);
     if (s.depth_load == KZ_LOAD_LOAD) add_unique(low.reads, img->mem);
+  }
+  /* colour and depth of a multisampled pass must have the same sample count (else the depth texels would
+   * be addressed with the wrong width): a mismatched depth attachment is left out */
+  if (s.depth && rp->depth_att >= 0 && fb->views[(size_t)rp->depth_att]->image->samples != s.samples) {
+    log_error("render pass: depth attachment sample count differs from the colour attachment's; depth ignored");
+    s.depth = 0;
   }
   s.tiles_x = (s.width + tile - 1) / tile;
   s.tiles_y = (s.height + tile - 1) / tile;
@@ -981,6 +1052,17 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
         cudaMemcpyAsync(op.dst, op.src, op.bytes, cudaMemcpyDeviceToDevice, st);
       } else if (op.kind == OpKind::Copy2D) {
         cudaMemcpy2DAsync(op.dst, op.dpitch, op.src, op.spitch, op.width_bytes, op.rows, cudaMemcpyDeviceToDevice, st);
+      } else if (op.kind == OpKind::Resolve) {
+        uint64_t src = (uint64_t)(uintptr_t)op.src, dst = (uint64_t)(uintptr_t)op.dst;
+        uint32_t spitch = (uint32_t)op.spitch, dpitch = (uint32_t)op.dpitch;
+        int32_t sx = op.rect[0], sy = op.rect[1], w = op.rect[2], h = op.rect[3], dx = op.dst_x, dy = op.dst_y;
+        void* args[] = {&src, &spitch, &sx, &sy, &dst, &dpitch, &dx, &dy, &w, &h};
+        cudaLaunchConfig_t cfg = {};
+        cfg.blockDim = dim3(256);
+        cfg.gridDim = dim3((unsigned)std::min<long long>(grid_cap(dev), ((long long)w * h + 255) / 256));
+        cfg.stream = st;
+        launch(dev, timing, KK_RESOLVE, cfg, ks->resolve, args);
+        launches++;
       }
     }
   }
@@ -1026,9 +1108,12 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
     const PassRec& pr = cb->passes[op.pass];
     bool vis_ok = true;
     if (pr.rp->depth_att >= 0 && (size_t)pr.rp->depth_att < pr.fb->views.size()) {
-      VkFormat df = pr.fb->views[(size_t)pr.rp->depth_att]->image->format;
-      vis_ok = df == VK_FORMAT_D32_SFLOAT;
+      const Image* di = pr.fb->views[(size_t)pr.rp->depth_att]->image;
+      vis_ok = di->format == VK_FORMAT_D32_SFLOAT && di->samples == 1;
     }
+    if (pr.rp->color_att >= 0 && (size_t)pr.rp->color_att < pr.fb->views.size() &&
+        pr.fb->views[(size_t)pr.rp->color_att]->image->samples > 1)
+      vis_ok = false;
     /* split the pass into segments */
     std::vector<std::pair<size_t, size_t>> runs; /* [begin, end) draw indices */
     if (low.mode == 2) {
@@ -1070,6 +1155,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
           s.vis_key = (uint32_t)dr.pipe->vis_key;
         }
         KzDraw d = dr.d;
+        d.samples = s.samples;
         d.rect[2] = std::min(d.rect[2], (int32_t)s.width);
         d.rect[3] = std::min(d.rect[3], (int32_t)s.height);
         d.pipe = pipe_of(dr.pipe, cb->have_blend_const ? cb->blend_const : nullptr);

@@ -158,7 +158,8 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
                {"kz_k_persistent", &ks->persistent}, {"kz_k_clear", &ks->clear},
                {"kz_k_vis_init", &ks->vis_init}, {"kz_k_vis_geometry", &ks->vis_geometry},
                {"kz_k_vis_large", &ks->vis_large}, {"kz_k_vis_resolve", &ks->vis_resolve},
-               {"kz_k_indirect", &ks->indirect}, {"kz_k_indirect_tables", &ks->indirect_tables}};
+               {"kz_k_indirect", &ks->indirect}, {"kz_k_indirect_tables", &ks->indirect_tables},
+               {"kz_k_resolve", &ks->resolve}};
   for (auto& n : names) {
     if (cudaLibraryGetKernel(n.k, ks->lib, n.name) != cudaSuccess) {
       err = std::string("kernel ") + n.name + " missing from the linked module";
@@ -370,8 +371,8 @@ static void VKAPI_CALL kzGetPhysicalDeviceProperties(VkPhysicalDevice physicalDe
   l.maxFramebufferWidth = 8192;
   l.maxFramebufferHeight = 8192;
   l.maxFramebufferLayers = 1;
-  l.framebufferColorSampleCounts = VK_SAMPLE_COUNT_1_BIT;
-  l.framebufferDepthSampleCounts = VK_SAMPLE_COUNT_1_BIT;
+  l.framebufferColorSampleCounts = VK_SAMPLE_COUNT_1_BIT | VK_SAMPLE_COUNT_4_BIT;
+  l.framebufferDepthSampleCounts = VK_SAMPLE_COUNT_1_BIT | VK_SAMPLE_COUNT_4_BIT;
   l.framebufferStencilSampleCounts = VK_SAMPLE_COUNT_1_BIT;
   l.framebufferNoAttachmentsSampleCounts = VK_SAMPLE_COUNT_1_BIT;
   l.maxColorAttachments = 1;
@@ -458,6 +459,8 @@ static VkResult VKAPI_CALL kzGetPhysicalDeviceImageFormatProperties(VkPhysicalDe
   p->maxMipLevels = 1;
   p->maxArrayLayers = 1;
   p->sampleCounts = VK_SAMPLE_COUNT_1_BIT;
+  if (format == VK_FORMAT_R8G8B8A8_UNORM || format == VK_FORMAT_B8G8R8A8_UNORM || format == VK_FORMAT_D32_SFLOAT)
+    p->sampleCounts |= VK_SAMPLE_COUNT_4_BIT; /* attachments of multisampled passes */
   p->maxResourceSize = (VkDeviceSize)8192 * 8192 * 4;
   return VK_SUCCESS;
 }
@@ -716,8 +719,11 @@ static VkResult VKAPI_CALL kzCreateImage(VkDevice, const VkImageCreateInfo* ci, 
    * B8G8R8A8_UNORM and D32_SFLOAT; both tilings are row-major with a tight 4-byte pixel pitch. */
   if (!ci || ci->sType != VK_STRUCTURE_TYPE_IMAGE_CREATE_INFO) return VK_ERROR_INITIALIZATION_FAILED;
   uint32_t bpp = format_bpp(ci->format);
+  const bool ms_ok = ci->samples == VK_SAMPLE_COUNT_4_BIT && !(ci->usage & VK_IMAGE_USAGE_SAMPLED_BIT) &&
+                     (ci->format == VK_FORMAT_R8G8B8A8_UNORM || ci->format == VK_FORMAT_B8G8R8A8_UNORM ||
+                      ci->format == VK_FORMAT_D32_SFLOAT);
   if (ci->imageType != VK_IMAGE_TYPE_2D || !bpp || ci->mipLevels != 1 || ci->arrayLayers != 1 ||
-      ci->samples != VK_SAMPLE_COUNT_1_BIT || ci->extent.width == 0 || ci->extent.height == 0 ||
+      (ci->samples != VK_SAMPLE_COUNT_1_BIT && !ms_ok) || ci->extent.width == 0 || ci->extent.height == 0 ||
       ci->extent.width > 8192 || ci->extent.height > 8192)
     return VK_ERROR_FORMAT_NOT_SUPPORTED;
   Image* img = new Image();
@@ -727,7 +733,10 @@ static VkResult VKAPI_CALL kzCreateImage(VkDevice, const VkImageCreateInfo* ci, 
   img->tiling = ci->tiling;
   img->usage = ci->usage;
   img->bpp = bpp;
-  img->pitch = (img->width * bpp + 3u) & ~3u; /* whole 32-bit words: a D16 row is cleared two texels per word */
+  img->samples = ms_ok ? KZ_MS_SAMPLES : 1u;
+  /* whole 32-bit words (a D16 row is cleared two texels per word); multisampled: the samples of a pixel
+   * side by side */
+  img->pitch = (img->width * bpp * img->samples + 3u) & ~3u;
   img->size = (VkDeviceSize)img->pitch * img->height;
   *out = to_handle<VkImage>(img);
   return VK_SUCCESS;
@@ -806,6 +815,9 @@ static VkResult VKAPI_CALL kzCreateRenderPass(VkDevice, const VkRenderPassCreate
     rp->color_att = (int)sp.pColorAttachments[0].attachment;
   if (sp.pDepthStencilAttachment && sp.pDepthStencilAttachment->attachment != VK_ATTACHMENT_UNUSED)
     rp->depth_att = (int)sp.pDepthStencilAttachment->attachment;
+  if (sp.colorAttachmentCount == 1 && sp.pResolveAttachments &&
+      sp.pResolveAttachments[0].attachment != VK_ATTACHMENT_UNUSED)
+    rp->resolve_att = (int)sp.pResolveAttachments[0].attachment;
   *out = to_handle<VkRenderPass>(rp);
   return VK_SUCCESS;
 }
@@ -1172,8 +1184,14 @@ static VkResult create_graphics_pipeline(const VkGraphicsPipelineCreateInfo& ci,
     kp.front_ccw = rs.frontFace == VK_FRONT_FACE_COUNTER_CLOCKWISE;
     p->rasterizer_discard = rs.rasterizerDiscardEnable != 0;
   }
-  if (ci.pMultisampleState && ci.pMultisampleState->rasterizationSamples != VK_SAMPLE_COUNT_1_BIT)
-    r = VK_ERROR_FEATURE_NOT_PRESENT;
+  if (ci.pMultisampleState) {
+    /* 1 or 4 samples; per-sample shading, alpha to coverage / one and sample masks are not supported */
+    const VkPipelineMultisampleStateCreateInfo& ms = *ci.pMultisampleState;
+    if ((ms.rasterizationSamples != VK_SAMPLE_COUNT_1_BIT && ms.rasterizationSamples != VK_SAMPLE_COUNT_4_BIT) ||
+        ms.sampleShadingEnable || ms.alphaToCoverageEnable || ms.alphaToOneEnable ||
+        (ms.pSampleMask && (ms.pSampleMask[0] & 0xFu) != 0xFu))
+      r = VK_ERROR_FEATURE_NOT_PRESENT;
+  }
   if (ci.pDepthStencilState) {
     const VkPipelineDepthStencilStateCreateInfo& ds = *ci.pDepthStencilState;
     if (ds.depthBoundsTestEnable) r = VK_ERROR_FEATURE_NOT_PRESENT;
@@ -1363,6 +1381,8 @@ void VKAPI_CALL kzCmdPushConstants(VkCommandBuffer, VkPipelineLayout, VkShaderSt
                                    const void*);
 void VKAPI_CALL kzCmdDraw(VkCommandBuffer, uint32_t, uint32_t, uint32_t, uint32_t);
 void VKAPI_CALL kzCmdDrawIndirect(VkCommandBuffer, VkBuffer, VkDeviceSize, uint32_t, uint32_t);
+void VKAPI_CALL kzCmdResolveImage(VkCommandBuffer, VkImage, VkImageLayout, VkImage, VkImageLayout, uint32_t,
+                                  const VkImageResolve*);
 void VKAPI_CALL kzCmdBindDescriptorSets(VkCommandBuffer, VkPipelineBindPoint, VkPipelineLayout, uint32_t, uint32_t,
                                         const VkDescriptorSet*, uint32_t, const uint32_t*);
 void VKAPI_CALL kzCmdDrawIndexedIndirect(VkCommandBuffer, VkBuffer, VkDeviceSize, uint32_t, uint32_t);
@@ -1492,6 +1512,7 @@ static const ProcEntry kProcs[] = {
     KZ_PROC("vkCmdPushConstants", kzCmdPushConstants),
     KZ_PROC("vkCmdDraw", kzCmdDraw),
     KZ_PROC("vkCmdDrawIndirect", kzCmdDrawIndirect),
+    KZ_PROC("vkCmdResolveImage", kzCmdResolveImage),
     KZ_PROC("vkCmdDrawIndexedIndirect", kzCmdDrawIndexedIndirect),
     KZ_PROC("vkCmdDrawIndirectCountKHR", kzCmdDrawIndirectCount),
     KZ_PROC("vkCmdDrawIndexedIndirectCountKHR", kzCmdDrawIndexedIndirectCount),

@@ -76,6 +76,7 @@ struct Buffer {
 struct Image {
   VkFormat format = VK_FORMAT_UNDEFINED;
   uint32_t width = 0, height = 0;
+  uint32_t samples = 1; /* 4: KZ_MS_SAMPLES consecutive samples per pixel */
   VkImageTiling tiling = VK_IMAGE_TILING_OPTIMAL;
   VkImageUsageFlags usage = 0;
   uint32_t bpp = 4;
@@ -162,6 +163,7 @@ struct RenderPass {
   std::vector<VkAttachmentDescription> atts;
   int color_att = -1;
   int depth_att = -1;
+  int resolve_att = -1; /* single-sample image the colour attachment resolves into at the end of the pass */
 };
 
 struct Framebuffer {
@@ -206,6 +208,7 @@ enum KernelKind {
   KK_CLEAR,
   KK_INDIRECT,
   KK_INDIRECT_TABLES,
+  KK_RESOLVE,
   KK_COUNT
 };
 
@@ -221,7 +224,7 @@ struct KernelSet {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t geometry = nullptr, scan = nullptr, bin = nullptr, raster = nullptr, persistent = nullptr,
                clear = nullptr, vis_init = nullptr, vis_geometry = nullptr, vis_large = nullptr,
-               vis_resolve = nullptr, indirect = nullptr, indirect_tables = nullptr;
+               vis_resolve = nullptr, indirect = nullptr, indirect_tables = nullptr, resolve = nullptr;
   int persistent_blocks = 0;
   int geometry_blocks = 0; /* resident blocks of kz_k_vis_geometry on the whole GPU */
 };
@@ -247,7 +250,7 @@ struct PassRec {
   std::vector<DrawRec> draws;
 };
 
-enum class OpKind { Pass, Clear, Copy, Copy2D, Fill };
+enum class OpKind { Pass, Clear, Copy, Copy2D, Fill, Resolve };
 
 struct RecOp {
   OpKind kind = OpKind::Pass;
@@ -257,7 +260,9 @@ struct RecOp {
   uint32_t pitch = 0;
   int32_t rect[4] = {0, 0, 0, 0};
   uint32_t value = 0;
-  /* Copy / Copy2D */
+  /* Copy / Copy2D / Resolve (Resolve: src/spitch the multisampled image at rect x0, y0; dst/dpitch the
+   * single-sample image at dst_x, dst_y; rect[2], rect[3] the extent) */
+  int32_t dst_x = 0, dst_y = 0;
   char* dst = nullptr;
   const char* src = nullptr;
   size_t bytes = 0, width_bytes = 0, rows = 0, dpitch = 0, spitch = 0;

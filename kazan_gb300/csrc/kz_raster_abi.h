@@ -141,7 +141,15 @@ typedef struct KzDraw {
   uint32_t call_index;          /* position of the command within its vkCmdDraw*Indirect*Count call */
   uint64_t count_addr;          /* vkCmdDraw*IndirectCount: device address of the u32 draw count (the draw is
                                    skipped when call_index >= count); 0: every recorded command draws */
+  uint32_t samples;             /* rasterizationSamples of its pass: 1, or 4 (KZ_SAMPLE_* positions) */
+  uint32_t pad;
 } KzDraw;
+
+/* the four sample positions of a 4x multisampled pixel (the Vulkan standard positions), in 1/256 pixel
+ * from the pixel's corner: (96, 32), (224, 96), (32, 160), (160, 224) */
+#define KZ_MS_SAMPLES 4
+#define KZ_MS_LO 32   /* smallest sample offset in either axis */
+#define KZ_MS_HI 224  /* largest */
 
 /* geometry work unit: a contiguous run of at most KZ_CHUNK triangles of one draw */
 #define KZ_CHUNK 256
@@ -224,6 +232,9 @@ typedef struct KzSegment {
   uint32_t depth_format;     /* KzDepthFormat; clear_depth holds the converted value for D16 / D24S8 */
   uint32_t stencil_load;     /* KzLoad of the stencil aspect (D24S8) */
   uint32_t clear_stencil;
+  uint32_t samples;          /* 1, or 4: colour and depth texels hold KZ_MS_SAMPLES samples each, sample s of
+                                pixel x at byte 16 x + 4 s of its row (ordered segments, D32 depth, tiles <= 16) */
+  uint32_t pad2;
 } KzSegment;
 
 /* status words written by the kernels (one per submission) */

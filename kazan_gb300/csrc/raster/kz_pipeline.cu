@@ -369,12 +369,14 @@ __device__ __forceinline__ bool make_record(const KzDraw& d, const KzPipe& pp, P
   }
   int32_t minx = min(v[0].X, min(v[1].X, v[2].X)), maxx = max(v[0].X, max(v[1].X, v[2].X));
   int32_t miny = min(v[0].Y, min(v[1].Y, v[2].Y)), maxy = max(v[0].Y, max(v[1].Y, v[2].Y));
-  /* pixels whose centre (p * 256 + 128) lies in [min, max]: ceil((min - 128) / 256) .. floor((max - 128) / 256);
-   * snapped coordinates stay within the guard band (|X| < 2^23), so 32-bit arithmetic shifts are exact */
-  int32_t bx0 = (minx + 127) >> 8;
-  int32_t by0 = (miny + 127) >> 8;
-  int32_t bx1 = (maxx - 128) >> 8;
-  int32_t by1 = (maxy - 128) >> 8;
+  /* pixels with a sample point (p * 256 + o, o = 128, or KZ_MS_LO..KZ_MS_HI when multisampled) in
+   * [min, max]: ceil((min - hi) / 256) .. floor((max - lo) / 256); snapped coordinates stay within the
+   * guard band (|X| < 2^23), so 32-bit arithmetic shifts are exact */
+  const int32_t lo = d.samples > 1 ? KZ_MS_LO : 128, hi = d.samples > 1 ? KZ_MS_HI : 128;
+  int32_t bx0 = (minx - hi + 255) >> 8;
+  int32_t by0 = (miny - hi + 255) >> 8;
+  int32_t bx1 = (maxx - lo) >> 8;
+  int32_t by1 = (maxy - lo) >> 8;
   if (bx0 < d.rect[0]) bx0 = d.rect[0];
   if (by0 < d.rect[1]) by0 = d.rect[1];
   if (bx1 > d.rect[2] - 1) bx1 = d.rect[2] - 1;
@@ -767,11 +769,13 @@ __device__ __forceinline__ void tile_range(const KzSegment& seg, const KzTriReco
   ty1 = (int)(r.bb1 >> 16) / T;
 }
 
-/* Conservative test: can any pixel centre of tile (tx, ty) be inside the record's three edges? */
+/* Conservative test: can any sample point of tile (tx, ty) (pixel centres, or the 4x sample positions of
+ * a multisampled pass) be inside the record's three edges? */
 __device__ __forceinline__ bool tile_overlaps(const KzSegment& seg, const Edges& e, int tx, int ty) {
   int T = (int)seg.tile;
-  int64_t x0 = (int64_t)(tx * T) * 256 + 128, x1 = x0 + (int64_t)(T - 1) * 256;
-  int64_t y0 = (int64_t)(ty * T) * 256 + 128, y1 = y0 + (int64_t)(T - 1) * 256;
+  const int64_t lo = seg.samples > 1 ? KZ_MS_LO : 128, hi = seg.samples > 1 ? KZ_MS_HI : 128;
+  int64_t x0 = (int64_t)(tx * T) * 256 + lo, x1 = (int64_t)(tx * T + T - 1) * 256 + hi;
+  int64_t y0 = (int64_t)(ty * T) * 256 + lo, y1 = (int64_t)(ty * T + T - 1) * 256 + hi;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     int64_t px = e.dy[k] < 0 ? x1 : x0; /* maximise -dy*px */
@@ -1808,7 +1812,21 @@ __device__ __forceinline__ uint32_t blend_straight_alpha(uint32_t dst, const flo
  * blockDim.x) (64x64 tiles take four calls).  The bin is sorted by primitive number; each batch of
  * KZ_BATCH triangles is set up in shared memory, then every thread runs its pixels through the batch in
  * order: coverage, depth test, fragment shader, depth write, blend.  `u8tab`: u8f(k) for k = 0..255. */
-template <int PER, bool DS>
+/* sample s of a 4x multisampled pixel, relative to the pixel centre in 1/256 pixel */
+__device__ __constant__ int32_t kz_ms_dx[KZ_MS_SAMPLES] = {-32, 96, -96, 32};
+__device__ __constant__ int32_t kz_ms_dy[KZ_MS_SAMPLES] = {-96, -32, 32, 96};
+
+__device__ __forceinline__ uint32_t* color_sample(const KzSegment& seg, int32_t x, int32_t y, int s) {
+  return reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(seg.color) + (size_t)y * seg.color_pitch) + 4 * x + s;
+}
+__device__ __forceinline__ float* depth_sample(const KzSegment& seg, int32_t x, int32_t y, int s) {
+  return reinterpret_cast<float*>(reinterpret_cast<char*>(seg.depth) + (size_t)y * seg.depth_pitch) + 4 * x + s;
+}
+
+/* MS: a 4x multisampled pass (PER 1, D32): coverage, depth test, depth write and colour per sample; the
+ * fragment shader runs once per pixel, at the pixel centre, when some covered sample passes the depth
+ * test */
+template <int PER, bool DS, bool MS>
 __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* smem, const float* u8tab, int base) {
   const KzSegment& seg = *c.seg;
   TileInfo ti;
@@ -1860,6 +1878,9 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
   uint32_t colv[PER];
   float depv[PER];
   uint32_t stv[PER];
+  constexpr int NS = MS ? KZ_MS_SAMPLES : 1;
+  uint32_t colm[NS];
+  float depm[NS];
 #pragma unroll
   for (int q = 0; q < PER; q++) {
     int i = base + (int)threadIdx.x + q * (int)blockDim.x;
@@ -1871,6 +1892,14 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
     depv[q] = 1.0f;
     stv[q] = 0;
     if (!in[q]) continue;
+    if constexpr (MS) {
+#pragma unroll
+      for (int s = 0; s < NS; s++) {
+        colm[s] = has_color ? to_rgba(clear_c ? seg.clear_color : *color_sample(seg, x, y, s), seg.color_format) : 0u;
+        depm[s] = has_depth ? (clear_d ? seg.clear_depth : *depth_sample(seg, x, y, s)) : 1.0f;
+      }
+      continue;
+    }
     if (has_color) colv[q] = to_rgba(clear_c ? seg.clear_color : *color_px(seg, x, y), seg.color_format);
     if (has_depth && DS) {
       uint32_t s0 = 0;
@@ -1944,6 +1973,55 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
       for (int q = 0; q < PER; q++) {
         if (!in[q]) continue;
         int64_t E[3];
+        if constexpr (MS) {
+          /* edge values at the pixel centre, then at each sample (the steps per 1/256 pixel are ex / 256 and
+           * ey / 256, exact) */
+          int64_t ec[3];
+#pragma unroll
+          for (int k = 0; k < 3; k++) ec[k] = be.e[k] + (int64_t)be.ex[k] * lx[q] + (int64_t)be.ey[k] * ly[q];
+          int64_t es[NS][3];
+          uint32_t cover = 0;
+#pragma unroll
+          for (int s = 0; s < NS; s++) {
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+              es[s][k] = ec[k] + (int64_t)kz_ms_dx[s] * (be.ex[k] / 256) + (int64_t)kz_ms_dy[s] * (be.ey[k] / 256);
+            if ((es[s][0] | es[s][1] | es[s][2]) >= 0) cover |= 1u << s;
+          }
+          if (!cover) continue;
+          frags++;
+          const KzTriRecord& r = be.s.r;
+          const bool dtest = (be.depth & 1u) && has_depth;
+          float zs[NS];
+          uint32_t pass = 0;
+#pragma unroll
+          for (int s = 0; s < NS; s++) {
+            if (!((cover >> s) & 1u)) continue;
+            float l1 = fmul(kz_i64_to_f32(es[s][1] + (int64_t)((be.thr >> 1) & 1u)), r.inv_s);
+            float l2 = fmul(kz_i64_to_f32(es[s][2] + (int64_t)(be.thr >> 2)), r.inv_s);
+            float z = ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0));
+            zs[s] = fadd(fminf(fmaxf(z, be.zmin), be.zmax), 0.0f);
+            if (!dtest || depth_cmp(be.depth >> 2, zs[s], depm[s])) pass |= 1u << s;
+          }
+          if (!pass) continue;
+          E[0] = ec[0] + (int64_t)(be.thr & 1u);
+          E[1] = ec[1] + (int64_t)((be.thr >> 1) & 1u);
+          E[2] = ec[2] + (int64_t)(be.thr >> 2);
+          float l1 = fmul(kz_i64_to_f32(E[1]), r.inv_s), l2 = fmul(kz_i64_to_f32(E[2]), r.inv_s);
+          float zc = fadd(fminf(fmaxf(ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0)), be.zmin), be.zmax), 0.0f);
+          int32_t x = ti.ox + lx[q], y = ti.oy + ly[q];
+          float col[4];
+          if (shade_pixel<false>(c, be.s, x, y, E, zc, col)) continue;
+#pragma unroll
+          for (int s = 0; s < NS; s++) {
+            if (!((pass >> s) & 1u)) continue;
+            if (dtest && (be.depth & 2u)) depm[s] = zs[s];
+            if (!has_color) continue;
+            if (be.blend == 1u) colm[s] = blend_straight_alpha(colm[s], col, u8tab, be.write_mask);
+            else colm[s] = color_write(c.pipes[be.s.pipe], colm[s], col, u8tab);
+          }
+          continue;
+        }
         if (be.fits) {
           /* the same integers in 32-bit arithmetic (bounded over the tile) */
           int32_t e0 = (int32_t)be.e[0] + be.ex[0] * lx[q] + be.ey[0] * ly[q];
@@ -2007,6 +2085,14 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
   for (int q = 0; q < PER; q++) {
     if (!in[q]) continue;
     int32_t x = ti.ox + lx[q], y = ti.oy + ly[q];
+    if constexpr (MS) {
+#pragma unroll
+      for (int s = 0; s < NS; s++) {
+        if (has_color) *color_sample(seg, x, y, s) = from_rgba(colm[s], seg.color_format);
+        if (has_depth) *depth_sample(seg, x, y, s) = depm[s];
+      }
+      continue;
+    }
     if (has_color) *color_px(seg, x, y) = from_rgba(colv[q], seg.color_format);
     if (has_depth && DS) store_depth(seg, x, y, depv[q], stv[q]);
     else if (has_depth) *depth_px(seg, x, y) = depv[q];
@@ -2016,14 +2102,16 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
 __device__ void raster_tile(const Ctx& c, uint32_t t, unsigned char* smem, const float* u8tab) {
   const uint32_t T = c.seg->tile;
   const bool ds = c.seg->depth_format != KZ_DF_D32;
-  if (T <= 16) {
-    if (ds) raster_tile_ordered<1, true>(c, t, smem, u8tab, 0);
-    else raster_tile_ordered<1, false>(c, t, smem, u8tab, 0);
+  if (c.seg->samples > 1) { /* tiles of at most 16 x 16 */
+    raster_tile_ordered<1, false, true>(c, t, smem, u8tab, 0);
+  } else if (T <= 16) {
+    if (ds) raster_tile_ordered<1, true, false>(c, t, smem, u8tab, 0);
+    else raster_tile_ordered<1, false, false>(c, t, smem, u8tab, 0);
   } else {
     for (int base = 0; base < (int)(T * T); base += 4 * KZ_THREADS) {
       __syncthreads();
-      if (ds) raster_tile_ordered<4, true>(c, t, smem, u8tab, base);
-      else raster_tile_ordered<4, false>(c, t, smem, u8tab, base);
+      if (ds) raster_tile_ordered<4, true, false>(c, t, smem, u8tab, base);
+      else raster_tile_ordered<4, false, false>(c, t, smem, u8tab, base);
     }
   }
   __syncthreads();
@@ -2391,6 +2479,29 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
 /* vkCmdClearColorImage / vkCmdClearDepthStencilImage / render-pass clears outside the raster:
  * fill rows [y0, y1) x [x0, x1) of a 4-byte-per-pixel image with `value` (16-byte stores where the
  * row segment is aligned) */
+/* multisample resolve of a w x h rectangle: per pixel and byte, (sum of the KZ_MS_SAMPLES samples + 2) / 4 */
+extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_resolve(uint64_t src, uint32_t spitch, int32_t sx,
+                                                                      int32_t sy, uint64_t dst, uint32_t dpitch,
+                                                                      int32_t dx, int32_t dy, int32_t w, int32_t h) {
+  const long long total = (long long)w * h;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    int32_t x = (int32_t)(i % w), y = (int32_t)(i / w);
+    /* four 32-bit loads: an image bound at any 4-byte memory offset keeps them aligned */
+    const uint32_t* p = reinterpret_cast<const uint32_t*>(reinterpret_cast<const char*>(src) + (size_t)(sy + y) * spitch +
+                                                          (size_t)(sx + x) * 16u);
+    const uint4 s = make_uint4(p[0], p[1], p[2], p[3]);
+    uint32_t out = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      uint32_t sum = 2u + ((s.x >> (8 * c)) & 0xFFu) + ((s.y >> (8 * c)) & 0xFFu) + ((s.z >> (8 * c)) & 0xFFu) +
+                     ((s.w >> (8 * c)) & 0xFFu);
+      out |= (sum >> 2) << (8 * c);
+    }
+    *reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(dst) + (size_t)(dy + y) * dpitch + (size_t)(dx + x) * 4u) = out;
+  }
+}
+
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_clear(uint64_t base, uint32_t pitch, int32_t x0,
                                                                     int32_t y0, int32_t x1, int32_t y1,
                                                                     uint32_t value) {

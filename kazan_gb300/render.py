@@ -151,11 +151,13 @@ class Renderer:
         self.end_submit_wait(cb)
         self.free_command_buffer(cb)
 
-    def create_image(self, width, height, fmt, usage, host_visible=True):
+    def create_image(self, width, height, fmt, usage, host_visible=True, samples=1):
+        """samples 4: a multisampled attachment (optimal tiling; the samples of a pixel side by side in its
+        host-visible memory, which the tests read directly)"""
         d = self.drv
         ici = vk.VkImageCreateInfo(vk.ST_IMAGE_CREATE_INFO, None, 0, vk.IMAGE_TYPE_2D, fmt,
-                                   vk.VkExtent3D(width, height, 1), 1, 1, vk.SAMPLE_COUNT_1,
-                                   vk.IMAGE_TILING_LINEAR if host_visible else vk.IMAGE_TILING_OPTIMAL,
+                                   vk.VkExtent3D(width, height, 1), 1, 1, samples,
+                                   vk.IMAGE_TILING_LINEAR if host_visible and samples == 1 else vk.IMAGE_TILING_OPTIMAL,
                                    usage | vk.IMAGE_USAGE_TRANSFER_SRC | vk.IMAGE_USAGE_TRANSFER_DST, 0, 0, None,
                                    vk.IMAGE_LAYOUT_UNDEFINED)
         h = c_void_p()
@@ -174,7 +176,9 @@ class Renderer:
         sub = vk.VkImageSubresource(aspect, 0, 0)
         lay = vk.VkSubresourceLayout()
         d.vkGetImageSubresourceLayout(self.device, h, byref(sub), byref(lay))
-        return Image(h, mem, view, width, height, fmt, host_visible, lay.rowPitch)
+        img = Image(h, mem, view, width, height, fmt, host_visible, lay.rowPitch)
+        img.samples = samples
+        return img
 
     def read_image(self, img):
         n = img.pitch * img.height
@@ -196,6 +200,13 @@ class Renderer:
             self.unmap(staging)
         # a host-visible image is read at its row pitch; a copy to a buffer packs rows tightly
         bpp = 2 if img.format == vk.FORMAT_D16_UNORM else 4
+        ns = getattr(img, "samples", 1)
+        if ns > 1:
+            assert img.host_visible, "multisampled images are read through host-visible memory"
+            raw = raw.reshape(img.height, img.pitch)[:, :img.width * bpp * ns].copy()
+            if img.format == vk.FORMAT_D32_SFLOAT:
+                return raw.view(np.float32).reshape(img.height, img.width, ns)
+            return raw.reshape(img.height, img.width, ns, 4)
         raw = raw.reshape(img.height, img.pitch) if img.host_visible else raw[:img.height * img.width * bpp].reshape(
             img.height, img.width * bpp)
         if img.format == vk.FORMAT_D32_SFLOAT:
@@ -240,18 +251,24 @@ class Renderer:
 
     # ---------------------------------------------------------------------------------------------
     def render_pass(self, color_fmt, depth, color_load=vk.LOAD_OP_CLEAR, depth_load=vk.LOAD_OP_CLEAR,
-                    depth_fmt=vk.FORMAT_D32_SFLOAT, stencil_load=vk.LOAD_OP_CLEAR):
-        atts = (vk.VkAttachmentDescription * 2)()
-        atts[0] = vk.VkAttachmentDescription(0, color_fmt, 1, color_load, vk.STORE_OP_STORE, 2, 1,
+                    depth_fmt=vk.FORMAT_D32_SFLOAT, stencil_load=vk.LOAD_OP_CLEAR, samples=1):
+        """colour (attachment 0) and depth (1) with `samples` samples; with 4 samples a single-sample resolve
+        attachment (2) receives the colour at the end of the subpass"""
+        atts = (vk.VkAttachmentDescription * 3)()
+        atts[0] = vk.VkAttachmentDescription(0, color_fmt, samples, color_load, vk.STORE_OP_STORE, 2, 1,
                                              vk.IMAGE_LAYOUT_UNDEFINED, vk.IMAGE_LAYOUT_GENERAL)
-        atts[1] = vk.VkAttachmentDescription(0, depth_fmt, 1, depth_load, vk.STORE_OP_STORE, stencil_load, 0,
+        atts[1] = vk.VkAttachmentDescription(0, depth_fmt, samples, depth_load, vk.STORE_OP_STORE, stencil_load, 0,
+                                             vk.IMAGE_LAYOUT_UNDEFINED, vk.IMAGE_LAYOUT_GENERAL)
+        atts[2] = vk.VkAttachmentDescription(0, color_fmt, 1, vk.LOAD_OP_DONT_CARE, vk.STORE_OP_STORE, 2, 1,
                                              vk.IMAGE_LAYOUT_UNDEFINED, vk.IMAGE_LAYOUT_GENERAL)
         cref = vk.VkAttachmentReference(0, vk.IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL)
         dref = vk.VkAttachmentReference(1, vk.IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL)
-        sp = vk.VkSubpassDescription(0, vk.BIND_POINT_GRAPHICS, 0, None, 1, pointer(cref), None,
+        rref = vk.VkAttachmentReference(2, vk.IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL)
+        sp = vk.VkSubpassDescription(0, vk.BIND_POINT_GRAPHICS, 0, None, 1, pointer(cref),
+                                     ctypes.cast(pointer(rref), c_void_p) if samples > 1 else None,
                                      pointer(dref) if depth else None, 0, None)
-        rci = vk.VkRenderPassCreateInfo(vk.ST_RENDER_PASS_CREATE_INFO, None, 0, 2 if depth else 1, atts, 1,
-                                        pointer(sp), 0, None)
+        rci = vk.VkRenderPassCreateInfo(vk.ST_RENDER_PASS_CREATE_INFO, None, 0,
+                                        (2 if depth else 1) + (1 if samples > 1 else 0), atts, 1, pointer(sp), 0, None)
         h = c_void_p()
         check("vkCreateRenderPass", self.drv.vkCreateRenderPass(self.device, byref(rci), None, byref(h)))
         self._objects.append(("RenderPass", h))
@@ -375,8 +392,8 @@ class Renderer:
                                                        vk.POLYGON_MODE_FILL, scene.cull,
                                                        vk.FRONT_FACE_CCW if scene.front_ccw else vk.FRONT_FACE_CW,
                                                        0, 0.0, 0.0, 0.0, 1.0)
-        ms = vk.VkPipelineMultisampleStateCreateInfo(vk.ST_PIPELINE_MULTISAMPLE_STATE_CREATE_INFO, None, 0, 1, 0,
-                                                     0.0, None, 0, 0)
+        ms = vk.VkPipelineMultisampleStateCreateInfo(vk.ST_PIPELINE_MULTISAMPLE_STATE_CREATE_INFO, None, 0,
+                                                     scene.samples, 0, 0.0, None, 0, 0)
         faces = [vk.VkStencilOpState(), vk.VkStencilOpState()]
         if scene.stencil is not None:
             faces = [vk.VkStencilOpState(so.fail, so.pass_, so.depth_fail, so.compare, so.compare_mask, so.write_mask,
@@ -448,13 +465,23 @@ class SceneRun:
         if scene.indexed:
             self.ib = r.create_buffer(scene.indices.nbytes, vk.BUFFER_USAGE_INDEX, host_visible)
             r.write_buffer(self.ib, scene.indices, keep_mapped=keep_mapped and host_visible)
+        ns = scene.samples
+        self.samples = None
+        if ns > 1:
+            # multisampled colour and depth in host-visible memory (read sample by sample by the tests); the
+            # pass resolves the colour into self.color
+            self.samples = r.create_image(scene.width, scene.height, vk.FORMAT_R8G8B8A8_UNORM,
+                                          vk.IMAGE_USAGE_COLOR_ATTACHMENT, True, samples=ns)
         self.color = r.create_image(scene.width, scene.height, vk.FORMAT_R8G8B8A8_UNORM,
                                     vk.IMAGE_USAGE_COLOR_ATTACHMENT, host_visible)
         self.depth = r.create_image(scene.width, scene.height, vk.DEPTH_FORMATS[scene.depth_format],
                                     vk.IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT,
-                                    host_visible if depth_host_visible is None else depth_host_visible)
-        self.rp = r.render_pass(vk.FORMAT_R8G8B8A8_UNORM, True, depth_fmt=vk.DEPTH_FORMATS[scene.depth_format])
-        self.fb = r.framebuffer(self.rp, [self.color.view, self.depth.view], scene.width, scene.height)
+                                    (host_visible if depth_host_visible is None else depth_host_visible) or ns > 1,
+                                    samples=ns)
+        self.rp = r.render_pass(vk.FORMAT_R8G8B8A8_UNORM, True, depth_fmt=vk.DEPTH_FORMATS[scene.depth_format],
+                                samples=ns)
+        views = [self.samples.view, self.depth.view, self.color.view] if ns > 1 else [self.color.view, self.depth.view]
+        self.fb = r.framebuffer(self.rp, views, scene.width, scene.height)
         # descriptor sets: the textured scene's sampler2D, or the Lambert matrices in a uniform buffer (one
         # 256-byte slot per draw, selected by a dynamic offset)
         self.set_layouts, self.dsets, self.ubo_buf, self.tex_image = [], [], None, None

@@ -124,6 +124,7 @@ class Scene:
     depth_format: str = "d32"  # "d32" (D32_SFLOAT), "d16" (D16_UNORM) or "d24s8" (D24_UNORM_S8_UINT)
     stencil: Optional[dict] = None  # stencil test: {"front": StencilOp, "back": StencilOp} (d24s8 only)
     clear_stencil: int = 0
+    samples: int = 1           # 1, or 4: multisampled colour and depth attachments, resolved at the end of the pass
 
     @property
     def triangles(self):

@@ -500,6 +500,11 @@ class VkRenderPassBeginInfo(Structure):
                 ("renderArea", VkRect2D), ("clearValueCount", c_uint32), ("pClearValues", POINTER(VkClearValue))]
 
 
+class VkImageResolve(Structure):
+    _fields_ = [("srcSubresource", VkImageSubresourceLayers), ("srcOffset", VkOffset3D),
+                ("dstSubresource", VkImageSubresourceLayers), ("dstOffset", VkOffset3D), ("extent", VkExtent3D)]
+
+
 class VkSamplerCreateInfo(Structure):
     _fields_ = [("sType", c_int), ("pNext", c_void_p), ("flags", c_uint32), ("magFilter", c_int),
                 ("minFilter", c_int), ("mipmapMode", c_int), ("addressModeU", c_int), ("addressModeV", c_int),
@@ -570,7 +575,7 @@ class VkBufferImageCopy(Structure):
 # kernel kinds of kzGetKernelTimes (KZ_KERNEL_KIND_NAMES)
 KERNEL_KINDS = ["kz_k_persistent", "kz_k_vis_init", "kz_k_vis_geometry", "kz_k_vis_large", "kz_k_vis_resolve",
                 "kz_k_geometry", "kz_k_scan", "kz_k_bin", "kz_k_raster", "kz_k_clear", "kz_k_indirect",
-                "kz_k_indirect_tables"]
+                "kz_k_indirect_tables", "kz_k_resolve"]
 
 
 class KzCommandBufferStats(Structure):
@@ -638,6 +643,7 @@ _PROTOS = {
     "vkCmdDrawIndexedIndirect": (None, [H, H, c_uint64, c_uint32, c_uint32]),
     "vkEnumerateDeviceExtensionProperties": (c_int, [H, ctypes.c_char_p, P(c_uint32), P(VkExtensionProperties)]),
     "vkGetPhysicalDeviceFeatures": (None, [H, P(c_uint32)]),
+    "vkCmdResolveImage": (None, [H, H, c_int, H, c_int, c_uint32, P(VkImageResolve)]),
     "vkCreateSampler": (c_int, [H, P(VkSamplerCreateInfo), c_void_p, P(H)]),
     "vkDestroySampler": (None, [H, H, c_void_p]),
     "vkCreateDescriptorSetLayout": (c_int, [H, P(VkDescriptorSetLayoutCreateInfo), c_void_p, P(H)]),

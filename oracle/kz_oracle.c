@@ -333,10 +333,12 @@ static void setup_tri(const kzo_draw* d, uint32_t di, const int32_t rect[4], con
     if (p.Y[i] < miny) miny = p.Y[i];
     if (p.Y[i] > maxy) maxy = p.Y[i];
   }
-  int64_t bx0 = -floordiv256(-((int64_t)minx - 128)); /* ceil((minx - 128) / 256) */
-  int64_t by0 = -floordiv256(-((int64_t)miny - 128));
-  int64_t bx1 = floordiv256((int64_t)maxx - 128);
-  int64_t by1 = floordiv256((int64_t)maxy - 128);
+  /* pixels with a sample point (offset 128, or 32..224 for 4 samples) in [min, max] */
+  const int64_t lo = d->samples == 4 ? 32 : 128, hi = d->samples == 4 ? 224 : 128;
+  int64_t bx0 = -floordiv256(-((int64_t)minx - hi)); /* ceil((minx - hi) / 256) */
+  int64_t by0 = -floordiv256(-((int64_t)miny - hi));
+  int64_t bx1 = floordiv256((int64_t)maxx - lo);
+  int64_t by1 = floordiv256((int64_t)maxy - lo);
   if (bx0 < rect[0]) bx0 = rect[0];
   if (by0 < rect[1]) by0 = rect[1];
   if (bx1 > rect[2] - 1) bx1 = rect[2] - 1;
@@ -500,6 +502,91 @@ static float blend_op(uint32_t op, float s, float sf, float d, float df) {
   }
 }
 
+/* colour write or blend of one fragment output into the RGBA8 texel c */
+static void write_color(const kzo_draw* d, uint8_t* c, const float out[4]) {
+  if (d->blend_enable) {
+    float s[4], dst[4];
+    for (int i = 0; i < 4; i++) {
+      s[i] = fminf(fmaxf(out[i], 0.0f), 1.0f);
+      dst[i] = u8_to_f32(c[i]);
+    }
+    for (int i = 0; i < 4; i++) {
+      if (!(d->write_mask & (1u << i))) continue;
+      float r;
+      if (i < 3)
+        r = blend_op(d->color_op, s[i], blend_factor(d->src_color, i, s, dst, d->blend_const), dst[i],
+                     blend_factor(d->dst_color, i, s, dst, d->blend_const));
+      else
+        r = blend_op(d->alpha_op, s[3], blend_factor(d->src_alpha, 3, s, dst, d->blend_const), dst[3],
+                     blend_factor(d->dst_alpha, 3, s, dst, d->blend_const));
+      c[i] = kzo_unorm8(r);
+    }
+  } else {
+    for (int i = 0; i < 4; i++)
+      if (d->write_mask & (1u << i)) c[i] = kzo_unorm8(out[i]);
+  }
+}
+
+static const int32_t ms_dx[4] = {96, 224, 32, 160}, ms_dy[4] = {32, 96, 160, 224};
+
+/* one pixel of a 4x multisampled draw (kzo_draw::samples) */
+static void raster_pixel_ms(const kzo_draw* d, const prep* p, int nc, int32_t x, int32_t y, size_t pix, uint8_t* color,
+                            float* depth, float zmin, float zmax, kzo_stats* st) {
+  int64_t Es[4][3];
+  unsigned cover = 0;
+  for (int s = 0; s < 4; s++) {
+    int64_t px = (int64_t)x * 256 + ms_dx[s], py = (int64_t)y * 256 + ms_dy[s];
+    int inside = 1;
+    for (int e = 0; e < 3; e++) {
+      int a = (e + 1) % 3, b = (e + 2) % 3;
+      Es[s][e] = (int64_t)(p->X[b] - p->X[a]) * (py - p->Y[a]) - (int64_t)(p->Y[b] - p->Y[a]) * (px - p->X[a]);
+      if (!(Es[s][e] > 0 || (Es[s][e] == 0 && p->tl[e]))) inside = 0;
+    }
+    if (inside) cover |= 1u << s;
+  }
+  if (!cover) return;
+  st->fragments++;
+  float zs[4];
+  unsigned pass = 0;
+  for (int s = 0; s < 4; s++) {
+    if (!((cover >> s) & 1u)) continue;
+    float l1 = (float)Es[s][1] * p->inv_s, l2 = (float)Es[s][2] * p->inv_s;
+    float z = fmaf(l2, p->dz2, fmaf(l1, p->dz1, p->z0));
+    zs[s] = fminf(fmaxf(z, zmin), zmax) + 0.0f;
+    if (!(d->depth_test && depth) || depth_cmp(d->depth_compare, zs[s], depth[pix * 4 + (size_t)s])) pass |= 1u << s;
+  }
+  if (!pass) return;
+  st->depth_pass++;
+  /* the fragment shader at the pixel centre */
+  int64_t px = (int64_t)x * 256 + 128, py = (int64_t)y * 256 + 128;
+  int64_t E[3];
+  for (int e = 0; e < 3; e++) {
+    int a = (e + 1) % 3, b = (e + 2) % 3;
+    E[e] = (int64_t)(p->X[b] - p->X[a]) * (py - p->Y[a]) - (int64_t)(p->Y[b] - p->Y[a]) * (px - p->X[a]);
+  }
+  float l0 = (float)E[0] * p->inv_s, l1 = (float)E[1] * p->inv_s, l2 = (float)E[2] * p->inv_s;
+  float q = fmaf(l2, p->iw[2], fmaf(l1, p->iw[1], l0 * p->iw[0]));
+  float rq = 1.0f / q;
+  float var[KZO_MAXK];
+  for (int k = 0; k < nc; k++) var[k] = fmaf(l2, p->a[2][k], fmaf(l1, p->a[1][k], l0 * p->a[0][k])) * rq;
+  float out[4];
+  run_fs(d, var, out);
+  for (int s = 0; s < 4; s++) {
+    if (!((pass >> s) & 1u)) continue;
+    if (d->depth_test && d->depth_write && depth) depth[pix * 4 + (size_t)s] = zs[s];
+    write_color(d, color + (pix * 4 + (size_t)s) * 4, out);
+  }
+}
+
+void kzo_resolve(uint32_t width, uint32_t height, const uint8_t* color4, uint8_t* color) {
+  for (size_t pix = 0; pix < (size_t)width * height; pix++)
+    for (int c = 0; c < 4; c++) {
+      unsigned sum = 2;
+      for (int s = 0; s < 4; s++) sum += color4[(pix * 4 + (size_t)s) * 4 + (size_t)c];
+      color[pix * 4 + (size_t)c] = (uint8_t)(sum / 4);
+    }
+}
+
 /* rasterise one prepared triangle over rows [ylo, yhi) */
 static void raster_prep(const kzo_draw* draws, const prep* p, uint32_t width, uint8_t* color, float* depth,
                         uint8_t* stencil, uint32_t depth_format, int32_t ylo, int32_t yhi, kzo_stats* st) {
@@ -510,6 +597,10 @@ static void raster_prep(const kzo_draw* draws, const prep* p, uint32_t width, ui
   for (int32_t y = y0; y <= y1; y++) {
     int64_t py = (int64_t)y * 256 + 128;
     for (int32_t x = p->bx0; x <= p->bx1; x++) {
+      if (d->samples == 4) {
+        raster_pixel_ms(d, p, nc, x, y, (size_t)y * width + (size_t)x, color, depth, zmin, zmax, st);
+        continue;
+      }
       int64_t px = (int64_t)x * 256 + 128;
       int64_t E[3];
       int inside = 1;

@@ -81,6 +81,11 @@ typedef struct kzo_draw {
   kzo_texture tex;          /* TEXTURED fragment shader: colour = texture(tex, uv) */
   uint32_t stencil_test;    /* stencil test against the stencil plane (D24S8 targets) */
   kzo_stencil front, back;
+  uint32_t samples;         /* 0 or 1: one sample at the pixel centre; 4: the standard 4x positions (96, 32),
+                               (224, 96), (32, 160), (160, 224) in 1/256 pixel, colour and depth planes holding
+                               4 samples per pixel (sample s of pixel p at p * 4 + s), coverage, depth and
+                               colour per sample, the fragment shader once per pixel at its centre (only D32,
+                               no stencil) */
 } kzo_draw;
 
 typedef struct kzo_stats {
@@ -106,6 +111,9 @@ int kzo_render(uint32_t width, uint32_t height, uint8_t* color, float* depth, co
 int kzo_render_ds(uint32_t width, uint32_t height, uint8_t* color, float* depth, uint8_t* stencil,
                   uint32_t depth_format, const int32_t render_area[4], uint32_t num_draws, const kzo_draw* draws,
                   int nthreads, kzo_stats* stats);
+
+/* the multisample resolve: per pixel and byte, (sum of the 4 samples + 2) / 4 */
+void kzo_resolve(uint32_t width, uint32_t height, const uint8_t* color4, uint8_t* color);
 
 /* the value a depth of z is compared and stored as in `depth_format` */
 float kzo_depth_value(float z, uint32_t depth_format);

@@ -39,7 +39,8 @@ class KzoDraw(ctypes.Structure):
                 ("color_op", ctypes.c_uint32), ("src_alpha", ctypes.c_uint32), ("dst_alpha", ctypes.c_uint32),
                 ("alpha_op", ctypes.c_uint32), ("write_mask", ctypes.c_uint32), ("blend_const", ctypes.c_float * 4),
                 ("viewport", ctypes.c_float * 6), ("scissor", ctypes.c_int32 * 4), ("tex", KzoTexture),
-                ("stencil_test", ctypes.c_uint32), ("front", KzoStencil), ("back", KzoStencil)]
+                ("stencil_test", ctypes.c_uint32), ("front", KzoStencil), ("back", KzoStencil),
+                ("samples", ctypes.c_uint32)]
 
 
 class KzoStats(ctypes.Structure):
@@ -74,6 +75,7 @@ def lib():
                                     ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32), ctypes.c_uint32,
                                     ctypes.POINTER(KzoDraw), ctypes.c_int, ctypes.POINTER(KzoStats)]
         L.kzo_render_ds.restype = ctypes.c_int
+        L.kzo_resolve.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p]
         L.kzo_depth_value.argtypes = [ctypes.c_float, ctypes.c_uint32]
         L.kzo_depth_value.restype = ctypes.c_float
         L.kzo_unorm8.argtypes = [ctypes.c_float]
@@ -156,6 +158,7 @@ def make_draws(scene, draws=None):
         k.scissor[:] = [0, 0, scene.width, scene.height]
         if scene.texture is not None:
             k.tex = texture_struct(scene.texture)
+        k.samples = scene.samples
         if scene.stencil is not None:
             k.stencil_test = 1
             for face in ("front", "back"):
@@ -165,9 +168,31 @@ def make_draws(scene, draws=None):
     return arr, len(draws)
 
 
+def render_ms(scene, threads=1):
+    """a 4x multisampled scene: (colour samples uint8 [H, W, 4, 4], depth samples float32 [H, W, 4], resolved
+    colour uint8 [H, W, 4], stats)"""
+    assert scene.samples == 4 and scene.depth_format == "d32"
+    c1, d1 = clear_images(scene)
+    color4 = np.ascontiguousarray(np.repeat(c1[:, :, None, :], 4, axis=2))
+    depth4 = np.ascontiguousarray(np.repeat(d1[:, :, None], 4, axis=2))
+    arr, n = make_draws(scene)
+    st = KzoStats()
+    area = (ctypes.c_int32 * 4)(0, 0, scene.width, scene.height)
+    rc = lib().kzo_render_ds(scene.width, scene.height, color4.ctypes.data, depth4.ctypes.data, None, 0, area, n, arr,
+                             threads, ctypes.byref(st))
+    if rc != 0:
+        raise RuntimeError("oracle failed")
+    resolved = np.empty((scene.height, scene.width, 4), dtype=np.uint8)
+    lib().kzo_resolve(scene.width, scene.height, color4.ctypes.data, resolved.ctypes.data)
+    return color4, depth4, resolved, st.as_dict()
+
+
 def render(scene, threads=1, draws=None, color=None, depth=None):
     """Render `scene` (a kazan_gb300.scenes.Scene) from cleared attachments; returns
     (color uint8 [H, W, 4], depth attachment texels [H, W] (float32 for d32, see packed_depth), stats dict)."""
+    if scene.samples == 4:
+        _, depth4, resolved, st = render_ms(scene, threads)
+        return resolved, depth4, st
     if color is None or depth is None:
         color, depth = clear_images(scene)
     arr, n = make_draws(scene, draws)
