@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--ndraws", type=int, default=4096)
     ap.add_argument("--tile", type=int, default=16)
     ap.add_argument("--mode", default="batched", choices=["persistent", "batched", "perdraw"])
+    ap.add_argument("--samples", type=int, default=1, choices=[1, 4],
+                    help="4: multisampled colour and depth attachments resolved at the end of the pass")
+    ap.add_argument("--depth-format", default="d32", choices=["d32", "d16", "d24s8"])
     ap.add_argument("--indirect", default="none", choices=["none", "host", "device"],
                     help="record the draws as vkCmdDraw*Indirect over commands in host-visible memory, or in "
                          "device memory written by a vkCmdCopyBuffer in the same command buffer")
@@ -56,6 +59,15 @@ def parse():
 
 
 def make_scene(args):
+    scene, cfg = _base_scene(args)
+    if args.samples != 1 or args.depth_format != "d32":
+        import dataclasses
+        scene = dataclasses.replace(scene, samples=args.samples, depth_format=args.depth_format)
+        cfg = dict(cfg, workload=cfg["workload"] + ", %dx samples, %s depth" % (args.samples, args.depth_format.upper()))
+    return scene, cfg
+
+
+def _base_scene(args):
     from kazan_gb300 import scenes
     if args.workload == "batched":
         return scenes.batched(ndraws=args.ndraws), {"workload": "batched: %d vkCmdDrawIndexed, 2048x2048 RGBA8+D32, "
