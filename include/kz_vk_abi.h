@@ -1050,6 +1050,24 @@ typedef struct VkBindImageMemoryInfo {
   VkDeviceSize memoryOffset;
 } VkBindImageMemoryInfo;
 
+typedef struct VkImageCopy {
+  VkImageSubresourceLayers srcSubresource;
+  VkOffset3D srcOffset;
+  VkImageSubresourceLayers dstSubresource;
+  VkOffset3D dstOffset;
+  VkExtent3D extent;
+} VkImageCopy;
+typedef struct VkClearAttachment {
+  VkImageAspectFlags aspectMask;
+  uint32_t colorAttachment;
+  VkClearValue clearValue;
+} VkClearAttachment;
+typedef struct VkClearRect {
+  VkRect2D rect;
+  uint32_t baseArrayLayer;
+  uint32_t layerCount;
+} VkClearRect;
+
 typedef struct VkImageResolve {
   VkImageSubresourceLayers srcSubresource;
   VkOffset3D srcOffset;

@@ -183,6 +183,15 @@ static bool begin_draw(CommandBuffer* cb, bool indexed, DrawRec& dr, int& nreads
   d.zmax = std::fmax(vp.minDepth, vp.maxDepth);
   draw_rect(pass.fb, pass.area, sc, vp, d.rect);
   std::memcpy(dr.push, cb->push, KZ_PUSH_BYTES);
+  /* stencil words of the draw: the pipeline's, with the dynamic compare mask / write mask / reference */
+  for (int f = 0; f < 2; f++) {
+    uint32_t w1 = p->pipe.stencil[2 * f + 1];
+    if (p->dyn_stencil & 1u) w1 = (w1 & ~0xFFu) | (cb->stencil_dyn[0][f] & 0xFFu);
+    if (p->dyn_stencil & 2u) w1 = (w1 & ~0xFF00u) | ((cb->stencil_dyn[1][f] & 0xFFu) << 8);
+    if (p->dyn_stencil & 4u) w1 = (w1 & ~0xFF0000u) | ((cb->stencil_dyn[2][f] & 0xFFu) << 16);
+    d.stencil[2 * f] = p->pipe.stencil[2 * f];
+    d.stencil[2 * f + 1] = w1;
+  }
   if (p->layout && !snapshot_descriptors(cb, p, dr)) return false;
   return true;
 }
@@ -340,6 +349,7 @@ static void reset_cb(CommandBuffer* cb) {
     cb->sets[s] = nullptr;
     cb->dyn_offsets[s].clear();
   }
+  std::memset(cb->stencil_dyn, 0, sizeof cb->stencil_dyn);
   cb->cur_pass = -1;
   cb->passes.clear();
   cb->ops.clear();
@@ -546,6 +556,8 @@ void VKAPI_CALL kzCmdBeginRenderPass(VkCommandBuffer cbh, const VkRenderPassBegi
   cb->ops.push_back(op);
 }
 
+static void clear_image(CommandBuffer* cb, Image* img, uint32_t value);
+
 static void record_resolve(CommandBuffer* cb, Image* src, Image* dst, int32_t sx, int32_t sy, int32_t dx, int32_t dy,
                            int32_t w, int32_t h) {
   RecOp op;
@@ -584,6 +596,68 @@ void VKAPI_CALL kzCmdEndRenderPass(VkCommandBuffer cbh) {
     }
   }
   cb->cur_pass = -1;
+}
+
+void VKAPI_CALL kzCmdClearAttachments(VkCommandBuffer cbh, uint32_t n, const VkClearAttachment* atts, uint32_t nr,
+                                      const VkClearRect* rects) {
+  /* vkCmdClearAttachments inside a render pass: the draws recorded so far and the ones after the clears
+   * become two passes over the same framebuffer (the second loads its attachments), with the clears, rects
+   * clipped to the framebuffer and render area, in between */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  if (cb->cur_pass < 0) {
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
+  const PassRec cur = cb->passes[(size_t)cb->cur_pass];
+  const RenderPass* rp = cur.rp;
+  for (uint32_t i = 0; i < n; i++) {
+    const VkClearAttachment& a = atts[i];
+    int att = (a.aspectMask & VK_IMAGE_ASPECT_COLOR_BIT) ? (a.colorAttachment == 0 ? rp->color_att : -1) : rp->depth_att;
+    if (att < 0 || (size_t)att >= cur.fb->views.size()) continue;
+    Image* img = cur.fb->views[(size_t)att]->image;
+    uint32_t value;
+    if (a.aspectMask & VK_IMAGE_ASPECT_COLOR_BIT) {
+      value = pack_color(img->format, a.clearValue.color.float32);
+    } else if (img->format == VK_FORMAT_D32_SFLOAT) {
+      value = float_bits(a.clearValue.depthStencil.depth);
+    } else if (img->format == VK_FORMAT_D24_UNORM_S8_UINT &&
+               (a.aspectMask & (VK_IMAGE_ASPECT_DEPTH_BIT | VK_IMAGE_ASPECT_STENCIL_BIT)) ==
+                   (VK_IMAGE_ASPECT_DEPTH_BIT | VK_IMAGE_ASPECT_STENCIL_BIT)) {
+      value = (uint32_t)std::rint(a.clearValue.depthStencil.depth * 16777215.0f) |
+              ((a.clearValue.depthStencil.stencil & 0xFFu) << 24);
+    } else {
+      log_error("vkCmdClearAttachments: D16 images and single aspects of D24S8 are not cleared by rectangle");
+      cb->record_error = VK_ERROR_FEATURE_NOT_PRESENT;
+      return;
+    }
+    for (uint32_t k = 0; k < nr; k++) {
+      const VkRect2D& r = rects[k].rect;
+      int32_t x0 = std::max({r.offset.x, cur.area[0], 0}), y0 = std::max({r.offset.y, cur.area[1], 0});
+      int32_t x1 = std::min({r.offset.x + (int32_t)r.extent.width, cur.area[2], (int32_t)img->width});
+      int32_t y1 = std::min({r.offset.y + (int32_t)r.extent.height, cur.area[3], (int32_t)img->height});
+      if (x1 <= x0 || y1 <= y0) continue;
+      clear_image(cb, img, value);
+      RecOp& op = cb->ops.back();
+      const int32_t spp = (int32_t)img->samples; /* 32-bit words per pixel */
+      op.rect[0] = x0 * spp;
+      op.rect[1] = y0;
+      op.rect[2] = x1 * spp;
+      op.rect[3] = y1;
+    }
+  }
+  PassRec next;
+  next.fb = cur.fb;
+  next.rp = cur.rp;
+  std::memcpy(next.area, cur.area, sizeof next.area);
+  next.clear_color = cur.clear_color;
+  next.clear_depth = cur.clear_depth;
+  next.cont = true;
+  cb->passes.push_back(next);
+  cb->cur_pass = (int)cb->passes.size() - 1;
+  RecOp op;
+  op.kind = OpKind::Pass;
+  op.pass = cb->passes.size() - 1;
+  cb->ops.push_back(op);
 }
 
 void VKAPI_CALL kzCmdResolveImage(VkCommandBuffer cbh, VkImage srcImage, VkImageLayout, VkImage dstImage,
@@ -715,6 +789,72 @@ void VKAPI_CALL kzCmdCopyBufferToImage(VkCommandBuffer cbh, VkBuffer buffer, VkI
   for (uint32_t i = 0; i < n; i++) image_buffer_copy(H<CommandBuffer>(cbh), H<Image>(image), H<Buffer>(buffer), r[i], false);
 }
 
+static void set_stencil_state(VkCommandBuffer cbh, int which, VkFlags faces, uint32_t v) {
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  if (faces & 1u) cb->stencil_dyn[which][0] = v; /* VK_STENCIL_FACE_FRONT_BIT */
+  if (faces & 2u) cb->stencil_dyn[which][1] = v; /* VK_STENCIL_FACE_BACK_BIT */
+}
+
+void VKAPI_CALL kzCmdSetStencilCompareMask(VkCommandBuffer cbh, VkFlags faces, uint32_t v) {
+  set_stencil_state(cbh, 0, faces, v);
+}
+void VKAPI_CALL kzCmdSetStencilWriteMask(VkCommandBuffer cbh, VkFlags faces, uint32_t v) {
+  set_stencil_state(cbh, 1, faces, v);
+}
+void VKAPI_CALL kzCmdSetStencilReference(VkCommandBuffer cbh, VkFlags faces, uint32_t v) {
+  set_stencil_state(cbh, 2, faces, v);
+}
+
+void VKAPI_CALL kzCmdUpdateBuffer(VkCommandBuffer cbh, VkBuffer buffer, VkDeviceSize off, VkDeviceSize size,
+                                  const void* data) {
+  /* vkCmdUpdateBuffer: the bytes are copied at recording and written at execution, in command order */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  Buffer* b = H<Buffer>(buffer);
+  if (!b || (off & 3) || (size & 3) || size > 65536 || off + size > b->size) {
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
+  RecOp op;
+  op.kind = OpKind::Copy;
+  op.dst = b->ptr() + off;
+  op.bytes = (size_t)size;
+  op.data.assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + size);
+  op.wmem = b->mem;
+  cb->ops.push_back(op);
+}
+
+void VKAPI_CALL kzCmdCopyImage(VkCommandBuffer cbh, VkImage srcImage, VkImageLayout, VkImage dstImage, VkImageLayout,
+                               uint32_t n, const VkImageCopy* regions) {
+  /* vkCmdCopyImage between images of the same texel size and sample count, clipped to both */
+  CommandBuffer* cb = H<CommandBuffer>(cbh);
+  Image* s = H<Image>(srcImage);
+  Image* d = H<Image>(dstImage);
+  if (s->bpp != d->bpp || s->samples != d->samples) {
+    cb->record_error = VK_ERROR_FORMAT_NOT_SUPPORTED;
+    return;
+  }
+  const size_t tb = (size_t)s->bpp * s->samples;
+  for (uint32_t i = 0; i < n; i++) {
+    const VkImageCopy& r = regions[i];
+    if (r.srcOffset.x < 0 || r.srcOffset.y < 0 || r.dstOffset.x < 0 || r.dstOffset.y < 0) continue;
+    int32_t w = std::min({(int32_t)r.extent.width, (int32_t)s->width - r.srcOffset.x, (int32_t)d->width - r.dstOffset.x});
+    int32_t h = std::min({(int32_t)r.extent.height, (int32_t)s->height - r.srcOffset.y,
+                          (int32_t)d->height - r.dstOffset.y});
+    if (w <= 0 || h <= 0) continue;
+    RecOp op;
+    op.kind = OpKind::Copy2D;
+    op.src = s->ptr() + (size_t)r.srcOffset.y * s->pitch + (size_t)r.srcOffset.x * tb;
+    op.spitch = s->pitch;
+    op.dst = d->ptr() + (size_t)r.dstOffset.y * d->pitch + (size_t)r.dstOffset.x * tb;
+    op.dpitch = d->pitch;
+    op.width_bytes = (size_t)w * tb;
+    op.rows = (size_t)h;
+    op.rmem = s->mem;
+    op.wmem = d->mem;
+    cb->ops.push_back(op);
+  }
+}
+
 void VKAPI_CALL kzCmdFillBuffer(VkCommandBuffer cbh, VkBuffer buffer, VkDeviceSize off, VkDeviceSize size,
                                 uint32_t data) {
   CommandBuffer* cb = H<CommandBuffer>(cbh);
@@ -754,6 +894,8 @@ void free_lowered(Lowered* low) {
   device_free(low->d_shades);
   low->d_shades = nullptr;
   device_free(low->d_tiles);
+  device_free(low->d_inline);
+  low->d_inline = nullptr;
   device_free(low->d_vis);
   low->d_vis = nullptr;
   if (low->h_status) cudaFreeHost(low->h_status);
@@ -1093,10 +1235,32 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
     pipe_index[p] = idx;
     return idx;
   };
+  /* vkCmdUpdateBuffer data: one device block, uploaded now, that the copies read at execution */
+  size_t inline_bytes = 0, inline_off = 0;
+  for (const RecOp& op : cb->ops) inline_bytes += align_up(op.data.size(), 16);
+  if (inline_bytes) {
+    void* ip = nullptr;
+    VkResult ir = device_alloc(inline_bytes, &ip);
+    if (ir != VK_SUCCESS) return ir;
+    low.d_inline = static_cast<char*>(ip);
+    std::vector<uint8_t> staged(inline_bytes, 0);
+    size_t o = 0;
+    for (const RecOp& op : cb->ops) {
+      if (op.data.empty()) continue;
+      std::memcpy(staged.data() + o, op.data.data(), op.data.size());
+      o += align_up(op.data.size(), 16);
+    }
+    cudaMemcpy(low.d_inline, staged.data(), inline_bytes, cudaMemcpyHostToDevice);
+  }
   for (const RecOp& op : cb->ops) {
     Lowered::LOp lop;
     lop.kind = op.kind;
     lop.op = op;
+    if (!op.data.empty()) {
+      lop.op.src = low.d_inline + inline_off;
+      lop.op.data.clear();
+      inline_off += align_up(op.data.size(), 16);
+    }
     lop.seg_begin = (uint32_t)low.segments.size();
     if (op.kind != OpKind::Pass) {
       add_unique(low.writes, op.wmem);
@@ -1126,16 +1290,17 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
           b = i;
         }
     }
-    bool needs_clear = false;
+    bool needs_clear = false; /* a continuation after vkCmdClearAttachments loads its attachments */
     if (pr.rp->color_att >= 0 && pr.rp->atts[(size_t)pr.rp->color_att].loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR)
       needs_clear = true;
     if (pr.rp->depth_att >= 0 && pr.rp->atts[(size_t)pr.rp->depth_att].loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR)
       needs_clear = true;
+    if (pr.cont) needs_clear = false;
     if (runs.empty() && needs_clear) runs.push_back({0, 0});
     for (size_t r = 0; r < runs.size(); r++) {
       KzSegment s;
       std::memset(&s, 0, sizeof s);
-      segment_target(pr, s, low.tile, r == 0, low);
+      segment_target(pr, s, low.tile, r == 0 && !pr.cont, low);
       s.segment_index = (uint32_t)low.segments.size();
       s.first_draw = (uint32_t)low.draws.size();
       s.first_chunk = (uint32_t)low.chunks.size();

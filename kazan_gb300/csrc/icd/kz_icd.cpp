@@ -1171,6 +1171,9 @@ static VkResult create_graphics_pipeline(const VkGraphicsPipelineCreateInfo& ci,
       if (d == VK_DYNAMIC_STATE_VIEWPORT) p->dyn_viewport = true;
       if (d == VK_DYNAMIC_STATE_SCISSOR) p->dyn_scissor = true;
       if (d == VK_DYNAMIC_STATE_BLEND_CONSTANTS) p->dyn_blend = true;
+      if (d == VK_DYNAMIC_STATE_STENCIL_COMPARE_MASK) p->dyn_stencil |= 1u;
+      if (d == VK_DYNAMIC_STATE_STENCIL_WRITE_MASK) p->dyn_stencil |= 2u;
+      if (d == VK_DYNAMIC_STATE_STENCIL_REFERENCE) p->dyn_stencil |= 4u;
     }
   if (ci.pViewportState) {
     if (!p->dyn_viewport && ci.pViewportState->pViewports) p->viewport = ci.pViewportState->pViewports[0];
@@ -1406,6 +1409,14 @@ void VKAPI_CALL kzCmdCopyImageToBuffer(VkCommandBuffer, VkImage, VkImageLayout, 
 void VKAPI_CALL kzCmdCopyBufferToImage(VkCommandBuffer, VkBuffer, VkImage, VkImageLayout, uint32_t,
                                        const VkBufferImageCopy*);
 void VKAPI_CALL kzCmdFillBuffer(VkCommandBuffer, VkBuffer, VkDeviceSize, VkDeviceSize, uint32_t);
+void VKAPI_CALL kzCmdUpdateBuffer(VkCommandBuffer, VkBuffer, VkDeviceSize, VkDeviceSize, const void*);
+void VKAPI_CALL kzCmdCopyImage(VkCommandBuffer, VkImage, VkImageLayout, VkImage, VkImageLayout, uint32_t,
+                               const VkImageCopy*);
+void VKAPI_CALL kzCmdClearAttachments(VkCommandBuffer, uint32_t, const VkClearAttachment*, uint32_t,
+                                      const VkClearRect*);
+void VKAPI_CALL kzCmdSetStencilCompareMask(VkCommandBuffer, VkFlags, uint32_t);
+void VKAPI_CALL kzCmdSetStencilWriteMask(VkCommandBuffer, VkFlags, uint32_t);
+void VKAPI_CALL kzCmdSetStencilReference(VkCommandBuffer, VkFlags, uint32_t);
 }
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -1528,6 +1539,14 @@ static const ProcEntry kProcs[] = {
     KZ_PROC("vkCmdCopyImageToBuffer", kzCmdCopyImageToBuffer),
     KZ_PROC("vkCmdCopyBufferToImage", kzCmdCopyBufferToImage),
     KZ_PROC("vkCmdFillBuffer", kzCmdFillBuffer),
+    KZ_PROC("vkCmdUpdateBuffer", kzCmdUpdateBuffer),
+    KZ_PROC("vkCmdCopyImage", kzCmdCopyImage),
+    KZ_PROC("vkCmdClearAttachments", kzCmdClearAttachments),
+    KZ_PROC("vkCmdSetStencilCompareMask", kzCmdSetStencilCompareMask),
+    KZ_PROC("vkCmdSetStencilWriteMask", kzCmdSetStencilWriteMask),
+    KZ_PROC("vkCmdSetStencilReference", kzCmdSetStencilReference),
+    KZ_PROC("vkCmdDrawIndirectCountAMD", kzCmdDrawIndirectCount),
+    KZ_PROC("vkCmdDrawIndexedIndirectCountAMD", kzCmdDrawIndexedIndirectCount),
 };
 
 static PFN_vkVoidFunction lookup(const char* name) {

@@ -179,6 +179,7 @@ struct Pipeline {
   VkViewport viewport{};
   VkRect2D scissor{};
   bool dyn_viewport = false, dyn_scissor = false, dyn_blend = false;
+  uint32_t dyn_stencil = 0; /* bit 0 compare mask, bit 1 write mask, bit 2 reference are dynamic state */
   bool rasterizer_discard = false;
   int vis_key = -1; /* KzVisKey when the pipeline can be resolved order-independently, else -1 */
   std::shared_ptr<PipelineLayoutInfo> layout;   /* descriptor slots (null: no descriptor sets) */
@@ -245,6 +246,7 @@ struct DrawRec {
 struct PassRec {
   Framebuffer* fb = nullptr;
   RenderPass* rp = nullptr;
+  bool cont = false; /* continues the render pass instance before a vkCmdClearAttachments: attachments load */
   int32_t area[4] = {0, 0, 0, 0};
   VkClearValue clear_color{}, clear_depth{};
   std::vector<DrawRec> draws;
@@ -268,6 +270,7 @@ struct RecOp {
   size_t bytes = 0, width_bytes = 0, rows = 0, dpitch = 0, spitch = 0;
   DeviceMemory* wmem = nullptr;          /* memory the op writes */
   DeviceMemory* rmem = nullptr;          /* memory the op reads */
+  std::vector<uint8_t> data;             /* vkCmdUpdateBuffer: the bytes, copied from device memory at execution */
 };
 
 /* lowered command buffer */
@@ -300,6 +303,7 @@ struct Lowered {
   uint32_t* d_tiles = nullptr;
   char* d_vis = nullptr;
   char* d_shades = nullptr;   /* ordered segments: per-record shading setup (KzSegment::shades) */
+  char* d_inline = nullptr;   /* vkCmdUpdateBuffer data of the command buffer */
   uint32_t shade_stride = 0;
   KzSegCounters* d_counters = nullptr;
   KzStatus* d_status = nullptr;
@@ -337,6 +341,7 @@ struct CommandBuffer : Dispatchable {
   VkIndexType ib_type = VK_INDEX_TYPE_UINT32;
   uint8_t push[KZ_PUSH_BYTES] = {};
   DescriptorSet* sets[KZ_MAX_DESC_SETS] = {};
+  uint32_t stencil_dyn[3][2] = {}; /* vkCmdSetStencil{CompareMask,WriteMask,Reference}: [state][front, back] */
   std::vector<uint32_t> dyn_offsets[KZ_MAX_DESC_SETS]; /* per bound set, its dynamic offsets */
   int cur_pass = -1;
   std::vector<PassRec> passes;

@@ -141,8 +141,10 @@ typedef struct KzDraw {
   uint32_t call_index;          /* position of the command within its vkCmdDraw*Indirect*Count call */
   uint64_t count_addr;          /* vkCmdDraw*IndirectCount: device address of the u32 draw count (the draw is
                                    skipped when call_index >= count); 0: every recorded command draws */
-  uint32_t samples;             /* rasterizationSamples of its pass: 1, or 4 (KZ_SAMPLE_* positions) */
+  uint32_t samples;             /* rasterizationSamples of its pass: 1, or 4 (KZ_MS_* positions) */
   uint32_t pad;
+  uint32_t stencil[4];          /* the draw's stencil state in KzPipe::stencil's encoding: the pipeline's, with
+                                   vkCmdSetStencilCompareMask / WriteMask / Reference applied where dynamic */
 } KzDraw;
 
 /* the four sample positions of a 4x multisampled pixel (the Vulkan standard positions), in 1/256 pixel

@@ -1947,7 +1947,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
       be.write_mask = bp.write_mask;
       be.stencil = bp.stencil_test && has_st ? (1u | (bp.fs_discards ? 2u : 0u)) : 0u;
 #pragma unroll
-      for (int k = 0; k < 4; k++) be.st[k] = bp.stencil[k];
+      for (int k = 0; k < 4; k++) be.st[k] = bd.stencil[k];
       /* edge values at the tile's first pixel centre, from the record that shading uses */
       Edges ed;
       edges_of(be.s.r, ed);

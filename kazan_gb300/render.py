@@ -361,7 +361,8 @@ class Renderer:
         self._objects.append(("PipelineLayout", h))
         return h
 
-    def pipeline(self, scene, rp, layout, vs_words, fs_words):
+    def pipeline(self, scene, rp, layout, vs_words, fs_words, dynamic=()):
+        """`dynamic`: VkDynamicState values the pipeline leaves to the command buffer"""
         vsm, fsm = self.shader_module(vs_words), self.shader_module(fs_words)
         stages = (vk.VkPipelineShaderStageCreateInfo * 2)()
         stages[0] = vk.VkPipelineShaderStageCreateInfo(vk.ST_PIPELINE_SHADER_STAGE_CREATE_INFO, None, 0,
@@ -413,9 +414,12 @@ class Renderer:
                                                          vk.COLOR_MASK_RGBA)
         cbs = vk.VkPipelineColorBlendStateCreateInfo(vk.ST_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO, None, 0, 0, 0, 1,
                                                      pointer(att), (c_float * 4)(0, 0, 0, 0))
+        dyn_arr = (ctypes.c_int * max(1, len(dynamic)))(*dynamic)
+        dyn = vk.VkPipelineDynamicStateCreateInfo(vk.ST_PIPELINE_DYNAMIC_STATE_CREATE_INFO, None, 0, len(dynamic),
+                                                  dyn_arr)
         gci = vk.VkGraphicsPipelineCreateInfo(vk.ST_GRAPHICS_PIPELINE_CREATE_INFO, None, 0, 2, stages, pointer(vis),
                                               pointer(ias), None, pointer(vps), pointer(rs), pointer(ms), pointer(ds),
-                                              pointer(cbs), None, layout, rp, 0, None, -1)
+                                              pointer(cbs), pointer(dyn) if dynamic else None, layout, rp, 0, None, -1)
         h = c_void_p()
         check("vkCreateGraphicsPipelines",
               self.drv.vkCreateGraphicsPipelines(self.device, None, 1, byref(gci), None, byref(h)))

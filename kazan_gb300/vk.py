@@ -45,6 +45,8 @@ ST_PIPELINE_MULTISAMPLE_STATE_CREATE_INFO = 24
 ST_PIPELINE_DEPTH_STENCIL_STATE_CREATE_INFO = 25
 ST_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO = 26
 ST_PIPELINE_DYNAMIC_STATE_CREATE_INFO = 27
+DYNAMIC_STATE_VIEWPORT, DYNAMIC_STATE_SCISSOR, DYNAMIC_STATE_BLEND_CONSTANTS = 0, 1, 4
+DYNAMIC_STATE_STENCIL_COMPARE_MASK, DYNAMIC_STATE_STENCIL_WRITE_MASK, DYNAMIC_STATE_STENCIL_REFERENCE = 6, 7, 8
 ST_GRAPHICS_PIPELINE_CREATE_INFO = 28
 ST_PIPELINE_LAYOUT_CREATE_INFO = 30
 ST_SAMPLER_CREATE_INFO = 31
@@ -495,9 +497,22 @@ class VkClearValue(Union):
     _fields_ = [("color", VkClearColorValue), ("depthStencil", VkClearDepthStencilValue)]
 
 
+class VkClearAttachment(Structure):
+    _fields_ = [("aspectMask", c_uint32), ("colorAttachment", c_uint32), ("clearValue", VkClearValue)]
+
+
+class VkClearRect(Structure):
+    _fields_ = [("rect", VkRect2D), ("baseArrayLayer", c_uint32), ("layerCount", c_uint32)]
+
+
 class VkRenderPassBeginInfo(Structure):
     _fields_ = [("sType", c_int), ("pNext", c_void_p), ("renderPass", c_void_p), ("framebuffer", c_void_p),
                 ("renderArea", VkRect2D), ("clearValueCount", c_uint32), ("pClearValues", POINTER(VkClearValue))]
+
+
+class VkImageCopy(Structure):
+    _fields_ = [("srcSubresource", VkImageSubresourceLayers), ("srcOffset", VkOffset3D),
+                ("dstSubresource", VkImageSubresourceLayers), ("dstOffset", VkOffset3D), ("extent", VkExtent3D)]
 
 
 class VkImageResolve(Structure):
@@ -644,6 +659,12 @@ _PROTOS = {
     "vkEnumerateDeviceExtensionProperties": (c_int, [H, ctypes.c_char_p, P(c_uint32), P(VkExtensionProperties)]),
     "vkGetPhysicalDeviceFeatures": (None, [H, P(c_uint32)]),
     "vkCmdResolveImage": (None, [H, H, c_int, H, c_int, c_uint32, P(VkImageResolve)]),
+    "vkCmdCopyImage": (None, [H, H, c_int, H, c_int, c_uint32, P(VkImageCopy)]),
+    "vkCmdUpdateBuffer": (None, [H, H, c_uint64, c_uint64, c_void_p]),
+    "vkCmdClearAttachments": (None, [H, c_uint32, c_void_p, c_uint32, c_void_p]),
+    "vkCmdSetStencilCompareMask": (None, [H, c_uint32, c_uint32]),
+    "vkCmdSetStencilWriteMask": (None, [H, c_uint32, c_uint32]),
+    "vkCmdSetStencilReference": (None, [H, c_uint32, c_uint32]),
     "vkCreateSampler": (c_int, [H, P(VkSamplerCreateInfo), c_void_p, P(H)]),
     "vkDestroySampler": (None, [H, H, c_void_p]),
     "vkCreateDescriptorSetLayout": (c_int, [H, P(VkDescriptorSetLayoutCreateInfo), c_void_p, P(H)]),

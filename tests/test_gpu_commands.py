@@ -1,0 +1,180 @@
+"""GPU checks of the transfer and state commands around the draw path: vkCmdUpdateBuffer (vertex data written by
+the command buffer itself), vkCmdCopyImage, vkCmdClearAttachments between draws of one render pass, and
+dynamic stencil reference / masks, each against the CPU oracle or a numpy restatement."""
+import ctypes
+import dataclasses
+from ctypes import byref, c_uint32, c_uint64, c_void_p
+
+import numpy as np
+import pytest
+
+from kazan_gb300 import render, scenes, vk
+from oracle import kz_oracle
+
+from scene_cases import small_cases
+
+
+def _record(run, body, before=None):
+    """a command buffer: `before(d, cb)` outside the pass, then the pass with the run's pipeline and vertex
+    buffer bound and `body(d, cb)` recording the draws"""
+    r, s, d = run.r, run.scene, run.r.drv
+    cb = r.begin()
+    if before:
+        before(d, cb)
+    clears = (vk.VkClearValue * 2)()
+    clears[0].color.float32[:] = list(s.clear_color)
+    clears[1].depthStencil.depth = s.clear_depth
+    clears[1].depthStencil.stencil = s.clear_stencil
+    rbi = vk.VkRenderPassBeginInfo(vk.ST_RENDER_PASS_BEGIN_INFO, None, run.rp, run.fb,
+                                   vk.VkRect2D(vk.VkOffset2D(0, 0), vk.VkExtent2D(s.width, s.height)), 2, clears)
+    d.vkCmdBeginRenderPass(cb, byref(rbi), vk.SUBPASS_CONTENTS_INLINE)
+    d.vkCmdBindPipeline(cb, vk.BIND_POINT_GRAPHICS, run.pipe)
+    bufs = (c_void_p * 1)(run.vb.handle.value)
+    d.vkCmdBindVertexBuffers(cb, 0, 1, bufs, (c_uint64 * 1)(0))
+    if run.ib is not None:
+        d.vkCmdBindIndexBuffer(cb, run.ib.handle, 0, vk.INDEX_TYPE_UINT32)
+    body(d, cb)
+    d.vkCmdEndRenderPass(cb)
+    vk.check("vkEndCommandBuffer", d.vkEndCommandBuffer(cb))
+    return cb
+
+
+def _submit(run, cb):
+    run.r.submit_wait(cb)
+    color, depth = run.read()
+    st = run.r.drv.stats(cb)
+    run.r.free_command_buffer(cb)
+    return color, depth, st
+
+
+def _draw(d, cb, run, dr):
+    if dr.mvp is not None:
+        m = np.ascontiguousarray(dr.mvp, dtype=np.float32)
+        d.vkCmdPushConstants(cb, run.layout, vk.SHADER_STAGE_VERTEX, 0, 64, m.ctypes.data)
+    if run.scene.indexed:
+        d.vkCmdDrawIndexed(cb, 3 * dr.count, 1, dr.first, dr.vertex_offset, 0)
+    else:
+        d.vkCmdDraw(cb, 3 * dr.count, 1, dr.first, 0)
+
+
+@pytest.mark.gpu
+def test_update_buffer_writes_vertex_data(renderer):
+    """the soup's vertices reach a device-local buffer only through vkCmdUpdateBuffer (64 KB pieces) in the
+    command buffer that draws them"""
+    scene = small_cases()["soup"]
+    run = render.SceneRun(renderer, scene, mode="batched", tile=16)
+    vb2 = renderer.create_buffer(scene.vertices.nbytes, vk.BUFFER_USAGE_VERTEX, False)
+    raw = np.ascontiguousarray(scene.vertices).view(np.uint8).ravel()
+
+    def before(d, cb):
+        for off in range(0, raw.size, 65536):
+            piece = np.ascontiguousarray(raw[off:off + 65536])
+            d.vkCmdUpdateBuffer(cb, vb2.handle, off, piece.size, piece.ctypes.data)
+
+    run.vb = vb2
+    cb = _record(run, lambda d, cb: _draw(d, cb, run, scene.draws[0]), before)
+    color, depth, st = _submit(run, cb)
+    ref_c, ref_d, ost = kz_oracle.render(scene, threads=8)
+    assert np.array_equal(color, ref_c) and np.array_equal(depth.view(np.uint32), ref_d.view(np.uint32))
+    assert st.fragments == ost["fragments"]
+
+
+@pytest.mark.gpu
+def test_copy_image_region(renderer):
+    scene = small_cases()["soup"]
+    run = render.SceneRun(renderer, scene, mode="batched", tile=16)
+    run.submit()
+    color, _ = run.read()
+    dst = renderer.create_image(90, 70, vk.FORMAT_R8G8B8A8_UNORM, vk.IMAGE_USAGE_COLOR_ATTACHMENT, True)
+    cb = renderer.begin()
+    sub = vk.VkImageSubresourceLayers(vk.IMAGE_ASPECT_COLOR, 0, 0, 1)
+    reg = vk.VkImageCopy(sub, vk.VkOffset3D(100, 33, 0), sub, vk.VkOffset3D(7, 3, 0), vk.VkExtent3D(80, 60, 1))
+    renderer.drv.vkCmdCopyImage(cb, run.color.handle, vk.IMAGE_LAYOUT_GENERAL, dst.handle, vk.IMAGE_LAYOUT_GENERAL, 1,
+                                byref(reg))
+    renderer.end_submit_wait(cb)
+    renderer.free_command_buffer(cb)
+    got = renderer.read_image(dst)
+    assert np.array_equal(got[3:63, 7:87], color[33:93, 100:180])
+    renderer.free_command_buffer(run.cb)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["batched", "persistent"])
+def test_clear_attachments_between_draws(renderer, mode):
+    """half of the 48 draws, a clear of two colour rectangles and one depth rectangle, then the other half:
+    the oracle renders the first half, applies the clears to its images and renders the rest into them"""
+    scene = small_cases()["batched"]
+    run = render.SceneRun(renderer, scene, mode=mode, tile=16)
+    half = len(scene.draws) // 2
+    crects = [(20, 30, 200, 100), (300, 250, 120, 220)]
+    drect = (150, 150, 256, 256)
+    ccol = (0.25, 0.5, 1.0, 0.75)
+
+    def body(d, cb):
+        for dr in scene.draws[:half]:
+            _draw(d, cb, run, dr)
+        atts = (vk.VkClearAttachment * 2)()
+        atts[0].aspectMask = vk.IMAGE_ASPECT_COLOR
+        atts[0].colorAttachment = 0
+        atts[0].clearValue.color.float32[:] = list(ccol)
+        atts[1].aspectMask = vk.IMAGE_ASPECT_DEPTH
+        atts[1].clearValue.depthStencil.depth = 0.0
+        rc = (vk.VkClearRect * 2)(*[vk.VkClearRect(vk.VkRect2D(vk.VkOffset2D(x, y), vk.VkExtent2D(w, h)), 0, 1)
+                                    for x, y, w, h in crects])
+        d.vkCmdClearAttachments(cb, 1, ctypes.cast(atts, c_void_p), 2, ctypes.cast(rc, c_void_p))
+        rd = vk.VkClearRect(vk.VkRect2D(vk.VkOffset2D(drect[0], drect[1]), vk.VkExtent2D(drect[2], drect[3])), 0, 1)
+        d.vkCmdClearAttachments(cb, 1, ctypes.cast(byref(atts[1]), c_void_p), 1, ctypes.cast(byref(rd), c_void_p))
+        for dr in scene.draws[half:]:
+            _draw(d, cb, run, dr)
+
+    color, depth, st = _submit(run, _record(run, body))
+    ref_c, ref_d, s0 = kz_oracle.render(scene, threads=8, draws=scene.draws[:half])
+    px = [kz_oracle.unorm8(v) for v in ccol]
+    for x, y, w, h in crects:
+        ref_c[y:y + h, x:x + w] = px
+    ref_d[drect[1]:drect[1] + drect[3], drect[0]:drect[0] + drect[2]] = 0.0
+    ref_c, ref_d, s1 = kz_oracle.render(scene, threads=8, draws=scene.draws[half:], color=ref_c, depth=ref_d)
+    assert np.array_equal(color, ref_c)
+    assert np.array_equal(depth.view(np.uint32), ref_d.view(np.uint32))
+    assert st.fragments == s0["fragments"] + s1["fragments"]
+    renderer.free_command_buffer(run.cb)
+
+
+@pytest.mark.gpu
+def test_dynamic_stencil_reference_and_masks(renderer):
+    """REPLACE with a dynamic reference: 3 for the first draw, then 7 for front faces only with a dynamic write
+    mask of 0x0F; the oracle renders the same two draws with those static states"""
+    S = scenes.StencilOp
+    base = small_cases()["soup"]
+    scene = dataclasses.replace(base, draws=[scenes.Draw(0, 1024), scenes.Draw(1024, 1024)], depth_format="d24s8",
+                                stencil=dict(front=S(pass_=2, depth_fail=2, write_mask=0xFF),
+                                             back=S(pass_=2, depth_fail=2, write_mask=0xFF)), clear_stencil=0x50)
+    run = render.SceneRun(renderer, scene, mode="batched", tile=16)
+    vs, fs = scene.shaders()
+    run.pipe = renderer.pipeline(scene, run.rp, run.layout, vs, fs,
+                                 dynamic=(vk.DYNAMIC_STATE_STENCIL_WRITE_MASK, vk.DYNAMIC_STATE_STENCIL_REFERENCE))
+
+    def body(d, cb):
+        d.vkCmdSetStencilWriteMask(cb, 3, 0xFF)
+        d.vkCmdSetStencilReference(cb, 3, 3)
+        _draw(d, cb, run, scene.draws[0])
+        d.vkCmdSetStencilReference(cb, 1, 7)
+        d.vkCmdSetStencilWriteMask(cb, 1, 0x0F)
+        _draw(d, cb, run, scene.draws[1])
+
+    color, depth, st = _submit(run, _record(run, body))
+    # the oracle: the same draws, each with its stencil state written out
+    col, dep = kz_oracle.clear_images(scene)
+    sten = np.full((scene.height, scene.width), 0x50, dtype=np.uint8)
+    arr, n = kz_oracle.make_draws(scene)
+    for face in ("front", "back"):
+        getattr(arr[0], face).reference = 3
+        getattr(arr[1], face).reference = 7 if face == "front" else 3
+    arr[1].front.write_mask = 0x0F
+    ost = kz_oracle.KzoStats()
+    area = (ctypes.c_int32 * 4)(0, 0, scene.width, scene.height)
+    kz_oracle.lib().kzo_render_ds(scene.width, scene.height, col.ctypes.data, dep.ctypes.data, sten.ctypes.data,
+                                  kz_oracle.DEPTH_FORMAT["d24s8"], area, n, arr, 8, byref(ost))
+    assert np.array_equal(color, col)
+    assert np.array_equal(depth, kz_oracle.packed_depth(dep, sten, "d24s8"))
+    assert len(np.unique(depth >> 24)) >= 3
