@@ -2,6 +2,8 @@
 
   kz_pipeline.cubin    relocatable sm_103a object with the pipeline kernels (nvcc -rdc -cubin); the
                        driver JIT-links it with each pipeline set's shader PTX at run time
+  kz_tex.cubin         relocatable object with the texture sampling functions the shaders call, built
+                       within 64 registers per thread (linked with the same PTX)
   libkazan_driver.so   the Vulkan driver (ICD) + shader compiler + PTX backend, C ABI
                        (include/kazan_driver.h, include/kz_shader_backend.h); CUDA runtime linked
                        statically, so the library loads on a machine without a GPU driver; it also
@@ -73,6 +75,19 @@ def pipeline_object(verbose=False):
     return out
 
 
+def texture_object(verbose=False):
+    """kz_tex.cubin: the texture sampling functions the shaders call, within 64 registers per thread"""
+    src = os.path.join(CSRC, "raster", "kz_tex.cu")
+    out = os.path.join(OUT, "kz_tex.cubin")
+    if _newer(out, [src, os.path.join(CSRC, "kz_raster_abi.h")]):
+        cmd = [NVCC, "-rdc=true", "-cubin"] + ARCH + ["-O3", "-lineinfo", "-fmad=false", "-maxrregcount=64", "-o", out,
+                                                     src]
+        log = _run(cmd)
+        if verbose:
+            sys.stdout.write(log)
+    return out
+
+
 def _compile_cpp(src):
     obj = os.path.join(OUT, "obj", os.path.basename(src).replace(".cpp", ".o"))
     if _newer(obj, [src] + _include_deps()):
@@ -119,7 +134,8 @@ def scene_library():
 def build_all(verbose=False):
     os.makedirs(OUT, exist_ok=True)
     with concurrent.futures.ThreadPoolExecutor(max_workers=3) as ex:
-        futs = [ex.submit(pipeline_object, verbose), ex.submit(driver_library), ex.submit(scene_library)]
+        futs = [ex.submit(pipeline_object, verbose), ex.submit(texture_object, verbose), ex.submit(driver_library),
+                ex.submit(scene_library)]
         return [f.result() for f in futs]
 
 

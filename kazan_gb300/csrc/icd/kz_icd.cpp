@@ -77,27 +77,36 @@ void device_free(void* p) {
   if (p) cudaFree(p);
 }
 
-/* the relocatable pipeline-kernel object built next to this library */
-const std::vector<char>& pipeline_object() {
-  static std::vector<char> obj = [] {
-    std::vector<char> v;
-    std::string path;
-    const char* env = std::getenv("KZ_PIPELINE_OBJECT");
-    if (env) {
-      path = env;
-    } else {
-      Dl_info info;
-      if (dladdr((void*)&pipeline_object, &info) && info.dli_fname) {
-        path = info.dli_fname;
-        size_t slash = path.rfind('/');
-        path = (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/kz_pipeline.cubin";
-      }
+/* a relocatable object built next to this library (`env` overrides its path) */
+static std::vector<char> load_object(const char* env, const char* name) {
+  std::vector<char> v;
+  std::string path;
+  const char* e = std::getenv(env);
+  if (e) {
+    path = e;
+  } else {
+    Dl_info info;
+    if (dladdr((void*)&load_object, &info) && info.dli_fname) {
+      path = info.dli_fname;
+      size_t slash = path.rfind('/');
+      path = (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/" + name;
     }
-    std::ifstream f(path, std::ios::binary);
-    if (f) v.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
-    else log_error("pipeline kernel object not found at %s", path.c_str());
-    return v;
-  }();
+  }
+  std::ifstream f(path, std::ios::binary);
+  if (f) v.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+  else log_error("object not found at %s", path.c_str());
+  return v;
+}
+
+/* the relocatable pipeline-kernel object */
+const std::vector<char>& pipeline_object() {
+  static std::vector<char> obj = load_object("KZ_PIPELINE_OBJECT", "kz_pipeline.cubin");
+  return obj;
+}
+
+/* the relocatable texture-sampling object the shaders call into */
+const std::vector<char>& texture_object() {
+  static std::vector<char> obj = load_object("KZ_TEXTURE_OBJECT", "kz_tex.cubin");
   return obj;
 }
 
@@ -141,7 +150,8 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
     return same->second;
   }
   std::vector<char> cubin;
-  err = ptx::link(ptx, obj.data(), obj.size(), cubin);
+  const std::vector<char>& tex = texture_object();
+  err = ptx::link(ptx, obj.data(), obj.size(), cubin, tex.data(), tex.size());
   if (!err.empty()) return nullptr;
   KernelSet* ks = new KernelSet();
   cudaSetDevice(dev->pd->cuda_device);

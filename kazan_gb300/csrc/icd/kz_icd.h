@@ -398,6 +398,7 @@ Options& options();
 VkResult device_alloc(size_t bytes, void** out);
 void device_free(void* p);
 const std::vector<char>& pipeline_object();
+const std::vector<char>& texture_object();
 KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std::string& err);
 void log_error(const char* fmt, ...);
 

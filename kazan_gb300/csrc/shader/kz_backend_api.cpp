@@ -12,6 +12,7 @@
 
 namespace kz {
 const std::vector<char>& pipeline_object();
+const std::vector<char>& texture_object();
 }
 
 namespace {
@@ -139,7 +140,8 @@ extern "C" KZ_API int kzShaderLink(const char* ptx, const void* object, size_t o
     object_size = o.size();
   }
   CompiledCode* c = new CompiledCode();
-  std::string e = kz::ptx::link(ptx, object, object_size, c->cubin);
+  const std::vector<char>& tex = kz::texture_object();
+  std::string e = kz::ptx::link(ptx, object, object_size, c->cubin, tex.data(), tex.size());
   if (!e.empty()) {
     set_err(err, err_size, e);
     delete c;

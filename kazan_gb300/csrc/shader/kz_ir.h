@@ -37,6 +37,13 @@ enum class Op : uint8_t {
   Tex,     /* dst..dst+3 (f32 registers allocated in a row) = the combined image sampler of binding imm2,
               array element imm (plus register c when c >= 0), sampled at (a, b) */
   TexFetch,/* dst..dst+3 = texel (a, b) (integers; outside the image: 0) of binding imm2, element imm (+ c) */
+  TexSize, /* dst, dst+1 (b32) = width, height of the image of binding imm2, element imm (+ c) */
+  Popc,    /* dst = number of set bits of a */
+  Brev,    /* dst = a with its 32 bits reversed */
+  Clz,     /* dst = leading zero bits of a (32 for 0) */
+  Bfe,     /* dst = bits [b, b + c) of a, sign-extended when imm != 0 (PTX bfe) */
+  F2H,     /* dst (b32) = a rounded to binary16 (nearest even), in the low 16 bits */
+  H2F,     /* dst (f32) = the binary16 value in the low 16 bits of a */
   FAdd, FSub, FMul, FDiv, FFma, FMin, FMax, FNeg, FAbs, FSqrt, FFloor, FCeil, FTrunc, FRoundEven,
   FSin, FCos, FEx2, FLg2,
   IAdd, ISub, IMul, UDiv, SDiv, URem, SRem, And, Or, Xor, Not, Shl, Shr, Sar, INeg,

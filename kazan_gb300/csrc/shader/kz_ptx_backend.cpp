@@ -303,6 +303,36 @@ class Emitter {
           uses_fetch |= i.op == Op::TexFetch;
           break;
         }
+        case Op::TexSize: {
+          uint32_t slot = slot_of(lay, i.imm2);
+          if (slot == ~0u) {
+            line("mov.b32 " + R(i.dst) + ", 0;");
+            line("mov.b32 " + R(i.dst + 1) + ", 0;");
+            break;
+          }
+          std::snprintf(buf, sizeof buf, "add.s64 %%kzd, %%kzpush, %u;", KZ_DESC_OFFSET + 32u * (slot + i.imm));
+          line(buf);
+          if (i.c >= 0) {
+            line("mul.wide.u32 %kzoff, " + R(i.c) + ", 32;");
+            line("add.s64 %kzd, %kzd, %kzoff;");
+          }
+          line("ld.global.nc.u32 " + R(i.dst) + ", [%kzd+12];");
+          line("ld.global.nc.u32 " + R(i.dst + 1) + ", [%kzd+16];");
+          break;
+        }
+        case Op::Popc: line("popc.b32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::Brev: line("brev.b32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::Clz: line("clz.b32 " + R(i.dst) + ", " + R(i.a) + ";"); break;
+        case Op::Bfe:
+          line(std::string(i.imm ? "bfe.s32 " : "bfe.u32 ") + R(i.dst) + ", " + R(i.a) + ", " + R(i.b) + ", " + R(i.c) +
+               ";");
+          break;
+        case Op::F2H:
+          line("{ .reg .b16 %kzh; cvt.rn.f16.f32 %kzh, " + R(i.a) + "; cvt.u32.u16 " + R(i.dst) + ", %kzh; }");
+          break;
+        case Op::H2F:
+          line("{ .reg .b16 %kzh; cvt.u16.u32 %kzh, " + R(i.a) + "; cvt.f32.f16 " + R(i.dst) + ", %kzh; }");
+          break;
         case Op::StOut: {
           if ((kind == Kind::VertexPos || kind == Kind::VertexPos3) && i.imm >= 16) break;
           if (kind == Kind::VertexPos3) {
@@ -582,7 +612,8 @@ std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vec
   return s + body;
 }
 
-std::string link(const std::string& ptx, const void* object, size_t object_size, std::vector<char>& cubin) {
+std::string link(const std::string& ptx, const void* object, size_t object_size, std::vector<char>& cubin,
+                 const void* tex_object, size_t tex_size) {
   nvJitLinkHandle h = nullptr;
   /* shader functions are called from kernels launched with at most 64 registers per thread (the geometry
    * kernel runs 4 blocks of 256 per SM); the linker rejects a callee that needs more than its caller's
@@ -599,6 +630,9 @@ std::string link(const std::string& ptx, const void* object, size_t object_size,
   };
   if (nvJitLinkAddData(h, NVJITLINK_INPUT_CUBIN, object, object_size, "kz_pipeline") != NVJITLINK_SUCCESS) {
     err = log("adding the pipeline kernels");
+  } else if (tex_object && tex_size &&
+             nvJitLinkAddData(h, NVJITLINK_INPUT_CUBIN, tex_object, tex_size, "kz_tex") != NVJITLINK_SUCCESS) {
+    err = log("adding the texture functions");
   } else if (nvJitLinkAddData(h, NVJITLINK_INPUT_PTX, ptx.c_str(), ptx.size() + 1, "kz_shaders") != NVJITLINK_SUCCESS) {
     err = log("adding the shader PTX");
   } else if (nvJitLinkComplete(h) != NVJITLINK_SUCCESS) {

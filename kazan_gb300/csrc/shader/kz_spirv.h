@@ -52,7 +52,8 @@ enum Op : uint16_t {
   OpFOrdGreaterThan = 186, OpFUnordGreaterThan = 187, OpFOrdLessThanEqual = 188, OpFUnordLessThanEqual = 189,
   OpFOrdGreaterThanEqual = 190, OpFUnordGreaterThanEqual = 191, OpShiftRightLogical = 194,
   OpShiftRightArithmetic = 195, OpShiftLeftLogical = 196, OpBitwiseOr = 197, OpBitwiseXor = 198,
-  OpBitwiseAnd = 199, OpNot = 200, OpDPdx = 207, OpDPdy = 208, OpFwidth = 209, OpPhi = 245,
+  OpBitwiseAnd = 199, OpNot = 200, OpBitFieldInsert = 201, OpBitFieldSExtract = 202, OpBitFieldUExtract = 203,
+  OpBitReverse = 204, OpBitCount = 205, OpDPdx = 207, OpDPdy = 208, OpFwidth = 209, OpPhi = 245,
   OpLoopMerge = 246, OpSelectionMerge = 247, OpLabel = 248, OpBranch = 249, OpBranchConditional = 250,
   OpSwitch = 251, OpKill = 252, OpReturn = 253, OpReturnValue = 254, OpUnreachable = 255,
   OpModuleProcessed = 330
@@ -93,8 +94,11 @@ enum GLSLstd450 : uint32_t {
   GPow = 26, GExp = 27, GLog = 28, GExp2 = 29, GLog2 = 30, GSqrt = 31, GInverseSqrt = 32, GDeterminant = 33,
   GMatrixInverse = 34, GModf = 35, GModfStruct = 36, GFMin = 37, GUMin = 38, GSMin = 39, GFMax = 40,
   GUMax = 41, GSMax = 42, GFClamp = 43, GUClamp = 44, GSClamp = 45, GFMix = 46, GIMix = 47, GStep = 48,
-  GSmoothStep = 49, GFma = 50, GLength = 66, GDistance = 67, GCross = 68, GNormalize = 69, GFaceForward = 70,
-  GReflect = 71
+  GSmoothStep = 49, GFma = 50, GFrexp = 51, GFrexpStruct = 52, GLdexp = 53, GPackSnorm4x8 = 54,
+  GPackUnorm4x8 = 55, GPackSnorm2x16 = 56, GPackUnorm2x16 = 57, GPackHalf2x16 = 58, GUnpackSnorm2x16 = 60,
+  GUnpackUnorm2x16 = 61, GUnpackHalf2x16 = 62, GUnpackSnorm4x8 = 63, GUnpackUnorm4x8 = 64, GLength = 66,
+  GDistance = 67, GCross = 68, GNormalize = 69, GFaceForward = 70, GReflect = 71, GRefract = 72, GFindILsb = 73,
+  GFindSMsb = 74, GFindUMsb = 75, GNMin = 79, GNMax = 80, GNClamp = 81
 };
 
 struct Insn {

@@ -1072,6 +1072,56 @@ bool Translator::ext_inst(const Insn& in) {
   auto per2 = [&](Op op, Ty t) {
     for (uint32_t k = 0; k < n; k++) out.regs.push_back(op2(op, t, args[0]->regs[k], args[1]->regs[k]));
   };
+  /* scalar building blocks (each a separately rounded single operation) */
+  auto F = [&](float v) {
+    uint32_t b;
+    std::memcpy(&b, &v, 4);
+    return konst(Ty::F32, b);
+  };
+  auto I = [&](uint32_t v) { return konst(Ty::B32, v); };
+  auto add = [&](int32_t a, int32_t b) { return op2(Op::FAdd, Ty::F32, a, b); };
+  auto sub = [&](int32_t a, int32_t b) { return op2(Op::FSub, Ty::F32, a, b); };
+  auto mul = [&](int32_t a, int32_t b) { return op2(Op::FMul, Ty::F32, a, b); };
+  auto div = [&](int32_t a, int32_t b) { return op2(Op::FDiv, Ty::F32, a, b); };
+  auto fma = [&](int32_t a, int32_t b, int32_t c) { return op3(Op::FFma, Ty::F32, a, b, c); };
+  auto sel = [&](Ty t, int32_t p, int32_t a, int32_t b) { return op3(Op::Selp, t, a, b, p); };
+  auto fcmp = [&](int32_t a, int32_t b, uint32_t c) { return op2(Op::SetpF, Ty::Pred, a, b, c); };
+  auto scmp = [&](int32_t a, int32_t b, uint32_t c) { return op2(Op::SetpS, Ty::Pred, a, b, c); };
+  /* e^x = 2^(x log2 e) and ln x = log2 x ln 2, with the hardware exp2 / log2 approximations */
+  auto fexp = [&](int32_t x) { return op1(Op::FEx2, Ty::F32, mul(x, F(1.44269504f))); };
+  auto flog = [&](int32_t x) { return mul(op1(Op::FLg2, Ty::F32, x), F(0.693147181f)); };
+  /* arctangent: |x| reduced to [0, 1] by atan x = pi/2 - atan(1/x), then to [0, tan(pi/12)] by the addition
+   * formula atan a = pi/6 + atan((a sqrt3 - 1) / (a + sqrt3)); there the Taylor series
+   * t - t^3/3 + ... + t^13/13 (truncation below 3e-10 for t <= 0.268) in Horner form; the sign restored */
+  auto fatan = [&](int32_t x) {
+    int32_t a = op1(Op::FAbs, Ty::F32, x);
+    int32_t big = fcmp(a, F(1.0f), CmpGt);
+    a = sel(Ty::F32, big, div(F(1.0f), a), a);
+    int32_t red = fcmp(a, F(0.267949192f), CmpGt);
+    int32_t ar = div(sub(mul(a, F(1.73205081f)), F(1.0f)), add(a, F(1.73205081f)));
+    int32_t t = sel(Ty::F32, red, ar, a);
+    int32_t t2 = mul(t, t);
+    int32_t p = F(1.0f / 13.0f);
+    const float c[] = {-1.0f / 11.0f, 1.0f / 9.0f, -1.0f / 7.0f, 1.0f / 5.0f, -1.0f / 3.0f};
+    for (float ck : c) p = fma(p, t2, F(ck));
+    int32_t r = fma(mul(p, t2), t, t);
+    r = sel(Ty::F32, red, add(r, F(0.523598776f)), r);
+    r = sel(Ty::F32, big, sub(F(1.57079633f), r), r);
+    return sel(Ty::F32, fcmp(x, F(0.0f), CmpLt), op1(Op::FNeg, Ty::F32, r), r);
+  };
+  /* atan2(y, x): atan(y / x) moved to the quadrant of (x, y) */
+  auto fatan2 = [&](int32_t y, int32_t x) {
+    int32_t r = fatan(div(y, x));
+    int32_t neg_x = fcmp(x, F(0.0f), CmpLt);
+    int32_t pi = sel(Ty::F32, fcmp(y, F(0.0f), CmpLt), F(-3.14159265f), F(3.14159265f));
+    r = sel(Ty::F32, neg_x, add(r, pi), r);
+    int32_t zx = fcmp(x, F(0.0f), CmpEq);
+    int32_t half = sel(Ty::F32, fcmp(y, F(0.0f), CmpLt), F(-1.57079633f), F(1.57079633f));
+    return sel(Ty::F32, zx, sel(Ty::F32, fcmp(y, F(0.0f), CmpEq), F(0.0f), half), r);
+  };
+  auto det2 = [&](int32_t a, int32_t b, int32_t c, int32_t d) { /* a d - b c */
+    return fma(a, d, op1(Op::FNeg, Ty::F32, mul(b, c)));
+  };
   switch (num) {
     case GFAbs: if (!need(1)) return false; per(Op::FAbs); break;
     case GFloor: if (!need(1)) return false; per(Op::FFloor); break;
@@ -1164,6 +1214,302 @@ bool Translator::ext_inst(const Insn& in) {
       /* pow(x, y) = exp2(y * log2(x)) with the hardware approximations */
       for (uint32_t k = 0; k < n; k++)
         out.regs.push_back(op1(Op::FEx2, Ty::F32, op2(Op::FMul, Ty::F32, args[1]->regs[k], op1(Op::FLg2, Ty::F32, args[0]->regs[k]))));
+      break;
+    }
+    case GSAbs:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) {
+        int32_t x = args[0]->regs[k];
+        out.regs.push_back(sel(Ty::B32, scmp(x, I(0), CmpLt), op1(Op::INeg, Ty::B32, x), x));
+      }
+      break;
+    case GFSign:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) {
+        int32_t x = args[0]->regs[k];
+        out.regs.push_back(sel(Ty::F32, fcmp(x, F(0.0f), CmpGt), F(1.0f),
+                               sel(Ty::F32, fcmp(x, F(0.0f), CmpLt), F(-1.0f), F(0.0f))));
+      }
+      break;
+    case GSSign:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) {
+        int32_t x = args[0]->regs[k];
+        out.regs.push_back(sel(Ty::B32, scmp(x, I(0), CmpGt), I(1), sel(Ty::B32, scmp(x, I(0), CmpLt), I(~0u), I(0))));
+      }
+      break;
+    case GRadians:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) out.regs.push_back(mul(args[0]->regs[k], F(0.0174532925f)));
+      break;
+    case GDegrees:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) out.regs.push_back(mul(args[0]->regs[k], F(57.2957795f)));
+      break;
+    case GTan:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++)
+        out.regs.push_back(div(op1(Op::FSin, Ty::F32, args[0]->regs[k]), op1(Op::FCos, Ty::F32, args[0]->regs[k])));
+      break;
+    case GExp:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) out.regs.push_back(fexp(args[0]->regs[k]));
+      break;
+    case GLog:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) out.regs.push_back(flog(args[0]->regs[k]));
+      break;
+    case GSinh:
+    case GCosh:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) {
+        int32_t e = fexp(args[0]->regs[k]), ei = div(F(1.0f), e);
+        out.regs.push_back(mul(num == GSinh ? sub(e, ei) : add(e, ei), F(0.5f)));
+      }
+      break;
+    case GTanh:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) { /* (e^2x - 1) / (e^2x + 1), |x| clamped to 10 (tanh 10 rounds to 1) */
+        int32_t x = op2(Op::FMin, Ty::F32, op2(Op::FMax, Ty::F32, args[0]->regs[k], F(-10.0f)), F(10.0f));
+        int32_t e = fexp(add(x, x));
+        out.regs.push_back(div(sub(e, F(1.0f)), add(e, F(1.0f))));
+      }
+      break;
+    case GAsinh:
+    case GAcosh:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) {
+        int32_t x = args[0]->regs[k];
+        if (num == GAsinh) { /* sign(x) ln(|x| + sqrt(x^2 + 1)) */
+          int32_t a = op1(Op::FAbs, Ty::F32, x);
+          int32_t r = flog(add(a, op1(Op::FSqrt, Ty::F32, fma(a, a, F(1.0f)))));
+          out.regs.push_back(sel(Ty::F32, fcmp(x, F(0.0f), CmpLt), op1(Op::FNeg, Ty::F32, r), r));
+        } else { /* ln(x + sqrt(x^2 - 1)) */
+          out.regs.push_back(flog(add(x, op1(Op::FSqrt, Ty::F32, fma(x, x, F(-1.0f))))));
+        }
+      }
+      break;
+    case GAtanh:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) { /* ln((1 + x) / (1 - x)) / 2 */
+        int32_t x = args[0]->regs[k];
+        out.regs.push_back(mul(flog(div(add(F(1.0f), x), sub(F(1.0f), x))), F(0.5f)));
+      }
+      break;
+    case GAtan:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) out.regs.push_back(fatan(args[0]->regs[k]));
+      break;
+    case GAtan2:
+      if (!need(2)) return false;
+      for (uint32_t k = 0; k < n; k++) out.regs.push_back(fatan2(args[0]->regs[k], args[1]->regs[k]));
+      break;
+    case GAsin:
+    case GAcos:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) { /* asin x = atan2(x, sqrt(1 - x^2)), acos x = atan2(sqrt(1 - x^2), x) */
+        int32_t x = args[0]->regs[k];
+        int32_t c = op1(Op::FSqrt, Ty::F32, fma(op1(Op::FNeg, Ty::F32, x), x, F(1.0f)));
+        out.regs.push_back(num == GAsin ? fatan2(x, c) : fatan2(c, x));
+      }
+      break;
+    case GSClamp:
+    case GUClamp:
+      if (!need(3)) return false;
+      for (uint32_t k = 0; k < n; k++) {
+        Op cmp = num == GSClamp ? Op::SetpS : Op::SetpU;
+        int32_t x = args[0]->regs[k], lo = args[1]->regs[k], hi = args[2]->regs[k];
+        int32_t m = sel(Ty::B32, op2(cmp, Ty::Pred, x, lo, CmpLt), lo, x);
+        out.regs.push_back(sel(Ty::B32, op2(cmp, Ty::Pred, m, hi, CmpGt), hi, m));
+      }
+      break;
+    case GNMin: if (!need(2)) return false; per2(Op::FMin, Ty::F32); break;
+    case GNMax: if (!need(2)) return false; per2(Op::FMax, Ty::F32); break;
+    case GNClamp:
+      if (!need(3)) return false;
+      for (uint32_t k = 0; k < n; k++)
+        out.regs.push_back(op2(Op::FMin, Ty::F32, op2(Op::FMax, Ty::F32, args[0]->regs[k], args[1]->regs[k]),
+                               args[2]->regs[k]));
+      break;
+    case GSmoothStep:
+      if (!need(3)) return false;
+      for (uint32_t k = 0; k < n; k++) { /* t = clamp((x - e0) / (e1 - e0), 0, 1); t t (3 - 2 t) */
+        int32_t e0 = args[0]->regs[k], e1 = args[1]->regs[k], x = args[2]->regs[k];
+        int32_t t = div(sub(x, e0), sub(e1, e0));
+        t = op2(Op::FMin, Ty::F32, op2(Op::FMax, Ty::F32, t, F(0.0f)), F(1.0f));
+        out.regs.push_back(mul(mul(t, t), fma(F(-2.0f), t, F(3.0f))));
+      }
+      break;
+    case GFaceForward: {
+      if (!need(3)) return false; /* dot(Nref, I) < 0 ? N : -N */
+      size_t m = args[0]->regs.size();
+      int32_t p = fcmp(dot(args[2]->regs, args[1]->regs, m), F(0.0f), CmpLt);
+      for (size_t k = 0; k < m; k++)
+        out.regs.push_back(sel(Ty::F32, p, args[0]->regs[k], op1(Op::FNeg, Ty::F32, args[0]->regs[k])));
+      break;
+    }
+    case GReflect: {
+      if (!need(2)) return false; /* I - 2 dot(N, I) N */
+      size_t m = args[0]->regs.size();
+      int32_t d2 = mul(F(2.0f), dot(args[1]->regs, args[0]->regs, m));
+      for (size_t k = 0; k < m; k++)
+        out.regs.push_back(fma(op1(Op::FNeg, Ty::F32, d2), args[1]->regs[k], args[0]->regs[k]));
+      break;
+    }
+    case GRefract: {
+      if (!need(3)) return false; /* k = 1 - eta^2 (1 - dot(N, I)^2); k < 0 ? 0 : eta I - (eta dot(N, I) + sqrt k) N */
+      size_t m = args[0]->regs.size();
+      int32_t eta = args[2]->regs[0];
+      int32_t d = dot(args[1]->regs, args[0]->regs, m);
+      int32_t kk = sub(F(1.0f), mul(mul(eta, eta), fma(op1(Op::FNeg, Ty::F32, d), d, F(1.0f))));
+      int32_t neg = fcmp(kk, F(0.0f), CmpLt);
+      int32_t f = fma(eta, d, op1(Op::FSqrt, Ty::F32, kk));
+      for (size_t k = 0; k < m; k++) {
+        int32_t r = fma(eta, args[0]->regs[k], op1(Op::FNeg, Ty::F32, mul(f, args[1]->regs[k])));
+        out.regs.push_back(sel(Ty::F32, neg, F(0.0f), r));
+      }
+      break;
+    }
+    case GLdexp:
+      if (!need(2)) return false;
+      for (uint32_t k = 0; k < n; k++) { /* x 2^e as two exact power-of-two products, e clamped to [-252, 254] */
+        int32_t e = args[1]->regs[k];
+        e = sel(Ty::B32, scmp(e, I((uint32_t)-252), CmpLt), I((uint32_t)-252), e);
+        e = sel(Ty::B32, scmp(e, I(254), CmpGt), I(254), e);
+        int32_t e1 = op2(Op::Sar, Ty::B32, e, I(1)), e2 = op2(Op::ISub, Ty::B32, e, e1);
+        int32_t p1 = op2(Op::Shl, Ty::B32, op2(Op::IAdd, Ty::B32, e1, I(127)), I(23));
+        int32_t p2 = op2(Op::Shl, Ty::B32, op2(Op::IAdd, Ty::B32, e2, I(127)), I(23));
+        out.regs.push_back(mul(mul(args[0]->regs[k], p1), p2));
+      }
+      break;
+    case GFindILsb:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) { /* x == 0 ? -1 : popc((x & -x) - 1) */
+        int32_t x = args[0]->regs[k];
+        int32_t low = op2(Op::And, Ty::B32, x, op1(Op::INeg, Ty::B32, x));
+        int32_t r = op1(Op::Popc, Ty::B32, op2(Op::ISub, Ty::B32, low, I(1)));
+        out.regs.push_back(sel(Ty::B32, op2(Op::SetpU, Ty::Pred, x, I(0), CmpEq), I(~0u), r));
+      }
+      break;
+    case GFindUMsb:
+    case GFindSMsb:
+      if (!need(1)) return false;
+      for (uint32_t k = 0; k < n; k++) { /* 31 - clz(x) (for signed: of ~x when x < 0); -1 when no bit */
+        int32_t x = args[0]->regs[k];
+        if (num == GFindSMsb) x = sel(Ty::B32, scmp(x, I(0), CmpLt), op1(Op::Not, Ty::B32, x), x);
+        out.regs.push_back(op2(Op::ISub, Ty::B32, I(31), op1(Op::Clz, Ty::B32, x)));
+      }
+      break;
+    case GPackUnorm4x8:
+    case GPackSnorm4x8: {
+      if (!need(1)) return false; /* rint(clamp(c) * 255 or 127), bytes from component 0 up */
+      bool sn = num == GPackSnorm4x8;
+      int32_t acc = I(0);
+      for (int k = 0; k < 4; k++) {
+        int32_t c = op2(Op::FMin, Ty::F32, op2(Op::FMax, Ty::F32, args[0]->regs[k], F(sn ? -1.0f : 0.0f)), F(1.0f));
+        int32_t q = op1(Op::CvtF2S, Ty::B32, op1(Op::FRoundEven, Ty::F32, mul(c, F(sn ? 127.0f : 255.0f))));
+        acc = op2(Op::Or, Ty::B32, acc, op2(Op::Shl, Ty::B32, op2(Op::And, Ty::B32, q, I(0xFF)), I(8 * k)));
+      }
+      out.regs.push_back(acc);
+      break;
+    }
+    case GUnpackUnorm4x8:
+    case GUnpackSnorm4x8: {
+      if (!need(1)) return false; /* byte / 255, or clamp(signed byte / 127, -1, 1) */
+      bool sn = num == GUnpackSnorm4x8;
+      for (int k = 0; k < 4; k++) {
+        Inst b;
+        b.op = Op::Bfe;
+        b.ty = Ty::B32;
+        b.dst = fn_.reg(Ty::B32);
+        b.a = args[0]->regs[0];
+        b.b = I(8 * k);
+        b.c = I(8);
+        b.imm = sn ? 1 : 0;
+        fn_.emit(b);
+        int32_t f = op1(sn ? Op::CvtS2F : Op::CvtU2F, Ty::F32, b.dst);
+        f = div(f, F(sn ? 127.0f : 255.0f));
+        if (sn) f = op2(Op::FMax, Ty::F32, f, F(-1.0f));
+        out.regs.push_back(f);
+      }
+      break;
+    }
+    case GPackHalf2x16:
+      if (!need(1)) return false;
+      out.regs.push_back(op2(Op::Or, Ty::B32, op1(Op::F2H, Ty::B32, args[0]->regs[0]),
+                             op2(Op::Shl, Ty::B32, op1(Op::F2H, Ty::B32, args[0]->regs[1]), I(16))));
+      break;
+    case GUnpackHalf2x16:
+      if (!need(1)) return false;
+      out.regs.push_back(op1(Op::H2F, Ty::F32, op2(Op::And, Ty::B32, args[0]->regs[0], I(0xFFFF))));
+      out.regs.push_back(op1(Op::H2F, Ty::F32, op2(Op::Shr, Ty::B32, args[0]->regs[0], I(16))));
+      break;
+    case GModfStruct:
+      if (!need(1)) return false; /* { x - trunc(x), trunc(x) } */
+      for (uint32_t k = 0; k < args[0]->regs.size(); k++)
+        out.regs.push_back(sub(args[0]->regs[k], op1(Op::FTrunc, Ty::F32, args[0]->regs[k])));
+      for (uint32_t k = 0; k < args[0]->regs.size(); k++) out.regs.push_back(op1(Op::FTrunc, Ty::F32, args[0]->regs[k]));
+      break;
+    case GDeterminant: {
+      if (!need(1)) return false;
+      const auto& a = args[0]->regs; /* column-major: element (row r, column c) at c * N + r */
+      size_t N = a.size() == 4 ? 2 : a.size() == 9 ? 3 : 4;
+      auto at = [&](size_t r, size_t c) { return a[c * N + r]; };
+      if (N == 2) {
+        out.regs.push_back(det2(at(0, 0), at(0, 1), at(1, 0), at(1, 1)));
+      } else if (N == 3) { /* expansion along row 0 */
+        int32_t c0 = det2(at(1, 1), at(1, 2), at(2, 1), at(2, 2));
+        int32_t c1 = det2(at(1, 0), at(1, 2), at(2, 0), at(2, 2));
+        int32_t c2 = det2(at(1, 0), at(1, 1), at(2, 0), at(2, 1));
+        out.regs.push_back(fma(at(0, 2), c2, fma(op1(Op::FNeg, Ty::F32, at(0, 1)), c1, mul(at(0, 0), c0))));
+      } else { /* Laplace expansion by the 2x2 minors of rows 0-1 and 2-3 */
+        int32_t s[6], c[6];
+        const int pr[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+        for (int k = 0; k < 6; k++) {
+          s[k] = det2(at(0, pr[k][0]), at(0, pr[k][1]), at(1, pr[k][0]), at(1, pr[k][1]));
+          c[k] = det2(at(2, pr[k][0]), at(2, pr[k][1]), at(3, pr[k][0]), at(3, pr[k][1]));
+        }
+        int32_t d = mul(s[0], c[5]);
+        d = fma(op1(Op::FNeg, Ty::F32, s[1]), c[4], d);
+        d = fma(s[2], c[3], d);
+        d = fma(s[3], c[2], d);
+        d = fma(op1(Op::FNeg, Ty::F32, s[4]), c[1], d);
+        d = fma(s[5], c[0], d);
+        out.regs.push_back(d);
+      }
+      break;
+    }
+    case GMatrixInverse: {
+      if (!need(1)) return false;
+      const auto& a = args[0]->regs;
+      size_t N = a.size() == 4 ? 2 : a.size() == 9 ? 3 : 4;
+      auto at = [&](size_t r, size_t c) { return a[c * N + r]; };
+      /* the adjugate divided by the determinant: cofactor C(r, c) = (-1)^(r+c) minor(r, c); inverse(c, r) = C / det */
+      auto minor = [&](size_t r, size_t c) -> int32_t {
+        std::vector<size_t> rs, cs;
+        for (size_t i = 0; i < N; i++) {
+          if (i != r) rs.push_back(i);
+          if (i != c) cs.push_back(i);
+        }
+        if (N == 2) return at(rs[0], cs[0]);
+        if (N == 3) return det2(at(rs[0], cs[0]), at(rs[0], cs[1]), at(rs[1], cs[0]), at(rs[1], cs[1]));
+        int32_t c0 = det2(at(rs[1], cs[1]), at(rs[1], cs[2]), at(rs[2], cs[1]), at(rs[2], cs[2]));
+        int32_t c1 = det2(at(rs[1], cs[0]), at(rs[1], cs[2]), at(rs[2], cs[0]), at(rs[2], cs[2]));
+        int32_t c2 = det2(at(rs[1], cs[0]), at(rs[1], cs[1]), at(rs[2], cs[0]), at(rs[2], cs[1]));
+        return fma(at(rs[0], cs[2]), c2, fma(op1(Op::FNeg, Ty::F32, at(rs[0], cs[1])), c1, mul(at(rs[0], cs[0]), c0)));
+      };
+      std::vector<int32_t> cof(N * N);
+      for (size_t r = 0; r < N; r++)
+        for (size_t c = 0; c < N; c++) {
+          int32_t m = minor(r, c);
+          cof[r * N + c] = ((r + c) & 1) ? op1(Op::FNeg, Ty::F32, m) : m;
+        }
+      int32_t det = mul(at(0, 0), cof[0]);
+      for (size_t c = 1; c < N; c++) det = fma(at(0, c), cof[c], det);
+      int32_t inv = div(F(1.0f), det);
+      out.regs.assign(N * N, -1);
+      for (size_t r = 0; r < N; r++)
+        for (size_t c = 0; c < N; c++) out.regs[r * N + c] = mul(cof[r * N + c], inv); /* inverse(c, r), column r */
       break;
     }
     default: return fail("unsupported GLSL.std.450 instruction " + std::to_string(num));
@@ -1488,6 +1834,134 @@ bool Translator::do_insn(const Insn& in) {
       Val r;
       r.type = o[0];
       for (int32_t x : a->regs) r.regs.push_back(op2(Op::SetpF, Ty::Pred, x, x, CmpNe | CmpUnordered));
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpIsInf: { /* |x| == +inf */
+      Val* a = val(o[2]);
+      if (!a) return false;
+      Val r;
+      r.type = o[0];
+      for (int32_t x : a->regs)
+        r.regs.push_back(op2(Op::SetpF, Ty::Pred, op1(Op::FAbs, Ty::F32, x), konst(Ty::F32, 0x7F800000u), CmpEq));
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpAny:
+    case OpAll: { /* OR / AND of a boolean vector */
+      Val* a = val(o[2]);
+      if (!a || a->regs.empty()) return false;
+      int32_t acc = a->regs[0];
+      for (size_t k = 1; k < a->regs.size(); k++)
+        acc = op2(in.opcode == OpAny ? Op::POr : Op::PAnd, Ty::Pred, acc, a->regs[k]);
+      Val r;
+      r.type = o[0];
+      r.regs.push_back(acc);
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpFMod:
+    case OpFRem: { /* x - y floor(x / y) (sign of y), or x - y trunc(x / y) (sign of x) */
+      Val* a = val(o[2]);
+      Val* b = val(o[3]);
+      if (!a || !b) return false;
+      Val r;
+      r.type = o[0];
+      for (size_t k = 0; k < a->regs.size() && k < b->regs.size(); k++) {
+        int32_t q = op2(Op::FDiv, Ty::F32, a->regs[k], b->regs[k]);
+        q = op1(in.opcode == OpFMod ? Op::FFloor : Op::FTrunc, Ty::F32, q);
+        r.regs.push_back(op3(Op::FFma, Ty::F32, op1(Op::FNeg, Ty::F32, b->regs[k]), q, a->regs[k]));
+      }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpSMod: { /* remainder with the sign of the divisor: srem, plus the divisor when the signs differ */
+      Val* a = val(o[2]);
+      Val* b = val(o[3]);
+      if (!a || !b) return false;
+      Val r;
+      r.type = o[0];
+      for (size_t k = 0; k < a->regs.size() && k < b->regs.size(); k++) {
+        int32_t rem = op2(Op::SRem, Ty::B32, a->regs[k], b->regs[k]);
+        int32_t nz = op2(Op::SetpS, Ty::Pred, rem, konst(Ty::B32, 0), CmpNe);
+        int32_t diff = op2(Op::SetpS, Ty::Pred, op2(Op::Xor, Ty::B32, rem, b->regs[k]), konst(Ty::B32, 0), CmpLt);
+        int32_t fix = op2(Op::PAnd, Ty::Pred, nz, diff);
+        r.regs.push_back(op3(Op::Selp, Ty::B32, op2(Op::IAdd, Ty::B32, rem, b->regs[k]), rem, fix));
+      }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpBitCount:
+    case OpBitReverse: {
+      Val* a = val(o[2]);
+      if (!a) return false;
+      Val r;
+      r.type = o[0];
+      for (int32_t x : a->regs) r.regs.push_back(op1(in.opcode == OpBitCount ? Op::Popc : Op::Brev, Ty::B32, x));
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpBitFieldSExtract:
+    case OpBitFieldUExtract: { /* bits [offset, offset + count) of each component */
+      Val* a = val(o[2]);
+      Val* off = val(o[3]);
+      Val* cnt = val(o[4]);
+      if (!a || !off || !cnt) return false;
+      Val r;
+      r.type = o[0];
+      for (int32_t x : a->regs) {
+        Inst i;
+        i.op = Op::Bfe;
+        i.ty = Ty::B32;
+        i.dst = fn_.reg(Ty::B32);
+        i.a = x;
+        i.b = off->regs[0];
+        i.c = cnt->regs[0];
+        i.imm = in.opcode == OpBitFieldSExtract ? 1u : 0u;
+        fn_.emit(i);
+        r.regs.push_back(i.dst);
+      }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpBitFieldInsert: { /* mask = ((1 << count) - 1) << offset; (base & ~mask) | ((insert << offset) & mask) */
+      Val* base = val(o[2]);
+      Val* ins = val(o[3]);
+      Val* off = val(o[4]);
+      Val* cnt = val(o[5]);
+      if (!base || !ins || !off || !cnt) return false;
+      int32_t ones = op2(Op::Shl, Ty::B32, konst(Ty::B32, 1), cnt->regs[0]); /* count 32: the shift gives 0 */
+      int32_t mask = op2(Op::Shl, Ty::B32, op2(Op::ISub, Ty::B32, ones, konst(Ty::B32, 1)), off->regs[0]);
+      Val r;
+      r.type = o[0];
+      for (size_t k = 0; k < base->regs.size() && k < ins->regs.size(); k++) {
+        int32_t keep = op2(Op::And, Ty::B32, base->regs[k], op1(Op::Not, Ty::B32, mask));
+        int32_t put = op2(Op::And, Ty::B32, op2(Op::Shl, Ty::B32, ins->regs[k], off->regs[0]), mask);
+        r.regs.push_back(op2(Op::Or, Ty::B32, keep, put));
+      }
+      vals_[o[1]] = r;
+      return true;
+    }
+    case OpDPdx:
+    case OpDPdy:
+    case OpFwidth:
+      return fail("derivatives (dFdx, dFdy, fwidth) are not supported: fragments are shaded one at a time");
+    case OpImageQuerySize:
+    case OpImageQuerySizeLod: { /* textureSize: (width, height) of the image */
+      Val* img = val(o[2]);
+      if (!img || !img->is_tex) return fail("textureSize of something that is not a combined image sampler");
+      Inst i;
+      i.op = Op::TexSize;
+      i.ty = Ty::B32;
+      i.dst = fn_.reg(Ty::B32);
+      fn_.reg(Ty::B32);
+      i.c = img->tex_dyn ? img->regs[0] : -1;
+      i.imm = img->tex_dyn ? 0u : img->tex_elem;
+      i.imm2 = img->tex_key;
+      fn_.emit(i);
+      Val r;
+      r.type = o[0];
+      r.regs = {i.dst, i.dst + 1};
       vals_[o[1]] = r;
       return true;
     }
@@ -1867,6 +2341,7 @@ std::vector<uint32_t> live_inputs(const Function& fn, uint32_t out_lo, uint32_t 
       bool live_dst = i.dst >= 0 && live[(size_t)i.dst];
       if ((i.op == Op::Tex || i.op == Op::TexFetch) && i.dst >= 0)
         for (int k = 1; k < 4; k++) live_dst |= live[(size_t)i.dst + k] != 0;
+      if (i.op == Op::TexSize && i.dst >= 0) live_dst |= live[(size_t)i.dst + 1] != 0;
       if (root || live_dst) {
         mark(i.a);
         mark(i.b);
