@@ -18,6 +18,13 @@
  *   Normalize(x)              x * (1 / sqrt(dot(x, x)))   (sqrt and divide correctly rounded)
  *   Length(x)                 sqrt(dot(x, x))
  *   FMix(x, y, a)             fma(a, y - x, x)
+ *   FMod / FRem(x, y)         fma(-y, floor / trunc(x / y), x)
+ *   Reflect(I, N)             fma(-(2 dot(N, I)), N, I)
+ *   Determinant / Inverse     2x2 minors a d - b c as fma(a, d, -(b c)); cofactor expansion along row 0
+ *   Exp, Log                  exp2(x log2 e), log2(x) ln 2 (hardware approximations)
+ *   Atan                      |x| reduced to [0, tan(pi/12)] (reciprocal, then the addition formula for
+ *                             pi/6), Taylor series to t^13; Asin / Acos / Atan2 through it
+ * Derivatives (dFdx, dFdy, fwidth) are refused: fragments are shaded one at a time, not in quads.
  */
 #include <cstring>
 #include <map>
