@@ -734,12 +734,26 @@ void VKAPI_CALL kzCmdPipelineBarrier(VkCommandBuffer, VkPipelineStageFlags, VkPi
   /* api_impl.rs:4863: every command executes in order on one stream, so barriers order nothing new */
 }
 
+/* A transfer region must lie inside memory the object has bound; a region that does not is a recording
+   error (the command buffer's vkEndCommandBuffer fails), so no copy or fill ever leaves its object. */
+static bool buffer_range_ok(const Buffer* b, VkDeviceSize off, VkDeviceSize size) {
+  return b && b->mem && off <= b->size && size <= b->size - off;
+}
+
+static bool image_rect_ok(const Image* img, int32_t x, int32_t y, uint32_t w, uint32_t h) {
+  return img && img->mem && x >= 0 && y >= 0 && (uint64_t)x + w <= img->width && (uint64_t)y + h <= img->height;
+}
+
 void VKAPI_CALL kzCmdCopyBuffer(VkCommandBuffer cbh, VkBuffer src, VkBuffer dst, uint32_t n, const VkBufferCopy* r) {
   /* api_impl.rs:4696 */
   CommandBuffer* cb = H<CommandBuffer>(cbh);
   Buffer* s = H<Buffer>(src);
   Buffer* d = H<Buffer>(dst);
   for (uint32_t i = 0; i < n; i++) {
+    if (!buffer_range_ok(s, r[i].srcOffset, r[i].size) || !buffer_range_ok(d, r[i].dstOffset, r[i].size)) {
+      cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+      return;
+    }
     RecOp op;
     op.kind = OpKind::Copy;
     op.src = s->ptr() + r[i].srcOffset;
@@ -752,10 +766,24 @@ void VKAPI_CALL kzCmdCopyBuffer(VkCommandBuffer cbh, VkBuffer src, VkBuffer dst,
 }
 
 static void image_buffer_copy(CommandBuffer* cb, Image* img, Buffer* buf, const VkBufferImageCopy& r, bool to_buffer) {
+  /* one-sample images only; the buffer's rows are bufferRowLength texels apart (the extent's width if 0) */
+  uint32_t row_len = r.bufferRowLength ? r.bufferRowLength : r.imageExtent.width;
+  if (!img || img->samples != 1 || row_len < r.imageExtent.width ||
+      !image_rect_ok(img, r.imageOffset.x, r.imageOffset.y, r.imageExtent.width, r.imageExtent.height)) {
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
+  size_t bpitch = (size_t)row_len * img->bpp;
+  VkDeviceSize span = r.imageExtent.height == 0 || r.imageExtent.width == 0
+                          ? 0
+                          : (VkDeviceSize)bpitch * (r.imageExtent.height - 1) + (VkDeviceSize)r.imageExtent.width * img->bpp;
+  if (!buffer_range_ok(buf, r.bufferOffset, span)) {
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
+  if (span == 0) return;
   RecOp op;
   op.kind = OpKind::Copy2D;
-  uint32_t row_len = r.bufferRowLength ? r.bufferRowLength : r.imageExtent.width;
-  size_t bpitch = (size_t)row_len * img->bpp;
   char* ip = img->ptr() + (size_t)r.imageOffset.y * img->pitch + (size_t)r.imageOffset.x * img->bpp;
   char* bp = buf->ptr() + r.bufferOffset;
   op.width_bytes = (size_t)r.imageExtent.width * img->bpp;
@@ -829,6 +857,10 @@ void VKAPI_CALL kzCmdCopyImage(VkCommandBuffer cbh, VkImage srcImage, VkImageLay
   CommandBuffer* cb = H<CommandBuffer>(cbh);
   Image* s = H<Image>(srcImage);
   Image* d = H<Image>(dstImage);
+  if (!s || !d || !s->mem || !d->mem) {
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
   if (s->bpp != d->bpp || s->samples != d->samples) {
     cb->record_error = VK_ERROR_FORMAT_NOT_SUPPORTED;
     return;
@@ -859,7 +891,12 @@ void VKAPI_CALL kzCmdFillBuffer(VkCommandBuffer cbh, VkBuffer buffer, VkDeviceSi
                                 uint32_t data) {
   CommandBuffer* cb = H<CommandBuffer>(cbh);
   Buffer* b = H<Buffer>(buffer);
-  if (size == VK_WHOLE_SIZE) size = (b->size - off) & ~(VkDeviceSize)3;
+  if (b && off <= b->size && size == VK_WHOLE_SIZE) size = (b->size - off) & ~(VkDeviceSize)3;
+  if (!buffer_range_ok(b, off, size) || (off & 3) || (size & 3) || size / 4 > (VkDeviceSize)INT32_MAX) {
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
+  if (size == 0) return;
   RecOp op;
   op.kind = OpKind::Fill;
   op.base = b->ptr() + off;

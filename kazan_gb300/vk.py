@@ -686,6 +686,7 @@ _PROTOS = {
     "vkCmdCopyBuffer": (None, [H, H, H, c_uint32, P(VkBufferCopy)]),
     "vkCmdCopyImageToBuffer": (None, [H, H, c_int, H, c_uint32, P(VkBufferImageCopy)]),
     "vkCmdCopyBufferToImage": (None, [H, H, H, c_int, c_uint32, P(VkBufferImageCopy)]),
+    "vkCmdFillBuffer": (None, [H, H, c_uint64, c_uint64, c_uint32]),
     "vkCreateFence": (c_int, [H, P(VkFenceCreateInfo), c_void_p, P(H)]),
     "vkDestroyFence": (None, [H, H, c_void_p]),
     "vkResetFences": (c_int, [H, c_uint32, P(H)]),

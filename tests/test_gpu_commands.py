@@ -178,3 +178,74 @@ def test_dynamic_stencil_reference_and_masks(renderer):
     assert np.array_equal(color, col)
     assert np.array_equal(depth, kz_oracle.packed_depth(dep, sten, "d24s8"))
     assert len(np.unique(depth >> 24)) >= 3
+
+
+def _region(buf_off, row_len, x, y, w, h):
+    return vk.VkBufferImageCopy(buf_off, row_len, 0, vk.VkImageSubresourceLayers(vk.IMAGE_ASPECT_COLOR, 0, 0, 1),
+                                vk.VkOffset3D(x, y, 0), vk.VkExtent3D(w, h, 1))
+
+
+@pytest.mark.gpu
+def test_fill_and_buffer_image_copies(renderer):
+    """vkCmdFillBuffer at an unaligned word offset, vkCmdCopyBufferToImage with and without bufferRowLength and
+    vkCmdCopyImageToBuffer at a buffer offset, in one command buffer, against the same steps in numpy"""
+    W, H = 64, 48
+    rng = np.random.default_rng(11)
+    raw = rng.integers(0, 256, W * H * 4 + 4096, dtype=np.uint8)
+    src = renderer.create_buffer(raw.size, 0, True)
+    renderer.write_buffer(src, raw)
+    img = renderer.create_image(W, H, vk.FORMAT_R8G8B8A8_UNORM, vk.IMAGE_USAGE_TRANSFER_DST, False)
+    out_w, out_h, out_off = W - 6, H - 9, 64
+    dst = renderer.create_buffer(out_off + out_w * out_h * 4, 0, True)
+    fill_off, word = W * H * 4 + 4, 0xA5C30F11
+    d = renderer.drv
+    cb = renderer.begin()
+    d.vkCmdFillBuffer(cb, src.handle, fill_off, 16 * 16 * 4, word)
+    regions = [_region(0, 0, 0, 0, W, H),                 # the whole image, tight rows
+               _region(fill_off, 16, 5, 7, 16, 16),       # the filled words
+               _region(12, 50, 30, 20, 20, 10)]           # rows 50 texels apart in the buffer
+    for reg in regions:
+        d.vkCmdCopyBufferToImage(cb, src.handle, img.handle, vk.IMAGE_LAYOUT_GENERAL, 1, byref(reg))
+    back = _region(out_off, 0, 2, 3, out_w, out_h)
+    d.vkCmdCopyImageToBuffer(cb, img.handle, vk.IMAGE_LAYOUT_GENERAL, dst.handle, 1, byref(back))
+    renderer.end_submit_wait(cb)
+    renderer.free_command_buffer(cb)
+
+    model = raw[:W * H * 4].reshape(H, W, 4).copy()
+    model[7:23, 5:21] = np.frombuffer(np.full(256, word, dtype="<u4").tobytes(), np.uint8).reshape(16, 16, 4)
+    rows = raw[12:12 + 50 * 4 * 10].reshape(10, 200)[:, :80]
+    model[20:30, 30:50] = rows.reshape(10, 20, 4)
+    p = renderer.map(dst)
+    got = np.ctypeslib.as_array((ctypes.c_uint8 * (out_w * out_h * 4)).from_address(p + out_off)).copy()
+    renderer.unmap(dst)
+    assert np.array_equal(got.reshape(out_h, out_w, 4), model[3:3 + out_h, 2:2 + out_w])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["copy_past_end", "fill_past_end", "fill_unaligned", "image_region_outside",
+                                  "buffer_too_small", "row_length_short"])
+def test_transfer_regions_outside_their_objects_are_recording_errors(renderer, case):
+    """a region that leaves its buffer or image fails vkEndCommandBuffer; nothing of it reaches the device"""
+    a = renderer.create_buffer(4096, 0, True)
+    b = renderer.create_buffer(1024, 0, True)
+    img = renderer.create_image(32, 16, vk.FORMAT_R8G8B8A8_UNORM, vk.IMAGE_USAGE_TRANSFER_DST, False)
+    d = renderer.drv
+    cb = renderer.begin()
+    if case == "copy_past_end":
+        reg = vk.VkBufferCopy(0, 512, 1024)
+        d.vkCmdCopyBuffer(cb, a.handle, b.handle, 1, byref(reg))
+    elif case == "fill_past_end":
+        d.vkCmdFillBuffer(cb, b.handle, 1020, 8, 0)
+    elif case == "fill_unaligned":
+        d.vkCmdFillBuffer(cb, b.handle, 2, 8, 0)
+    elif case == "image_region_outside":
+        reg = _region(0, 0, 20, 0, 16, 4)
+        d.vkCmdCopyBufferToImage(cb, a.handle, img.handle, vk.IMAGE_LAYOUT_GENERAL, 1, byref(reg))
+    elif case == "buffer_too_small":
+        reg = _region(0, 0, 0, 0, 32, 16)
+        d.vkCmdCopyImageToBuffer(cb, img.handle, vk.IMAGE_LAYOUT_GENERAL, b.handle, 1, byref(reg))
+    else:
+        reg = _region(0, 8, 0, 0, 16, 4)
+        d.vkCmdCopyBufferToImage(cb, a.handle, img.handle, vk.IMAGE_LAYOUT_GENERAL, 1, byref(reg))
+    assert d.vkEndCommandBuffer(cb) == vk.VK_ERROR_INITIALIZATION_FAILED
+    renderer.free_command_buffer(cb)
