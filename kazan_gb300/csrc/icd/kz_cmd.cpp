@@ -196,6 +196,8 @@ static bool begin_draw(CommandBuffer* cb, bool indexed, DrawRec& dr, int& nreads
   return true;
 }
 
+static uint32_t fetch_limit(const CommandBuffer* cb, const KzPipe& kp, bool per_instance);
+
 static void record_draw(CommandBuffer* cb, uint32_t tri_count, uint32_t instances, uint32_t first_instance, bool indexed,
                         uint32_t first_index, int32_t vertex_offset) {
   if (!draw_state_ok(cb) || cb->pipe->rasterizer_discard || tri_count == 0 || instances == 0) return;
@@ -203,6 +205,18 @@ static void record_draw(CommandBuffer* cb, uint32_t tri_count, uint32_t instance
   int nreads = 0;
   if (!begin_draw(cb, indexed, dr, nreads)) return;
   KzDraw& d = dr.d;
+  /* the draw's elements and instances must lie in the bound buffers, as kz_k_indirect checks for indirect
+   * commands; a draw outside them is skipped, so no fetch leaves a buffer */
+  const KzPipe& kp = cb->pipe->pipe;
+  uint64_t elems = indexed ? (cb->ib_off < cb->ib->size ? (cb->ib->size - cb->ib_off) / (d.indexed == 1 ? 4u : 2u) : 0)
+                           : fetch_limit(cb, kp, false);
+  uint64_t first_elem = indexed ? first_index : (uint64_t)(uint32_t)vertex_offset;
+  if (first_elem + 3ull * tri_count > elems || (uint64_t)first_instance + instances > fetch_limit(cb, kp, true)) {
+    log_error("draw skipped: elements [%llu, %llu) or instances [%u, %llu) outside the bound buffers",
+              (unsigned long long)first_elem, (unsigned long long)(first_elem + 3ull * tri_count), first_instance,
+              (unsigned long long)first_instance + instances);
+    return;
+  }
   if (indexed) d.ib = d.ib_base + (uint64_t)first_index * (d.indexed == 1 ? 4u : 2u);
   d.vertex_offset = vertex_offset;
   d.first_instance = first_instance;

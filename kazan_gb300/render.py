@@ -361,8 +361,9 @@ class Renderer:
         self._objects.append(("PipelineLayout", h))
         return h
 
-    def pipeline(self, scene, rp, layout, vs_words, fs_words, dynamic=()):
-        """`dynamic`: VkDynamicState values the pipeline leaves to the command buffer"""
+    def pipeline(self, scene, rp, layout, vs_words, fs_words, dynamic=(), instance_attr=None):
+        """`dynamic`: VkDynamicState values the pipeline leaves to the command buffer; `instance_attr`:
+        (location, format, stride) of an attribute read per instance from vertex binding 1"""
         vsm, fsm = self.shader_module(vs_words), self.shader_module(fs_words)
         stages = (vk.VkPipelineShaderStageCreateInfo * 2)()
         stages[0] = vk.VkPipelineShaderStageCreateInfo(vk.ST_PIPELINE_SHADER_STAGE_CREATE_INFO, None, 0,
@@ -381,8 +382,16 @@ class Renderer:
         else:
             attrs[0] = vk.VkVertexInputAttributeDescription(0, 0, vk.FORMAT_R32G32B32_SFLOAT, 0)
             attrs[1] = vk.VkVertexInputAttributeDescription(1, 0, vk.FORMAT_R32G32B32_SFLOAT, 12)
-        vis = vk.VkPipelineVertexInputStateCreateInfo(vk.ST_PIPELINE_VERTEX_INPUT_STATE_CREATE_INFO, None, 0, 1,
-                                                      pointer(binding), 2, attrs)
+        nb, na = 1, 2
+        if instance_attr is not None:
+            loc, fmt, istride = instance_attr
+            bindings = (vk.VkVertexInputBindingDescription * 2)(
+                binding, vk.VkVertexInputBindingDescription(1, istride, vk.VERTEX_INPUT_RATE_INSTANCE))
+            attrs3 = (vk.VkVertexInputAttributeDescription * 3)(
+                attrs[0], attrs[1], vk.VkVertexInputAttributeDescription(loc, 1, fmt, 0))
+            binding, attrs, nb, na = bindings, attrs3, 2, 3
+        vis = vk.VkPipelineVertexInputStateCreateInfo(vk.ST_PIPELINE_VERTEX_INPUT_STATE_CREATE_INFO, None, 0, nb,
+                                                      binding if nb > 1 else pointer(binding), na, attrs)
         ias = vk.VkPipelineInputAssemblyStateCreateInfo(vk.ST_PIPELINE_INPUT_ASSEMBLY_STATE_CREATE_INFO, None, 0,
                                                         vk.TOPOLOGY_TRIANGLE_LIST, 0)
         vp = vk.VkViewport(0.0, 0.0, float(scene.width), float(scene.height), 0.0, 1.0)

@@ -131,6 +131,7 @@ COMMAND_BUFFER_LEVEL_PRIMARY = 0
 INDEX_TYPE_UINT16, INDEX_TYPE_UINT32 = 0, 1
 SUBPASS_CONTENTS_INLINE = 0
 VERTEX_INPUT_RATE_VERTEX = 0
+VERTEX_INPUT_RATE_INSTANCE = 1
 FENCE_CREATE_SIGNALED = 0x1
 SAMPLE_COUNT_1 = 0x1
 ATTACHMENT_UNUSED = 0xFFFFFFFF

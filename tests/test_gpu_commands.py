@@ -249,3 +249,204 @@ def test_transfer_regions_outside_their_objects_are_recording_errors(renderer, c
         d.vkCmdCopyBufferToImage(cb, a.handle, img.handle, vk.IMAGE_LAYOUT_GENERAL, 1, byref(reg))
     assert d.vkEndCommandBuffer(cb) == vk.VK_ERROR_INITIALIZATION_FAILED
     renderer.free_command_buffer(cb)
+
+
+# (x, y, width, height, minDepth, maxDepth): the whole framebuffer; a fractional offset with a narrowed
+# depth range; a viewport reaching past the left edge with an inverted depth range; a y-flipped viewport
+_VIEWPORTS = [None, (37.5, 20.25, 300.0, 260.0, 0.2, 0.9), (-100.0, 64.0, 700.0, 380.0, 1.0, 0.0),
+              (20.0, 460.0, 420.0, -400.0, 0.0, 1.0)]
+_SCISSORS = [None, (0, 0, 256, 512), (100, 37, 333, 250), (60, 0, 1000, 1000)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["batched", "blend"])
+def test_viewports_scissors_and_render_area(renderer, case):
+    """dynamic viewport and scissor changed between draws, inside a render area smaller than the framebuffer
+    whose loadOp CLEAR clears only that area: the attachments were filled beforehand by vkCmdClearColorImage
+    and vkCmdClearDepthStencilImage, and the oracle gets the same per-draw rectangles"""
+    scene = small_cases()[case]
+    W, H = scene.width, scene.height
+    area = (16, 24, W - 52, H - 40)                      # x, y, width, height
+    run = render.SceneRun(renderer, scene, mode="batched", tile=16)
+    vs, fs = scene.shaders()
+    run.pipe = renderer.pipeline(scene, run.rp, run.layout, vs, fs,
+                                 dynamic=(vk.DYNAMIC_STATE_VIEWPORT, vk.DYNAMIC_STATE_SCISSOR))
+    pre_color, pre_depth = (0.9, 0.1, 0.4, 0.6), 0.8
+
+    def viewport(i):
+        v = _VIEWPORTS[i % len(_VIEWPORTS)] or (0.0, 0.0, float(W), float(H), 0.0, 1.0)
+        return vk.VkViewport(*v), list(v)
+
+    def scissor(i):
+        s = _SCISSORS[(i // 2) % len(_SCISSORS)] or (0, 0, W, H)
+        return vk.VkRect2D(vk.VkOffset2D(s[0], s[1]), vk.VkExtent2D(s[2], s[3])), list(s)
+
+    r, d = renderer, renderer.drv
+    cb = r.begin()
+    cc = vk.VkClearColorValue()
+    cc.float32[:] = list(pre_color)
+    d.vkCmdClearColorImage(cb, run.color.handle, vk.IMAGE_LAYOUT_GENERAL, byref(cc), 1,
+                           byref(vk.VkImageSubresourceRange(vk.IMAGE_ASPECT_COLOR, 0, 1, 0, 1)))
+    d.vkCmdClearDepthStencilImage(cb, run.depth.handle, vk.IMAGE_LAYOUT_GENERAL,
+                                  byref(vk.VkClearDepthStencilValue(pre_depth, 0)), 1,
+                                  byref(vk.VkImageSubresourceRange(render._aspect(run.depth.format), 0, 1, 0, 1)))
+    clears = (vk.VkClearValue * 2)()
+    clears[0].color.float32[:] = list(scene.clear_color)
+    clears[1].depthStencil.depth = scene.clear_depth
+    rbi = vk.VkRenderPassBeginInfo(vk.ST_RENDER_PASS_BEGIN_INFO, None, run.rp, run.fb,
+                                   vk.VkRect2D(vk.VkOffset2D(area[0], area[1]), vk.VkExtent2D(area[2], area[3])),
+                                   2, clears)
+    d.vkCmdBeginRenderPass(cb, byref(rbi), vk.SUBPASS_CONTENTS_INLINE)
+    d.vkCmdBindPipeline(cb, vk.BIND_POINT_GRAPHICS, run.pipe)
+    d.vkCmdBindVertexBuffers(cb, 0, 1, (c_void_p * 1)(run.vb.handle.value), (c_uint64 * 1)(0))
+    if run.ib is not None:
+        d.vkCmdBindIndexBuffer(cb, run.ib.handle, 0, vk.INDEX_TYPE_UINT32)
+    for i, dr in enumerate(scene.draws):
+        vp, _ = viewport(i)
+        sc, _ = scissor(i)
+        d.vkCmdSetViewport(cb, 0, 1, byref(vp))
+        d.vkCmdSetScissor(cb, 0, 1, byref(sc))
+        _draw(d, cb, run, dr)
+    d.vkCmdEndRenderPass(cb)
+    vk.check("vkEndCommandBuffer", d.vkEndCommandBuffer(cb))
+    color, depth, st = _submit(run, cb)
+
+    col = np.empty((H, W, 4), dtype=np.uint8)
+    col[:] = [kz_oracle.unorm8(v) for v in pre_color]
+    dep = np.full((H, W), np.float32(pre_depth), dtype=np.float32)
+    x0, y0, x1, y1 = area[0], area[1], area[0] + area[2], area[1] + area[3]
+    col[y0:y1, x0:x1] = [kz_oracle.unorm8(v) for v in scene.clear_color]
+    dep[y0:y1, x0:x1] = np.float32(scene.clear_depth)
+    arr, n = kz_oracle.make_draws(scene)
+    for i in range(n):
+        arr[i].viewport[:] = viewport(i)[1]
+        arr[i].scissor[:] = scissor(i)[1]
+    ost = kz_oracle.KzoStats()
+    rect = (ctypes.c_int32 * 4)(x0, y0, x1, y1)
+    rc = kz_oracle.lib().kzo_render_ds(W, H, col.ctypes.data, dep.ctypes.data, None, kz_oracle.DEPTH_FORMAT["d32"],
+                                       rect, n, arr, 8, byref(ost))
+    assert rc == 0
+    assert np.array_equal(color, col)
+    assert np.array_equal(depth.view(np.uint32), dep.view(np.uint32))
+    assert st.fragments == ost.as_dict()["fragments"]
+    assert 0 < st.fragments
+    r.free_command_buffer(run.cb)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["soup", "batched"])
+def test_empty_and_ragged_draws(renderer, case):
+    """draws with no vertices, with no instances, and with 1 or 2 vertices past the last whole triangle
+    (ignored) among the scene's draws, and one draw reaching past the end of its buffer (skipped): the image
+    is the scene's own"""
+    scene = small_cases()[case]
+    run = render.SceneRun(renderer, scene, mode="batched", tile=16)
+
+    def body(d, cb):
+        for k, dr in enumerate(scene.draws):
+            if dr.mvp is not None:
+                m = np.ascontiguousarray(dr.mvp, dtype=np.float32)
+                d.vkCmdPushConstants(cb, run.layout, vk.SHADER_STAGE_VERTEX, 0, 64, m.ctypes.data)
+            extra = 1 + k % 2
+            if scene.indexed:
+                d.vkCmdDrawIndexed(cb, 0, 1, dr.first, dr.vertex_offset, 0)
+                d.vkCmdDrawIndexed(cb, 3 * dr.count, 0, dr.first, dr.vertex_offset, 0)
+                d.vkCmdDrawIndexed(cb, 3 * dr.count + extra, 1, dr.first, dr.vertex_offset, 0)
+            else:
+                d.vkCmdDraw(cb, 0, 1, dr.first, 0)
+                d.vkCmdDraw(cb, 3 * dr.count, 0, dr.first, 0)
+                d.vkCmdDraw(cb, 3 * dr.count + extra, 1, dr.first, 0)
+        # past the end of the bound index or vertex buffer: skipped at recording
+        if scene.indexed:
+            d.vkCmdDrawIndexed(cb, 6, 1, len(scene.indices) - 3, 0, 0)
+        else:
+            d.vkCmdDraw(cb, 6, 1, len(scene.vertices) - 3, 0)
+
+    color, depth, st = _submit(run, _record(run, body))
+    ref_c, ref_d, ost = kz_oracle.render(scene, threads=8)
+    assert np.array_equal(color, ref_c)
+    assert np.array_equal(depth.view(np.uint32), ref_d.view(np.uint32))
+    assert st.fragments == ost["fragments"]
+    renderer.free_command_buffer(run.cb)
+
+
+@pytest.mark.gpu
+def test_pass_without_draws_only_clears(renderer):
+    scene = small_cases()["batched"]
+    run = render.SceneRun(renderer, scene, mode="batched", tile=16)
+    color, depth, st = _submit(run, _record(run, lambda d, cb: None))
+    ref_c, ref_d = kz_oracle.clear_images(scene)
+    assert np.array_equal(color, ref_c) and np.array_equal(depth.view(np.uint32), ref_d.view(np.uint32))
+    assert st.fragments == 0
+    renderer.free_command_buffer(run.cb)
+
+
+def _instanced_vs():
+    """gl_Position = in0 + in2 (in2 read per instance); out0 = in1 + (gl_InstanceIndex * 0.125, 0, 0, 0)"""
+    from kazan_gb300 import spirv_asm as sa
+    m = sa.Module()
+    m.capability(sa.CapShader)
+    f32, i32 = m.f32(), m.i32(1)
+    v4 = m.vec(f32, 4)
+    pv = sa._per_vertex(m)
+    in_pos, in_col = sa._io(m, sa.SCInput, v4, 0), sa._io(m, sa.SCInput, v4, 1)
+    in_off = sa._io(m, sa.SCInput, v4, 2)
+    inst = m.variable(sa.SCInput, m.ptr(sa.SCInput, i32))
+    m.decorate(inst, sa.DecBuiltIn, sa.BuiltInInstanceIndex)
+    out_col = sa._io(m, sa.SCOutput, v4, 0)
+    fn = sa._begin_main(m)
+    p = m.res(sa.OpFAdd, v4, m.res(sa.OpLoad, v4, in_pos), m.res(sa.OpLoad, v4, in_off))
+    m.op(sa.OpStore, m.res(sa.OpAccessChain, m.ptr(sa.SCOutput, v4), pv, m.ci(0)), p)
+    c = m.res(sa.OpLoad, v4, in_col)
+    k = m.res(sa.OpFMul, f32, m.res(sa.OpConvertSToF, f32, m.res(sa.OpLoad, i32, inst)), m.cf(0.125))
+    comps = [m.res(sa.OpCompositeExtract, f32, c, j) for j in range(4)]
+    comps[0] = m.res(sa.OpFAdd, f32, comps[0], k)
+    m.op(sa.OpStore, out_col, m.res(sa.OpCompositeConstruct, v4, *comps))
+    sa._end_main(m)
+    m.entry(sa.ExecVertex, fn, "main", [pv, in_pos, in_col, in_off, inst, out_col])
+    return m.to_words()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("indirect", [False, True])
+def test_instanced_draw_with_per_instance_attribute(renderer, indirect):
+    """3 instances from firstInstance 1 of the 2,048-triangle soup: each instance moved by its own offset
+    (a per-instance vertex attribute) and tinted by gl_InstanceIndex; the oracle draws the instances one
+    after another (instance-major primitive order) with the same arithmetic done in float32"""
+    base = small_cases()["soup"]
+    offs = np.array([[9, 9, 9, 0], [0.05, -0.1, 0.02, 0.0], [-0.125, 0.0625, -0.05, 0.0], [0.2, 0.15, 0.1, 0.0]],
+                    dtype=np.float32)
+    first, count = 1, 3
+    run = render.SceneRun(renderer, base, mode="batched", tile=16)
+    _, fs = base.shaders()
+    run.pipe = renderer.pipeline(base, run.rp, run.layout, _instanced_vs(), fs,
+                                 instance_attr=(2, vk.FORMAT_R32G32B32A32_SFLOAT, 16))
+    ibuf = renderer.create_buffer(offs.nbytes, vk.BUFFER_USAGE_VERTEX, True)
+    renderer.write_buffer(ibuf, offs)
+    cmd = renderer.create_buffer(16, vk.BUFFER_USAGE_INDIRECT, True)
+    renderer.write_buffer(cmd, np.array([3 * base.draws[0].count, count, 0, first], dtype=np.uint32))
+
+    def body(d, cb):
+        d.vkCmdBindVertexBuffers(cb, 1, 1, (c_void_p * 1)(ibuf.handle.value), (c_uint64 * 1)(0))
+        if indirect:
+            d.vkCmdDrawIndirect(cb, cmd.handle, 0, 1, 16)
+        else:
+            d.vkCmdDraw(cb, 3 * base.draws[0].count, count, 0, first)
+        # one instance past the instance buffer's 4 entries: skipped
+        d.vkCmdDraw(cb, 3, 1, 0, 4)
+
+    color, depth, st = _submit(run, _record(run, body))
+    verts = []
+    for i in range(first, first + count):
+        v = base.vertices.copy()
+        v[:, 0:4] = v[:, 0:4] + offs[i]
+        v[:, 4] = v[:, 4] + np.float32(i * 0.125)
+        verts.append(v)
+    nt = base.draws[0].count
+    scene = dataclasses.replace(base, vertices=np.concatenate(verts),
+                                draws=[scenes.Draw(3 * nt * k, nt) for k in range(count)])
+    ref_c, ref_d, ost = kz_oracle.render(scene, threads=8)
+    assert np.array_equal(color, ref_c)
+    assert np.array_equal(depth.view(np.uint32), ref_d.view(np.uint32))
+    assert st.fragments == ost["fragments"]
+    renderer.free_command_buffer(run.cb)
