@@ -1030,9 +1030,14 @@ __device__ __forceinline__ uint32_t stencil_apply(uint32_t op, uint32_t s, uint3
 
 #define KZ_SMALL_PX 32      /* clipped sub-triangles with boxes of at most this many pixels are rasterised by
                                their geometry thread */
+#ifndef KZ_WARP_PX
 #define KZ_WARP_PX 192      /* unclipped triangles with boxes of at most this many pixels are rasterised by
                                their geometry warp (vis_warp_raster); larger ones become jobs */
-#define KZ_JOB_BLOCKS 16    /* 8x8 pixel blocks per large-triangle job */
+#endif
+#ifndef KZ_JOB_BLOCKS
+#define KZ_JOB_BLOCKS 16    /* 8x8 pixel blocks per large-triangle job (at most 32: one lane each) */
+#endif
+static_assert(KZ_JOB_BLOCKS >= 1 && KZ_JOB_BLOCKS <= 32, "one lane per block of a job");
 
 __device__ __forceinline__ unsigned long long* vis_px(const KzSegment& seg, int32_t x, int32_t y) {
   return reinterpret_cast<unsigned long long*>(seg.vis) + (size_t)y * seg.width + x;
@@ -1281,7 +1286,8 @@ __device__ __forceinline__ int vis_triangle(const Ctx& c, const KzDraw& d, const
 }
 
 #define KZ_GEO_SMEM (KZ_THREADS * (96 + 1))
-#define KZ_MAGIC_MAX 128 /* at least the pixel pairs per row of a warp-rasterised box: ceil(w / 2), w * h <= KZ_WARP_PX */
+/* at least the pixel pairs per row of a warp-rasterised box: ceil(w / 2), w * h <= KZ_WARP_PX */
+#define KZ_MAGIC_MAX ((KZ_WARP_PX + 1) / 2 > 128 ? (KZ_WARP_PX + 1) / 2 : 128)
 static_assert((KZ_WARP_PX + 1) / 2 <= KZ_MAGIC_MAX, "the divisor table covers every warp-rasterised box width");
 
 /* table[pw] = floor((2^32 - 1) / pw) + 1 for pw in [2, KZ_MAGIC_MAX] (0 for 0 and 1), filled by the block */
