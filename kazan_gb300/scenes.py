@@ -151,7 +151,9 @@ class Scene:
         return vs, fs
 
     def algorithmic_bytes(self):
-        """B = 12 T_indexed + S_v V + 64 draws + W H (colour + depth traffic)"""
+        """algorithmic HBM bytes of one submission: 12 B of indices per indexed triangle, the vertex stride
+        per vertex, 64 B of push constants per draw, and the framebuffer read and written once (colour and
+        depth 4 B each per pixel; depth read but not written when depth writes are off)"""
         t_idx = self.triangles if self.indexed else 0
         v = len(self.vertices) if self.indexed else 3 * self.triangles
         push = 64 * len(self.draws) if self.shader == "lambert" else 0
