@@ -4,10 +4,12 @@
 Workload (default): the batched command buffer - 4,096 vkCmdDrawIndexed draws (log-uniform triangle
 counts in [16, 65536], each its own sphere mesh and MVP push constant, Lambert VS/FS) into a 2048x2048
 RGBA8 + D32 target, seeded synthetic scene (seed 3).  One step = one vkQueueSubmit of the recorded command
-buffer (--mode batched: one launch per pipeline phase), i.e. one full render of the scene.  The timed
-command buffer is recorded with the driver's kernel timing on, so every kernel launch inside the timed
-region is bracketed by CUDA events on the queue stream; the roofline uses the dominant kernel's mean
-duration from those events.
+buffer (--mode batched: one launch per pipeline phase), i.e. one full render of the scene.  `value` times
+K submissions of the command buffer as an application records it (a CUDA graph whose kernels are chained
+by programmatic dependent launch).  The same K submissions are then timed again from a second recording
+of the same draws with the driver's kernel timing on, where every kernel launch is bracketed by CUDA
+events on the queue stream: the `kernels` table and the roofline (the dominant kernel's mean duration)
+come from that pass, `kernel_pass` gives its step time.
 
 Printed JSON line (rank 0):
   value      Mtris/s with vertex/index buffers and attachments resident in HBM (device-local memory),
@@ -247,41 +249,55 @@ def main():
         mode, tile = best.mode, best.tile
         tuning = {"signature": sig, "chosen": {"mode": mode, "tile": tile},
                   "ms": None if table is None else {"%s/%d" % (c.mode, c.tile): round(v, 4) for c, v in table.items()}}
-    # the timed command buffer launches its kernels at submit with timing events around each launch
+    # two command buffers of the same draws: `graph_cb` is what an application submits (captured as a CUDA
+    # graph at vkEndCommandBuffer, its kernels chained by programmatic dependent launch); `timed_cb`
+    # launches its kernels at submit with an event pair around each launch, for the per-kernel times
     r.drv.set_option("mode", mode)
     r.drv.set_option("tile", tile)
-    r.drv.set_option("kernel_timing", 1)
     old_cb = run.cb
-    run.cb = run.record()
-    r.free_command_buffer(old_cb)
+    graph_cb = run.record()
+    r.drv.set_option("kernel_timing", 1)
+    timed_cb = run.record()
     r.drv.set_option("kernel_timing", 0)
+    r.free_command_buffer(old_cb)
     stream = torch.cuda.ExternalStream(r.stream())
 
     def barrier():
         replicas.barrier(rk)
 
-    for _ in range(max(3, args.warmup)):
-        run.submit()
-    r.drv.kernel_times(run.cb, reset=True)
-    barrier()
-    torch.cuda.synchronize()
-    clocks = Clocks(local)
-    clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    w0 = time.monotonic()
-    e0.record(stream)
-    for _ in range(args.steps):
-        run.submit(wait=False)
-    e1.record(stream)
-    e1.synchronize()
-    w1 = time.monotonic()
-    r.drv.vkQueueWaitIdle(r.queue)
-    ck = clocks.stop(w0, w1)
-    torch.cuda.synchronize()
-    barrier()
-    ms = replicas.max_over_ranks(rk, e0.elapsed_time(e1) / args.steps, device="cuda")
-    # per-kernel device time over the timed submissions (events on the queue stream around each launch)
-    ktimes = r.drv.kernel_times(run.cb)
+    def timed_region(cb):
+        """K submissions of `cb` between a barrier + synchronize on both sides, timed by CUDA events on the
+        queue stream; returns (ms per step over all ranks, clock record)"""
+        run.cb = cb
+        for _ in range(max(3, args.warmup)):
+            run.submit()
+        r.drv.kernel_times(cb, reset=True)
+        barrier()
+        torch.cuda.synchronize()
+        clocks = Clocks(local)
+        clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0 = time.monotonic()
+        e0.record(stream)
+        for _ in range(args.steps):
+            run.submit(wait=False)
+        e1.record(stream)
+        e1.synchronize()
+        w1 = time.monotonic()
+        r.drv.vkQueueWaitIdle(r.queue)
+        ck = clocks.stop(w0, w1)
+        torch.cuda.synchronize()
+        barrier()
+        return replicas.max_over_ranks(rk, e0.elapsed_time(e1) / args.steps, device="cuda"), ck
+
+    # the headline: the application's command buffer
+    ms, ck = timed_region(graph_cb)
+    launches = run.stats().launches * args.steps
+    # the same K submissions again with an event pair around each launch: per-kernel device time
+    ms_k, ck_k = timed_region(timed_cb)
+    ktimes = r.drv.kernel_times(timed_cb)
+    run.cb = graph_cb
+    r.free_command_buffer(timed_cb)
     kernels = {k: {"launches": n, "ms_per_launch": round(t / max(n, 1), 4),
                    "share": round(t / max(sum(x[0] for x in ktimes.values()), 1e-9), 4)}
                for k, (t, n) in ktimes.items()}
@@ -309,7 +325,9 @@ def main():
                         "bytes_formula": kformula,
                         "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"},
            "kernels": kernels,
-           "clocks": ck, "gpu_launches": int(sum(n for _, n in ktimes.values())), "autotune": tuning}
+           "kernel_pass": {"ms_per_step": round(ms_k, 4), "steps": args.steps, "clocks": ck_k,
+                           "how": "the same submissions with an event pair around each kernel launch"},
+           "clocks": ck, "gpu_launches": int(launches), "autotune": tuning}
     if not args.no_perdraw:
         pd = render.SceneRun(r, scene, host_visible=False, mode="perdraw", tile=args.tile, indirect=indirect)
         pd.submit()

@@ -1120,8 +1120,12 @@ static cudaEvent_t timing_event(Device* dev) {
 }
 
 /* one kernel launch; with `timing` set, bracketed by a pair of timing events on the same stream */
+/* `chain`: the previous operation on the stream was one of the pipeline kernels.  Such a kernel is then
+ * launched with programmatic stream serialization, so its launch overlaps the previous kernel's
+ * completion; each kernel waits at entry (griddepcontrol.wait) until its predecessor has completed.
+ * Timed launches (an event between the kernels) and cooperative launches are not chained. */
 static void launch(Device* dev, std::vector<TimedLaunch>* timing, int kind, const cudaLaunchConfig_t& cfg,
-                   cudaKernel_t fn, void** args) {
+                   cudaKernel_t fn, void** args, bool& chain) {
   TimedLaunch t;
   if (timing) {
     t.kind = kind;
@@ -1129,11 +1133,20 @@ static void launch(Device* dev, std::vector<TimedLaunch>* timing, int kind, cons
     t.after = timing_event(dev);
     cudaEventRecord(t.before, cfg.stream);
   }
-  cudaLaunchKernelExC(&cfg, (const void*)fn, args);
+  cudaLaunchAttribute at[1];
+  cudaLaunchConfig_t c = cfg;
+  if (chain && !timing && options().pdl && cfg.numAttrs == 0) {
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    c.attrs = at;
+    c.numAttrs = 1;
+  }
+  cudaLaunchKernelExC(&c, (const void*)fn, args);
   if (timing) {
     cudaEventRecord(t.after, cfg.stream);
     timing->push_back(t);
   }
+  chain = true;
 }
 
 /* enqueue the lowered command buffer from segment `start` on */
@@ -1149,6 +1162,7 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
   if (capture) cudaEventRecordWithFlags(low.ev_begin, st, cudaEventRecordExternal);
   else cudaEventRecord(low.ev_begin, st);
   KernelSet* ks = low.ks;
+  bool chain = false;
   for (const Lowered::LOp& lop : low.ops) {
     if (lop.kind == OpKind::Pass) {
       if (lop.seg_end <= start) continue;
@@ -1162,11 +1176,11 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
         cfg.gridDim = dim3(1);
         cfg.blockDim = dim3(1024);
         cfg.stream = st;
-        launch(dev, timing, KK_INDIRECT, cfg, ks->indirect, args);
+        launch(dev, timing, KK_INDIRECT, cfg, ks->indirect, args, chain);
         const KzSegment& sg = low.segments[s];
         cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (std::max(sg.chunk_cap, sg.lut_cap) + 255) / 256)));
         cfg.blockDim = dim3(256);
-        launch(dev, timing, KK_INDIRECT_TABLES, cfg, ks->indirect_tables, args);
+        launch(dev, timing, KK_INDIRECT_TABLES, cfg, ks->indirect_tables, args, chain);
         launches += 2;
       }
       if (low.mode == 0) {
@@ -1184,7 +1198,7 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
         at[0].val.cooperative = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        launch(dev, timing, KK_PERSISTENT, cfg, ks->persistent, args);
+        launch(dev, timing, KK_PERSISTENT, cfg, ks->persistent, args, chain);
         launches++;
       } else {
         for (uint32_t s = s0; s < lop.seg_end; s++) {
@@ -1196,32 +1210,32 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
           cfg.stream = st;
           if (seg.mode == KZ_MODE_VISIBILITY) {
             cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (seg.width * seg.height + 255) / 256)));
-            launch(dev, timing, KK_VIS_INIT, cfg, ks->vis_init, args);
+            launch(dev, timing, KK_VIS_INIT, cfg, ks->vis_init, args, chain);
             if (seg.num_chunks || seg.indirect) {
               uint32_t gb = (uint32_t)std::max(1, ks->geometry_blocks);
               cfg.gridDim = dim3(seg.indirect ? gb : std::min<uint32_t>(seg.num_chunks, gb));
-              launch(dev, timing, KK_VIS_GEOMETRY, cfg, ks->vis_geometry, args);
+              launch(dev, timing, KK_VIS_GEOMETRY, cfg, ks->vis_geometry, args, chain);
               cfg.gridDim = dim3(grid_cap(dev));
-              launch(dev, timing, KK_VIS_LARGE, cfg, ks->vis_large, args);
+              launch(dev, timing, KK_VIS_LARGE, cfg, ks->vis_large, args, chain);
               launches += 2;
             }
             cfg.gridDim = dim3(grid_cap(dev));
-            launch(dev, timing, KK_VIS_RESOLVE, cfg, ks->vis_resolve, args);
+            launch(dev, timing, KK_VIS_RESOLVE, cfg, ks->vis_resolve, args, chain);
             launches += 2;
             continue;
           }
           if (seg.num_chunks || seg.indirect) {
             cfg.gridDim = dim3(seg.indirect ? grid_cap(dev) : seg.num_chunks);
-            launch(dev, timing, KK_GEOMETRY, cfg, ks->geometry, args);
+            launch(dev, timing, KK_GEOMETRY, cfg, ks->geometry, args, chain);
             launches++;
           }
           cfg.gridDim = dim3(1);
-          launch(dev, timing, KK_SCAN, cfg, ks->scan, args);
+          launch(dev, timing, KK_SCAN, cfg, ks->scan, args, chain);
           cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (seg.rec_cap + 255) / 256)));
-          launch(dev, timing, KK_BIN, cfg, ks->bin, args);
+          launch(dev, timing, KK_BIN, cfg, ks->bin, args, chain);
           cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, seg.tiles_x * seg.tiles_y)));
           cfg.dynamicSmemBytes = KZ_DYN_SMEM;
-          launch(dev, timing, KK_RASTER, cfg, ks->raster, args);
+          launch(dev, timing, KK_RASTER, cfg, ks->raster, args, chain);
           launches += 3;
         }
       }
@@ -1239,12 +1253,14 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
         long long work = (long long)(x1 - x0) * (y1 - y0) / 4 + 1;
         cfg.gridDim = dim3((unsigned)std::min<long long>(grid_cap(dev), (work + 255) / 256));
         cfg.stream = st;
-        launch(dev, timing, KK_CLEAR, cfg, ks->clear, args);
+        launch(dev, timing, KK_CLEAR, cfg, ks->clear, args, chain);
         launches++;
       } else if (op.kind == OpKind::Copy) {
         cudaMemcpyAsync(op.dst, op.src, op.bytes, cudaMemcpyDeviceToDevice, st);
+        chain = false;
       } else if (op.kind == OpKind::Copy2D) {
         cudaMemcpy2DAsync(op.dst, op.dpitch, op.src, op.spitch, op.width_bytes, op.rows, cudaMemcpyDeviceToDevice, st);
+        chain = false;
       } else if (op.kind == OpKind::Resolve) {
         uint64_t src = (uint64_t)(uintptr_t)op.src, dst = (uint64_t)(uintptr_t)op.dst;
         uint32_t spitch = (uint32_t)op.spitch, dpitch = (uint32_t)op.dpitch;
@@ -1254,7 +1270,7 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
         cfg.blockDim = dim3(256);
         cfg.gridDim = dim3((unsigned)std::min<long long>(grid_cap(dev), ((long long)w * h + 255) / 256));
         cfg.stream = st;
-        launch(dev, timing, KK_RESOLVE, cfg, ks->resolve, args);
+        launch(dev, timing, KK_RESOLVE, cfg, ks->resolve, args, chain);
         launches++;
       }
     }
@@ -1262,6 +1278,7 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
   if (capture) cudaEventRecordWithFlags(low.ev_end, st, cudaEventRecordExternal);
   else cudaEventRecord(low.ev_end, st);
   cudaMemcpyAsync(low.h_status, low.d_status, sizeof(KzStatus), cudaMemcpyDeviceToHost, st);
+  if (start == 0) low.launches = launches;
   return launches;
 }
 
@@ -1811,16 +1828,6 @@ extern "C" KZ_API int kzGetCommandBufferStats(VkCommandBuffer cbh, KzCommandBuff
   out->rec_cap = low.rec_cap;
   out->pair_cap = low.pair_cap;
   out->gpu_ms = cb->last_ms;
-  uint32_t launches = 0;
-  for (const auto& op : low.ops) {
-    if (op.kind == kz::OpKind::Pass) {
-      if (low.mode == 0) launches += op.seg_end > op.seg_begin ? 1 : 0;
-      else
-        for (uint32_t s = op.seg_begin; s < op.seg_end; s++) launches += (low.segments[s].num_chunks ? 4 : 2);
-    } else if (op.kind == kz::OpKind::Clear || op.kind == kz::OpKind::Fill) {
-      launches++;
-    }
-  }
-  out->launches = launches;
+  out->launches = low.launches; /* counted by the launch sequence itself when it was captured or last ran */
   return 0;
 }

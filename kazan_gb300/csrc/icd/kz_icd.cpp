@@ -44,6 +44,8 @@ Options& options() {
     if (f && !std::strncmp(f, "alloc:", 6)) r.fault_alloc = std::atol(f + 6);
     const char* kt = std::getenv("KZ_KERNEL_TIMING");
     if (kt) r.kernel_timing = std::atoi(kt);
+    const char* pd = std::getenv("KZ_PDL");
+    if (pd) r.pdl = std::atoi(pd) != 0;
     return r;
   }();
   return o;
@@ -1624,6 +1626,11 @@ extern "C" KZ_API int kzDriverSetOption(const char* key, const char* value) {
   if (!std::strcmp(key, "kernel_timing")) {
     if (std::strcmp(value, "0") && std::strcmp(value, "1")) return -1;
     o.kernel_timing = value[0] == '1';
+    return 0;
+  }
+  if (!std::strcmp(key, "pdl")) {
+    if (std::strcmp(value, "0") && std::strcmp(value, "1")) return -1;
+    o.pdl = value[0] == '1';
     return 0;
   }
   if (!std::strcmp(key, "fault_alloc")) {

@@ -275,6 +275,7 @@ struct RecOp {
 
 /* lowered command buffer */
 struct Lowered {
+  uint32_t launches = 0;                   /* kernels one submission of the whole command buffer launches */
   std::vector<KzDraw> draws;
   std::vector<KzPipe> pipes;
   std::vector<Pipeline*> pipe_objs;
@@ -391,6 +392,8 @@ struct Options {
   int trace = 0;      /* KZ_TRACE */
   long fault_alloc = -1; /* KZ_FAULT=alloc:N: the Nth device allocation fails */
   int kernel_timing = 0; /* KZ_KERNEL_TIMING */
+  int pdl = 1;        /* KZ_PDL: a kernel that follows another kernel in a submission is launched with
+                         programmatic stream serialization (its launch overlaps the predecessor's completion) */
 };
 Options& options();
 

@@ -2082,7 +2082,17 @@ __device__ __forceinline__ uint32_t grab(uint32_t* counter, uint32_t* sh) {
 
 /* ================= kernels ================= */
 
+/* Programmatic dependent launch: the driver may launch a kernel before the kernel ahead of it in the
+ * stream has completed (cudaLaunchAttributeProgrammaticStreamSerialization), so the launch overlaps the
+ * predecessor's completion.  Every kernel first waits until its predecessor has completed and that grid's
+ * writes are visible (a no-op when it was launched the ordinary way).  No kernel triggers its successor
+ * early (griddepcontrol.launch_dependents): successor blocks scheduled while the predecessor still ran
+ * made every workload slower (0.2295 -> 0.242 ms on a 1M-triangle draw), so a successor starts once its
+ * predecessor's blocks have all exited. */
+__device__ __forceinline__ void kz_pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_geometry(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
   __shared__ uint32_t sh[40];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
@@ -2137,6 +2147,7 @@ __device__ __forceinline__ IndirectCmd load_indirect(const KzDraw& d, bool& bad)
  * sums over the segment in draw order (a chunk never spans two draws, as in the chunk table of direct
  * draws); finally the segment's num_prims, num_chunks and draw lookup pointer. */
 extern "C" __global__ void __launch_bounds__(KZ_IND_THREADS) kz_k_indirect(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
   __shared__ unsigned long long warp_p[KZ_IND_THREADS / 32], warp_c[KZ_IND_THREADS / 32];
   KzSegment* seg = reinterpret_cast<KzSegment*>(f.segments) + s;
   KzDraw* draws = reinterpret_cast<KzDraw*>(f.draws) + seg->first_draw;
@@ -2219,6 +2230,7 @@ extern "C" __global__ void __launch_bounds__(KZ_IND_THREADS) kz_k_indirect(KzFra
 /* after kz_k_indirect, every thread of the grid: the chunk table (KzChunk per chunk, as for direct draws)
  * and the draw lookup (draw holding primitive 256 i) of an indirect segment, where they fit their room */
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_indirect_tables(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
   const KzSegment& seg = reinterpret_cast<const KzSegment*>(f.segments)[s];
   const KzDraw* draws = reinterpret_cast<const KzDraw*>(f.draws);
   const uint32_t nc = seg.num_chunks <= seg.chunk_cap ? seg.num_chunks : 0u;
@@ -2241,6 +2253,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_indirect_tables(Kz
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_scan(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
   __shared__ uint32_t sh[KZ_THREADS + 1];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
@@ -2248,6 +2261,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_scan(KzFrame f, ui
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_bin(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
   uint32_t n = min(c.cnt->rec_count, c.seg->rec_cap);
@@ -2260,6 +2274,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_bin(KzFrame f, uin
 /* 4 blocks per SM (at most 64 registers, some spilled): measured on the ordered blend workload at 2.90 ms
  * against 3.44 (3 blocks, 85 registers), 3.78 (2 blocks, 128 registers) and 3.06 (5 blocks) */
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float u8tab[256];
   Ctx c = make_ctx(f, s);
@@ -2270,12 +2285,14 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster(KzFrame 
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_vis_init(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
   vis_init_range(*c.seg, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_geometry(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
   __shared__ __align__(16) unsigned char slots[KZ_GEO_SMEM];
   __shared__ uint32_t magic_tab[KZ_MAGIC_MAX + 1];
   Ctx c = make_ctx(f, s);
@@ -2288,6 +2305,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_geometry(Kz
 
 /* 4 blocks per SM: 0.313 ms on the 4,096-draw workload against 0.357 (3 blocks) and 0.341 (5 blocks) */
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_large(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s) || !vis_check(c, s)) return;
   uint32_t njobs = c.cnt->pair_count;
@@ -2305,6 +2323,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_large(KzFra
 /* 4 blocks per SM (64 registers, the most its fragment-shader callee allows at 5 is 51): 0.155 ms against
  * 0.162 at 3 resident blocks */
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_resolve(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
   uint32_t items = ((c.seg->width + 31) / 32) * c.seg->height;
@@ -2396,6 +2415,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_resolve(uint64_t src, uint32_t spitch, int32_t sx,
                                                                       int32_t sy, uint64_t dst, uint32_t dpitch,
                                                                       int32_t dx, int32_t dy, int32_t w, int32_t h) {
+  kz_pdl_enter();
   const long long total = (long long)w * h;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
@@ -2418,6 +2438,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_resolve(uint64_t s
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_clear(uint64_t base, uint32_t pitch, int32_t x0,
                                                                     int32_t y0, int32_t x1, int32_t y1,
                                                                     uint32_t value) {
+  kz_pdl_enter();
   int32_t w = x1 - x0, h = y1 - y0;
   if (w <= 0 || h <= 0) return;
   int32_t lead = (int32_t)((4 - (x0 & 3)) & 3);

@@ -129,3 +129,25 @@ def test_shaders_with_function_calls(renderer, mode):
     for scene in (soup, loops, lam):
         color, depth, stats = _render(renderer, scene, mode, 16)
         _check(scene, color, depth, stats)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["batched", "blend", "clip"])
+def test_chained_and_unchained_launches_agree(driver, renderer, case):
+    """kernels chained by programmatic dependent launch (the default) and launched one after another
+    render the same pixels; both match the oracle"""
+    scene = CASES[case]
+    outs = []
+    for pdl in ("1", "0"):
+        driver.set_option("pdl", pdl)
+        try:
+            run = render.SceneRun(renderer, scene, mode="batched", tile=16)
+        finally:
+            driver.set_option("pdl", "1")
+        for _ in range(2):
+            run.submit()
+        color, depth = run.read()
+        _check(scene, color, depth, run.stats())
+        outs.append((color, depth))
+        renderer.free_command_buffer(run.cb)
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
