@@ -208,7 +208,8 @@ static void record_draw(CommandBuffer* cb, uint32_t tri_count, uint32_t instance
   /* the draw's elements and instances must lie in the bound buffers, as kz_k_indirect checks for indirect
    * commands; a draw outside them is skipped, so no fetch leaves a buffer */
   const KzPipe& kp = cb->pipe->pipe;
-  uint64_t elems = indexed ? (cb->ib_off < cb->ib->size ? (cb->ib->size - cb->ib_off) / (d.indexed == 1 ? 4u : 2u) : 0)
+  uint64_t elems = indexed ? (cb->ib->mem && cb->ib_off < cb->ib->size
+                                  ? (cb->ib->size - cb->ib_off) / (d.indexed == 1 ? 4u : 2u) : 0)
                            : fetch_limit(cb, kp, false);
   uint64_t first_elem = indexed ? first_index : (uint64_t)(uint32_t)vertex_offset;
   if (first_elem + 3ull * tri_count > elems || (uint64_t)first_instance + instances > fetch_limit(cb, kp, true)) {
@@ -244,7 +245,7 @@ static uint32_t fetch_limit(const CommandBuffer* cb, const KzPipe& kp, bool per_
     const KzAttr& a = kp.attrs[i];
     if (!((used >> a.location) & 1u) || (((kp.binding_instanced >> a.binding) & 1u) != 0) != per_instance) continue;
     const Buffer* b = cb->vb[a.binding];
-    uint64_t avail = b && cb->vb_off[a.binding] < b->size ? b->size - cb->vb_off[a.binding] : 0;
+    uint64_t avail = b && b->mem && cb->vb_off[a.binding] < b->size ? b->size - cb->vb_off[a.binding] : 0;
     uint64_t need = (uint64_t)a.offset + attr_bytes(a.format), stride = kp.binding_stride[a.binding];
     uint64_t n = avail < need ? 0 : stride == 0 ? 0xFFFFFFFFull : (avail - need) / stride + 1;
     lim = std::min(lim, n);
@@ -261,14 +262,14 @@ static void record_indirect(CommandBuffer* cb, VkBuffer buffer, VkDeviceSize off
   if (!draw_state_ok(cb) || cb->pipe->rasterizer_discard || draw_count == 0) return;
   const Buffer* buf = H<Buffer>(buffer);
   const Buffer* cbuf = H<Buffer>(count_buffer);
-  if (count_buffer && (!cbuf || (count_offset & 3) || count_offset + 4 > cbuf->size)) {
+  if (count_buffer && (!cbuf || !cbuf->mem || (count_offset & 3) || count_offset + 4 > cbuf->size)) {
     log_error("indirect draw count: offset %llu does not fit the count buffer", (unsigned long long)count_offset);
     cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
     return;
   }
   uint32_t cmd_bytes = indexed ? 20u : 16u;
   if (draw_count == 1) stride = cmd_bytes;
-  if (!buf || (offset & 3) || (stride & 3) || stride < cmd_bytes ||
+  if (!buf || !buf->mem || (offset & 3) || (stride & 3) || stride < cmd_bytes ||
       offset + (VkDeviceSize)(draw_count - 1) * stride + cmd_bytes > buf->size) {
     log_error("indirect draw: offset %llu, stride %u, %u commands do not fit the buffer",
               (unsigned long long)offset, stride, draw_count);
@@ -285,8 +286,8 @@ static void record_indirect(CommandBuffer* cb, VkBuffer buffer, VkDeviceSize off
   const KzPipe& kp = cb->pipe->pipe;
   if (indexed) {
     uint32_t isz = d.indexed == 1 ? 4u : 2u;
-    d.elem_limit = (uint32_t)std::min<uint64_t>(cb->ib_off < cb->ib->size ? (cb->ib->size - cb->ib_off) / isz : 0,
-                                                0xFFFFFFFFull);
+    d.elem_limit = (uint32_t)std::min<uint64_t>(
+        cb->ib->mem && cb->ib_off < cb->ib->size ? (cb->ib->size - cb->ib_off) / isz : 0, 0xFFFFFFFFull);
   } else {
     d.elem_limit = fetch_limit(cb, kp, false);
   }
@@ -548,9 +549,27 @@ void VKAPI_CALL kzCmdDrawIndexedIndirectCount(VkCommandBuffer cbh, VkBuffer buff
   record_indirect(H<CommandBuffer>(cbh), buffer, offset, maxDrawCount, stride, true, countBuffer, countBufferOffset);
 }
 
+/* every attachment of the pass is an image with memory bound and at least the framebuffer's size, so no
+ * kernel of the pass addresses memory outside an attachment */
+static bool pass_targets_ok(const Framebuffer* fb, const RenderPass* rp) {
+  if (!fb || !rp) return false;
+  for (int a : {rp->color_att, rp->depth_att, rp->resolve_att}) {
+    if (a < 0) continue;
+    if ((size_t)a >= fb->views.size() || !fb->views[(size_t)a] || !fb->views[(size_t)a]->image) return false;
+    const Image* im = fb->views[(size_t)a]->image;
+    if (!im->mem || im->width < fb->width || im->height < fb->height) return false;
+  }
+  return true;
+}
+
 void VKAPI_CALL kzCmdBeginRenderPass(VkCommandBuffer cbh, const VkRenderPassBeginInfo* bi, VkSubpassContents) {
   /* api_impl.rs:4944 */
   CommandBuffer* cb = H<CommandBuffer>(cbh);
+  if (!bi || !pass_targets_ok(H<Framebuffer>(bi->framebuffer), H<RenderPass>(bi->renderPass))) {
+    log_error("render pass begun with a missing attachment, one without memory, or one smaller than the framebuffer");
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
   PassRec pr;
   pr.fb = H<Framebuffer>(bi->framebuffer);
   pr.rp = H<RenderPass>(bi->renderPass);
@@ -680,6 +699,10 @@ void VKAPI_CALL kzCmdResolveImage(VkCommandBuffer cbh, VkImage srcImage, VkImage
   CommandBuffer* cb = H<CommandBuffer>(cbh);
   Image* src = H<Image>(srcImage);
   Image* dst = H<Image>(dstImage);
+  if (!src || !dst || !src->mem || !dst->mem) {
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
   if (src->samples <= 1 || dst->samples != 1) {
     cb->record_error = VK_ERROR_FEATURE_NOT_PRESENT;
     return;
@@ -695,6 +718,10 @@ void VKAPI_CALL kzCmdResolveImage(VkCommandBuffer cbh, VkImage srcImage, VkImage
 }
 
 static void clear_image(CommandBuffer* cb, Image* img, uint32_t value) {
+  if (!img || !img->mem) {
+    cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
+    return;
+  }
   RecOp op;
   op.kind = OpKind::Clear;
   op.base = img->ptr();

@@ -450,3 +450,50 @@ def test_instanced_draw_with_per_instance_attribute(renderer, indirect):
     assert np.array_equal(depth.view(np.uint32), ref_d.view(np.uint32))
     assert st.fragments == ost["fragments"]
     renderer.free_command_buffer(run.cb)
+
+
+@pytest.mark.gpu
+def test_framebuffer_larger_than_its_attachments_is_a_recording_error(renderer):
+    scene = small_cases()["soup"]
+    run = render.SceneRun(renderer, scene, mode="batched", tile=16)
+    fb = renderer.framebuffer(run.rp, [run.color.view, run.depth.view], scene.width + 16, scene.height)
+    d = renderer.drv
+    cb = renderer.begin()
+    clears = (vk.VkClearValue * 2)()
+    rbi = vk.VkRenderPassBeginInfo(vk.ST_RENDER_PASS_BEGIN_INFO, None, run.rp, fb,
+                                   vk.VkRect2D(vk.VkOffset2D(0, 0), vk.VkExtent2D(scene.width + 16, scene.height)),
+                                   2, clears)
+    d.vkCmdBeginRenderPass(cb, byref(rbi), vk.SUBPASS_CONTENTS_INLINE)
+    d.vkCmdBindPipeline(cb, vk.BIND_POINT_GRAPHICS, run.pipe)
+    d.vkCmdDraw(cb, 3, 1, 0, 0)
+    d.vkCmdEndRenderPass(cb)
+    assert d.vkEndCommandBuffer(cb) == vk.VK_ERROR_INITIALIZATION_FAILED
+    renderer.free_command_buffer(cb)
+    renderer.free_command_buffer(run.cb)
+
+
+@pytest.mark.gpu
+def test_buffers_without_memory(renderer):
+    """a vertex buffer with no memory bound fetches nothing (its draw is skipped: the pass only clears), and
+    a fill of such a buffer is a recording error"""
+    scene = small_cases()["soup"]
+    run = render.SceneRun(renderer, scene, mode="batched", tile=16)
+    d = renderer.drv
+    bci = vk.VkBufferCreateInfo(vk.ST_BUFFER_CREATE_INFO, None, 0, scene.vertices.nbytes,
+                                vk.BUFFER_USAGE_VERTEX | vk.BUFFER_USAGE_TRANSFER_DST, 0, 0, None)
+    h = c_void_p()
+    vk.check("vkCreateBuffer", d.vkCreateBuffer(renderer.device, byref(bci), None, byref(h)))
+    try:
+        unbound = render.Buffer(h, None, scene.vertices.nbytes, False)
+        run.vb = unbound
+        color, depth, st = _submit(run, _record(run, lambda d, cb: _draw(d, cb, run, scene.draws[0])))
+        ref_c, ref_d = kz_oracle.clear_images(scene)
+        assert np.array_equal(color, ref_c) and np.array_equal(depth.view(np.uint32), ref_d.view(np.uint32))
+        assert st.fragments == 0
+        cb = renderer.begin()
+        d.vkCmdFillBuffer(cb, h, 0, 64, 0)
+        assert d.vkEndCommandBuffer(cb) == vk.VK_ERROR_INITIALIZATION_FAILED
+        renderer.free_command_buffer(cb)
+    finally:
+        d.vkDestroyBuffer(renderer.device, h, None)
+    renderer.free_command_buffer(run.cb)
