@@ -165,6 +165,7 @@ typedef enum VkFormat {
   VK_FORMAT_R8G8B8A8_UNORM = 37,
   VK_FORMAT_R8G8B8A8_SRGB = 43,
   VK_FORMAT_B8G8R8A8_UNORM = 44,
+  VK_FORMAT_B8G8R8A8_SRGB = 50,
   VK_FORMAT_R32_UINT = 98,
   VK_FORMAT_R32_SINT = 99,
   VK_FORMAT_R32_SFLOAT = 100,

@@ -36,6 +36,7 @@ DRIVER_SOURCES = [
 ]
 HEADERS = [
     "kz_raster_abi.h",
+    "kz_srgb_table.h",
     "icd/kz_icd.h",
     "shader/kz_ir.h",
     "shader/kz_spirv.h",
@@ -65,7 +66,7 @@ def _include_deps():
 def pipeline_object(verbose=False):
     src = os.path.join(CSRC, "raster", "kz_pipeline.cu")
     out = os.path.join(OUT, "kz_pipeline.cubin")
-    if _newer(out, [src, os.path.join(CSRC, "kz_raster_abi.h")]):
+    if _newer(out, [src, os.path.join(CSRC, "kz_raster_abi.h"), os.path.join(CSRC, "kz_srgb_table.h")]):
         cmd = [NVCC, "-rdc=true", "-cubin"] + ARCH + ["-O3", "-lineinfo", "-fmad=false", "-o", out, src]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
@@ -79,7 +80,7 @@ def texture_object(verbose=False):
     """kz_tex.cubin: the texture sampling functions the shaders call, within 64 registers per thread"""
     src = os.path.join(CSRC, "raster", "kz_tex.cu")
     out = os.path.join(OUT, "kz_tex.cubin")
-    if _newer(out, [src, os.path.join(CSRC, "kz_raster_abi.h")]):
+    if _newer(out, [src, os.path.join(CSRC, "kz_raster_abi.h"), os.path.join(CSRC, "kz_srgb_table.h")]):
         cmd = [NVCC, "-rdc=true", "-cubin"] + ARCH + ["-O3", "-lineinfo", "-fmad=false", "-maxrregcount=64", "-o", out,
                                                      src]
         log = _run(cmd)

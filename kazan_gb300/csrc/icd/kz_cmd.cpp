@@ -20,6 +20,7 @@
 
 #include "kazan_driver.h"
 #include "kz_icd.h"
+#include "../kz_srgb_table.h"
 
 namespace kz {
 
@@ -33,9 +34,25 @@ static uint8_t unorm8(float v) {
   return (uint8_t)(int)std::rint(c * 255.0f);
 }
 
+static const float kz_srgb_thr[255] = KZ_SRGB_THRESHOLDS;
+
+/* the 8-bit sRGB code of linear v (the kernels' srgb8, over the same table) */
+static uint8_t srgb8(float v) {
+  if (!(v > 0.0f)) return 0;
+  if (v >= 1.0f) return 255;
+  uint32_t n = 0;
+  for (uint32_t step = 128; step > 0; step >>= 1)
+    if (n + step <= 255u && kz_srgb_thr[n + step - 1] <= v) n += step;
+  return (uint8_t)n;
+}
+
+/* a clear colour as the attachment's texel: UNORM8 channels, or sRGB codes for red, green and blue */
 static uint32_t pack_color(VkFormat f, const float* c) {
-  uint8_t r = unorm8(c[0]), g = unorm8(c[1]), b = unorm8(c[2]), a = unorm8(c[3]);
-  if (f == VK_FORMAT_B8G8R8A8_UNORM) return (uint32_t)b | ((uint32_t)g << 8) | ((uint32_t)r << 16) | ((uint32_t)a << 24);
+  const bool srgb = f == VK_FORMAT_R8G8B8A8_SRGB || f == VK_FORMAT_B8G8R8A8_SRGB;
+  uint8_t r = srgb ? srgb8(c[0]) : unorm8(c[0]), g = srgb ? srgb8(c[1]) : unorm8(c[1]);
+  uint8_t b = srgb ? srgb8(c[2]) : unorm8(c[2]), a = unorm8(c[3]);
+  if (f == VK_FORMAT_B8G8R8A8_UNORM || f == VK_FORMAT_B8G8R8A8_SRGB)
+    return (uint32_t)b | ((uint32_t)g << 8) | ((uint32_t)r << 16) | ((uint32_t)a << 24);
   return (uint32_t)r | ((uint32_t)g << 8) | ((uint32_t)b << 16) | ((uint32_t)a << 24);
 }
 
@@ -992,9 +1009,16 @@ static void add_unique(std::vector<DeviceMemory*>& v, DeviceMemory* m) {
 }
 
 static uint32_t color_format(VkFormat f) {
+  /* texture images: UNORM only (sampling does not decode sRGB) */
   if (f == VK_FORMAT_R8G8B8A8_UNORM) return KZ_CF_RGBA8;
   if (f == VK_FORMAT_B8G8R8A8_UNORM) return KZ_CF_BGRA8;
   return KZ_CF_NONE;
+}
+
+static uint32_t attachment_format(VkFormat f) {
+  if (f == VK_FORMAT_R8G8B8A8_SRGB) return KZ_CF_RGBA8_SRGB;
+  if (f == VK_FORMAT_B8G8R8A8_SRGB) return KZ_CF_BGRA8_SRGB;
+  return color_format(f);
 }
 
 /* fill the framebuffer part of a segment from a render pass instance */
@@ -1025,7 +1049,7 @@ static void segment_target(const PassRec& pr, KzSegment& s, uint32_t tile, bool 
     Image* img = fb->views[(size_t)rp->color_att]->image;
     s.color = (uint64_t)(uintptr_t)img->ptr();
     s.color_pitch = img->pitch;
-    s.color_format = color_format(img->format);
+    s.color_format = attachment_format(img->format);
     s.width = std::min(s.width, img->width);
     s.height = std::min(s.height, img->height);
     const VkAttachmentDescription& a = rp->atts[(size_t)rp->color_att];

@@ -229,6 +229,8 @@ static uint32_t format_bpp(VkFormat f) {
   switch (f) {
     case VK_FORMAT_R8G8B8A8_UNORM:
     case VK_FORMAT_B8G8R8A8_UNORM:
+    case VK_FORMAT_R8G8B8A8_SRGB:
+    case VK_FORMAT_B8G8R8A8_SRGB:
     case VK_FORMAT_D32_SFLOAT:
     case VK_FORMAT_D24_UNORM_S8_UINT: return 4;
     case VK_FORMAT_D16_UNORM: return 2;
@@ -450,6 +452,11 @@ static void VKAPI_CALL kzGetPhysicalDeviceFormatProperties(VkPhysicalDevice, VkF
       p->optimalTilingFeatures = p->linearTilingFeatures =
           VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT | VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT | xfer |
           VK_FORMAT_FEATURE_SAMPLED_IMAGE_BIT | VK_FORMAT_FEATURE_SAMPLED_IMAGE_FILTER_LINEAR_BIT;
+      break;
+    case VK_FORMAT_R8G8B8A8_SRGB:
+    case VK_FORMAT_B8G8R8A8_SRGB: /* colour attachments (encoded at store, decoded for blending); not sampled */
+      p->optimalTilingFeatures = p->linearTilingFeatures =
+          VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT | VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT | xfer;
       break;
     case VK_FORMAT_D32_SFLOAT:
     case VK_FORMAT_D16_UNORM:
@@ -728,7 +735,8 @@ static VkResult VKAPI_CALL kzBindBufferMemory2(VkDevice device, uint32_t n, cons
 static VkResult VKAPI_CALL kzCreateImage(VkDevice, const VkImageCreateInfo* ci, const VkAllocationCallbacks*,
                                          VkImage* out) {
   /* api_impl.rs:3851 vkCreateImage; image.rs:58-87 accepts only RGBA8, 1 mip, 1 sample.  This driver adds
-   * B8G8R8A8_UNORM and D32_SFLOAT; both tilings are row-major with a tight 4-byte pixel pitch. */
+   * B8G8R8A8_UNORM, the two 8-bit sRGB formats (one sample) and the depth formats; both tilings are
+   * row-major. */
   if (!ci || ci->sType != VK_STRUCTURE_TYPE_IMAGE_CREATE_INFO) return VK_ERROR_INITIALIZATION_FAILED;
   uint32_t bpp = format_bpp(ci->format);
   const bool ms_ok = ci->samples == VK_SAMPLE_COUNT_4_BIT && !(ci->usage & VK_IMAGE_USAGE_SAMPLED_BIT) &&

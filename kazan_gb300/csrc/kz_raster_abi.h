@@ -71,8 +71,15 @@ enum KzVisKey {
 /* attachment load ops as the tiles see them */
 enum KzLoad { KZ_LOAD_LOAD = 0, KZ_LOAD_CLEAR = 1, KZ_LOAD_DONT_CARE = 2 };
 
-/* colour formats the raster stores */
-enum KzColorFormat { KZ_CF_NONE = 0, KZ_CF_RGBA8 = 1, KZ_CF_BGRA8 = 2 };
+/* colour formats the raster stores.  The sRGB formats hold the 8-bit sRGB codes of the red, green and
+ * blue channels (encoded at store, decoded before blending, kz_srgb_table.h) and a linear alpha. */
+enum KzColorFormat {
+  KZ_CF_NONE = 0,
+  KZ_CF_RGBA8 = 1,
+  KZ_CF_BGRA8 = 2,
+  KZ_CF_RGBA8_SRGB = 3,
+  KZ_CF_BGRA8_SRGB = 4
+};
 
 /* depth attachment formats.  D16 and D24 depths are compared and stored as rint(z * (2^bits - 1)), an
  * integer the kernels hold in a float (exact below 2^24); D24S8 texels keep the depth in bits 0..23 and

@@ -22,6 +22,7 @@
 #include <stdint.h>
 
 #include "../kz_raster_abi.h"
+#include "../kz_srgb_table.h"
 #include "kz_exact.h"
 
 /* vertex shader functions fetch their own attributes from the draw's vertex buffers */
@@ -70,6 +71,33 @@ __device__ __forceinline__ uint8_t unorm8(float v) {
   return (uint8_t)__float2int_rn(fmul(c, 255.0f));
 }
 __device__ __forceinline__ float u8f(uint32_t u) { return fdiv(__uint2float_rn(u), 255.0f); }
+
+/* the 8-bit sRGB formats (red, green and blue as sRGB codes, alpha linear): the exact encode steps and
+ * decode values of kz_srgb_table.h, here for kernels without their own shared copy */
+__device__ const float kz_srgb_thr_g[256] = KZ_SRGB_THRESHOLDS; /* 255 steps; the last entry is padding */
+__device__ const float kz_srgb_dec_g[256] = KZ_SRGB_DECODE;
+
+__device__ __forceinline__ bool cf_srgb(uint32_t fmt) { return fmt == KZ_CF_RGBA8_SRGB || fmt == KZ_CF_BGRA8_SRGB; }
+__device__ __forceinline__ bool cf_bgra(uint32_t fmt) { return fmt == KZ_CF_BGRA8 || fmt == KZ_CF_BGRA8_SRGB; }
+
+/* the 8-bit sRGB code of linear v: the number of encode steps thr[0..254] (ascending) at or below v, by
+ * binary search; 0 for v <= 0 or NaN, 255 for v >= 1 */
+__device__ __forceinline__ uint32_t srgb8(float v, const float* thr) {
+  if (!(v > 0.0f)) return 0u;
+  if (v >= 1.0f) return 255u;
+  uint32_t n = 0;
+#pragma unroll
+  for (uint32_t step = 128; step > 0; step >>= 1)
+    if (n + step <= 255u && thr[n + step - 1] <= v) n += step;
+  return n;
+}
+
+/* shared-memory table of the raster kernels: u8f(k) for k = 0..255 (the sRGB tables stay in global
+ * memory: with them the persistent kernel's static and dynamic shared memory would pass 48 KB) */
+#define KZ_CTAB_FLOATS 256
+__device__ __forceinline__ void fill_color_tabs(float* t) {
+  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) t[i] = u8f(i);
+}
 
 
 /* ---------------- frame access ---------------- */
@@ -572,21 +600,25 @@ __device__ __forceinline__ float blend_op(uint32_t op, float s, float sf, float 
 
 /* colour in attachment byte order -> RGBA channel order */
 __device__ __forceinline__ uint32_t to_rgba(uint32_t px, uint32_t fmt) {
-  if (fmt == KZ_CF_BGRA8) return (px & 0xFF00FF00u) | ((px >> 16) & 0xFFu) | ((px & 0xFFu) << 16);
+  if (cf_bgra(fmt)) return (px & 0xFF00FF00u) | ((px >> 16) & 0xFFu) | ((px & 0xFFu) << 16);
   return px;
 }
 __device__ __forceinline__ uint32_t from_rgba(uint32_t px, uint32_t fmt) { return to_rgba(px, fmt); }
 
 /* apply blend + write mask; dst/out packed RGBA (R in the low byte).  `u8tab`, when given, holds u8f(k)
- * for k = 0..255 (the same quotients, read instead of divided). */
-__device__ uint32_t color_write(const KzPipe& p, uint32_t dst, const float col[4], const float* u8tab = nullptr) {
+ * for k = 0..255 (the same quotients, read instead of divided); `srgb`: the attachment is 8-bit sRGB. */
+__device__ uint32_t color_write(const KzPipe& p, uint32_t dst, const float col[4], const float* u8tab = nullptr,
+                                bool srgb = false) {
+  /* sRGB attachments: red, green and blue are decoded to linear before blending and encoded after */
+  const float* thr = kz_srgb_thr_g;
   uint32_t out = dst;
   if (p.blend_enable) {
+    const float* dec = kz_srgb_dec_g;
     float s[4], dd[4];
     for (int i = 0; i < 4; i++) {
       s[i] = fminf(fmaxf(col[i], 0.0f), 1.0f);
       uint32_t u = (dst >> (8 * i)) & 0xFFu;
-      dd[i] = u8tab ? u8tab[u] : u8f(u);
+      dd[i] = srgb && i < 3 ? dec[u] : (u8tab ? u8tab[u] : u8f(u));
     }
     for (int i = 0; i < 4; i++) {
       if (!((p.write_mask >> i) & 1u)) continue;
@@ -597,11 +629,15 @@ __device__ uint32_t color_write(const KzPipe& p, uint32_t dst, const float col[4
       else
         r = blend_op(p.alpha_op, s[3], blend_factor(p.src_alpha, 3, s, dd, p.blend_const), dd[3],
                      blend_factor(p.dst_alpha, 3, s, dd, p.blend_const));
-      out = (out & ~(0xFFu << (8 * i))) | ((uint32_t)unorm8(r) << (8 * i));
+      uint32_t b = srgb && i < 3 ? srgb8(r, thr) : (uint32_t)unorm8(r);
+      out = (out & ~(0xFFu << (8 * i))) | (b << (8 * i));
     }
   } else {
-    for (int i = 0; i < 4; i++)
-      if ((p.write_mask >> i) & 1u) out = (out & ~(0xFFu << (8 * i))) | ((uint32_t)unorm8(col[i]) << (8 * i));
+    for (int i = 0; i < 4; i++) {
+      if (!((p.write_mask >> i) & 1u)) continue;
+      uint32_t b = srgb && i < 3 ? srgb8(col[i], thr) : (uint32_t)unorm8(col[i]);
+      out = (out & ~(0xFFu << (8 * i))) | (b << (8 * i));
+    }
   }
   return out;
 }
@@ -1651,7 +1687,8 @@ __device__ void vis_resolve_run(const Ctx& c, uint32_t item) {
       const KzPipe& p = c.pipes[s.pipe];
       if (has_color) {
         uint32_t dst = clear_c ? seg.clear_color : *color_px(seg, x, y);
-        *color_px(seg, x, y) = from_rgba(color_write(p, to_rgba(dst, seg.color_format), col), seg.color_format);
+        *color_px(seg, x, y) = from_rgba(color_write(p, to_rgba(dst, seg.color_format), col, nullptr,
+                                                     cf_srgb(seg.color_format)), seg.color_format);
       }
       if (has_depth && p.depth_test && p.depth_write) *depth_px(seg, x, y) = z;
       else if (has_depth && clear_d) *depth_px(seg, x, y) = seg.clear_depth;
@@ -1742,6 +1779,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
   bool clear_c = seg.color_load == KZ_LOAD_CLEAR, clear_d = seg.depth_load == KZ_LOAD_CLEAR;
   /* DS: a D16 / D24S8 attachment (integer depths, stencil); otherwise D32 without stencil */
   const bool has_st = DS && seg.depth_format == KZ_DF_D24S8, clear_s = has_st && seg.stencil_load == KZ_LOAD_CLEAR;
+  const bool srgb = cf_srgb(seg.color_format);
   if (ti.n == 0 && !clear_c && !clear_d && !clear_s) return;
   if (ti.n > KZ_SORT_CAP) {
     if (threadIdx.x == 0) atomicOr(&c.st->flags, KZ_STATUS_BIN_TOO_LARGE);
@@ -1851,7 +1889,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
       be.depth = (bp.depth_test ? 1u : 0u) | (bp.depth_write ? 2u : 0u) | (bp.depth_compare << 2);
       bool straight = bp.src_color == 6 && bp.dst_color == 7 && bp.color_op == 0 && bp.src_alpha == 6 &&
                       bp.dst_alpha == 7 && bp.alpha_op == 0;
-      be.blend = bp.blend_enable ? (straight ? 1u : 2u) : 0u;
+      be.blend = bp.blend_enable ? (straight && !srgb ? 1u : 2u) : 0u;
       be.write_mask = bp.write_mask;
       be.stencil = bp.stencil_test && has_st ? (1u | (bp.fs_discards ? 2u : 0u)) : 0u;
 #pragma unroll
@@ -1926,7 +1964,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
             if (dtest && (be.depth & 2u)) depm[s] = zs[s];
             if (!has_color) continue;
             if (be.blend == 1u) colm[s] = blend_straight_alpha(colm[s], col, u8tab, be.write_mask);
-            else colm[s] = color_write(c.pipes[be.s.pipe], colm[s], col, u8tab);
+            else colm[s] = color_write(c.pipes[be.s.pipe], colm[s], col, u8tab, srgb);
           }
           continue;
         }
@@ -1981,7 +2019,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
         if (dtest && (be.depth & 2u)) depv[q] = zq;
         if (!has_color) continue;
         if (be.blend == 1u) colv[q] = blend_straight_alpha(colv[q], col, u8tab, be.write_mask);
-        else colv[q] = color_write(c.pipes[be.s.pipe], colv[q], col, u8tab);
+        else colv[q] = color_write(c.pipes[be.s.pipe], colv[q], col, u8tab, srgb);
       }
     }
   }
@@ -2276,10 +2314,10 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_bin(KzFrame f, uin
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster(KzFrame f, uint32_t s) {
   kz_pdl_enter();
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ float u8tab[256];
+  __shared__ float u8tab[KZ_CTAB_FLOATS];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
-  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) u8tab[i] = u8f(i);
+  fill_color_tabs(u8tab);
   uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) raster_tile(c, t, smem, u8tab);
 }
@@ -2338,9 +2376,9 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
   __shared__ uint32_t item;
   __shared__ uint32_t scan_sh[KZ_THREADS + 1];
   __shared__ uint32_t geo_sh[40];
-  __shared__ float u8tab[256];
+  __shared__ float u8tab[KZ_CTAB_FLOATS];
   __shared__ uint32_t magic_tab[KZ_MAGIC_MAX + 1];
-  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) u8tab[i] = u8f(i);
+  fill_color_tabs(u8tab);
   fill_magic(magic_tab);
   KzStatus* st = reinterpret_cast<KzStatus*>(f.status);
   for (uint32_t s = f.first_segment; s < f.num_segments; s++) {

@@ -485,13 +485,13 @@ class SceneRun:
             # pass resolves the colour into self.color
             self.samples = r.create_image(scene.width, scene.height, vk.FORMAT_R8G8B8A8_UNORM,
                                           vk.IMAGE_USAGE_COLOR_ATTACHMENT, True, samples=ns)
-        self.color = r.create_image(scene.width, scene.height, vk.FORMAT_R8G8B8A8_UNORM,
+        self.color = r.create_image(scene.width, scene.height, vk.COLOR_FORMATS[scene.color_format],
                                     vk.IMAGE_USAGE_COLOR_ATTACHMENT, host_visible)
         self.depth = r.create_image(scene.width, scene.height, vk.DEPTH_FORMATS[scene.depth_format],
                                     vk.IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT,
                                     (host_visible if depth_host_visible is None else depth_host_visible) or ns > 1,
                                     samples=ns)
-        self.rp = r.render_pass(vk.FORMAT_R8G8B8A8_UNORM, True, depth_fmt=vk.DEPTH_FORMATS[scene.depth_format],
+        self.rp = r.render_pass(vk.COLOR_FORMATS[scene.color_format], True, depth_fmt=vk.DEPTH_FORMATS[scene.depth_format],
                                 samples=ns)
         views = [self.samples.view, self.depth.view, self.color.view] if ns > 1 else [self.color.view, self.depth.view]
         self.fb = r.framebuffer(self.rp, views, scene.width, scene.height)
@@ -597,7 +597,11 @@ class SceneRun:
             self.r.submit(self.cb)
 
     def read(self):
-        return self.r.read_image(self.color), self.r.read_image(self.depth)
+        """(colour bytes in R, G, B, A order whatever the attachment's byte order, depth texels)"""
+        color = self.r.read_image(self.color)
+        if self.scene.color_format.startswith("bgra"):
+            color = color[..., [2, 1, 0, 3]].copy()
+        return color, self.r.read_image(self.depth)
 
     def stats(self):
         return self.r.drv.stats(self.cb)

@@ -125,6 +125,12 @@ class Scene:
     stencil: Optional[dict] = None  # stencil test: {"front": StencilOp, "back": StencilOp} (d24s8 only)
     clear_stencil: int = 0
     samples: int = 1           # 1, or 4: multisampled colour and depth attachments, resolved at the end of the pass
+    color_format: str = "rgba8"  # colour attachment: "rgba8", "bgra8", "rgba8_srgb" or "bgra8_srgb" (the sRGB
+                                 # formats store sRGB-encoded red, green and blue)
+
+    @property
+    def srgb(self):
+        return self.color_format.endswith("_srgb")
 
     @property
     def triangles(self):

@@ -70,6 +70,10 @@ ST_RENDER_PASS_BEGIN_INFO = 43
 
 FORMAT_R8G8B8A8_UNORM = 37
 FORMAT_B8G8R8A8_UNORM = 44
+FORMAT_R8G8B8A8_SRGB = 43
+FORMAT_B8G8R8A8_SRGB = 50
+COLOR_FORMATS = {"rgba8": FORMAT_R8G8B8A8_UNORM, "bgra8": FORMAT_B8G8R8A8_UNORM,
+                 "rgba8_srgb": FORMAT_R8G8B8A8_SRGB, "bgra8_srgb": FORMAT_B8G8R8A8_SRGB}
 FORMAT_R32G32_SFLOAT = 103
 FORMAT_R32G32B32_SFLOAT = 106
 FORMAT_R32G32B32A32_SFLOAT = 109
@@ -578,6 +582,13 @@ class VkExtensionProperties(Structure):
     _fields_ = [("extensionName", ctypes.c_char * 256), ("specVersion", c_uint32)]
 
 
+class VkFormatProperties(Structure):
+    _fields_ = [("linearTilingFeatures", c_uint32), ("optimalTilingFeatures", c_uint32), ("bufferFeatures", c_uint32)]
+
+
+FORMAT_FEATURE_SAMPLED_IMAGE, FORMAT_FEATURE_COLOR_ATTACHMENT = 0x1, 0x80
+
+
 class VkBufferCopy(Structure):
     _fields_ = [("srcOffset", c_uint64), ("dstOffset", c_uint64), ("size", c_uint64)]
 
@@ -688,6 +699,7 @@ _PROTOS = {
     "vkCmdCopyImageToBuffer": (None, [H, H, c_int, H, c_uint32, P(VkBufferImageCopy)]),
     "vkCmdCopyBufferToImage": (None, [H, H, H, c_int, c_uint32, P(VkBufferImageCopy)]),
     "vkCmdFillBuffer": (None, [H, H, c_uint64, c_uint64, c_uint32]),
+    "vkGetPhysicalDeviceFormatProperties": (None, [H, c_int, P(VkFormatProperties)]),
     "vkCreateFence": (c_int, [H, P(VkFenceCreateInfo), c_void_p, P(H)]),
     "vkDestroyFence": (None, [H, H, c_void_p]),
     "vkResetFences": (c_int, [H, c_uint32, P(H)]),

@@ -7,6 +7,7 @@
  * Build: gcc -O2 -ffp-contract=off -fPIC -shared -pthread (see oracle/Makefile).
  */
 #include "kz_oracle.h"
+#include "../kazan_gb300/csrc/kz_srgb_table.h"
 
 #include <math.h>
 #include <pthread.h>
@@ -502,13 +503,31 @@ static float blend_op(uint32_t op, float s, float sf, float d, float df) {
   }
 }
 
+/* 8-bit sRGB: the encode steps (threshold k - 1 is the smallest float with code k) and the decode values
+ * of the sRGB transfer function, exact to the float (generated in 60-digit arithmetic) */
+static const float srgb_thr[255] = KZ_SRGB_THRESHOLDS;
+static const float srgb_dec[256] = KZ_SRGB_DECODE;
+
+uint8_t kzo_srgb8(float v) {
+  if (!(v > 0.0f)) return 0;
+  if (v >= 1.0f) return 255;
+  int n = 0;
+  while (n < 255 && srgb_thr[n] <= v) n++; /* the steps at or below v */
+  return (uint8_t)n;
+}
+
+/* one channel of a fragment output stored into the colour texel */
+static uint8_t store_channel(const kzo_draw* d, int i, float v) {
+  return d->srgb && i < 3 ? kzo_srgb8(v) : kzo_unorm8(v);
+}
+
 /* colour write or blend of one fragment output into the RGBA8 texel c */
 static void write_color(const kzo_draw* d, uint8_t* c, const float out[4]) {
   if (d->blend_enable) {
     float s[4], dst[4];
     for (int i = 0; i < 4; i++) {
       s[i] = fminf(fmaxf(out[i], 0.0f), 1.0f);
-      dst[i] = u8_to_f32(c[i]);
+      dst[i] = d->srgb && i < 3 ? srgb_dec[c[i]] : u8_to_f32(c[i]);
     }
     for (int i = 0; i < 4; i++) {
       if (!(d->write_mask & (1u << i))) continue;
@@ -519,11 +538,11 @@ static void write_color(const kzo_draw* d, uint8_t* c, const float out[4]) {
       else
         r = blend_op(d->alpha_op, s[3], blend_factor(d->src_alpha, 3, s, dst, d->blend_const), dst[3],
                      blend_factor(d->dst_alpha, 3, s, dst, d->blend_const));
-      c[i] = kzo_unorm8(r);
+      c[i] = store_channel(d, i, r);
     }
   } else {
     for (int i = 0; i < 4; i++)
-      if (d->write_mask & (1u << i)) c[i] = kzo_unorm8(out[i]);
+      if (d->write_mask & (1u << i)) c[i] = store_channel(d, i, out[i]);
   }
 }
 
@@ -639,28 +658,7 @@ static void raster_prep(const kzo_draw* draws, const prep* p, uint32_t width, ui
       float out[4];
       run_fs(d, var, out);
       if (d->depth_test && d->depth_write && depth) depth[pix] = zc;
-      uint8_t* c = color + pix * 4;
-      if (d->blend_enable) {
-        float s[4], dst[4];
-        for (int i = 0; i < 4; i++) {
-          s[i] = fminf(fmaxf(out[i], 0.0f), 1.0f);
-          dst[i] = u8_to_f32(c[i]);
-        }
-        for (int i = 0; i < 4; i++) {
-          if (!(d->write_mask & (1u << i))) continue;
-          float r;
-          if (i < 3)
-            r = blend_op(d->color_op, s[i], blend_factor(d->src_color, i, s, dst, d->blend_const), dst[i],
-                         blend_factor(d->dst_color, i, s, dst, d->blend_const));
-          else
-            r = blend_op(d->alpha_op, s[3], blend_factor(d->src_alpha, 3, s, dst, d->blend_const), dst[3],
-                         blend_factor(d->dst_alpha, 3, s, dst, d->blend_const));
-          c[i] = kzo_unorm8(r);
-        }
-      } else {
-        for (int i = 0; i < 4; i++)
-          if (d->write_mask & (1u << i)) c[i] = kzo_unorm8(out[i]);
-      }
+      write_color(d, color + pix * 4, out);
     }
   }
 }
@@ -789,6 +787,12 @@ int kzo_render_ds(uint32_t width, uint32_t height, uint8_t* color, float* depth,
   free(base);
   free(rects);
   return 0;
+}
+
+void kzo_clear_color_srgb(uint32_t width, uint8_t* color, const int32_t rect[4], const float rgba[4]) {
+  uint8_t px[4] = {kzo_srgb8(rgba[0]), kzo_srgb8(rgba[1]), kzo_srgb8(rgba[2]), kzo_unorm8(rgba[3])};
+  for (int32_t y = rect[1]; y < rect[3]; y++)
+    for (int32_t x = rect[0]; x < rect[2]; x++) memcpy(color + ((size_t)y * width + (size_t)x) * 4, px, 4);
 }
 
 void kzo_clear_color(uint32_t width, uint8_t* color, const int32_t rect[4], const float rgba[4]) {

@@ -86,6 +86,9 @@ typedef struct kzo_draw {
                                4 samples per pixel (sample s of pixel p at p * 4 + s), coverage, depth and
                                colour per sample, the fragment shader once per pixel at its centre (only D32,
                                no stencil) */
+  uint32_t srgb;            /* 1: the colour attachment is 8-bit sRGB: red, green and blue are stored as sRGB
+                               codes (the Vulkan specification's sRGB transfer function, rounded to nearest)
+                               and decoded to linear before blending; alpha stays linear */
 } kzo_draw;
 
 typedef struct kzo_stats {
@@ -120,6 +123,11 @@ float kzo_depth_value(float z, uint32_t depth_format);
 
 /* vkCmdClearColorImage / vkCmdClearDepthStencilImage restated for a rectangle */
 void kzo_clear_color(uint32_t width, uint8_t* color, const int32_t rect[4], const float rgba[4]);
+
+/* the 8-bit sRGB code of linear v, and the clear of an sRGB colour image (sRGB red, green, blue; linear
+ * alpha) */
+uint8_t kzo_srgb8(float v);
+void kzo_clear_color_srgb(uint32_t width, uint8_t* color, const int32_t rect[4], const float rgba[4]);
 void kzo_clear_depth(uint32_t width, float* depth, const int32_t rect[4], float value);
 
 /* f32 -> UNORM8 as the driver stores it */

@@ -40,7 +40,7 @@ class KzoDraw(ctypes.Structure):
                 ("alpha_op", ctypes.c_uint32), ("write_mask", ctypes.c_uint32), ("blend_const", ctypes.c_float * 4),
                 ("viewport", ctypes.c_float * 6), ("scissor", ctypes.c_int32 * 4), ("tex", KzoTexture),
                 ("stencil_test", ctypes.c_uint32), ("front", KzoStencil), ("back", KzoStencil),
-                ("samples", ctypes.c_uint32)]
+                ("samples", ctypes.c_uint32), ("srgb", ctypes.c_uint32)]
 
 
 class KzoStats(ctypes.Structure):
@@ -82,6 +82,9 @@ def lib():
         L.kzo_unorm8.restype = ctypes.c_uint8
         L.kzo_clear_color.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
                                       ctypes.POINTER(ctypes.c_float)]
+        L.kzo_clear_color_srgb.argtypes = L.kzo_clear_color.argtypes
+        L.kzo_srgb8.argtypes = [ctypes.c_float]
+        L.kzo_srgb8.restype = ctypes.c_uint8
         L.kzo_clear_depth.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
                                       ctypes.c_float]
         _LIB = L
@@ -113,7 +116,8 @@ def clear_images(scene):
     color = np.empty((h, w, 4), dtype=np.uint8)
     depth = np.empty((h, w), dtype=np.float32)
     rect = (ctypes.c_int32 * 4)(0, 0, w, h)
-    lib().kzo_clear_color(w, color.ctypes.data, rect, (ctypes.c_float * 4)(*scene.clear_color))
+    clear = lib().kzo_clear_color_srgb if getattr(scene, "srgb", False) else lib().kzo_clear_color
+    clear(w, color.ctypes.data, rect, (ctypes.c_float * 4)(*scene.clear_color))
     fmt = DEPTH_FORMAT[scene.depth_format]
     lib().kzo_clear_depth(w, depth.ctypes.data, rect, lib().kzo_depth_value(scene.clear_depth, fmt))
     return color, depth
@@ -159,6 +163,7 @@ def make_draws(scene, draws=None):
         if scene.texture is not None:
             k.tex = texture_struct(scene.texture)
         k.samples = scene.samples
+        k.srgb = int(getattr(scene, "srgb", False))
         if scene.stencil is not None:
             k.stencil_test = 1
             for face in ("front", "back"):
