@@ -116,7 +116,7 @@ static bool snapshot_descriptors(CommandBuffer* cb, const Pipeline* p, DrawRec& 
         if (!sb || e >= sb->count) continue;
         const DescriptorEntry& de = ds->entries[sb->first + e];
         uint32_t dyn_off = 0;
-        if (sb->type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC) {
+        if (sb->type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC || sb->type == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC) {
           const std::vector<uint32_t>& offs = cb->dyn_offsets[s];
           dyn_off = dyn < offs.size() ? offs[dyn] : 0;
           dyn++;

@@ -920,15 +920,18 @@ static void VKAPI_CALL kzDestroySampler(VkDevice, VkSampler s, const VkAllocatio
 
 static VkResult VKAPI_CALL kzCreateDescriptorSetLayout(VkDevice, const VkDescriptorSetLayoutCreateInfo* ci,
                                                        const VkAllocationCallbacks*, VkDescriptorSetLayout* out) {
-  /* api_impl.rs:4218; uniform buffers (plain and dynamic) and combined image samplers */
+  /* api_impl.rs:4218; uniform and storage buffers (plain and dynamic; storage buffers are read-only to the
+   * shaders) and combined image samplers */
   if (!ci || ci->sType != VK_STRUCTURE_TYPE_DESCRIPTOR_SET_LAYOUT_CREATE_INFO) return VK_ERROR_INITIALIZATION_FAILED;
   auto info = std::make_shared<SetLayoutInfo>();
   for (uint32_t i = 0; i < ci->bindingCount; i++) {
     const VkDescriptorSetLayoutBinding& b = ci->pBindings[i];
     if (b.descriptorType != VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER &&
         b.descriptorType != VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC &&
+        b.descriptorType != VK_DESCRIPTOR_TYPE_STORAGE_BUFFER &&
+        b.descriptorType != VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC &&
         b.descriptorType != VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER) {
-      log_error("descriptor type %d is not supported (uniform buffers and combined image samplers are)",
+      log_error("descriptor type %d is not supported (uniform and storage buffers, combined image samplers are)",
                 (int)b.descriptorType);
       return VK_ERROR_FEATURE_NOT_PRESENT;
     }
@@ -946,7 +949,8 @@ static VkResult VKAPI_CALL kzCreateDescriptorSetLayout(VkDevice, const VkDescrip
   for (SetBinding& b : info->bindings) {
     b.first = info->descriptors;
     info->descriptors += b.count;
-    if (b.type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC) info->dynamic += b.count;
+    if (b.type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC || b.type == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC)
+      info->dynamic += b.count;
   }
   if (info->descriptors > KZ_MAX_DESC_SLOTS) return VK_ERROR_FEATURE_NOT_PRESENT;
   DescriptorSetLayout* l = new DescriptorSetLayout();
@@ -1259,9 +1263,11 @@ static VkResult create_graphics_pipeline(const VkGraphicsPipelineCreateInfo& ci,
       const SetBinding* sb = p->layout && b.set < p->layout->sets.size() ? p->layout->sets[b.set]->find(b.binding)
                                                                          : nullptr;
       bool ok = sb && sb->count >= b.count &&
-                (b.kind == 1 ? sb->type == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER
-                             : (sb->type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER ||
-                                sb->type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC));
+                (b.kind == 1   ? sb->type == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER
+                 : b.kind == 2 ? (sb->type == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER ||
+                                  sb->type == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC)
+                               : (sb->type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER ||
+                                  sb->type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC));
       if (!ok) {
         log_error("pipeline: set %u binding %u of the shaders is missing from the pipeline layout or has another type",
                   b.set, b.binding);

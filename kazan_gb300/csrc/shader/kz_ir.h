@@ -34,6 +34,7 @@ enum class Op : uint8_t {
   StOut,   /* 32-bit store of a to the stage output block at byte offset imm */
   LdUbo,   /* dst = 32-bit load from the uniform buffer of binding imm2 (set << 16 | binding) at byte offset
               imm, plus the byte offset in register a when a >= 0 */
+  LdDescRange, /* dst = bytes of the buffer range bound to binding imm2 (its descriptor's range) */
   Tex,     /* dst..dst+3 (f32 registers allocated in a row) = the combined image sampler of binding imm2,
               array element imm (plus register c when c >= 0), sampled at (a, b) */
   TexFetch,/* dst..dst+3 = texel (a, b) (integers; outside the image: 0) of binding imm2, element imm (+ c) */
@@ -103,7 +104,7 @@ struct Interface {
   /* descriptor bindings the stage declares (every module-scope Uniform / UniformConstant variable) */
   struct Binding {
     uint32_t set = 0, binding = 0;
-    uint32_t kind = 0;   /* 0 uniform buffer, 1 combined image sampler */
+    uint32_t kind = 0;   /* 0 uniform buffer, 1 combined image sampler, 2 storage buffer */
     uint32_t count = 1;  /* array elements */
     uint32_t bytes = 0;  /* uniform buffer: bytes of the block (the range a descriptor must cover) */
   };

@@ -274,6 +274,17 @@ class Emitter {
           line(buf);
           break;
         }
+        case Op::LdDescRange: { /* KzDescriptor::range of the binding's slot in the draw's snapshot */
+          uint32_t slot = slot_of(lay, i.imm2);
+          if (slot == ~0u) { /* not in the layout (pipeline creation rejects this) */
+            line("mov.b32 " + R(i.dst) + ", 0;");
+            break;
+          }
+          std::snprintf(buf, sizeof buf, "ld.global.nc.u32 %s, [%%kzpush+%u];", R(i.dst).c_str(),
+                        KZ_DESC_OFFSET + 32u * slot + 8u);
+          line(buf);
+          break;
+        }
         case Op::Tex:
         case Op::TexFetch: {
           /* descriptor address (generic): push + KZ_DESC_OFFSET + 32 * (slot + element) */

@@ -84,6 +84,10 @@ struct Var {
   uint32_t storage = 0;
   uint32_t type = 0; /* pointee type */
   std::vector<Slot> slots;
+  /* a storage block ending in a runtime-sized array: the array's byte offset in the block, its element
+   * stride, and the bytes of an element the shader can read (its slots hold element 0) */
+  bool has_rt = false;
+  uint32_t rt_base = 0, rt_stride = 0, rt_end = 0;
 };
 
 struct Place {
@@ -95,6 +99,7 @@ struct Place {
    * first + dyn * dyn_stride (constant indices after it are already in `first`) */
   int32_t dyn = -1;
   uint32_t dyn_stride = 0, dyn_count = 0;
+  bool rt = false; /* dyn indexes the variable's runtime-sized array: its length comes from the descriptor */
 };
 
 struct Val {
@@ -337,6 +342,9 @@ class Translator {
   Space block_space_ = Space::Push; /* what assign_push lays out: push constants or a uniform block */
   uint32_t block_key_ = 0;
   uint32_t block_bytes_ = 0;
+  bool block_storage_ = false; /* laying out a storage block: a last runtime-sized array member is allowed */
+  bool block_rt_ = false;
+  uint32_t block_rt_base_ = 0, block_rt_stride_ = 0, block_rt_end_ = 0;
 
   /* ---- function body ---- */
   bool translate_entry();
@@ -715,6 +723,30 @@ void Translator::assign_push(uint32_t t, uint32_t byte, std::vector<Slot>& slots
         assign_push(ti.members[i], byte + off, slots, ms, rm);
       }
       break;
+    case TypeInfo::RuntimeArray: {
+      /* the last member of a storage block: element 0 is laid out; other elements are addressed at run
+       * time from the array's stride, and the bound range limits the index */
+      if (block_space_ != Space::Ubo || !block_storage_ || block_rt_) {
+        fail("a runtime-sized array is supported only as the last member of a storage buffer");
+        break;
+      }
+      uint32_t stride = 0;
+      decs_[t].get(DecArrayStride, stride);
+      if (!stride) stride = 4 * scalars(ti.elem);
+      size_t first = slots.size();
+      assign_push(ti.elem, byte, slots, stride_hint, row_major);
+      uint32_t end = 0;
+      for (size_t k = first; k < slots.size(); k++) end = std::max(end, slots[k].offset + 4 - byte);
+      if (end > stride) {
+        fail("runtime-sized array elements wider than their stride");
+        break;
+      }
+      block_rt_ = true;
+      block_rt_base_ = byte;
+      block_rt_stride_ = stride;
+      block_rt_end_ = end;
+      break;
+    }
     default: fail("unsupported push-constant member type"); break;
   }
 }
@@ -728,7 +760,7 @@ bool Translator::layout_interface(uint32_t var_id, Var& v) {
   } else if (v.storage == SCPushConstant) {
     block_space_ = Space::Push;
     assign_push(v.type, 0, v.slots, 0, false);
-  } else if (v.storage == SCUniform || v.storage == SCUniformConstant) {
+  } else if (v.storage == SCUniform || v.storage == SCUniformConstant || v.storage == SCStorageBuffer) {
     if (!layout_descriptor(var_id, v)) return false;
   } else if (v.storage == SCPrivate || v.storage == SCFunction) {
     std::vector<Ty> tys;
@@ -829,15 +861,26 @@ bool Translator::layout_descriptor(uint32_t var_id, Var& v) {
       v.slots.push_back(s);
     }
   } else {
-    if (t != v.type) return fail("arrays of uniform blocks are not supported");
-    if (decs_[t].has(DecBufferBlock)) return fail("storage buffers are not supported");
+    /* uniform blocks, and storage blocks (StorageBuffer storage class, or Uniform with BufferBlock), which
+     * shaders read only: stores to them are refused */
+    const bool storage = v.storage == SCStorageBuffer || decs_[t].has(DecBufferBlock);
+    if (t != v.type) return fail("arrays of uniform or storage blocks are not supported");
     if (ti.kind != TypeInfo::Struct) return fail("a Uniform variable that is not a block");
     block_space_ = Space::Ubo;
     block_key_ = key;
     block_bytes_ = 0;
+    block_storage_ = storage;
+    block_rt_ = false;
     assign_push(t, 0, v.slots, 0, false);
     block_space_ = Space::Push;
-    b.kind = 0;
+    block_storage_ = false;
+    if (block_rt_) {
+      v.has_rt = true;
+      v.rt_base = block_rt_base_;
+      v.rt_stride = block_rt_stride_;
+      v.rt_end = block_rt_end_;
+    }
+    b.kind = storage ? 2 : 0;
     b.bytes = block_bytes_;
   }
   out_.iface.bindings.push_back(b);
@@ -851,7 +894,21 @@ bool Translator::load(const Place& p, Val& v) {
      * array, then addressed directly */
     const Var& var = vars_[p.var];
     const Slot& s0 = var.slots[p.first];
-    int32_t lim = konst(Ty::B32, p.dyn_count - 1);
+    int32_t lim;
+    if (p.rt) {
+      /* the last element the bound range holds: (range - base - element bytes) / stride (recording checks
+       * that the range covers the block with one element) */
+      Inst r;
+      r.op = Op::LdDescRange;
+      r.ty = Ty::B32;
+      r.dst = fn_.reg(Ty::B32);
+      r.imm2 = s0.key;
+      fn_.emit(r);
+      int32_t avail = op2(Op::ISub, Ty::B32, r.dst, konst(Ty::B32, var.rt_base + var.rt_end));
+      lim = op2(Op::UDiv, Ty::B32, avail, konst(Ty::B32, var.rt_stride));
+    } else {
+      lim = konst(Ty::B32, p.dyn_count - 1);
+    }
     int32_t idx = op3(Op::Selp, Ty::B32, lim, p.dyn, op2(Op::SetpU, Ty::Pred, p.dyn, lim, CmpGt));
     v.type = p.type;
     v.regs.clear();
@@ -861,7 +918,8 @@ bool Translator::load(const Place& p, Val& v) {
       v.regs.push_back(op2(Op::IAdd, Ty::B32, idx, konst(Ty::B32, s0.offset)));
       return true;
     }
-    uint32_t stride = p.dyn_count > 1 && p.first + p.dyn_stride < var.slots.size()
+    uint32_t stride = p.rt ? var.rt_stride
+                  : p.dyn_count > 1 && p.first + p.dyn_stride < var.slots.size()
                           ? var.slots[p.first + p.dyn_stride].offset - s0.offset
                           : 0;
     int32_t boff = op2(Op::IMul, Ty::B32, idx, konst(Ty::B32, stride));
@@ -978,6 +1036,8 @@ bool Translator::load(const Place& p, Val& v) {
 
 bool Translator::store(const Place& p, const Val& v) {
   Var& var = vars_[p.var];
+  if (p.rt || var.storage == SCUniform || var.storage == SCStorageBuffer)
+    return fail("writes to uniform and storage buffers are not supported (shaders only read them)");
   if (p.dyn >= 0) {
     /* run-time index: every candidate element keeps its value unless the index names it */
     for (uint32_t e = 0; e < p.dyn_count; e++) {
@@ -1593,6 +1653,26 @@ bool Translator::do_insn(const Insn& in) {
       if (it == places_.end()) return fail("access chain on something that is not a variable");
       Place p = it->second;
       for (size_t i = 3; i < o.size(); i++) {
+        if (ty(p.type).kind == TypeInfo::RuntimeArray) {
+          /* an element of a storage block's runtime-sized array: a run-time index (a constant one too),
+           * limited by the bound range when it is loaded */
+          if (!vars_[p.var].has_rt || p.dyn >= 0) return fail("unsupported access to a runtime-sized array");
+          auto ci = consts_.find(o[i]);
+          int32_t reg;
+          if (ci != consts_.end() && !ci->second.second.empty()) {
+            reg = konst(Ty::B32, ci->second.second[0]);
+          } else {
+            Val* iv = val(o[i]);
+            if (!iv || iv->regs.empty() || reg_ty(iv->regs[0]) != Ty::B32) return fail("bad run-time index");
+            reg = iv->regs[0];
+          }
+          p.dyn = reg;
+          p.dyn_stride = scalars(ty(p.type).elem);
+          p.dyn_count = 0;
+          p.rt = true;
+          p.type = ty(p.type).elem;
+          continue;
+        }
         auto c = consts_.find(o[i]);
         if (c == consts_.end() || c->second.second.empty()) {
           /* an index known at run time: into an array, matrix or vector (one such index per chain) */

@@ -58,6 +58,8 @@ ST_COPY_DESCRIPTOR_SET = 36
 DESCRIPTOR_COMBINED_IMAGE_SAMPLER = 1
 DESCRIPTOR_UNIFORM_BUFFER = 6
 DESCRIPTOR_UNIFORM_BUFFER_DYNAMIC = 8
+DESCRIPTOR_STORAGE_BUFFER = 7
+DESCRIPTOR_STORAGE_BUFFER_DYNAMIC = 9
 FILTER_NEAREST, FILTER_LINEAR = 0, 1
 ADDRESS_REPEAT, ADDRESS_MIRRORED_REPEAT, ADDRESS_CLAMP_TO_EDGE, ADDRESS_CLAMP_TO_BORDER, ADDRESS_MIRROR_CLAMP = 0, 1, 2, 3, 4
 VK_ERROR_OUT_OF_POOL_MEMORY = -1000069000
@@ -96,6 +98,7 @@ IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL = 7
 BUFFER_USAGE_TRANSFER_SRC = 0x1
 BUFFER_USAGE_TRANSFER_DST = 0x2
 BUFFER_USAGE_UNIFORM = 0x10
+BUFFER_USAGE_STORAGE = 0x20
 BUFFER_USAGE_INDEX = 0x40
 BUFFER_USAGE_VERTEX = 0x80
 BUFFER_USAGE_INDIRECT = 0x100

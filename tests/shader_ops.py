@@ -126,3 +126,39 @@ def fma(a, b, c):
     if not (np.isfinite(a) and np.isfinite(b) and np.isfinite(c)):
         return f32(np.float64(a) * np.float64(b) + np.float64(c))
     return round_f32(Fraction(float(a)) * Fraction(float(b)) + Fraction(float(c)))
+
+
+# ---- a read-only storage buffer (set 0, binding 0) with a runtime-sized array ----
+OpConvertFToU, OpBitwiseXor, OpTypeRuntimeArray = 109, 198, 29
+DecBufferBlock, DecArrayStride = 3, 6
+SSBO_BASE, SSBO_STRIDE = 16, 8  # block { uint bias; uint pad[3]; uvec2 vals[]; } in std430
+
+
+def storage_fs(store=False):
+    """fragment shader reading b.vals[uint(a.x)].y ^ b.bias from the storage block
+    `layout(set = 0, binding = 0) buffer B { uint bias; uint pad[3]; uvec2 vals[]; } b` (Uniform storage
+    class with BufferBlock); `store`: also writes b.bias (which translation must refuse)"""
+
+    def body(c):
+        m = c.m
+        uv2 = m.vec(c.u32, 2)
+        rt = m._type(("rtarr", uv2), OpTypeRuntimeArray, uv2)
+        m.decorate(rt, DecArrayStride, SSBO_STRIDE)
+        pad = m.array(c.u32, 3)
+        m.decorate(pad, DecArrayStride, 4)
+        blk = m.struct(c.u32, pad, rt)
+        for k, off in enumerate((0, 4, SSBO_BASE)):
+            m.member_decorate(blk, k, sa.DecOffset, off)
+        m.decorate(blk, DecBufferBlock)
+        var = m.variable(sa.SCUniform, m.ptr(sa.SCUniform, blk))
+        m.decorate(var, sa.DecDescriptorSet, 0)
+        m.decorate(var, sa.DecBinding, 0)
+        pu = m.ptr(sa.SCUniform, c.u32)
+        idx = m.res(OpConvertFToU, c.u32, c.x)
+        v = m.res(sa.OpLoad, c.u32, m.res(sa.OpAccessChain, pu, var, m.ci(2), idx, m.ci(1)))
+        bias_p = m.res(sa.OpAccessChain, pu, var, m.ci(0))
+        if store:
+            m.op(sa.OpStore, bias_p, v)
+        return m.res(OpBitwiseXor, c.u32, v, m.res(sa.OpLoad, c.u32, bias_p)), "u32"
+
+    return op_fs(body)

@@ -183,8 +183,24 @@ def test_descriptor_bindings_translate_and_link(built):
     assert img[:4] == b"\x7fELF"
 
 
+def test_storage_buffer_translates_read_only(built):
+    """a storage block with a runtime-sized array: binding kind 2 whose range must cover the block with one
+    element (16 + 8 bytes); the PTX limits the index by the descriptor's range (byte 8 of its slot); a
+    store into the block is refused"""
+    import shader_ops
+    fs = shader.Shader(shader_ops.storage_fs(), shader.FRAGMENT)
+    assert fs.bindings() == [(0, 0, 2, 1, 24)]
+    ptx = shader.emit_ptx([(shader.Shader(spirv_asm.color_vs(), shader.VERTEX), fs)],
+                          [shader.layout([(0, 0, 4, 0), (1, 0, 4, 16)], [32])], [{(0, 0): 3}])
+    assert "[%kzpush+232]" in ptx  # 128 + 32 * 3 + 8: the range of descriptor slot 3
+    assert "div.u32" in ptx
+    shader.link(ptx)
+    with pytest.raises(shader.ShaderError, match="storage buffers"):
+        shader.Shader(shader_ops.storage_fs(store=True), shader.FRAGMENT)
+
+
 def test_unsupported_descriptor_forms_are_rejected(built):
-    """separate images and samplers and storage buffers are reported, not mistranslated"""
+    """separate images and samplers are reported, not mistranslated"""
     from kazan_gb300.spirv_asm import (Module, CapShader, SCUniformConstant, OpTypeImage, ExecFragment,
                                        ModeOriginUpperLeft, DecDescriptorSet, DecBinding, _begin_main, _end_main,
                                        _io, SCOutput)
