@@ -67,7 +67,7 @@ KZ_API size_t kzShaderEmitPtx(const void* const* vs, const void* const* fs, cons
 /* Descriptor bindings a compiled stage declares (module-scope Uniform / UniformConstant variables). */
 typedef struct KzShaderBinding {
   uint32_t set, binding;
-  uint32_t kind;   /* 0 uniform buffer, 1 combined image sampler, 2 storage buffer */
+  uint32_t kind;   /* 0 uniform buffer, 1 combined image sampler, 2 storage buffer, 3 sampled image, 4 sampler */
   uint32_t count;  /* array elements */
   uint32_t bytes;  /* uniform buffer: bytes of the block */
 } KzShaderBinding;

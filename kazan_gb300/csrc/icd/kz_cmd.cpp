@@ -123,7 +123,10 @@ static bool snapshot_descriptors(CommandBuffer* cb, const Pipeline* p, DrawRec& 
         }
         if (!de.written) continue;
         KzDescriptor& d = dr.desc[L.slot_base[s] + lb.first + e];
-        if (sb->type == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER) {
+        if (sb->type == VK_DESCRIPTOR_TYPE_SAMPLER) {
+          d.sampler = de.sampler;
+          d.range = 1; /* written */
+        } else if (sb->type == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER || sb->type == VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE) {
           if (!de.view || !de.view->image || !de.view->image->mem) continue;
           const Image* img = de.view->image;
           d.addr = (uint64_t)(uintptr_t)img->ptr();
@@ -131,7 +134,7 @@ static bool snapshot_descriptors(CommandBuffer* cb, const Pipeline* p, DrawRec& 
           d.height = img->height;
           d.pitch = img->pitch;
           d.format = color_format(img->format);
-          d.sampler = de.sampler;
+          d.sampler = sb->type == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER ? de.sampler : 0u;
           dr.desc_reads.push_back(img->mem);
         } else {
           if (!de.buffer || !de.buffer->mem) continue;
@@ -149,10 +152,13 @@ static bool snapshot_descriptors(CommandBuffer* cb, const Pipeline* p, DrawRec& 
     const SetBinding* lb = b.set < L.sets.size() ? L.sets[b.set]->find(b.binding) : nullptr;
     for (uint32_t e = 0; lb && e < b.count; e++) {
       const KzDescriptor& d = dr.desc[L.slot_base[b.set] + lb->first + e];
-      bool ok = b.kind == 1 ? d.addr && d.width && d.height && d.format != KZ_CF_NONE : d.addr && d.range >= b.bytes;
+      const bool image = b.kind == 1 || b.kind == 3;
+      bool ok = image         ? d.addr && d.width && d.height && d.format != KZ_CF_NONE
+                : b.kind == 4 ? d.range != 0
+                              : d.addr && d.range >= b.bytes;
       if (!ok) {
         log_error("draw: set %u binding %u element %u is not bound or not written with a %s", b.set, b.binding, e,
-                  b.kind == 1 ? "RGBA8/BGRA8 image" : "buffer range covering the uniform block");
+                  image ? "RGBA8/BGRA8 image" : b.kind == 4 ? "sampler" : "buffer range covering the block");
         cb->record_error = VK_ERROR_INITIALIZATION_FAILED;
         return false;
       }

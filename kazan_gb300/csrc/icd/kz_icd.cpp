@@ -930,8 +930,10 @@ static VkResult VKAPI_CALL kzCreateDescriptorSetLayout(VkDevice, const VkDescrip
         b.descriptorType != VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC &&
         b.descriptorType != VK_DESCRIPTOR_TYPE_STORAGE_BUFFER &&
         b.descriptorType != VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC &&
-        b.descriptorType != VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER) {
-      log_error("descriptor type %d is not supported (uniform and storage buffers, combined image samplers are)",
+        b.descriptorType != VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER &&
+        b.descriptorType != VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE && b.descriptorType != VK_DESCRIPTOR_TYPE_SAMPLER) {
+      log_error("descriptor type %d is not supported (uniform and storage buffers, samplers, sampled images and "
+                "combined image samplers are)",
                 (int)b.descriptorType);
       return VK_ERROR_FEATURE_NOT_PRESENT;
     }
@@ -940,7 +942,8 @@ static VkResult VKAPI_CALL kzCreateDescriptorSetLayout(VkDevice, const VkDescrip
     sb.binding = b.binding;
     sb.type = b.descriptorType;
     sb.count = b.descriptorCount;
-    if (b.descriptorType == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER && b.pImmutableSamplers)
+    if ((b.descriptorType == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER || b.descriptorType == VK_DESCRIPTOR_TYPE_SAMPLER) &&
+        b.pImmutableSamplers)
       for (uint32_t k = 0; k < b.descriptorCount; k++) sb.immutable.push_back(from_handle<Sampler>(b.pImmutableSamplers[k])->bits);
     info->bindings.push_back(sb);
   }
@@ -1005,7 +1008,11 @@ static VkResult VKAPI_CALL kzAllocateDescriptorSets(VkDevice, const VkDescriptor
     s->layout = from_handle<DescriptorSetLayout>(ai->pSetLayouts[i])->info;
     s->entries.resize(s->layout->descriptors);
     for (const SetBinding& b : s->layout->bindings)
-      for (uint32_t k = 0; k < b.count && k < b.immutable.size(); k++) s->entries[b.first + k].sampler = b.immutable[k];
+      for (uint32_t k = 0; k < b.count && k < b.immutable.size(); k++) {
+        s->entries[b.first + k].sampler = b.immutable[k];
+        /* a sampler binding with immutable samplers is complete without a write */
+        if (b.type == VK_DESCRIPTOR_TYPE_SAMPLER) s->entries[b.first + k].written = true;
+      }
     s->pool = p;
     p->sets.push_back(s);
     out[i] = to_handle<VkDescriptorSet>(s);
@@ -1059,9 +1066,12 @@ static void VKAPI_CALL kzUpdateDescriptorSets(VkDevice, uint32_t nw, const VkWri
                                  DescriptorEntry& d = s->entries[e];
                                  if (b.type != w.descriptorType) return;
                                  d.written = true;
-                                 if (w.descriptorType == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER) {
-                                   d.view = from_handle<ImageView>(w.pImageInfo[k].imageView);
-                                   if (b.immutable.empty())
+                                 if (w.descriptorType == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER ||
+                                     w.descriptorType == VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE ||
+                                     w.descriptorType == VK_DESCRIPTOR_TYPE_SAMPLER) {
+                                   if (w.descriptorType != VK_DESCRIPTOR_TYPE_SAMPLER)
+                                     d.view = from_handle<ImageView>(w.pImageInfo[k].imageView);
+                                   if (w.descriptorType != VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE && b.immutable.empty())
                                      d.sampler = from_handle<Sampler>(w.pImageInfo[k].sampler)->bits;
                                  } else {
                                    d.buffer = from_handle<Buffer>(w.pBufferInfo[k].buffer);
@@ -1264,6 +1274,8 @@ static VkResult create_graphics_pipeline(const VkGraphicsPipelineCreateInfo& ci,
                                                                          : nullptr;
       bool ok = sb && sb->count >= b.count &&
                 (b.kind == 1   ? sb->type == VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER
+                 : b.kind == 3 ? sb->type == VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE
+                 : b.kind == 4 ? sb->type == VK_DESCRIPTOR_TYPE_SAMPLER
                  : b.kind == 2 ? (sb->type == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER ||
                                   sb->type == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC)
                                : (sb->type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER ||

@@ -71,6 +71,9 @@ struct Inst {
   int32_t dst = -1, a = -1, b = -1, c = -1;
   uint32_t imm = 0;
   uint32_t imm2 = 0;
+  /* Tex through OpSampledImage of a separate sampler: the sampler's binding (set << 16 | binding) and
+   * array element; ~0u for a combined image sampler */
+  uint32_t smp = ~0u, smp_elem = 0;
 };
 
 struct Function {
@@ -104,7 +107,8 @@ struct Interface {
   /* descriptor bindings the stage declares (every module-scope Uniform / UniformConstant variable) */
   struct Binding {
     uint32_t set = 0, binding = 0;
-    uint32_t kind = 0;   /* 0 uniform buffer, 1 combined image sampler, 2 storage buffer */
+    uint32_t kind = 0;   /* 0 uniform buffer, 1 combined image sampler, 2 storage buffer, 3 sampled image,
+                          4 sampler */
     uint32_t count = 1;  /* array elements */
     uint32_t bytes = 0;  /* uniform buffer: bytes of the block (the range a descriptor must cover) */
   };

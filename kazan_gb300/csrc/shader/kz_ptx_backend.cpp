@@ -75,6 +75,7 @@ class Emitter {
   std::map<uint32_t, std::string> ubo_regs;  /* uniform-buffer binding -> register holding its address */
   uint32_t nu = 0;                            /* %kzu registers */
   bool uses_tex = false, uses_fetch = false;  /* calls kz_tex2d / kz_tex_fetch */
+  bool uses_sep = false;                      /* samples through a separate sampler (a local descriptor) */
   uint32_t copy = 0;                          /* VertexPos3: which vertex the body computes */
 
   static uint32_t slot_of(const VertexLayout* lay, uint32_t key) {
@@ -298,6 +299,21 @@ class Emitter {
           if (i.c >= 0) {
             line("mul.wide.u32 %kzoff, " + R(i.c) + ", 32;");
             line("add.s64 %kzd, %kzd, %kzoff;");
+          }
+          const uint32_t sslot = i.smp == ~0u ? ~0u : slot_of(lay, i.smp);
+          if (i.op == Op::Tex && sslot != ~0u) {
+            /* a separate sampler: a local copy of the image's descriptor with the sampler's state word
+             * (KzDescriptor::sampler, byte 28) in place of its own */
+            line("ld.v4.u32 {%kzs0, %kzs1, %kzs2, %kzs3}, [%kzd];");
+            line("ld.v4.u32 {%kzs4, %kzs5, %kzs6, %kzs7}, [%kzd+16];");
+            std::snprintf(buf, sizeof buf, "ld.global.nc.u32 %%kzs7, [%%kzpush+%u];",
+                          KZ_DESC_OFFSET + 32u * (sslot + i.smp_elem) + 28u);
+            line(buf);
+            line("st.local.v4.u32 [kzsd], {%kzs0, %kzs1, %kzs2, %kzs3};");
+            line("st.local.v4.u32 [kzsd+16], {%kzs4, %kzs5, %kzs6, %kzs7};");
+            line("mov.u64 %kzd, kzsd;");
+            line("cvta.local.u64 %kzd, %kzd;");
+            uses_sep = true;
           }
           const char* fnn = i.op == Op::Tex ? "kz_tex2d" : "kz_tex_fetch";
           const char* at = i.op == Op::Tex ? "f32" : "b32";
@@ -553,6 +569,7 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
        "  .reg .b64 %kzin, %kzpush, %kzout, %kzdraw, %kzoff, %kzpg, %kzub, %kzd;\n  .reg .b64 %kzvb<8>;\n"
        "  .reg .pred %kzp;\n";
   if (e.nu) s += "  .reg .b64 %kzu<" + std::to_string(e.nu) + ">;\n";
+  if (e.uses_sep) s += "  .reg .b32 %kzs<8>;\n  .local .align 16 .b8 kzsd[32];\n";
   uses_tex |= e.uses_tex;
   uses_fetch |= e.uses_fetch;
   if (e.nk) s += "  .reg .b32 %kp<" + std::to_string(e.nk) + ">;\n";

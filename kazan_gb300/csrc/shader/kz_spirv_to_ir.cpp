@@ -109,6 +109,9 @@ struct Val {
    * tex_dyn, the element in regs[0] */
   bool is_tex = false, tex_dyn = false;
   uint32_t tex_key = 0, tex_elem = 0;
+  /* OpSampledImage of a separate image and sampler: the sampler's binding and array element */
+  bool has_smp = false;
+  uint32_t smp_key = 0, smp_elem = 0;
 };
 
 struct PhiInfo {
@@ -818,6 +821,10 @@ bool Translator::image_sample(const Insn& in) {
   i.c = img->tex_dyn ? img->regs[0] : -1;
   i.imm = img->tex_dyn ? 0u : img->tex_elem;
   i.imm2 = img->tex_key;
+  if (img->has_smp) {
+    i.smp = img->smp_key;
+    i.smp_elem = img->smp_elem;
+  }
   fn_.emit(i);
   Val r;
   r.type = o[0];
@@ -847,11 +854,12 @@ bool Translator::layout_descriptor(uint32_t var_id, Var& v) {
   }
   const TypeInfo& ti = ty(t);
   if (v.storage == SCUniformConstant) {
-    if (ti.kind == TypeInfo::Image || ti.kind == TypeInfo::Sampler)
-      return fail("separate images and samplers are not supported (combined image samplers are)");
-    if (ti.kind != TypeInfo::SampledImage || !count) return fail("unsupported UniformConstant variable");
-    if (ty(ti.elem).count != 1) return fail("only 2D images are supported");
-    b.kind = 1;
+    /* combined image samplers, and separate sampled images and samplers (combined by OpSampledImage) */
+    if (!count || (ti.kind != TypeInfo::SampledImage && ti.kind != TypeInfo::Image && ti.kind != TypeInfo::Sampler))
+      return fail("unsupported UniformConstant variable");
+    if ((ti.kind == TypeInfo::SampledImage && ty(ti.elem).count != 1) || (ti.kind == TypeInfo::Image && ti.count != 1))
+      return fail("only 2D images are supported");
+    b.kind = ti.kind == TypeInfo::SampledImage ? 1 : ti.kind == TypeInfo::Image ? 3 : 4;
     b.count = count;
     for (uint32_t k = 0; k < count; k++) {
       Slot s;
@@ -974,8 +982,8 @@ bool Translator::load(const Place& p, Val& v) {
   v.regs.clear();
   if (p.first < var.slots.size() && var.slots[p.first].space == Space::Tex) {
     const TypeInfo& ti = ty(p.type);
-    if (ti.kind != TypeInfo::SampledImage && ti.kind != TypeInfo::Image)
-      return fail("load of a whole array of combined image samplers");
+    if (ti.kind != TypeInfo::SampledImage && ti.kind != TypeInfo::Image && ti.kind != TypeInfo::Sampler)
+      return fail("load of a whole array of images or samplers");
     v.is_tex = true;
     v.tex_key = var.slots[p.first].key;
     v.tex_elem = var.slots[p.first].offset;
@@ -1750,8 +1758,19 @@ bool Translator::do_insn(const Insn& in) {
       vals_[o[1]].type = o[0];
       return true;
     }
-    case OpSampledImage:
-      return fail("OpSampledImage: separate images and samplers are not supported (combined image samplers are)");
+    case OpSampledImage: { /* a separate image and sampler combined: the image's binding, the sampler's state */
+      Val* img = val(o[2]);
+      Val* smp = val(o[3]);
+      if (!img || !smp || !img->is_tex || !smp->is_tex) return fail("OpSampledImage of something that is not a descriptor");
+      if (smp->tex_dyn) return fail("run-time indices into arrays of samplers are not supported");
+      Val r = *img;
+      r.type = o[0];
+      r.has_smp = true;
+      r.smp_key = smp->tex_key;
+      r.smp_elem = smp->tex_elem;
+      vals_[o[1]] = r;
+      return true;
+    }
     case OpImageSampleImplicitLod:
     case OpImageSampleExplicitLod:
     case OpImageSampleProjImplicitLod:

@@ -338,10 +338,11 @@ class Renderer:
         check("vkAllocateDescriptorSets", self.drv.vkAllocateDescriptorSets(self.device, byref(ai), sets))
         return [c_void_p(s) for s in sets]
 
-    def write_image_descriptor(self, dset, binding, element, sampler, image):
-        ii = vk.VkDescriptorImageInfo(sampler, image.view, vk.IMAGE_LAYOUT_GENERAL)
+    def write_image_descriptor(self, dset, binding, element, sampler, image, dtype=vk.DESCRIPTOR_COMBINED_IMAGE_SAMPLER):
+        """a combined image sampler, or (dtype) a sampled image (sampler None) or a sampler (image None)"""
+        ii = vk.VkDescriptorImageInfo(sampler, image.view if image is not None else None, vk.IMAGE_LAYOUT_GENERAL)
         w = vk.VkWriteDescriptorSet(vk.ST_WRITE_DESCRIPTOR_SET, None, dset, binding, element, 1,
-                                    vk.DESCRIPTOR_COMBINED_IMAGE_SAMPLER, pointer(ii), None, None)
+                                    dtype, pointer(ii), None, None)
         self.drv.vkUpdateDescriptorSets(self.device, 1, byref(w), 0, None)
 
     def write_buffer_descriptor(self, dset, binding, buf, offset, size, dtype=vk.DESCRIPTOR_UNIFORM_BUFFER):

@@ -33,6 +33,7 @@ OpTypeFloat = 22
 OpTypeVector = 23
 OpTypeMatrix = 24
 OpTypeImage = 25
+OpTypeSampler = 26
 OpTypeSampledImage = 27
 OpTypeArray = 28
 OpTypeStruct = 30
@@ -58,6 +59,7 @@ OpImageSampleExplicitLod = 88
 OpImageSampleProjImplicitLod = 91
 OpImageFetch = 95
 OpImage = 100
+OpSampledImage = 86
 OpVectorExtractDynamic = 77
 OpVectorInsertDynamic = 78
 OpVectorShuffle = 79
@@ -500,6 +502,34 @@ def textured_fs(set_=0, binding=0, explicit_lod=False):
     m.op(OpStore, o, c)
     _end_main(m)
     m.entry(ExecFragment, fn, "main", [tex, v_uv, o])
+    m.mode(fn, ModeOriginUpperLeft)
+    return m.to_words()
+
+
+def textured_separate_fs(set_=0, image_binding=0, sampler_binding=1):
+    """colour = texture(sampler2D(tex, smp), uv): a separate texture2D and sampler (set `set_`, bindings
+    `image_binding` and `sampler_binding`) combined by OpSampledImage"""
+    m = Module()
+    m.capability(CapShader)
+    f32 = m.f32()
+    v2, v4 = m.vec(f32, 2), m.vec(f32, 4)
+    img = m._type(("image2d",), OpTypeImage, f32, 1, 0, 0, 0, 1, 0)
+    smp_t = m._type(("sampler",), OpTypeSampler)
+    simg = m._type(("sampledimage", img), OpTypeSampledImage, img)
+    tex = m.variable(SCUniformConstant, m.ptr(SCUniformConstant, img))
+    m.decorate(tex, DecDescriptorSet, set_)
+    m.decorate(tex, DecBinding, image_binding)
+    smp = m.variable(SCUniformConstant, m.ptr(SCUniformConstant, smp_t))
+    m.decorate(smp, DecDescriptorSet, set_)
+    m.decorate(smp, DecBinding, sampler_binding)
+    v_uv = _io(m, SCInput, v2, 0)
+    o = _io(m, SCOutput, v4, 0)
+    fn = _begin_main(m)
+    si = m.res(OpSampledImage, simg, m.res(OpLoad, img, tex), m.res(OpLoad, smp_t, smp))
+    c = m.res(OpImageSampleImplicitLod, v4, si, m.res(OpLoad, v2, v_uv))
+    m.op(OpStore, o, c)
+    _end_main(m)
+    m.entry(ExecFragment, fn, "main", [tex, smp, v_uv, o])
     m.mode(fn, ModeOriginUpperLeft)
     return m.to_words()
 

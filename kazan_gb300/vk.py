@@ -55,7 +55,9 @@ ST_DESCRIPTOR_POOL_CREATE_INFO = 33
 ST_DESCRIPTOR_SET_ALLOCATE_INFO = 34
 ST_WRITE_DESCRIPTOR_SET = 35
 ST_COPY_DESCRIPTOR_SET = 36
+DESCRIPTOR_SAMPLER = 0
 DESCRIPTOR_COMBINED_IMAGE_SAMPLER = 1
+DESCRIPTOR_SAMPLED_IMAGE = 2
 DESCRIPTOR_UNIFORM_BUFFER = 6
 DESCRIPTOR_UNIFORM_BUFFER_DYNAMIC = 8
 DESCRIPTOR_STORAGE_BUFFER = 7

@@ -184,3 +184,28 @@ def test_missing_descriptors_are_recording_errors(renderer):
     h = c_void_p()
     assert d.vkCreateSampler(r.device, byref(ci), None, byref(h)) == vk.VK_ERROR_FEATURE_NOT_PRESENT
     r.free_command_buffer(run.cb)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["nearest_repeat", "linear_edge_border", "linear_unnormalized_bgra"])
+def test_separate_image_and_sampler(renderer, name):
+    """texture(sampler2D(tex, smp), uv) with a sampled image at binding 0 and a sampler at binding 1 (the
+    sampler's state replaces the image descriptor's in a local copy): the same pixels as the combined image
+    sampler, checked against the oracle"""
+    scene = _scene(name)
+    r = renderer
+    run = render.SceneRun(r, scene, mode="batched", tile=16)
+    lay = r.set_layout([(0, vk.DESCRIPTOR_SAMPLED_IMAGE, 1), (1, vk.DESCRIPTOR_SAMPLER, 1)])
+    dset = r.descriptor_sets(lay)[0]
+    r.write_image_descriptor(dset, 0, 0, None, run.tex_image, vk.DESCRIPTOR_SAMPLED_IMAGE)
+    r.write_image_descriptor(dset, 1, 0, r.sampler(scene.texture), None, vk.DESCRIPTOR_SAMPLER)
+    run.layout = r.pipeline_layout(0, [lay])
+    vs, _ = scene.shaders()
+    run.pipe = r.pipeline(scene, run.rp, run.layout, vs, spirv_asm.textured_separate_fs())
+    run.dsets = [dset]
+    r.free_command_buffer(run.cb)
+    run.cb = run.record()
+    run.submit()
+    color, depth = run.read()
+    _check(scene, color, depth, run.stats())
+    r.free_command_buffer(run.cb)

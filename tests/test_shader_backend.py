@@ -199,15 +199,29 @@ def test_storage_buffer_translates_read_only(built):
         shader.Shader(shader_ops.storage_fs(store=True), shader.FRAGMENT)
 
 
+def test_separate_image_and_sampler_translate(built):
+    """a texture2D and a sampler combined by OpSampledImage: bindings of kind 3 (sampled image) and 4
+    (sampler); the PTX copies the image descriptor to local memory with the sampler's state word (byte 28 of
+    the sampler's slot) and samples through the copy"""
+    fs = shader.Shader(spirv_asm.textured_separate_fs(0, 2, 5), shader.FRAGMENT)
+    assert sorted(fs.bindings()) == [(0, 2, 3, 1, 0), (0, 5, 4, 1, 0)]
+    tex = shader.layout([(0, 0, 4, 0), (1, 0, 2, 16)], [24])
+    ptx = shader.emit_ptx([(shader.Shader(spirv_asm.textured_vs(), shader.VERTEX), fs)], [tex],
+                          [{(0, 2): 0, (0, 5): 1}])
+    assert "[%kzpush+188]" in ptx  # 128 + 32 * 1 + 28
+    assert "st.local.v4.u32 [kzsd+16]" in ptx and "cvta.local.u64 %kzd" in ptx
+    shader.link(ptx)
+
+
 def test_unsupported_descriptor_forms_are_rejected(built):
-    """separate images and samplers are reported, not mistranslated"""
+    """unsupported image forms are reported, not mistranslated"""
     from kazan_gb300.spirv_asm import (Module, CapShader, SCUniformConstant, OpTypeImage, ExecFragment,
                                        ModeOriginUpperLeft, DecDescriptorSet, DecBinding, _begin_main, _end_main,
                                        _io, SCOutput)
     m = Module()
     m.capability(CapShader)
     f32 = m.f32()
-    img = m._type(("image2d",), OpTypeImage, f32, 1, 0, 0, 0, 1, 0)
+    img = m._type(("image3d",), OpTypeImage, f32, 2, 0, 0, 0, 1, 0)  # Dim 3D
     var = m.variable(SCUniformConstant, m.ptr(SCUniformConstant, img))
     m.decorate(var, DecDescriptorSet, 0)
     m.decorate(var, DecBinding, 0)
@@ -216,5 +230,5 @@ def test_unsupported_descriptor_forms_are_rejected(built):
     _end_main(m)
     m.entry(ExecFragment, fn, "main", [var, o])
     m.mode(fn, ModeOriginUpperLeft)
-    with pytest.raises(shader.ShaderError, match="separate images"):
+    with pytest.raises(shader.ShaderError, match="only 2D images"):
         shader.Shader(m.to_words(), shader.FRAGMENT)
