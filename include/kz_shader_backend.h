@@ -69,7 +69,8 @@ typedef struct KzShaderBinding {
   uint32_t set, binding;
   uint32_t kind;   /* 0 uniform buffer, 1 combined image sampler, 2 storage buffer, 3 sampled image, 4 sampler */
   uint32_t count;  /* array elements */
-  uint32_t bytes;  /* uniform buffer: bytes of the block */
+  uint32_t bytes;  /* uniform or storage buffer: bytes the bound range must cover (the block; for a storage
+                      block ending in a runtime-sized array, the block with one element) */
 } KzShaderBinding;
 /* Writes at most `max` bindings into out (may be NULL) and returns how many the stage declares. */
 KZ_API uint32_t kzShaderBindings(const void* shader, KzShaderBinding* out, uint32_t max);

@@ -110,7 +110,8 @@ struct Interface {
     uint32_t kind = 0;   /* 0 uniform buffer, 1 combined image sampler, 2 storage buffer, 3 sampled image,
                           4 sampler */
     uint32_t count = 1;  /* array elements */
-    uint32_t bytes = 0;  /* uniform buffer: bytes of the block (the range a descriptor must cover) */
+    uint32_t bytes = 0;  /* uniform or storage buffer: bytes the bound range must cover (the block; with a
+                            runtime-sized array, the block with one element) */
   };
   std::vector<Binding> bindings;
 };
