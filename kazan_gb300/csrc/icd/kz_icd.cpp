@@ -348,7 +348,7 @@ static void VKAPI_CALL kzGetPhysicalDeviceProperties(VkPhysicalDevice physicalDe
   l.maxImageArrayLayers = 1;
   l.maxTexelBufferElements = 0;
   l.maxUniformBufferRange = 65536;
-  l.maxStorageBufferRange = 0;
+  l.maxStorageBufferRange = 0xFFFFFFFFu; /* read-only storage buffers: the descriptor's range is 32-bit */
   l.maxPushConstantsSize = KZ_PUSH_BYTES;
   l.maxMemoryAllocationCount = 1u << 20;
   l.maxSamplerAllocationCount = 1u << 16;
@@ -360,6 +360,9 @@ static void VKAPI_CALL kzGetPhysicalDeviceProperties(VkPhysicalDevice physicalDe
   l.maxDescriptorSetSamplers = l.maxDescriptorSetSampledImages = KZ_MAX_DESC_SLOTS;
   l.maxDescriptorSetUniformBuffers = KZ_MAX_DESC_SLOTS;
   l.maxDescriptorSetUniformBuffersDynamic = KZ_MAX_DESC_SLOTS;
+  l.maxPerStageDescriptorStorageBuffers = KZ_MAX_DESC_SLOTS;
+  l.maxDescriptorSetStorageBuffers = KZ_MAX_DESC_SLOTS;
+  l.maxDescriptorSetStorageBuffersDynamic = KZ_MAX_DESC_SLOTS;
   l.maxVertexInputAttributes = KZ_MAX_VS_INPUTS;
   l.maxVertexInputBindings = KZ_MAX_BINDINGS;
   l.maxVertexInputAttributeOffset = 2047;

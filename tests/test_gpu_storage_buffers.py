@@ -11,9 +11,31 @@ from kazan_gb300 import render, vk
 import shader_ops as so
 
 
+def _record_dynamic(run, dset, dyn_offset):
+    """the run's draw with its set bound at a dynamic offset"""
+    from ctypes import byref, c_uint32, c_uint64, c_void_p
+    r, s, d = run.r, run.scene, run.r.drv
+    cb = r.begin()
+    clears = (vk.VkClearValue * 2)()
+    clears[0].color.float32[:] = list(s.clear_color)
+    clears[1].depthStencil.depth = s.clear_depth
+    rbi = vk.VkRenderPassBeginInfo(vk.ST_RENDER_PASS_BEGIN_INFO, None, run.rp, run.fb,
+                                   vk.VkRect2D(vk.VkOffset2D(0, 0), vk.VkExtent2D(s.width, s.height)), 2, clears)
+    d.vkCmdBeginRenderPass(cb, byref(rbi), vk.SUBPASS_CONTENTS_INLINE)
+    d.vkCmdBindPipeline(cb, vk.BIND_POINT_GRAPHICS, run.pipe)
+    d.vkCmdBindVertexBuffers(cb, 0, 1, (c_void_p * 1)(run.vb.handle.value), (c_uint64 * 1)(0))
+    d.vkCmdBindDescriptorSets(cb, vk.BIND_POINT_GRAPHICS, run.layout, 0, 1, (c_void_p * 1)(dset.value), 1,
+                              (c_uint32 * 1)(dyn_offset))
+    d.vkCmdDraw(cb, 3 * s.draws[0].count, 1, s.draws[0].first, 0)
+    d.vkCmdEndRenderPass(cb)
+    vk.check("vkEndCommandBuffer", d.vkEndCommandBuffer(cb))
+    return cb
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("dynamic", [False, True])
 @pytest.mark.parametrize("n, extra", [(100, 0), (37, 4)])
-def test_runtime_array_read_and_clamped(renderer, n, extra):
+def test_runtime_array_read_and_clamped(renderer, n, extra, dynamic):
     r = renderer
     idx = np.concatenate([np.arange(0, 120), np.arange(120, 1000, 7)[:100],
                           [1e4, 65535, 3e6, 4e9, 0.5, 36.9, 37.0, 99.0]]).astype(np.float32)[:so.GRID * so.GRID]
@@ -30,15 +52,17 @@ def test_runtime_array_read_and_clamped(renderer, n, extra):
 
     # the run's own pipeline with the plain colour shader, then the storage-buffer pipeline in its place
     run = render.SceneRun(r, dataclasses.replace(scene, fs_words=None), mode="batched", tile=16)
-    lay = r.set_layout([(0, vk.DESCRIPTOR_STORAGE_BUFFER, 1)])
+    dtype = vk.DESCRIPTOR_STORAGE_BUFFER_DYNAMIC if dynamic else vk.DESCRIPTOR_STORAGE_BUFFER
+    lay = r.set_layout([(0, dtype, 1)])
     dset = r.descriptor_sets(lay)[0]
-    r.write_buffer_descriptor(dset, 0, buf, offset, rng_bytes, dtype=vk.DESCRIPTOR_STORAGE_BUFFER)
+    # dynamic: the descriptor at offset 0, the block's 64 bytes given as the dynamic offset at binding
+    r.write_buffer_descriptor(dset, 0, buf, 0 if dynamic else offset, rng_bytes, dtype=dtype)
     run.layout = r.pipeline_layout(0, [lay])
     vs, _ = scene.shaders()
     run.pipe = r.pipeline(scene, run.rp, run.layout, vs, scene.fs_words)
     run.dsets = [dset]
     r.free_command_buffer(run.cb)
-    run.cb = run.record()
+    run.cb = _record_dynamic(run, dset, offset) if dynamic else run.record()
     run.submit()
     color, _ = run.read()
     got = so.read_bits(color, len(idx))
