@@ -75,3 +75,27 @@ def test_oracle_srgb_clear():
     L.kzo_clear_color_srgb(6, img.ctypes.data, rect, (ctypes.c_float * 4)(0.5, 0.2140, 1.0, 0.6))
     assert list(img[2, 3]) == [188, 127, 255, kz_oracle.unorm8(0.6)]
     assert not img[0].any() and not img[:, 0].any()
+
+
+def test_oracle_srgb_render_relates_to_unorm():
+    """the same opaque scene stored as sRGB and as UNORM: alpha is the same; each red, green and blue code is
+    the sRGB code of a value whose UNORM code is the UNORM image's (the transfer function lies above the
+    identity, so sRGB >= UNORM, with equality at 0 and 255)"""
+    import dataclasses
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from scene_cases import small_cases
+
+    base = small_cases()["sphere"]
+    u, _, _ = kz_oracle.render(dataclasses.replace(base, color_format="rgba8"), threads=4)
+    s, _, _ = kz_oracle.render(dataclasses.replace(base, color_format="rgba8_srgb"), threads=4)
+    assert np.array_equal(u[..., 3], s[..., 3])
+    assert np.all(s[..., :3] >= u[..., :3])
+    assert np.all(s[..., :3][u[..., :3] == 255] == 255)
+    # a UNORM code k means v in [(k - 1/2)/255, (k + 1/2)/255): its sRGB code lies between those of the ends
+    L = kz_oracle.lib()
+    lo = np.array([L.kzo_srgb8(max(0.0, (k - 0.5) / 255)) for k in range(256)])
+    hi = np.array([L.kzo_srgb8(min(1.0, (k + 0.5) / 255)) for k in range(256)])
+    rgb_u, rgb_s = u[..., :3].astype(int), s[..., :3].astype(int)
+    assert np.all((rgb_s >= lo[rgb_u]) & (rgb_s <= hi[rgb_u]))
+    assert (rgb_s != rgb_u).any()
