@@ -49,8 +49,10 @@ KZ_API PFN_vkVoidFunction vk_icdGetPhysicalDeviceProcAddr(VkInstance instance, c
  *   "fault_alloc" "N": the Nth device allocation from now fails with VK_ERROR_OUT_OF_DEVICE_MEMORY
  *   "kernel_timing" "0" / "1": command buffers ended while it is on launch their kernels at each submit
  *           (no graph capture) with a pair of timing events around every launch; see kzGetKernelTimes
- * Returns 0, or -1 for an unknown key or value.  The KZ_MODE, KZ_TILE, KZ_TRACE, KZ_KERNEL_TIMING and
- * KZ_FAULT=alloc:N environment variables set the initial values. */
+ *   "pdl"   "1" (default) / "0": command buffers ended while it is on launch each kernel that follows
+ *           another with programmatic stream serialization (its launch overlaps the predecessor's end)
+ * Returns 0, or -1 for an unknown key or value.  The KZ_MODE, KZ_TILE, KZ_TRACE, KZ_KERNEL_TIMING, KZ_PDL
+ * and KZ_FAULT=alloc:N environment variables set the initial values. */
 KZ_API int kzDriverSetOption(const char* key, const char* value);
 
 /* The CUDA stream (cudaStream_t) a queue executes on, for callers that time submissions with CUDA
