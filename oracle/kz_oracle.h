@@ -21,7 +21,10 @@
  *     that order, new vertices interpolated from the inside vertex towards the outside one);
  *   - screen-space barycentrics l_i = (float)E_i * (1/(float)S); depth z0 + l1 dz1 + l2 dz2 by fma,
  *     clamped to the viewport depth range; perspective-correct varyings divided by the interpolated 1/w;
- *   - UNORM8 stores rint(clamp(c, 0, 1) * 255); blending in f32 with dst = u8 / 255.
+ *   - UNORM8 stores rint(clamp(c, 0, 1) * 255); blending in f32 with dst = u8 / 255;
+ *   - 8-bit sRGB attachments store the sRGB transfer function's code of red, green and blue and blend
+ *     with their decoded values, both from kazan_gb300/csrc/kz_srgb_table.h (generated in 60-digit
+ *     decimal arithmetic; tests/test_srgb.py checks it against the transfer function in float64).
  * Every float operation is an explicit IEEE single operation (built with -ffp-contract=off and fmaf
  * where the GPU fuses), so results are bit-identical to the kernels.
  */
