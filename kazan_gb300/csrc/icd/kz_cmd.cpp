@@ -206,6 +206,10 @@ static bool begin_draw(CommandBuffer* cb, bool indexed, DrawRec& dr, int& nreads
   d.zmax = std::fmax(vp.minDepth, vp.maxDepth);
   draw_rect(pass.fb, pass.area, sc, vp, d.rect);
   std::memcpy(dr.push, cb->push, KZ_PUSH_BYTES);
+  /* blend constants in effect at this draw.  The colour attachments are unsigned normalized, so the
+   * constants are clamped to [0, 1] before they act as blend factors, as source and destination are. */
+  const float* bc = p->dyn_blend && cb->have_blend_const ? cb->blend_const : p->pipe.blend_const;
+  for (int k = 0; k < 4; k++) d.blend_const[k] = std::fmin(std::fmax(bc[k], 0.0f), 1.0f);
   /* stencil words of the draw: the pipeline's, with the dynamic compare mask / write mask / reference */
   for (int f = 0; f < 2; f++) {
     uint32_t w1 = p->pipe.stencil[2 * f + 1];
@@ -1349,11 +1353,10 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   low.tile = options().tile;
   low.timed = options().kernel_timing != 0;
   std::map<Pipeline*, uint32_t> pipe_index;
-  auto pipe_of = [&](Pipeline* p, const float* blend) -> uint32_t {
+  auto pipe_of = [&](Pipeline* p) -> uint32_t {
     auto it = pipe_index.find(p);
-    if (it != pipe_index.end() && !(p->dyn_blend && blend)) return it->second;
+    if (it != pipe_index.end()) return it->second;
     KzPipe kp = p->pipe;
-    if (p->dyn_blend && blend) std::memcpy(kp.blend_const, blend, sizeof kp.blend_const);
     uint32_t idx = (uint32_t)low.pipes.size();
     low.pipes.push_back(kp);
     low.pipe_objs.push_back(p);
@@ -1448,7 +1451,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
         d.samples = s.samples;
         d.rect[2] = std::min(d.rect[2], (int32_t)s.width);
         d.rect[3] = std::min(d.rect[3], (int32_t)s.height);
-        d.pipe = pipe_of(dr.pipe, cb->have_blend_const ? cb->blend_const : nullptr);
+        d.pipe = pipe_of(dr.pipe);
         d.prim_base = (uint32_t)prims;
         /* the draw's snapshot: push constants, then its descriptors, padded to whole KZ_PUSH_BYTES units */
         d.push_index = (uint32_t)(low.push.size() / KZ_PUSH_BYTES);

@@ -112,7 +112,7 @@ typedef struct KzPipe {
   uint32_t write_mask;        /* VkColorComponentFlags */
   uint32_t fs_discards;
   uint32_t has_fs;
-  float blend_const[4];
+  float blend_const[4];       /* VkPipelineColorBlendStateCreateInfo::blendConstants (draws carry their own copy) */
   uint32_t fs_passthrough;    /* the fragment shader only copies varyings 0..3 to colour components 0..3 */
   uint32_t stencil_test;      /* VkPipelineDepthStencilStateCreateInfo::stencilTestEnable */
   /* front and back VkStencilOpState, two words each: failOp | passOp << 3 | depthFailOp << 6 | compareOp << 9,
@@ -152,6 +152,8 @@ typedef struct KzDraw {
   uint32_t pad;
   uint32_t stencil[4];          /* the draw's stencil state in KzPipe::stencil's encoding: the pipeline's, with
                                    vkCmdSetStencilCompareMask / WriteMask / Reference applied where dynamic */
+  float blend_const[4];         /* the blend constants in effect at the draw (the pipeline's, or
+                                   vkCmdSetBlendConstants where dynamic), clamped to [0, 1] */
 } KzDraw;
 
 /* the four sample positions of a 4x multisampled pixel (the Vulkan standard positions), in 1/256 pixel

@@ -605,10 +605,11 @@ __device__ __forceinline__ uint32_t to_rgba(uint32_t px, uint32_t fmt) {
 }
 __device__ __forceinline__ uint32_t from_rgba(uint32_t px, uint32_t fmt) { return to_rgba(px, fmt); }
 
-/* apply blend + write mask; dst/out packed RGBA (R in the low byte).  `u8tab`, when given, holds u8f(k)
- * for k = 0..255 (the same quotients, read instead of divided); `srgb`: the attachment is 8-bit sRGB. */
-__device__ uint32_t color_write(const KzPipe& p, uint32_t dst, const float col[4], const float* u8tab = nullptr,
-                                bool srgb = false) {
+/* apply blend + write mask; dst/out packed RGBA (R in the low byte).  `k`: the draw's blend constants
+ * (clamped to [0, 1] at recording).  `u8tab`, when given, holds u8f(k) for k = 0..255 (the same quotients,
+ * read instead of divided); `srgb`: the attachment is 8-bit sRGB. */
+__device__ uint32_t color_write(const KzPipe& p, const float* k, uint32_t dst, const float col[4],
+                                const float* u8tab = nullptr, bool srgb = false) {
   /* sRGB attachments: red, green and blue are decoded to linear before blending and encoded after */
   const float* thr = kz_srgb_thr_g;
   uint32_t out = dst;
@@ -624,11 +625,11 @@ __device__ uint32_t color_write(const KzPipe& p, uint32_t dst, const float col[4
       if (!((p.write_mask >> i) & 1u)) continue;
       float r;
       if (i < 3)
-        r = blend_op(p.color_op, s[i], blend_factor(p.src_color, i, s, dd, p.blend_const), dd[i],
-                     blend_factor(p.dst_color, i, s, dd, p.blend_const));
+        r = blend_op(p.color_op, s[i], blend_factor(p.src_color, i, s, dd, k), dd[i],
+                     blend_factor(p.dst_color, i, s, dd, k));
       else
-        r = blend_op(p.alpha_op, s[3], blend_factor(p.src_alpha, 3, s, dd, p.blend_const), dd[3],
-                     blend_factor(p.dst_alpha, 3, s, dd, p.blend_const));
+        r = blend_op(p.alpha_op, s[3], blend_factor(p.src_alpha, 3, s, dd, k), dd[3],
+                     blend_factor(p.dst_alpha, 3, s, dd, k));
       uint32_t b = srgb && i < 3 ? srgb8(r, thr) : (uint32_t)unorm8(r);
       out = (out & ~(0xFFu << (8 * i))) | (b << (8 * i));
     }
@@ -1687,8 +1688,9 @@ __device__ void vis_resolve_run(const Ctx& c, uint32_t item) {
       const KzPipe& p = c.pipes[s.pipe];
       if (has_color) {
         uint32_t dst = clear_c ? seg.clear_color : *color_px(seg, x, y);
-        *color_px(seg, x, y) = from_rgba(color_write(p, to_rgba(dst, seg.color_format), col, nullptr,
-                                                     cf_srgb(seg.color_format)), seg.color_format);
+        *color_px(seg, x, y) = from_rgba(color_write(p, c.draws[s.draw].blend_const, to_rgba(dst, seg.color_format),
+                                                     col, nullptr, cf_srgb(seg.color_format)),
+                                         seg.color_format);
       }
       if (has_depth && p.depth_test && p.depth_write) *depth_px(seg, x, y) = z;
       else if (has_depth && clear_d) *depth_px(seg, x, y) = seg.clear_depth;
@@ -1964,7 +1966,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
             if (dtest && (be.depth & 2u)) depm[s] = zs[s];
             if (!has_color) continue;
             if (be.blend == 1u) colm[s] = blend_straight_alpha(colm[s], col, u8tab, be.write_mask);
-            else colm[s] = color_write(c.pipes[be.s.pipe], colm[s], col, u8tab, srgb);
+            else colm[s] = color_write(c.pipes[be.s.pipe], c.draws[be.s.draw].blend_const, colm[s], col, u8tab, srgb);
           }
           continue;
         }
@@ -2019,7 +2021,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
         if (dtest && (be.depth & 2u)) depv[q] = zq;
         if (!has_color) continue;
         if (be.blend == 1u) colv[q] = blend_straight_alpha(colv[q], col, u8tab, be.write_mask);
-        else colv[q] = color_write(c.pipes[be.s.pipe], colv[q], col, u8tab, srgb);
+        else colv[q] = color_write(c.pipes[be.s.pipe], c.draws[be.s.draw].blend_const, colv[q], col, u8tab, srgb);
       }
     }
   }

@@ -32,8 +32,8 @@ struct VertexLayout {
 std::string module_text(const std::vector<const ir::Shader*>& vs, const std::vector<const ir::Shader*>& fs,
                         const std::vector<VertexLayout>& layouts);
 
-/* nvJitLink the relocatable pipeline-kernel object with the shader PTX; returns "" on success */
-/* nvJitLink the shader PTX with the relocatable kernel object and, when given, the texture-sampling object */
+/* nvJitLink the shader PTX with the relocatable kernel object and, when given, the texture-sampling object;
+ * returns "" on success */
 std::string link(const std::string& ptx, const void* object, size_t object_size, std::vector<char>& cubin,
                  const void* tex_object = nullptr, size_t tex_size = 0);
 

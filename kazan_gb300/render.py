@@ -414,16 +414,13 @@ class Renderer:
                                                       scene.depth_compare, 0, int(scene.stencil is not None),
                                                       faces[0], faces[1], 0.0, 1.0)
         if scene.blend:
-            att = vk.VkPipelineColorBlendAttachmentState(1, vk.BLEND_SRC_ALPHA, vk.BLEND_ONE_MINUS_SRC_ALPHA,
-                                                         vk.BLEND_OP_ADD, vk.BLEND_SRC_ALPHA,
-                                                         vk.BLEND_ONE_MINUS_SRC_ALPHA, vk.BLEND_OP_ADD,
-                                                         vk.COLOR_MASK_RGBA)
+            att = vk.VkPipelineColorBlendAttachmentState(1, *scene.blend_factors(), scene.write_mask)
         else:
             att = vk.VkPipelineColorBlendAttachmentState(0, vk.BLEND_ONE, vk.BLEND_ZERO, vk.BLEND_OP_ADD,
                                                          vk.BLEND_ONE, vk.BLEND_ZERO, vk.BLEND_OP_ADD,
-                                                         vk.COLOR_MASK_RGBA)
+                                                         scene.write_mask)
         cbs = vk.VkPipelineColorBlendStateCreateInfo(vk.ST_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO, None, 0, 0, 0, 1,
-                                                     pointer(att), (c_float * 4)(0, 0, 0, 0))
+                                                     pointer(att), (c_float * 4)(*scene.blend_const))
         dyn_arr = (ctypes.c_int * max(1, len(dynamic)))(*dynamic)
         dyn = vk.VkPipelineDynamicStateCreateInfo(vk.ST_PIPELINE_DYNAMIC_STATE_CREATE_INFO, None, 0, len(dynamic),
                                                   dyn_arr)

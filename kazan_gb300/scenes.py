@@ -114,6 +114,10 @@ class Scene:
     depth_write: bool = True
     depth_compare: int = 1     # VK_COMPARE_OP_LESS
     blend: bool = False
+    blend_state: Optional[tuple] = None  # with blend: (srcColor, dstColor, colorOp, srcAlpha, dstAlpha, alphaOp) as
+                                         # VkBlendFactor / VkBlendOp; None: SRC_ALPHA, ONE_MINUS_SRC_ALPHA, ADD
+    blend_const: tuple = (0.0, 0.0, 0.0, 0.0)  # VkPipelineColorBlendStateCreateInfo::blendConstants
+    write_mask: int = 0xF      # VkColorComponentFlags of the colour attachment
     clear_color: tuple = (0.0, 0.0, 0.0, 1.0)
     clear_depth: float = 1.0
     fs_words: Optional[np.ndarray] = field(default=None, repr=False)  # overrides the default fragment shader
@@ -127,6 +131,10 @@ class Scene:
     samples: int = 1           # 1, or 4: multisampled colour and depth attachments, resolved at the end of the pass
     color_format: str = "rgba8"  # colour attachment: "rgba8", "bgra8", "rgba8_srgb" or "bgra8_srgb" (the sRGB
                                  # formats store sRGB-encoded red, green and blue)
+
+    def blend_factors(self):
+        """(srcColor, dstColor, colorOp, srcAlpha, dstAlpha, alphaOp) of the colour attachment's blend state"""
+        return tuple(int(x) for x in self.blend_state) if self.blend_state is not None else (6, 7, 0, 6, 7, 0)
 
     @property
     def srgb(self):

@@ -666,6 +666,7 @@ _PROTOS = {
     "vkCmdBindPipeline": (None, [H, c_int, H]),
     "vkCmdSetViewport": (None, [H, c_uint32, c_uint32, P(VkViewport)]),
     "vkCmdSetScissor": (None, [H, c_uint32, c_uint32, P(VkRect2D)]),
+    "vkCmdSetBlendConstants": (None, [H, P(ctypes.c_float)]),
     "vkCmdBindVertexBuffers": (None, [H, c_uint32, c_uint32, P(H), P(c_uint64)]),
     "vkCmdBindIndexBuffer": (None, [H, H, c_uint64, c_int]),
     "vkCmdPushConstants": (None, [H, H, c_uint32, c_uint32, c_uint32, c_void_p]),

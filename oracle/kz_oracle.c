@@ -521,23 +521,26 @@ static uint8_t store_channel(const kzo_draw* d, int i, float v) {
   return d->srgb && i < 3 ? kzo_srgb8(v) : kzo_unorm8(v);
 }
 
-/* colour write or blend of one fragment output into the RGBA8 texel c */
+/* colour write or blend of one fragment output into the RGBA8 texel c.  The attachment is unsigned
+ * normalized, so source, destination and the blend constants are clamped to [0, 1] before blending
+ * (Vulkan specification, "Blend Operations"). */
 static void write_color(const kzo_draw* d, uint8_t* c, const float out[4]) {
   if (d->blend_enable) {
-    float s[4], dst[4];
+    float s[4], dst[4], k[4];
     for (int i = 0; i < 4; i++) {
       s[i] = fminf(fmaxf(out[i], 0.0f), 1.0f);
       dst[i] = d->srgb && i < 3 ? srgb_dec[c[i]] : u8_to_f32(c[i]);
+      k[i] = fminf(fmaxf(d->blend_const[i], 0.0f), 1.0f);
     }
     for (int i = 0; i < 4; i++) {
       if (!(d->write_mask & (1u << i))) continue;
       float r;
       if (i < 3)
-        r = blend_op(d->color_op, s[i], blend_factor(d->src_color, i, s, dst, d->blend_const), dst[i],
-                     blend_factor(d->dst_color, i, s, dst, d->blend_const));
+        r = blend_op(d->color_op, s[i], blend_factor(d->src_color, i, s, dst, k), dst[i],
+                     blend_factor(d->dst_color, i, s, dst, k));
       else
-        r = blend_op(d->alpha_op, s[3], blend_factor(d->src_alpha, 3, s, dst, d->blend_const), dst[3],
-                     blend_factor(d->dst_alpha, 3, s, dst, d->blend_const));
+        r = blend_op(d->alpha_op, s[3], blend_factor(d->src_alpha, 3, s, dst, k), dst[3],
+                     blend_factor(d->dst_alpha, 3, s, dst, k));
       c[i] = store_channel(d, i, r);
     }
   } else {

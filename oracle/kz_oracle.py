@@ -155,9 +155,9 @@ def make_draws(scene, draws=None):
         k.depth_write = int(scene.depth_write)
         k.depth_compare = scene.depth_compare
         k.blend_enable = int(scene.blend)
-        k.src_color, k.dst_color, k.color_op = 6, 7, 0
-        k.src_alpha, k.dst_alpha, k.alpha_op = 6, 7, 0
-        k.write_mask = 0xF
+        k.src_color, k.dst_color, k.color_op, k.src_alpha, k.dst_alpha, k.alpha_op = scene.blend_factors()
+        k.write_mask = scene.write_mask
+        k.blend_const[:] = [float(x) for x in scene.blend_const]
         k.viewport[:] = [0.0, 0.0, float(scene.width), float(scene.height), 0.0, 1.0]
         k.scissor[:] = [0, 0, scene.width, scene.height]
         if scene.texture is not None:

@@ -4,7 +4,8 @@ The reference pins its SPIR-V decoder with three binary modules (spirv-parser/te
 test2.spv, test3.spv) and the exact dump text each must produce (raw strings in
 spirv-parser/src/lib.rs, tests parse_test, parse_test2, parse_test3).  This script copies the
 modules and extracts the expected text into tests/golden/spirv/ so that the tests run without the
-reference checkout.  Usage: python tests/golden/make_spirv_golden.py [reference_root]
+reference checkout.  Usage: python tests/golden/make_spirv_golden.py REFERENCE_ROOT (the checkout of
+kazan-3d/kazan to read the modules and dumps from)
 """
 import os
 import re
@@ -33,4 +34,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    sys.exit(main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_spirv_golden.py REFERENCE_ROOT")
+    sys.exit(main(sys.argv[1]))

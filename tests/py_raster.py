@@ -4,15 +4,17 @@ It is test infrastructure: it checks the C oracle (oracle/kz_oracle.c) on hand-s
 rational arithmetic with one explicit round-to-nearest-even to binary32 per operation, so every fma is a
 true single-rounding fma.  Coverage: colour pipeline (pass-through vertex shader, colour fragment shader),
 non-indexed triangle lists with no clipping needed (0 <= z <= w, inside the guard band), full-framebuffer
-viewport with depth range [0, 1], no culling, depth test LESS with writes, no blending.
+viewport with depth range [0, 1], no culling.
 
 Rules (Vulkan specification, with the choices the spec leaves open fixed as the GPU path fixes them):
 viewport x_f = fma(x * (1/w), W/2, W/2), snapped to 16.8 fixed point with round-to-nearest-even; signed
 area S of the snapped vertices decides orientation; pixel (x, y) is sampled at (256 x + 128, 256 y + 128);
 edge e runs from vertex e+1 to vertex e+2 and a pixel is covered when every edge function is > 0, or
-== 0 on a top or left edge; depth z = fma(l2, z2 - z0, fma(l1, z1 - z0, z0)) with l_i = E_i * (1 / S);
+== 0 on a top or left edge; depth z = fma(l2, z2 - z0, fma(l1, z1 - z0, z0)) with l_i = E_i * (1 / S),
+tested with any VkCompareOp and written or not;
 colour = perspective-correct interpolation q = fma(l2, 1/w2, fma(l1, 1/w1, l0 * 1/w0)),
-c = fma(l2, c2/w2, fma(l1, c1/w1, l0 * c0/w0)) * (1 / q), stored as round(clamp(c, 0, 1) * 255).
+c = fma(l2, c2/w2, fma(l1, c1/w1, l0 * c0/w0)) * (1 / q), stored as round(clamp(c, 0, 1) * 255) through
+the colour write mask, or blended (the 15 single-source factors, the 5 ops, constants; blend_texel).
 """
 from fractions import Fraction
 import math
@@ -66,9 +68,57 @@ def unorm8(v):
     return int(rne(mul(c, Fraction(255))))
 
 
-def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_depth=1.0):
+def depth_cmp(op, z, d):
+    """VkCompareOp `op` of fragment depth z against stored depth d"""
+    return [False, z < d, z == d, z <= d, z > d, z != d, z >= d, True][op]
+
+
+def _factor(f, ch, s, d, k):
+    """VkBlendFactor f for channel ch (the 15 single-source factors)"""
+    one = Fraction(1)
+    table = {0: lambda: Fraction(0), 1: lambda: one, 2: lambda: s[ch], 3: lambda: f32(one - s[ch]),
+             4: lambda: d[ch], 5: lambda: f32(one - d[ch]), 6: lambda: s[3], 7: lambda: f32(one - s[3]),
+             8: lambda: d[3], 9: lambda: f32(one - d[3]), 10: lambda: k[ch], 11: lambda: f32(one - k[ch]),
+             12: lambda: k[3], 13: lambda: f32(one - k[3]),
+             14: lambda: min(s[3], f32(one - d[3])) if ch < 3 else one}
+    return table[f]()
+
+
+def _blend_op(op, s, sf, d, df):
+    """VkBlendOp with the products and fma the GPU path uses: ADD fma(s, sf, d df), SUBTRACT fma(s, sf, -(d df)),
+    REVERSE_SUBTRACT fma(d, df, -(s sf)), MIN, MAX"""
+    if op == 0:
+        return fma(s, sf, mul(d, df))
+    if op == 1:
+        return fma(s, sf, -mul(d, df))
+    if op == 2:
+        return fma(d, df, -mul(s, sf))
+    return min(s, d) if op == 3 else max(s, d)
+
+
+def blend_texel(texel, out, factors, consts, write_mask):
+    """the RGBA8 texel after blending fragment colour `out` (four exact binary32 values) into `texel`
+    (unsigned normalized: source, destination and constants clamped to [0, 1]); factors = (srcColor, dstColor,
+    colorOp, srcAlpha, dstAlpha, alphaOp)"""
+    clamp = lambda v: min(max(v, Fraction(0)), Fraction(1))
+    s = [clamp(v) for v in out]
+    d = [div(int(t), 255) for t in texel]
+    k = [clamp(Fraction(float(np.float32(c)))) for c in consts]
+    res = list(texel)
+    for ch in range(4):
+        if not (write_mask >> ch) & 1:
+            continue
+        sf_i, df_i, op = (factors[0], factors[1], factors[2]) if ch < 3 else (factors[3], factors[4], factors[5])
+        r = _blend_op(op, s[ch], _factor(sf_i, ch, s, d, k), d[ch], _factor(df_i, ch, s, d, k))
+        res[ch] = unorm8(r)
+    return res
+
+
+def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_depth=1.0, compare=1, depth_write=True,
+           blend=None, blend_const=(0.0, 0.0, 0.0, 0.0), write_mask=0xF):
     """vertices: float32 [3T, 8] (x, y, z, w, r, g, b, a); returns (colour uint8 [H, W, 4], depth float32
-    [H, W], fragment count)"""
+    [H, W], fragment count).  compare: the VkCompareOp of the depth test; blend: None, or the six blend
+    factors and ops of blend_texel."""
     v = np.asarray(vertices, dtype=np.float32).reshape(-1, 8)
     color = np.empty((height, width, 4), dtype=np.uint8)
     color[:] = [unorm8(Fraction(float(np.float32(c)))) for c in clear_color]
@@ -120,13 +170,18 @@ def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_dept
                 l = [mul(f32(E[e]), inv_s) for e in range(3)]
                 z = fma(l[2], dz2, fma(l[1], dz1, z0))
                 z = min(max(z, Fraction(0)), Fraction(1))
-                if not z < depth[py][px]:
+                if not depth_cmp(compare, z, depth[py][px]):
                     continue
-                depth[py][px] = z
+                if depth_write:
+                    depth[py][px] = z
                 q = fma(l[2], IW[2], fma(l[1], IW[1], mul(l[0], IW[0])))
                 rq = div(1, q)
-                for k in range(4):
-                    num = fma(l[2], A[2][k], fma(l[1], A[1][k], mul(l[0], A[0][k])))
-                    color[py, px, k] = unorm8(mul(num, rq))
+                out = [mul(fma(l[2], A[2][k], fma(l[1], A[1][k], mul(l[0], A[0][k]))), rq) for k in range(4)]
+                if blend is not None:
+                    color[py, px] = blend_texel(color[py, px], out, blend, blend_const, write_mask)
+                else:
+                    for k in range(4):
+                        if (write_mask >> k) & 1:
+                            color[py, px, k] = unorm8(out[k])
     dep = np.array([[float(d) for d in row] for row in depth], dtype=np.float32)
     return color, dep, frags

@@ -173,3 +173,57 @@ def test_oracle_matches_python_on_plain_draw_prefix(built):
     assert st["fragments"] == pf > 0
     assert np.array_equal(od.view(np.uint32), pd.view(np.uint32))
     assert np.array_equal(oc, pc)
+
+
+def _state_rows(seed, n, size):
+    """random triangles whose colours reach outside [0, 1] (clamped before blending and storing) and whose alpha
+    varies, half of them coplanar at depth 0.25 (ties for EQUAL, LEQUAL and GEQUAL)"""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for t in range(n):
+        c = rng.uniform(0, size, 2)
+        pts = [tuple(c + rng.normal(0, size / 4, 2)) for _ in range(3)]
+        z = [0.25] * 3 if t % 2 else [float(rng.uniform(0.05, 0.95)) for _ in range(3)]
+        col = rng.uniform(-0.25, 1.25, (3, 4))
+        for j in range(3):
+            x, y = pts[j]
+            rows.append([_pix_to_ndc(x, size), _pix_to_ndc(y, size), z[j], 1.0] + list(col[j]))
+    return rows
+
+
+def _compare_states(oc, od, pc, pd):
+    assert np.array_equal(od.view(np.uint32), pd.view(np.uint32)), "depth differs"
+    mism = np.argwhere(np.any(oc != pc, axis=-1))
+    assert mism.size == 0, "colour differs at %d pixels, first %s: oracle %s python %s" % (
+        len(mism), mism[0], oc[tuple(mism[0])], pc[tuple(mism[0])])
+
+
+@pytest.mark.parametrize("depth_write", [True, False])
+@pytest.mark.parametrize("op", range(8))
+def test_oracle_depth_compare_ops_match_python(built, op, depth_write):
+    """every VkCompareOp, with and without depth writes, against the exact restatement"""
+    from fixed_function_cases import CLEAR_DEPTH
+    size = 16
+    sc = scenes.triangles_from(np.array(_state_rows(10 + op, 10, size), dtype=np.float32), size, size,
+                               clear_color=(0.1, 0.2, 0.3, 0.4), clear_depth=CLEAR_DEPTH[op], depth_compare=op,
+                               depth_write=depth_write)
+    oc, od, _ = kz_oracle.render(sc, threads=1)
+    pc, pd, _ = py_raster.render(sc.vertices, size, size, clear_color=sc.clear_color, clear_depth=sc.clear_depth,
+                                 compare=op, depth_write=depth_write)
+    _compare_states(oc, od, pc, pd)
+
+
+@pytest.mark.parametrize("i", range(15))
+def test_oracle_blend_states_match_python(built, i):
+    """every blend factor in every slot, every op, constants and write masks, against the exact restatement"""
+    from fixed_function_cases import BLEND_CONSTS, WRITE_MASKS, blend_states
+    size = 16
+    state = blend_states()[i]
+    sc = scenes.triangles_from(np.array(_state_rows(40 + i, 10, size), dtype=np.float32), size, size,
+                               clear_color=(0.3, 0.6, 0.9, 0.45), depth_compare=3, depth_write=False, blend=True,
+                               blend_state=state, blend_const=BLEND_CONSTS[i % len(BLEND_CONSTS)],
+                               write_mask=WRITE_MASKS[i % len(WRITE_MASKS)])
+    oc, od, _ = kz_oracle.render(sc, threads=1)
+    pc, pd, _ = py_raster.render(sc.vertices, size, size, clear_color=sc.clear_color, compare=3, depth_write=False,
+                                 blend=state, blend_const=sc.blend_const, write_mask=sc.write_mask)
+    _compare_states(oc, od, pc, pd)
