@@ -1,14 +1,13 @@
 /*
  * kz_noalloc.cu - an entry point that renders without allocating any device memory.
  *
- * Some callers of this library cannot call cudaMalloc: code that runs while a CUDA stream is being
- * captured into a graph in global or thread-local capture mode (cudaMalloc is an unsafe call there and
- * invalidates the capture), latency-critical serving loops that must not take the implicit device
- * synchronisation cudaMalloc / cudaFree can cause, and host programs that hand all device memory to
- * their own pool allocator.  The Vulkan path allocates its scratch (visibility keys, triangle records,
- * work lists) at vkEndCommandBuffer; kzRasterTrianglesNoAlloc instead keeps that scratch in one
- * file-scope __device__ array of fixed size, which every GPU that loads this library holds until the
- * process exits (KZ_NOALLOC_SCRATCH_BYTES, about 24 MiB).
+ * Some callers of this library cannot call cudaMalloc when they draw: programs that hand all device memory
+ * to their own pool allocator up front (so a cudaMalloc of the driver's scratch would fail or fragment
+ * their pool), and latency-bound serving loops that must not take the implicit device-wide
+ * synchronisation cudaMalloc and cudaFree can cause.  The Vulkan path allocates its scratch (visibility
+ * keys, triangle records, work lists) at vkEndCommandBuffer; kzRasterTrianglesNoAlloc instead keeps that
+ * scratch in one file-scope __device__ array of fixed size, which every GPU that loads this library holds
+ * until the process exits (KZ_NOALLOC_SCRATCH_BYTES, about 24 MiB).
  *
  * It runs the same visibility-buffer kernels as the Vulkan path (this file compiles kz_pipeline.cu
  * together with the pass-through colour stage: gl_Position = attribute 0, colour = attribute 1), so the
@@ -115,23 +114,48 @@ extern "C" __global__ void kz_k_noalloc_setup(KzDraw draw, KzPipe pipe, KzSegmen
 
 namespace {
 
-std::mutex g_mu;
-void* g_base[64];
+/* the driver API's cuCtxGetCurrent, reached through the runtime (the library links no libcuda) */
+typedef int (*CtxGetCurrentFn)(void** ctx);
 
-/* once per device, with that device current: the device address of the scratch array */
+std::mutex g_mu;
+struct ScratchAddr {
+  void* ctx = nullptr;   /* the context the address belongs to */
+  void* base = nullptr;  /* device address of kz_noalloc_scratch in it */
+};
+ScratchAddr g_base[64];
+CtxGetCurrentFn g_ctx_get = nullptr;
+
+/* Set-up, with the device current: the device address of the scratch array, looked up with
+ * cudaGetSymbolAddress the first time a device is used, and again whenever the device's current context
+ * is not the one the address was taken in (after cudaDeviceReset the module is loaded anew, at another
+ * address).  The array's name in host code is only a host-side stand-in for the symbol; kernels must be
+ * given this address. */
 cudaError_t scratch_base(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_base[dev]) {
+  if (!g_ctx_get) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) return e != cudaSuccess ? e : cudaErrorUnknown;
+    g_ctx_get = reinterpret_cast<CtxGetCurrentFn>(fn);
+  }
+  void* ctx = nullptr;
+  if (g_ctx_get(&ctx) != 0) return cudaErrorDeviceUninitialized;
+  ScratchAddr& a = g_base[dev];
+  if (!ctx || !a.base || a.ctx != ctx) {
+    /* the lookup also makes the device's primary context current when no context is */
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, kz_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    g_base[dev] = p;
+    if (g_ctx_get(&ctx) != 0 || !ctx) return cudaErrorDeviceUninitialized;
+    a.base = p;
+    a.ctx = ctx;
   }
-  *out = g_base[dev];
+  *out = a.base;
   return cudaSuccess;
 }
 
@@ -146,16 +170,19 @@ uint8_t host_unorm8(float v) {
  * w then colour r, g, b, a) into a width x height RGBA8 colour image and D32 depth image (tightly packed
  * rows), both cleared first: depth test LESS with writes, no culling, no blending.  All pointers are
  * device pointers owned by the caller; `stream` is a cudaStream_t (NULL for the legacy default stream).
- * The call returns after the rendering finished on `stream`.
+ * The call synchronises `stream` and returns after the rendering finished.
  *
- * Limits: width * height <= 1048576 pixels (KZ_NOALLOC_MAX_PIXELS), triangle_count <= 65536, and at
- * most 2^20 warp jobs for triangles larger than 32 pixels (about 1 Gi covered-or-tested pixels).
- * Returns 0 on success, -1 for arguments beyond these limits, -2 for a CUDA error, -3 when the
- * large-triangle jobs exceed their scratch.
+ * Limits: width * height <= 1048576 pixels (KZ_NOALLOC_MAX_PIXELS), triangle_count <= 65536, at most
+ * 131072 large-triangle records (one per triangle whose box exceeds 192 pixels, and per clipped
+ * sub-triangle whose box exceeds 32), and at most 2^20 8x8-block warp jobs of those records.  Returns 0 on
+ * success, -1 for arguments beyond the first two limits (before any GPU work), -2 for a CUDA error, -3
+ * when the records or the jobs overflow their scratch (the image is then incomplete).
  *
- * Allocates nothing.  The first call on a device looks up the scratch array's device address; make that
- * first call before any stream capture.  Every call shares the scratch array (it keeps the last call's
- * contents and is re-initialised by each call), so calls whose work overlaps on the GPU race. */
+ * Allocates nothing: no cudaMalloc, cudaFree or allocating library call.  The first call on a device (and
+ * the first after the device's context changed) looks up the scratch array's device address.  Every call
+ * shares the scratch array, which keeps the last call's contents; each call clears what must start at
+ * zero (counters and status) and initialises the visibility keys, but calls whose work overlaps on the GPU
+ * (other streams, other threads) race on it. */
 extern "C" KZ_API int kzRasterTrianglesNoAlloc(const float* vertices, uint32_t triangle_count, uint32_t width,
                                                       uint32_t height, uint32_t* color, float* depth,
                                                       const float clear_color[4], float clear_depth, void* stream) {
@@ -258,6 +285,10 @@ extern "C" KZ_API int kzRasterTrianglesNoAlloc(const float* vertices, uint32_t t
   f.status = (uint64_t)(uintptr_t)(base + KZ_NA_STATUS);
   f.num_segments = 1;
   f.first_segment = 0;
+  f.chunk_begin = 0;
+  f.chunk_end = 0xFFFFFFFFu;
+  f.jobs_incremental = 0;
+  f.barrier_ns = 0; /* no persistent kernel runs here */
 
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
