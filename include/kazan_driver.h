@@ -51,6 +51,10 @@ KZ_API PFN_vkVoidFunction vk_icdGetPhysicalDeviceProcAddr(VkInstance instance, c
  *           (no graph capture) with a pair of timing events around every launch; see kzGetKernelTimes
  *   "pdl"   "1" (default) / "0": command buffers ended while it is on launch each kernel that follows
  *           another with programmatic stream serialization (its launch overlaps the predecessor's end)
+ *   "barrier_ns" "N": command buffers ended while it is set give their persistent kernels' grid barriers
+ *           up after waiting N nanoseconds (default 4000000000; 0 gives up at the first check).  A barrier
+ *           that gives up sets KZ_STATUS_BARRIER_TIMEOUT and the submission completes with
+ *           VK_ERROR_DEVICE_LOST; the kernel returns and the CUDA context stays usable
  * Returns 0, or -1 for an unknown key or value.  The KZ_MODE, KZ_TILE, KZ_TRACE, KZ_KERNEL_TIMING, KZ_PDL
  * and KZ_FAULT=alloc:N environment variables set the initial values. */
 KZ_API int kzDriverSetOption(const char* key, const char* value);
@@ -81,8 +85,8 @@ KZ_API int kzGetCommandBufferStats(VkCommandBuffer commandBuffer, KzCommandBuffe
 #define KZ_KERNEL_KIND_NAMES                                                                          \
   {"kz_k_persistent", "kz_k_vis_init", "kz_k_vis_geometry", "kz_k_vis_large", "kz_k_vis_resolve",      \
    "kz_k_geometry",   "kz_k_scan",     "kz_k_bin",          "kz_k_raster",    "kz_k_clear",         \
-   "kz_k_indirect",   "kz_k_indirect_tables", "kz_k_resolve"}
-#define KZ_KERNEL_KINDS 13
+   "kz_k_indirect",   "kz_k_indirect_tables", "kz_k_resolve", "kz_k_persistent_vis"}
+#define KZ_KERNEL_KINDS 14
 
 /* Device time of a command buffer recorded with "kernel_timing" on: for each kernel kind, the summed
  * durations (CUDA events on the queue stream around each launch) and the number of launches over all
@@ -92,25 +96,28 @@ KZ_API int kzGetCommandBufferStats(VkCommandBuffer commandBuffer, KzCommandBuffe
 KZ_API int kzGetKernelTimes(VkCommandBuffer commandBuffer, double* totalMs, uint32_t* launches, uint32_t count,
                             int reset);
 
-/* No counterpart in the reference.  Renders without allocating device memory, for callers that cannot
- * call cudaMalloc when they draw: code running while a stream is captured into a CUDA graph (an allocation
- * breaks the capture), serving loops that must not take the synchronisation an allocation or free may
- * cause, and programs whose own pool owns all device memory.  The Vulkan path allocates its scratch at
- * vkEndCommandBuffer; this call uses one fixed scratch array inside the library (about 24 MiB, held on
- * every GPU that loads the library until the process exits).
+/* No counterpart in the reference.  Renders without allocating device memory, for callers that cannot call
+ * cudaMalloc when they draw: programs that hand all device memory to their own pool allocator up front, and
+ * latency-bound serving loops that must not take the device-wide synchronisation an allocation or free
+ * may cause.  The Vulkan path allocates its scratch at vkEndCommandBuffer; this call uses one fixed scratch
+ * array inside the library instead (about 24 MiB, held on every GPU that loads the library until the
+ * process exits).
  *
  * Draws `triangleCount` triangles (non-indexed list, 8 floats per vertex: clip-space x, y, z, w, then
  * colour r, g, b, a) into a width x height RGBA8 image and D32 depth image (tight rows), both cleared
  * first: full viewport, depth range [0, 1], depth test LESS with writes, no culling, no blending -- the
  * same pixels the Vulkan path gives for that pipeline.  Pointers are device pointers owned by the caller;
- * `stream` is a cudaStream_t (NULL: legacy default stream); the call returns once the work has finished.
- * Limits: width * height <= 1048576, triangleCount <= 65536, at most 2^20 8x8-block jobs for triangles
- * larger than 32 pixels.  Returns 0; -1 for arguments beyond the limits (no GPU work); -2 for a CUDA
- * error; -3 when the large-triangle jobs overflow the scratch.
+ * `stream` is a cudaStream_t (NULL: legacy default stream); the call synchronises that stream and returns
+ * once the work has finished.
+ * Limits: width * height <= 1048576 and triangleCount <= 65536 (else -1, before any GPU work); at most
+ * 131072 large-triangle records (one per triangle whose box exceeds 192 pixels, and per clipped
+ * sub-triangle whose box exceeds 32) and 2^20 8x8-block jobs of those records (else -3: the scratch
+ * overflowed and the image is incomplete).  Returns 0 on success and -2 for a CUDA error.  Allocates
+ * nothing: no cudaMalloc, cudaFree or allocating library call.
  *
- * The first call on a device looks up the scratch array's device address: make it before any stream
- * capture.  All calls share the scratch; each call re-initialises what it reads, but calls whose work
- * overlaps on the GPU (other streams, other threads) race. */
+ * The first call on a device, and the first after its context changed, looks up the scratch array's device
+ * address.  All calls share the scratch, which keeps the last call's contents; each call clears what must
+ * start at zero, but calls whose work overlaps on the GPU (other streams, other threads) race. */
 KZ_API int kzRasterTrianglesNoAlloc(const float* vertices, uint32_t triangleCount, uint32_t width, uint32_t height,
                                     uint32_t* color, float* depth, const float clearColor[4], float clearDepth,
                                     void* stream);

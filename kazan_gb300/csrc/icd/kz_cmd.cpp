@@ -1249,17 +1249,21 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
         f.first_segment = s0;
         f.num_segments = lop.seg_end;
         void* args[] = {&f};
+        /* passes whose segments are all opaque run the kernel with only the visibility phases */
+        bool all_vis = true;
+        for (uint32_t s = s0; s < lop.seg_end; s++) all_vis &= low.segments[s].mode == KZ_MODE_VISIBILITY;
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((unsigned)ks->persistent_blocks);
+        cfg.gridDim = dim3((unsigned)(all_vis ? ks->persistent_vis_blocks : ks->persistent_blocks));
         cfg.blockDim = dim3(256);
-        cfg.dynamicSmemBytes = KZ_DYN_SMEM;
+        cfg.dynamicSmemBytes = all_vis ? 0 : KZ_DYN_SMEM;
         cfg.stream = st;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeCooperative;
         at[0].val.cooperative = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        launch(dev, timing, KK_PERSISTENT, cfg, ks->persistent, args, chain);
+        if (all_vis) launch(dev, timing, KK_PERSISTENT_VIS, cfg, ks->persistent_vis, args, chain);
+        else launch(dev, timing, KK_PERSISTENT, cfg, ks->persistent, args, chain);
         launches++;
       } else {
         for (uint32_t s = s0; s < lop.seg_end; s++) {
@@ -1269,11 +1273,29 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
           cudaLaunchConfig_t cfg = {};
           cfg.blockDim = dim3(256);
           cfg.stream = st;
+          /* the per-draw launch form: each direct draw's geometry is a launch of its own (with, for opaque
+           * segments, the large-triangle jobs it made); the pass-wide phases run once per segment */
+          const bool per_draw = low.mode == 2 && !seg.indirect;
+          const uint32_t gb = (uint32_t)std::max(1, ks->geometry_blocks);
           if (seg.mode == KZ_MODE_VISIBILITY) {
             cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (seg.width * seg.height + 255) / 256)));
             launch(dev, timing, KK_VIS_INIT, cfg, ks->vis_init, args, chain);
-            if (seg.num_chunks || seg.indirect) {
-              uint32_t gb = (uint32_t)std::max(1, ks->geometry_blocks);
+            if (per_draw) {
+              for (uint32_t di = seg.first_draw; di < seg.first_draw + seg.num_draws; di++) {
+                const std::pair<uint32_t, uint32_t> dc = low.draw_chunks[di];
+                if (dc.first == dc.second) continue;
+                KzFrame fd = f;
+                fd.chunk_begin = dc.first;
+                fd.chunk_end = dc.second;
+                fd.jobs_incremental = 1;
+                void* dargs[] = {&fd, &s};
+                cfg.gridDim = dim3(std::min<uint32_t>(dc.second - dc.first, gb));
+                launch(dev, timing, KK_VIS_GEOMETRY, cfg, ks->vis_geometry, dargs, chain);
+                cfg.gridDim = dim3(grid_cap(dev));
+                launch(dev, timing, KK_VIS_LARGE, cfg, ks->vis_large, dargs, chain);
+                launches += 2;
+              }
+            } else if (seg.num_chunks || seg.indirect) {
               cfg.gridDim = dim3(seg.indirect ? gb : std::min<uint32_t>(seg.num_chunks, gb));
               launch(dev, timing, KK_VIS_GEOMETRY, cfg, ks->vis_geometry, args, chain);
               cfg.gridDim = dim3(grid_cap(dev));
@@ -1285,7 +1307,19 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
             launches += 2;
             continue;
           }
-          if (seg.num_chunks || seg.indirect) {
+          if (per_draw) {
+            for (uint32_t di = seg.first_draw; di < seg.first_draw + seg.num_draws; di++) {
+              const std::pair<uint32_t, uint32_t> dc = low.draw_chunks[di];
+              if (dc.first == dc.second) continue;
+              KzFrame fd = f;
+              fd.chunk_begin = dc.first;
+              fd.chunk_end = dc.second;
+              void* dargs[] = {&fd, &s};
+              cfg.gridDim = dim3(dc.second - dc.first);
+              launch(dev, timing, KK_GEOMETRY, cfg, ks->geometry, dargs, chain);
+              launches++;
+            }
+          } else if (seg.num_chunks || seg.indirect) {
             cfg.gridDim = dim3(seg.indirect ? grid_cap(dev) : seg.num_chunks);
             launch(dev, timing, KK_GEOMETRY, cfg, ks->geometry, args, chain);
             launches++;
@@ -1408,9 +1442,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
       vis_ok = false;
     /* split the pass into segments */
     std::vector<std::pair<size_t, size_t>> runs; /* [begin, end) draw indices */
-    if (low.mode == 2) {
-      for (size_t i = 0; i < pr.draws.size(); i++) runs.push_back({i, i + 1});
-    } else {
+    {
       size_t b = 0;
       for (size_t i = 1; i <= pr.draws.size(); i++)
         if (i == pr.draws.size() || raster_class(pr.draws[i], vis_ok) != raster_class(pr.draws[b], vis_ok)) {
@@ -1463,6 +1495,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
         }
         for (DeviceMemory* m : dr.desc_reads) add_unique(low.reads, m);
         uint32_t di = (uint32_t)low.draws.size();
+        const uint32_t chunk0 = (uint32_t)(low.chunks.size() - s.first_chunk);
         for (uint64_t c = 0; !dr.indirect && c < dr.triangles; c += KZ_CHUNK) {
           KzChunk ch;
           ch.draw = di;
@@ -1472,6 +1505,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
           low.chunks.push_back(ch);
         }
         low.draws.push_back(d);
+        low.draw_chunks.push_back({chunk0, (uint32_t)(low.chunks.size() - s.first_chunk)});
         for (DeviceMemory* m : dr.reads) add_unique(low.reads, m);
         prims += dr.triangles;
       }
@@ -1581,6 +1615,10 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   low.frame.status = (uint64_t)(uintptr_t)low.d_status;
   low.frame.num_segments = (uint32_t)low.segments.size();
   low.frame.first_segment = 0;
+  low.frame.chunk_begin = 0;
+  low.frame.chunk_end = 0xFFFFFFFFu;
+  low.frame.jobs_incremental = 0;
+  low.frame.barrier_ns = options().barrier_ns;
   upload_tables(low);
   if (cudaMallocHost((void**)&low.h_status, sizeof(KzStatus)) != cudaSuccess) return VK_ERROR_OUT_OF_HOST_MEMORY;
   std::memset(low.h_status, 0, sizeof(KzStatus));

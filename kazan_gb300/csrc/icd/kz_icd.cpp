@@ -167,7 +167,8 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
     cudaKernel_t* k;
   } names[] = {{"kz_k_geometry", &ks->geometry}, {"kz_k_scan", &ks->scan},
                {"kz_k_bin", &ks->bin},           {"kz_k_raster", &ks->raster},
-               {"kz_k_persistent", &ks->persistent}, {"kz_k_clear", &ks->clear},
+               {"kz_k_persistent", &ks->persistent}, {"kz_k_persistent_vis", &ks->persistent_vis},
+               {"kz_k_clear", &ks->clear},
                {"kz_k_vis_init", &ks->vis_init}, {"kz_k_vis_geometry", &ks->vis_geometry},
                {"kz_k_vis_large", &ks->vis_large}, {"kz_k_vis_resolve", &ks->vis_resolve},
                {"kz_k_indirect", &ks->indirect}, {"kz_k_indirect_tables", &ks->indirect_tables},
@@ -188,6 +189,13 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
     per_sm = 1;
   }
   ks->persistent_blocks = per_sm * dev->pd->sm_count;
+  int vis_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&vis_sm, (const void*)ks->persistent_vis, 256, 0) != cudaSuccess ||
+      vis_sm < 1) {
+    cudaGetLastError();
+    vis_sm = 1;
+  }
+  ks->persistent_vis_blocks = vis_sm * dev->pd->sm_count;
   int geo_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&geo_sm, (const void*)ks->vis_geometry, 256, 0) != cudaSuccess ||
       geo_sm < 1) {
@@ -1660,6 +1668,13 @@ extern "C" KZ_API int kzDriverSetOption(const char* key, const char* value) {
   if (!std::strcmp(key, "pdl")) {
     if (std::strcmp(value, "0") && std::strcmp(value, "1")) return -1;
     o.pdl = value[0] == '1';
+    return 0;
+  }
+  if (!std::strcmp(key, "barrier_ns")) {
+    char* end = nullptr;
+    unsigned long long v = std::strtoull(value, &end, 10);
+    if (!*value || *end || v > 0xFFFFFFFFull) return -1;
+    o.barrier_ns = (uint32_t)v;
     return 0;
   }
   if (!std::strcmp(key, "fault_alloc")) {

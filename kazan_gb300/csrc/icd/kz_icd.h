@@ -210,6 +210,7 @@ enum KernelKind {
   KK_INDIRECT,
   KK_INDIRECT_TABLES,
   KK_RESOLVE,
+  KK_PERSISTENT_VIS,
   KK_COUNT
 };
 
@@ -224,9 +225,11 @@ struct PipelineCache {};
 struct KernelSet {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t geometry = nullptr, scan = nullptr, bin = nullptr, raster = nullptr, persistent = nullptr,
-               clear = nullptr, vis_init = nullptr, vis_geometry = nullptr, vis_large = nullptr,
-               vis_resolve = nullptr, indirect = nullptr, indirect_tables = nullptr, resolve = nullptr;
+               persistent_vis = nullptr, clear = nullptr, vis_init = nullptr, vis_geometry = nullptr,
+               vis_large = nullptr, vis_resolve = nullptr, indirect = nullptr, indirect_tables = nullptr,
+               resolve = nullptr;
   int persistent_blocks = 0;
+  int persistent_vis_blocks = 0; /* resident blocks of kz_k_persistent_vis (opaque passes) */
   int geometry_blocks = 0; /* resident blocks of kz_k_vis_geometry on the whole GPU */
 };
 
@@ -285,6 +288,8 @@ struct Lowered {
   std::vector<uint64_t> table_guess;       /* per indirect segment: triangles its device tables have room for */
   std::vector<uint8_t> push;
   std::vector<uint32_t> draw_lut;          /* all segments' draw lookup tables, back to back */
+  std::vector<std::pair<uint32_t, uint32_t>> draw_chunks; /* per draw: its chunks [begin, end) within its segment
+                                                             (direct draws; the per-draw launch form) */
   std::vector<size_t> draw_lut_offset;     /* per segment: first entry in draw_lut */
   struct LOp {
     OpKind kind;
@@ -314,7 +319,8 @@ struct Lowered {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
-  int mode = 0; /* 0 persistent, 1 batched, 2 per-draw */
+  int mode = 0; /* 0 persistent, 1 batched, 2 per-draw (geometry launched per draw, the pass-wide phases once
+                   per segment; launched at submit, not captured) */
   uint32_t tile = 16;
   bool timed = false; /* kernel timing: launched at submit with an event pair around each kernel */
 };
@@ -394,6 +400,7 @@ struct Options {
   int kernel_timing = 0; /* KZ_KERNEL_TIMING */
   int pdl = 1;        /* KZ_PDL: a kernel that follows another kernel in a submission is launched with
                          programmatic stream serialization (its launch overlaps the predecessor's completion) */
+  uint32_t barrier_ns = 4000000000u; /* a persistent kernel's grid barrier gives up after waiting this long */
 };
 Options& options();
 

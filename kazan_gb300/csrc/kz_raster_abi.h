@@ -194,7 +194,9 @@ typedef struct KzSegCounters {
   uint32_t tile_next;   /* work-stealing cursor over tiles */
   uint32_t fragments;   /* statistics: covered fragments (visibility mode counts depth-pass candidates) */
   uint32_t max_bin;     /* largest bin */
-  uint32_t pad;
+  uint32_t large_done;  /* per-draw launches: large-triangle jobs the earlier kz_k_vis_large launches processed */
+  uint32_t large_blocks;/* per-draw launches: blocks of the current kz_k_vis_large launch that have finished */
+  uint32_t pad[2];
 } KzSegCounters;
 
 typedef struct KzSegment {
@@ -280,6 +282,13 @@ typedef struct KzFrame {
   uint64_t status;           /* KzStatus* */
   uint32_t num_segments;
   uint32_t first_segment;    /* segments before it are skipped (restart after an overflow) */
+  /* one launch of the geometry kernels processes chunks [chunk_begin, min(chunk_end, num_chunks)) of its
+   * segment: all of them (0, ~0u), or one draw's in the per-draw launch form */
+  uint32_t chunk_begin, chunk_end;
+  uint32_t jobs_incremental; /* kz_k_vis_large: process only the jobs added since the previous launch for
+                                this segment (per-draw launch form), else all of the segment's jobs */
+  uint32_t barrier_ns;       /* persistent kernels: a grid barrier gives up (KZ_STATUS_BARRIER_TIMEOUT) after
+                                waiting this many nanoseconds */
 } KzFrame;
 
 /* --- shader call ABI (kernels <-> JIT-linked shader device functions) --- */

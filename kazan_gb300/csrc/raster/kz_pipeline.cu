@@ -52,7 +52,6 @@ extern "C" __device__ KzPos3 kz_vs_pos3(uint32_t pipe, const KzDraw* draw, uint3
 #define KZ_THREADS 256
 #define KZ_SORT_CAP 4096          /* ordered mode: largest bin sorted in shared memory */
 #define KZ_BATCH 32               /* ordered mode: triangles set up per batch */
-#define KZ_BARRIER_NS 4000000000ull /* grid barrier gives up after 4 s */
 
 /* texture sampling (kz_tex2d, kz_tex_fetch) lives in kz_tex.cu, a separate object linked with the shaders */
 
@@ -1520,17 +1519,19 @@ __device__ __forceinline__ uint32_t vis_geometry_warp(const Ctx& c, uint32_t chu
 }
 
 /* the geometry of a segment by warps: warp w of `warps` takes the 32-triangle groups w, w + warps, ...
- * (8 groups per chunk), then adds its fragment count to the statistics.  `smem`: 8 warps x 32 WarpTri,
+ * (8 groups per chunk) of the launch's chunks [chunk_begin, chunk_end), then adds its fragment count to the
+ * statistics.  `smem`: 8 warps x 32 WarpTri,
  * then 8 warps x 32 owner bytes (KZ_GEO_SMEM bytes). */
 __device__ void vis_geometry_warps(const Ctx& c, unsigned char* smem, const uint32_t* magic_tab, uint32_t w,
                                    uint32_t warps) {
   const uint32_t wib = threadIdx.x >> 5;
   WarpTri* slots = reinterpret_cast<WarpTri*>(smem) + wib * 32;
   uint8_t* owner = smem + KZ_THREADS * sizeof(WarpTri) + wib * 32;
-  const uint32_t groups = c.seg->num_chunks * 8;
+  const uint32_t cb = c.f->chunk_begin, ce = min(c.f->chunk_end, c.seg->num_chunks);
+  const uint32_t groups = cb < ce ? (ce - cb) * 8 : 0u;
   uint32_t frags = 0;
   for (uint32_t i = w; i < groups; i += warps)
-    frags += vis_geometry_warp(c, i / 8, i % 8, slots, owner, magic_tab);
+    frags += vis_geometry_warp(c, cb + i / 8, i % 8, slots, owner, magic_tab);
   for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
   if ((threadIdx.x & 31) == 0 && frags) {
     atomicAdd(&c.cnt->fragments, frags);
@@ -1699,6 +1700,27 @@ __device__ void vis_resolve_run(const Ctx& c, uint32_t item) {
   }
   if (has_color && clear_c) *color_px(seg, x, y) = seg.clear_color;
   if (has_depth && clear_d) *depth_px(seg, x, y) = seg.clear_depth;
+}
+
+/* the large-triangle jobs [j0, njobs) of a segment, warp w of `warps` taking jobs j0 + w, j0 + w + warps, ...;
+ * adds the fragments to the statistics */
+__device__ __forceinline__ void vis_large_phase(const Ctx& c, uint32_t j0, uint32_t njobs, uint32_t w,
+                                                uint32_t warps) {
+  const uint2* jobs = reinterpret_cast<const uint2*>(c.seg->bins);
+  const int lane = threadIdx.x & 31;
+  uint32_t frags = 0;
+  for (uint32_t j = j0 + w; j < njobs; j += warps) frags += vis_large_job(c, jobs[j], lane);
+  for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
+  if (lane == 0 && frags) {
+    atomicAdd(&c.cnt->fragments, frags);
+    atomicAdd(&c.st->fragments_lo, frags);
+  }
+}
+
+/* the resolve of a segment's 32-pixel row runs, warp w of `warps` taking runs w, w + warps, ... */
+__device__ __forceinline__ void vis_resolve_phase(const Ctx& c, uint32_t w, uint32_t warps) {
+  const uint32_t items = ((c.seg->width + 31) / 32) * c.seg->height;
+  for (uint32_t i = w; i < items; i += warps) vis_resolve_run(c, i);
 }
 
 /* after geometry: large-triangle scratch overflow check (every block reads the same final counts) */
@@ -2075,9 +2097,10 @@ __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
-/* Every block arrives once per call.  Gives up after KZ_BARRIER_NS and flags KZ_STATUS_BARRIER_TIMEOUT
- * so that all blocks leave the kernel instead of spinning. */
-__device__ bool grid_barrier(KzStatus* st) {
+/* Every block arrives once per call.  A block that has waited `limit_ns` nanoseconds (KzFrame::barrier_ns;
+ * 0: it gives up at its first check) flags KZ_STATUS_BARRIER_TIMEOUT, and every block that sees the flag
+ * leaves the kernel instead of spinning.  No block passes a barrier before all blocks have arrived at it. */
+__device__ bool grid_barrier(KzStatus* st, uint32_t limit_ns) {
   __syncthreads();
   __shared__ uint32_t ok;
   if (threadIdx.x == 0) {
@@ -2097,7 +2120,7 @@ __device__ bool grid_barrier(KzStatus* st) {
           ok = 0;
           break;
         }
-        if (globaltimer() - t0 > KZ_BARRIER_NS) {
+        if (globaltimer() - t0 >= (unsigned long long)limit_ns) {
           atomicOr(&st->flags, KZ_STATUS_BARRIER_TIMEOUT);
           ok = 0;
           break;
@@ -2136,7 +2159,8 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_geometry(KzFrame f
   __shared__ uint32_t sh[40];
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
-  for (uint32_t k = blockIdx.x; k < c.seg->num_chunks; k += gridDim.x) geometry_chunk(c, k, sh);
+  const uint32_t ce = min(f.chunk_end, c.seg->num_chunks);
+  for (uint32_t k = f.chunk_begin + blockIdx.x; k < ce; k += gridDim.x) geometry_chunk(c, k, sh);
 }
 
 #define KZ_IND_THREADS 1024
@@ -2344,19 +2368,23 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_geometry(Kz
 }
 
 /* 4 blocks per SM: 0.313 ms on the 4,096-draw workload against 0.357 (3 blocks) and 0.341 (5 blocks) */
+/* With f.jobs_incremental (the per-draw launch form: one launch after each draw's geometry), a launch takes
+ * the jobs [large_done, pair_count) and its last block to finish moves large_done to pair_count for the next
+ * launch; otherwise it takes all of the segment's jobs. */
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_large(KzFrame f, uint32_t s) {
   kz_pdl_enter();
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s) || !vis_check(c, s)) return;
-  uint32_t njobs = c.cnt->pair_count;
-  const uint2* jobs = reinterpret_cast<const uint2*>(c.seg->bins);
-  uint32_t warps = gridDim.x * (blockDim.x >> 5), w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  uint32_t frags = 0;
-  for (uint32_t j = w; j < njobs; j += warps) frags += vis_large_job(c, jobs[j], threadIdx.x & 31);
-  for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
-  if ((threadIdx.x & 31) == 0 && frags) {
-    atomicAdd(&c.cnt->fragments, frags);
-    atomicAdd(&c.st->fragments_lo, frags);
+  const uint32_t njobs = c.cnt->pair_count;
+  const uint32_t j0 = f.jobs_incremental ? *reinterpret_cast<volatile uint32_t*>(&c.cnt->large_done) : 0u;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5), w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  vis_large_phase(c, j0, njobs, w, warps);
+  if (f.jobs_incremental) {
+    __syncthreads();
+    if (threadIdx.x == 0 && atomicAdd(&c.cnt->large_blocks, 1u) == gridDim.x - 1) {
+      c.cnt->large_done = njobs;
+      c.cnt->large_blocks = 0;
+    }
   }
 }
 
@@ -2366,13 +2394,33 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_vis_resolve(KzF
   kz_pdl_enter();
   Ctx c = make_ctx(f, s);
   if (segment_blocked(c, s)) return;
-  uint32_t items = ((c.seg->width + 31) / 32) * c.seg->height;
-  uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < items; i += warps) vis_resolve_run(c, i);
+  vis_resolve_phase(c, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), gridDim.x * (blockDim.x >> 5));
 }
 
-/* the whole command buffer in one cooperative launch: phases separated by bounded grid barriers,
- * work stolen from per-segment counters */
+/* The phases of visibility segment s inside a persistent kernel: key init, geometry, large-triangle jobs
+ * and resolve, separated by grid barriers.  Pixels, 32-triangle groups, jobs and row runs are strided
+ * statically over the grid's warps, as the separate kernels stride them.  Returns 0 to go on with the next
+ * segment, 1 when the segment's scratch overflowed (every block stops at the same segment, the host replays
+ * from it), 2 when a barrier gave up (the kernel ends).  `last`: no barrier after the resolve. */
+__device__ int persistent_vis_segment(const KzFrame& f, uint32_t s, unsigned char* geo_smem,
+                                      const uint32_t* magic_tab, bool last) {
+  Ctx c = make_ctx(f, s);
+  KzStatus* st = c.st;
+  const uint32_t warps = gridDim.x * (KZ_THREADS / 32), w = blockIdx.x * (KZ_THREADS / 32) + (threadIdx.x >> 5);
+  vis_init_range(*c.seg, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+  if (!grid_barrier(st, f.barrier_ns)) return 2;
+  vis_geometry_warps(c, geo_smem, magic_tab, w, warps);
+  if (!grid_barrier(st, f.barrier_ns)) return 2;
+  if (!vis_check(c, s)) return 1;
+  vis_large_phase(c, 0, c.cnt->pair_count, w, warps);
+  if (!grid_barrier(st, f.barrier_ns)) return 2;
+  vis_resolve_phase(c, w, warps);
+  if (!last && !grid_barrier(st, f.barrier_ns)) return 2;
+  return 0;
+}
+
+/* the whole command buffer in one cooperative launch: phases separated by bounded grid barriers; ordered
+ * segments take their chunks, records and tiles from per-segment work-stealing counters */
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFrame f) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t item;
@@ -2387,38 +2435,10 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
     Ctx c = make_ctx(f, s);
     if (segment_blocked(c, s)) break;
     if (c.seg->mode == KZ_MODE_VISIBILITY) {
-      vis_init_range(*c.seg, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
-      if (!grid_barrier(st)) return;
-      vis_geometry_warps(c, smem, magic_tab, blockIdx.x * (KZ_THREADS / 32) + (threadIdx.x >> 5),
-                         gridDim.x * (KZ_THREADS / 32));
-      if (!grid_barrier(st)) return;
-      if (!vis_check(c, s)) break;
-      uint32_t njobs = c.cnt->pair_count;
-      const uint2* jobs = reinterpret_cast<const uint2*>(c.seg->bins);
-      uint32_t frags = 0;
-      int lane = threadIdx.x & 31;
-      for (;;) {
-        uint32_t j = 0;
-        if (lane == 0) j = atomicAdd(&c.cnt->bin_next, 1u);
-        j = __shfl_sync(0xFFFFFFFFu, j, 0);
-        if (j >= njobs) break;
-        frags += vis_large_job(c, jobs[j], lane);
-      }
-      for (int o = 16; o > 0; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
-      if (lane == 0 && frags) {
-        atomicAdd(&c.cnt->fragments, frags);
-        atomicAdd(&c.st->fragments_lo, frags);
-      }
-      if (!grid_barrier(st)) return;
-      uint32_t items = ((c.seg->width + 31) / 32) * c.seg->height;
-      for (;;) {
-        uint32_t i = 0;
-        if (lane == 0) i = atomicAdd(&c.cnt->tile_next, 1u);
-        i = __shfl_sync(0xFFFFFFFFu, i, 0);
-        if (i >= items) break;
-        vis_resolve_run(c, i);
-      }
-      if (!grid_barrier(st)) return;
+      __syncthreads();
+      const int r = persistent_vis_segment(f, s, smem, magic_tab, false);
+      if (r == 2) return;
+      if (r == 1) break;
       continue;
     }
     for (;;) {
@@ -2426,9 +2446,9 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
       if (k >= c.seg->num_chunks) break;
       geometry_chunk(c, k, geo_sh);
     }
-    if (!grid_barrier(st)) return;
+    if (!grid_barrier(st, f.barrier_ns)) return;
     if (blockIdx.x == 0) scan_tiles(c, s, scan_sh);
-    if (!grid_barrier(st)) return;
+    if (!grid_barrier(st, f.barrier_ns)) return;
     if (segment_blocked(c, s)) break;
     uint32_t n = min(c.cnt->rec_count, c.seg->rec_cap);
     for (;;) {
@@ -2437,14 +2457,29 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
       if (k * blockDim.x >= n) break;
       bin_record(c, i, i < n);
     }
-    if (!grid_barrier(st)) return;
+    if (!grid_barrier(st, f.barrier_ns)) return;
     uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
     for (;;) {
       uint32_t t = grab(&c.cnt->tile_next, &item);
       if (t >= ntiles) break;
       raster_tile(c, t, smem, u8tab);
     }
-    if (!grid_barrier(st)) return;
+    if (!grid_barrier(st, f.barrier_ns)) return;
+  }
+}
+
+/* the persistent form of passes whose segments are all opaque (visibility mode): only the visibility
+ * phases, so the kernel keeps the 64-register budget and the 4 resident blocks per SM of the separate
+ * kernels; the last segment ends without a barrier */
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_persistent_vis(KzFrame f) {
+  __shared__ __align__(16) unsigned char slots[KZ_GEO_SMEM];
+  __shared__ uint32_t magic_tab[KZ_MAGIC_MAX + 1];
+  fill_magic(magic_tab);
+  __syncthreads();
+  for (uint32_t s = f.first_segment; s < f.num_segments; s++) {
+    Ctx c = make_ctx(f, s);
+    if (segment_blocked(c, s)) break;
+    if (persistent_vis_segment(f, s, slots, magic_tab, s + 1 == f.num_segments) != 0) return;
   }
 }
 

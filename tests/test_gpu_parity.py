@@ -77,8 +77,8 @@ def test_kernel_timing_keeps_parity_and_counts_launches(driver, renderer, mode):
     times = driver.kernel_times(run.cb, reset=True)
     assert sum(n for _, n in times.values()) == 2 * run.stats().launches
     assert all(ms > 0 for ms, _ in times.values())
-    if mode == "persistent":
-        assert "kz_k_persistent" in times and "kz_k_vis_geometry" not in times
+    if mode == "persistent":  # an opaque pass: the persistent kernel with only the visibility phases
+        assert "kz_k_persistent_vis" in times and "kz_k_vis_geometry" not in times
     assert driver.kernel_times(run.cb) == {}
 
 
@@ -151,3 +151,13 @@ def test_chained_and_unchained_launches_agree(driver, renderer, case):
         outs.append((color, depth))
         renderer.free_command_buffer(run.cb)
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.gpu
+def test_per_draw_form_launches_geometry_per_draw(renderer):
+    """the per-draw launch form: the key init and the resolve once per pass, the geometry and its
+    large-triangle jobs once per draw"""
+    scene = CASES["batched"]
+    color, depth, stats = _render(renderer, scene, "perdraw", 16)
+    _check(scene, color, depth, stats)
+    assert stats.launches == 2 + 2 * len(scene.draws)
