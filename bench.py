@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (use --mode / --tile as given)")
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip the short timings of the other render configurations in the default run")
     return ap.parse_args()
 
 
@@ -75,7 +77,12 @@ def _base_scene(args):
         return scenes.batched(ndraws=args.ndraws), {"workload": "batched: %d vkCmdDrawIndexed, 2048x2048 RGBA8+D32, "
                                                     "tris/draw log-uniform [16,65536], Lambert, seed 3" % args.ndraws}
     if args.workload == "single":
-        return scenes.single_large(), {"workload": "single large draw: 1M indexed tris, 1920x1080, Lambert, seed 2"}
+        sc = scenes.single_large()
+        nvis, area = scenes.visible_triangles(sc)
+        return sc, {"workload": "single large draw: 1M indexed tris, 1920x1080, Lambert, back-face cull, seed 2",
+                    "visible_triangles": nvis, "visible_mean_area_px": round(area, 3),
+                    "calibration": "camera distance %.3f: the front-facing triangles inside the frustum average "
+                                   "%.2f px" % (scenes.SINGLE_DISTANCE, area)}
     if args.workload == "soup":
         return scenes.small_soup(), {"workload": "plain single draw: 2048 tris, 256x256, seed 1"}
     if args.workload == "textured":
@@ -265,9 +272,10 @@ def main():
     def barrier():
         replicas.barrier(rk)
 
-    def timed_region(cb):
+    def timed_region(cb, run=run, steps=None):
         """K submissions of `cb` between a barrier + synchronize on both sides, timed by CUDA events on the
         queue stream; returns (ms per step over all ranks, clock record)"""
+        steps = args.steps if steps is None else steps
         run.cb = cb
         for _ in range(max(3, args.warmup)):
             run.submit()
@@ -279,7 +287,7 @@ def main():
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         w0 = time.monotonic()
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             run.submit(wait=False)
         e1.record(stream)
         e1.synchronize()
@@ -288,7 +296,7 @@ def main():
         ck = clocks.stop(w0, w1)
         torch.cuda.synchronize()
         barrier()
-        return replicas.max_over_ranks(rk, e0.elapsed_time(e1) / args.steps, device="cuda"), ck
+        return replicas.max_over_ranks(rk, e0.elapsed_time(e1) / steps, device="cuda"), ck
 
     # the headline: the application's command buffer
     ms, ck = timed_region(graph_cb)
@@ -345,6 +353,23 @@ def main():
         out["per_draw"] = {"value": round(tris / (pms / 1e3) / 1e6, 2), "unit": "Mtris/s", "ms_per_step": round(pms, 3),
                            "launches_per_step": int(pst.launches), "steps": steps}
         out["batched_vs_per_draw"] = round(out["value"] / world / out["per_draw"]["value"], 2)
+    # the graph-captured persistent form (one cooperative launch per submission), timed as the headline
+    if mode == "persistent":
+        pers_ms = ms
+    else:
+        r.drv.set_option("mode", "persistent")
+        pcb = run.record()
+        r.drv.set_option("mode", mode)
+        pers_ms, _ = timed_region(pcb)
+        run.cb = graph_cb
+        r.free_command_buffer(pcb)
+    out["persistent"] = {"value": round(replicas.aggregate_rate(rk, tris, pers_ms) / 1e6, 2), "unit": "Mtris/s",
+                         "ms_per_step": round(pers_ms, 4), "steps": args.steps,
+                         "how": "the same draws recorded in the persistent schedule, graph-launched"}
+    if "per_draw" in out:
+        out["persistent_vs_per_draw"] = round(out["persistent"]["value"] / world / out["per_draw"]["value"], 2)
+    if not args.no_others and args.workload == "batched" and args.ndraws == 4096 and not indirect:
+        out["other_workloads"] = other_workloads(r, render, timed_region, rk)
     if not args.no_e2e:
         import ctypes
         import numpy as np
@@ -397,6 +422,42 @@ def main():
     return 0
 
 
+def other_workloads(r, render, timed_region, rk, steps=20):
+    """short timings of the other render configurations (seeded synthetic scenes): each recorded in the
+    batched schedule at tile 16 and graph-launched `steps` times, then once more with kernel timing on for
+    the dominant kernel; device-resident inputs"""
+    from kazan_gb300 import scenes
+    out = {}
+    cases = [("plain small draw: 2,048 non-indexed tris, 256x256, seed 1", scenes.small_soup()),
+             ("single large draw: 1M indexed tris, 1920x1080, Lambert, back-face cull, seed 2", scenes.single_large()),
+             ("ordered blend: 200K tris, 1920x1080, SRC_ALPHA / ONE_MINUS_SRC_ALPHA, depth writes off, seed 4",
+              scenes.ordered_blend())]
+    for name, scene in cases:
+        r.drv.set_option("mode", "batched")
+        r.drv.set_option("tile", 16)
+        run = render.SceneRun(r, scene, host_visible=False, mode="batched", tile=16)
+        ms, ck = timed_region(run.cb, run=run, steps=steps)
+        st = run.stats()
+        r.drv.set_option("kernel_timing", 1)
+        tcb = run.record()
+        r.drv.set_option("kernel_timing", 0)
+        timed_region(tcb, run=run, steps=steps)
+        kt = r.drv.kernel_times(tcb)
+        total = sum(t for t, _ in kt.values())
+        dom = max(kt, key=lambda k: kt[k][0])
+        row = {"ms_per_step": round(ms, 4), "mtris_per_s": round(scene.triangles / (ms / 1e3) / 1e6, 2),
+               "gfrag_per_s": round(st.fragments / (ms / 1e3) / 1e9, 3), "fragments": int(st.fragments),
+               "triangles": scene.triangles, "dominant_kernel": dom, "dominant_share": round(kt[dom][0] / total, 4),
+               "clocks": ck}
+        if scene.shader == "lambert":
+            nvis, area = scenes.visible_triangles(scene)
+            row["visible_triangles"] = nvis
+            row["visible_mean_area_px"] = round(area, 3)
+        out[name] = row
+        r.free_command_buffer(tcb)
+    return out
+
+
 def serve_main(args, rk):
     """the serving configuration: 64 clients with resident scenes, Poisson arrivals swept over rates;
     batched submissions against one request at a time on the same request streams"""
@@ -404,11 +465,12 @@ def serve_main(args, rk):
     r = render.Renderer()
     specs = serving.client_specs()
     t0 = time.perf_counter()
-    backend = serving.VulkanBackend(r, specs, n_views=4, mode=args.mode)
+    backend = serving.VulkanBackend(r, specs, mode=args.mode)
     setup_s = time.perf_counter() - t0
     admitted, resident = serving.admit(backend.sizes, args.budget_gb * 1e9)
-    for i in admitted:  # warm-up: every view once
-        backend.wait(backend.submit([serving.Request(i, v, 0.0) for v in range(4)]))
+    for i in admitted:  # warm-up: every command buffer once
+        backend.wait(backend.submit([serving.Request(i, 0, 0.0, res, serving.TMAX)
+                                     for res in range(len(serving.RESOLUTIONS))]))
     rates = [100, 250, 500, 1000, 2500, 5000, 10000, 20000, 40000]  # the configured sweep, then past saturation
     clocks = Clocks(rk.local)
     clocks.start()
@@ -416,21 +478,23 @@ def serve_main(args, rk):
     rows, best = [], None
     for rate in rates:
         n = int(min(3000, max(200, rate * 1.5)))
-        b, one = serving.sweep(backend, admitted, [rate], n, 4)
+        b, one = serving.sweep(backend, admitted, [rate], n)
         b, one = b[0], one[0]
         rows.append({"rate_req_per_s": rate, "requests": n, "batched": b.as_dict(), "one_at_a_time": one.as_dict()})
         print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
         best = b
     ck = clocks.stop(w0, time.monotonic())
-    launches = sum(r.drv.stats(backend.cbs[i][0]).launches for i in admitted) / max(1, len(admitted))
+    launches = sum(r.drv.stats(backend.runs[i][0].cb).launches for i in admitted) / max(1, len(admitted))
     value = replicas.aggregate_rate(rk, best.mtris_per_s * best.wall_s * 1e6, replicas.max_over_ranks(
         rk, best.wall_s * 1e3, device="cuda")) / 1e6
     out = {"metric": "Mtris/s (serving: 64 clients, Poisson arrivals, batched submissions)", "value": round(value, 2),
            "unit": "Mtris/s", "n_gpus": rk.world, "steps": len(rates), "warmup": 1,
            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32+int64 (16.8 fixed-point edges)", "data": "synthetic (seeded scene generator)",
-           "config": {"workload": "serving: 64 clients, sphere meshes log-uniform [1K, 500K] tris, resolutions "
-                                  "256^2/512^2/1024^2/1920x1080, 4 recorded views each, Poisson arrivals",
+           "config": {"workload": "serving: 64 clients, Poisson arrivals; per request a resolution uniform over "
+                                  "256^2/512^2/1024^2/1920x1080, a triangle count log-uniform in [1K, 500K] (a "
+                                  "prefix of the client's resident 500K-triangle sphere mesh) and its own random MVP "
+                                  "(uniform buffer + indirect command written per request)",
                       "mode": args.mode, "budget_gb": args.budget_gb, "admitted_clients": len(admitted),
                       "resident_gb": round(resident / 1e9, 3), "setup_s": round(setup_s, 2),
                       "max_batch": 64, "max_inflight": 4, "value_at_rate": rates[-1],

@@ -1102,6 +1102,28 @@ static void segment_target(const PassRec& pr, KzSegment& s, uint32_t tile, bool 
   s.area[3] = std::min((int32_t)s.height, s.area[3]);
 }
 
+/* a vertex fetch with vector loads can merge some of the pipeline's attribute loads: an attribute the shaders
+ * read with at least two 32-bit components, in a binding whose stride is a multiple of 8 bytes */
+static bool fetch_vectorizable(const KzPipe& kp) {
+  uint32_t used = kp.pos_input_mask | kp.full_input_mask;
+  for (uint32_t i = 0; i < kp.num_attrs && i < KZ_MAX_VS_INPUTS; i++) {
+    const KzAttr& a = kp.attrs[i];
+    bool wide = (a.format >= KZ_FMT_F32x2 && a.format <= KZ_FMT_F32x4) || (a.format >= KZ_FMT_U32x2 && a.format <= KZ_FMT_U32x4);
+    if (((used >> a.location) & 1u) && wide && kp.binding_stride[a.binding] % 8 == 0) return true;
+  }
+  return false;
+}
+
+/* every binding the shaders read starts 16-byte aligned in this draw */
+static bool bases_aligned16(const KzDraw& d, const KzPipe& kp) {
+  uint32_t used = kp.pos_input_mask | kp.full_input_mask;
+  for (uint32_t i = 0; i < kp.num_attrs && i < KZ_MAX_VS_INPUTS; i++) {
+    const KzAttr& a = kp.attrs[i];
+    if (((used >> a.location) & 1u) && (d.vb[a.binding] & 15u)) return false;
+  }
+  return true;
+}
+
 static int raster_class(const DrawRec& d, bool vis_ok) {
   /* draws that share a class can share one segment: visibility mode with the same key and write mask,
    * or ordered mode; indirect draws never share a segment with direct ones.  Passes whose depth
@@ -1386,15 +1408,20 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   low.mode = options().mode;
   low.tile = options().tile;
   low.timed = options().kernel_timing != 0;
-  std::map<Pipeline*, uint32_t> pipe_index;
-  auto pipe_of = [&](Pipeline* p) -> uint32_t {
-    auto it = pipe_index.find(p);
+  /* one pipeline entry per pipeline and vertex-buffer alignment class: draws whose bound vertex buffers all
+   * start 16-byte aligned use an entry whose vertex fetch uses vector loads */
+  std::map<std::pair<Pipeline*, uint32_t>, uint32_t> pipe_index;
+  auto pipe_of = [&](Pipeline* p, const KzDraw& d) -> uint32_t {
+    uint32_t align = fetch_vectorizable(p->pipe) && bases_aligned16(d, p->pipe) ? 16u : 4u;
+    auto key = std::make_pair(p, align);
+    auto it = pipe_index.find(key);
     if (it != pipe_index.end()) return it->second;
     KzPipe kp = p->pipe;
     uint32_t idx = (uint32_t)low.pipes.size();
     low.pipes.push_back(kp);
     low.pipe_objs.push_back(p);
-    pipe_index[p] = idx;
+    low.pipe_align.push_back(align);
+    pipe_index[key] = idx;
     return idx;
   };
   /* vkCmdUpdateBuffer data: one device block, uploaded now, that the copies read at execution */
@@ -1483,7 +1510,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
         d.samples = s.samples;
         d.rect[2] = std::min(d.rect[2], (int32_t)s.width);
         d.rect[3] = std::min(d.rect[3], (int32_t)s.height);
-        d.pipe = pipe_of(dr.pipe);
+        d.pipe = pipe_of(dr.pipe, d);
         d.prim_base = (uint32_t)prims;
         /* the draw's snapshot: push constants, then its descriptors, padded to whole KZ_PUSH_BYTES units */
         d.push_index = (uint32_t)(low.push.size() / KZ_PUSH_BYTES);
@@ -1625,7 +1652,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   cudaEventCreate(&low.ev_begin);
   cudaEventCreate(&low.ev_end);
   std::string err;
-  low.ks = kernel_set_for(dev, low.pipe_objs, err);
+  low.ks = kernel_set_for(dev, low.pipe_objs, low.pipe_align, err);
   if (!low.ks) {
     log_error("pipeline link failed: %s", err.c_str());
     return VK_ERROR_INITIALIZATION_FAILED;

@@ -112,9 +112,10 @@ const std::vector<char>& texture_object() {
   return obj;
 }
 
-KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std::string& err) {
+KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, const std::vector<uint32_t>& base_align,
+                          std::string& err) {
   std::vector<uint64_t> key;
-  for (Pipeline* p : pipes) key.push_back(p->uid);
+  for (size_t i = 0; i < pipes.size(); i++) key.push_back((pipes[i]->uid << 5) | (base_align[i] & 31u));
   auto it = dev->kernel_sets.find(key);
   if (it != dev->kernel_sets.end()) return it->second;
   const std::vector<char>& obj = pipeline_object();
@@ -124,10 +125,12 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std:
   }
   std::vector<const ir::Shader*> vs, fs;
   std::vector<ptx::VertexLayout> layouts;
-  for (Pipeline* p : pipes) {
+  for (size_t i = 0; i < pipes.size(); i++) {
+    Pipeline* p = pipes[i];
     vs.push_back(p->vs.get());
     fs.push_back(p->fs.get());
     ptx::VertexLayout l;
+    l.base_align = base_align[i];
     l.num_attrs = p->pipe.num_attrs;
     for (uint32_t k = 0; k < p->pipe.num_attrs; k++) {
       l.location[k] = p->pipe.attrs[k].location;

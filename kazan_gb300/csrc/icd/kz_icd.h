@@ -282,6 +282,7 @@ struct Lowered {
   std::vector<KzDraw> draws;
   std::vector<KzPipe> pipes;
   std::vector<Pipeline*> pipe_objs;
+  std::vector<uint32_t> pipe_align;        /* per pipeline entry: alignment of its draws' vertex-buffer bases */
   std::vector<KzChunk> chunks;
   std::vector<KzSegment> segments;
   std::vector<uint64_t> prims_guess;       /* per segment: triangles the scratch is first sized for */
@@ -409,7 +410,10 @@ VkResult device_alloc(size_t bytes, void** out);
 void device_free(void* p);
 const std::vector<char>& pipeline_object();
 const std::vector<char>& texture_object();
-KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, std::string& err);
+/* the linked kernel image for the pipeline entries of a command buffer; base_align[i]: the alignment of the
+ * vertex-buffer base addresses of the draws that use entry i (4 or 16) */
+KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, const std::vector<uint32_t>& base_align,
+                          std::string& err);
 void log_error(const char* fmt, ...);
 
 /* command buffer / queue entry points implemented in kz_cmd.cpp */

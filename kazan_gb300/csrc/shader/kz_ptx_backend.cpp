@@ -134,12 +134,74 @@ class Emitter {
 
   void line(const std::string& s) { out += "  " + s + "\n"; }
 
+  /* vertex inputs loaded in the prologue (vector fetch): bit 4a + c set when component c of attribute a is in
+   * register %kza<4a + c> */
+  uint32_t preloaded = 0;
+
+  /* attribute index of a location in the layout, or -1 */
+  static int attr_of(const VertexLayout* lay, uint32_t loc) {
+    int a = -1;
+    for (uint32_t i = 0; lay && i < lay->num_attrs; i++)
+      if (lay->location[i] == loc) a = (int)i;
+    return a;
+  }
+
+  /* The vector fetch: with 16-byte aligned binding bases, the components the function reads of each 32-bit
+   * attribute are loaded once at the start, with ld.global.nc.v4 where a run of four starts 16-byte aligned
+   * (attribute offset and binding stride), v2 where a run of two starts 8-byte aligned, single words
+   * otherwise; only the attribute's own bytes are read.  The loads then become register moves. */
+  void vertex_preload(const Function& fn, const VertexLayout* lay) {
+    preloaded = 0;
+    if (!lay || lay->base_align < 16) return;
+    uint32_t comps[8] = {};  /* per attribute: components read (bit c) */
+    for (const Inst& i : fn.code) {
+      if (i.op != Op::LdIn || i.imm >= 128) continue;
+      int a = attr_of(lay, i.imm / 16);
+      if (a < 0) continue;
+      uint32_t fmt = lay->format[a];
+      uint32_t ncomp = (fmt >= 1 && fmt <= 4) ? fmt : (fmt >= 6 && fmt <= 9) ? fmt - 5 : 0u;
+      uint32_t c = (i.imm % 16) / 4;
+      if (c < ncomp) comps[a] |= 1u << c;
+    }
+    char buf[200];
+    for (uint32_t a = 0; a < lay->num_attrs && a < 8; a++) {
+      if (!comps[a]) continue;
+      uint32_t k = 32 - __builtin_clz(comps[a]); /* components 0..k-1 are loaded */
+      uint32_t b = lay->binding[a], stride = lay->stride[b];
+      for (uint32_t j = 0; j < k;) {
+        uint32_t o = lay->offset[a] + 4 * j, r = 4 * a + j;
+        if (k - j >= 4 && o % 16 == 0 && stride % 16 == 0) {
+          std::snprintf(buf, sizeof buf, "ld.global.nc.v4.b32 {%%kza%u, %%kza%u, %%kza%u, %%kza%u}, [%%kzvb%u+%u];", r,
+                        r + 1, r + 2, r + 3, b, o);
+          j += 4;
+        } else if (k - j >= 2 && o % 8 == 0 && stride % 8 == 0) {
+          std::snprintf(buf, sizeof buf, "ld.global.nc.v2.b32 {%%kza%u, %%kza%u}, [%%kzvb%u+%u];", r, r + 1, b, o);
+          j += 2;
+        } else {
+          std::snprintf(buf, sizeof buf, "ld.global.nc.b32 %%kza%u, [%%kzvb%u+%u];", r, b, o);
+          j += 1;
+        }
+        line(buf);
+      }
+      preloaded |= ((1u << k) - 1u) << (4 * a);
+    }
+  }
+
   /* load of vertex input (location, component) for the generated fetch */
   void vertex_load(const VertexLayout* lay, uint32_t off, Ty ty, const std::string& dst) {
     char buf[160];
     if (off == 128 || off == 132) {
       line("mov.b32 " + dst + ", " + (off == 128 ? "%kzvid" : "%kziid") + ";");
       return;
+    }
+    {
+      int a = attr_of(lay, off / 16);
+      uint32_t c = (off % 16) / 4;
+      if (a >= 0 && a < 8 && ((preloaded >> (4 * a + c)) & 1u)) {
+        std::snprintf(buf, sizeof buf, "mov.b32 %s, %%kza%u;", dst.c_str(), 4 * (uint32_t)a + c);
+        line(buf);
+        return;
+      }
     }
     uint32_t loc = off / 16, comp = (off % 16) / 4;
     int a = -1;
@@ -202,7 +264,10 @@ class Emitter {
     auto L = [&](uint32_t l) { return "$" + pfx + "_L" + std::to_string(l); };
     char buf[160];
     bool vertex = kind != Kind::Fragment && kind != Kind::FragmentRegs;
-    if (vertex) vertex_prologue(lay);
+    if (vertex) {
+      vertex_prologue(lay);
+      vertex_preload(fn, lay);
+    }
     for (const Inst& i : fn.code) {
       switch (i.op) {
         case Op::Const:
@@ -567,6 +632,7 @@ std::string function_text(const char* fname, Kind kind, const std::vector<const 
   s += buf;
   s += "  .reg .b32 %kzsel, %kzt, %kzvid, %kziid, %kzv0, %kzv1, %kzv2;\n"
        "  .reg .b64 %kzin, %kzpush, %kzout, %kzdraw, %kzoff, %kzpg, %kzub, %kzd;\n  .reg .b64 %kzvb<8>;\n"
+       "  .reg .b32 %kza<32>;\n"
        "  .reg .pred %kzp;\n";
   if (e.nu) s += "  .reg .b64 %kzu<" + std::to_string(e.nu) + ">;\n";
   if (e.uses_sep) s += "  .reg .b32 %kzs<8>;\n  .local .align 16 .b8 kzsd[32];\n";

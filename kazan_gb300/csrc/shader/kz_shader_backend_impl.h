@@ -18,6 +18,10 @@ struct VertexLayout {
   uint32_t location[8] = {}, binding[8] = {}, format[8] = {}, offset[8] = {}; /* format: KzAttrFormat */
   uint32_t stride[8] = {};
   uint32_t instanced = 0; /* bit b: binding b advances per instance */
+  /* byte alignment every binding's base address (buffer + bind offset) has in the draws that use this entry:
+   * 4 (what Vulkan requires of 32-bit components), or 16; with 16, attribute components are fetched with
+   * 8- and 16-byte vector loads where their offsets and the binding stride allow */
+  uint32_t base_align = 4;
   /* descriptor slot of the first array element of (set, binding) in the pipeline layout (KZ_DESC_OFFSET +
    * 32 * slot bytes into a draw's push snapshot); ~0u for bindings the layout does not have */
   uint32_t desc_slot[KZ_MAX_DESC_SETS][KZ_MAX_DESC_BINDINGS];

@@ -459,10 +459,13 @@ class SceneRun:
     become one indirect call each, the others one call of drawCount = len(draws).
     counts: with indirect, record the vkCmdDraw*IndirectCountKHR variants instead, with maxDrawCount as
     above and each call's draw count read from a host-visible buffer of one u32 per call (`counts` gives
-    the initial words; the test rewrites them with write_buffer(run.count_buf, ...))."""
+    the initial words; the test rewrites them with write_buffer(run.count_buf, ...)).
+    ubo_host_visible: the uniform buffer of a scene with `ubo` in host-visible memory (default: as
+    host_visible).  buffers: (vertex buffer, index buffer) already holding the scene's data, shared instead
+    of created.  vb_offset: bytes before the vertex data in its buffer (the vkCmdBindVertexBuffers offset)."""
 
     def __init__(self, r, scene, host_visible=False, mode=None, tile=None, keep_mapped=False, depth_host_visible=None,
-                 indirect=None, counts=None):
+                 indirect=None, counts=None, ubo_host_visible=None, buffers=None, vb_offset=0):
         self.r, self.scene = r, scene
         self.indirect = indirect
         d = r.drv
@@ -470,12 +473,20 @@ class SceneRun:
             d.set_option("mode", mode)
         if tile is not None:
             d.set_option("tile", tile)
-        self.vb = r.create_buffer(scene.vertices.nbytes, vk.BUFFER_USAGE_VERTEX, host_visible)
-        r.write_buffer(self.vb, scene.vertices, keep_mapped=keep_mapped and host_visible)
-        self.ib = None
-        if scene.indexed:
-            self.ib = r.create_buffer(scene.indices.nbytes, vk.BUFFER_USAGE_INDEX, host_visible)
-            r.write_buffer(self.ib, scene.indices, keep_mapped=keep_mapped and host_visible)
+        self.vb_offset = vb_offset
+        if buffers is not None:
+            self.vb, self.ib = buffers
+        else:
+            # the vertex data starts `vb_offset` bytes into the buffer, where vkCmdBindVertexBuffers binds it
+            data = np.ascontiguousarray(scene.vertices).view(np.uint8).ravel()
+            if vb_offset:
+                data = np.concatenate([np.zeros(vb_offset, np.uint8), data])
+            self.vb = r.create_buffer(data.nbytes, vk.BUFFER_USAGE_VERTEX, host_visible)
+            r.write_buffer(self.vb, data, keep_mapped=keep_mapped and host_visible)
+            self.ib = None
+            if scene.indexed:
+                self.ib = r.create_buffer(scene.indices.nbytes, vk.BUFFER_USAGE_INDEX, host_visible)
+                r.write_buffer(self.ib, scene.indices, keep_mapped=keep_mapped and host_visible)
         ns = scene.samples
         self.samples = None
         if ns > 1:
@@ -510,7 +521,8 @@ class SceneRun:
             for i, dr in enumerate(scene.draws):
                 if dr.mvp is not None:
                     mats[i, :16] = dr.mvp
-            self.ubo_buf = r.create_buffer(mats.nbytes, vk.BUFFER_USAGE_UNIFORM, host_visible)
+            self.ubo_buf = r.create_buffer(mats.nbytes, vk.BUFFER_USAGE_UNIFORM,
+                                           host_visible if ubo_host_visible is None else ubo_host_visible)
             r.write_buffer(self.ubo_buf, mats)
             self.set_layouts = [r.set_layout([(0, vk.DESCRIPTOR_UNIFORM_BUFFER_DYNAMIC, 1)])]
             self.dsets = r.descriptor_sets(self.set_layouts[0])
@@ -552,7 +564,7 @@ class SceneRun:
             sets = (c_void_p * 1)(self.dsets[0].value)
             d.vkCmdBindDescriptorSets(cb, vk.BIND_POINT_GRAPHICS, self.layout, 0, 1, sets, 0, None)
         bufs = (c_void_p * 1)(self.vb.handle.value)
-        offs = (c_uint64 * 1)(0)
+        offs = (c_uint64 * 1)(self.vb_offset)
         d.vkCmdBindVertexBuffers(cb, 0, 1, bufs, offs)
         if self.ib is not None:
             d.vkCmdBindIndexBuffer(cb, self.ib.handle, 0, vk.INDEX_TYPE_UINT32)

@@ -1,14 +1,21 @@
 """Serving loop for the draw path: render requests from many clients arrive over time and are submitted to
 one Vulkan queue in batches.
 
-Workload (the serving configuration): 64 clients; aggregate Poisson arrivals at rate lambda; each client owns
-a resident scene (a sphere mesh from the single-draw generator with a log-uniform triangle count in
-[1,000, 500,000], one resolution drawn from {256x256, 512x512, 1024x1024, 1920x1080}, Lambert shading) and a
-few recorded camera views; a request renders one view of its client's scene.
+Workload (the serving configuration): 64 clients; aggregate Poisson arrivals at rate lambda.  Every request
+carries its own data: a resolution drawn uniformly from {256x256, 512x512, 1024x1024, 1920x1080}, a triangle
+count log-uniform in [1,000, 500,000] and a random model-view-projection matrix (a uniform random rotation
+and a translation in [-5, 5]^3, as the batched draws).  Each client keeps resident a sphere mesh of 500,000
+triangles from the single-draw generator; a request draws the first `triangles` of them.
 
-- Residency and admission: vertex/index buffers, attachments and the driver's per-command-buffer scratch
-  stay on the device.  Clients are admitted in order while their device bytes fit the HBM budget;
-  requests of clients that were not admitted are rejected (counted, not served).
+- Residency and admission: the clients' meshes, one colour + depth framebuffer per client and resolution,
+  and one recorded command buffer per client and resolution (with the driver's scratch) stay on the device.
+  Clients are admitted in order while their device bytes fit the HBM budget; requests of clients that were
+  not admitted are rejected (counted, not served).
+- Per-request data: the command buffers draw through vkCmdDrawIndexedIndirect with the matrix in a uniform
+  buffer; before a request is submitted the host writes its matrix (64 bytes) and its indirect command
+  (20 bytes) into that command buffer's host-visible parameter buffers, which the driver uploads with the
+  submission.  Two requests that need the same command buffer are never in flight together: the dispatcher
+  holds the later one back.
 - Batching: the dispatcher submits every request that has arrived (up to `max_batch`) with one
   vkQueueSubmit and one fence, keeping at most `max_inflight` submissions in flight.
 - Latency: arrival time -> the host sees the submission's fence signalled.
@@ -16,6 +23,7 @@ few recorded camera views; a request renders one view of its client's scene.
 
 The scheduler (`serve`) drives any backend with submit / poll, so the policy is tested on the CPU with a
 simulated queue (tests/test_serving.py)."""
+import ctypes
 import math
 import time
 from dataclasses import dataclass, field
@@ -24,47 +32,44 @@ from typing import List, Optional
 import numpy as np
 
 RESOLUTIONS = [(256, 256), (512, 512), (1024, 1024), (1920, 1080)]
+TMIN, TMAX = 1000, 500_000
 
 
 @dataclass
 class ClientSpec:
     index: int
-    triangles: int
-    width: int
-    height: int
+    triangles: int   # triangles of the client's resident mesh (requests draw a prefix of them)
     seed: int
 
 
 @dataclass
 class Request:
     client: int
-    view: int
+    view: int                      # the request's camera: stream index of its random MVP (kz_mvp_batched)
     arrival: float                 # seconds from the start of the run
+    res: int = 0                   # index into RESOLUTIONS
+    triangles: int = TMIN          # triangles drawn (a prefix of the client's mesh)
     start: Optional[float] = None  # submitted
     done: Optional[float] = None   # fence seen signalled
     rejected: bool = False
 
 
-def client_specs(n_clients=64, seed=5, tmin=1000, tmax=500_000):
-    """the clients' scenes: triangle count log-uniform in [tmin, tmax], resolution uniform over RESOLUTIONS"""
-    rng = np.random.default_rng(seed)
-    out = []
-    for i in range(n_clients):
-        t = int(math.exp(rng.uniform(math.log(tmin), math.log(tmax))))
-        w, h = RESOLUTIONS[int(rng.integers(len(RESOLUTIONS)))]
-        out.append(ClientSpec(i, t, w, h, seed ^ (i + 1)))
-    return out
+def client_specs(n_clients=64, seed=5, tmax=TMAX):
+    """the clients' resident meshes: `tmax` triangles each, their own seeds"""
+    return [ClientSpec(i, tmax, seed ^ (i + 1)) for i in range(n_clients)]
 
 
-def poisson_requests(rate, n_requests, n_clients, n_views, seed=5):
-    """`n_requests` arrivals of a Poisson process of aggregate rate `rate` (per second); each request names
-    a uniformly drawn client and view"""
+def poisson_requests(rate, n_requests, n_clients, seed=5, tmin=TMIN, tmax=TMAX):
+    """`n_requests` arrivals of a Poisson process of aggregate rate `rate` (per second); each request names a
+    uniformly drawn client and resolution, a triangle count log-uniform in [tmin, tmax] and its own camera"""
     rng = np.random.default_rng(seed * 7919 + int(rate))
     gaps = rng.exponential(1.0 / rate, n_requests)
     t = np.cumsum(gaps)
     clients = rng.integers(0, n_clients, n_requests)
-    views = rng.integers(0, n_views, n_requests)
-    return [Request(int(c), int(v), float(a)) for a, c, v in zip(t, clients, views)]
+    res = rng.integers(0, len(RESOLUTIONS), n_requests)
+    tris = np.exp(rng.uniform(math.log(tmin), math.log(tmax), n_requests)).astype(np.int64)
+    tris = np.clip(tris, tmin, tmax)
+    return [Request(int(c), k, float(a), int(rz), int(n)) for k, (a, c, rz, n) in enumerate(zip(t, clients, res, tris))]
 
 
 def admit(sizes, budget):
@@ -106,6 +111,11 @@ class Backend:
     def triangles(self, request):
         raise NotImplementedError
 
+    def slot(self, request):
+        """what a request occupies while it is in flight (two requests with the same slot are never in flight
+        together); None: nothing"""
+        return None
+
 
 @dataclass
 class ServeResult:
@@ -136,6 +146,7 @@ def serve(backend, requests, admitted, max_batch=64, max_inflight=4, clock=time.
     admitted = set(admitted)
     pending = []          # arrived, not yet submitted
     inflight = []         # (handle, [requests])
+    busy = set()          # slots of the requests in flight
     batches = []
     served = []
     i, n = 0, len(requests)
@@ -155,15 +166,26 @@ def serve(backend, requests, admitted, max_batch=64, max_inflight=4, clock=time.
             t = clock() - t0
             for r in reqs:
                 r.done = t
+                busy.discard(backend.slot(r))
             served.extend(reqs)
         if pending and len(inflight) < max_inflight:
-            batch, pending = pending[:max_batch], pending[max_batch:]
-            t = clock() - t0
-            for r in batch:
-                r.start = t
-            inflight.append((backend.submit(batch), batch))
-            batches.append(len(batch))
-            continue
+            batch, held = [], []
+            for r in pending:
+                sl = backend.slot(r)
+                if len(batch) < max_batch and (sl is None or sl not in busy):
+                    batch.append(r)
+                    if sl is not None:
+                        busy.add(sl)
+                else:
+                    held.append(r)
+            if batch:
+                pending = held
+                t = clock() - t0
+                for r in batch:
+                    r.start = t
+                inflight.append((backend.submit(batch), batch))
+                batches.append(len(batch))
+                continue
         if not pending and not inflight and i < n:
             wait = requests[i].arrival - (clock() - t0)
             if wait > 0:
@@ -181,37 +203,55 @@ def serve(backend, requests, admitted, max_batch=64, max_inflight=4, clock=time.
 
 
 class VulkanBackend(Backend):
-    """the clients' resident scenes on one Vulkan device of this driver; one recorded command buffer per
-    (client, view); a submission is one vkQueueSubmit of its requests' command buffers with one fence"""
+    """the clients' resident meshes, framebuffers and command buffers on one Vulkan device of this driver; a
+    submission is one vkQueueSubmit of its requests' command buffers with one fence"""
 
-    def __init__(self, renderer, specs, n_views=4, mode="batched"):
+    def __init__(self, renderer, specs, mode="batched"):
         from ctypes import byref, c_uint32, c_void_p
         from . import render, scenes, vk
-        self.r, self.vk = renderer, vk
+        self.r, self.vk, self.render, self.scenes = renderer, vk, render, scenes
         self.specs = specs
-        self.n_views = n_views
-        self.cbs = []         # per client: one recorded command buffer per view
-        self.sizes = []       # per client: device bytes (buffers, attachments, driver scratch per view)
+        self.meshes = []      # per client: (vertices, indices) on the host (for checks)
+        self.runs = []        # per client: one SceneRun per resolution (indirect draw, matrix in a uniform buffer)
+        self.params = []      # per client and resolution: (mapped uniform buffer, mapped indirect command)
+        self.sizes = []       # per client: device bytes (mesh, framebuffers, command buffers' scratch)
         for sp in specs:
             v, idx = scenes.sphere_mesh(sp.seed, sp.triangles)
-            mvps = []
-            for k in range(n_views):
-                m = np.empty(16, dtype=np.float32)
-                scenes.lib().kz_mvp_batched(sp.seed, k, sp.width, sp.height, scenes._fp(m))
-                mvps.append(m)
-            sc = scenes.Scene("serve", sp.width, sp.height, "lambert", v, idx,
-                              [scenes.Draw(0, sp.triangles, 0, mvps[0])], cull=2)
-            run = render.SceneRun(renderer, sc, host_visible=False, mode=mode)
-            views = [run.cb]
-            for m in mvps[1:]:
-                sc.draws[0].mvp = m
-                views.append(run.record())
-            self.cbs.append(views)
-            st = renderer.drv.stats(run.cb)
-            per_view_scratch = st.rec_cap * 64 + st.pair_cap * 4 + sp.width * sp.height * 8 + 4096
-            self.sizes.append(v.nbytes + idx.nbytes + sp.width * sp.height * 8 + n_views * per_view_scratch)
+            self.meshes.append((v, idx))
+            vb = renderer.create_buffer(v.nbytes, vk.BUFFER_USAGE_VERTEX, False)
+            renderer.write_buffer(vb, v)
+            ib = renderer.create_buffer(idx.nbytes, vk.BUFFER_USAGE_INDEX, False)
+            renderer.write_buffer(ib, idx)
+            size = v.nbytes + idx.nbytes
+            runs, params = [], []
+            for w, h in RESOLUTIONS:
+                sc = scenes.Scene("serve", w, h, "lambert", v, idx, [scenes.Draw(0, sp.triangles, 0, self.mvp(sp, 0, w, h))],
+                                  cull=2, ubo=True)
+                run = render.SceneRun(renderer, sc, host_visible=False, mode=mode, indirect="host",
+                                      ubo_host_visible=True, buffers=(vb, ib))
+                runs.append(run)
+                params.append((renderer.map(run.ubo_buf), renderer.map(run.cmds)))
+                st = renderer.drv.stats(run.cb)
+                size += w * h * 8 + st.rec_cap * 64 + st.pair_cap * 4 + w * h * 8 + 65536
+            self.runs.append(runs)
+            self.params.append(params)
+            self.sizes.append(size)
         self._fences = []
         self._c_void_p, self._byref, self._c_uint32 = c_void_p, byref, c_uint32
+
+    def mvp(self, spec, view, width, height):
+        """the column-major matrix of camera `view` of a client (random rotation, translation in [-5, 5]^3)"""
+        m = np.empty(16, dtype=np.float32)
+        self.scenes.lib().kz_mvp_batched(spec.seed, view, width, height, self.scenes._fp(m))
+        return m
+
+    def request_scene(self, q):
+        """what request q renders, as a scene (for the oracle)"""
+        v, idx = self.meshes[q.client]
+        w, h = RESOLUTIONS[q.res]
+        sp = self.specs[q.client]
+        return self.scenes.Scene("serve", w, h, "lambert", v, idx,
+                                 [self.scenes.Draw(0, q.triangles, 0, self.mvp(sp, q.view, w, h))], cull=2, ubo=True)
 
     def _fence(self):
         if self._fences:
@@ -224,7 +264,15 @@ class VulkanBackend(Backend):
 
     def submit(self, requests):
         vk = self.vk
-        cbs = (self._c_void_p * len(requests))(*[self.cbs[q.client][q.view].value for q in requests])
+        for q in requests:
+            sp = self.specs[q.client]
+            w, h = RESOLUTIONS[q.res]
+            ubo, cmd = self.params[q.client][q.res]
+            m = self.mvp(sp, q.view, w, h)
+            ctypes.memmove(ubo, m.ctypes.data, 64)
+            c = np.array([3 * min(q.triangles, sp.triangles), 1, 0, 0, 0], dtype=np.uint32)
+            ctypes.memmove(cmd, c.ctypes.data, c.nbytes)
+        cbs = (self._c_void_p * len(requests))(*[self.runs[q.client][q.res].cb.value for q in requests])
         si = vk.VkSubmitInfo(vk.ST_SUBMIT_INFO, None, 0, None, None, len(requests), cbs, 0, None)
         f = self._fence()
         vk.check("vkQueueSubmit", self.r.drv.vkQueueSubmit(self.r.queue, 1, self._byref(si), f))
@@ -242,7 +290,14 @@ class VulkanBackend(Backend):
         return False
 
     def triangles(self, request):
-        return self.specs[request.client].triangles
+        return min(request.triangles, self.specs[request.client].triangles)
+
+    def slot(self, request):
+        return (request.client, request.res)
+
+    def image(self, request):
+        """the colour image of request's framebuffer (read after the request completed)"""
+        return self.runs[request.client][request.res].read()[0]
 
     def close(self):
         for f in self._fences:
@@ -250,12 +305,12 @@ class VulkanBackend(Backend):
         self._fences = []
 
 
-def sweep(backend, admitted, rates, n_requests, n_views, seed=5, max_batch=64, max_inflight=4):
+def sweep(backend, admitted, rates, n_requests, seed=5, max_batch=64, max_inflight=4, tmin=TMIN, tmax=TMAX):
     """serve the same-rate request streams batched and one at a time; returns (batched, one_at_a_time)"""
     batched, single = [], []
     for rate in rates:
-        reqs = poisson_requests(rate, n_requests, len(backend.specs), n_views, seed)
+        reqs = poisson_requests(rate, n_requests, len(backend.specs), seed, tmin, tmax)
         batched.append(serve(backend, reqs, admitted, max_batch=max_batch, max_inflight=max_inflight))
-        reqs = poisson_requests(rate, n_requests, len(backend.specs), n_views, seed)
+        reqs = poisson_requests(rate, n_requests, len(backend.specs), seed, tmin, tmax)
         single.append(serve(backend, reqs, admitted, max_batch=1, max_inflight=1))
     return batched, single

@@ -92,7 +92,7 @@ def small_cases():
     """the draw-path scene families at sizes the oracle finishes in well under a second"""
     return {
         "soup": scenes.small_soup(),
-        "sphere": scenes.single_large(tris=60_000, width=480, height=270),
+        "sphere": scenes.single_large(tris=60_000, width=480, height=270, dist=1.30),
         "batched": scenes.batched(ndraws=48, width=512, height=512, lo=16, hi=4096),
         "blend": scenes.ordered_blend(n=4000, width=640, height=360, amin=4.0, amax=2048.0),
         "tess": tessellated_square(),

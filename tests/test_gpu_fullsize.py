@@ -110,15 +110,51 @@ def test_injected_allocation_failures(driver, renderer):
 @pytest.mark.gpu
 def test_serving_loop_serves_a_request_stream(renderer):
     specs = serving.client_specs(n_clients=4, tmax=20_000)
-    backend = serving.VulkanBackend(renderer, specs, n_views=2)
+    backend = serving.VulkanBackend(renderer, specs)
     admitted, resident = serving.admit(backend.sizes, 40e9)
     assert admitted == [0, 1, 2, 3] and resident > 0
-    reqs = serving.poisson_requests(2000, 300, len(specs), 2)
+    reqs = serving.poisson_requests(2000, 300, len(specs), tmin=1000, tmax=20_000)
     res = serving.serve(backend, reqs, admitted, max_batch=16, max_inflight=2)
     assert res.served == 300 and res.rejected == 0
     assert 0 < res.p50_ms <= res.p99_ms
     # a budget below one client's bytes admits nobody, and every request is rejected
     none, _ = serving.admit(backend.sizes, min(backend.sizes) - 1)
-    res = serving.serve(backend, serving.poisson_requests(2000, 50, len(specs), 2), none)
+    res = serving.serve(backend, serving.poisson_requests(2000, 50, len(specs)), none)
     assert res.served == 0 and res.rejected == 50
+    backend.close()
+
+
+class _CheckingBackend(serving.VulkanBackend):
+    """reads each request's image back as soon as its fence signals (one request in flight at a time)"""
+
+    def submit(self, requests):
+        self.last = list(requests)
+        return super().submit(requests)
+
+    def poll(self, handle):
+        done = super().poll(handle)
+        if done:
+            for q in self.last:
+                self.images.append((q, self.image(q)))
+        return done
+
+
+@pytest.mark.gpu
+def test_served_images_match_the_oracle(renderer):
+    """a seeded sample of requests, each with its own resolution, triangle count and camera, served one at a
+    time; every image equals the oracle's render of that request"""
+    specs = serving.client_specs(n_clients=3, tmax=20_000)
+    backend = _CheckingBackend(renderer, specs)
+    backend.images = []
+    reqs = serving.poisson_requests(500, 12, len(specs), seed=11, tmin=1000, tmax=20_000)
+    res = serving.serve(backend, reqs, [0, 1, 2], max_batch=1, max_inflight=1)
+    assert res.served == 12 and len(backend.images) == 12
+    assert len({q.res for q in reqs}) >= 3 and len({q.triangles for q in reqs}) == 12
+    lit = 0
+    for q, img in backend.images:
+        ref_c, _, st = kz_oracle.render(backend.request_scene(q), threads=8)
+        mism = np.argwhere(np.any(img != ref_c, axis=-1))
+        assert mism.size == 0, "request %d: colour differs at %d pixels" % (q.view, len(mism))
+        lit += st["fragments"] > 0
+    assert lit >= 6
     backend.close()

@@ -161,3 +161,16 @@ def test_per_draw_form_launches_geometry_per_draw(renderer):
     color, depth, stats = _render(renderer, scene, "perdraw", 16)
     _check(scene, color, depth, stats)
     assert stats.launches == 2 + 2 * len(scene.draws)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("offset", [0, 4, 8, 12, 16, 48])
+@pytest.mark.parametrize("case", ["soup", "sphere", "batched"])
+def test_vertex_buffer_bind_offsets(renderer, case, offset):
+    """vertex buffers bound at offsets that are and are not multiples of 16 bytes: the draws with 16-byte
+    aligned bases fetch attributes with vector loads, the others word by word; the images are the same"""
+    scene = CASES[case]
+    run = render.SceneRun(renderer, scene, mode="batched", tile=16, vb_offset=offset)
+    run.submit()
+    color, depth = run.read()
+    _check(scene, color, depth, run.stats())
