@@ -51,12 +51,15 @@ KZ_API PFN_vkVoidFunction vk_icdGetPhysicalDeviceProcAddr(VkInstance instance, c
  *           (no graph capture) with a pair of timing events around every launch; see kzGetKernelTimes
  *   "pdl"   "1" (default) / "0": command buffers ended while it is on launch each kernel that follows
  *           another with programmatic stream serialization (its launch overlaps the predecessor's end)
+ *   "tma"   "1" (default) / "0": command buffers ended while it is on stage the colour and depth of each
+ *           tile of kz_k_raster_direct through TMA tensor copies (where the attachment's base address and
+ *           row pitch are multiples of 16 bytes); with "0" the tiles are read and written with plain loads
  *   "barrier_ns" "N": command buffers ended while it is set give their persistent kernels' grid barriers
  *           up after waiting N nanoseconds (default 4000000000; 0 gives up at the first check).  A barrier
  *           that gives up sets KZ_STATUS_BARRIER_TIMEOUT and the submission completes with
  *           VK_ERROR_DEVICE_LOST; the kernel returns and the CUDA context stays usable
- * Returns 0, or -1 for an unknown key or value.  The KZ_MODE, KZ_TILE, KZ_TRACE, KZ_KERNEL_TIMING, KZ_PDL
- * and KZ_FAULT=alloc:N environment variables set the initial values. */
+ * Returns 0, or -1 for an unknown key or value.  The KZ_MODE, KZ_TILE, KZ_TRACE, KZ_KERNEL_TIMING, KZ_PDL,
+ * KZ_TMA and KZ_FAULT=alloc:N environment variables set the initial values. */
 KZ_API int kzDriverSetOption(const char* key, const char* value);
 
 /* The CUDA stream (cudaStream_t) a queue executes on, for callers that time submissions with CUDA
@@ -85,8 +88,8 @@ KZ_API int kzGetCommandBufferStats(VkCommandBuffer commandBuffer, KzCommandBuffe
 #define KZ_KERNEL_KIND_NAMES                                                                          \
   {"kz_k_persistent", "kz_k_vis_init", "kz_k_vis_geometry", "kz_k_vis_large", "kz_k_vis_resolve",      \
    "kz_k_geometry",   "kz_k_scan",     "kz_k_bin",          "kz_k_raster",    "kz_k_clear",         \
-   "kz_k_indirect",   "kz_k_indirect_tables", "kz_k_resolve", "kz_k_persistent_vis"}
-#define KZ_KERNEL_KINDS 14
+   "kz_k_indirect",   "kz_k_indirect_tables", "kz_k_resolve", "kz_k_persistent_vis", "kz_k_raster_direct"}
+#define KZ_KERNEL_KINDS 15
 
 /* Device time of a command buffer recorded with "kernel_timing" on: for each kernel kind, the summed
  * durations (CUDA events on the queue stream around each launch) and the number of launches over all

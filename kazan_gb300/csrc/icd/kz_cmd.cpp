@@ -18,6 +18,9 @@
 #include <cstring>
 #include <thread>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "kazan_driver.h"
 #include "kz_icd.h"
 #include "../kz_srgb_table.h"
@@ -1170,6 +1173,37 @@ static VkResult size_scratch(Device* dev, Lowered& low, uint32_t rec_cap, uint32
   return VK_SUCCESS;
 }
 
+/* cuTensorMapEncodeTiled, reached through the runtime (the library links no libcuda) */
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+/* The tensor map of a tile's block of a 4-byte-per-texel attachment: 32-bit texels, width x height, rows
+ * `pitch` bytes apart, box tile x tile.  Needs a 16-byte aligned base and pitch (the tensor copies' rule);
+ * false (plain loads and stores) otherwise. */
+static bool encode_tile_map(CUtensorMap* m, uint64_t base, uint32_t width, uint32_t height, uint32_t pitch,
+                            uint32_t tile) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || !base || (base & 15u) || (pitch & 15u) || tile > 16 || width == 0 || height == 0) return false;
+  cuuint64_t dims[2] = {width, height};
+  cuuint64_t strides[1] = {pitch};
+  cuuint32_t box[2] = {tile, tile};
+  cuuint32_t elem[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, reinterpret_cast<void*>(base), dims, strides, box, elem,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 static void upload_tables(Lowered& low) {
   size_t o_draws = 0;
   size_t o_pipes = align_up(o_draws + low.draws.size() * sizeof(KzDraw), 256);
@@ -1187,6 +1221,7 @@ static void upload_tables(Lowered& low) {
     std::memcpy(host.data() + o_segs, low.segments.data(), low.segments.size() * sizeof(KzSegment));
   if (!low.push.empty()) std::memcpy(host.data() + o_push, low.push.data(), low.push.size());
   cudaMemcpy(low.d_tables, host.data(), o_lut + low.draw_lut.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  if (!low.tmaps.empty()) cudaMemcpy(low.d_tables + low.o_tmaps, low.tmaps.data(), low.tmaps.size(), cudaMemcpyHostToDevice);
 }
 
 static uint32_t grid_cap(Device* dev) { return (uint32_t)std::max(1, dev->pd->sm_count) * 8u; }
@@ -1230,6 +1265,17 @@ static void launch(Device* dev, std::vector<TimedLaunch>* timing, int kind, cons
     timing->push_back(t);
   }
   chain = true;
+}
+
+/* an ordered segment that kz_k_raster_direct serves: one sample per pixel, D32 depth, tiles of at most
+ * 16x16, and no draw whose fragment shader is a function call (only none, or the colour pass-through) */
+static bool raster_direct(const Lowered& low, const KzSegment& seg) {
+  if (seg.samples > 1 || seg.depth_format != KZ_DF_D32 || seg.tile > 16) return false;
+  for (uint32_t i = seg.first_draw; i < seg.first_draw + seg.num_draws; i++) {
+    const KzPipe& p = low.pipes[low.draws[i].pipe];
+    if (p.has_fs && !p.fs_passthrough) return false;
+  }
+  return true;
 }
 
 /* enqueue the lowered command buffer from segment `start` on */
@@ -1352,7 +1398,8 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
           launch(dev, timing, KK_BIN, cfg, ks->bin, args, chain);
           cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, seg.tiles_x * seg.tiles_y)));
           cfg.dynamicSmemBytes = KZ_DYN_SMEM;
-          launch(dev, timing, KK_RASTER, cfg, ks->raster, args, chain);
+          if (raster_direct(low, seg)) launch(dev, timing, KK_RASTER_DIRECT, cfg, ks->raster_direct, args, chain);
+          else launch(dev, timing, KK_RASTER, cfg, ks->raster, args, chain);
           launches += 3;
         }
       }
@@ -1598,7 +1645,8 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   size_t o_push = align_up(o_segs + low.segments.size() * sizeof(KzSegment), 256);
   size_t o_lut = align_up(o_push + low.push.size(), 256);
   size_t o_ind = align_up(o_lut + low.draw_lut.size() * sizeof(uint32_t), 256);
-  size_t o_counters = align_up(o_ind + ind_words * sizeof(uint32_t), 256);
+  size_t o_tmaps = align_up(o_ind + ind_words * sizeof(uint32_t), 256);
+  size_t o_counters = align_up(o_tmaps + low.segments.size() * 2 * sizeof(CUtensorMap), 256);
   size_t o_status = align_up(o_counters + low.segments.size() * sizeof(KzSegCounters), 256);
   low.tables_bytes = o_status + sizeof(KzStatus);
   void* p = nullptr;
@@ -1631,6 +1679,18 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
       s.chunk_table = (uint64_t)(uintptr_t)(low.d_tables + o_ind + ind_off[i] * sizeof(uint32_t));
       s.lut_table = s.chunk_table + (uint64_t)s.chunk_cap * sizeof(KzChunk);
     }
+  }
+  /* ordered segments that kz_k_raster_direct serves stage each tile's colour and depth through tensor copies */
+  static_assert(sizeof(CUtensorMap) == 128, "tensor map size");
+  low.o_tmaps = o_tmaps;
+  low.tmaps.assign(low.segments.size() * 2 * sizeof(CUtensorMap), 0);
+  for (size_t i = 0; i < low.segments.size() && options().tma; i++) {
+    KzSegment& s = low.segments[i];
+    if (s.mode != KZ_MODE_ORDERED || !raster_direct(low, s)) continue;
+    CUtensorMap* m = reinterpret_cast<CUtensorMap*>(low.tmaps.data()) + 2 * i;
+    const uint64_t at = (uint64_t)(uintptr_t)(low.d_tables + o_tmaps + 2 * i * sizeof(CUtensorMap));
+    if (encode_tile_map(m, s.color, s.width, s.height, s.color_pitch, s.tile)) s.tmap_color = at;
+    if (encode_tile_map(m + 1, s.depth, s.width, s.height, s.depth_pitch, s.tile)) s.tmap_depth = at + sizeof(CUtensorMap);
   }
   r = size_scratch(dev, low, (uint32_t)rec_cap, (uint32_t)pair_cap);
   if (r != VK_SUCCESS) return r;

@@ -44,6 +44,8 @@ Options& options() {
     if (f && !std::strncmp(f, "alloc:", 6)) r.fault_alloc = std::atol(f + 6);
     const char* kt = std::getenv("KZ_KERNEL_TIMING");
     if (kt) r.kernel_timing = std::atoi(kt);
+    const char* tm = std::getenv("KZ_TMA");
+    if (tm) r.tma = std::atoi(tm) != 0;
     const char* pd = std::getenv("KZ_PDL");
     if (pd) r.pdl = std::atoi(pd) != 0;
     return r;
@@ -171,6 +173,7 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, cons
   } names[] = {{"kz_k_geometry", &ks->geometry}, {"kz_k_scan", &ks->scan},
                {"kz_k_bin", &ks->bin},           {"kz_k_raster", &ks->raster},
                {"kz_k_persistent", &ks->persistent}, {"kz_k_persistent_vis", &ks->persistent_vis},
+               {"kz_k_raster_direct", &ks->raster_direct},
                {"kz_k_clear", &ks->clear},
                {"kz_k_vis_init", &ks->vis_init}, {"kz_k_vis_geometry", &ks->vis_geometry},
                {"kz_k_vis_large", &ks->vis_large}, {"kz_k_vis_resolve", &ks->vis_resolve},
@@ -1671,6 +1674,11 @@ extern "C" KZ_API int kzDriverSetOption(const char* key, const char* value) {
   if (!std::strcmp(key, "pdl")) {
     if (std::strcmp(value, "0") && std::strcmp(value, "1")) return -1;
     o.pdl = value[0] == '1';
+    return 0;
+  }
+  if (!std::strcmp(key, "tma")) {
+    if (std::strcmp(value, "0") && std::strcmp(value, "1")) return -1;
+    o.tma = value[0] == '1';
     return 0;
   }
   if (!std::strcmp(key, "barrier_ns")) {

@@ -211,6 +211,7 @@ enum KernelKind {
   KK_INDIRECT_TABLES,
   KK_RESOLVE,
   KK_PERSISTENT_VIS,
+  KK_RASTER_DIRECT,
   KK_COUNT
 };
 
@@ -225,7 +226,8 @@ struct PipelineCache {};
 struct KernelSet {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t geometry = nullptr, scan = nullptr, bin = nullptr, raster = nullptr, persistent = nullptr,
-               persistent_vis = nullptr, clear = nullptr, vis_init = nullptr, vis_geometry = nullptr,
+               persistent_vis = nullptr, raster_direct = nullptr, clear = nullptr, vis_init = nullptr,
+               vis_geometry = nullptr,
                vis_large = nullptr, vis_resolve = nullptr, indirect = nullptr, indirect_tables = nullptr,
                resolve = nullptr;
   int persistent_blocks = 0;
@@ -304,6 +306,8 @@ struct Lowered {
   /* device memory */
   char* d_tables = nullptr;
   size_t tables_bytes = 0;
+  std::vector<uint8_t> tmaps;              /* per segment: the colour and depth tensor maps (128 bytes each) */
+  size_t o_tmaps = 0;                      /* their offset in d_tables */
   KzFrame frame{};
   char* d_records = nullptr;
   char* d_bins = nullptr;
@@ -402,6 +406,7 @@ struct Options {
   int pdl = 1;        /* KZ_PDL: a kernel that follows another kernel in a submission is launched with
                          programmatic stream serialization (its launch overlaps the predecessor's completion) */
   uint32_t barrier_ns = 4000000000u; /* a persistent kernel's grid barrier gives up after waiting this long */
+  int tma = 1;        /* KZ_TMA: kz_k_raster_direct stages each tile's colour and depth through tensor copies */
 };
 Options& options();
 

@@ -248,6 +248,10 @@ typedef struct KzSegment {
   uint32_t samples;          /* 1, or 4: colour and depth texels hold KZ_MS_SAMPLES samples each, sample s of
                                 pixel x at byte 16 x + 4 s of its row (ordered segments, D32 depth, tiles <= 16) */
   uint32_t pad2;
+  /* ordered segments raster by kz_k_raster_direct: device addresses of the TMA tensor maps (CUtensorMap, 128
+   * bytes, 64-byte aligned) of the colour and depth attachments -- 32-bit texels, width x height, box of
+   * tile x tile texels -- or 0 where the tile is read and written with plain loads and stores */
+  uint64_t tmap_color, tmap_depth;
 } KzSegment;
 
 /* status words written by the kernels (one per submission) */
@@ -258,7 +262,8 @@ enum KzStatusBits {
   KZ_STATUS_BARRIER_TIMEOUT = 4,
   KZ_STATUS_BIN_TOO_LARGE = 8,
   KZ_STATUS_INDIRECT_RANGE = 16,  /* an indirect command reads past its bound buffers: that draw was skipped */
-  KZ_STATUS_INDIRECT_LIMIT = 32   /* an indirect segment's triangles reach 2^32: the segment was skipped */
+  KZ_STATUS_INDIRECT_LIMIT = 32,  /* an indirect segment's triangles reach 2^32: the segment was skipped */
+  KZ_STATUS_TMA_TIMEOUT = 64      /* a tile's tensor copy did not complete within its wait limit */
 };
 
 typedef struct KzStatus {

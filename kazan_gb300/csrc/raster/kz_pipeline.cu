@@ -165,8 +165,9 @@ __device__ __forceinline__ KzChunk chunk_at(const Ctx& c, uint32_t k) {
 }
 
 __device__ void tri_vertices(const KzDraw& d, uint32_t local, uint32_t vid[3], uint32_t& iid) {
-  uint32_t inst = local / d.tri_count;
-  uint32_t t = local - inst * d.tri_count;
+  /* one instance (the common case, warp-uniform): no division */
+  const uint32_t inst = d.instance_count == 1 ? 0u : local / d.tri_count;
+  const uint32_t t = local - inst * d.tri_count;
   iid = d.first_instance + inst;
   if (d.indexed == 1) {
     const uint32_t* ib = reinterpret_cast<const uint32_t*>(d.ib) + (size_t)3 * t;
@@ -485,8 +486,10 @@ __device__ bool shade_setup(const Ctx& c, uint32_t g, int32_t x, int32_t y, uint
 
 /* interpolate varyings and run the fragment shader.  REGS: pass the inputs in registers (kz_fs_r8) when
  * the interface has at most 8 varyings; otherwise through a KzFsIn in local memory (kz_fs), which costs
- * fewer registers in kernels that are already at their register limit. */
-template <bool REGS>
+ * fewer registers in kernels that are already at their register limit.  CALLS false: the caller knows that
+ * every pipeline of the segment has no fragment shader or one that only copies varyings 0..3 to the colour,
+ * so no shader function is called (and none of the call's register saving is compiled in). */
+template <bool REGS, bool CALLS = true>
 __device__ __forceinline__ uint32_t shade_pixel(const Ctx& c, const Shade& s, int32_t x, int32_t y, const int64_t E[3],
                                                 float z, float col[4]) {
   const KzPipe& p = c.pipes[s.pipe];
@@ -503,7 +506,7 @@ __device__ __forceinline__ uint32_t shade_pixel(const Ctx& c, const Shade& s, in
     col[0] = col[1] = col[2] = col[3] = 0.0f;
     return 0;
   }
-  if (p.fs_passthrough) {
+  if (!CALLS || p.fs_passthrough) {
     /* the shader only copies varyings 0..3 to the colour: the same values without the call */
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -684,12 +687,17 @@ __device__ __forceinline__ bool vis_decode(uint32_t mode, unsigned long long k, 
 __device__ __forceinline__ uint32_t status_flags(const KzStatus* st) {
   return *reinterpret_cast<const volatile uint32_t*>(&st->flags);
 }
+/* Whether segment s must be skipped (a barrier gave up, or an earlier or this segment overflowed its
+ * scratch).  Called by every thread of the block at once; the answer is the same for all of them: other
+ * blocks may set the flags while this block reads them, and a block whose threads disagreed would leave some
+ * of them waiting at a later __syncthreads for threads that have left. */
 __device__ __forceinline__ bool segment_blocked(const Ctx& c, uint32_t s) {
   uint32_t f = status_flags(c.st);
-  if (f & KZ_STATUS_BARRIER_TIMEOUT) return true;
-  if (f & (KZ_STATUS_RECORD_OVERFLOW | KZ_STATUS_PAIR_OVERFLOW))
-    return *reinterpret_cast<const volatile uint32_t*>(&c.st->failed_segment) <= s;
-  return false;
+  bool blocked = false;
+  if (f & KZ_STATUS_BARRIER_TIMEOUT) blocked = true;
+  else if (f & (KZ_STATUS_RECORD_OVERFLOW | KZ_STATUS_PAIR_OVERFLOW))
+    blocked = *reinterpret_cast<const volatile uint32_t*>(&c.st->failed_segment) <= s;
+  return __syncthreads_or(blocked ? 1 : 0) != 0;
 }
 __device__ void mark_failed(KzStatus* st, uint32_t bits, uint32_t s) {
   atomicMin(&st->failed_segment, s);
@@ -1250,10 +1258,11 @@ struct VEntry {
                     a clip plane (near, far, guard band); bit 12 non-finite */
 };
 
-__device__ __forceinline__ VEntry vertex_entry(const KzDraw& d, float4 clip) {
+/* the clip position and clip outcode of a shaded vertex (its projection follows in vertex_project) */
+__device__ __forceinline__ VEntry vertex_code(float4 clip) {
   VEntry e;
   e.clip = clip;
-  const float c[4] = {e.clip.x, e.clip.y, e.clip.z, e.clip.w};
+  const float c[4] = {clip.x, clip.y, clip.z, clip.w};
   uint32_t code = 0;
   if (!(isfinite(c[0]) && isfinite(c[1]) && isfinite(c[2]) && isfinite(c[3]))) {
     code = 1u << 12;
@@ -1268,7 +1277,7 @@ __device__ __forceinline__ VEntry vertex_entry(const KzDraw& d, float4 clip) {
      * signs of those float sums equal these comparisons (4w is an exact scaling, and a rounded sum of two
      * floats has the sign of the exact sum), so the codes are the same */
     const float gw = fmul(KZ_GUARD_BAND, c[3]);
-    code |= (code & 48u) << 2; /* near z < 0, far z > w */
+    code |= (code & 48u) << 2;
     code |= (c[0] < -gw) ? 256u : 0u;
     code |= (c[0] > gw) ? 512u : 0u;
     code |= (c[1] < -gw) ? 1024u : 0u;
@@ -1276,14 +1285,19 @@ __device__ __forceinline__ VEntry vertex_entry(const KzDraw& d, float4 clip) {
   }
   e.X = e.Y = 0;
   e.z = 0.0f;
-  if (!(code & ((63u << 6) | (1u << 12)))) {
+  e.code = code;
+  return e;
+}
+
+/* the projected 16.8 position and depth of a vertex with a clip position inside every clip plane */
+__device__ __forceinline__ void vertex_project(const KzDraw& d, VEntry& e) {
+  if (!(e.code & ((63u << 6) | (1u << 12)))) {
+    const float c[4] = {e.clip.x, e.clip.y, e.clip.z, e.clip.w};
     Proj p = project(d, c);
     e.X = p.X;
     e.Y = p.Y;
     e.z = p.z;
   }
-  e.code = code;
-  return e;
 }
 
 /* set up the triangle of three shaded vertices.  Returns 1 with `out` set when the triangle's box holds
@@ -1510,7 +1524,14 @@ __device__ __forceinline__ uint32_t vis_geometry_warp(const Ctx& c, uint32_t chu
     const KzPos3 q = kz_vs_pos3(d.pipe, &d, vid[0], vid[1], vid[2], iid, push);
     VEntry e[3];
 #pragma unroll
-    for (int j = 0; j < 3; j++) e[j] = vertex_entry(d, q.p[j]);
+    for (int j = 0; j < 3; j++) e[j] = vertex_code(q.p[j]);
+    /* project only triangles that are not trivially outside the view volume (whole off-screen meshes skip
+     * the divisions); vis_triangle rejects the others on the same codes */
+    const uint32_t any = e[0].code | e[1].code | e[2].code;
+    if (!(any & (1u << 12)) && !(e[0].code & e[1].code & e[2].code & 63u)) {
+#pragma unroll
+      for (int j = 0; j < 3; j++) vertex_project(d, e[j]);
+    }
     kind = vis_triangle(c, d, p, ch.draw, d.prim_base + local, e, r, frags);
   }
   vis_emit_large_warp(c, r, kind == 2);
@@ -1792,24 +1813,97 @@ __device__ __forceinline__ float* depth_sample(const KzSegment& seg, int32_t x, 
   return reinterpret_cast<float*>(reinterpret_cast<char*>(seg.depth) + (size_t)y * seg.depth_pitch) + 4 * x + s;
 }
 
+/* ---------------- TMA staging of a tile's framebuffer block (kz_k_raster_direct) ---------------- */
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+/* the shared-memory copy of one tile's colour and depth texels (row-major, tile x tile) and the mbarrier its
+ * tensor loads complete on */
+struct TileStage {
+  uint32_t* color;
+  float* depth;
+  uint64_t* mbar;
+  uint32_t phase; /* parity of the mbarrier phase the next load completes */
+};
+
+#define KZ_TMA_WAIT_NS 100000000ull /* a tile's tensor loads complete within microseconds; give up after 100 ms */
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+/* one 2-D tensor load of the box at texel (x, y) into shared memory, completing its bytes on the mbarrier */
+__device__ __forceinline__ void tma_load_2d(void* dst, uint64_t tmap, int32_t x, int32_t y, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_addr(dst)), "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(mbar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_store_2d(uint64_t tmap, int32_t x, int32_t y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];"
+               ::"l"(tmap), "r"(x), "r"(y), "r"(smem_addr(src))
+               : "memory");
+}
+
+/* wait until the mbarrier completes the phase of parity `parity`; false after KZ_TMA_WAIT_NS */
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
+  const uint32_t a = smem_addr(mbar);
+  unsigned long long t0 = 0;
+  for (uint32_t i = 0;; i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (i == 0) t0 = globaltimer();
+    else if (globaltimer() - t0 > KZ_TMA_WAIT_NS) return false;
+  }
+}
+
 /* MS: a 4x multisampled pass (PER 1, D32): coverage, depth test, depth write and colour per sample; the
  * fragment shader runs once per pixel, at the pixel centre, when some covered sample passes the depth
  * test */
-template <int PER, bool DS, bool MS>
-__device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* smem, const float* u8tab, int base) {
+/* CALLS: see shade_pixel.  TMA (PER 1, one sample, D32): `ts` holds the tile's colour and depth in shared
+ * memory for the attachments that have a tensor map: thread 0 starts their tensor loads before the bin is
+ * sorted, every thread waits for them before reading its pixels, and after the raster thread 0 writes the
+ * block back with tensor stores (pixels outside the framebuffer are neither read nor written; pixels of the
+ * tile outside the render area are written back unchanged).  Returns false when a load did not complete
+ * (KZ_STATUS_TMA_TIMEOUT). */
+template <int PER, bool DS, bool MS, bool CALLS, bool TMA = false>
+__device__ bool raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* smem, const float* u8tab, int base,
+                                    TileStage* ts = nullptr) {
+  static_assert(!TMA || (PER == 1 && !DS && !MS), "TMA staging: one pixel per thread, one sample, D32");
   const KzSegment& seg = *c.seg;
   TileInfo ti;
-  if (!tile_info(seg, t, ti)) return;
+  if (!tile_info(seg, t, ti)) return true;
   bool clear_c = seg.color_load == KZ_LOAD_CLEAR, clear_d = seg.depth_load == KZ_LOAD_CLEAR;
   /* DS: a D16 / D24S8 attachment (integer depths, stencil); otherwise D32 without stencil */
   const bool has_st = DS && seg.depth_format == KZ_DF_D24S8, clear_s = has_st && seg.stencil_load == KZ_LOAD_CLEAR;
   const bool srgb = cf_srgb(seg.color_format);
-  if (ti.n == 0 && !clear_c && !clear_d && !clear_s) return;
+  if (ti.n == 0 && !clear_c && !clear_d && !clear_s) return true;
   if (ti.n > KZ_SORT_CAP) {
     if (threadIdx.x == 0) atomicOr(&c.st->flags, KZ_STATUS_BIN_TOO_LARGE);
-    return;
+    return true;
   }
   const int T = (int)seg.tile;
+  const bool tma_c = TMA && seg.tmap_color && seg.color, tma_d = TMA && seg.tmap_depth && seg.depth;
+  if (TMA && (tma_c || tma_d) && threadIdx.x == 0) {
+    const uint32_t bytes = (uint32_t)(T * T * 4) * ((tma_c ? 1u : 0u) + (tma_d ? 1u : 0u));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(ts->mbar)), "r"(bytes)
+                 : "memory");
+    if (tma_c) tma_load_2d(ts->color, seg.tmap_color, ti.ox, ti.oy, ts->mbar);
+    if (tma_d) tma_load_2d(ts->depth, seg.tmap_depth, ti.ox, ti.oy, ts->mbar);
+  }
   unsigned long long* sk = reinterpret_cast<unsigned long long*>(smem);
   BatchEntry* batch = reinterpret_cast<BatchEntry*>(smem + KZ_SORT_CAP * 8);
   const KzTriRecord* recs = reinterpret_cast<const KzTriRecord*>(seg.records);
@@ -1841,6 +1935,16 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
       __syncthreads();
     }
   }
+  if (TMA && (tma_c || tma_d)) {
+    /* the tile's texels in shared memory before any thread reads them */
+    bool ok = __syncthreads_and(mbar_wait(ts->mbar, ts->phase) ? 1 : 0) != 0;
+    if (!ok) { /* give up: flag it, wait once more (bounded) for the copies in flight, and end the kernel */
+      if (threadIdx.x == 0) atomicOr(&c.st->flags, KZ_STATUS_TMA_TIMEOUT);
+      __syncthreads_and(mbar_wait(ts->mbar, ts->phase) ? 1 : 0);
+      return false;
+    }
+    ts->phase ^= 1u;
+  }
   /* this thread's pixels: offsets in the tile and whether they lie in the framebuffer and render area */
   const bool has_color = seg.color != 0, has_depth = seg.depth != 0;
   int lx[PER], ly[PER];
@@ -1870,8 +1974,11 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
       }
       continue;
     }
-    if (has_color) colv[q] = to_rgba(clear_c ? seg.clear_color : *color_px(seg, x, y), seg.color_format);
-    if (has_depth && DS) {
+    if (TMA && tma_c) colv[q] = to_rgba(clear_c ? seg.clear_color : ts->color[ly[q] * T + lx[q]], seg.color_format);
+    else if (has_color) colv[q] = to_rgba(clear_c ? seg.clear_color : *color_px(seg, x, y), seg.color_format);
+    if (TMA && tma_d) {
+      depv[q] = clear_d ? seg.clear_depth : ts->depth[ly[q] * T + lx[q]];
+    } else if (has_depth && DS) {
       uint32_t s0 = 0;
       float d0 = clear_d && (clear_s || !has_st) ? 0.0f : load_depth(seg, x, y, s0);
       depv[q] = clear_d ? seg.clear_depth : d0;
@@ -1981,7 +2088,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
           float zc = fadd(fminf(fmaxf(ffma(l2, r.dz2, ffma(l1, r.dz1, r.z0)), be.zmin), be.zmax), 0.0f);
           int32_t x = ti.ox + lx[q], y = ti.oy + ly[q];
           float col[4];
-          if (shade_pixel<false>(c, be.s, x, y, E, zc, col)) continue;
+          if (shade_pixel<false, CALLS>(c, be.s, x, y, E, zc, col)) continue;
 #pragma unroll
           for (int s = 0; s < NS; s++) {
             if (!((pass >> s) & 1u)) continue;
@@ -2024,7 +2131,7 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
         float col[4];
         if (DS && be.stencil) {
           /* late tests when the shader may discard: a discarded fragment changes nothing */
-          if ((be.stencil & 2u) && shade_pixel<false>(c, be.s, x, y, E, z, col)) continue;
+          if ((be.stencil & 2u) && shade_pixel<false, CALLS>(c, be.s, x, y, E, z, col)) continue;
           const bool dpass = !dtest || depth_cmp(be.depth >> 2, zq, depv[q]);
           const bool front = (be.s.r.info >> 8) & 1u;
           const uint32_t w0 = front ? be.st[0] : be.st[2], w1 = front ? be.st[1] : be.st[3];
@@ -2035,10 +2142,10 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
           }
           stv[q] = stencil_apply(dpass ? (w0 >> 3) & 7u : (w0 >> 6) & 7u, sv, w1);
           if (!dpass) continue;
-          if (!(be.stencil & 2u) && shade_pixel<false>(c, be.s, x, y, E, z, col)) continue;
+          if (!(be.stencil & 2u) && shade_pixel<false, CALLS>(c, be.s, x, y, E, z, col)) continue;
         } else {
           if (dtest && !depth_cmp(be.depth >> 2, zq, depv[q])) continue;
-          if (shade_pixel<false>(c, be.s, x, y, E, z, col)) continue;
+          if (shade_pixel<false, CALLS>(c, be.s, x, y, E, z, col)) continue;
         }
         if (dtest && (be.depth & 2u)) depv[q] = zq;
         if (!has_color) continue;
@@ -2063,25 +2170,41 @@ __device__ void raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
       }
       continue;
     }
-    if (has_color) *color_px(seg, x, y) = from_rgba(colv[q], seg.color_format);
-    if (has_depth && DS) store_depth(seg, x, y, depv[q], stv[q]);
+    if (TMA && tma_c) ts->color[ly[q] * T + lx[q]] = from_rgba(colv[q], seg.color_format);
+    else if (has_color) *color_px(seg, x, y) = from_rgba(colv[q], seg.color_format);
+    if (TMA && tma_d) ts->depth[ly[q] * T + lx[q]] = depv[q];
+    else if (has_depth && DS) store_depth(seg, x, y, depv[q], stv[q]);
     else if (has_depth) *depth_px(seg, x, y) = depv[q];
   }
+  if (TMA && (tma_c || tma_d)) {
+    /* the block back to the attachments: the shared-memory writes made visible to the tensor stores, then
+     * thread 0 stores and waits until the stores have read shared memory (the next tile reuses it) */
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (tma_c) tma_store_2d(seg.tmap_color, ti.ox, ti.oy, ts->color);
+      if (tma_d) tma_store_2d(seg.tmap_depth, ti.ox, ti.oy, ts->depth);
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    }
+    __syncthreads();
+  }
+  return true;
 }
 
 __device__ void raster_tile(const Ctx& c, uint32_t t, unsigned char* smem, const float* u8tab) {
   const uint32_t T = c.seg->tile;
   const bool ds = c.seg->depth_format != KZ_DF_D32;
   if (c.seg->samples > 1) { /* tiles of at most 16 x 16 */
-    raster_tile_ordered<1, false, true>(c, t, smem, u8tab, 0);
+    raster_tile_ordered<1, false, true, true>(c, t, smem, u8tab, 0);
   } else if (T <= 16) {
-    if (ds) raster_tile_ordered<1, true, false>(c, t, smem, u8tab, 0);
-    else raster_tile_ordered<1, false, false>(c, t, smem, u8tab, 0);
+    if (ds) raster_tile_ordered<1, true, false, true>(c, t, smem, u8tab, 0);
+    else raster_tile_ordered<1, false, false, true>(c, t, smem, u8tab, 0);
   } else {
     for (int base = 0; base < (int)(T * T); base += 4 * KZ_THREADS) {
       __syncthreads();
-      if (ds) raster_tile_ordered<4, true, false>(c, t, smem, u8tab, base);
-      else raster_tile_ordered<4, false, false>(c, t, smem, u8tab, base);
+      if (ds) raster_tile_ordered<4, true, false, true>(c, t, smem, u8tab, base);
+      else raster_tile_ordered<4, false, false, true>(c, t, smem, u8tab, base);
     }
   }
   __syncthreads();
@@ -2090,12 +2213,6 @@ __device__ void raster_tile(const Ctx& c, uint32_t t, unsigned char* smem, const
 }
 
 /* ---------------- grid barrier (persistent kernel) ---------------- */
-
-__device__ __forceinline__ unsigned long long globaltimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 
 /* Every block arrives once per call.  A block that has waited `limit_ns` nanoseconds (KzFrame::barrier_ns;
  * 0: it gives up at its first check) flags KZ_STATUS_BARRIER_TIMEOUT, and every block that sees the flag
@@ -2346,6 +2463,37 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster(KzFrame 
   fill_color_tabs(u8tab);
   uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) raster_tile(c, t, smem, u8tab);
+}
+
+/* kz_k_raster for the common ordered segment -- one sample per pixel, D32 depth, tiles of at most 16x16, and
+ * pipelines that call no fragment-shader function (none, or one that only copies the interpolated colour):
+ * a kernel with only that instance of the tile raster, so that its register allocation serves it alone;
+ * each tile's colour and depth are staged in shared memory by TMA tensor copies where the segment has
+ * tensor maps */
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster_direct(KzFrame f, uint32_t s) {
+  kz_pdl_enter();
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float u8tab[KZ_CTAB_FLOATS];
+  /* the tile's framebuffer block (tiles of at most 16 x 16 texels) */
+  __shared__ __align__(128) uint32_t tile_color[16 * 16];
+  __shared__ __align__(128) float tile_depth[16 * 16];
+  __shared__ __align__(8) uint64_t tile_mbar;
+  Ctx c = make_ctx(f, s);
+  if (segment_blocked(c, s)) return;
+  fill_color_tabs(u8tab);
+  if (threadIdx.x == 0) mbar_init(&tile_mbar, 1);
+  __syncthreads();
+  TileStage ts;
+  ts.color = tile_color;
+  ts.depth = tile_depth;
+  ts.mbar = &tile_mbar;
+  ts.phase = 0;
+  uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    if (!raster_tile_ordered<1, false, false, false, true>(c, t, smem, u8tab, 0, &ts)) return;
+    __syncthreads();
+    if (threadIdx.x == 0) reinterpret_cast<uint32_t*>(c.seg->tile_count)[t] = 0; /* as raster_tile leaves it */
+  }
 }
 
 extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_vis_init(KzFrame f, uint32_t s) {

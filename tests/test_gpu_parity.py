@@ -1,10 +1,12 @@
 """GPU parity: every scene rendered through the driver's Vulkan entry points must equal the CPU oracle
 bit for bit (colour bytes, depth bits) and cover the same number of fragments, in each execution mode
 and for each bin tile size."""
+import dataclasses
+
 import numpy as np
 import pytest
 
-from kazan_gb300 import render
+from kazan_gb300 import render, scenes
 from oracle import kz_oracle
 
 from scene_cases import small_cases
@@ -174,3 +176,28 @@ def test_vertex_buffer_bind_offsets(renderer, case, offset):
     run.submit()
     color, depth = run.read()
     _check(scene, color, depth, run.stats())
+
+
+def _blend_scene(width, height, seed=12):
+    """3,000 blended triangles of 4 to 1,500 px, fewer on framebuffers so small that their clipped pieces
+    would pass the 4,096 records one tile's bin sorts"""
+    n = 3000 if width * height >= 64 * 64 else 300
+    return dataclasses.replace(scenes.ordered_blend(seed=seed, n=n, width=width, height=height, amin=4.0,
+                                                    amax=1500.0), clear_color=(0.2, 0.3, 0.4, 0.5))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tma", [1, 0])
+@pytest.mark.parametrize("size", [(640, 360), (100, 37), (333, 200), (8, 8)])
+@pytest.mark.parametrize("tile", [8, 16])
+def test_tile_staging_by_tensor_copies(driver, renderer, size, tile, tma):
+    """the ordered tile raster with each tile's colour and depth staged through TMA tensor copies (and, for
+    comparison, with plain loads): partial tiles at the right and bottom edges, a width whose rows are not a
+    multiple of 16 bytes (333: plain loads and stores), and a framebuffer smaller than a tile"""
+    scene = _blend_scene(*size)
+    driver.set_option("tma", tma)
+    try:
+        color, depth, stats = _render(renderer, scene, "batched", tile)
+    finally:
+        driver.set_option("tma", 1)
+    _check(scene, color, depth, stats)
