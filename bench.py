@@ -422,17 +422,18 @@ def main():
     return 0
 
 
-def other_workloads(r, render, timed_region, rk, steps=20):
+def other_workloads(r, render, timed_region, rk):
     """short timings of the other render configurations (seeded synthetic scenes): each recorded in the
-    batched schedule at tile 16 and graph-launched `steps` times, then once more with kernel timing on for
-    the dominant kernel; device-resident inputs"""
+    batched schedule at tile 16 and graph-launched for a few hundred milliseconds, then once more with kernel
+    timing on for the dominant kernel; device-resident inputs"""
     from kazan_gb300 import scenes
     out = {}
-    cases = [("plain small draw: 2,048 non-indexed tris, 256x256, seed 1", scenes.small_soup()),
-             ("single large draw: 1M indexed tris, 1920x1080, Lambert, back-face cull, seed 2", scenes.single_large()),
+    cases = [("plain small draw: 2,048 non-indexed tris, 256x256, seed 1", scenes.small_soup(), 2000),
+             ("single large draw: 1M indexed tris, 1920x1080, Lambert, back-face cull, seed 2", scenes.single_large(),
+              800),
              ("ordered blend: 200K tris, 1920x1080, SRC_ALPHA / ONE_MINUS_SRC_ALPHA, depth writes off, seed 4",
-              scenes.ordered_blend())]
-    for name, scene in cases:
+              scenes.ordered_blend(), 100)]
+    for name, scene, steps in cases:
         r.drv.set_option("mode", "batched")
         r.drv.set_option("tile", 16)
         run = render.SceneRun(r, scene, host_visible=False, mode="batched", tile=16)

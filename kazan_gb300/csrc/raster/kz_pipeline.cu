@@ -767,7 +767,9 @@ __device__ void store_record(const Ctx& c, uint32_t idx, const KzTriRecord& r) {
   }
 }
 
-/* slow path (clipped primitives): one record at a time */
+/* slow path (clipped primitives): one record at a time.  Its tile counts follow the rule bin_record places
+ * the record by: a record whose box lies in one tile is counted there without the overlap test (as
+ * count_tiles counts it); a count that missed a record its bin receives would spill into the next tile's bin */
 __device__ void emit_record(const Ctx& c, KzTriRecord& r) {
   uint32_t idx = atomicAdd(&c.cnt->rec_count, 1u);
   store_record(c, idx, r);
@@ -775,6 +777,10 @@ __device__ void emit_record(const Ctx& c, KzTriRecord& r) {
   int tx0, ty0, tx1, ty1;
   tile_range(seg, r, tx0, ty0, tx1, ty1);
   uint32_t* tc = reinterpret_cast<uint32_t*>(seg.tile_count);
+  if (tx0 == tx1 && ty0 == ty1) {
+    atomicAdd(&tc[ty0 * seg.tiles_x + tx0], 1u);
+    return;
+  }
   Edges e;
   edges_of(r, e);
   for (int ty = ty0; ty <= ty1; ty++)
@@ -958,7 +964,12 @@ __device__ void bin_record(const Ctx& c, uint32_t ri, bool active) {
   uint32_t base = 0;
   if (single && leader == (int)(threadIdx.x & 31)) base = to[t] + atomicAdd(&cur[t], (uint32_t)__popc(peers));
   base = __shfl_sync(0xFFFFFFFFu, base, leader);
-  if (single) bins[base + __popc(peers & lanemask_lt())] = ri;
+  /* every write stays inside its tile's bin [to[t], to[t + 1]) (the counts and this placement follow one rule,
+   * so none is dropped; the bound keeps a miscount from reaching another tile's bin or past the buffer) */
+  if (single) {
+    const uint32_t pos = base + (uint32_t)__popc(peers & lanemask_lt());
+    if (pos < to[t + 1]) bins[pos] = ri;
+  }
   if (!active || single) return;
   Edges e;
   edges_of(r, e);
@@ -966,7 +977,8 @@ __device__ void bin_record(const Ctx& c, uint32_t ri, bool active) {
     for (int tx = tx0; tx <= tx1; tx++)
       if (tile_overlaps(seg, e, tx, ty)) {
         uint32_t tt = ty * seg.tiles_x + tx;
-        bins[to[tt] + atomicAdd(&cur[tt], 1u)] = ri;
+        const uint32_t pos = to[tt] + atomicAdd(&cur[tt], 1u);
+        if (pos < to[tt + 1]) bins[pos] = ri;
       }
 }
 

@@ -181,19 +181,21 @@ def test_vertex_buffer_bind_offsets(renderer, case, offset):
 def _blend_scene(width, height, seed=12):
     """3,000 blended triangles of 4 to 1,500 px, fewer on framebuffers so small that their clipped pieces
     would pass the 4,096 records one tile's bin sorts"""
-    n = 3000 if width * height >= 64 * 64 else 300
+    n = 3000 if width * height >= 16 * 16 else 1000
     return dataclasses.replace(scenes.ordered_blend(seed=seed, n=n, width=width, height=height, amin=4.0,
                                                     amax=1500.0), clear_color=(0.2, 0.3, 0.4, 0.5))
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("tma", [1, 0])
-@pytest.mark.parametrize("size", [(640, 360), (100, 37), (333, 200), (8, 8)])
+@pytest.mark.parametrize("size", [(640, 360), (100, 37), (333, 200), (8, 8), (16, 16)])
 @pytest.mark.parametrize("tile", [8, 16])
 def test_tile_staging_by_tensor_copies(driver, renderer, size, tile, tma):
     """the ordered tile raster with each tile's colour and depth staged through TMA tensor copies (and, for
     comparison, with plain loads): partial tiles at the right and bottom edges, a width whose rows are not a
-    multiple of 16 bytes (333: plain loads and stores), and a framebuffer smaller than a tile"""
+    multiple of 16 bytes (333: plain loads and stores), a framebuffer of one tile, and tiny framebuffers where
+    most triangles are clipped into several pieces, many of them inside one tile without covering a sample
+    (they are counted and binned by the same rule)"""
     scene = _blend_scene(*size)
     driver.set_option("tma", tma)
     try:
@@ -201,3 +203,17 @@ def test_tile_staging_by_tensor_copies(driver, renderer, size, tile, tma):
     finally:
         driver.set_option("tma", 1)
     _check(scene, color, depth, stats)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["batched", "persistent"])
+@pytest.mark.parametrize("tile", [8, 16, 32])
+def test_heavily_clipped_blend_is_stable(renderer, mode, tile):
+    """a 16x16 framebuffer under 3,000 triangles of up to 1,500 px: about 3,200 clipped pieces in the bins;
+    three submissions give the oracle's image and fragment count each time"""
+    scene = _blend_scene(16, 16)
+    run = render.SceneRun(renderer, scene, mode=mode, tile=tile)
+    for _ in range(3):
+        run.submit()
+        color, depth = run.read()
+        _check(scene, color, depth, run.stats())
