@@ -54,12 +54,14 @@ KZ_API PFN_vkVoidFunction vk_icdGetPhysicalDeviceProcAddr(VkInstance instance, c
  *   "tma"   "1" (default) / "0": command buffers ended while it is on stage the colour and depth of each
  *           tile of kz_k_raster_direct through TMA tensor copies (where the attachment's base address and
  *           row pitch are multiples of 16 bytes); with "0" the tiles are read and written with plain loads
+ *   "vector_fetch" "1" (default) / "0": command buffers ended while it is on fetch vertex attributes with
+ *           8- and 16-byte vector loads in draws whose bound vertex buffers start 16-byte aligned
  *   "barrier_ns" "N": command buffers ended while it is set give their persistent kernels' grid barriers
  *           up after waiting N nanoseconds (default 4000000000; 0 gives up at the first check).  A barrier
  *           that gives up sets KZ_STATUS_BARRIER_TIMEOUT and the submission completes with
  *           VK_ERROR_DEVICE_LOST; the kernel returns and the CUDA context stays usable
  * Returns 0, or -1 for an unknown key or value.  The KZ_MODE, KZ_TILE, KZ_TRACE, KZ_KERNEL_TIMING, KZ_PDL,
- * KZ_TMA and KZ_FAULT=alloc:N environment variables set the initial values. */
+ * KZ_TMA, KZ_VECTOR_FETCH and KZ_FAULT=alloc:N environment variables set the initial values. */
 KZ_API int kzDriverSetOption(const char* key, const char* value);
 
 /* The CUDA stream (cudaStream_t) a queue executes on, for callers that time submissions with CUDA

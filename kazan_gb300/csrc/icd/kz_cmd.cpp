@@ -1459,7 +1459,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
    * start 16-byte aligned use an entry whose vertex fetch uses vector loads */
   std::map<std::pair<Pipeline*, uint32_t>, uint32_t> pipe_index;
   auto pipe_of = [&](Pipeline* p, const KzDraw& d) -> uint32_t {
-    uint32_t align = fetch_vectorizable(p->pipe) && bases_aligned16(d, p->pipe) ? 16u : 4u;
+    uint32_t align = options().vector_fetch && fetch_vectorizable(p->pipe) && bases_aligned16(d, p->pipe) ? 16u : 4u;
     auto key = std::make_pair(p, align);
     auto it = pipe_index.find(key);
     if (it != pipe_index.end()) return it->second;

@@ -46,6 +46,8 @@ Options& options() {
     if (kt) r.kernel_timing = std::atoi(kt);
     const char* tm = std::getenv("KZ_TMA");
     if (tm) r.tma = std::atoi(tm) != 0;
+    const char* vf = std::getenv("KZ_VECTOR_FETCH");
+    if (vf) r.vector_fetch = std::atoi(vf) != 0;
     const char* pd = std::getenv("KZ_PDL");
     if (pd) r.pdl = std::atoi(pd) != 0;
     return r;
@@ -1674,6 +1676,11 @@ extern "C" KZ_API int kzDriverSetOption(const char* key, const char* value) {
   if (!std::strcmp(key, "pdl")) {
     if (std::strcmp(value, "0") && std::strcmp(value, "1")) return -1;
     o.pdl = value[0] == '1';
+    return 0;
+  }
+  if (!std::strcmp(key, "vector_fetch")) {
+    if (std::strcmp(value, "0") && std::strcmp(value, "1")) return -1;
+    o.vector_fetch = value[0] == '1';
     return 0;
   }
   if (!std::strcmp(key, "tma")) {

@@ -407,6 +407,8 @@ struct Options {
                          programmatic stream serialization (its launch overlaps the predecessor's completion) */
   uint32_t barrier_ns = 4000000000u; /* a persistent kernel's grid barrier gives up after waiting this long */
   int tma = 1;        /* KZ_TMA: kz_k_raster_direct stages each tile's colour and depth through tensor copies */
+  int vector_fetch = 1; /* KZ_VECTOR_FETCH: draws whose vertex buffers start 16-byte aligned fetch attributes with
+                           vector loads */
 };
 Options& options();
 

@@ -1348,9 +1348,9 @@ __device__ __forceinline__ int vis_triangle(const Ctx& c, const KzDraw& d, const
 }
 
 #define KZ_GEO_SMEM (KZ_THREADS * (96 + 1))
-/* at least the pixel pairs per row of a warp-rasterised box: ceil(w / 2), w * h <= KZ_WARP_PX */
-#define KZ_MAGIC_MAX ((KZ_WARP_PX + 1) / 2 > 128 ? (KZ_WARP_PX + 1) / 2 : 128)
-static_assert((KZ_WARP_PX + 1) / 2 <= KZ_MAGIC_MAX, "the divisor table covers every warp-rasterised box width");
+/* at least the pixel quads per row of a warp-rasterised box: ceil(w / 4), w * h <= KZ_WARP_PX */
+#define KZ_MAGIC_MAX ((KZ_WARP_PX + 3) / 4 > 128 ? (KZ_WARP_PX + 3) / 4 : 128)
+static_assert((KZ_WARP_PX + 3) / 4 <= KZ_MAGIC_MAX, "the divisor table covers every warp-rasterised box width");
 
 /* table[pw] = floor((2^32 - 1) / pw) + 1 for pw in [2, KZ_MAGIC_MAX] (0 for 0 and 1), filled by the block */
 __device__ __forceinline__ void fill_magic(uint32_t* table) {
@@ -1364,8 +1364,8 @@ struct WarpTri {
   int32_t ex[3];      /* edge function step per pixel in x (-dy * 256) */
   int32_t ey[3];      /* ... and in y (dx * 256) */
   int32_t ox, oy;     /* first pixel of the box */
-  uint32_t pw, magic; /* pixel pairs per box row, ceil(w / 2); umulhi(i, magic) = i / pw for i < 2^16 */
-  uint32_t start, w;  /* number of the box's first pair in the warp's list; box width */
+  uint32_t pw, magic; /* pixel quads per box row, ceil(w / 4); umulhi(i, magic) = i / pw for i < 2^16 */
+  uint32_t start, w;  /* number of the box's first quad in the warp's list; box width */
   float z0, dz1, dz2, inv_s;
   uint32_t g, thr;    /* primitive number; bit k: edge k's threshold is 1; bit 3: every edge value over the
                          box fits in 32 bits */
@@ -1394,10 +1394,11 @@ __device__ __forceinline__ void warp_fragment32(const KzSegment& seg, const Warp
 }
 
 /* rasterise every lane's record (valid where `have`) into the keys with the whole warp.  Each box row is
- * cut into pairs of horizontally adjacent pixels; the pairs of all lanes' boxes are numbered consecutively
- * and the warp takes 32 consecutive pairs per step, so lanes stay busy however unequal the boxes are and
- * neighbouring lanes write neighbouring keys.  In a step, each triangle whose pairs meet the step's window
- * writes its lane into `owner` at the window position of its first pair there; lane l's triangle is the
+ * cut into quads of four horizontally adjacent pixels (the last one of a row may be shorter); the quads of
+ * all lanes' boxes are numbered consecutively and the warp takes 32 consecutive quads per step, so lanes stay
+ * busy however unequal the boxes are and neighbouring lanes write neighbouring keys (four pixels a lane: 1 %
+ * less kernel time than two on the 4,096-draw frame).  In a step, each triangle whose quads meet the step's
+ * window writes its lane into `owner` at the window position of its first quad there; lane l's triangle is the
  * one marked at the highest position <= l.  `slots`: this warp's 32 WarpTri, `owner`: its 32-entry table,
  * both in shared memory. */
 __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const KzTriRecord& r, bool have, float zmin,
@@ -1407,7 +1408,7 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
   uint32_t n = 0;
   if (have) {
     uint32_t w = (r.bb1 & 0xFFFFu) - (r.bb0 & 0xFFFFu) + 1;
-    n = ((r.bb1 >> 16) - (r.bb0 >> 16) + 1) * ((w + 1) >> 1);
+    n = ((r.bb1 >> 16) - (r.bb0 >> 16) + 1) * ((w + 3) >> 2);
   }
   uint32_t incl = n;
 #pragma unroll
@@ -1425,7 +1426,7 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
     t.ox = (int32_t)(r.bb0 & 0xFFFFu);
     t.oy = (int32_t)(r.bb0 >> 16);
     t.w = (r.bb1 & 0xFFFFu) - (r.bb0 & 0xFFFFu) + 1;
-    t.pw = (t.w + 1) >> 1;
+    t.pw = (t.w + 3) >> 2;
     /* floor((2^32 - 1) / pw) + 1: the rounded-up reciprocal for every pw > 1 (exact when pw is a power of 2);
      * from the block's table for the widths warp-rasterised boxes have */
     t.magic = t.pw <= KZ_MAGIC_MAX ? magic_tab[t.pw] : 0xFFFFFFFFu / t.pw + 1u;
@@ -1440,9 +1441,9 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
       t.ex[k] = -e.dy[k] * 256;
       t.ey[k] = e.dx[k] * 256;
       thr |= (uint32_t)e.thr[k] << k;
-      /* largest |value| the edge takes over the box (plus one step past its last column) */
+      /* largest |value| the edge takes over the box (with margin: three steps past its last column) */
       int64_t ae = t.e[k] < 0 ? -t.e[k] : t.e[k];
-      int64_t bound = ae + (int64_t)abs(t.ex[k]) * (w1 + 1) + (int64_t)abs(t.ey[k]) * h1 + 1;
+      int64_t bound = ae + (int64_t)abs(t.ex[k]) * (w1 + 3) + (int64_t)abs(t.ey[k]) * h1 + 1;
       fits = fits && bound < 0x7FFFFFFFll;
     }
     t.thr = thr | (fits ? 8u : 0u);
@@ -1468,7 +1469,7 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
     uint32_t local = idx - t.start;
     uint32_t pw = t.pw;
     uint32_t y = pw > 1 ? __umulhi(local, t.magic) : local;
-    int32_t x = (int32_t)(local - y * pw) * 2;
+    int32_t x = (int32_t)(local - y * pw) * 4;
     int32_t sx0 = t.ex[0], sx1 = t.ex[1], sx2 = t.ex[2];
     int32_t px = t.ox + x, py = t.oy + (int32_t)y;
     const uint32_t tthr = t.thr;
@@ -1477,18 +1478,17 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
       int32_t e0 = (int32_t)t.e[0] + sx0 * x + t.ey[0] * (int32_t)y;
       int32_t e1 = (int32_t)t.e[1] + sx1 * x + t.ey[1] * (int32_t)y;
       int32_t e2 = (int32_t)t.e[2] + sx2 * x + t.ey[2] * (int32_t)y;
-      if ((e0 | e1 | e2) >= 0) {
-        frags++;
-        warp_fragment32(seg, t, e1 + (int32_t)((tthr >> 1) & 1u), e2 + (int32_t)((tthr >> 2) & 1u), zmin, zmax, px, py);
-      }
-      if ((uint32_t)x + 1 < t.w) {
-        e0 += sx0;
-        e1 += sx1;
-        e2 += sx2;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        if (k > 0) {
+          if ((uint32_t)x + k >= t.w) break;
+          e0 += sx0;
+          e1 += sx1;
+          e2 += sx2;
+        }
         if ((e0 | e1 | e2) >= 0) {
           frags++;
-          warp_fragment32(seg, t, e1 + (int32_t)((tthr >> 1) & 1u), e2 + (int32_t)((tthr >> 2) & 1u), zmin, zmax, px + 1,
-                          py);
+          warp_fragment32(seg, t, e1 + (int32_t)((tthr >> 1) & 1u), e2 + (int32_t)((tthr >> 2) & 1u), zmin, zmax, px + k, py);
         }
       }
       continue;
@@ -1496,17 +1496,17 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
     int64_t e0 = t.e[0] + (int64_t)sx0 * x + (int64_t)t.ey[0] * (int32_t)y;
     int64_t e1 = t.e[1] + (int64_t)sx1 * x + (int64_t)t.ey[1] * (int32_t)y;
     int64_t e2 = t.e[2] + (int64_t)sx2 * x + (int64_t)t.ey[2] * (int32_t)y;
-    if ((e0 | e1 | e2) >= 0) {
-      frags++;
-      warp_fragment(seg, t, e1, e2, zmin, zmax, px, py);
-    }
-    if ((uint32_t)x + 1 < t.w) {
-      e0 += sx0;
-      e1 += sx1;
-      e2 += sx2;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (k > 0) {
+        if ((uint32_t)x + k >= t.w) break;
+        e0 += sx0;
+        e1 += sx1;
+        e2 += sx2;
+      }
       if ((e0 | e1 | e2) >= 0) {
         frags++;
-        warp_fragment(seg, t, e1, e2, zmin, zmax, px + 1, py);
+        warp_fragment(seg, t, e1, e2, zmin, zmax, px + k, py);
       }
     }
   }
