@@ -254,8 +254,11 @@ def main():
         best, table = autotune.Tuner().choose(sig, autotune.scene_timer(run),
                                               autotune.candidates(ordered=scene.blend))
         mode, tile = best.mode, best.tile
-        tuning = {"signature": sig, "chosen": {"mode": mode, "tile": tile},
-                  "ms": None if table is None else {"%s/%d" % (c.mode, c.tile): round(v, 4) for c, v in table.items()}}
+        tuning = {"signature": sig, "chosen": best.options(),
+                  "ms": None if table is None else {c.label(): round(v, 4) for c, v in table.items()}}
+        # the chosen knobs hold for the command buffers recorded below
+        for k in ("warp_px", "job_blocks", "geo_blocks"):
+            r.drv.set_option(k, getattr(best, k))
     # two command buffers of the same draws: `graph_cb` is what an application submits (captured as a CUDA
     # graph at vkEndCommandBuffer, its kernels chained by programmatic dependent launch); `timed_cb`
     # launches its kernels at submit with an event pair around each launch, for the per-kernel times
@@ -424,10 +427,12 @@ def main():
 
 def other_workloads(r, render, timed_region, rk):
     """short timings of the other render configurations (seeded synthetic scenes): each recorded in the
-    batched schedule at tile 16 and graph-launched for a few hundred milliseconds, then once more with kernel
-    timing on for the dominant kernel; device-resident inputs"""
-    from kazan_gb300 import scenes
+    batched schedule at tile 16 with the visibility path's default knobs and graph-launched for a few hundred
+    milliseconds, then once more with kernel timing on for the dominant kernel; device-resident inputs"""
+    from kazan_gb300 import autotune, scenes
     out = {}
+    for k, v in autotune.DEFAULTS.items():
+        r.drv.set_option(k, v)
     cases = [("plain small draw: 2,048 non-indexed tris, 256x256, seed 1", scenes.small_soup(), 2000),
              ("single large draw: 1M indexed tris, 1920x1080, Lambert, back-face cull, seed 2", scenes.single_large(),
               800),

@@ -54,6 +54,12 @@ KZ_API PFN_vkVoidFunction vk_icdGetPhysicalDeviceProcAddr(VkInstance instance, c
  *   "tma"   "1" (default) / "0": command buffers ended while it is on stage the colour and depth of each
  *           tile of kz_k_raster_direct through TMA tensor copies (where the attachment's base address and
  *           row pitch are multiples of 16 bytes); with "0" the tiles are read and written with plain loads
+ *   "warp_px" "N" (1..4096, default 192): in opaque passes of command buffers ended while it is set, unclipped
+ *           triangles whose boxes hold at most N pixels are rasterised by their geometry warp, larger ones are
+ *           split into jobs of 8x8-pixel blocks
+ *   "job_blocks" "N" (1..32, default 16): 8x8-pixel blocks per large-triangle job
+ *   "geo_blocks" "N" (0..64, default 0): blocks per SM of the batched geometry launches (0: as many as
+ *           are resident)
  *   "vector_fetch" "1" (default) / "0": command buffers ended while it is on fetch vertex attributes with
  *           8- and 16-byte vector loads in draws whose bound vertex buffers start 16-byte aligned
  *   "barrier_ns" "N": command buffers ended while it is set give their persistent kernels' grid barriers

@@ -1,5 +1,8 @@
-"""Autotuner for the draw path's execution choices: the screen-tile side of ordered (blending) passes and
-the launch schedule of a command buffer (batched phases or one persistent kernel).
+"""Autotuner for the draw path's execution choices: the launch schedule of a command buffer (batched phases
+or one persistent kernel), the screen-tile side of ordered (blending) passes, and for opaque passes the
+visibility path's knobs: the largest triangle box a geometry warp rasterises (`warp_px`; larger triangles
+become jobs), the 8x8 blocks per large-triangle job (`job_blocks`) and the geometry kernel's blocks per SM
+(`geo_blocks`, 0 = all resident).
 
 `tune(time_config, ...)` measures every candidate with a caller-supplied timing function and returns the
 fastest; `Tuner` wraps it with a JSON cache keyed by a workload signature (GPU name, raster classes,
@@ -14,19 +17,43 @@ from dataclasses import dataclass
 
 MODES = ("batched", "persistent")
 TILES = (8, 16, 32, 64)
+WARP_PX = (96, 128, 256, 384)
+JOB_BLOCKS = (8, 32)
+GEO_BLOCKS = (2, 3)
+DEFAULTS = {"warp_px": 192, "job_blocks": 16, "geo_blocks": 0}
 
 
 @dataclass(frozen=True)
 class Config:
     mode: str
     tile: int
+    warp_px: int = DEFAULTS["warp_px"]
+    job_blocks: int = DEFAULTS["job_blocks"]
+    geo_blocks: int = DEFAULTS["geo_blocks"]
+
+    def label(self):
+        """'mode/tile', followed by the knobs that differ from their defaults"""
+        extra = "".join("/%s%d" % (k, getattr(self, k)) for k in ("warp_px", "job_blocks", "geo_blocks")
+                        if getattr(self, k) != DEFAULTS[k])
+        return "%s/%d%s" % (self.mode, self.tile, extra)
+
+    def options(self):
+        """the driver options that select this configuration"""
+        return {"mode": self.mode, "tile": self.tile, "warp_px": self.warp_px, "job_blocks": self.job_blocks,
+                "geo_blocks": self.geo_blocks}
 
 
-def candidates(modes=MODES, tiles=TILES, ordered=True):
-    """every (mode, tile) pair; the tile side only matters to ordered passes, so opaque-only workloads
-    try one tile"""
-    ts = tiles if ordered else (16,)
-    return [Config(m, t) for m in modes for t in ts]
+def candidates(modes=MODES, tiles=TILES, ordered=True, knobs=True):
+    """ordered workloads: every (mode, tile) pair.  Opaque workloads (the tile side does not matter to
+    them): each mode at the default knobs, then, in the batched schedule, each knob varied alone"""
+    if ordered:
+        return [Config(m, t) for m in modes for t in tiles]
+    out = [Config(m, 16) for m in modes]
+    if knobs and "batched" in modes:
+        out += [Config("batched", 16, warp_px=w) for w in WARP_PX]
+        out += [Config("batched", 16, job_blocks=j) for j in JOB_BLOCKS]
+        out += [Config("batched", 16, geo_blocks=g) for g in GEO_BLOCKS]
+    return out
 
 
 def tune(time_config, configs, repeats=1):
@@ -34,7 +61,7 @@ def tune(time_config, configs, repeats=1):
     table = {}
     for cfg in configs:
         table[cfg] = min(time_config(cfg) for _ in range(max(1, repeats)))
-    best = min(table, key=lambda c: (table[c], c.mode != "batched", c.tile))
+    best = min(table, key=lambda c: (table[c], c.mode != "batched", c.tile, c.label()))
     return best, table
 
 
@@ -61,7 +88,10 @@ class Tuner:
 
     def lookup(self, sig):
         e = self.cache.get(sig)
-        return Config(e["mode"], int(e["tile"])) if e else None
+        if not e:
+            return None
+        return Config(e["mode"], int(e["tile"]), *(int(e.get(k, DEFAULTS[k])) for k in
+                                                   ("warp_px", "job_blocks", "geo_blocks")))
 
     def choose(self, sig, time_config, configs, repeats=1):
         """the cached choice for `sig`, or measure `configs` and remember the best; returns (config, table or
@@ -70,8 +100,7 @@ class Tuner:
         if hit is not None:
             return hit, None
         best, table = tune(time_config, configs, repeats)
-        self.cache[sig] = {"mode": best.mode, "tile": best.tile,
-                           "ms": {"%s/%d" % (c.mode, c.tile): round(v, 4) for c, v in table.items()}}
+        self.cache[sig] = dict(best.options(), ms={c.label(): round(v, 4) for c, v in table.items()})
         self.save()
         return best, table
 
@@ -90,10 +119,14 @@ def scene_timer(run, steps=5, warmup=2):
 
     def time_config(cfg):
         d = run.r.drv
-        d.set_option("mode", cfg.mode)
-        d.set_option("tile", cfg.tile)
+        for k, v in cfg.options().items():
+            d.set_option(k, v)
         old = run.cb
-        run.cb = run.record()
+        try:
+            run.cb = run.record()
+        finally:
+            for k, v in DEFAULTS.items():
+                d.set_option(k, v)
         run.r.free_command_buffer(old)
         stream = torch.cuda.ExternalStream(run.r.stream())
         for _ in range(warmup):

@@ -1344,7 +1344,8 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
           /* the per-draw launch form: each direct draw's geometry is a launch of its own (with, for opaque
            * segments, the large-triangle jobs it made); the pass-wide phases run once per segment */
           const bool per_draw = low.mode == 2 && !seg.indirect;
-          const uint32_t gb = (uint32_t)std::max(1, ks->geometry_blocks);
+          uint32_t gb = (uint32_t)std::max(1, ks->geometry_blocks);
+          if (low.geo_blocks) gb = std::min(gb, low.geo_blocks * (uint32_t)dev->pd->sm_count);
           if (seg.mode == KZ_MODE_VISIBILITY) {
             cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, (seg.width * seg.height + 255) / 256)));
             launch(dev, timing, KK_VIS_INIT, cfg, ks->vis_init, args, chain);
@@ -1455,6 +1456,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   low.mode = options().mode;
   low.tile = options().tile;
   low.timed = options().kernel_timing != 0;
+  low.geo_blocks = options().geo_blocks;
   /* one pipeline entry per pipeline and vertex-buffer alignment class: draws whose bound vertex buffers all
    * start 16-byte aligned use an entry whose vertex fetch uses vector loads */
   std::map<std::pair<Pipeline*, uint32_t>, uint32_t> pipe_index;
@@ -1706,6 +1708,8 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   low.frame.chunk_end = 0xFFFFFFFFu;
   low.frame.jobs_incremental = 0;
   low.frame.barrier_ns = options().barrier_ns;
+  low.frame.warp_px = options().warp_px;
+  low.frame.job_blocks = options().job_blocks;
   upload_tables(low);
   if (cudaMallocHost((void**)&low.h_status, sizeof(KzStatus)) != cudaSuccess) return VK_ERROR_OUT_OF_HOST_MEMORY;
   std::memset(low.h_status, 0, sizeof(KzStatus));

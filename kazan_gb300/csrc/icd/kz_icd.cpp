@@ -1688,6 +1688,22 @@ extern "C" KZ_API int kzDriverSetOption(const char* key, const char* value) {
     o.tma = value[0] == '1';
     return 0;
   }
+  if (!std::strcmp(key, "warp_px") || !std::strcmp(key, "job_blocks") || !std::strcmp(key, "geo_blocks")) {
+    char* end = nullptr;
+    unsigned long v = std::strtoul(value, &end, 10);
+    if (!*value || *end) return -1;
+    if (key[0] == 'w') {
+      if (v < 1 || v > 4096) return -1;
+      o.warp_px = (uint32_t)v;
+    } else if (key[0] == 'j') {
+      if (v < 1 || v > 32) return -1;
+      o.job_blocks = (uint32_t)v;
+    } else {
+      if (v > 64) return -1;
+      o.geo_blocks = (uint32_t)v;
+    }
+    return 0;
+  }
   if (!std::strcmp(key, "barrier_ns")) {
     char* end = nullptr;
     unsigned long long v = std::strtoull(value, &end, 10);

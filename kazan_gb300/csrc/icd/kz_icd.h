@@ -328,6 +328,7 @@ struct Lowered {
                    per segment; launched at submit, not captured) */
   uint32_t tile = 16;
   bool timed = false; /* kernel timing: launched at submit with an event pair around each kernel */
+  uint32_t geo_blocks = 0; /* blocks per SM of the batched geometry launches (0: all resident) */
 };
 
 struct CommandPool {
@@ -409,6 +410,9 @@ struct Options {
   int tma = 1;        /* KZ_TMA: kz_k_raster_direct stages each tile's colour and depth through tensor copies */
   int vector_fetch = 1; /* KZ_VECTOR_FETCH: draws whose vertex buffers start 16-byte aligned fetch attributes with
                            vector loads */
+  uint32_t warp_px = KZ_WARP_PX_DEFAULT;       /* visibility path: largest box (pixels) a geometry warp rasterises */
+  uint32_t job_blocks = KZ_JOB_BLOCKS_DEFAULT; /* visibility path: 8x8 blocks per large-triangle job */
+  uint32_t geo_blocks = 0; /* blocks per SM of the batched geometry launches (0: as many as are resident) */
 };
 Options& options();
 

@@ -294,7 +294,13 @@ typedef struct KzFrame {
                                 this segment (per-draw launch form), else all of the segment's jobs */
   uint32_t barrier_ns;       /* persistent kernels: a grid barrier gives up (KZ_STATUS_BARRIER_TIMEOUT) after
                                 waiting this many nanoseconds */
+  uint32_t warp_px;          /* visibility path: unclipped triangles whose boxes hold at most this many pixels
+                                are rasterised by their geometry warp, larger ones become jobs */
+  uint32_t job_blocks;       /* visibility path: 8x8 pixel blocks per large-triangle job, 1..32 */
 } KzFrame;
+
+#define KZ_WARP_PX_DEFAULT 192
+#define KZ_JOB_BLOCKS_DEFAULT 16
 
 /* --- shader call ABI (kernels <-> JIT-linked shader device functions) --- */
 

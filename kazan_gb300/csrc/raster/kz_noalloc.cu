@@ -289,6 +289,8 @@ extern "C" KZ_API int kzRasterTrianglesNoAlloc(const float* vertices, uint32_t t
   f.chunk_end = 0xFFFFFFFFu;
   f.jobs_incremental = 0;
   f.barrier_ns = 0; /* no persistent kernel runs here */
+  f.warp_px = KZ_WARP_PX_DEFAULT;
+  f.job_blocks = KZ_JOB_BLOCKS_DEFAULT;
 
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);

@@ -1086,14 +1086,10 @@ __device__ __forceinline__ uint32_t stencil_apply(uint32_t op, uint32_t s, uint3
 
 #define KZ_SMALL_PX 32      /* clipped sub-triangles with boxes of at most this many pixels are rasterised by
                                their geometry thread */
-#ifndef KZ_WARP_PX
-#define KZ_WARP_PX 192      /* unclipped triangles with boxes of at most this many pixels are rasterised by
-                               their geometry warp (vis_warp_raster); larger ones become jobs */
-#endif
-#ifndef KZ_JOB_BLOCKS
-#define KZ_JOB_BLOCKS 16    /* 8x8 pixel blocks per large-triangle job (at most 32: one lane each) */
-#endif
-static_assert(KZ_JOB_BLOCKS >= 1 && KZ_JOB_BLOCKS <= 32, "one lane per block of a job");
+/* KzFrame::warp_px: unclipped triangles with boxes of at most this many pixels are rasterised by their
+ * geometry warp (vis_warp_raster), larger ones become jobs of KzFrame::job_blocks 8x8 blocks (1..32: one lane
+ * per block); both are set per command buffer (the autotuner's knobs) */
+__device__ __forceinline__ uint32_t job_blocks(const Ctx& c) { return min(max(c.f->job_blocks, 1u), 32u); }
 
 __device__ __forceinline__ unsigned long long* vis_px(const KzSegment& seg, int32_t x, int32_t y) {
   return reinterpret_cast<unsigned long long*>(seg.vis) + (size_t)y * seg.width + x;
@@ -1191,22 +1187,24 @@ __device__ void vis_emit_large(const Ctx& c, const KzTriRecord& r) {
   uint32_t idx = atomicAdd(&c.cnt->rec_count, 1u);
   store_record(c, idx, r);
   uint32_t nbx, nb = box_blocks(r, nbx);
-  uint32_t njobs = (nb + KZ_JOB_BLOCKS - 1) / KZ_JOB_BLOCKS;
+  const uint32_t jb = job_blocks(c);
+  uint32_t njobs = (nb + jb - 1) / jb;
   uint32_t j0 = atomicAdd(&c.cnt->pair_count, njobs);
   uint32_t cap = c.seg->pair_cap / 2;
   if (idx >= c.seg->rec_cap) return;
   uint2* jobs = reinterpret_cast<uint2*>(c.seg->bins);
-  for (uint32_t j = 0; j < njobs && j0 + j < cap; j++) jobs[j0 + j] = make_uint2(idx, j * KZ_JOB_BLOCKS);
+  for (uint32_t j = 0; j < njobs && j0 + j < cap; j++) jobs[j0 + j] = make_uint2(idx, j * jb);
 }
 
-/* emit the records of the lanes where `large` holds (their boxes exceed KZ_WARP_PX pixels) with one
+/* emit the records of the lanes where `large` holds (their boxes exceed warp_px pixels) with one
  * record and one job reservation for the whole warp (all lanes call it) */
 __device__ __forceinline__ void vis_emit_large_warp(const Ctx& c, const KzTriRecord& r, bool large) {
   const uint32_t m = __ballot_sync(0xFFFFFFFFu, large);
   if (!m) return;
   const int lane = threadIdx.x & 31;
+  const uint32_t jb = job_blocks(c);
   uint32_t nbx = 0, njobs = 0;
-  if (large) njobs = (box_blocks(r, nbx) + KZ_JOB_BLOCKS - 1) / KZ_JOB_BLOCKS;
+  if (large) njobs = (box_blocks(r, nbx) + jb - 1) / jb;
   uint32_t jincl = njobs;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -1228,7 +1226,7 @@ __device__ __forceinline__ void vis_emit_large_warp(const Ctx& c, const KzTriRec
   if (idx >= c.seg->rec_cap) return;
   uint32_t j0 = jbase + jincl - njobs, cap = c.seg->pair_cap / 2;
   uint2* jobs = reinterpret_cast<uint2*>(c.seg->bins);
-  for (uint32_t j = 0; j < njobs && j0 + j < cap; j++) jobs[j0 + j] = make_uint2(idx, j * KZ_JOB_BLOCKS);
+  for (uint32_t j = 0; j < njobs && j0 + j < cap; j++) jobs[j0 + j] = make_uint2(idx, j * jb);
 }
 
 /* one record: small -> rasterise now, large -> jobs */
@@ -1313,7 +1311,7 @@ __device__ __forceinline__ void vertex_project(const KzDraw& d, VEntry& e) {
 }
 
 /* set up the triangle of three shaded vertices.  Returns 1 with `out` set when the triangle's box holds
- * at most KZ_WARP_PX pixels (the warp rasterises it, vis_warp_raster), 2 with `out` set when it is larger
+ * at most warp_px pixels (the warp rasterises it, vis_warp_raster), 2 with `out` set when it is larger
  * (jobs, vis_emit_large_warp), 0 otherwise; clipped triangles are rasterised here (their fragments are
  * added to `frags`). */
 __device__ __forceinline__ int vis_triangle(const Ctx& c, const KzDraw& d, const KzPipe& p, uint32_t di, uint32_t g,
@@ -1344,13 +1342,13 @@ __device__ __forceinline__ int vis_triangle(const Ctx& c, const KzDraw& d, const
   out.g = g;
   out.draw = di;
   out.pad = 0;
-  return box_area(out) <= KZ_WARP_PX ? 1 : 2;
+  return box_area(out) <= c.f->warp_px ? 1 : 2;
 }
 
 #define KZ_GEO_SMEM (KZ_THREADS * (96 + 1))
-/* at least the pixel quads per row of a warp-rasterised box: ceil(w / 4), w * h <= KZ_WARP_PX */
-#define KZ_MAGIC_MAX ((KZ_WARP_PX + 3) / 4 > 128 ? (KZ_WARP_PX + 3) / 4 : 128)
-static_assert((KZ_WARP_PX + 3) / 4 <= KZ_MAGIC_MAX, "the divisor table covers every warp-rasterised box width");
+/* the divisor table's range: the pixel quads per row, ceil(w / 4), of every warp-rasterised box of width up
+ * to 512 (wider ones compute their divisor) */
+#define KZ_MAGIC_MAX 128
 
 /* table[pw] = floor((2^32 - 1) / pw) + 1 for pw in [2, KZ_MAGIC_MAX] (0 for 0 and 1), filled by the block */
 __device__ __forceinline__ void fill_magic(uint32_t* table) {
@@ -1572,8 +1570,8 @@ __device__ void vis_geometry_warps(const Ctx& c, unsigned char* smem, const uint
   }
 }
 
-/* one large-triangle job, one warp: up to KZ_JOB_BLOCKS 8x8 blocks of the record's box.
- * Lane b < KZ_JOB_BLOCKS first evaluates the three edge functions at block b's first pixel centre and
+/* one large-triangle job, one warp: up to job_blocks 8x8 blocks of the record's box.
+ * Lane b < job_blocks first evaluates the three edge functions at block b's first pixel centre and
  * drops the block when, for some edge, even the block's largest value (at the corner the edge's
  * gradient points to) is below the threshold.  The warp then walks the remaining blocks: each lane adds
  * its fixed offset within the block to the block's edge values (the same integers as evaluating the edge
@@ -1590,7 +1588,7 @@ __device__ uint32_t vis_large_job(const Ctx& c, uint2 job, int lane) {
   uint32_t nbx, nb = box_blocks(r, nbx);
   /* block test, one block per lane; E* hold the edge values minus their thresholds (covered iff all >= 0) */
   uint32_t b = job.y + (uint32_t)lane;
-  bool live = lane < KZ_JOB_BLOCKS && b < nb;
+  bool live = (uint32_t)lane < job_blocks(c) && b < nb;
   int32_t ox = 0, oy = 0;
   int64_t E0 = 0, E1 = 0, E2 = 0;
   if (live) {

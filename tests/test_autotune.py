@@ -4,7 +4,31 @@ from kazan_gb300 import autotune
 
 def test_candidates():
     assert len(autotune.candidates(ordered=True)) == 8
-    assert [c.tile for c in autotune.candidates(ordered=False)] == [16, 16]
+    opaque = autotune.candidates(ordered=False)
+    assert {c.tile for c in opaque} == {16}
+    assert [c.mode for c in opaque[:2]] == ["batched", "persistent"]
+    # each knob varied alone, in the batched schedule, the others at their defaults
+    varied = opaque[2:]
+    assert all(c.mode == "batched" for c in varied) and len(set(varied)) == len(varied)
+    for c in varied:
+        assert sum(getattr(c, k) != v for k, v in autotune.DEFAULTS.items()) == 1
+    assert {c.warp_px for c in varied} >= set(autotune.WARP_PX)
+    assert [c.label() for c in opaque[:3]] == ["batched/16", "persistent/16", "batched/16/warp_px96"]
+    assert autotune.candidates(ordered=False, knobs=False) == opaque[:2]
+
+
+def test_knob_choice_round_trips_through_the_cache(tmp_path):
+    path = str(tmp_path / "tune.json")
+
+    def timer(c):
+        return 1.0 if (c.warp_px, c.geo_blocks) == (256, 0) else 2.0
+
+    sig = autotune.signature("GB300", False, 4096, 32_650_790, 2048, 2048)
+    best, table = autotune.Tuner(path).choose(sig, timer, autotune.candidates(ordered=False))
+    assert (best.mode, best.warp_px, best.job_blocks) == ("batched", 256, 16) and table[best] == 1.0
+    again, table2 = autotune.Tuner(path).choose(sig, timer, autotune.candidates(ordered=False))
+    assert again == best and table2 is None
+    assert best.options() == {"mode": "batched", "tile": 16, "warp_px": 256, "job_blocks": 16, "geo_blocks": 0}
 
 
 def test_tune_picks_fastest_and_breaks_ties_towards_batched():

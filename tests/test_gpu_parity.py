@@ -217,3 +217,25 @@ def test_heavily_clipped_blend_is_stable(renderer, mode, tile):
         run.submit()
         color, depth = run.read()
         _check(scene, color, depth, run.stats())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("knobs", [{"warp_px": 1}, {"warp_px": 16, "job_blocks": 1}, {"warp_px": 4096},
+                                   {"job_blocks": 7}, {"job_blocks": 32}, {"geo_blocks": 1},
+                                   {"warp_px": 96, "job_blocks": 8, "geo_blocks": 2}])
+@pytest.mark.parametrize("mode", ["batched", "persistent", "perdraw"])
+@pytest.mark.parametrize("case", ["soup", "sphere", "batched", "clip"])
+def test_visibility_path_knobs(driver, renderer, case, mode, knobs):
+    """the autotuner's knobs of the visibility path: the largest box a geometry warp rasterises (1 px: every
+    triangle becomes large-triangle jobs; 4,096 px: nearly none), the 8x8 blocks per job and the geometry
+    blocks per SM change which kernel covers a pixel, never the image"""
+    scene = CASES[case]
+    for k, v in knobs.items():
+        driver.set_option(k, v)
+    try:
+        color, depth, stats = _render(renderer, scene, mode, 16)
+    finally:
+        driver.set_option("warp_px", 192)
+        driver.set_option("job_blocks", 16)
+        driver.set_option("geo_blocks", 0)
+    _check(scene, color, depth, stats)
