@@ -20,6 +20,10 @@ Printed JSON line (rank 0):
   roofline   achieved HBM bandwidth of the dominant kernel (algorithmic bytes / kernel time) vs measured peak
   cpu_baseline  the CPU oracle (project restatement; the reference has no CPU rasteriser) on a bounded
              sample of the draws, all host threads
+  persistent the same draws in the persistent schedule (one cooperative kernel per submission)
+  autotune   the autotuner's measured candidates and its choice (schedule, tile, visibility-path knobs)
+  other_workloads  short timings of the other render configurations (plain small draw, single large draw,
+             ordered blend, textured draw) and one rate of the serving loop (p50 / p99 latency)
 --impl reference times that CPU path alone (the reference arm).  Under torchrun each rank renders its own
 replica (no data-path collective); value = triangles of all ranks / max time.
 """
@@ -86,12 +90,18 @@ def _base_scene(args):
     if args.workload == "soup":
         return scenes.small_soup(), {"workload": "plain single draw: 2048 tris, 256x256, seed 1"}
     if args.workload == "textured":
-        return (scenes.textured(seed=6, n=200_000, width=1920, height=1080, tex_w=1024, tex_h=1024, size_lo=0.004,
-                                size_hi=0.08, linear=True),
-                {"workload": "textured: 200K tris (vertex radius log-uniform 0.004-0.08 NDC), 1920x1080, "
-                             "1024x1024 RGBA8 combined image sampler, LINEAR / REPEAT, perspective-correct uv, "
-                             "seed 6"})
+        return textured_scene(), {"workload": TEXTURED}
     return scenes.ordered_blend(), {"workload": "ordered blend: 200K tris, 1920x1080, SRC_ALPHA blend, seed 4"}
+
+
+TEXTURED = ("textured: 200K tris (vertex radius log-uniform 0.004-0.08 NDC), 1920x1080, 1024x1024 RGBA8 combined "
+            "image sampler, LINEAR / REPEAT, perspective-correct uv, seed 6")
+
+
+def textured_scene():
+    from kazan_gb300 import scenes
+    return scenes.textured(seed=6, n=200_000, width=1920, height=1080, tex_w=1024, tex_h=1024, size_lo=0.004,
+                           size_hi=0.08, linear=True)
 
 
 class Clocks:
@@ -437,7 +447,8 @@ def other_workloads(r, render, timed_region, rk):
              ("single large draw: 1M indexed tris, 1920x1080, Lambert, back-face cull, seed 2", scenes.single_large(),
               800),
              ("ordered blend: 200K tris, 1920x1080, SRC_ALPHA / ONE_MINUS_SRC_ALPHA, depth writes off, seed 4",
-              scenes.ordered_blend(), 100)]
+              scenes.ordered_blend(), 100),
+             (TEXTURED, textured_scene(), 400)]
     for name, scene, steps in cases:
         r.drv.set_option("mode", "batched")
         r.drv.set_option("tile", 16)
@@ -461,7 +472,27 @@ def other_workloads(r, render, timed_region, rk):
             row["visible_mean_area_px"] = round(area, 3)
         out[name] = row
         r.free_command_buffer(tcb)
+    out.update(serving_summary(r))
     return out
+
+
+def serving_summary(r, rate=5000, n=1500):
+    """the serving configuration at one rate of the configured sweep: 64 clients with resident scenes, the
+    same Poisson request stream served batched and one request at a time (latency arrival -> fence)"""
+    from kazan_gb300 import serving
+    t0 = time.perf_counter()
+    backend = serving.VulkanBackend(r, serving.client_specs(), mode="batched")
+    setup_s = time.perf_counter() - t0
+    admitted, resident = serving.admit(backend.sizes, 40e9)
+    for i in admitted:  # warm-up: every command buffer once
+        backend.wait(backend.submit([serving.Request(i, 0, 0.0, res, serving.TMAX)
+                                     for res in range(len(serving.RESOLUTIONS))]))
+    b, one = serving.sweep(backend, admitted, [rate], n)
+    backend.close()
+    name = ("serving: 64 clients, Poisson arrivals at %d req/s, %d requests, each with its own resolution "
+            "(256^2..1920x1080), triangle count (log-uniform 1K-500K) and camera" % (rate, n))
+    return {name: {"admitted_clients": len(admitted), "resident_gb": round(resident / 1e9, 3),
+                   "setup_s": round(setup_s, 2), "batched": b[0].as_dict(), "one_at_a_time": one[0].as_dict()}}
 
 
 def serve_main(args, rk):

@@ -1429,20 +1429,35 @@ __device__ __forceinline__ uint32_t vis_warp_raster(const KzSegment& seg, const 
      * from the block's table for the widths warp-rasterised boxes have */
     t.magic = t.pw <= KZ_MAGIC_MAX ? magic_tab[t.pw] : 0xFFFFFFFFu / t.pw + 1u;
     t.start = start;
-    int64_t px = (int64_t)t.ox * 256 + 128, py = (int64_t)t.oy * 256 + 128;
     uint32_t thr = 0;
-    bool fits = true;
-    const int64_t h1 = (int64_t)((r.bb1 >> 16) - (r.bb0 >> 16)), w1 = (int64_t)t.w - 1;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      t.e[k] = edge_at(e, k, px, py) - e.thr[k];
       t.ex[k] = -e.dy[k] * 256;
       t.ey[k] = e.dx[k] * 256;
       thr |= (uint32_t)e.thr[k] << k;
-      /* largest |value| the edge takes over the box (with margin: three steps past its last column) */
-      int64_t ae = t.e[k] < 0 ? -t.e[k] : t.e[k];
-      int64_t bound = ae + (int64_t)abs(t.ex[k]) * (w1 + 3) + (int64_t)abs(t.ey[k]) * h1 + 1;
-      fits = fits && bound < 0x7FFFFFFFll;
+    }
+    bool fits = true;
+    const int32_t xlo = min(r.x[0], min(r.x[1], r.x[2])), xhi = max(r.x[0], max(r.x[1], r.x[2]));
+    const int32_t ylo = min(r.y[0], min(r.y[1], r.y[2])), yhi = max(r.y[0], max(r.y[1], r.y[2]));
+    if (xhi - xlo < (1 << 14) && yhi - ylo < (1 << 14)) {
+      /* vertices within 64 px of each other: every edge vector component and every offset from a vertex to a
+       * pixel centre of the box (the one-sample box of centres lies inside the vertices' extent) is below 2^14
+       * in magnitude, so each product is below 2^28 and every edge value over the box below 2^29: exact in
+       * 32 bits */
+      const int32_t px = t.ox * 256 + 128, py = t.oy * 256 + 128;
+#pragma unroll
+      for (int k = 0; k < 3; k++) t.e[k] = e.dx[k] * (py - e.ya[k]) - e.dy[k] * (px - e.xa[k]) - e.thr[k];
+    } else {
+      const int64_t px = (int64_t)t.ox * 256 + 128, py = (int64_t)t.oy * 256 + 128;
+      const int64_t h1 = (int64_t)((r.bb1 >> 16) - (r.bb0 >> 16)), w1 = (int64_t)t.w - 1;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        t.e[k] = edge_at(e, k, px, py) - e.thr[k];
+        /* largest |value| the edge takes over the box (with margin: three steps past its last column) */
+        int64_t ae = t.e[k] < 0 ? -t.e[k] : t.e[k];
+        int64_t bound = ae + (int64_t)abs(t.ex[k]) * (w1 + 3) + (int64_t)abs(t.ey[k]) * h1 + 1;
+        fits = fits && bound < 0x7FFFFFFFll;
+      }
     }
     t.thr = thr | (fits ? 8u : 0u);
     t.z0 = r.z0;

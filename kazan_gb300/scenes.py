@@ -213,7 +213,7 @@ def visible_triangles(scene):
     count, area_sum = 0, 0.0
     for dr in scene.draws:
         m = np.asarray(dr.mvp, np.float64).reshape(4, 4).T  # the push constant is column-major
-        tri = idx[3 * dr.first: 3 * (dr.first + dr.count)].reshape(-1, 3) + dr.vertex_offset
+        tri = idx[dr.first: dr.first + 3 * dr.count].reshape(-1, 3) + dr.vertex_offset  # first: firstIndex
         p = (pos @ m.T)[tri]  # [T, 3, 4]
         x, y, z, w = p[..., 0], p[..., 1], p[..., 2], p[..., 3]
         outside = (np.all(x > w, 1) | np.all(x < -w, 1) | np.all(y > w, 1) | np.all(y < -w, 1) | np.all(z < 0, 1) |
