@@ -1791,7 +1791,9 @@ struct BatchEntry {
   int64_t e[3];            /* edge functions at the centre of the tile's first pixel, minus their thresholds */
   int32_t ex[3], ey[3];    /* edge steps per pixel in x (-dy * 256) and y (dx * 256) */
   float zmin, zmax;
-  uint32_t valid;
+  uint32_t valid;          /* bit 0: the entry has a fragment setup; bit 1: `rect` cuts the tile */
+  int8_t rect[4];          /* the draw's rectangle (first and last pixel column and row) relative to the tile,
+                              clamped to [-1, 64] */
   uint32_t fits;           /* every edge value over the tile fits in 32 bits */
   uint32_t depth;          /* bit 0 test, bit 1 write, bits 2.. compare op */
   uint32_t blend;          /* 0 none, 1 straight alpha (SRC_ALPHA, ONE_MINUS_SRC_ALPHA, ADD), 2 any other */
@@ -2040,6 +2042,13 @@ __device__ bool raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
       }
       const KzDraw& bd = c.draws[r.draw];
       const KzPipe& bp = c.pipes[bd.pipe];
+      if (bd.rect[0] > ti.x0 || bd.rect[1] > ti.y0 || bd.rect[2] - 1 < ti.x1 || bd.rect[3] - 1 < ti.y1) {
+        be.valid |= be.valid << 1;
+        be.rect[0] = (int8_t)min(max(bd.rect[0] - ti.ox, -1), 64);
+        be.rect[1] = (int8_t)min(max(bd.rect[1] - ti.oy, -1), 64);
+        be.rect[2] = (int8_t)min(max(bd.rect[2] - 1 - ti.ox, -1), 64);
+        be.rect[3] = (int8_t)min(max(bd.rect[3] - 1 - ti.oy, -1), 64);
+      }
       be.zmin = bd.zmin;
       be.zmax = bd.zmax;
       be.depth = (bp.depth_test ? 1u : 0u) | (bp.depth_write ? 2u : 0u) | (bp.depth_compare << 2);
@@ -2071,9 +2080,14 @@ __device__ bool raster_tile_ordered(const Ctx& c, uint32_t t, unsigned char* sme
     for (uint32_t j = 0; j < nb; j++) {
       const BatchEntry& be = batch[j];
       if (!be.valid) continue;
+      /* bit 1: the draw's viewport and scissor rectangle cuts this tile, so pixels outside it are skipped
+       * (bins hold every tile the clamped box meets; inside the tile the edges alone would also cover pixels
+       * beyond the rectangle) */
+      const bool cut = (be.valid & 2u) != 0;
 #pragma unroll
       for (int q = 0; q < PER; q++) {
         if (!in[q]) continue;
+        if (cut && (lx[q] < be.rect[0] || lx[q] > be.rect[2] || ly[q] < be.rect[1] || ly[q] > be.rect[3])) continue;
         int64_t E[3];
         if constexpr (MS) {
           /* edge values at the pixel centre, then at each sample (the steps per 1/256 pixel are ex / 256 and

@@ -258,13 +258,22 @@ _VIEWPORTS = [None, (37.5, 20.25, 300.0, 260.0, 0.2, 0.9), (-100.0, 64.0, 700.0,
 _SCISSORS = [None, (0, 0, 256, 512), (100, 37, 333, 250), (60, 0, 1000, 1000)]
 
 
+def _split_draws(scene, parts):
+    """the same triangles as `parts` consecutive non-indexed draws"""
+    n = scene.draws[0].count
+    step = (n + parts - 1) // parts
+    draws = [scenes.Draw(3 * k, min(step, n - k)) for k in range(0, n, step)]
+    return dataclasses.replace(scene, draws=draws)
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["batched", "blend"])
+@pytest.mark.parametrize("case", ["batched", "blend", "blend8"])
 def test_viewports_scissors_and_render_area(renderer, case):
     """dynamic viewport and scissor changed between draws, inside a render area smaller than the framebuffer
     whose loadOp CLEAR clears only that area: the attachments were filled beforehand by vkCmdClearColorImage
-    and vkCmdClearDepthStencilImage, and the oracle gets the same per-draw rectangles"""
-    scene = small_cases()[case]
+    and vkCmdClearDepthStencilImage, and the oracle gets the same per-draw rectangles.  blend8: the blended
+    scene as 8 draws, so that every viewport and scissor reaches the ordered (tile) path"""
+    scene = _split_draws(small_cases()["blend"], 8) if case == "blend8" else small_cases()[case]
     W, H = scene.width, scene.height
     area = (16, 24, W - 52, H - 40)                      # x, y, width, height
     run = render.SceneRun(renderer, scene, mode="batched", tile=16)
