@@ -267,16 +267,17 @@ def _split_draws(scene, parts):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["batched", "blend", "blend8"])
-def test_viewports_scissors_and_render_area(renderer, case):
+@pytest.mark.parametrize("case,tile", [("batched", 16), ("blend", 16), ("blend8", 16), ("blend8", 32)])
+def test_viewports_scissors_and_render_area(renderer, case, tile):
     """dynamic viewport and scissor changed between draws, inside a render area smaller than the framebuffer
     whose loadOp CLEAR clears only that area: the attachments were filled beforehand by vkCmdClearColorImage
     and vkCmdClearDepthStencilImage, and the oracle gets the same per-draw rectangles.  blend8: the blended
-    scene as 8 draws, so that every viewport and scissor reaches the ordered (tile) path"""
+    scene as 8 draws, so that every viewport and scissor reaches the ordered (tile) path, in its common kernel
+    (tile 16) and its general one (tile 32)"""
     scene = _split_draws(small_cases()["blend"], 8) if case == "blend8" else small_cases()[case]
     W, H = scene.width, scene.height
     area = (16, 24, W - 52, H - 40)                      # x, y, width, height
-    run = render.SceneRun(renderer, scene, mode="batched", tile=16)
+    run = render.SceneRun(renderer, scene, mode="batched", tile=tile)
     vs, fs = scene.shaders()
     run.pipe = renderer.pipeline(scene, run.rp, run.layout, vs, fs,
                                  dynamic=(vk.DYNAMIC_STATE_VIEWPORT, vk.DYNAMIC_STATE_SCISSOR))

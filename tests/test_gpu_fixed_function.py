@@ -160,3 +160,52 @@ def test_dynamic_blend_constants_between_draws(renderer, mode):
     only_first = dataclasses.replace(scene, blend_const=consts[0])
     c1, _, _ = kz_oracle.render(only_first, threads=8)
     assert not np.array_equal(c1, col)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["batched", "persistent", "perdraw"])
+@pytest.mark.parametrize("compare", [1, 3])
+def test_opaque_and_blended_draws_in_one_pass(renderer, mode, compare):
+    """one render pass whose pipelines alternate between an opaque one (depth writes on: the visibility path)
+    and a blended one (depth writes off: the ordered tile path) over the same vertex buffer: each segment
+    starts from the attachments the previous one left, as the oracle draws them in API order"""
+    base = SCENES["mixed"]
+    opaque = dataclasses.replace(base, depth_compare=compare)
+    blended = dataclasses.replace(base, blend=True, depth_compare=compare, depth_write=False)
+    order = [(opaque, scenes.Draw(0, 150)), (blended, scenes.Draw(450, 150)), (opaque, scenes.Draw(900, 150)),
+             (blended, scenes.Draw(1350, 150))]
+    run = render.SceneRun(renderer, opaque, mode=mode, tile=16)
+    vs, fs = opaque.shaders()
+    pipes = {id(opaque): run.pipe,
+             id(blended): renderer.pipeline(blended, run.rp, run.layout, vs, fs)}
+    d = renderer.drv
+    d.set_option("mode", mode)
+    cb = renderer.begin()
+    clears = (vk.VkClearValue * 2)()
+    clears[0].color.float32[:] = list(base.clear_color)
+    clears[1].depthStencil.depth = base.clear_depth
+    rbi = vk.VkRenderPassBeginInfo(vk.ST_RENDER_PASS_BEGIN_INFO, None, run.rp, run.fb,
+                                   vk.VkRect2D(vk.VkOffset2D(0, 0), vk.VkExtent2D(base.width, base.height)), 2,
+                                   clears)
+    d.vkCmdBeginRenderPass(cb, byref(rbi), vk.SUBPASS_CONTENTS_INLINE)
+    d.vkCmdBindVertexBuffers(cb, 0, 1, (ctypes.c_void_p * 1)(run.vb.handle.value), (ctypes.c_uint64 * 1)(0))
+    for sc, dr in order:
+        d.vkCmdBindPipeline(cb, vk.BIND_POINT_GRAPHICS, pipes[id(sc)])
+        d.vkCmdDraw(cb, 3 * dr.count, 1, dr.first, 0)
+    d.vkCmdEndRenderPass(cb)
+    vk.check("vkEndCommandBuffer", d.vkEndCommandBuffer(cb))
+    renderer.submit_wait(cb)
+    color, depth = run.read()
+    stats = d.stats(cb)
+    renderer.free_command_buffer(cb)
+    col, dep = kz_oracle.clear_images(base)
+    arr = (kz_oracle.KzoDraw * len(order))()
+    for i, (sc, dr) in enumerate(order):
+        one, _ = kz_oracle.make_draws(sc, [dr])
+        arr[i] = one[0]
+    ost = kz_oracle.KzoStats()
+    area = (ctypes.c_int32 * 4)(0, 0, base.width, base.height)
+    kz_oracle.lib().kzo_render_ds(base.width, base.height, col.ctypes.data, dep.ctypes.data, None, 0, area,
+                                  len(order), arr, 8, byref(ost))
+    _check(base, color, depth, stats, ref=(col, dep, ost.as_dict()))
+    assert stats.segments == len(order)
