@@ -209,3 +209,19 @@ def test_opaque_and_blended_draws_in_one_pass(renderer, mode, compare):
                                   len(order), arr, 8, byref(ost))
     _check(base, color, depth, stats, ref=(col, dep, ost.as_dict()))
     assert stats.segments == len(order)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("front_ccw", [True, False])
+@pytest.mark.parametrize("cull", [0, 1, 2, 3])
+@pytest.mark.parametrize("path", ["opaque", "blended"])
+def test_cull_modes_and_front_faces(renderer, path, cull, front_ccw):
+    """VkCullModeFlags NONE / FRONT / BACK / FRONT_AND_BACK under both front-face windings, on the visibility
+    path (opaque) and the tile path (blended), over triangles of both windings"""
+    scene = dataclasses.replace(SCENES["mixed"], cull=cull, front_ccw=front_ccw)
+    if path == "blended":
+        scene = dataclasses.replace(scene, blend=True, depth_write=False)
+    color, depth, stats = _render(renderer, scene, "batched")
+    _check(scene, color, depth, stats)
+    if cull == 3:
+        assert stats.fragments == 0
