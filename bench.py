@@ -189,6 +189,32 @@ def profiled_traffic(workload, kernel):
         return None
 
 
+def profiled_instructions(workload, kernel):
+    """warp instructions per launch of `kernel` on `workload` from the committed ncu summary (None if absent)"""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get("instructions", {}).get(workload, {}).get(kernel)
+    except (OSError, ValueError, AttributeError):
+        return None
+
+
+def issue_roofline(workload, kernel, kernel_ms, sm_mhz):
+    """the dominant kernel against the SMs' instruction issue rate (one warp instruction per cycle per
+    scheduler, 4 schedulers per SM, at the SM clock measured during the timed region): its warp instructions
+    per launch (ncu, committed) over its live CUDA-event duration; None without a profile"""
+    import torch
+    inst = profiled_instructions(workload, kernel)
+    if not inst or not sm_mhz:
+        return None
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    achieved = inst / (kernel_ms / 1e3) / 1e9
+    peak = sms * 4 * sm_mhz * 1e6 / 1e9
+    return {"achieved": round(achieved, 1), "peak": round(peak, 1), "unit": "G warp instructions/s",
+            "frac": round(achieved / peak, 4), "warp_instructions": inst,
+            "peak_source": "%d SMs x 4 schedulers x %.0f MHz (median SM clock under load)" % (sms, sm_mhz)}
+
+
 def kernel_bytes(scene, kernel):
     """algorithmic HBM bytes of one launch of `kernel` over the whole scene (one segment):
       kz_k_persistent            the whole path: 12 T_indexed + S_v V + 64 draws + framebuffer traffic
@@ -259,10 +285,13 @@ def main():
         # launch schedule and tile side from the autotuner (measured here unless cached for this workload)
         from kazan_gb300 import autotune
         gpu = r.props.deviceName.decode(errors="replace")
-        sig = autotune.signature(gpu, scene.blend, len(scene.draws), scene.triangles, scene.width, scene.height)
+        # blending, a D16 / D24S8 attachment or multisampling puts the pass on the ordered (tile) path
+        ordered = scene.blend or scene.depth_format != "d32" or scene.samples > 1
+        sig = autotune.signature(gpu, ordered, len(scene.draws), scene.triangles, scene.width, scene.height)
         sig += "|indirect" if indirect else ""
-        best, table = autotune.Tuner().choose(sig, autotune.scene_timer(run),
-                                              autotune.candidates(ordered=scene.blend))
+        sig += "" if (scene.depth_format, scene.samples) == ("d32", 1) else "|%s|%dx" % (scene.depth_format,
+                                                                                        scene.samples)
+        best, table = autotune.Tuner().choose(sig, autotune.scene_timer(run), autotune.candidates(ordered=ordered))
         mode, tile = best.mode, best.tile
         tuning = {"signature": sig, "chosen": best.options(),
                   "ms": None if table is None else {c.label(): round(v, 4) for c, v in table.items()}}
@@ -329,6 +358,8 @@ def main():
     value = replicas.aggregate_rate(rk, tris, ms) / 1e6
     peak, peak_kind = measured_peak()
     kb, kformula = kernel_bytes(scene, dom)
+    # the committed ncu figures hold for the default workloads only (the batched one at 4,096 draws)
+    prof_key = args.workload if args.workload != "batched" or args.ndraws == 4096 else None
     achieved = kb / (dom_ms / 1e3) / 1e9
     out = {"metric": "Mtris/s (batched command buffer, exact coverage)", "value": round(value, 2),
            "unit": "Mtris/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
@@ -341,10 +372,11 @@ def main():
            "gfrag_per_s": round(st.fragments / (ms / 1e3) / 1e9, 3),
            "fragments": int(st.fragments),
            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                        "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.workload, dom),
+                        "frac": round(achieved / peak, 4), "traffic": profiled_traffic(prof_key, dom),
                         "kernel": dom, "kernel_ms": round(dom_ms, 4), "algorithmic_bytes": kb,
                         "bytes_formula": kformula,
-                        "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"},
+                        "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                        "issue": issue_roofline(prof_key, dom, dom_ms, (ck_k or {}).get("sm_mhz"))},
            "kernels": kernels,
            "kernel_pass": {"ms_per_step": round(ms_k, 4), "steps": args.steps, "clocks": ck_k,
                            "how": "the same submissions with an event pair around each kernel launch"},
