@@ -221,7 +221,7 @@ def kernel_bytes(scene, kernel):
       kz_k_vis_geometry / geometry  index + vertex-position bytes + push constants: 12 T_indexed + P V + 64 draws
                                  (P = 12 B position of the Lambert layout, 16 B of the colour layout)
       kz_k_vis_resolve           colour + depth stores: W H (4 + 4)
-      kz_k_raster(_direct)       framebuffer read + write (depth written or not)
+      kz_k_raster(_direct/_ds/_ms)  framebuffer read + write (depth written or not)
     returns (bytes, formula)"""
     t_idx = scene.triangles if scene.indexed else 0
     v = len(scene.vertices) if scene.indexed else 3 * scene.triangles
@@ -232,7 +232,7 @@ def kernel_bytes(scene, kernel):
         return 12 * t_idx + pos * v + push, "12*T_indexed + %d*V + 64*draws" % pos
     if kernel == "kz_k_vis_resolve":
         return wh * 8, "W*H*(4+4)"
-    if kernel in ("kz_k_raster", "kz_k_raster_direct"):
+    if kernel in ("kz_k_raster", "kz_k_raster_direct", "kz_k_raster_ds", "kz_k_raster_ms"):
         return wh * ((4 + 4) * 2 if scene.depth_write else (2 * 4 + 4)), "W*H*framebuffer read+write"
     return scene.algorithmic_bytes(), "12*T_indexed + S_v*V + 64*draws + W*H*(4+4)*2"
 

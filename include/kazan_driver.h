@@ -96,8 +96,9 @@ KZ_API int kzGetCommandBufferStats(VkCommandBuffer commandBuffer, KzCommandBuffe
 #define KZ_KERNEL_KIND_NAMES                                                                          \
   {"kz_k_persistent", "kz_k_vis_init", "kz_k_vis_geometry", "kz_k_vis_large", "kz_k_vis_resolve",      \
    "kz_k_geometry",   "kz_k_scan",     "kz_k_bin",          "kz_k_raster",    "kz_k_clear",         \
-   "kz_k_indirect",   "kz_k_indirect_tables", "kz_k_resolve", "kz_k_persistent_vis", "kz_k_raster_direct"}
-#define KZ_KERNEL_KINDS 15
+   "kz_k_indirect",   "kz_k_indirect_tables", "kz_k_resolve", "kz_k_persistent_vis", "kz_k_raster_direct",  \
+   "kz_k_raster_ds",  "kz_k_raster_ms"}
+#define KZ_KERNEL_KINDS 17
 
 /* Device time of a command buffer recorded with "kernel_timing" on: for each kernel kind, the summed
  * durations (CUDA events on the queue stream around each launch) and the number of launches over all

@@ -1400,6 +1400,9 @@ static uint32_t launch_ops(CommandBuffer* cb, cudaStream_t st, uint32_t start, b
           cfg.gridDim = dim3(std::min(grid_cap(dev), std::max(1u, seg.tiles_x * seg.tiles_y)));
           cfg.dynamicSmemBytes = KZ_DYN_SMEM;
           if (raster_direct(low, seg)) launch(dev, timing, KK_RASTER_DIRECT, cfg, ks->raster_direct, args, chain);
+          else if (seg.samples > 1) launch(dev, timing, KK_RASTER_MS, cfg, ks->raster_ms, args, chain);
+          else if (seg.depth_format != KZ_DF_D32 && seg.tile <= 16)
+            launch(dev, timing, KK_RASTER_DS, cfg, ks->raster_ds, args, chain);
           else launch(dev, timing, KK_RASTER, cfg, ks->raster, args, chain);
           launches += 3;
         }

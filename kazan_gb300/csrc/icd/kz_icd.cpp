@@ -175,7 +175,8 @@ KernelSet* kernel_set_for(Device* dev, const std::vector<Pipeline*>& pipes, cons
   } names[] = {{"kz_k_geometry", &ks->geometry}, {"kz_k_scan", &ks->scan},
                {"kz_k_bin", &ks->bin},           {"kz_k_raster", &ks->raster},
                {"kz_k_persistent", &ks->persistent}, {"kz_k_persistent_vis", &ks->persistent_vis},
-               {"kz_k_raster_direct", &ks->raster_direct},
+               {"kz_k_raster_direct", &ks->raster_direct}, {"kz_k_raster_ds", &ks->raster_ds},
+               {"kz_k_raster_ms", &ks->raster_ms},
                {"kz_k_clear", &ks->clear},
                {"kz_k_vis_init", &ks->vis_init}, {"kz_k_vis_geometry", &ks->vis_geometry},
                {"kz_k_vis_large", &ks->vis_large}, {"kz_k_vis_resolve", &ks->vis_resolve},

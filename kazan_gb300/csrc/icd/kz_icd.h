@@ -212,6 +212,8 @@ enum KernelKind {
   KK_RESOLVE,
   KK_PERSISTENT_VIS,
   KK_RASTER_DIRECT,
+  KK_RASTER_DS,
+  KK_RASTER_MS,
   KK_COUNT
 };
 
@@ -226,7 +228,8 @@ struct PipelineCache {};
 struct KernelSet {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t geometry = nullptr, scan = nullptr, bin = nullptr, raster = nullptr, persistent = nullptr,
-               persistent_vis = nullptr, raster_direct = nullptr, clear = nullptr, vis_init = nullptr,
+               persistent_vis = nullptr, raster_direct = nullptr, raster_ds = nullptr, raster_ms = nullptr,
+               clear = nullptr, vis_init = nullptr,
                vis_geometry = nullptr,
                vis_large = nullptr, vis_resolve = nullptr, indirect = nullptr, indirect_tables = nullptr,
                resolve = nullptr;

@@ -2509,6 +2509,32 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster(KzFrame 
  * a kernel with only that instance of the tile raster, so that its register allocation serves it alone;
  * each tile's colour and depth are staged in shared memory by TMA tensor copies where the segment has
  * tensor maps */
+/* the ordered tile raster of one segment kind as a kernel of its own, so that its registers serve that
+ * instance alone: DS, a D16 / D24S8 attachment with one sample per pixel (tiles of at most 16 x 16); MS, four
+ * samples per pixel */
+template <bool DS, bool MS>
+__device__ __forceinline__ void raster_tiles_of(const KzFrame& f, uint32_t s, unsigned char* smem, float* u8tab) {
+  kz_pdl_enter();
+  Ctx c = make_ctx(f, s);
+  if (segment_blocked(c, s)) return;
+  fill_color_tabs(u8tab);
+  uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    raster_tile_ordered<1, DS, MS, true>(c, t, smem, u8tab, 0);
+    __syncthreads();
+    if (threadIdx.x == 0) reinterpret_cast<uint32_t*>(c.seg->tile_count)[t] = 0; /* as raster_tile leaves it */
+  }
+}
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster_ds(KzFrame f, uint32_t s) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float u8tab[KZ_CTAB_FLOATS];
+  raster_tiles_of<true, false>(f, s, smem, u8tab);
+}
+extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster_ms(KzFrame f, uint32_t s) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float u8tab[KZ_CTAB_FLOATS];
+  raster_tiles_of<false, true>(f, s, smem, u8tab);
+}
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster_direct(KzFrame f, uint32_t s) {
   kz_pdl_enter();
   extern __shared__ __align__(16) unsigned char smem[];

@@ -607,7 +607,8 @@ class VkBufferImageCopy(Structure):
 # kernel kinds of kzGetKernelTimes (KZ_KERNEL_KIND_NAMES)
 KERNEL_KINDS = ["kz_k_persistent", "kz_k_vis_init", "kz_k_vis_geometry", "kz_k_vis_large", "kz_k_vis_resolve",
                 "kz_k_geometry", "kz_k_scan", "kz_k_bin", "kz_k_raster", "kz_k_clear", "kz_k_indirect",
-                "kz_k_indirect_tables", "kz_k_resolve", "kz_k_persistent_vis", "kz_k_raster_direct"]
+                "kz_k_indirect_tables", "kz_k_resolve", "kz_k_persistent_vis", "kz_k_raster_direct",
+                "kz_k_raster_ds", "kz_k_raster_ms"]
 
 
 class KzCommandBufferStats(Structure):
