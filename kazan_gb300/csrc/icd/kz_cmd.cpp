@@ -1660,7 +1660,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
   low.d_tables = static_cast<char*>(p);
   low.d_counters = reinterpret_cast<KzSegCounters*>(low.d_tables + o_counters);
   low.d_status = reinterpret_cast<KzStatus*>(low.d_tables + o_status);
-  r = device_alloc(std::max<size_t>(4, (size_t)(low.max_tiles + 1) * 3 * 4), &p);
+  r = device_alloc(std::max<size_t>(4, (size_t)(low.max_tiles + 1) * 4 * 4), &p);
   if (r != VK_SUCCESS) return r;
   low.d_tiles = static_cast<uint32_t*>(p);
   size_t vis_px = 0;
@@ -1676,6 +1676,7 @@ VkResult lower_command_buffer(CommandBuffer* cb) {
     s.tile_count = (uint64_t)(uintptr_t)low.d_tiles;
     s.tile_offset = (uint64_t)(uintptr_t)(low.d_tiles + low.max_tiles);
     s.tile_cursor = (uint64_t)(uintptr_t)(low.d_tiles + 2 * (size_t)low.max_tiles + 1);
+    s.tile_order = (uint64_t)(uintptr_t)(low.d_tiles + 3 * (size_t)low.max_tiles + 1);
     s.counters = (uint64_t)(uintptr_t)(low.d_counters + i);
     s.draw_lut = s.num_prims ? (uint64_t)(uintptr_t)(low.d_tables + o_lut + low.draw_lut_offset[i] * sizeof(uint32_t))
                              : 0;

@@ -224,6 +224,7 @@ typedef struct KzSegment {
   uint64_t tile_count;       /* u32[tiles] */
   uint64_t tile_offset;      /* u32[tiles + 1] */
   uint64_t tile_cursor;      /* u32[tiles] */
+  uint64_t tile_order;       /* u32[tiles]: the tiles by decreasing bin size (powers of two), for the raster */
   uint64_t bins;             /* u32[pair_cap] */
   uint64_t counters;         /* KzSegCounters* */
   uint64_t vis;              /* visibility mode: u64 (depth, primitive) key per pixel, width * height */

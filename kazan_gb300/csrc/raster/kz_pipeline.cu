@@ -928,6 +928,27 @@ __device__ void scan_tiles(const Ctx& c, uint32_t s, uint32_t* sh) {
   }
   atomicMax(&c.cnt->max_bin, mx);
   __syncthreads();
+  /* the raster's tile order: by decreasing bucket floor(log2(bin size)) + 1 (empty bins last), so that the
+   * largest bins start first and the kernel's tail is made of small ones */
+  if (seg.tile_order) {
+    uint32_t* hist = sh; /* 33 buckets, reusing the block's scan words */
+    if (threadIdx.x <= 32) hist[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t i = b0; i < b1; i++) atomicAdd(&hist[32 - __clz(tc[i])], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t at = 0;
+      for (int k = 32; k >= 0; k--) {
+        const uint32_t v = hist[k];
+        hist[k] = at;
+        at += v;
+      }
+    }
+    __syncthreads();
+    uint32_t* order = reinterpret_cast<uint32_t*>(seg.tile_order);
+    for (uint32_t i = b0; i < b1; i++) order[atomicAdd(&hist[32 - __clz(tc[i])], 1u)] = i;
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
     uint32_t pairs = sh[blockDim.x];
     to[n] = pairs;
@@ -2493,6 +2514,20 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS) kz_k_bin(KzFrame f, uin
 
 /* 4 blocks per SM (at most 64 registers, some spilled): measured on the ordered blend workload at 2.90 ms
  * against 3.44 (3 blocks, 85 registers), 3.78 (2 blocks, 128 registers) and 3.06 (5 blocks) */
+/* the next tile for this block of a tile-raster kernel: the segment's tile cursor indexes the tile order the
+ * scan wrote (largest bins first), so blocks that finish early take more tiles and the tail is made of small
+ * bins (bins differ by tens of times in size); `slot` is a shared word of the block */
+__device__ __forceinline__ uint32_t next_tile(const Ctx& c, uint32_t& slot) {
+  if (threadIdx.x == 0) {
+    const uint32_t k = atomicAdd(&c.cnt->tile_next, 1u), n = c.seg->tiles_x * c.seg->tiles_y;
+    slot = k < n && c.seg->tile_order ? reinterpret_cast<const uint32_t*>(c.seg->tile_order)[k] : k;
+  }
+  __syncthreads();
+  const uint32_t t = slot;
+  __syncthreads();
+  return t;
+}
+
 extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster(KzFrame f, uint32_t s) {
   kz_pdl_enter();
   extern __shared__ __align__(16) unsigned char smem[];
@@ -2501,7 +2536,12 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster(KzFrame 
   if (segment_blocked(c, s)) return;
   fill_color_tabs(u8tab);
   uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) raster_tile(c, t, smem, u8tab);
+  __shared__ uint32_t tnext;
+  for (;;) {
+    const uint32_t t = next_tile(c, tnext);
+    if (t >= ntiles) break;
+    raster_tile(c, t, smem, u8tab);
+  }
 }
 
 /* kz_k_raster for the common ordered segment -- one sample per pixel, D32 depth, tiles of at most 16x16, and
@@ -2519,7 +2559,10 @@ __device__ __forceinline__ void raster_tiles_of(const KzFrame& f, uint32_t s, un
   if (segment_blocked(c, s)) return;
   fill_color_tabs(u8tab);
   uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  __shared__ uint32_t tnext;
+  for (;;) {
+    const uint32_t t = next_tile(c, tnext);
+    if (t >= ntiles) break;
     raster_tile_ordered<1, DS, MS, true>(c, t, smem, u8tab, 0);
     __syncthreads();
     if (threadIdx.x == 0) reinterpret_cast<uint32_t*>(c.seg->tile_count)[t] = 0; /* as raster_tile leaves it */
@@ -2554,7 +2597,10 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 4) kz_k_raster_direct(K
   ts.mbar = &tile_mbar;
   ts.phase = 0;
   uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  __shared__ uint32_t tnext;
+  for (;;) {
+    const uint32_t t = next_tile(c, tnext);
+    if (t >= ntiles) break;
     if (!raster_tile_ordered<1, false, false, false, true>(c, t, smem, u8tab, 0, &ts)) return;
     __syncthreads();
     if (threadIdx.x == 0) reinterpret_cast<uint32_t*>(c.seg->tile_count)[t] = 0; /* as raster_tile leaves it */
