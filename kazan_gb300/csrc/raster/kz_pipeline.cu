@@ -2719,7 +2719,7 @@ extern "C" __global__ void __launch_bounds__(KZ_THREADS, 3) kz_k_persistent(KzFr
     if (!grid_barrier(st, f.barrier_ns)) return;
     uint32_t ntiles = c.seg->tiles_x * c.seg->tiles_y;
     for (;;) {
-      uint32_t t = grab(&c.cnt->tile_next, &item);
+      uint32_t t = next_tile(c, item);
       if (t >= ntiles) break;
       raster_tile(c, t, smem, u8tab);
     }
