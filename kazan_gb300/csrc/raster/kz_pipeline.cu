@@ -7,13 +7,24 @@
  * counterpart for any kernel here (vulkan-driver/src/api_impl.rs:4632-4653 are `unimplemented!()`).
  *
  * Phases of one raster segment (see kz_raster_abi.h):
- *   geometry  per triangle: index + attribute fetch, position-only vertex shader, guard-band clip,
- *             viewport transform, 16.8 snap, facing/cull, bounding box -> KzTriRecord, tile pair counts
- *   scan      per tile: exclusive prefix of pair counts -> bin offsets; capacity checks
- *   bin       per record: scatter record index into each overlapped tile's bin
- *   raster    per tile: visibility mode  - shared-memory 64-bit atomicMin of (depth, primitive) keys,
- *                                          then one fragment-shader call per pixel for the winner
- *                       ordered mode     - bin sorted by primitive, per-pixel in-order depth/blend
+ *   visibility mode (opaque segments: no blending, a depth rule a minimum can express)
+ *     vis_init      per pixel: the 64-bit key (depth, primitive) of the cleared or loaded depth
+ *     vis_geometry  per 32-triangle group, one warp: index fetch, position-only vertex shader, clip codes,
+ *                   projection, 16.8 snap, cull, setup; the warp rasterises the small triangles itself
+ *                   (64-bit atomicMin into the keys) and turns the large ones into 8x8-block jobs
+ *     vis_large     per job, one warp: the job's blocks
+ *     vis_resolve   per 32-pixel row run, one warp: the winning primitive's setup again, one fragment-shader
+ *                   call per pixel, colour and depth stored
+ *   ordered mode (blending, discard, stencil, other compare ops, D16 / D24S8, multisampling)
+ *     geometry      per triangle: as above, plus the record's shading setup -> KzTriRecord, tile counts
+ *     scan          per tile: exclusive prefix of the counts -> bin offsets; capacity checks; the tiles'
+ *                   raster order (largest bins first)
+ *     bin           per record: its index into each overlapped tile's bin
+ *     raster        per tile, taken from a counter in that order: bin sorted by primitive in shared
+ *                   memory, each pixel run through it in API order (coverage, depth / stencil, fragment
+ *                   shader, blend); the common case stages the tile's colour and depth through TMA
+ *   Both run as separate kernels (chained by programmatic dependent launch) or inside one persistent
+ *   cooperative kernel with bounded grid barriers between the phases.
  *
  * Arithmetic follows the rules the CPU oracle restates (every float op an explicit IEEE single op;
  * the file is built with -fmad=false and uses the __f*_rn intrinsics), so coverage, depth and colour
