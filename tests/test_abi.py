@@ -71,10 +71,23 @@ def test_instance_without_gpu_has_no_physical_device(driver):
                                           ("mode", "perdraw", True), ("mode", "fast", False),
                                           ("tile", "16", True), ("tile", "12", False),
                                           ("kernel_timing", "1", True), ("kernel_timing", "2", False),
-                                          ("trace", "0", True), ("no_such_option", "1", False)])
+                                          ("trace", "0", True), ("no_such_option", "1", False),
+                                          ("pdl", "0", True), ("pdl", "yes", False),
+                                          ("tma", "0", True), ("tma", "2", False),
+                                          ("vector_fetch", "0", True), ("vector_fetch", "", False),
+                                          ("barrier_ns", "0", True), ("barrier_ns", "4294967296", False),
+                                          ("barrier_ns", "-1", False),
+                                          ("warp_px", "1", True), ("warp_px", "4096", True),
+                                          ("warp_px", "0", False), ("warp_px", "4097", False),
+                                          ("warp_px", "12a", False),
+                                          ("job_blocks", "1", True), ("job_blocks", "32", True),
+                                          ("job_blocks", "0", False), ("job_blocks", "33", False),
+                                          ("geo_blocks", "0", True), ("geo_blocks", "64", True),
+                                          ("geo_blocks", "65", False), ("geo_blocks", "", False)])
 def test_driver_options(driver, key, value, ok):
     rc = driver.lib.kzDriverSetOption(key.encode(), value.encode())
     assert (rc == 0) == ok
-    driver.lib.kzDriverSetOption(b"mode", b"persistent")
-    driver.lib.kzDriverSetOption(b"tile", b"16")
-    driver.lib.kzDriverSetOption(b"kernel_timing", b"0")
+    for k, v in ((b"mode", b"persistent"), (b"tile", b"16"), (b"kernel_timing", b"0"), (b"pdl", b"1"),
+                 (b"tma", b"1"), (b"vector_fetch", b"1"), (b"barrier_ns", b"4000000000"), (b"warp_px", b"192"),
+                 (b"job_blocks", b"16"), (b"geo_blocks", b"0")):
+        driver.lib.kzDriverSetOption(k, v)
