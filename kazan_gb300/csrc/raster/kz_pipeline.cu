@@ -911,42 +911,54 @@ __device__ void scan_tiles(const Ctx& c, uint32_t s, uint32_t* sh) {
   const uint32_t* tc = reinterpret_cast<const uint32_t*>(seg.tile_count);
   uint32_t* to = reinterpret_cast<uint32_t*>(seg.tile_offset);
   uint32_t* cur = reinterpret_cast<uint32_t*>(seg.tile_cursor);
-  uint32_t per = (n + blockDim.x - 1) / blockDim.x;
-  uint32_t b0 = threadIdx.x * per, b1 = min(n, b0 + per);
-  uint32_t sum = 0, mx = 0;
-  for (uint32_t i = b0; i < b1; i++) {
-    uint32_t v = tc[i];
-    sum += v;
+  uint32_t* order = reinterpret_cast<uint32_t*>(seg.tile_order);
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  /* sh: [0, 32) per-warp sums, [32, 65) the order's buckets (floor(log2(bin size)) + 1, empty bins 0),
+   * [blockDim.x] the running total */
+  uint32_t* wsum = sh;
+  uint32_t* hist = sh + 32;
+  if (threadIdx.x <= 32) hist[threadIdx.x] = 0;
+  if (threadIdx.x == 0) sh[blockDim.x] = 0;
+  __syncthreads();
+  /* exclusive prefix of the counts, blockDim.x tiles at a time (coalesced), with a warp-shuffle scan */
+  uint32_t mx = 0;
+  for (uint32_t base = 0; base < n; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < n ? tc[i] : 0u;
     mx = max(mx, v);
-  }
-  sh[threadIdx.x] = sum;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t run = 0;
-    for (uint32_t i = 0; i < blockDim.x; i++) {
-      uint32_t v = sh[i];
-      sh[i] = run;
-      run += v;
+    if (i < n && order) atomicAdd(&hist[32 - __clz(v)], 1u);
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= (uint32_t)o) incl += t;
     }
-    sh[blockDim.x] = run;
-  }
-  __syncthreads();
-  uint32_t run = sh[threadIdx.x];
-  for (uint32_t i = b0; i < b1; i++) {
-    to[i] = run;
-    cur[i] = 0;
-    run += tc[i];
-  }
-  atomicMax(&c.cnt->max_bin, mx);
-  __syncthreads();
-  /* the raster's tile order: by decreasing bucket floor(log2(bin size)) + 1 (empty bins last), so that the
-   * largest bins start first and the kernel's tail is made of small ones */
-  if (seg.tile_order) {
-    uint32_t* hist = sh; /* 33 buckets, reusing the block's scan words */
-    if (threadIdx.x <= 32) hist[threadIdx.x] = 0;
+    if (lane == 31) wsum[wid] = incl;
     __syncthreads();
-    for (uint32_t i = b0; i < b1; i++) atomicAdd(&hist[32 - __clz(tc[i])], 1u);
+    if (wid == 0) {
+      uint32_t w = lane < nw ? wsum[lane] : 0u, wi = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+        if (lane >= (uint32_t)o) wi += t;
+      }
+      if (lane < nw) wsum[lane] = wi - w; /* exclusive per warp */
+    }
     __syncthreads();
+    const uint32_t carry = sh[blockDim.x];
+    if (i < n) {
+      to[i] = carry + wsum[wid] + incl - v;
+      cur[i] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) sh[blockDim.x] = carry + wsum[wid] + incl;
+    __syncthreads();
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+  if (lane == 0) atomicMax(&c.cnt->max_bin, mx);
+  /* the raster's tile order: by decreasing bucket, empty bins last, so that the largest bins start first
+   * and the raster kernel's tail is made of small ones */
+  if (order) {
     if (threadIdx.x == 0) {
       uint32_t at = 0;
       for (int k = 32; k >= 0; k--) {
@@ -956,10 +968,9 @@ __device__ void scan_tiles(const Ctx& c, uint32_t s, uint32_t* sh) {
       }
     }
     __syncthreads();
-    uint32_t* order = reinterpret_cast<uint32_t*>(seg.tile_order);
-    for (uint32_t i = b0; i < b1; i++) order[atomicAdd(&hist[32 - __clz(tc[i])], 1u)] = i;
-    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) order[atomicAdd(&hist[32 - __clz(tc[i])], 1u)] = i;
   }
+  __syncthreads();
   if (threadIdx.x == 0) {
     uint32_t pairs = sh[blockDim.x];
     to[n] = pairs;
