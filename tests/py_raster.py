@@ -15,6 +15,12 @@ tested with any VkCompareOp and written or not;
 colour = perspective-correct interpolation q = fma(l2, 1/w2, fma(l1, 1/w1, l0 * 1/w0)),
 c = fma(l2, c2/w2, fma(l1, c1/w1, l0 * c0/w0)) * (1 / q), stored as round(clamp(c, 0, 1) * 255) through
 the colour write mask, or blended (the 15 single-source factors, the 5 ops, constants; blend_texel).
+Optionally (render's `cull`, `front_ccw`, `viewport`, `scissor`): the polygon's area in framebuffer
+coordinates a = -1/2 sum(x_i y_i+1 - x_i+1 y_i) decides facing (a > 0 is counter-clockwise), culled by
+VkCullModeFlags; a viewport (x, y, width, height, minDepth, maxDepth) maps x_f = fma(x_d, w/2, x + w/2) and
+z_f = fma(z_d, maxDepth - minDepth, minDepth) (each constant one binary32 operation), clamps depth to its
+depth range, and admits pixel column p when p + 1/2 lies in [x, x + width) (rows likewise, for either sign
+of the height); a scissor rectangle (x, y, width, height) admits its pixels.
 """
 from fractions import Fraction
 import math
@@ -114,16 +120,37 @@ def blend_texel(texel, out, factors, consts, write_mask):
     return res
 
 
+def _pixel_range(lo, extent):
+    """first and one-past-last pixel p with p + 1/2 in [lo, lo + extent) (extent may be negative), from the
+    binary32 operations ceil(lo - 1/2) and ceil((lo + extent) - 1/2)"""
+    end = f32(lo + extent)
+    a, b = (lo, end) if extent >= 0 else (end, lo)
+    return math.ceil(f32(a - HALF)), math.ceil(f32(b - HALF))
+
+
 def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_depth=1.0, compare=1, depth_write=True,
-           blend=None, blend_const=(0.0, 0.0, 0.0, 0.0), write_mask=0xF):
+           blend=None, blend_const=(0.0, 0.0, 0.0, 0.0), write_mask=0xF, cull=0, front_ccw=True, viewport=None,
+           scissor=None):
     """vertices: float32 [3T, 8] (x, y, z, w, r, g, b, a); returns (colour uint8 [H, W, 4], depth float32
     [H, W], fragment count).  compare: the VkCompareOp of the depth test; blend: None, or the six blend
-    factors and ops of blend_texel."""
+    factors and ops of blend_texel; cull: VkCullModeFlags; viewport: (x, y, width, height, minDepth,
+    maxDepth), default the whole framebuffer with depths [0, 1]; scissor: (x, y, width, height)."""
     v = np.asarray(vertices, dtype=np.float32).reshape(-1, 8)
     color = np.empty((height, width, 4), dtype=np.uint8)
     color[:] = [unorm8(Fraction(float(np.float32(c)))) for c in clear_color]
     depth = [[Fraction(float(np.float32(clear_depth)))] * width for _ in range(height)]
-    hx, hy = f32(Fraction(width) / 2), f32(Fraction(height) / 2)
+    vp = [Fraction(float(np.float32(c))) for c in (viewport or (0, 0, width, height, 0, 1))]
+    hx, hy = mul(vp[2], HALF), mul(vp[3], HALF)
+    ox, oy = f32(vp[0] + hx), f32(vp[1] + hy)
+    pz, oz = f32(vp[5] - vp[4]), vp[4]
+    zlo, zhi = min(vp[4], vp[5]), max(vp[4], vp[5])
+    # the pixels a draw may touch: framebuffer, scissor and viewport
+    rx0, rx1 = _pixel_range(vp[0], vp[2])
+    ry0, ry1 = _pixel_range(vp[1], vp[3])
+    rx0, ry0, rx1, ry1 = max(rx0, 0), max(ry0, 0), min(rx1, width), min(ry1, height)
+    if scissor is not None:
+        rx0, ry0 = max(rx0, scissor[0]), max(ry0, scissor[1])
+        rx1, ry1 = min(rx1, scissor[0] + scissor[2]), min(ry1, scissor[1] + scissor[3])
     frags = 0
     for t in range(len(v) // 3):
         P = [[Fraction(float(c)) for c in v[3 * t + j]] for j in range(3)]
@@ -132,22 +159,26 @@ def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_dept
             x, y, z, w = p[:4]
             assert w > 0 and 0 <= z <= w and abs(x) <= 4 * w and abs(y) <= 4 * w, "case needs clipping"
             iw = div(1, w)
-            X.append(int(rne(mul(fma(mul(x, iw), hx, hx), 256))))
-            Y.append(int(rne(mul(fma(mul(y, iw), hy, hy), 256))))
-            Z.append(fma(mul(z, iw), Fraction(1), Fraction(0)))
+            X.append(int(rne(mul(fma(mul(x, iw), hx, ox), 256))))
+            Y.append(int(rne(mul(fma(mul(y, iw), hy, oy), 256))))
+            Z.append(fma(mul(z, iw), pz, oz))
             IW.append(iw)
             A.append([mul(c, iw) for c in p[4:8]])
         S = (X[1] - X[0]) * (Y[2] - Y[0]) - (X[2] - X[0]) * (Y[1] - Y[0])
         if S == 0:
             continue
+        area = -Fraction(sum(X[i] * Y[(i + 1) % 3] - X[(i + 1) % 3] * Y[i] for i in range(3)), 2)
+        front = area > 0 if front_ccw else area < 0
+        if (cull & 2 and not front) or (cull & 1 and front):
+            continue
         if S < 0:
             for arr in (X, Y, Z, IW, A):
                 arr[1], arr[2] = arr[2], arr[1]
             S = -S
-        bx0 = max(0, -((-(min(X) - 128)) // 256))
-        by0 = max(0, -((-(min(Y) - 128)) // 256))
-        bx1 = min(width - 1, (max(X) - 128) // 256)
-        by1 = min(height - 1, (max(Y) - 128) // 256)
+        bx0 = max(rx0, -((-(min(X) - 128)) // 256))
+        by0 = max(ry0, -((-(min(Y) - 128)) // 256))
+        bx1 = min(rx1 - 1, (max(X) - 128) // 256)
+        by1 = min(ry1 - 1, (max(Y) - 128) // 256)
         inv_s = div(1, f32(S))
         z0, dz1, dz2 = Z[0], f32(Z[1] - Z[0]), f32(Z[2] - Z[0])
         tl, dxs, dys = [], [], []
@@ -169,7 +200,7 @@ def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_dept
                 frags += 1
                 l = [mul(f32(E[e]), inv_s) for e in range(3)]
                 z = fma(l[2], dz2, fma(l[1], dz1, z0))
-                z = min(max(z, Fraction(0)), Fraction(1))
+                z = min(max(z, zlo), zhi)
                 if not depth_cmp(compare, z, depth[py][px]):
                     continue
                 if depth_write:

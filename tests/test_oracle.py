@@ -227,3 +227,52 @@ def test_oracle_blend_states_match_python(built, i):
     pc, pd, _ = py_raster.render(sc.vertices, size, size, clear_color=sc.clear_color, compare=3, depth_write=False,
                                  blend=state, blend_const=sc.blend_const, write_mask=sc.write_mask)
     _compare_states(oc, od, pc, pd)
+
+
+@pytest.mark.parametrize("front_ccw", [True, False])
+@pytest.mark.parametrize("cull", range(4))
+def test_oracle_cull_modes_match_python(built, cull, front_ccw):
+    """VkCullModeFlags NONE / FRONT / BACK / FRONT_AND_BACK under both windings against the restatement, which
+    decides facing from the specification's polygon area formula"""
+    size = 16
+    sc = scenes.triangles_from(np.array(_state_rows(70 + cull, 12, size), dtype=np.float32), size, size,
+                               clear_color=(0.1, 0.2, 0.3, 0.4), cull=cull, front_ccw=front_ccw)
+    oc, od, ost = kz_oracle.render(sc, threads=1)
+    pc, pd, pf = py_raster.render(sc.vertices, size, size, clear_color=sc.clear_color, cull=cull,
+                                  front_ccw=front_ccw)
+    _compare_states(oc, od, pc, pd)
+    assert ost["fragments"] == pf
+    if cull == 3:
+        assert pf == 0
+
+
+# (x, y, width, height, minDepth, maxDepth) on a 24x24 framebuffer: the whole framebuffer; a fractional
+# offset with a narrowed depth range; one reaching past the left edge with an inverted depth range; a
+# y-flipped one
+VIEWPORTS = [(0.0, 0.0, 24.0, 24.0, 0.0, 1.0), (3.5, 2.25, 15.0, 17.0, 0.2, 0.9), (-4.0, 3.0, 30.0, 16.0, 1.0, 0.0),
+             (2.0, 21.0, 18.0, -17.5, 0.0, 1.0)]
+SCISSORS = [(0, 0, 24, 24), (5, 3, 11, 14), (10, 0, 100, 100)]
+
+
+@pytest.mark.parametrize("scissor", range(len(SCISSORS)))
+@pytest.mark.parametrize("viewport", range(len(VIEWPORTS)))
+def test_oracle_viewports_and_scissors_match_python(built, viewport, scissor):
+    """the viewport transform (offsets, depth ranges, flips) and the pixel rectangle of viewport and scissor,
+    against the restatement"""
+    import ctypes
+    size = 24
+    vp, sci = VIEWPORTS[viewport], SCISSORS[scissor]
+    sc = scenes.triangles_from(np.array(_random_rows(80 + viewport, 12, size, True), dtype=np.float32), size, size,
+                               clear_color=(0.1, 0.2, 0.3, 0.4))
+    col, dep = kz_oracle.clear_images(sc)
+    arr, n = kz_oracle.make_draws(sc)
+    arr[0].viewport[:] = list(vp)
+    arr[0].scissor[:] = list(sci)
+    ost = kz_oracle.KzoStats()
+    area = (ctypes.c_int32 * 4)(0, 0, size, size)
+    assert kz_oracle.lib().kzo_render_ds(size, size, col.ctypes.data, dep.ctypes.data, None, 0, area, n, arr, 1,
+                                         ctypes.byref(ost)) == 0
+    pc, pd, pf = py_raster.render(sc.vertices, size, size, clear_color=sc.clear_color, viewport=vp, scissor=sci)
+    _compare_states(col, dep, pc, pd)
+    assert ost.as_dict()["fragments"] == pf
+    assert pf > 0
