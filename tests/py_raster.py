@@ -20,7 +20,11 @@ coordinates a = -1/2 sum(x_i y_i+1 - x_i+1 y_i) decides facing (a > 0 is counter
 VkCullModeFlags; a viewport (x, y, width, height, minDepth, maxDepth) maps x_f = fma(x_d, w/2, x + w/2) and
 z_f = fma(z_d, maxDepth - minDepth, minDepth) (each constant one binary32 operation), clamps depth to its
 depth range, and admits pixel column p when p + 1/2 lies in [x, x + width) (rows likewise, for either sign
-of the height); a scissor rectangle (x, y, width, height) admits its pixels.
+of the height); a scissor rectangle (x, y, width, height) admits its pixels.  D16 / D24 depth attachments
+(`depth_format`) hold round(z * (2^n - 1)) of the binary32 product, compared and stored as integers; the
+stencil test (`stencil`: per face (fail, pass, depth_fail, compare, compare_mask, write_mask, reference))
+compares the masked reference with the masked stored value, then applies the VkStencilOp of its outcome
+through the write mask, before the depth result decides whether the fragment goes on.
 """
 from fractions import Fraction
 import math
@@ -128,17 +132,35 @@ def _pixel_range(lo, extent):
     return math.ceil(f32(a - HALF)), math.ceil(f32(b - HALF))
 
 
+DEPTH_BITS = {"d32": None, "d16": 16, "d24s8": 24}
+
+
+def stencil_op(op, s, write_mask, reference):
+    """VkStencilOp on the stored 8-bit value s, through the write mask"""
+    v = {0: s, 1: 0, 2: reference & 0xFF, 3: min(s + 1, 255), 4: max(s - 1, 0), 5: ~s & 0xFF, 6: (s + 1) & 0xFF,
+         7: (s - 1) & 0xFF}[op]
+    return (s & ~write_mask & 0xFF) | (v & write_mask & 0xFF)
+
+
 def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_depth=1.0, compare=1, depth_write=True,
            blend=None, blend_const=(0.0, 0.0, 0.0, 0.0), write_mask=0xF, cull=0, front_ccw=True, viewport=None,
-           scissor=None):
+           scissor=None, depth_test=True, depth_format="d32", stencil=None, clear_stencil=0):
     """vertices: float32 [3T, 8] (x, y, z, w, r, g, b, a); returns (colour uint8 [H, W, 4], depth float32
-    [H, W], fragment count).  compare: the VkCompareOp of the depth test; blend: None, or the six blend
-    factors and ops of blend_texel; cull: VkCullModeFlags; viewport: (x, y, width, height, minDepth,
-    maxDepth), default the whole framebuffer with depths [0, 1]; scissor: (x, y, width, height)."""
+    [H, W], fragment count), and the stencil plane uint8 [H, W] fourth when `stencil` is given.  compare: the
+    VkCompareOp of the depth test; blend: None, or the six blend factors and ops of blend_texel; cull:
+    VkCullModeFlags; viewport: (x, y, width, height, minDepth, maxDepth), default the whole framebuffer with
+    depths [0, 1]; scissor: (x, y, width, height); depth_format: "d32", "d16" or "d24s8" (the depth plane then
+    holds the integer texel values); stencil: {"front": (...), "back": (...)} as in the module docstring."""
     v = np.asarray(vertices, dtype=np.float32).reshape(-1, 8)
     color = np.empty((height, width, 4), dtype=np.uint8)
     color[:] = [unorm8(Fraction(float(np.float32(c)))) for c in clear_color]
-    depth = [[Fraction(float(np.float32(clear_depth)))] * width for _ in range(height)]
+    bits = DEPTH_BITS[depth_format]
+
+    def depth_value(z):
+        return z if bits is None else Fraction(rne(mul(z, (1 << bits) - 1)))
+
+    depth = [[depth_value(Fraction(float(np.float32(clear_depth))))] * width for _ in range(height)]
+    sten = [[clear_stencil & 0xFF] * width for _ in range(height)]
     vp = [Fraction(float(np.float32(c))) for c in (viewport or (0, 0, width, height, 0, 1))]
     hx, hy = mul(vp[2], HALF), mul(vp[3], HALF)
     ox, oy = f32(vp[0] + hx), f32(vp[1] + hy)
@@ -200,10 +222,18 @@ def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_dept
                 frags += 1
                 l = [mul(f32(E[e]), inv_s) for e in range(3)]
                 z = fma(l[2], dz2, fma(l[1], dz1, z0))
-                z = min(max(z, zlo), zhi)
-                if not depth_cmp(compare, z, depth[py][px]):
+                z = depth_value(min(max(z, zlo), zhi))
+                dpass = not depth_test or depth_cmp(compare, z, depth[py][px])
+                if stencil is not None:
+                    fail, pas, dfail, cmp_op, cmask, wmask, ref = stencil["front" if front else "back"]
+                    sv = sten[py][px]
+                    if not depth_cmp(cmp_op, ref & cmask & 0xFF, sv & cmask):
+                        sten[py][px] = stencil_op(fail, sv, wmask, ref)
+                        continue
+                    sten[py][px] = stencil_op(pas if dpass else dfail, sv, wmask, ref)
+                if not dpass:
                     continue
-                if depth_write:
+                if depth_test and depth_write:
                     depth[py][px] = z
                 q = fma(l[2], IW[2], fma(l[1], IW[1], mul(l[0], IW[0])))
                 rq = div(1, q)
@@ -215,4 +245,6 @@ def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_dept
                         if (write_mask >> k) & 1:
                             color[py, px, k] = unorm8(out[k])
     dep = np.array([[float(d) for d in row] for row in depth], dtype=np.float32)
+    if stencil is not None:
+        return color, dep, frags, np.array(sten, dtype=np.uint8)
     return color, dep, frags

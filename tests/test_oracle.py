@@ -276,3 +276,47 @@ def test_oracle_viewports_and_scissors_match_python(built, viewport, scissor):
     _compare_states(col, dep, pc, pd)
     assert ost.as_dict()["fragments"] == pf
     assert pf > 0
+
+
+# per face (fail, pass, depth_fail, compare, compare_mask, write_mask, reference); VkStencilOp KEEP 0, ZERO 1,
+# REPLACE 2, INCREMENT_AND_CLAMP 3, DECREMENT_AND_CLAMP 4, INVERT 5, INCREMENT_AND_WRAP 6, DECREMENT_AND_WRAP 7
+STENCIL_CASES = {
+    "count_overdraw": ({"front": (0, 6, 0, 7, 0xFF, 0xFF, 0), "back": (0, 6, 0, 7, 0xFF, 0xFF, 0)},
+                       dict(depth_test=False, depth_write=False), 0),
+    "first_wins": ({"front": (0, 3, 7, 2, 0xFF, 0xFF, 0), "back": (0, 3, 7, 2, 0xFF, 0xFF, 0)}, {}, 0),
+    "faces_masks": ({"front": (1, 6, 4, 5, 0x03, 0x0F, 2), "back": (2, 5, 3, 6, 0xF0, 0xF3, 0x35)}, {}, 0x5A),
+    "replace_greater": ({"front": (7, 2, 1, 4, 0xFF, 0xFF, 6), "back": (3, 2, 0, 3, 0xFF, 0xFF, 6)},
+                        dict(depth_compare=3), 5),
+}
+
+
+@pytest.mark.parametrize("fmt,case", [("d16", None), ("d24s8", None)] + [("d24s8", c) for c in sorted(STENCIL_CASES)])
+def test_oracle_depth_formats_and_stencil_match_python(built, fmt, case):
+    """D16 and D24 depth (integer texels), and on D24S8 the stencil test with per-face ops, compare and write
+    masks, against the restatement: colour, depth texels, stencil values and fragment counts"""
+    import ctypes
+    size = 16
+    faces, state, clear_s = STENCIL_CASES[case] if case else (None, {}, 0)
+    stencil = None
+    if faces:
+        stencil = {f: scenes.StencilOp(*faces[f]) for f in ("front", "back")}
+    sc = scenes.triangles_from(np.array(_state_rows(90 + len(str(case)), 12, size), dtype=np.float32), size, size,
+                               clear_color=(0.1, 0.2, 0.3, 0.4), clear_depth=0.6, depth_format=fmt,
+                               stencil=stencil, clear_stencil=clear_s, **state)
+    col, dep = kz_oracle.clear_images(sc)
+    st_plane = np.full((size, size), clear_s & 0xFF, dtype=np.uint8) if fmt == "d24s8" else None
+    arr, n = kz_oracle.make_draws(sc)
+    ost = kz_oracle.KzoStats()
+    area = (ctypes.c_int32 * 4)(0, 0, size, size)
+    assert kz_oracle.lib().kzo_render_ds(size, size, col.ctypes.data, dep.ctypes.data,
+                                         st_plane.ctypes.data if st_plane is not None else None,
+                                         kz_oracle.DEPTH_FORMAT[fmt], area, n, arr, 1, ctypes.byref(ost)) == 0
+    out = py_raster.render(sc.vertices, size, size, clear_color=sc.clear_color, clear_depth=sc.clear_depth,
+                           compare=sc.depth_compare, depth_write=sc.depth_write, depth_test=sc.depth_test,
+                           depth_format=fmt, stencil=faces, clear_stencil=clear_s)
+    pc, pd, pf = out[:3]
+    _compare_states(col, dep, pc, pd)
+    assert ost.as_dict()["fragments"] == pf
+    if faces:
+        assert np.array_equal(st_plane, out[3]), "stencil differs"
+        assert len(np.unique(out[3])) >= 2
