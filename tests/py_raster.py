@@ -24,7 +24,10 @@ of the height); a scissor rectangle (x, y, width, height) admits its pixels.  D1
 (`depth_format`) hold round(z * (2^n - 1)) of the binary32 product, compared and stored as integers; the
 stencil test (`stencil`: per face (fail, pass, depth_fail, compare, compare_mask, write_mask, reference))
 compares the masked reference with the masked stored value, then applies the VkStencilOp of its outcome
-through the write mask, before the depth result decides whether the fragment goes on.
+through the write mask, before the depth result decides whether the fragment goes on.  With `samples`=4
+(the standard sample positions (3/8, 1/8), (7/8, 3/8), (1/8, 5/8), (5/8, 7/8) of a pixel) each sample has
+its own coverage, depth and depth test; the fragment shader runs once at the pixel centre (extrapolated
+when the centre lies outside) and its colour is written to every sample that passed.
 """
 from fractions import Fraction
 import math
@@ -133,6 +136,7 @@ def _pixel_range(lo, extent):
 
 
 DEPTH_BITS = {"d32": None, "d16": 16, "d24s8": 24}
+MS_POS = [(96, 32), (224, 96), (32, 160), (160, 224)]  # sample offsets in 1/256 pixel
 
 
 def stencil_op(op, s, write_mask, reference):
@@ -142,15 +146,52 @@ def stencil_op(op, s, write_mask, reference):
     return (s & ~write_mask & 0xFF) | (v & write_mask & 0xFF)
 
 
+def _pixel_ms(px, py, X, Y, dxs, dys, tl, inv_s, z0, dz1, dz2, zlo, zhi, IW, A, compare, depth_test, depth_write,
+              depth4, color4, blend, blend_const, write_mask):
+    """one pixel of a 4x multisampled attachment; returns 1 when a sample is covered"""
+    def edges(sx, sy):
+        return [dxs[e] * (sy - Y[(e + 1) % 3]) - dys[e] * (sx - X[(e + 1) % 3]) for e in range(3)]
+
+    passed, zs, covered = [], {}, False
+    for s, (ox, oy) in enumerate(MS_POS):
+        E = edges(256 * px + ox, 256 * py + oy)
+        if not all(E[e] > 0 or (E[e] == 0 and tl[e]) for e in range(3)):
+            continue
+        covered = True
+        z = fma(mul(f32(E[2]), inv_s), dz2, fma(mul(f32(E[1]), inv_s), dz1, z0))
+        zs[s] = min(max(z, zlo), zhi)
+        if not depth_test or depth_cmp(compare, zs[s], depth4[py][px][s]):
+            passed.append(s)
+    if not covered:
+        return 0
+    if passed:
+        E = edges(256 * px + 128, 256 * py + 128)  # the fragment shader at the pixel centre
+        l = [mul(f32(E[e]), inv_s) for e in range(3)]
+        q = fma(l[2], IW[2], fma(l[1], IW[1], mul(l[0], IW[0])))
+        rq = div(1, q)
+        out = [mul(fma(l[2], A[2][k], fma(l[1], A[1][k], mul(l[0], A[0][k]))), rq) for k in range(4)]
+        for s in passed:
+            if depth_test and depth_write:
+                depth4[py][px][s] = zs[s]
+            if blend is not None:
+                color4[py, px, s] = blend_texel(color4[py, px, s], out, blend, blend_const, write_mask)
+            else:
+                for k in range(4):
+                    if (write_mask >> k) & 1:
+                        color4[py, px, s, k] = unorm8(out[k])
+    return 1
+
+
 def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_depth=1.0, compare=1, depth_write=True,
            blend=None, blend_const=(0.0, 0.0, 0.0, 0.0), write_mask=0xF, cull=0, front_ccw=True, viewport=None,
-           scissor=None, depth_test=True, depth_format="d32", stencil=None, clear_stencil=0):
+           scissor=None, depth_test=True, depth_format="d32", stencil=None, clear_stencil=0, samples=1):
     """vertices: float32 [3T, 8] (x, y, z, w, r, g, b, a); returns (colour uint8 [H, W, 4], depth float32
     [H, W], fragment count), and the stencil plane uint8 [H, W] fourth when `stencil` is given.  compare: the
     VkCompareOp of the depth test; blend: None, or the six blend factors and ops of blend_texel; cull:
     VkCullModeFlags; viewport: (x, y, width, height, minDepth, maxDepth), default the whole framebuffer with
     depths [0, 1]; scissor: (x, y, width, height); depth_format: "d32", "d16" or "d24s8" (the depth plane then
-    holds the integer texel values); stencil: {"front": (...), "back": (...)} as in the module docstring."""
+    holds the integer texel values); stencil: {"front": (...), "back": (...)} as in the module docstring;
+    samples: 1, or 4 (D32, no stencil), which returns colour [H, W, 4 samples, 4] and depth [H, W, 4]."""
     v = np.asarray(vertices, dtype=np.float32).reshape(-1, 8)
     color = np.empty((height, width, 4), dtype=np.uint8)
     color[:] = [unorm8(Fraction(float(np.float32(c)))) for c in clear_color]
@@ -161,6 +202,10 @@ def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_dept
 
     depth = [[depth_value(Fraction(float(np.float32(clear_depth))))] * width for _ in range(height)]
     sten = [[clear_stencil & 0xFF] * width for _ in range(height)]
+    if samples == 4:
+        assert bits is None and stencil is None
+        color4 = np.repeat(color[:, :, None, :], 4, axis=2)
+        depth4 = [[[depth[0][0]] * 4 for _ in range(width)] for _ in range(height)]
     vp = [Fraction(float(np.float32(c))) for c in (viewport or (0, 0, width, height, 0, 1))]
     hx, hy = mul(vp[2], HALF), mul(vp[3], HALF)
     ox, oy = f32(vp[0] + hx), f32(vp[1] + hy)
@@ -197,10 +242,11 @@ def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_dept
             for arr in (X, Y, Z, IW, A):
                 arr[1], arr[2] = arr[2], arr[1]
             S = -S
-        bx0 = max(rx0, -((-(min(X) - 128)) // 256))
-        by0 = max(ry0, -((-(min(Y) - 128)) // 256))
-        bx1 = min(rx1 - 1, (max(X) - 128) // 256)
-        by1 = min(ry1 - 1, (max(Y) - 128) // 256)
+        lo, hi = (32, 224) if samples == 4 else (128, 128)  # the sample offsets' range
+        bx0 = max(rx0, -((-(min(X) - hi)) // 256))
+        by0 = max(ry0, -((-(min(Y) - hi)) // 256))
+        bx1 = min(rx1 - 1, (max(X) - lo) // 256)
+        by1 = min(ry1 - 1, (max(Y) - lo) // 256)
         inv_s = div(1, f32(S))
         z0, dz1, dz2 = Z[0], f32(Z[1] - Z[0]), f32(Z[2] - Z[0])
         tl, dxs, dys = [], [], []
@@ -212,6 +258,10 @@ def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_dept
             tl.append(dy < 0 or (dy == 0 and dx > 0))
         for py in range(by0, by1 + 1):
             for px in range(bx0, bx1 + 1):
+                if samples == 4:
+                    frags += _pixel_ms(px, py, X, Y, dxs, dys, tl, inv_s, z0, dz1, dz2, zlo, zhi, IW, A, compare,
+                                       depth_test, depth_write, depth4, color4, blend, blend_const, write_mask)
+                    continue
                 sx, sy = 256 * px + 128, 256 * py + 128
                 E = []
                 for e in range(3):
@@ -244,6 +294,8 @@ def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_dept
                     for k in range(4):
                         if (write_mask >> k) & 1:
                             color[py, px, k] = unorm8(out[k])
+    if samples == 4:
+        return color4, np.array([[[float(d) for d in px] for px in row] for row in depth4], dtype=np.float32), frags
     dep = np.array([[float(d) for d in row] for row in depth], dtype=np.float32)
     if stencil is not None:
         return color, dep, frags, np.array(sten, dtype=np.uint8)

@@ -320,3 +320,25 @@ def test_oracle_depth_formats_and_stencil_match_python(built, fmt, case):
     if faces:
         assert np.array_equal(st_plane, out[3]), "stencil differs"
         assert len(np.unique(out[3])) >= 2
+
+
+@pytest.mark.parametrize("blend", [False, True])
+def test_oracle_multisampling_matches_python(built, blend):
+    """4x multisampling: per-sample coverage, depth and depth test at the standard sample positions, one
+    fragment-shader run at the pixel centre, colour to the passing samples; and the resolve, (s0 + s1 + s2 +
+    s3 + 2) / 4 per channel"""
+    size = 16
+    state = dict(blend=True, blend_state=(6, 7, 0, 6, 7, 0), depth_compare=3, depth_write=False) if blend else {}
+    sc = scenes.triangles_from(np.array(_state_rows(95 + int(blend), 10, size), dtype=np.float32), size, size,
+                               clear_color=(0.1, 0.2, 0.3, 0.4), samples=4, **state)
+    oc4, od4, ores, ost = kz_oracle.render_ms(sc, threads=1)
+    pc4, pd4, pf = py_raster.render(sc.vertices, size, size, clear_color=sc.clear_color, compare=sc.depth_compare,
+                                    depth_write=sc.depth_write, blend=sc.blend_factors() if blend else None,
+                                    samples=4)
+    assert ost["fragments"] == pf
+    assert np.array_equal(od4.view(np.uint32), pd4.view(np.uint32)), "sample depths differ"
+    assert np.array_equal(oc4, pc4), "sample colours differ"
+    resolved = ((pc4.astype(np.uint32).sum(axis=2) + 2) // 4).astype(np.uint8)
+    assert np.array_equal(ores, resolved)
+    # samples of one pixel differ along edges (partial coverage)
+    assert np.any(np.any(pc4 != pc4[:, :, :1, :], axis=(2, 3)))
