@@ -38,3 +38,16 @@ def test_blend_scene_areas():
     area = 0.5 * np.abs((x[:, 1] - x[:, 0]) * (y[:, 2] - y[:, 0]) - (x[:, 2] - x[:, 0]) * (y[:, 1] - y[:, 0]))
     assert area.min() > 3.9 and area.max() < 4100
     assert np.allclose(v[:, :, 7], 0.5)
+
+
+def test_visible_triangles_of_a_multi_draw_scene():
+    """the visible-triangle count of a scene of several indexed draws reads each draw's indices from its
+    firstIndex: a mesh drawn twice (the second draw's indices after the first's) counts twice"""
+    import dataclasses
+    one = scenes.single_large(tris=20_000, width=480, height=270)
+    n1, area1 = scenes.visible_triangles(one)
+    d = one.draws[0]
+    twice = dataclasses.replace(one, indices=np.concatenate([one.indices, one.indices]),
+                                draws=[d, scenes.Draw(3 * d.count, d.count, d.vertex_offset, d.mvp)])
+    n2, area2 = scenes.visible_triangles(twice)
+    assert n1 > 0 and n2 == 2 * n1 and abs(area2 - area1) < 1e-9
