@@ -3,8 +3,14 @@
 It is test infrastructure: it checks the C oracle (oracle/kz_oracle.c) on hand-sized cases, using exact
 rational arithmetic with one explicit round-to-nearest-even to binary32 per operation, so every fma is a
 true single-rounding fma.  Coverage: colour pipeline (pass-through vertex shader, colour fragment shader),
-non-indexed triangle lists with no clipping needed (0 <= z <= w, inside the guard band), full-framebuffer
-viewport with depth range [0, 1], no culling.
+non-indexed triangle lists, full-framebuffer viewport with depth range [0, 1], no culling, unless the
+options below say otherwise.  Clipping: a triangle with all vertices beyond one plane of the view volume
+(x > w, x < -w, y > w, y < -w, z < 0, z > w) is dropped; one with a vertex outside z >= 0, z <= w or the
+guard band |x|, |y| <= 4w is clipped against those six planes in that order (Sutherland-Hodgman, a plane
+skipped when no vertex is outside it), each new vertex on edge (inside i, outside o) being
+fma(t, o_k - i_k, i_k) for every component with t = d_i / (d_i - d_o), d the plane's distance in binary32
+(z, w - z, x + 4w, 4w - x, y + 4w, 4w - y); a polygon with a vertex at w <= 0 left is dropped, the rest
+drawn as the fan (v0, v_i, v_i+1).
 
 Rules (Vulkan specification, with the choices the spec leaves open fixed as the GPU path fixes them):
 viewport x_f = fma(x * (1/w), W/2, W/2), snapped to 16.8 fixed point with round-to-nearest-even; signed
@@ -127,6 +133,45 @@ def blend_texel(texel, out, factors, consts, write_mask):
     return res
 
 
+def _plane_dist(p, plane):
+    x, y, z, w = p[:4]
+    g = 4 * w  # exact
+    return [z, f32(w - z), f32(x + g), f32(g - x), f32(y + g), f32(g - y)][plane]
+
+
+def clip_triangle(P):
+    """the sub-triangles of triangle P (three lists of 8 exact binary32 values) after clipping, in fan order;
+    [] when it is dropped"""
+    if any(all(cond(p) for p in P) for cond in (lambda p: p[0] > p[3], lambda p: p[0] < -p[3],
+                                               lambda p: p[1] > p[3], lambda p: p[1] < -p[3],
+                                               lambda p: p[2] < 0, lambda p: p[2] > p[3])):
+        return []
+    if not any(_plane_dist(p, k) < 0 for p in P for k in range(6)):
+        return [P]
+    poly = [list(p) for p in P]
+    for plane in range(6):
+        if not any(_plane_dist(p, plane) < 0 for p in poly):
+            continue
+        out = []
+        for i in range(len(poly)):
+            p, q = poly[i], poly[(i + 1) % len(poly)]
+            dp, dq = _plane_dist(p, plane), _plane_dist(q, plane)
+            pin, qin = dp >= 0, dq >= 0
+            if pin:
+                out.append(p)
+            if pin != qin:
+                vi, vo = (p, q) if pin else (q, p)
+                di, do = (dp, dq) if pin else (dq, dp)
+                t = div(di, f32(di - do))
+                out.append([fma(t, f32(vo[k] - vi[k]), vi[k]) for k in range(len(vi))])
+        poly = out
+        if len(poly) < 3:
+            return []
+    if not all(p[3] > 0 for p in poly):
+        return []
+    return [[poly[0], poly[i], poly[i + 1]] for i in range(1, len(poly) - 1)]
+
+
 def _pixel_range(lo, extent):
     """first and one-past-last pixel p with p + 1/2 in [lo, lo + extent) (extent may be negative), from the
     binary32 operations ceil(lo - 1/2) and ceil((lo + extent) - 1/2)"""
@@ -219,12 +264,13 @@ def render(vertices, width, height, clear_color=(0.0, 0.0, 0.0, 1.0), clear_dept
         rx0, ry0 = max(rx0, scissor[0]), max(ry0, scissor[1])
         rx1, ry1 = min(rx1, scissor[0] + scissor[2]), min(ry1, scissor[1] + scissor[3])
     frags = 0
+    pieces = []
     for t in range(len(v) // 3):
-        P = [[Fraction(float(c)) for c in v[3 * t + j]] for j in range(3)]
+        pieces += clip_triangle([[Fraction(float(c)) for c in v[3 * t + j]] for j in range(3)])
+    for P in pieces:
         X, Y, Z, IW, A = [], [], [], [], []
         for p in P:
             x, y, z, w = p[:4]
-            assert w > 0 and 0 <= z <= w and abs(x) <= 4 * w and abs(y) <= 4 * w, "case needs clipping"
             iw = div(1, w)
             X.append(int(rne(mul(fma(mul(x, iw), hx, ox), 256))))
             Y.append(int(rne(mul(fma(mul(y, iw), hy, oy), 256))))

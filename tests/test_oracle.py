@@ -342,3 +342,35 @@ def test_oracle_multisampling_matches_python(built, blend):
     assert np.array_equal(ores, resolved)
     # samples of one pixel differ along edges (partial coverage)
     assert np.any(np.any(pc4 != pc4[:, :, :1, :], axis=(2, 3)))
+
+
+def _clip_rows(seed, n, size):
+    """triangles reaching past the near and far planes, behind the eye (w < 0) and past the guard band"""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for _ in range(n):
+        c = rng.uniform(-1.0, 1.0, 2)
+        for _ in range(3):
+            w = float(rng.choice([rng.uniform(0.5, 2.0), rng.uniform(-1.0, 0.3)]))
+            xy = (c + rng.normal(0.0, 0.8, 2) * float(rng.choice([1.0, 8.0]))) * abs(w)
+            z = float(rng.uniform(-0.6, 1.6)) * abs(w)
+            rows.append([float(xy[0]), float(xy[1]), z, w] + list(rng.uniform(0, 1, 4)))
+    return rows
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_clipping_matches_python(built, seed):
+    """near, far and guard-band clipping, triangles behind the eye, fan triangulation of the clipped polygon,
+    against the restatement's Sutherland-Hodgman clipper"""
+    import scene_cases
+    size = 24
+    if seed == 0:
+        sc = scene_cases.guard_band_and_near(width=size, height=size)
+    else:
+        sc = scenes.triangles_from(np.array(_clip_rows(seed, 14, size), dtype=np.float32), size, size,
+                                   clear_color=(0.1, 0.2, 0.3, 0.4))
+    oc, od, ost = kz_oracle.render(sc, threads=1)
+    pc, pd, pf = py_raster.render(sc.vertices, size, size, clear_color=sc.clear_color)
+    _compare_states(oc, od, pc, pd)
+    assert ost["fragments"] == pf
+    assert ost["clipped"] > 0 and pf > 0
