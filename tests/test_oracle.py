@@ -1,7 +1,9 @@
 """The CPU oracle (oracle/kz_oracle.c) on the CPU: checked against an independent pure-Python restatement
-of the rules (tests/py_raster.py, exact rational arithmetic) on small scenes, against properties that
-follow from the rules by hand (watertight tessellations, no double coverage at shared vertices, invariance
-under vertex rotation, UNORM8 rounding), and against its own committed golden digests.
+of the rules (tests/py_raster.py, exact rational arithmetic) on small scenes -- coverage and interpolation,
+every depth compare op, every blend state, cull modes and facing, viewports and scissors, D16 / D24 depth
+and the stencil test, 4x multisampling and its resolve, and clipping --, against properties that follow
+from the rules by hand (watertight tessellations, no double coverage at shared vertices, invariance under
+vertex rotation, UNORM8 rounding), and against its own committed golden digests.
 
 The reference driver has no rasteriser to pin against (vulkan-driver/src/api_impl.rs:4632-4653 are
 `unimplemented!()`); these checks are what pins the oracle."""
